@@ -1,0 +1,408 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 MD hot path in atom-timesteps/s.
+
+Default workload (one GPU): the copper-like eam_alloy FCC crystal of
+100x100x100 unit cells (4,000,000 atoms, a = 3.615 A, 5,000-point splines,
+rcut 5.0 A, skin 0.3 A, 300 K, dt = 1 fs), NVE velocity Verlet with a
+neighbour rebuild every 10 steps, mixed precision (FP32 pair arithmetic,
+FP64 state).  One step = first half push + (rebuild) + density/embedding +
+force + second half push, for all atoms.
+
+Reported (one JSON line on rank 0):
+  value      device-resident throughput (state in HBM, K steps timed with
+             CUDA events on the library's stream, CUDA graph of 2 rebuild
+             intervals, thermo every 20 steps)
+  e2e        the same step through the C ABI with the grid state on the
+             host: per step r,v,a copied in from pinned memory, one
+             gbmd_run_nve step, r,v,a copied out
+  roofline   the final pair kernel (force + fused Verlet halves), algorithmic
+             bytes per launch / its CUDA-event duration, against the measured
+             HBM copy bandwidth
+  fp64       the same steps through the plain-FP64 kernels, and the
+             mixed-vs-FP64 force error and energy drift
+  cpu_baseline  the FP64 OpenMP oracle on a bounded sample, all host threads
+
+--impl reference times the reference's CPU path of this workload on the
+host cores: the reference cannot be built here (it needs onika, exaNBody,
+yaml-cpp and MPI), so it is the project's FP64 OpenMP restatement of the
+reference operators (oracle/), on a sample sized to finish in minutes.
+Multi-GPU (torchrun): independent replicas, one per rank, weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "eam_cu_4m": dict(kind="eam", ncell=100, a=3.615, T=300.0, seed=2, rcut=5.0, skin=0.3, dt=1e-3,
+                      desc="eam_alloy Cu-like FCC 100^3 cells (4,000,000 atoms), 5000-point splines, "
+                           "rcut 5.0 A, skin 0.3 A, 300 K, dt 1 fs, NVE, rebuild every 10"),
+    "lj_fcc_32k": dict(kind="lj", ncell=20, T=1.0, seed=1, rcut=2.5, skin=0.3, dt=0.005,
+                       desc="LJ FCC 20^3 cells (32,000 atoms), rho*=0.8442, rc 2.5, skin 0.3, T*=1, "
+                            "dt 0.005, NVE, rebuild every 10"),
+}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=1000)
+    p.add_argument("--warmup", type=int, default=20)
+    p.add_argument("--impl", default="gbmd", choices=["gbmd", "reference"])
+    p.add_argument("--workload", default="eam_cu_4m", choices=sorted(WORKLOADS))
+    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    p.add_argument("--rebuild-every", type=int, default=10)
+    p.add_argument("--e2e-steps", type=int, default=20)
+    p.add_argument("--fp64-steps", type=int, default=40)
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--lanes", type=int, default=0, help="lanes per atom (0: autotune)")
+    p.add_argument("--block", type=int, default=0)
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def make_system(w):
+    from exastamp_gb300 import systems as S
+    if w["kind"] == "eam":
+        return S.eam_cu_fcc(ncell=w["ncell"], a=w["a"], T=w["T"], seed=w["seed"])
+    return S.lj_fcc(ncell=w["ncell"], T=w["T"], seed=w["seed"])
+
+
+def bind_potential(ctx, w):
+    from exastamp_gb300 import setfl, systems as S
+    if w["kind"] == "eam":
+        sf = setfl.tabulate(setfl.load_cu_params())
+        ctx.set_eam_alloy(sf, w["rcut"], S.EV, S.EV)
+    else:
+        ctx.set_lj(1.0, 1.0, w["rcut"])
+    ctx.set_skin(w["skin"])
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        rows = []
+        for ln in open(self.path):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(rows), "reasons": reasons}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return ws, rank, local
+
+
+def dist_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+def cpu_oracle_rate(w, target_s=12.0, ncell=None):
+    """FP64 OpenMP oracle NVE throughput on a sample of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from exastamp_gb300 import setfl, systems as S
+    O.build()
+    if w["kind"] == "eam":
+        cfg = setfl.load_cu_params()
+        tab = O.EamOracleTables.from_setfl(setfl.tabulate(cfg), S.EV, S.EV, rcut=w["rcut"])
+        pot_kind, pot = O.POT_EAM, tab
+        mk = lambda nc: S.eam_cu_fcc(ncell=nc, a=w["a"], T=w["T"], seed=w["seed"])  # noqa: E731
+    else:
+        pot_kind, pot = O.POT_LJ, O.LJParams(1.0, 1.0, w["rcut"])
+        mk = lambda nc: S.lj_fcc(ncell=nc, T=w["T"], seed=w["seed"])  # noqa: E731
+    nc = ncell or min(w["ncell"], 24 if w["kind"] == "eam" else 20)
+    s = mk(nc)
+    st = s.state()
+    t0 = time.perf_counter()
+    O.run_nve(st, s.masses, s.lo, s.hi, pot_kind, pot, w["skin"], w["dt"], 2, 10, thermo=False)
+    t_cal = (time.perf_counter() - t0) / 3.0
+    steps = int(max(3, min(200, target_s / max(t_cal, 1e-6))))
+    st = s.state()
+    t0 = time.perf_counter()
+    O.run_nve(st, s.masses, s.lo, s.hi, pot_kind, pot, w["skin"], w["dt"], steps, 10, thermo=False)
+    dt = time.perf_counter() - t0
+    return s.n * steps / dt, {"atoms": s.n, "steps": steps, "seconds": dt, "threads": O.num_threads(),
+                              "ncell": nc}
+
+
+def run_reference(args, w, ws, rank):
+    """--impl reference: the FP64 OpenMP restatement of the reference
+    operators (the reference itself does not build here), all host threads,
+    each step one NVE step of a sample sized so W+K steps fit in minutes."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    # size the sample: ~150 s for warmup + steps at the calibrated rate
+    rate, _ = cpu_oracle_rate(w, target_s=3.0, ncell=8 if w["kind"] == "eam" else 10)
+    budget = 150.0
+    atoms = rate * budget / max(1, args.steps + args.warmup)
+    per = 4
+    nc = int(max(4, min(w["ncell"], round((atoms / per) ** (1.0 / 3.0)))))
+    from exastamp_gb300 import setfl, systems as S
+    if w["kind"] == "eam":
+        tab = O.EamOracleTables.from_setfl(setfl.tabulate(setfl.load_cu_params()), S.EV, S.EV, rcut=w["rcut"])
+        pot_kind, pot = O.POT_EAM, tab
+        s = S.eam_cu_fcc(ncell=nc, a=w["a"], T=w["T"], seed=w["seed"])
+    else:
+        pot_kind, pot = O.POT_LJ, O.LJParams(1.0, 1.0, w["rcut"])
+        s = S.lj_fcc(ncell=nc, T=w["T"], seed=w["seed"])
+    st = s.state()
+    O.run_nve(st, s.masses, s.lo, s.hi, pot_kind, pot, w["skin"], w["dt"], args.warmup, args.rebuild_every,
+              thermo=False)
+    t0 = time.perf_counter()
+    O.run_nve(st, s.masses, s.lo, s.hi, pot_kind, pot, w["skin"], w["dt"], args.steps, args.rebuild_every,
+              thermo=False)
+    sec = time.perf_counter() - t0
+    value = s.n * args.steps / sec
+    sample = "%d-atom sample (%d^3 FCC cells) of the workload, %d NVE steps, rebuild every %d" % (
+        s.n, nc, args.steps, args.rebuild_every)
+    line = {"impl": "reference", "metric": "atom-timesteps/s", "value": value, "unit": "atom-timesteps/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded FCC lattice, Maxwell-Boltzmann velocities)",
+            "config": {"workload": args.workload, "description": w["desc"], "sample_atoms": s.n},
+            "cpu_baseline": {"value": value, "unit": "atom-timesteps/s", "cores": O.num_threads(),
+                             "kind": "port", "sample": sample,
+                             "note": "reference unbuildable here (needs onika, exaNBody, yaml-cpp, MPI); "
+                                     "FP64 OpenMP restatement of its operators"},
+            "e2e": {"value": value, "unit": "atom-timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def main():
+    args = parse()
+    w = WORKLOADS[args.workload]
+    ws, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, w, ws, rank)
+        return
+    import torch
+    from exastamp_gb300 import _capi
+    assert torch.cuda.is_available(), "bench.py needs a GPU (no CPU fallback)"
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    s = make_system(w)
+    ctx = _capi.Context(dev, stream.cuda_stream)
+    ctx.upload_system(s)
+    bind_potential(ctx, w)
+    ctx.set_precision(args.precision == "mixed")
+    if args.lanes:
+        ctx.set_launch(args.lanes, args.block or 128)
+    else:
+        from exastamp_gb300 import autotune
+        lanes, block, _ = autotune.tune(ctx, key="%s-%s" % (args.workload, args.precision))
+        ctx.set_launch(lanes, block)
+    R, dt = args.rebuild_every, w["dt"]
+    thermo_every = 2 * R if R > 0 else 0
+    # warm-up (also captures the CUDA graph)
+    ctx.run_nve(max(args.warmup, 3), dt, R, thermo_every, use_graph=True)
+    npairs, maxnb, nc = ctx.neighbor_stats()
+
+    # ---- timed region: K steps, device resident --------------------------
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        barrier(ws)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        th = ctx.run_nve(args.steps, dt, R, thermo_every, use_graph=True)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier(ws)
+    ms = ev0.elapsed_time(ev1)
+    ms = dist_max(ms, ws)
+    clocks = clk.summary()
+    value = s.n * args.steps * ws / (ms * 1e-3)
+    etot = th[:, 21:24].sum(1) + th[:, 24]
+    drift = (etot[-1] - etot[0]) / s.n / max(args.steps, 1) * 1000.0
+    rebuilds = args.steps // R if R > 0 else 0
+    kernels_per_step = 2 if w["kind"] == "eam" else 1
+    gpu_launches = kernels_per_step * args.steps + 9 * rebuilds + 2 * (args.steps // thermo_every if thermo_every else 0)
+
+    out = {"metric": "atom-timesteps/s", "value": value, "unit": "atom-timesteps/s", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32-pair/f64-state" if args.precision == "mixed" else "f64",
+           "data": "synthetic (seeded FCC lattice, Maxwell-Boltzmann velocities)",
+           "config": {"workload": args.workload, "description": w["desc"], "atoms": s.n,
+                      "precision": args.precision, "rebuild_every": R, "thermo_every": thermo_every,
+                      "neighbours_per_atom": npairs / s.n, "cells": nc.tolist(),
+                      "lanes_per_atom": ctx.get_launch()[0], "block": ctx.get_launch()[1],
+                      "parallelism": "replicas" if ws > 1 else "single-gpu",
+                      "l2": "inputs larger than L2 (neighbour list %.2f GB)" % (npairs * 4 / 1e9)
+                      if npairs * 4 > 129e6 else "inputs resident in L2 (not flushed)",
+                      "cuda_graph": True},
+           "gpu_launches": gpu_launches, "clocks": clocks,
+           "nve_energy_drift_per_1000_steps_per_atom": drift}
+
+    # ---- per-kernel timing for the roofline -------------------------------
+    prof = ctx.profile_step(reps=10)
+    peak, peak_kind = measured_peaks()
+    nbar = npairs / s.n
+    if w["kind"] == "eam":
+        # list 4 B/entry, own posf 16 B + F' 4 B, state r 24+24, v 24+24, a 24, posf 16, posd 32 written
+        per_atom = 4.0 * nbar + 16 + 4 + 48 + 48 + 24 + 16 + 32
+    else:
+        per_atom = 4.0 * nbar + 16 + 48 + 48 + 24 + 16 + 32
+    alg_bytes = per_atom * s.n
+    t_pair = prof["pair"] * 1e-3
+    achieved = alg_bytes / t_pair / 1e9
+    out["roofline"] = {"kernel": "k_eam_force (mixed, fused Verlet halves)" if w["kind"] == "eam" else "k_lj",
+                       "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                       "frac": achieved / peak, "peak_source": peak_kind,
+                       "algorithmic_bytes_per_launch": alg_bytes, "bytes_per_atom": per_atom,
+                       "traffic": None, "kernel_ms": prof}
+
+    # ---- FP64 comparison ----------------------------------------------------
+    if not args.no_fp64 and ws == 1:
+        d_mixed = ctx.download(("ax", "ay", "az"))
+        ctx.set_precision(False)
+        ctx.compute_forces(energy=False)
+        d64 = ctx.download(("ax", "ay", "az"))
+        A = np.stack([d_mixed[k] for k in ("ax", "ay", "az")], 1)
+        B = np.stack([d64[k] for k in ("ax", "ay", "az")], 1)
+        ferr = float(np.sqrt(((A - B) ** 2).sum() / (B ** 2).sum()))
+        ctx.run_nve(3, dt, R, 0, use_graph=False)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        ctx.run_nve(args.fp64_steps, dt, R, 0, use_graph=True)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = ev0.elapsed_time(ev1)
+        v64 = s.n * args.fp64_steps / (ms64 * 1e-3)
+        out["fp64"] = {"value": v64, "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps,
+                       "mixed_over_fp64": value / v64, "force_rel_rms_error_mixed_vs_fp64": ferr}
+        ctx.set_precision(args.precision == "mixed")
+
+    # ---- end-to-end through the C ABI with host buffers -----------------------
+    if not args.no_e2e:
+        n = s.n
+        pin = lambda: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()  # noqa: E731
+        host = {k: pin() for k in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az")}
+        d = ctx.download(tuple(host))
+        for k in host:
+            host[k][:] = d[k]
+        L = ctx._L
+        ptr = lambda k: host[k].ctypes.data  # noqa: E731
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            ctx._chk(L.gbmd_upload_state(ctx.h, *[ptr(k) for k in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az")]))
+            ctx._chk(L.gbmd_run_nve(ctx.h, 1, dt, R, 0, None, 0))
+            ctx._chk(L.gbmd_download(ctx.h, ptr("x"), ptr("y"), ptr("z"), ptr("vx"), ptr("vy"), ptr("vz"),
+                                     ptr("ax"), ptr("ay"), ptr("az"), None, None))
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        mse = ev0.elapsed_time(ev1)
+        mse = dist_max(max(mse, wall * 1e3), ws)
+        out["e2e"] = {"value": n * args.e2e_steps * ws / (mse * 1e-3), "unit": "atom-timesteps/s",
+                      "h2d_bytes_per_step": 72 * n, "d2h_bytes_per_step": 72 * n, "steps": args.e2e_steps,
+                      "ms_per_step": mse / args.e2e_steps,
+                      "path": "gbmd_upload_state(pinned r,v,a) + gbmd_run_nve(1) + gbmd_download(r,v,a)"}
+
+    # ---- CPU baseline (rank 0, N=1) -------------------------------------------
+    if not args.no_cpu and ws == 1 and rank == 0:
+        rate, info = cpu_oracle_rate(w)
+        out["cpu_baseline"] = {"value": rate, "unit": "atom-timesteps/s", "cores": info["threads"],
+                               "kind": "port",
+                               "sample": "%d-atom sample (%d^3 FCC cells) of the workload, %d FP64 NVE steps "
+                                         "on the OpenMP oracle (%.1f s)" % (info["atoms"], info["ncell"],
+                                                                            info["steps"], info["seconds"])}
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,272 @@
+"""ctypes binding of libgbmd.so (include/gbmd.h).
+
+There is no fallback: if the library is missing or no GPU is present, the
+calls raise.  `Context` is a thin RAII wrapper that turns status codes into
+exceptions and numpy arrays into pointers.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+LIB_PATH = os.path.join(PKG, "libgbmd.so")
+HEADER = os.path.join(ROOT, "include", "gbmd.h")
+
+OK = 0
+ERR_NAMES = {1: "INVALID", 2: "CUDA", 3: "NO_DEVICE", 4: "NEIGHBOR_OVERFLOW", 5: "LOST_ATOM",
+             6: "NONFINITE", 7: "IO", 8: "UNSUPPORTED", 9: "TOO_LARGE"}
+PRECISION_FP64, PRECISION_MIXED = 0, 1
+POT_NONE, POT_LJ, POT_LJ_MULTI, POT_EAM_ALLOY = 0, 1, 2, 3
+FORCE_ENERGY, FORCE_VIRIAL = 1, 2
+
+
+class GbmdError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("gbmd error %d (%s): %s" % (code, ERR_NAMES.get(code, "?"), msg))
+        self.code = code
+
+
+def declared_symbols(header: str = HEADER):
+    """Function names declared in include/gbmd.h."""
+    txt = open(header).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(gbmd_[a-z0-9_]+)\s*\(", txt)))
+
+
+_lib = None
+
+
+def lib(path: str = LIB_PATH):
+    """Load libgbmd.so (raises OSError if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise OSError("libgbmd.so not built (run __graft_entry__.build())")
+        L = C.CDLL(path)
+        vp, i64, i32, dbl = C.c_void_p, C.c_int64, C.c_int, C.c_double
+        P = C.POINTER
+        sig = {
+            "gbmd_abi_version": ([], i32),
+            "gbmd_last_error": ([vp], C.c_char_p),
+            "gbmd_create": ([P(vp), i32, vp], i32),
+            "gbmd_destroy": ([vp], i32),
+            "gbmd_synchronize": ([vp], i32),
+            "gbmd_set_box": ([vp, vp, vp, vp], i32),
+            "gbmd_set_species": ([vp, i32, vp], i32),
+            "gbmd_upload_atoms": ([vp, i64, vp, vp, vp, vp, vp, vp, vp, vp], i32),
+            "gbmd_upload_positions": ([vp, vp, vp, vp, vp, vp, vp], i32),
+            "gbmd_upload_state": ([vp] + [vp] * 9, i32),
+            "gbmd_download": ([vp] + [vp] * 11, i32),
+            "gbmd_profile_step": ([vp, i32, vp], i32),
+            "gbmd_num_atoms": ([vp, P(i64)], i32),
+            "gbmd_set_lj": ([vp, dbl, dbl, dbl], i32),
+            "gbmd_set_lj_multi": ([vp, i32, vp, vp, vp, dbl], i32),
+            "gbmd_set_eam_alloy": ([vp, i32, i32, dbl, i32, dbl, vp, vp, vp, dbl, dbl, dbl], i32),
+            "gbmd_load_setfl": ([vp, C.c_char_p, dbl, dbl, dbl], i32),
+            "gbmd_set_precision": ([vp, i32], i32),
+            "gbmd_set_launch": ([vp, i32, i32], i32),
+            "gbmd_get_launch": ([vp, P(i32), P(i32)], i32),
+            "gbmd_set_skin": ([vp, dbl], i32),
+            "gbmd_build_neighbors": ([vp], i32),
+            "gbmd_export_pairs": ([vp, i64, vp, vp, vp, P(i64)], i32),
+            "gbmd_neighbor_stats": ([vp, P(i64), P(i32), vp], i32),
+            "gbmd_compute_forces": ([vp, i32], i32),
+            "gbmd_push_f_v_r": ([vp, dbl, dbl], i32),
+            "gbmd_push_f_v": ([vp, dbl, dbl], i32),
+            "gbmd_push_min": ([vp, dbl, dbl, dbl], i32),
+            "gbmd_run_nve": ([vp, i32, dbl, i32, i32, vp, i32], i32),
+            "gbmd_run_minimize": ([vp, i32, dbl, dbl, i32], i32),
+            "gbmd_thermo": ([vp, vp], i32),
+            "gbmd_device_state": ([vp] + [vp] * 11, i32),
+        }
+        for name, (args, res) in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    if a is None:
+        return None
+    if not a.flags.c_contiguous:
+        raise ValueError("arrays must be C-contiguous")
+    return a.ctypes.data
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Context:
+    """One device context of the hot path (see include/gbmd.h)."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        self._L = lib()
+        h = C.c_void_p()
+        rc = self._L.gbmd_create(C.byref(h), device, stream)
+        if rc != OK:
+            raise GbmdError(rc, "gbmd_create failed")
+        self.h = h
+
+    # -- plumbing --------------------------------------------------------
+    def _chk(self, rc):
+        if rc != OK:
+            raise GbmdError(rc, self._L.gbmd_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.gbmd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- set-up -----------------------------------------------------------
+    def set_box(self, lo, hi):
+        lo, hi = _f64(lo), _f64(hi)
+        per = np.ones(3, dtype=np.int32)
+        self._chk(self._L.gbmd_set_box(self.h, _p(lo), _p(hi), _p(per)))
+
+    def set_species(self, masses):
+        m = _f64(masses)
+        self._chk(self._L.gbmd_set_species(self.h, len(m), _p(m)))
+
+    def upload(self, x, y, z, vx=None, vy=None, vz=None, types=None, ids=None):
+        x, y, z, vx, vy, vz = (_f64(a) for a in (x, y, z, vx, vy, vz))
+        t = None if types is None else np.ascontiguousarray(types, np.uint8)
+        i = None if ids is None else np.ascontiguousarray(ids, np.uint64)
+        self._keep = (x, y, z, vx, vy, vz, t, i)
+        self._chk(self._L.gbmd_upload_atoms(self.h, len(x), _p(x), _p(y), _p(z), _p(vx), _p(vy), _p(vz),
+                                            _p(t), _p(i)))
+
+    def upload_system(self, s):
+        self.set_box(s.lo, s.hi)
+        self.set_species(s.masses)
+        self.upload(s.x, s.y, s.z, s.vx, s.vy, s.vz, s.type, s.id)
+
+    def upload_positions(self, x, y, z, vx=None, vy=None, vz=None):
+        x, y, z, vx, vy, vz = (_f64(a) for a in (x, y, z, vx, vy, vz))
+        self._chk(self._L.gbmd_upload_positions(self.h, _p(x), _p(y), _p(z), _p(vx), _p(vy), _p(vz)))
+
+    def upload_state(self, x, y, z, vx, vy, vz, ax, ay, az):
+        arrs = [_f64(a) for a in (x, y, z, vx, vy, vz, ax, ay, az)]
+        self._chk(self._L.gbmd_upload_state(self.h, *[_p(a) for a in arrs]))
+
+    def profile_step(self, reps=10):
+        ms = np.zeros(5)
+        self._chk(self._L.gbmd_profile_step(self.h, int(reps), _p(ms)))
+        return dict(zip(("rebuild", "density", "pair", "first_half", "thermo"), ms.tolist()))
+
+    @property
+    def n(self) -> int:
+        v = C.c_int64()
+        self._chk(self._L.gbmd_num_atoms(self.h, C.byref(v)))
+        return v.value
+
+    def download(self, fields=("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "ep"), virial=False):
+        n = self.n
+        names = ["x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "ep"]
+        out = {k: np.empty(n) for k in names if k in fields}
+        vir = np.empty((n, 9)) if virial else None
+        self._chk(self._L.gbmd_download(self.h, *[_p(out.get(k)) for k in names], _p(vir)))
+        if virial:
+            out["vir"] = vir
+        return out
+
+    def set_lj(self, epsilon, sigma, rcut):
+        self._chk(self._L.gbmd_set_lj(self.h, float(epsilon), float(sigma), float(rcut)))
+
+    def set_lj_multi(self, eps, sig, rc, rcut_common=0.0):
+        eps, sig, rc = _f64(eps), _f64(sig), _f64(rc)
+        self._chk(self._L.gbmd_set_lj_multi(self.h, eps.shape[0], _p(eps), _p(sig), _p(rc), float(rcut_common)))
+
+    def set_eam_alloy(self, sf, rcut, conv_z2r, conv_frho):
+        frho = np.ascontiguousarray(np.stack(sf.frho), np.float64)
+        rhor = np.ascontiguousarray(np.stack(sf.rhor), np.float64)
+        z2r = np.ascontiguousarray(np.stack(sf.z2r), np.float64)
+        self._chk(self._L.gbmd_set_eam_alloy(self.h, sf.nelements, sf.nrho, sf.drho, sf.nr, sf.dr, _p(frho),
+                                             _p(rhor), _p(z2r), float(rcut), float(conv_z2r), float(conv_frho)))
+
+    def load_setfl(self, path, rcut, conv_z2r, conv_frho):
+        self._chk(self._L.gbmd_load_setfl(self.h, path.encode(), float(rcut), float(conv_z2r), float(conv_frho)))
+
+    def set_precision(self, mixed: bool):
+        self._chk(self._L.gbmd_set_precision(self.h, PRECISION_MIXED if mixed else PRECISION_FP64))
+
+    def set_launch(self, lanes_per_atom, block):
+        self._chk(self._L.gbmd_set_launch(self.h, int(lanes_per_atom), int(block)))
+
+    def get_launch(self):
+        t, b = C.c_int(), C.c_int()
+        self._chk(self._L.gbmd_get_launch(self.h, C.byref(t), C.byref(b)))
+        return t.value, b.value
+
+    def set_skin(self, skin):
+        self._chk(self._L.gbmd_set_skin(self.h, float(skin)))
+
+    # -- operators --------------------------------------------------------
+    def build_neighbors(self):
+        self._chk(self._L.gbmd_build_neighbors(self.h))
+
+    def export_pairs(self):
+        cnt = C.c_int64()
+        self._chk(self._L.gbmd_export_pairs(self.h, 0, None, None, None, C.byref(cnt)))
+        n = cnt.value
+        a = np.empty(max(n, 1), np.uint64)
+        b = np.empty(max(n, 1), np.uint64)
+        img = np.empty((max(n, 1), 3), np.int8)
+        self._chk(self._L.gbmd_export_pairs(self.h, n, _p(a), _p(b), _p(img), C.byref(cnt)))
+        return np.column_stack([a[:n].astype(np.int64), b[:n].astype(np.int64), img[:n].astype(np.int64)])
+
+    def neighbor_stats(self):
+        npairs, maxnb = C.c_int64(), C.c_int()
+        nc = np.zeros(3, np.int32)
+        self._chk(self._L.gbmd_neighbor_stats(self.h, C.byref(npairs), C.byref(maxnb), _p(nc)))
+        return npairs.value, maxnb.value, nc
+
+    def compute_forces(self, energy=True, virial=False):
+        flags = (FORCE_ENERGY if energy else 0) | (FORCE_VIRIAL if virial else 0)
+        self._chk(self._L.gbmd_compute_forces(self.h, flags))
+
+    def push_f_v_r(self, dt, dt_scale=1.0):
+        self._chk(self._L.gbmd_push_f_v_r(self.h, float(dt), float(dt_scale)))
+
+    def push_f_v(self, dt, dt_scale=0.5):
+        self._chk(self._L.gbmd_push_f_v(self.h, float(dt), float(dt_scale)))
+
+    def push_min(self, dt, dt_scale=1.0, tolF=0.0):
+        self._chk(self._L.gbmd_push_min(self.h, float(dt), float(dt_scale), float(tolF)))
+
+    def run_nve(self, nsteps, dt, rebuild_every=10, thermo_every=0, use_graph=False):
+        rows = (nsteps // thermo_every + 1) if thermo_every > 0 else 0
+        out = np.zeros((max(rows, 1), 27))
+        self._chk(self._L.gbmd_run_nve(self.h, int(nsteps), float(dt), int(rebuild_every), int(thermo_every),
+                                       _p(out) if rows else None, 1 if use_graph else 0))
+        return out[:rows] if rows else None
+
+    def run_minimize(self, nsteps, dt, tolF=0.0, rebuild_every=10):
+        self._chk(self._L.gbmd_run_minimize(self.h, int(nsteps), float(dt), float(tolF), int(rebuild_every)))
+
+    def thermo(self):
+        out = np.zeros(27)
+        self._chk(self._L.gbmd_thermo(self.h, _p(out)))
+        return out
+
+    def synchronize(self):
+        self._chk(self._L.gbmd_synchronize(self.h))

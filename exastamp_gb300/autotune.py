@@ -1,0 +1,75 @@
+"""Autotuner for the pair kernels' launch shape.
+
+The knobs are the lanes that share one atom's neighbour list (1-16; more
+lanes give more parallelism for small systems, fewer lanes avoid the
+per-atom shuffle reduction for large ones) and the threads per block.  Each
+candidate is timed with gbmd_profile_step (CUDA events on the context's
+stream, density + final pair kernel) and the fastest is kept.  Results are
+cached in a JSON file keyed by GPU name, workload key and atom count
+($GBMD_AUTOTUNE_CACHE, default ~/.cache/exastamp_gb300/autotune.json).
+"""
+from __future__ import annotations
+
+import json
+import os
+
+LANES = (1, 2, 4, 8, 16)
+BLOCKS = (128, 256)
+
+
+def _cache_path():
+    return os.environ.get("GBMD_AUTOTUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "exastamp_gb300", "autotune.json"))
+
+
+def _gpu_name():
+    try:
+        import torch
+        return torch.cuda.get_device_name(0)
+    except Exception:
+        return "unknown"
+
+
+def _load():
+    try:
+        with open(_cache_path()) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
+def _store(d):
+    p = _cache_path()
+    try:
+        os.makedirs(os.path.dirname(p), exist_ok=True)
+        with open(p + ".tmp", "w") as fh:
+            json.dump(d, fh, indent=1)
+        os.replace(p + ".tmp", p)
+    except OSError:
+        pass
+
+
+def tune(ctx, key: str, lanes=LANES, blocks=BLOCKS, reps: int = 3, use_cache: bool = True):
+    """Return (lanes, block, timings) for this context's system and potential."""
+    n = ctx.n
+    ck = "%s|%s|%d" % (_gpu_name(), key, n)
+    cache = _load() if use_cache else {}
+    if ck in cache:
+        e = cache[ck]
+        return int(e["lanes"]), int(e["block"]), e.get("timings", {})
+    timings = {}
+    best = None
+    for t in lanes:
+        for b in blocks:
+            if b % t:
+                continue
+            ctx.set_launch(t, b)
+            prof = ctx.profile_step(reps=reps)
+            ms = prof["density"] + prof["pair"]
+            timings["%dx%d" % (t, b)] = ms
+            if best is None or ms < best[0]:
+                best = (ms, t, b)
+    cache[ck] = {"lanes": best[1], "block": best[2], "timings": timings}
+    if use_cache:
+        _store(cache)
+    return best[1], best[2], timings

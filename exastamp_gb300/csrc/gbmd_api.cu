@@ -1,0 +1,925 @@
+// gbmd_api.cu -- the C ABI (include/gbmd.h): contexts, atom transfer,
+// potential set-up, operators and the verlet_nve runner.
+//
+// The host side mirrors the reference operators that the onika graph binds
+// into the compute_force / verlet_first_half / verlet_second_half /
+// update_particle_neighbors slots (data/config/config_numerical_schemes.msp
+// L8-52, data/config/config_move_particles.msp L54-68).
+#include <cerrno>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+#include "gbmd_internal.cuh"
+
+namespace gbmd {
+
+int set_error(gbmd_context* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+int check_cuda(gbmd_context* c, cudaError_t e, const char* what) {
+  return set_error(c, GBMD_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int sync_error_word(gbmd_context* c) {
+  GBMD_CUDA(c, cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int) * 8, cudaMemcpyDeviceToHost, c->stream));
+  GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBMD_OK;
+}
+
+static void free_atoms(gbmd_context* c) {
+  for (int b = 0; b < 2; ++b) {
+    cudaFree(c->rbuf[b]); cudaFree(c->vbuf[b]); cudaFree(c->abuf[b]);
+    cudaFree(c->posf[b]); cudaFree(c->posd[b]);
+    cudaFree(c->typeb[b]); cudaFree(c->idb[b]); cudaFree(c->userb[b]);
+    c->rbuf[b] = c->vbuf[b] = c->abuf[b] = nullptr;
+    c->posf[b] = nullptr; c->posd[b] = nullptr;
+    c->typeb[b] = nullptr; c->idb[b] = nullptr; c->userb[b] = nullptr;
+  }
+  cudaFree(c->ep); cudaFree(c->vir); cudaFree(c->cellpack); cudaFree(c->cell_of);
+  cudaFree(c->order); cudaFree(c->src); cudaFree(c->fpf); cudaFree(c->fpd); cudaFree(c->epf);
+  cudaFree(c->stage); cudaFree(c->rref); cudaFree(c->nnb); cudaFree(c->d_part);
+  c->ep = c->vir = nullptr;
+  c->cellpack = c->cell_of = c->order = c->src = nullptr;
+  c->fpf = c->epf = nullptr;
+  c->fpd = c->stage = c->rref = nullptr;
+  c->nnb = nullptr;
+  c->d_part = nullptr;
+  c->cap = 0;
+}
+
+int ensure_atom_capacity(gbmd_context* c, int64_t n) {
+  if (n <= c->cap) return GBMD_OK;
+  free_atoms(c);
+  const int64_t cap = n;
+  const size_t d3 = sizeof(double) * 3 * cap;
+  for (int b = 0; b < 2; ++b) {
+    GBMD_CUDA(c, cudaMalloc(&c->rbuf[b], d3));
+    GBMD_CUDA(c, cudaMalloc(&c->vbuf[b], d3));
+    GBMD_CUDA(c, cudaMalloc(&c->abuf[b], d3));
+    GBMD_CUDA(c, cudaMalloc(&c->posf[b], sizeof(float4) * cap));
+    GBMD_CUDA(c, cudaMalloc(&c->posd[b], sizeof(double4_32a) * cap));
+    GBMD_CUDA(c, cudaMalloc(&c->typeb[b], cap));
+    GBMD_CUDA(c, cudaMalloc(&c->idb[b], sizeof(uint64_t) * cap));
+    GBMD_CUDA(c, cudaMalloc(&c->userb[b], sizeof(int32_t) * cap));
+  }
+  GBMD_CUDA(c, cudaMalloc(&c->ep, sizeof(double) * cap));
+  GBMD_CUDA(c, cudaMalloc(&c->cellpack, sizeof(int32_t) * cap));
+  GBMD_CUDA(c, cudaMalloc(&c->cell_of, sizeof(int32_t) * cap));
+  GBMD_CUDA(c, cudaMalloc(&c->order, sizeof(int32_t) * cap));
+  GBMD_CUDA(c, cudaMalloc(&c->src, sizeof(int32_t) * cap));
+  GBMD_CUDA(c, cudaMalloc(&c->fpf, sizeof(float) * cap));
+  GBMD_CUDA(c, cudaMalloc(&c->epf, sizeof(float) * cap));
+  GBMD_CUDA(c, cudaMalloc(&c->fpd, sizeof(double) * cap));
+  GBMD_CUDA(c, cudaMalloc(&c->stage, sizeof(double) * 9 * cap));
+  GBMD_CUDA(c, cudaMalloc(&c->rref, d3));
+  GBMD_CUDA(c, cudaMalloc(&c->nnb, sizeof(int32_t) * cap));
+  GBMD_CUDA(c, cudaMalloc(&c->d_part, sizeof(double) * 26 * thermo_blocks(cap)));
+  c->cap = cap;
+  c->cur = c->cur_s = 0;
+  return GBMD_OK;
+}
+
+static void drop_graph(gbmd_context* c) {
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  c->graph_exec = nullptr;
+}
+
+static void invalidate_list(gbmd_context* c) {
+  c->list_valid = false;
+  c->forces_valid_step = -1;
+  drop_graph(c);
+}
+
+static void set_rlist(gbmd_context* c, double rcut_max) {
+  const double R = rcut_max + c->skin;
+  if (R != c->rlist) {
+    c->rlist = R;
+    c->grid_valid = false;
+    c->maxnb = 0;
+  }
+  invalidate_list(c);
+}
+
+static double pot_rcut_max(const gbmd_context* c) {
+  if (c->pot == GBMD_POT_LJ || c->pot == GBMD_POT_LJ_MULTI) return c->lj.rcut_max;
+  if (c->pot == GBMD_POT_EAM_ALLOY) return c->eam.rcut;
+  return 0.0;
+}
+
+// --- device helpers for reordering ----------------------------------------
+__global__ void k_to_user(int64_t n, const double* __restrict__ src, const int32_t* __restrict__ user,
+                          double* __restrict__ dst, int width) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int64_t u = user[p];
+  for (int q = 0; q < width; ++q) dst[u * width + q] = src[p * width + q];
+}
+
+__global__ void k_from_user(int64_t n, const double* __restrict__ src, const int32_t* __restrict__ user,
+                            double* __restrict__ dst) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  dst[p] = src[user[p]];
+}
+
+__global__ void k_iota(int64_t n, int32_t* __restrict__ user, uint64_t* __restrict__ id, int with_id) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  user[p] = (int32_t)p;
+  if (with_id) id[p] = (uint64_t)p;
+}
+
+__global__ void k_displ_over(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
+                             const double* __restrict__ z, const double* __restrict__ rref, int64_t cap,
+                             double thr2, int* __restrict__ flag) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const double dx = x[p] - rref[p], dy = y[p] - rref[cap + p], dz = z[p] - rref[2 * cap + p];
+  if (dx * dx + dy * dy + dz * dz > thr2) *flag = 1;
+}
+
+static inline unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+
+static int copy_rref(gbmd_context* c) {
+  for (int d = 0; d < 3; ++d)
+    GBMD_CUDA(c, cudaMemcpyAsync(c->rref + d * c->cap, c->rbuf[c->cur] + d * c->cap, sizeof(double) * c->n,
+                                 cudaMemcpyDeviceToDevice, c->stream));
+  return GBMD_OK;
+}
+
+static int do_rebuild(gbmd_context* c, bool check) {
+  int rc = rebuild(c, check);
+  if (rc) return rc;
+  return copy_rref(c);
+}
+
+// --- EAM spline build (eam_alloy.cpp L29-58, LAMMPS array2spline) ---------
+static void spline7(int n, double delta, const double* f /* 1..n */, double* s /* (n+1) x 8 */) {
+#define S(m, k) s[(size_t)(m) * 8 + (k)]
+  std::memset(s, 0, sizeof(double) * 8 * (size_t)(n + 1));
+  for (int m = 1; m <= n; m++) S(m, 6) = f[m];
+  S(1, 5) = S(2, 6) - S(1, 6);
+  S(2, 5) = 0.5 * (S(3, 6) - S(1, 6));
+  S(n - 1, 5) = 0.5 * (S(n, 6) - S(n - 2, 6));
+  S(n, 5) = S(n, 6) - S(n - 1, 6);
+  for (int m = 3; m <= n - 2; m++)
+    S(m, 5) = ((S(m - 2, 6) - S(m + 2, 6)) + 8.0 * (S(m + 1, 6) - S(m - 1, 6))) / 12.0;
+  for (int m = 1; m <= n - 1; m++) {
+    S(m, 4) = 3.0 * (S(m + 1, 6) - S(m, 6)) - 2.0 * S(m, 5) - S(m + 1, 5);
+    S(m, 3) = S(m, 5) + S(m + 1, 5) - 2.0 * (S(m + 1, 6) - S(m, 6));
+  }
+  S(n, 4) = 0.0;
+  S(n, 3) = 0.0;
+  for (int m = 1; m <= n; m++) {
+    S(m, 2) = S(m, 5) / delta;
+    S(m, 1) = 2.0 * S(m, 4) / delta;
+    S(m, 0) = 3.0 * S(m, 3) / delta;
+  }
+#undef S
+}
+
+}  // namespace gbmd
+
+using namespace gbmd;
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int gbmd_abi_version(void) { return GBMD_ABI_VERSION; }
+
+const char* gbmd_last_error(const gbmd_context* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int gbmd_create(gbmd_context** out, int device, void* stream) {
+  if (!out) return GBMD_ERR_INVALID;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GBMD_ERR_NO_DEVICE;
+  if (device < 0 || device >= ndev) return GBMD_ERR_INVALID;
+  gbmd_context* c = new gbmd_context();
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess) {
+    delete c;
+    return GBMD_ERR_CUDA;
+  }
+  if (stream) {
+    c->stream = (cudaStream_t)stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete c;
+      return GBMD_ERR_CUDA;
+    }
+    c->own_stream = true;
+  }
+  if (cudaMalloc(&c->d_err, sizeof(int) * 8) != cudaSuccess ||
+      cudaMallocHost(&c->h_err, sizeof(int) * 8) != cudaSuccess ||
+      cudaMalloc(&c->d_thermo, sizeof(double) * 27) != cudaSuccess ||
+      cudaMallocHost(&c->h_thermo, sizeof(double) * 27) != cudaSuccess) {
+    gbmd_destroy(c);
+    return GBMD_ERR_CUDA;
+  }
+  int init[8] = {0, 0, 0, -1, -1, 0, 0, 0};
+  cudaMemcpy(c->d_err, init, sizeof(init), cudaMemcpyHostToDevice);
+  *out = c;
+  return GBMD_OK;
+}
+
+int gbmd_destroy(gbmd_context* c) {
+  if (!c) return GBMD_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  drop_graph(c);
+  free_atoms(c);
+  cudaFree(c->cell_start); cudaFree(c->cell_fill); cudaFree(c->scan_tmp); cudaFree(c->nbr);
+  cudaFree(c->eam_d); cudaFree(c->eam_f); cudaFree(c->lj_tab_d);
+  cudaFree(c->d_err); cudaFree(c->d_thermo); cudaFree(c->d_rows);
+  if (c->h_err) cudaFreeHost(c->h_err);
+  if (c->h_thermo) cudaFreeHost(c->h_thermo);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return GBMD_OK;
+}
+
+int gbmd_synchronize(gbmd_context* c) {
+  if (!c) return GBMD_ERR_INVALID;
+  GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBMD_OK;
+}
+
+int gbmd_set_box(gbmd_context* c, const double lo[3], const double hi[3], const int periodic[3]) {
+  if (!c || !lo || !hi) return GBMD_ERR_INVALID;
+  for (int d = 0; d < 3; ++d) {
+    if (!(hi[d] > lo[d])) return set_error(c, GBMD_ERR_INVALID, "box hi must exceed lo");
+    if (periodic && !periodic[d]) return set_error(c, GBMD_ERR_UNSUPPORTED, "only periodic boxes are supported");
+  }
+  for (int d = 0; d < 3; ++d) {
+    c->lo[d] = lo[d];
+    c->hi[d] = hi[d];
+  }
+  c->box_set = true;
+  c->grid_valid = false;
+  invalidate_list(c);
+  return GBMD_OK;
+}
+
+int gbmd_set_species(gbmd_context* c, int ntypes, const double* masses) {
+  if (!c || ntypes < 1 || ntypes > GBMD_MAX_TYPES || !masses)
+    return set_error(c, GBMD_ERR_INVALID, "ntypes must be in [1,%d]", GBMD_MAX_TYPES);
+  for (int t = 0; t < ntypes; ++t)
+    if (!(masses[t] > 0.0)) return set_error(c, GBMD_ERR_INVALID, "masses must be positive");
+  if (c->n > 0 && ntypes < c->ntypes)
+    return set_error(c, GBMD_ERR_INVALID, "cannot drop species while atoms are loaded");
+  c->ntypes = ntypes;
+  for (int t = 0; t < ntypes; ++t) c->mass[t] = masses[t];
+  drop_graph(c);
+  return GBMD_OK;
+}
+
+int gbmd_upload_atoms(gbmd_context* c, int64_t n, const double* rx, const double* ry, const double* rz,
+                      const double* vx, const double* vy, const double* vz, const uint8_t* type,
+                      const uint64_t* id) {
+  if (!c || n < 0 || (n > 0 && (!rx || !ry || !rz))) return set_error(c, GBMD_ERR_INVALID, "bad atom arrays");
+  if (n > GBMD_MAX_ATOMS) return set_error(c, GBMD_ERR_TOO_LARGE, "at most %lld atoms", (long long)GBMD_MAX_ATOMS);
+  if (c->ntypes < 1) return set_error(c, GBMD_ERR_INVALID, "call gbmd_set_species first");
+  if (type)
+    for (int64_t i = 0; i < n; ++i)
+      if (type[i] >= c->ntypes) return set_error(c, GBMD_ERR_INVALID, "atom %lld has type %d >= ntypes", (long long)i, type[i]);
+  cudaSetDevice(c->device);
+  GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
+  int rc = ensure_atom_capacity(c, n > 0 ? n : 1);
+  if (rc) return rc;
+  c->n = n;
+  cudaStream_t s = c->stream;
+  const size_t b = sizeof(double) * n;
+  const int64_t cap = c->cap;
+  const double* r[3] = {rx, ry, rz};
+  const double* v[3] = {vx, vy, vz};
+  for (int d = 0; d < 3; ++d) {
+    GBMD_CUDA(c, cudaMemcpyAsync(c->rbuf[c->cur] + d * cap, r[d], b, cudaMemcpyHostToDevice, s));
+    if (v[d]) GBMD_CUDA(c, cudaMemcpyAsync(c->vbuf[c->cur_s] + d * cap, v[d], b, cudaMemcpyHostToDevice, s));
+    else GBMD_CUDA(c, cudaMemsetAsync(c->vbuf[c->cur_s] + d * cap, 0, b, s));
+    GBMD_CUDA(c, cudaMemsetAsync(c->abuf[c->cur_s] + d * cap, 0, b, s));
+  }
+  if (type) GBMD_CUDA(c, cudaMemcpyAsync(c->TYPE(), type, n, cudaMemcpyHostToDevice, s));
+  else GBMD_CUDA(c, cudaMemsetAsync(c->TYPE(), 0, n, s));
+  if (id) GBMD_CUDA(c, cudaMemcpyAsync(c->ID(), id, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, s));
+  GBMD_CUDA(c, cudaMemsetAsync(c->ep, 0, b, s));
+  if (n > 0) k_iota<<<nblk(n, 256), 256, 0, s>>>(n, c->USER(), c->ID(), id ? 0 : 1);
+  int init[8] = {0, 0, 0, -1, -1, 0, 0, 0};
+  GBMD_CUDA(c, cudaMemcpyAsync(c->d_err, init, sizeof(init), cudaMemcpyHostToDevice, s));
+  GBMD_CUDA(c, cudaStreamSynchronize(s));
+  invalidate_list(c);
+  return GBMD_OK;
+}
+
+int gbmd_upload_positions(gbmd_context* c, const double* rx, const double* ry, const double* rz,
+                          const double* vx, const double* vy, const double* vz) {
+  if (!c || !rx || !ry || !rz) return GBMD_ERR_INVALID;
+  const int64_t n = c->n, cap = c->cap;
+  if (n == 0) return GBMD_OK;
+  cudaStream_t s = c->stream;
+  const double* r[3] = {rx, ry, rz};
+  const double* v[3] = {vx, vy, vz};
+  for (int d = 0; d < 3; ++d) {
+    GBMD_CUDA(c, cudaMemcpyAsync(c->stage + d * cap, r[d], sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    k_from_user<<<nblk(n, 256), 256, 0, s>>>(n, c->stage + d * cap, c->USER(), c->rbuf[c->cur] + d * cap);
+  }
+  if (vx && vy && vz)
+    for (int d = 0; d < 3; ++d) {
+      GBMD_CUDA(c, cudaMemcpyAsync(c->stage + d * cap, v[d], sizeof(double) * n, cudaMemcpyHostToDevice, s));
+      k_from_user<<<nblk(n, 256), 256, 0, s>>>(n, c->stage + d * cap, c->USER(), c->vbuf[c->cur_s] + d * cap);
+    }
+  c->forces_valid_step = -1;
+  if (c->list_valid) {
+    // particle_displ_over: rebuild when an atom moved more than skin/2 since
+    // the last rebuild (config_move_particles.msp L19-22, L116-118)
+    GBMD_CUDA(c, cudaMemsetAsync(c->d_err + 7, 0, sizeof(int), s));
+    const double thr = 0.5 * c->skin;
+    k_displ_over<<<nblk(n, 256), 256, 0, s>>>(n, c->X(), c->Y(), c->Z(), c->rref, cap, thr * thr, c->d_err + 7);
+    int rc = sync_error_word(c);
+    if (rc) return rc;
+    if (c->h_err[7]) invalidate_list(c);
+    else launch_posf(c);
+  }
+  return GBMD_OK;
+}
+
+int gbmd_upload_state(gbmd_context* c, const double* rx, const double* ry, const double* rz, const double* vx,
+                      const double* vy, const double* vz, const double* ax, const double* ay, const double* az) {
+  if (!c || !vx || !vy || !vz || !ax || !ay || !az) return GBMD_ERR_INVALID;
+  int rc = gbmd_upload_positions(c, rx, ry, rz, vx, vy, vz);
+  if (rc) return rc;
+  const int64_t n = c->n, cap = c->cap;
+  if (n == 0) return GBMD_OK;
+  cudaStream_t s = c->stream;
+  const double* a[3] = {ax, ay, az};
+  for (int d = 0; d < 3; ++d) {
+    GBMD_CUDA(c, cudaMemcpyAsync(c->stage + d * cap, a[d], sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    k_from_user<<<nblk(n, 256), 256, 0, s>>>(n, c->stage + d * cap, c->USER(), c->abuf[c->cur_s] + d * cap);
+  }
+  c->forces_valid_step = c->step;
+  return GBMD_OK;
+}
+
+int gbmd_download(gbmd_context* c, double* rx, double* ry, double* rz, double* vx, double* vy, double* vz,
+                  double* ax, double* ay, double* az, double* ep, double* vir) {
+  if (!c) return GBMD_ERR_INVALID;
+  const int64_t n = c->n;
+  if (n == 0) return GBMD_OK;
+  cudaStream_t s = c->stream;
+  struct F {
+    double* host;
+    const double* dev;
+    int width;
+  } f[11] = {{rx, c->X(), 1}, {ry, c->Y(), 1}, {rz, c->Z(), 1}, {vx, c->VX(), 1}, {vy, c->VY(), 1},
+             {vz, c->VZ(), 1}, {ax, c->AX(), 1}, {ay, c->AY(), 1}, {az, c->AZ(), 1}, {ep, c->ep, 1},
+             {vir, c->vir, 9}};
+  for (int k = 0; k < 11; ++k) {
+    if (!f[k].host) continue;
+    if (!f[k].dev) {
+      std::memset(f[k].host, 0, sizeof(double) * n * f[k].width);
+      continue;
+    }
+    k_to_user<<<nblk(n, 256), 256, 0, s>>>(n, f[k].dev, c->USER(), c->stage, f[k].width);
+    GBMD_CUDA(c, cudaMemcpyAsync(f[k].host, c->stage, sizeof(double) * n * f[k].width, cudaMemcpyDeviceToHost, s));
+  }
+  GBMD_CUDA(c, cudaStreamSynchronize(s));
+  return GBMD_OK;
+}
+
+int gbmd_num_atoms(const gbmd_context* c, int64_t* n) {
+  if (!c || !n) return GBMD_ERR_INVALID;
+  *n = c->n;
+  return GBMD_OK;
+}
+
+static double lj_e(double eps, double sig, double r) {
+  const double ratio = sig / r;
+  const double ratio2 = ratio * ratio;
+  const double ratio6 = ratio2 * ratio2 * ratio2;
+  const double ratio12 = ratio6 * ratio6;
+  return 4. * eps * (ratio12 - ratio6);
+}
+
+static LJPair make_pair(double eps, double sig, double rc) {
+  LJPair p{};
+  p.eps = eps;
+  p.sig = sig;
+  p.rc = rc;
+  p.ecut = rc > 0.0 ? lj_e(eps, sig, rc) : 0.0;
+  p.rc2 = rc * rc;
+  p.sig2f = (float)(sig * sig);
+  p.eps24f = (float)(24.0 * eps);
+  p.eps4f = (float)(4.0 * eps);
+  p.ecutf = (float)p.ecut;
+  p.rc2f = (float)p.rc2;
+  p.rc2lo = (float)(p.rc2 * (1.0 - 0x1p-12));
+  p.rc2hi = (float)(p.rc2 * (1.0 + 0x1p-12));
+  return p;
+}
+
+int gbmd_set_lj(gbmd_context* c, double epsilon, double sigma, double rcut) {
+  if (!c || !(rcut > 0.0) || !(sigma > 0.0)) return set_error(c, GBMD_ERR_INVALID, "bad LJ parameters");
+  c->pot = GBMD_POT_LJ;
+  c->lj.ntypes = 1;
+  c->lj.p[0] = make_pair(epsilon, sigma, rcut);
+  c->lj.rcut_max = rcut;
+  c->lj.rcut_max2 = rcut * rcut;
+  set_rlist(c, rcut);
+  return GBMD_OK;
+}
+
+int gbmd_set_lj_multi(gbmd_context* c, int ntypes, const double* eps, const double* sig, const double* rc,
+                      double rcut_common) {
+  if (!c || ntypes < 1 || ntypes > GBMD_MAX_TYPES || !eps || !sig || !rc)
+    return set_error(c, GBMD_ERR_INVALID, "bad LJ multi tables");
+  double rmax = rcut_common;
+  for (int q = 0; q < ntypes * ntypes; ++q) rmax = rmax > rc[q] ? rmax : rc[q];
+  if (!(rmax > 0.0)) return set_error(c, GBMD_ERR_INVALID, "cutoffs must be positive");
+  for (int a = 0; a < ntypes; ++a)
+    for (int b = 0; b < ntypes; ++b) {
+      const int q = a * ntypes + b, t = b * ntypes + a;
+      if (eps[q] != eps[t] || sig[q] != sig[t] || rc[q] != rc[t])
+        return set_error(c, GBMD_ERR_INVALID, "type-pair tables must be symmetric");
+      c->lj.p[q] = make_pair(eps[q], sig[q] > 0 ? sig[q] : 1.0, rc[q]);
+      if (!(sig[q] > 0)) c->lj.p[q].eps = 0.0, c->lj.p[q].eps24f = 0.f, c->lj.p[q].eps4f = 0.f;
+    }
+  c->pot = GBMD_POT_LJ_MULTI;
+  c->lj.ntypes = ntypes;
+  c->lj.rcut_max = rmax;
+  c->lj.rcut_max2 = rmax * rmax;
+  if (!c->lj_tab_d) GBMD_CUDA(c, cudaMalloc(&c->lj_tab_d, sizeof(LJPair) * GBMD_MAX_TYPES * GBMD_MAX_TYPES));
+  GBMD_CUDA(c, cudaMemcpy(c->lj_tab_d, c->lj.p, sizeof(LJPair) * ntypes * ntypes, cudaMemcpyHostToDevice));
+  set_rlist(c, rmax);
+  return GBMD_OK;
+}
+
+int gbmd_set_eam_alloy(gbmd_context* c, int nel, int nrho, double drho, int nr, double dr, const double* frho,
+                       const double* rhor, const double* z2r, double rcut, double conv_z2r, double conv_frho) {
+  if (!c || nel < 1 || nel > 7 || nrho < 5 || nr < 5 || !(drho > 0) || !(dr > 0) || !frho || !rhor || !z2r ||
+      !(rcut > 0))
+    return set_error(c, GBMD_ERR_INVALID, "bad eam_alloy tables");
+  const int npairs = nel * (nel + 1) / 2;
+  const size_t kr = (size_t)nr + 1, kp = (size_t)nrho + 1;
+  c->eam_host_frho.assign(nel * kp * 8, 0.0);
+  c->eam_host_rhor.assign(nel * kr * 8, 0.0);
+  c->eam_host_z2r.assign(npairs * kr * 8, 0.0);
+  std::vector<double> f(std::max(kr, kp));
+  for (int e = 0; e < nel; ++e) {
+    for (int k = 0; k < nrho; ++k) f[k + 1] = frho[(size_t)e * nrho + k];
+    spline7(nrho, drho, f.data(), &c->eam_host_frho[e * kp * 8]);
+    for (int k = 0; k < nr; ++k) f[k + 1] = rhor[(size_t)e * nr + k];
+    spline7(nr, dr, f.data(), &c->eam_host_rhor[e * kr * 8]);
+  }
+  for (int q = 0; q < npairs; ++q) {
+    for (int k = 0; k < nr; ++k) f[k + 1] = z2r[(size_t)q * nr + k];
+    spline7(nr, dr, f.data(), &c->eam_host_z2r[q * kr * 8]);
+  }
+  const size_t nd = c->eam_host_frho.size() + c->eam_host_rhor.size() + c->eam_host_z2r.size();
+  const size_t nf = nel * kp + nel * kr + npairs * kr;
+  cudaFree(c->eam_d);
+  cudaFree(c->eam_f);
+  c->eam_d = nullptr;
+  c->eam_f = nullptr;
+  GBMD_CUDA(c, cudaMalloc(&c->eam_d, sizeof(double) * nd));
+  GBMD_CUDA(c, cudaMalloc(&c->eam_f, sizeof(float4) * nf));
+  std::vector<double> hd;
+  hd.reserve(nd);
+  hd.insert(hd.end(), c->eam_host_frho.begin(), c->eam_host_frho.end());
+  hd.insert(hd.end(), c->eam_host_rhor.begin(), c->eam_host_rhor.end());
+  hd.insert(hd.end(), c->eam_host_z2r.begin(), c->eam_host_z2r.end());
+  std::vector<float4> hf(nf);
+  size_t o = 0;
+  auto put = [&](const std::vector<double>& src, size_t tables, size_t knots, double scale) {
+    for (size_t t = 0; t < tables; ++t)
+      for (size_t m = 0; m < knots; ++m) {
+        const double* s = &src[(t * knots + m) * 8];
+        hf[o++] = make_float4((float)(s[3] * scale), (float)(s[4] * scale), (float)(s[5] * scale),
+                              (float)(s[6] * scale));
+      }
+  };
+  put(c->eam_host_frho, nel, kp, conv_frho);
+  put(c->eam_host_rhor, nel, kr, 1.0);
+  put(c->eam_host_z2r, npairs, kr, conv_z2r);
+  GBMD_CUDA(c, cudaMemcpy(c->eam_d, hd.data(), sizeof(double) * nd, cudaMemcpyHostToDevice));
+  GBMD_CUDA(c, cudaMemcpy(c->eam_f, hf.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice));
+  EamDev& E = c->eam;
+  E.nel = nel;
+  E.nr = nr;
+  E.nrho = nrho;
+  E.npairs = npairs;
+  E.rdr = 1.0 / dr;
+  E.rdrho = 1.0 / drho;
+  E.rhomax = (nrho - 1) * drho;
+  E.conv_z2r = conv_z2r;
+  E.conv_frho = conv_frho;
+  E.rcut = rcut;
+  E.rcut2 = rcut * rcut;
+  E.frho = c->eam_d;
+  E.rhor = c->eam_d + c->eam_host_frho.size();
+  E.z2r = E.rhor + c->eam_host_rhor.size();
+  E.frho4 = c->eam_f;
+  E.rhor4 = c->eam_f + nel * kp;
+  E.z2r4 = E.rhor4 + nel * kr;
+  E.rdrf = (float)E.rdr;
+  E.rdrhof = (float)E.rdrho;
+  E.rhomaxf = (float)E.rhomax;
+  E.rc2f = (float)E.rcut2;
+  E.rc2lo = (float)(E.rcut2 * (1.0 - 0x1p-12));
+  E.rc2hi = (float)(E.rcut2 * (1.0 + 0x1p-12));
+  c->pot = GBMD_POT_EAM_ALLOY;
+  set_rlist(c, rcut);
+  return GBMD_OK;
+}
+
+int gbmd_load_setfl(gbmd_context* c, const char* path, double rcut, double conv_z2r, double conv_frho) {
+  if (!c || !path) return GBMD_ERR_INVALID;
+  std::ifstream in(path);
+  if (!in) return set_error(c, GBMD_ERR_IO, "cannot open %s", path);
+  std::string line;
+  for (int k = 0; k < 3; ++k) std::getline(in, line);  // comment lines (eam_alloy.cpp L89-93)
+  int nel = 0;
+  in >> nel;
+  if (!in || nel < 1 || nel > 7) return set_error(c, GBMD_ERR_IO, "bad element count in %s", path);
+  for (int e = 0; e < nel; ++e) in >> line;
+  int nrho = 0, nr = 0;
+  double drho = 0, dr = 0, rc = 0;
+  in >> nrho >> drho >> nr >> dr >> rc;
+  if (!in || nrho < 5 || nr < 5) return set_error(c, GBMD_ERR_IO, "bad grid line in %s", path);
+  std::vector<double> frho((size_t)nel * nrho), rhor((size_t)nel * nr), z2r((size_t)nel * (nel + 1) / 2 * nr);
+  for (int e = 0; e < nel; ++e) {
+    int z;
+    double mass, a0;
+    std::string st;
+    in >> z >> mass >> a0 >> st;
+    for (int k = 0; k < nrho; ++k) in >> frho[(size_t)e * nrho + k];
+    for (int k = 0; k < nr; ++k) in >> rhor[(size_t)e * nr + k];
+  }
+  for (size_t k = 0; k < z2r.size(); ++k) in >> z2r[k];
+  if (!in) return set_error(c, GBMD_ERR_IO, "truncated setfl file %s", path);
+  return gbmd_set_eam_alloy(c, nel, nrho, drho, nr, dr, frho.data(), rhor.data(), z2r.data(),
+                            rcut > 0 ? rcut : rc, conv_z2r, conv_frho);
+}
+
+int gbmd_set_precision(gbmd_context* c, int precision) {
+  if (!c || (precision != GBMD_PRECISION_FP64 && precision != GBMD_PRECISION_MIXED)) return GBMD_ERR_INVALID;
+  if (c->precision != precision) {
+    c->precision = precision;
+    c->forces_valid_step = -1;
+    drop_graph(c);
+  }
+  return GBMD_OK;
+}
+
+int gbmd_set_launch(gbmd_context* c, int tpa, int block) {
+  if (!c) return GBMD_ERR_INVALID;
+  if (tpa != 1 && tpa != 2 && tpa != 4 && tpa != 8 && tpa != 16)
+    return set_error(c, GBMD_ERR_INVALID, "lanes per atom must be 1,2,4,8 or 16");
+  if (block < 32 || block > 256 || block % 32 || block % tpa)
+    return set_error(c, GBMD_ERR_INVALID, "block must be a multiple of 32 in [32,256]");
+  if (tpa != c->tpa) {
+    c->tpa = tpa;
+    if (c->maxnb > 0) c->maxnb = ((c->maxnb + tpa - 1) / tpa) * tpa;
+    invalidate_list(c);
+  }
+  c->block = block;
+  drop_graph(c);
+  return GBMD_OK;
+}
+
+int gbmd_get_launch(const gbmd_context* c, int* tpa, int* block) {
+  if (!c) return GBMD_ERR_INVALID;
+  if (tpa) *tpa = c->tpa;
+  if (block) *block = c->block;
+  return GBMD_OK;
+}
+
+int gbmd_set_skin(gbmd_context* c, double skin) {
+  if (!c || !(skin >= 0.0)) return GBMD_ERR_INVALID;
+  c->skin = skin;
+  set_rlist(c, pot_rcut_max(c));
+  return GBMD_OK;
+}
+
+int gbmd_build_neighbors(gbmd_context* c) {
+  if (!c) return GBMD_ERR_INVALID;
+  int rc = do_rebuild(c, true);
+  if (rc) return rc;
+  c->forces_valid_step = -1;
+  return GBMD_OK;
+}
+
+int gbmd_export_pairs(gbmd_context* c, int64_t cap, uint64_t* id_i, uint64_t* id_j, int8_t* img, int64_t* count) {
+  if (!c || !count) return GBMD_ERR_INVALID;
+  return export_pairs(c, cap, id_i, id_j, img, count);
+}
+
+int gbmd_neighbor_stats(gbmd_context* c, int64_t* npairs, int* maxnb, int* nc3) {
+  if (!c) return GBMD_ERR_INVALID;
+  if (npairs) {
+    int rc = export_pairs(c, 0, nullptr, nullptr, nullptr, npairs);
+    if (rc) return rc;
+  }
+  if (maxnb) *maxnb = c->maxnb;
+  if (nc3)
+    for (int d = 0; d < 3; ++d) nc3[d] = c->grid.nc[d];
+  return GBMD_OK;
+}
+
+static int ensure_list(gbmd_context* c) {
+  if (c->list_valid) return GBMD_OK;
+  return do_rebuild(c, true);
+}
+
+static int ensure_virial(gbmd_context* c) {
+  if (!c->vir && c->cap > 0) GBMD_CUDA(c, cudaMalloc(&c->vir, sizeof(double) * 9 * c->cap));
+  return GBMD_OK;
+}
+
+static int check_device_errors(gbmd_context* c) {
+  int rc = sync_error_word(c);
+  if (rc) return rc;
+  const int f = c->h_err[ERRW_FLAGS];
+  if (!f) return GBMD_OK;
+  int init[8] = {0, 0, 0, -1, -1, 0, 0, 0};
+  cudaMemcpy(c->d_err, init, sizeof(init), cudaMemcpyHostToDevice);
+  if (f & GBMD_DEVERR_LOST_ATOM) return set_error(c, GBMD_ERR_LOST_ATOM, "%d atoms lost", c->h_err[ERRW_LOST]);
+  if (f & GBMD_DEVERR_NBR_OVERFLOW)
+    return set_error(c, GBMD_ERR_NEIGHBOR_OVERFLOW, "neighbour overflow (max %d > capacity %d)",
+                     c->h_err[ERRW_MAXNB], c->maxnb);
+  if (f & GBMD_DEVERR_NONFINITE)
+    return set_error(c, GBMD_ERR_NONFINITE, "non-finite force on atom %d", c->h_err[ERRW_BADATOM]);
+  return set_error(c, GBMD_ERR_CUDA, "device error flags %d", f);
+}
+
+int gbmd_compute_forces(gbmd_context* c, int flags) {
+  if (!c) return GBMD_ERR_INVALID;
+  if (c->pot == GBMD_POT_NONE) return set_error(c, GBMD_ERR_INVALID, "no potential set");
+  cudaSetDevice(c->device);
+  int rc = ensure_list(c);
+  if (rc) return rc;
+  ForceFlags f;
+  f.energy = (flags & GBMD_FORCE_ENERGY) != 0;
+  f.virial = (flags & GBMD_FORCE_VIRIAL) != 0;
+  if (f.virial && (rc = ensure_virial(c))) return rc;
+  f.fuse = FUSE_NONE;
+  rc = launch_forces(c, f);
+  if (rc) return rc;
+  GBMD_CUDA(c, cudaGetLastError());
+  c->forces_valid_step = c->step;
+  return GBMD_OK;
+}
+
+int gbmd_push_f_v_r(gbmd_context* c, double dt, double dt_scale) {
+  if (!c) return GBMD_ERR_INVALID;
+  launch_push_f_v_r(c, dt, dt_scale);
+  c->forces_valid_step = -1;
+  GBMD_CUDA(c, cudaGetLastError());
+  return GBMD_OK;
+}
+
+int gbmd_push_f_v(gbmd_context* c, double dt, double dt_scale) {
+  if (!c) return GBMD_ERR_INVALID;
+  launch_push_f_v(c, dt, dt_scale);
+  GBMD_CUDA(c, cudaGetLastError());
+  return GBMD_OK;
+}
+
+int gbmd_push_min(gbmd_context* c, double dt, double dt_scale, double tolF) {
+  if (!c) return GBMD_ERR_INVALID;
+  launch_push_min(c, dt, dt_scale, tolF);
+  c->forces_valid_step = -1;
+  GBMD_CUDA(c, cudaGetLastError());
+  return GBMD_OK;
+}
+
+int gbmd_thermo(gbmd_context* c, double out[27]) {
+  if (!c || !out) return GBMD_ERR_INVALID;
+  launch_thermo(c, c->vir != nullptr);
+  GBMD_CUDA(c, cudaMemcpyAsync(c->h_thermo, c->d_thermo, sizeof(double) * 27, cudaMemcpyDeviceToHost, c->stream));
+  GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
+  std::memcpy(out, c->h_thermo, sizeof(double) * 27);
+  return GBMD_OK;
+}
+
+// One verlet_nve step after the first half has been applied (pending == true):
+// optional rebuild, forces with the second half fused, and either the next
+// step's first half fused (fuse 2) or, on thermo/last steps, only the second
+// half followed by the thermo reduction and a standalone first half.
+struct StepPlan {
+  bool rebuild, thermo, last;
+};
+
+static int one_step(gbmd_context* c, double dt, const StepPlan& p, bool check, double* thermo_row) {
+  int rc;
+  if (p.rebuild && (rc = do_rebuild(c, check))) return rc;
+  ForceFlags f;
+  f.energy = p.thermo;
+  f.virial = p.thermo;
+  f.sp.dt = dt;
+  f.sp.dth = dt * 0.5;
+  f.sp.dt2h = dt * dt * 0.5;
+  f.fuse = (p.thermo || p.last) ? FUSE_PUSH2 : FUSE_PUSH2_PUSH1;
+  if ((rc = launch_forces(c, f))) return rc;
+  if (p.thermo) {
+    launch_thermo(c, true);
+    if (thermo_row)
+      GBMD_CUDA(c, cudaMemcpyAsync(thermo_row, c->d_thermo, sizeof(double) * 27, cudaMemcpyDeviceToDevice, c->stream));
+    if (!p.last) launch_first_half(c, dt);
+  }
+  return GBMD_OK;
+}
+
+// A graph covers two rebuild intervals (2R steps) so that every buffer swap
+// inside it happens an even number of times and the captured pointers are
+// valid again when it is replayed.  With thermo, the reduction is captured at
+// the chunk's last step only (thermo_every == 2R).
+static int capture_graph(gbmd_context* c, double dt, int R, bool thermo_end) {
+  drop_graph(c);
+  cudaGraph_t g;
+  GBMD_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = GBMD_OK;
+  for (int l = 1; l <= 2 * R && rc == GBMD_OK; ++l) {
+    StepPlan p{l % R == 0, thermo_end && l == 2 * R, false};
+    rc = one_step(c, dt, p, false, nullptr);
+  }
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (rc) {
+    if (e == cudaSuccess) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return check_cuda(c, e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&c->graph_exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return check_cuda(c, e, "cudaGraphInstantiate");
+  c->graph_rebuild_every = R;
+  c->graph_dt = dt;
+  c->graph_thermo_end = thermo_end ? 1 : 0;
+  c->graph_key_n = c->n;
+  c->graph_key_maxnb = c->maxnb;
+  c->graph_key_tpa = c->tpa;
+  c->graph_key_block = c->block;
+  c->graph_key_prec = c->precision;
+  return GBMD_OK;
+}
+
+static bool graph_matches(const gbmd_context* c, double dt, int R, bool thermo_end) {
+  return c->graph_exec && c->graph_rebuild_every == R && c->graph_dt == dt &&
+         c->graph_thermo_end == (thermo_end ? 1 : 0) && c->graph_key_n == c->n && c->graph_key_maxnb == c->maxnb &&
+         c->graph_key_tpa == c->tpa && c->graph_key_block == c->block && c->graph_key_prec == c->precision;
+}
+
+int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int thermo_every, double* thermo_out,
+                 int use_graph) {
+  if (!c || nsteps < 0) return GBMD_ERR_INVALID;
+  if (c->pot == GBMD_POT_NONE) return set_error(c, GBMD_ERR_INVALID, "no potential set");
+  cudaSetDevice(c->device);
+  int rc = ensure_list(c);
+  if (rc) return rc;
+  if ((rc = ensure_virial(c))) return rc;
+  const bool want_thermo = thermo_every > 0;
+  // thermo rows are collected on the device and copied out once at the end,
+  // so the host never waits inside the step loop
+  const int64_t nrows = want_thermo ? nsteps / thermo_every + 1 : 0;
+  if (nrows > c->rows_cap) {
+    cudaFree(c->d_rows);
+    c->d_rows = nullptr;
+    GBMD_CUDA(c, cudaMalloc(&c->d_rows, sizeof(double) * 27 * nrows));
+    c->rows_cap = nrows;
+  }
+  double* rows = c->d_rows;
+  if (c->forces_valid_step != c->step || want_thermo) {
+    ForceFlags f;
+    f.energy = f.virial = want_thermo;
+    if ((rc = launch_forces(c, f))) return rc;
+  }
+  if (want_thermo) {
+    launch_thermo(c, true);
+    GBMD_CUDA(c, cudaMemcpyAsync(rows, c->d_thermo, sizeof(double) * 27, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  if (nsteps == 0) {
+    GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
+    return check_device_errors(c);
+  }
+  launch_first_half(c, dt);
+  const int R = rebuild_every;
+  const bool graph_ok = use_graph && R > 0 && (!want_thermo || thermo_every == 2 * R);
+  int s = 1;
+  while (s <= nsteps) {
+    // a graph chunk covers steps s..s+2R-1; it starts right after a rebuild
+    // interval and must end before the last step (which may not fuse the
+    // next first half)
+    if (graph_ok && (s - 1) % (2 * R) == 0 && s + 2 * R - 1 < nsteps) {
+      if (!graph_matches(c, dt, R, want_thermo) && (rc = capture_graph(c, dt, R, want_thermo))) return rc;
+      GBMD_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
+      if (want_thermo)
+        GBMD_CUDA(c, cudaMemcpyAsync(rows + 27 * (size_t)((s + 2 * R - 1) / thermo_every), c->d_thermo,
+                                     sizeof(double) * 27, cudaMemcpyDeviceToDevice, c->stream));
+      s += 2 * R;
+      continue;
+    }
+    StepPlan p{R > 0 && s % R == 0, want_thermo && s % thermo_every == 0, s == nsteps};
+    double* row = p.thermo ? rows + 27 * (size_t)(s / thermo_every) : nullptr;
+    if ((rc = one_step(c, dt, p, !use_graph, row))) return rc;
+    ++s;
+  }
+  GBMD_CUDA(c, cudaGetLastError());
+  if (want_thermo && thermo_out)
+    GBMD_CUDA(c, cudaMemcpyAsync(thermo_out, rows, sizeof(double) * 27 * nrows, cudaMemcpyDeviceToHost, c->stream));
+  GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->step += nsteps;
+  c->forces_valid_step = c->step;
+  return check_device_errors(c);
+}
+
+int gbmd_run_minimize(gbmd_context* c, int nsteps, double dt, double tolF, int rebuild_every) {
+  if (!c || nsteps < 0) return GBMD_ERR_INVALID;
+  int rc = ensure_list(c);
+  if (rc) return rc;
+  for (int s = 1; s <= nsteps; ++s) {
+    ForceFlags f;
+    if ((rc = launch_forces(c, f))) return rc;
+    launch_push_min(c, dt, 1.0, tolF);
+    if (rebuild_every > 0 && s % rebuild_every == 0 && (rc = do_rebuild(c, true))) return rc;
+  }
+  c->forces_valid_step = -1;
+  GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
+  return check_device_errors(c);
+}
+
+int gbmd_profile_step(gbmd_context* c, int reps, double ms[5]) {
+  if (!c || !ms || reps < 1) return GBMD_ERR_INVALID;
+  if (c->pot == GBMD_POT_NONE) return set_error(c, GBMD_ERR_INVALID, "no potential set");
+  cudaSetDevice(c->device);
+  int rc = ensure_list(c);
+  if (rc) return rc;
+  if ((rc = ensure_virial(c))) return rc;
+  cudaEvent_t e0, e1;
+  GBMD_CUDA(c, cudaEventCreate(&e0));
+  GBMD_CUDA(c, cudaEventCreate(&e1));
+  for (int k = 0; k < 5; ++k) {
+    float acc = 0.f;
+    for (int r = 0; r < reps && rc == GBMD_OK; ++r) {
+      cudaEventRecord(e0, c->stream);
+      ForceFlags f;
+      f.sp.dt = f.sp.dth = f.sp.dt2h = 0.0;
+      switch (k) {
+        case 0: rc = do_rebuild(c, false); break;
+        case 1: f.part = 1; rc = launch_forces(c, f); break;
+        case 2: f.part = 2; f.fuse = FUSE_PUSH2_PUSH1; rc = launch_forces(c, f); break;
+        case 3: launch_first_half(c, 0.0); break;
+        case 4: launch_thermo(c, true); break;
+      }
+      cudaEventRecord(e1, c->stream);
+      cudaEventSynchronize(e1);
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e0, e1);
+      acc += t;
+      if (k == 2 && (r & 1) == 0 && r + 1 == reps) {
+        // keep the double-buffer parity unchanged: one more swap
+        f.part = 2;
+        f.fuse = FUSE_PUSH2_PUSH1;
+        rc = launch_forces(c, f);
+      }
+    }
+    ms[k] = acc / reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->forces_valid_step = -1;
+  return check_device_errors(c);
+}
+
+int gbmd_device_state(gbmd_context* c, double** rx, double** ry, double** rz, double** vx, double** vy,
+                      double** vz, double** ax, double** ay, double** az, double** ep, int32_t** user) {
+  if (!c) return GBMD_ERR_INVALID;
+  if (rx) *rx = c->X();
+  if (ry) *ry = c->Y();
+  if (rz) *rz = c->Z();
+  if (vx) *vx = c->VX();
+  if (vy) *vy = c->VY();
+  if (vz) *vz = c->VZ();
+  if (ax) *ax = c->AX();
+  if (ay) *ay = c->AY();
+  if (az) *az = c->AZ();
+  if (ep) *ep = c->ep;
+  if (user) *user = c->USER();
+  return GBMD_OK;
+}
+
+}  // extern "C"

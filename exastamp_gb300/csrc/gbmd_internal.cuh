@@ -1,0 +1,298 @@
+// gbmd_internal.cuh -- shared device/host definitions of the GB300 MD hot path.
+//
+// Data layout in HBM (all per-atom arrays in cell-sorted order, rebuilt every
+// neighbour rebuild):
+//   x,y,z / vx,vy,vz / ax,ay,az / ep     FP64 SoA (positions double-buffered)
+//   type (u8), id (u64), user (i32: index in the caller's upload order)
+//   cellpack (i32): home cell at the last rebuild, cx | cy<<10 | cz<<20
+//   posf (float4): FP32 position relative to the home-cell corner, w = type bits
+//   posd (double4_32a): FP64 absolute position, w = type bits (FP64 path gathers)
+//   nbr (u32): full neighbour list entries j | code<<26, code = (dx+1)|(dy+1)<<2|(dz+1)<<4
+//              the stencil offset of j's cell; laid out for T lanes per atom as
+//              nbr[(k/T)*(npad*T) + i*T + k%T]
+//   nnb (i32): neighbours per atom
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/gbmd.h"
+
+#define GBMD_MAX_TYPES 8
+#define GBMD_IDX_BITS 26
+#define GBMD_IDX_MASK ((1u << GBMD_IDX_BITS) - 1u)
+#define GBMD_MAX_ATOMS (1ll << GBMD_IDX_BITS)
+
+// device error word layout (int[8])
+enum {
+  ERRW_FLAGS = 0,     // bitmask of GBMD_DEVERR_*
+  ERRW_MAXNB = 1,     // largest neighbour count seen by the last list build
+  ERRW_LOST = 2,      // atoms found outside the box after the wrap
+  ERRW_STEP = 3,      // step index of the first error (-1 none)
+  ERRW_BADATOM = 4,   // first offending atom (sorted index)
+};
+enum {
+  GBMD_DEVERR_NBR_OVERFLOW = 1,
+  GBMD_DEVERR_LOST_ATOM = 2,
+  GBMD_DEVERR_NONFINITE = 4,
+  GBMD_DEVERR_TABLE_RANGE = 8,
+};
+
+namespace gbmd {
+
+// Per-type-pair LJ coefficients (both precisions carried; kernels pick one).
+struct LJPair {
+  double eps, sig, rc, ecut;     // FP64 reference values
+  double rc2;                    // rc*rc
+  float sig2f, eps24f, eps4f, ecutf, rc2f, rc2lo, rc2hi, pad;
+};
+
+struct LJTable {
+  int ntypes;
+  double rcut_max, rcut_max2;
+  LJPair p[GBMD_MAX_TYPES * GBMD_MAX_TYPES];
+};
+
+// eam_alloy tables: FP64 copies in the reference's 8-double knot layout and
+// FP32 value-coefficient float4 copies (c3,c4,c5,c6) for the mixed path.
+struct EamDev {
+  int nel, nr, nrho, npairs;
+  double rdr, rdrho, rhomax, conv_z2r, conv_frho, rcut, rcut2;
+  const double* frho;  // nel x (nrho+1) x 8
+  const double* rhor;  // nel x (nr+1) x 8
+  const double* z2r;   // npairs x (nr+1) x 8
+  const float4* frho4; // nel x (nrho+1)      F * conv_frho
+  const float4* rhor4; // nel x (nr+1)
+  const float4* z2r4;  // npairs x (nr+1)      z2r * conv_z2r
+  float rdrf, rdrhof, rhomaxf, rc2f, rc2lo, rc2hi;
+};
+
+struct Grid {
+  int nc[3];
+  double h[3], L[3], lo[3];
+  float hf[3];
+  int64_t ncells;
+};
+
+struct StepParams {
+  double dt, dth, dt2h;     // dt, dt/2, dt*dt/2
+  int64_t step;             // step index (for error records)
+};
+
+}  // namespace gbmd
+
+struct gbmd_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+
+  // box
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  bool box_set = false;
+
+  // species
+  int ntypes = 0;
+  double mass[GBMD_MAX_TYPES] = {0};
+
+  // atoms (device, cell-sorted).  Each FP64 vector block holds x|y|z (3*cap);
+  // index 0/1 double-buffer them: sorts gather into the other buffer and the
+  // fused force+push kernel writes new positions there, so no kernel ever
+  // reads a neighbour position that another thread is updating.
+  int64_t n = 0, cap = 0;
+  double* rbuf[2] = {nullptr, nullptr};
+  double* vbuf[2] = {nullptr, nullptr};
+  double* abuf[2] = {nullptr, nullptr};
+  float4* posf[2] = {nullptr, nullptr};   // FP32 home-cell-relative coords, w = type bits
+  double4_32a* posd[2] = {nullptr, nullptr};  // FP64 absolute coords, w = type bits
+  uint8_t* typeb[2] = {nullptr, nullptr};
+  uint64_t* idb[2] = {nullptr, nullptr};
+  int32_t* userb[2] = {nullptr, nullptr};
+  int cur = 0;                            // which of r/posf/posd is current
+  int cur_s = 0;                          // which of v/a/type/id/user is current
+  double* ep = nullptr;
+  double* vir = nullptr;                  // 9n, allocated when virials are requested
+  int32_t* cellpack = nullptr;            // home cell at the last rebuild
+  int32_t* cell_of = nullptr;             // scratch: linear cell per atom (pre-sort order)
+  int32_t* order = nullptr;               // scratch: atoms scattered by cell
+  int32_t* src = nullptr;                 // scratch: new position -> old position
+  float* fpf = nullptr;                   // EAM F'(rho) FP32 (mixed)
+  double* fpd = nullptr;                  // EAM rho_dEmb FP64
+  double* stage = nullptr;                // 9n staging for host<->device reorders
+  double* rref = nullptr;                 // 3n positions at the last rebuild (displacement trigger)
+  float* epf = nullptr;                   // EAM embedding energy FP32 (mixed energy steps)
+
+  double* X() const { return rbuf[cur]; }
+  double* Y() const { return rbuf[cur] + cap; }
+  double* Z() const { return rbuf[cur] + 2 * cap; }
+  double* VX() const { return vbuf[cur_s]; }
+  double* VY() const { return vbuf[cur_s] + cap; }
+  double* VZ() const { return vbuf[cur_s] + 2 * cap; }
+  double* AX() const { return abuf[cur_s]; }
+  double* AY() const { return abuf[cur_s] + cap; }
+  double* AZ() const { return abuf[cur_s] + 2 * cap; }
+  uint8_t* TYPE() const { return typeb[cur_s]; }
+  uint64_t* ID() const { return idb[cur_s]; }
+  int32_t* USER() const { return userb[cur_s]; }
+  float4* POSF() const { return posf[cur]; }
+  double4_32a* POSD() const { return posd[cur]; }
+
+  // cell grid + neighbour list
+  gbmd::Grid grid{};
+  bool grid_valid = false;
+  int32_t *cell_start = nullptr, *cell_fill = nullptr;
+  int64_t cells_cap = 0;
+  int32_t* scan_tmp = nullptr;
+  int64_t scan_cap = 0;
+  uint32_t* nbr = nullptr;
+  int32_t* nnb = nullptr;
+  int64_t nbr_cap = 0;          // entries allocated
+  int maxnb = 0;                // per-atom capacity (multiple of tpa)
+  int tpa = 4;                  // lanes per atom (autotuned)
+  int block = 128;              // threads per block (autotuned)
+  double skin = 0.0, rlist = 0.0;
+  bool list_valid = false;
+  int64_t list_builds = 0;
+  int64_t npad = 0;
+
+  // potential
+  int pot = GBMD_POT_NONE;
+  gbmd::LJTable lj{};
+  gbmd::EamDev eam{};
+  double* eam_d = nullptr;      // device FP64 tables (one allocation)
+  float4* eam_f = nullptr;      // device FP32 tables (one allocation)
+  gbmd::LJPair* lj_tab_d = nullptr;  // device copy of the type-pair LJ table
+  std::vector<double> eam_host_frho, eam_host_rhor, eam_host_z2r;  // spline copies for the adjoint
+
+  int precision = GBMD_PRECISION_FP64;
+
+  // errors + reductions
+  int* d_err = nullptr;
+  int* h_err = nullptr;         // pinned
+  double* d_part = nullptr;     // per-block thermo partials
+  int64_t part_cap = 0;
+  double* d_thermo = nullptr;   // 27
+  double* h_thermo = nullptr;   // pinned 27
+  double* d_rows = nullptr;     // thermo rows of a run (27 per row)
+  int64_t rows_cap = 0;
+
+  int64_t step = 0;
+  int64_t forces_valid_step = -1;
+
+  // CUDA graph of a chunk of steps
+  cudaGraphExec_t graph_exec = nullptr;
+  int graph_rebuild_every = 0;
+  double graph_dt = 0.0;
+  int graph_thermo_end = 0;
+  int64_t graph_key_n = -1;
+  int graph_key_maxnb = -1, graph_key_tpa = -1, graph_key_block = -1, graph_key_prec = -1;
+};
+
+// ---------------------------------------------------------------------------
+// internal launch helpers (implemented in the .cu files)
+// ---------------------------------------------------------------------------
+namespace gbmd {
+
+int set_error(gbmd_context* c, int code, const char* fmt, ...);
+int check_cuda(gbmd_context* c, cudaError_t e, const char* what);
+int ensure_atom_capacity(gbmd_context* c, int64_t n);
+int sync_error_word(gbmd_context* c);  // copies device error word, returns status
+
+// neighbours (gbmd_neighbors.cu)
+int grid_dims(const double lo[3], const double hi[3], double R, int nc[3]);
+int rebuild(gbmd_context* c, bool check_capacity);
+void launch_posf(gbmd_context* c);
+int export_pairs(gbmd_context* c, int64_t cap, uint64_t* id_i, uint64_t* id_j, int8_t* img, int64_t* count);
+
+// forces (gbmd_forces.cu)
+enum FuseMode { FUSE_NONE = 0, FUSE_PUSH2 = 1, FUSE_PUSH2_PUSH1 = 2 };
+struct ForceFlags {
+  bool energy = false, virial = false, thermo = false;
+  int fuse = FUSE_NONE;
+  int part = 0;   // 0 all kernels, 1 EAM density pass only, 2 final pair kernel only
+  StepParams sp{};
+};
+int launch_forces(gbmd_context* c, const ForceFlags& f);
+
+// integration (gbmd_integrate.cu)
+void launch_push_f_v_r(gbmd_context* c, double dt, double dt_scale);
+void launch_push_f_v(gbmd_context* c, double dt, double dt_scale);
+void launch_push_min(gbmd_context* c, double dt, double dt_scale, double tolF);
+void launch_first_half(gbmd_context* c, double dt);
+void launch_thermo(gbmd_context* c, bool with_virial);
+int thermo_blocks(int64_t n);
+
+}  // namespace gbmd
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+#define GBMD_CUDA(c, call)                                  \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return gbmd::check_cuda((c), e_, #call); \
+  } while (0)
+
+__device__ __forceinline__ void kahan_add(float& s, float& comp, float v) {
+  const float y = v - comp;
+  const float t = s + y;
+  comp = (t - s) - y;
+  s = t;
+}
+
+// Combine two compensated sums (s1 - c1) + (s2 - c2) with an exact two-sum.
+__device__ __forceinline__ void kahan_merge(float& s, float& comp, float s2, float c2) {
+  const float t = s + s2;
+  const float bb = t - s;
+  const float e = (s - (t - bb)) + (s2 - bb);
+  comp = comp + c2 - e;
+  s = t;
+}
+
+template <int T>
+__device__ __forceinline__ void group_reduce_kahan(float& s, float& c) {
+#pragma unroll
+  for (int off = T / 2; off > 0; off >>= 1) {
+    const float s2 = __shfl_xor_sync(0xffffffffu, s, off);
+    const float c2 = __shfl_xor_sync(0xffffffffu, c, off);
+    kahan_merge(s, c, s2, c2);
+  }
+}
+
+template <int T>
+__device__ __forceinline__ double group_reduce_d(double v) {
+#pragma unroll
+  for (int off = T / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+// stencil code -> offsets in {-1,0,1}
+__device__ __forceinline__ int code_dx(uint32_t code) { return int(code & 3u) - 1; }
+__device__ __forceinline__ int code_dy(uint32_t code) { return int((code >> 2) & 3u) - 1; }
+__device__ __forceinline__ int code_dz(uint32_t code) { return int((code >> 4) & 3u) - 1; }
+
+__device__ __forceinline__ float code_shift(uint32_t bits2, float h) {
+  // bits2 in {0,1,2} -> -h, 0, +h
+  return bits2 == 0u ? -h : (bits2 == 2u ? h : 0.0f);
+}
+
+__device__ __forceinline__ int image_of(int c, int d, int nc) {
+  const int cj = c + d;
+  return cj < 0 ? -1 : (cj >= nc ? 1 : 0);
+}
+
+// Exact FP64 d2 of (i, image n of j): ((xj + n*L) - xi)^2 summed left to right,
+// no contraction -- the rounding of the list builder and of the oracle.
+__device__ __forceinline__ double exact_d2(double xi, double yi, double zi, double xj, double yj,
+                                           double zj, double sx, double sy, double sz, double& dx,
+                                           double& dy, double& dz) {
+  dx = __dsub_rn(__dadd_rn(xj, sx), xi);
+  dy = __dsub_rn(__dadd_rn(yj, sy), yi);
+  dz = __dsub_rn(__dadd_rn(zj, sz), zi);
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+__device__ __forceinline__ size_t nbr_slot(int64_t i, int k, int T, int64_t stride) {
+  return (size_t)(k / T) * (size_t)stride + (size_t)i * T + (k % T);
+}

@@ -1,0 +1,480 @@
+// gbmd_neighbors.cu -- cell grid, cell sort and full neighbour list on sm_103a.
+//
+// Restates exaNBody's move_particles (periodic wrap, rebinning) and
+// chunk_neighbors with chunk_size 1 (data/config/config_move_particles.msp
+// L54-68).  The pair set is the one the reference decodes in
+// src/debug/atom_neighbors_stats.cpp L169-228: every (i, j, image n) with
+// d2 <= (rcut_max + skin)^2, d2 computed in FP64 from ((x_j + n*L) - x_i)
+// without contraction.  Candidates are screened in FP32 on home-cell-relative
+// coordinates; only those within 2^-12 of the radius are re-tested in FP64,
+// so the list is bit-identical to an all-FP64 build.
+//
+// Kernels (per rebuild):
+//   k_wrap_bin    wrap into [lo,hi), bin, count per cell        HBM: 24 B r/w + 8 B
+//   k_scan_*      exclusive scan of cell counts                 negligible
+//   k_scatter     atoms -> cell segments (atomic slot)          HBM: 12 B
+//   k_cell_rank   canonical (id, upload index) order per cell   L1-resident
+//   k_gather      permute the FP64 state into cell order        HBM: ~130 B r/w
+//   k_posf        FP32 local + FP64 packed gather copies        HBM: 24 B r, 48 B w
+//   k_build_list  27-cell stencil scan, write entries           HBM: 4 B per entry
+#include <cstdio>
+#include <cstring>
+
+#include "gbmd_internal.cuh"
+
+namespace gbmd {
+
+int grid_dims(const double lo[3], const double hi[3], double R, int nc[3]) {
+  for (int d = 0; d < 3; ++d) {
+    const double L = hi[d] - lo[d];
+    if (!(L > 0.0) || !(R > 0.0)) return -1;
+    double q = floor(L / (R * (1.0 + 0x1p-40)));
+    if (q < 1.0) return -2;
+    if (q > 1024.0) q = 1024.0;
+    nc[d] = (int)q;
+  }
+  return 0;
+}
+
+struct BoxArgs {
+  double lo[3], hi[3], L[3], inv_h[3];
+  int nc[3];
+};
+
+__global__ void k_wrap_bin(int64_t n, double* __restrict__ x, double* __restrict__ y,
+                           double* __restrict__ z, BoxArgs b, int32_t* __restrict__ cell_of,
+                           int32_t* __restrict__ cell_count, int* __restrict__ err) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double* r[3] = {x, y, z};
+  int c[3];
+  bool lost = false;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    double v = r[d][i];
+    if (v < b.lo[d]) v = __dadd_rn(v, b.L[d]);
+    else if (v >= b.hi[d]) v = __dsub_rn(v, b.L[d]);
+    if (!(v >= b.lo[d] && v < b.hi[d])) lost = true;
+    r[d][i] = v;
+    int q = (int)__dmul_rn(__dsub_rn(v, b.lo[d]), b.inv_h[d]);
+    q = q < 0 ? 0 : (q > b.nc[d] - 1 ? b.nc[d] - 1 : q);
+    c[d] = q;
+  }
+  if (lost) {
+    atomicAdd(&err[ERRW_LOST], 1);
+    atomicOr(&err[ERRW_FLAGS], GBMD_DEVERR_LOST_ATOM);
+  }
+  const int32_t lin = (int32_t)(((int64_t)c[2] * b.nc[1] + c[1]) * b.nc[0] + c[0]);
+  cell_of[i] = lin;
+  atomicAdd(&cell_count[lin], 1);
+}
+
+// --- exclusive scan (256 threads x 8 items per block) ----------------------
+constexpr int SCAN_T = 256, SCAN_I = 8, SCAN_B = SCAN_T * SCAN_I;
+
+__device__ __forceinline__ int block_exclusive(int v, int* smem, int& total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) smem[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < (int)(blockDim.x >> 5) ? smem[lane] : 0;
+    int wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += t;
+    }
+    if (lane < (int)(blockDim.x >> 5)) smem[lane] = wi - w;
+    if (lane == 31) smem[32] = wi;
+  }
+  __syncthreads();
+  total = smem[32];
+  const int r = smem[wid] + inc - v;
+  __syncthreads();
+  return r;
+}
+
+// in[0..n) -> out[0..n] exclusive (out[n] = total when this block holds n)
+__global__ void k_scan_block(const int32_t* __restrict__ in, int32_t* __restrict__ out, int64_t n,
+                             int32_t* __restrict__ sums) {
+  __shared__ int smem[33];
+  const int64_t base = (int64_t)blockIdx.x * SCAN_B + (int64_t)threadIdx.x * SCAN_I;
+  int it[SCAN_I];
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_I; ++k) {
+    const int64_t q = base + k;
+    it[k] = q < n ? in[q] : 0;
+    s += it[k];
+  }
+  int total;
+  int off = block_exclusive(s, smem, total);
+#pragma unroll
+  for (int k = 0; k < SCAN_I; ++k) {
+    const int64_t q = base + k;
+    if (q <= n) out[q] = off;
+    off += it[k];
+  }
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void k_scan_sums(int32_t* sums, int nb) {
+  __shared__ int smem[33];
+  int carry = 0;
+  for (int base = 0; base < nb; base += SCAN_B) {
+    int it[SCAN_I];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_I; ++k) {
+      const int q = base + threadIdx.x * SCAN_I + k;
+      it[k] = q < nb ? sums[q] : 0;
+      s += it[k];
+    }
+    int total;
+    int off = block_exclusive(s, smem, total);
+#pragma unroll
+    for (int k = 0; k < SCAN_I; ++k) {
+      const int q = base + threadIdx.x * SCAN_I + k;
+      if (q < nb) sums[q] = off + carry;
+      off += it[k];
+    }
+    carry += total;
+  }
+}
+
+__global__ void k_scan_add(int32_t* __restrict__ out, int64_t n, const int32_t* __restrict__ sums) {
+  const int64_t base = (int64_t)blockIdx.x * SCAN_B;
+  const int add = sums[blockIdx.x];
+  for (int k = threadIdx.x; k < SCAN_B; k += blockDim.x) {
+    const int64_t q = base + k;
+    if (q <= n) out[q] += add;
+  }
+}
+
+static int scan(gbmd_context* c, const int32_t* in, int32_t* out, int64_t n) {
+  const int64_t nb = (n + 1 + SCAN_B - 1) / SCAN_B;
+  if (c->scan_cap < nb) {
+    if (c->scan_tmp) cudaFree(c->scan_tmp);
+    GBMD_CUDA(c, cudaMalloc(&c->scan_tmp, sizeof(int32_t) * nb));
+    c->scan_cap = nb;
+  }
+  k_scan_block<<<(unsigned)nb, SCAN_T, 0, c->stream>>>(in, out, n, c->scan_tmp);
+  k_scan_sums<<<1, SCAN_T, 0, c->stream>>>(c->scan_tmp, (int)nb);
+  k_scan_add<<<(unsigned)nb, SCAN_T, 0, c->stream>>>(out, n, c->scan_tmp);
+  return GBMD_OK;
+}
+
+__global__ void k_scatter(int64_t n, const int32_t* __restrict__ cell_of, const int32_t* __restrict__ cstart,
+                          int32_t* __restrict__ fill, int32_t* __restrict__ order) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t cl = cell_of[i];
+  const int32_t slot = cstart[cl] + atomicAdd(&fill[cl], 1);
+  order[slot] = (int32_t)i;
+}
+
+// one warp per cell: rank by (id, upload index) -> src[new] = old
+__global__ void k_cell_rank(int64_t ncells, const int32_t* __restrict__ cstart, const int32_t* __restrict__ order,
+                            const uint64_t* __restrict__ id, const int32_t* __restrict__ user,
+                            int32_t* __restrict__ src) {
+  const int64_t cell = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (cell >= ncells) return;
+  const int beg = cstart[cell], m = cstart[cell + 1] - beg;
+  for (int e = lane; e < m; e += 32) {
+    const int32_t a = order[beg + e];
+    const uint64_t ka = id[a];
+    const int32_t ua = user[a];
+    int rank = 0;
+    for (int f = 0; f < m; ++f) {
+      const int32_t b = order[beg + f];
+      const uint64_t kb = id[b];
+      rank += (kb < ka) || (kb == ka && user[b] < ua);
+    }
+    src[beg + rank] = a;
+  }
+}
+
+struct GatherArgs {
+  const double *r0, *v0, *a0;
+  double *r1, *v1, *a1;
+  const uint8_t* t0;
+  uint8_t* t1;
+  const uint64_t* i0;
+  uint64_t* i1;
+  const int32_t* u0;
+  int32_t* u1;
+  const double* ep0;
+  double* ep1;
+  int64_t cap;
+};
+
+__global__ void k_gather(int64_t n, const int32_t* __restrict__ src, GatherArgs g,
+                         const int32_t* __restrict__ cell_of, int ncx, int ncy,
+                         int32_t* __restrict__ cellpack) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int64_t o = src[p];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    g.r1[d * g.cap + p] = g.r0[d * g.cap + o];
+    g.v1[d * g.cap + p] = g.v0[d * g.cap + o];
+    g.a1[d * g.cap + p] = g.a0[d * g.cap + o];
+  }
+  g.t1[p] = g.t0[o];
+  g.i1[p] = g.i0[o];
+  g.u1[p] = g.u0[o];
+  g.ep1[p] = g.ep0[o];
+  const int32_t lin = cell_of[o];
+  const int cx = lin % ncx, cy = (lin / ncx) % ncy, cz = lin / (ncx * ncy);
+  cellpack[p] = cx | (cy << 10) | (cz << 20);
+}
+
+__global__ void k_posf(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
+                       const double* __restrict__ z, const uint8_t* __restrict__ type,
+                       const int32_t* __restrict__ cellpack, Grid g, float4* __restrict__ pf,
+                       double4_32a* __restrict__ pd) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cp = cellpack[i];
+  const double cx = (double)(cp & 1023), cy = (double)((cp >> 10) & 1023), cz = (double)(cp >> 20);
+  const double xi = x[i], yi = y[i], zi = z[i];
+  const int t = type[i];
+  pf[i] = make_float4((float)(xi - cx * g.h[0] - g.lo[0]), (float)(yi - cy * g.h[1] - g.lo[1]),
+                      (float)(zi - cz * g.h[2] - g.lo[2]), __int_as_float(t));
+  pd[i] = make_double4_32a(xi, yi, zi, (double)t);
+}
+
+__global__ void k_build_list(int64_t n, const float4* __restrict__ pf, const double* __restrict__ x,
+                             const double* __restrict__ y, const double* __restrict__ z,
+                             const int32_t* __restrict__ cellpack, const int32_t* __restrict__ cstart,
+                             Grid g, double R2, float R2lo, float R2hi, uint32_t* __restrict__ nbr,
+                             int32_t* __restrict__ nnb, int maxnb, int T, int64_t stride,
+                             int* __restrict__ err) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int cnt = 0;
+  if (i < n) {
+    const int cp = cellpack[i];
+    const int cx = cp & 1023, cy = (cp >> 10) & 1023, cz = cp >> 20;
+    const float4 pi = pf[i];
+    const double xi = x[i], yi = y[i], zi = z[i];
+    for (int dz = -1; dz <= 1; ++dz) {
+      const int nz = image_of(cz, dz, g.nc[2]);
+      const int wz = cz + dz - nz * g.nc[2];
+      const float sz = (float)dz * g.hf[2];
+      const double Sz = (double)nz * g.L[2];
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int ny = image_of(cy, dy, g.nc[1]);
+        const int wy = cy + dy - ny * g.nc[1];
+        const float sy = (float)dy * g.hf[1];
+        const double Sy = (double)ny * g.L[1];
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int nx = image_of(cx, dx, g.nc[0]);
+          const int wx = cx + dx - nx * g.nc[0];
+          const float sx = (float)dx * g.hf[0];
+          const double Sx = (double)nx * g.L[0];
+          const uint32_t code = (uint32_t)(dx + 1) | ((uint32_t)(dy + 1) << 2) | ((uint32_t)(dz + 1) << 4);
+          const int64_t cell = ((int64_t)wz * g.nc[1] + wy) * g.nc[0] + wx;
+          const int beg = cstart[cell], end = cstart[cell + 1];
+          const bool self = (nx | ny | nz) == 0;
+          for (int k = beg; k < end; ++k) {
+            if (self && k == i) continue;
+            const float4 pj = pf[k];
+            const float ddx = (pj.x - pi.x) + sx;
+            const float ddy = (pj.y - pi.y) + sy;
+            const float ddz = (pj.z - pi.z) + sz;
+            const float d2f = ddx * ddx + ddy * ddy + ddz * ddz;
+            bool in;
+            if (d2f > R2hi) in = false;
+            else if (d2f < R2lo) in = true;
+            else {
+              double a, b, c;
+              in = exact_d2(xi, yi, zi, x[k], y[k], z[k], Sx, Sy, Sz, a, b, c) <= R2;
+            }
+            if (in) {
+              if (cnt < maxnb) nbr[nbr_slot(i, cnt, T, stride)] = (uint32_t)k | (code << GBMD_IDX_BITS);
+              ++cnt;
+            }
+          }
+        }
+      }
+    }
+    nnb[i] = cnt;
+    if (cnt > maxnb) atomicOr(&err[ERRW_FLAGS], GBMD_DEVERR_NBR_OVERFLOW);
+  }
+  int m = cnt;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(&err[ERRW_MAXNB], m);
+}
+
+static inline unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+
+void launch_posf(gbmd_context* c) {
+  if (c->n == 0) return;
+  k_posf<<<nblk(c->n, 256), 256, 0, c->stream>>>(c->n, c->X(), c->Y(), c->Z(), c->TYPE(), c->cellpack,
+                                                  c->grid, c->POSF(), c->POSD());
+}
+
+static int build_list(gbmd_context* c) {
+  const double R = c->rlist;
+  const double R2 = R * R;
+  const float R2lo = (float)(R2 * (1.0 - 0x1p-12));
+  const float R2hi = (float)(R2 * (1.0 + 0x1p-12));
+  const int64_t npad = ((c->n + 31) / 32) * 32;
+  const int64_t stride = npad * c->tpa;
+  const int64_t need = (int64_t)(c->maxnb / c->tpa) * stride;
+  if (need > c->nbr_cap) {
+    if (c->nbr) cudaFree(c->nbr);
+    c->nbr = nullptr;
+    GBMD_CUDA(c, cudaMalloc(&c->nbr, sizeof(uint32_t) * (size_t)need));
+    c->nbr_cap = need;
+  }
+  c->npad = npad;
+  GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_MAXNB, 0, sizeof(int), c->stream));
+  k_build_list<<<nblk(c->n, 128), 128, 0, c->stream>>>(c->n, c->POSF(), c->X(), c->Y(), c->Z(), c->cellpack,
+                                                        c->cell_start, c->grid, R2, R2lo, R2hi, c->nbr, c->nnb,
+                                                        c->maxnb, c->tpa, stride, c->d_err);
+  return GBMD_OK;
+}
+
+int rebuild(gbmd_context* c, bool check_capacity) {
+  if (!c->box_set) return set_error(c, GBMD_ERR_INVALID, "box not set");
+  if (c->pot == GBMD_POT_NONE) return set_error(c, GBMD_ERR_INVALID, "no potential set");
+  if (c->n == 0) {
+    c->list_valid = true;
+    return GBMD_OK;
+  }
+  const double R = c->rlist;
+  if (!c->grid_valid) {
+    int nc[3];
+    const int rc = grid_dims(c->lo, c->hi, R, nc);
+    if (rc != 0) return set_error(c, GBMD_ERR_INVALID, "box edge shorter than neighbour radius %g", R);
+    Grid& g = c->grid;
+    g.ncells = (int64_t)nc[0] * nc[1] * nc[2];
+    if (g.ncells > (1ll << 27)) return set_error(c, GBMD_ERR_TOO_LARGE, "too many cells");
+    for (int d = 0; d < 3; ++d) {
+      g.nc[d] = nc[d];
+      g.L[d] = c->hi[d] - c->lo[d];
+      g.h[d] = g.L[d] / nc[d];
+      g.hf[d] = (float)g.h[d];
+      g.lo[d] = c->lo[d];
+    }
+    if (c->cells_cap < g.ncells + 1) {
+      if (c->cell_start) cudaFree(c->cell_start);
+      if (c->cell_fill) cudaFree(c->cell_fill);
+      GBMD_CUDA(c, cudaMalloc(&c->cell_start, sizeof(int32_t) * (g.ncells + 1)));
+      GBMD_CUDA(c, cudaMalloc(&c->cell_fill, sizeof(int32_t) * (g.ncells + 1)));
+      c->cells_cap = g.ncells + 1;
+    }
+    c->grid_valid = true;
+  }
+  Grid& g = c->grid;
+  BoxArgs b;
+  for (int d = 0; d < 3; ++d) {
+    b.lo[d] = c->lo[d];
+    b.hi[d] = c->hi[d];
+    b.L[d] = g.L[d];
+    b.inv_h[d] = (double)g.nc[d] / g.L[d];
+    b.nc[d] = g.nc[d];
+  }
+  const int64_t n = c->n;
+  cudaStream_t s = c->stream;
+  GBMD_CUDA(c, cudaMemsetAsync(c->cell_fill, 0, sizeof(int32_t) * (g.ncells + 1), s));
+  k_wrap_bin<<<nblk(n, 256), 256, 0, s>>>(n, c->X(), c->Y(), c->Z(), b, c->cell_of, c->cell_fill, c->d_err);
+  int rc = scan(c, c->cell_fill, c->cell_start, g.ncells);
+  if (rc) return rc;
+  GBMD_CUDA(c, cudaMemsetAsync(c->cell_fill, 0, sizeof(int32_t) * (g.ncells + 1), s));
+  k_scatter<<<nblk(n, 256), 256, 0, s>>>(n, c->cell_of, c->cell_start, c->cell_fill, c->order);
+  k_cell_rank<<<nblk(g.ncells * 32, 256), 256, 0, s>>>(g.ncells, c->cell_start, c->order, c->ID(), c->USER(),
+                                                        c->src);
+  GatherArgs ga;
+  const int o = c->cur, os = c->cur_s;
+  ga.r0 = c->rbuf[o]; ga.r1 = c->rbuf[o ^ 1];
+  ga.v0 = c->vbuf[os]; ga.v1 = c->vbuf[os ^ 1];
+  ga.a0 = c->abuf[os]; ga.a1 = c->abuf[os ^ 1];
+  ga.t0 = c->typeb[os]; ga.t1 = c->typeb[os ^ 1];
+  ga.i0 = c->idb[os]; ga.i1 = c->idb[os ^ 1];
+  ga.u0 = c->userb[os]; ga.u1 = c->userb[os ^ 1];
+  ga.ep0 = c->ep; ga.ep1 = c->stage;
+  ga.cap = c->cap;
+  k_gather<<<nblk(n, 256), 256, 0, s>>>(n, c->src, ga, c->cell_of, g.nc[0], g.nc[1], c->cellpack);
+  GBMD_CUDA(c, cudaMemcpyAsync(c->ep, c->stage, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  c->cur ^= 1;
+  c->cur_s ^= 1;
+  launch_posf(c);
+  if (c->maxnb <= 0) {
+    // first estimate: 1.35x the mean count of an ideal gas at this density
+    const double V = g.L[0] * g.L[1] * g.L[2];
+    const double mean = (double)n / V * 4.18879020478639 * R * R * R;
+    int m = (int)(mean * 1.35) + 16;
+    c->maxnb = ((m + c->tpa - 1) / c->tpa) * c->tpa;
+  }
+  rc = build_list(c);
+  if (rc) return rc;
+  c->list_valid = true;
+  c->list_builds++;
+  if (check_capacity) {
+    rc = sync_error_word(c);
+    if (c->h_err[ERRW_FLAGS] & GBMD_DEVERR_LOST_ATOM)
+      return set_error(c, GBMD_ERR_LOST_ATOM, "%d atoms left the box by more than one image",
+                       c->h_err[ERRW_LOST]);
+    const int maxc = c->h_err[ERRW_MAXNB];
+    if (maxc > c->maxnb) {
+      int m = (int)(maxc * 1.2) + 8;
+      c->maxnb = ((m + c->tpa - 1) / c->tpa) * c->tpa;
+      GBMD_CUDA(c, cudaMemsetAsync(c->d_err, 0, sizeof(int) * 8, s));
+      rc = build_list(c);
+      if (rc) return rc;
+      rc = sync_error_word(c);
+      if (c->h_err[ERRW_FLAGS] & GBMD_DEVERR_NBR_OVERFLOW)
+        return set_error(c, GBMD_ERR_NEIGHBOR_OVERFLOW, "neighbour list overflow after regrow");
+    }
+  }
+  return GBMD_OK;
+}
+
+int export_pairs(gbmd_context* c, int64_t cap, uint64_t* id_i, uint64_t* id_j, int8_t* img, int64_t* count) {
+  if (!c->list_valid) {
+    int rc = rebuild(c, true);
+    if (rc) return rc;
+  }
+  const int64_t n = c->n;
+  std::vector<int32_t> nnb(n), cp(n);
+  std::vector<uint64_t> ids(n);
+  GBMD_CUDA(c, cudaMemcpyAsync(nnb.data(), c->nnb, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
+  GBMD_CUDA(c, cudaMemcpyAsync(cp.data(), c->cellpack, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
+  GBMD_CUDA(c, cudaMemcpyAsync(ids.data(), c->ID(), sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, c->stream));
+  GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
+  int64_t total = 0;
+  for (int64_t i = 0; i < n; ++i) total += nnb[i];
+  *count = total;
+  if (cap < total || !id_i) return GBMD_OK;
+  const int64_t stride = c->npad * c->tpa;
+  std::vector<uint32_t> nb((size_t)c->nbr_cap);
+  GBMD_CUDA(c, cudaMemcpy(nb.data(), c->nbr, sizeof(uint32_t) * c->nbr_cap, cudaMemcpyDeviceToHost));
+  int64_t row = 0;
+  const Grid& g = c->grid;
+  for (int64_t i = 0; i < n; ++i) {
+    const int cx = cp[i] & 1023, cy = (cp[i] >> 10) & 1023, cz = cp[i] >> 20;
+    for (int k = 0; k < nnb[i] && k < c->maxnb; ++k) {
+      const uint32_t e = nb[(size_t)(k / c->tpa) * stride + (size_t)i * c->tpa + (k % c->tpa)];
+      const uint32_t j = e & GBMD_IDX_MASK, code = e >> GBMD_IDX_BITS;
+      const int d[3] = {int(code & 3) - 1, int((code >> 2) & 3) - 1, int((code >> 4) & 3) - 1};
+      const int cc[3] = {cx + d[0], cy + d[1], cz + d[2]};
+      id_i[row] = ids[i];
+      id_j[row] = ids[j];
+      for (int q = 0; q < 3; ++q) img[3 * row + q] = (int8_t)(cc[q] < 0 ? -1 : (cc[q] >= g.nc[q] ? 1 : 0));
+      ++row;
+    }
+  }
+  return GBMD_OK;
+}
+
+}  // namespace gbmd

@@ -1,0 +1,212 @@
+/*
+ * gbmd.h -- C ABI of the GB300 (sm_103a) MD hot path: cell-grid neighbour
+ * list, Lennard-Jones and eam_alloy force operators, velocity-Verlet push and
+ * the thermodynamic reduction of exaStamp.
+ *
+ * Conventions
+ *   - Every call returns an int status: GBMD_OK (0) or a positive GBMD_ERR_*;
+ *     gbmd_last_error() gives a one-line message.  Nothing aborts or traps.
+ *   - Host arrays are SoA FP64 in the caller's atom order (the order of the
+ *     last gbmd_upload_atoms); the library keeps atoms cell-sorted internally
+ *     and reorders on the way in and out.
+ *   - Units are the caller's: the reference's internal system is angstrom,
+ *     dalton, picosecond (energy Da*A^2/ps^2); Lennard-Jones runs may use
+ *     reduced units.  eam_alloy tables are in eV and are scaled by the
+ *     conversion factors given to gbmd_set_eam_alloy.
+ *   - One context = one device + one CUDA stream, driven by one host thread
+ *     at a time.  All work is stream-ordered; calls that return host data
+ *     synchronise the stream.
+ *
+ * The reference entry points each call replaces are cited per function
+ * (paths inside the exaStamp / exaNBody trees).
+ */
+#ifndef GBMD_H
+#define GBMD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBMD_ABI_VERSION 1
+
+typedef struct gbmd_context gbmd_context;
+
+enum gbmd_status {
+  GBMD_OK = 0,
+  GBMD_ERR_INVALID = 1,          /* bad argument or call order */
+  GBMD_ERR_CUDA = 2,             /* CUDA runtime error */
+  GBMD_ERR_NO_DEVICE = 3,
+  GBMD_ERR_NEIGHBOR_OVERFLOW = 4,/* a list build exceeded its per-atom capacity */
+  GBMD_ERR_LOST_ATOM = 5,        /* an atom left the periodic box by more than one image */
+  GBMD_ERR_NONFINITE = 6,        /* NaN/Inf force */
+  GBMD_ERR_IO = 7,               /* setfl file unreadable */
+  GBMD_ERR_UNSUPPORTED = 8,
+  GBMD_ERR_TOO_LARGE = 9
+};
+
+enum gbmd_precision {
+  GBMD_PRECISION_FP64 = 0,  /* plain FP64 pair arithmetic */
+  GBMD_PRECISION_MIXED = 1  /* FP32 pair arithmetic on cell-relative coordinates, compensated
+                               FP32 sums; FP64 state, push, wrap and reductions */
+};
+
+enum gbmd_potential {
+  GBMD_POT_NONE = 0,
+  GBMD_POT_LJ = 1,          /* lj_compute_force */
+  GBMD_POT_LJ_MULTI = 2,    /* lj_multi_force */
+  GBMD_POT_EAM_ALLOY = 3    /* eam_alloy_force (rho, rho2emb, force passes) */
+};
+
+enum gbmd_force_flags {
+  GBMD_FORCE_ENERGY = 1,    /* per-atom ep (trigger_thermo_state) */
+  GBMD_FORCE_VIRIAL = 2     /* per-atom virial tensor (compute_virial) */
+};
+
+/* ---- context --------------------------------------------------------------
+ * Replaces the onika execution context + grid ownership that every operator
+ * receives (src/tutorial/my_gpu_test.cxx L80-92: parallel_execution_context()
+ * ->gpu_stream()).  stream may be NULL (the context creates its own) or a
+ * cudaStream_t cast to void*. */
+int gbmd_create(gbmd_context** ctx, int device, void* stream);
+int gbmd_destroy(gbmd_context* ctx);
+const char* gbmd_last_error(const gbmd_context* ctx);
+int gbmd_abi_version(void);
+
+/* Orthorhombic periodic domain [lo, hi) (exaNBody Domain bounds/periodic,
+ * set by the reference's `domain` setup operator; xform identity).  Only
+ * fully periodic boxes are supported. */
+int gbmd_set_box(gbmd_context* ctx, const double lo[3], const double hi[3], const int periodic[3]);
+
+/* Per-type masses (ParticleSpecies m_mass: include/exaStamp/particle_species/
+ * particle_specie.h L52-70); used by force_to_accel and the push. */
+int gbmd_set_species(gbmd_context* ctx, int ntypes, const double* masses);
+
+/* Copy atoms in (grid cell arrays rx,ry,rz,vx,vy,vz,type,id:
+ * include/exaStamp/fields.h L64-79).  vx/vy/vz/type/id may be NULL
+ * (zero velocity, type 0, id = index). Invalidates the neighbour list. */
+int gbmd_upload_atoms(gbmd_context* ctx, int64_t n, const double* rx, const double* ry,
+                      const double* rz, const double* vx, const double* vy, const double* vz,
+                      const uint8_t* type, const uint64_t* id);
+/* Positions (and optionally velocities) only, same atoms and order as the
+ * last upload; keeps the neighbour list (the adapter's per-step copy-in). */
+int gbmd_upload_positions(gbmd_context* ctx, const double* rx, const double* ry, const double* rz,
+                          const double* vx, const double* vy, const double* vz);
+/* The whole per-step grid state in upload order: positions, velocities and
+ * accelerations (the r, v and f fields the exaNBody grid keeps between
+ * operators).  The given accelerations are taken as the forces of these
+ * positions, so a following gbmd_run_nve continues without a force call.
+ * The list is kept unless an atom moved more than skin/2 since the last
+ * rebuild (particle_displ_over, config_move_particles.msp L19-22). */
+int gbmd_upload_state(gbmd_context* ctx, const double* rx, const double* ry, const double* rz,
+                      const double* vx, const double* vy, const double* vz, const double* ax,
+                      const double* ay, const double* az);
+/* Copy state out in upload order; any pointer may be NULL.  a* is the
+ * acceleration (force_to_accel writes f/m into the force fields,
+ * src/compute/force_to_accel.cu L42-48); vir is n x 9 row-major. */
+int gbmd_download(gbmd_context* ctx, double* rx, double* ry, double* rz, double* vx, double* vy,
+                  double* vz, double* ax, double* ay, double* az, double* ep, double* vir);
+int gbmd_num_atoms(const gbmd_context* ctx, int64_t* n);
+
+/* ---- potentials ----------------------------------------------------------- */
+/* lj_compute_force: slots parameters{epsilon,sigma}, rcut
+ * (src/potential/pair_potential_template/pair_potential_impl.hxx L104-121,
+ * pair function lennard_jones.h L41-50, ecut = e(rcut) L489-498). */
+int gbmd_set_lj(gbmd_context* ctx, double epsilon, double sigma, double rcut);
+/* lj_multi_force: per type-pair (epsilon, sigma, rcut) tables, ntypes x ntypes
+ * symmetric, plus the operator's common rcut (rcut_max = max of all)
+ * (pair_potential_force_op_multiparam.h L57-118, YAML L249-284). */
+int gbmd_set_lj_multi(gbmd_context* ctx, int ntypes, const double* epsilon, const double* sigma,
+                      const double* rcut, double rcut_common);
+/* eam_alloy parameters from raw setfl tables (eam_alloy.cpp): F(rho)
+ * nel x nrho, rho(r) nel x nr, z2r (nel*(nel+1)/2) x nr in file order; the
+ * library builds the 7-coefficient splines (eam_alloy.cpp L29-58).  rcut is
+ * the operator's rcut slot (eam_potential_multimat.cu L91); conv_z2r and
+ * conv_frho convert eV*A and eV to internal energy (eam_alloy.h L156-157). */
+int gbmd_set_eam_alloy(gbmd_context* ctx, int nelements, int nrho, double drho, int nr, double dr,
+                       const double* frho, const double* rhor, const double* z2r, double rcut,
+                       double conv_z2r, double conv_frho);
+/* eam_alloy_init: read a setfl (.eam.alloy) file (eam_alloy.cpp L66-201). */
+int gbmd_load_setfl(gbmd_context* ctx, const char* path, double rcut, double conv_z2r,
+                    double conv_frho);
+
+int gbmd_set_precision(gbmd_context* ctx, int precision);
+/* Lanes per atom (1,2,4,8,16,32) and threads per block for the pair kernels;
+ * the autotuner's knobs.  Invalidates the neighbour list layout. */
+int gbmd_set_launch(gbmd_context* ctx, int lanes_per_atom, int block);
+int gbmd_get_launch(const gbmd_context* ctx, int* lanes_per_atom, int* block);
+
+/* ---- neighbour list --------------------------------------------------------
+ * chunk_neighbors (exaNBody; config data/config/config_move_particles.msp
+ * L54-68, decode contract src/debug/atom_neighbors_stats.cpp L169-228) with
+ * chunk_size 1, preceded by the periodic wrap and rebinning of
+ * move_particles.  Radius = rcut_max + skin (global.rcut_inc,
+ * data/config/config_globals.msp L8).  The pair set is {(i, j, image n) :
+ * d2 <= (rcut_max+skin)^2} with d2 from ((x_j + n L) - x_i) in FP64 without
+ * contraction. */
+int gbmd_set_skin(gbmd_context* ctx, double skin);
+int gbmd_build_neighbors(gbmd_context* ctx);
+/* Export the list as (id_i, id_j, n_x, n_y, n_z) rows, rows of one atom in
+ * list order, atoms in cell-sorted order. count receives the number of rows
+ * (call with cap 0 to size). */
+int gbmd_export_pairs(gbmd_context* ctx, int64_t cap, uint64_t* id_i, uint64_t* id_j, int8_t* img,
+                      int64_t* count);
+int gbmd_neighbor_stats(gbmd_context* ctx, int64_t* npairs, int* maxnb, int* nc3);
+
+/* ---- force operators -------------------------------------------------------
+ * compute_all_forces_energy = zero_force_energy + compute_force +
+ * force_to_accel (data/config/config_numerical_schemes.msp L8-15): after this
+ * call a* holds f/m, ep the per-atom energy (GBMD_FORCE_ENERGY) and vir the
+ * per-atom virial (GBMD_FORCE_VIRIAL). Builds the list first if needed. */
+int gbmd_compute_forces(gbmd_context* ctx, int flags);
+
+/* ---- integration -----------------------------------------------------------
+ * push_f_v_r: r += v*dt' + a*dt'^2/2, dt' = dt*dt_scale; push_f_v: v += a*dt*
+ * dt_scale (exaNBody; schedule config_numerical_schemes.msp L23-28, formula
+ * src/numerical_schemes/push_vec3_2nd_order_xform_minimization.cpp L33-38). */
+int gbmd_push_f_v_r(gbmd_context* ctx, double dt, double dt_scale);
+int gbmd_push_f_v(gbmd_context* ctx, double dt, double dt_scale);
+/* push_f_v_r_xform_minimization, identity xform (same file L116-149):
+ * r += a*dt'^2/2; tolF > 0 clips each acceleration component first. */
+int gbmd_push_min(gbmd_context* ctx, double dt, double dt_scale, double tolF);
+
+/* verlet_nve for nsteps (config_numerical_schemes.msp L44-52): first half,
+ * rebuild every `rebuild_every` steps (0 = never), forces, second half.
+ * thermo_every > 0 writes the 27-double reduction every thermo_every steps
+ * into thermo_out (rows of 27, step 0 first); thermo_out may be NULL.
+ * use_graph != 0 captures a rebuild-interval chunk in a CUDA graph. */
+int gbmd_run_nve(gbmd_context* ctx, int nsteps, double dt, int rebuild_every, int thermo_every,
+                 double* thermo_out, int use_graph);
+/* Minimiser: nsteps of compute forces + push_min (r += a dt^2/2, clipped). */
+int gbmd_run_minimize(gbmd_context* ctx, int nsteps, double dt, double tolF, int rebuild_every);
+
+/* ---- thermodynamic state ---------------------------------------------------
+ * simulation_thermodynamic_state (src/thermo_state/
+ * simulation_thermodynamic_state.cpp L101-163): out[27] = virial(9),
+ * ke_tensor(9), momentum(3), kinetic energy(3), potential energy, mass,
+ * particle count, reduced in FP64 on the device. */
+int gbmd_thermo(gbmd_context* ctx, double out[27]);
+
+/* Per-kernel timing of one step's kernels with CUDA events on the context
+ * stream, averaged over `reps` launches of each (the analogue of onika's
+ * per-operator profiling timers, data/config/config_defaults.msp L21-23):
+ * ms[0] neighbour rebuild (wrap, sort, list), ms[1] EAM density+embedding
+ * pass (0 for LJ), ms[2] final pair kernel with the fused Verlet halves,
+ * ms[3] standalone first-half push, ms[4] thermo reduction.  Positions are
+ * pushed with dt = 0, so the state is unchanged. */
+int gbmd_profile_step(gbmd_context* ctx, int reps, double ms[5]);
+
+/* Device pointers of the cell-sorted FP64 state (for zero-copy adapters):
+ * order is internal; user_index[i] gives the upload index of sorted atom i. */
+int gbmd_device_state(gbmd_context* ctx, double** rx, double** ry, double** rz, double** vx,
+                      double** vy, double** vz, double** ax, double** ay, double** az, double** ep,
+                      int32_t** user_index);
+
+int gbmd_synchronize(gbmd_context* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBMD_H */

@@ -1,0 +1,731 @@
+/*
+ * gbmd_oracle.c -- CPU FP64 restatement of exaStamp's MD hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the correctness oracle and the timed CPU baseline
+ * for the GB300 kernels.  The product path never links or calls this file.
+ *
+ * Build: gcc -O3 -fopenmp -ffp-contract=off -fPIC -shared (see oracle/oracle.py).
+ * -ffp-contract=off matters: the neighbour test d2 <= R^2 must round exactly
+ * like the GPU list builder, which evaluates it with explicit _rn intrinsics.
+ *
+ * Reference files restated (paths inside the exaStamp tree):
+ *   LJ pair      src/potential/pair_potentials/lennard_jones/include/exaStamp/
+ *                potential/pair_potentials/lennard_jones/lennard_jones.h L41-50
+ *   LJ per atom  src/potential/pair_potential_template/force_op_impl2.hxx L22-78
+ *   LJ ecut      src/potential/pair_potential_template/pair_potential_impl.hxx L489-498
+ *   LJ multi     src/potential/pair_potential_template/pair_potential_force_op_multiparam.h L75-118
+ *   EAM spline   src/potential/eam_potentials/eam_alloy/eam_alloy.cpp L29-58
+ *   EAM lookups  src/potential/eam_potentials/eam_alloy/eam_alloy.h L198-313
+ *   EAM passes   src/potential/eam_potential_template/eam_force_op_multimat.h L114-343
+ *   zero / accel src/compute/zero_force_energy.cu L38-47, src/compute/force_to_accel.cu L42-48
+ *   push         src/numerical_schemes/push_vec3_2nd_order_xform_minimization.cpp L33-38, L116-149
+ *   thermo       src/thermo_state/simulation_thermodynamic_state.cpp L101-163
+ *   pair decode  src/debug/atom_neighbors_stats.cpp L169-209 (d2 formula and d2 <= R^2 test)
+ */
+#include "gbmd_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* Cell grid                                                                 */
+/* ------------------------------------------------------------------------ */
+
+/* Cells per dimension: the largest count whose edge stays >= R (with a 2^-40
+ * relative margin so that binning round-off can never hide a pair), capped at
+ * 1024 so that cell coordinates pack into 10 bits on the GPU. */
+int orc_grid_dims(const double lo[3], const double hi[3], double R, int nc[3]) {
+  for (int d = 0; d < 3; ++d) {
+    double L = hi[d] - lo[d];
+    if (!(L > 0.0) || !(R > 0.0)) return -1;
+    double q = floor(L / (R * (1.0 + 0x1p-40)));
+    if (q < 1.0) return -2; /* box thinner than the neighbour radius */
+    if (q > 1024.0) q = 1024.0;
+    nc[d] = (int)q;
+  }
+  return 0;
+}
+
+/* Periodic wrap into [lo, hi), one image at most (exaNBody move_particles
+ * contract; atoms move far less than a box length between rebuilds).
+ * Returns how many atoms are still outside afterwards ("lost atoms"). */
+int64_t orc_wrap(int64_t n, double* x, double* y, double* z, const double lo[3], const double hi[3]) {
+  int64_t lost = 0;
+  double* r[3] = {x, y, z};
+  for (int d = 0; d < 3; ++d) {
+    const double L = hi[d] - lo[d];
+    double* a = r[d];
+#pragma omp parallel for schedule(static) reduction(+ : lost)
+    for (int64_t i = 0; i < n; ++i) {
+      double v = a[i];
+      if (v < lo[d]) v += L;
+      else if (v >= hi[d]) v -= L;
+      if (v < lo[d] || v >= hi[d]) ++lost;
+      a[i] = v;
+    }
+  }
+  return lost;
+}
+
+static inline int cell_coord(double v, double lo, double inv_h, int nc) {
+  int c = (int)((v - lo) * inv_h);
+  if (c < 0) c = 0;
+  if (c > nc - 1) c = nc - 1;
+  return c;
+}
+
+typedef struct {
+  int nc[3];
+  int64_t ncells;
+  int64_t* start; /* ncells+1 */
+  int64_t* atoms; /* n, sorted by (cell, id, index) */
+  int32_t* cell_of; /* n */
+} orc_grid;
+
+static int grid_build(orc_grid* g, int64_t n, const double* x, const double* y, const double* z,
+                      const uint64_t* id, const double lo[3], const double hi[3], double R) {
+  if (orc_grid_dims(lo, hi, R, g->nc) != 0) return -1;
+  double inv_h[3];
+  for (int d = 0; d < 3; ++d) inv_h[d] = (double)g->nc[d] / (hi[d] - lo[d]);
+  g->ncells = (int64_t)g->nc[0] * g->nc[1] * g->nc[2];
+  g->start = (int64_t*)calloc((size_t)g->ncells + 1, sizeof(int64_t));
+  g->atoms = (int64_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
+  g->cell_of = (int32_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int32_t));
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    int cx = cell_coord(x[i], lo[0], inv_h[0], g->nc[0]);
+    int cy = cell_coord(y[i], lo[1], inv_h[1], g->nc[1]);
+    int cz = cell_coord(z[i], lo[2], inv_h[2], g->nc[2]);
+    g->cell_of[i] = (int32_t)(((int64_t)cz * g->nc[1] + cy) * g->nc[0] + cx);
+  }
+  for (int64_t i = 0; i < n; ++i) g->start[g->cell_of[i] + 1]++;
+  for (int64_t c = 0; c < g->ncells; ++c) g->start[c + 1] += g->start[c];
+  int64_t* fill = (int64_t*)malloc((size_t)g->ncells * sizeof(int64_t));
+  memcpy(fill, g->start, (size_t)g->ncells * sizeof(int64_t));
+  for (int64_t i = 0; i < n; ++i) g->atoms[fill[g->cell_of[i]]++] = i;
+  free(fill);
+  /* canonical order inside a cell: ascending id, then ascending input index */
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t c = 0; c < g->ncells; ++c) {
+    int64_t b = g->start[c], e = g->start[c + 1];
+    for (int64_t k = b + 1; k < e; ++k) {
+      int64_t a = g->atoms[k];
+      int64_t m = k - 1;
+      while (m >= b) {
+        int64_t o = g->atoms[m];
+        int later = id ? (id[o] > id[a] || (id[o] == id[a] && o > a)) : (o > a);
+        if (!later) break;
+        g->atoms[m + 1] = o;
+        --m;
+      }
+      g->atoms[m + 1] = a;
+    }
+  }
+  return 0;
+}
+
+static void grid_free(orc_grid* g) {
+  free(g->start);
+  free(g->atoms);
+  free(g->cell_of);
+}
+
+/* d2 of the pair (i, image n of j), no FMA: the reference's pair-decode
+ * formula (atom_neighbors_stats.cpp L201-204) on ghost coordinates x_j + n*L. */
+static inline double pair_d2(const double* x, const double* y, const double* z, int64_t i, int64_t j,
+                             const int n[3], const double L[3], double* dx, double* dy, double* dz) {
+  const double sx = (double)n[0] * L[0], sy = (double)n[1] * L[1], sz = (double)n[2] * L[2];
+  *dx = (x[j] + sx) - x[i];
+  *dy = (y[j] + sy) - y[i];
+  *dz = (z[j] + sz) - z[i];
+  return *dx * *dx + *dy * *dy + *dz * *dz;
+}
+
+/* Visit the 27-cell stencil of atom i in canonical order: stencil code
+ * s = (dz+1)*9 + (dy+1)*3 + (dx+1) ascending, then the cell's atoms in
+ * (id, index) order.  The image shift follows from wrapping the stencil cell. */
+static int64_t visit_atom(const orc_grid* g, int64_t i, const double* x, const double* y,
+                          const double* z, const double L[3], double R2, int32_t* nbr, int8_t* img) {
+  const int c = g->cell_of[i];
+  const int cx = c % g->nc[0], cy = (c / g->nc[0]) % g->nc[1], cz = c / (g->nc[0] * g->nc[1]);
+  int64_t cnt = 0;
+  for (int s = 0; s < 27; ++s) {
+    const int d[3] = {s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1};
+    const int cc[3] = {cx + d[0], cy + d[1], cz + d[2]};
+    int n[3], w[3];
+    for (int k = 0; k < 3; ++k) {
+      n[k] = cc[k] < 0 ? -1 : (cc[k] >= g->nc[k] ? 1 : 0);
+      w[k] = cc[k] - n[k] * g->nc[k];
+    }
+    const int64_t cj = ((int64_t)w[2] * g->nc[1] + w[1]) * g->nc[0] + w[0];
+    const int self_image = (n[0] == 0 && n[1] == 0 && n[2] == 0);
+    for (int64_t k = g->start[cj]; k < g->start[cj + 1]; ++k) {
+      const int64_t j = g->atoms[k];
+      if (j == i && self_image) continue;
+      double dx, dy, dz;
+      const double d2 = pair_d2(x, y, z, i, j, n, L, &dx, &dy, &dz);
+      if (d2 <= R2) {
+        if (nbr) {
+          nbr[cnt] = (int32_t)j;
+          img[3 * cnt + 0] = (int8_t)n[0];
+          img[3 * cnt + 1] = (int8_t)n[1];
+          img[3 * cnt + 2] = (int8_t)n[2];
+        }
+        ++cnt;
+      }
+    }
+  }
+  return cnt;
+}
+
+/* Full (non-Newton) neighbour list within R = rcut + skin, CSR by atom.
+ * Restates the pair set of exaNBody's chunk_neighbors with chunk_size 1, as
+ * decoded by atom_neighbors_stats.cpp L169-228.  Returns the total number of
+ * pairs; nbr/img are written only when cap is large enough (else call again). */
+int64_t orc_build_neighbors(int64_t n, const double* x, const double* y, const double* z,
+                            const uint64_t* id, const double lo[3], const double hi[3], double R,
+                            int64_t* offsets, int64_t cap, int32_t* nbr, int8_t* img) {
+  orc_grid g;
+  if (grid_build(&g, n, x, y, z, id, lo, hi, R) != 0) return -1;
+  const double L[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+  const double R2 = R * R;
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t i = 0; i < n; ++i) offsets[i + 1] = visit_atom(&g, i, x, y, z, L, R2, NULL, NULL);
+  offsets[0] = 0;
+  for (int64_t i = 0; i < n; ++i) offsets[i + 1] += offsets[i];
+  const int64_t total = offsets[n];
+  if (nbr && total <= cap) {
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < n; ++i) visit_atom(&g, i, x, y, z, L, R2, nbr + offsets[i], img + 3 * offsets[i]);
+  }
+  grid_free(&g);
+  return total;
+}
+
+/* O(N^2 * 27) all-image pair enumeration; independent check of the cell list. */
+int64_t orc_brute_pairs(int64_t n, const double* x, const double* y, const double* z,
+                        const double lo[3], const double hi[3], double R, int64_t cap,
+                        int32_t* pi, int32_t* pj, int8_t* img) {
+  const double L[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+  const double R2 = R * R;
+  int64_t cnt = 0;
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t j = 0; j < n; ++j)
+      for (int s = 0; s < 27; ++s) {
+        const int nn[3] = {s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1};
+        if (i == j && nn[0] == 0 && nn[1] == 0 && nn[2] == 0) continue;
+        double dx, dy, dz;
+        if (pair_d2(x, y, z, i, j, nn, L, &dx, &dy, &dz) <= R2) {
+          if (cnt < cap) {
+            pi[cnt] = (int32_t)i;
+            pj[cnt] = (int32_t)j;
+            img[3 * cnt] = (int8_t)nn[0];
+            img[3 * cnt + 1] = (int8_t)nn[1];
+            img[3 * cnt + 2] = (int8_t)nn[2];
+          }
+          ++cnt;
+        }
+      }
+  return cnt;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Lennard-Jones                                                             */
+/* ------------------------------------------------------------------------ */
+
+/* lennard_jones.h L41-50: e = 4 eps (s12 - s6), de = dE/dr. */
+void orc_lj_pair(double epsilon, double sigma, double r, double* e, double* de) {
+  const double ratio = sigma / r;
+  const double ratio2 = ratio * ratio;
+  const double ratio6 = ratio2 * ratio2 * ratio2;
+  const double ratio12 = ratio6 * ratio6;
+  *e = 4. * epsilon * (ratio12 - ratio6);
+  *de = (-24. * epsilon * (2. * ratio12 - ratio6)) / r;
+}
+
+/* pair_potential_impl.hxx L489-498: ecut = e(rcut), 0 when rcut <= 0. */
+double orc_lj_energy_cut(double epsilon, double sigma, double rcut) {
+  double e = 0.0, de = 0.0;
+  if (rcut > 0.0) orc_lj_pair(epsilon, sigma, rcut, &e, &de);
+  return e;
+}
+
+static inline void add_vir(double* v, double fx, double fy, double fz, double dx, double dy, double dz) {
+  /* tensor(fe, dr) * -0.5, row-major m11..m33 */
+  v[0] += fx * dx * -0.5; v[1] += fx * dy * -0.5; v[2] += fx * dz * -0.5;
+  v[3] += fy * dx * -0.5; v[4] += fy * dy * -0.5; v[5] += fy * dz * -0.5;
+  v[6] += fz * dx * -0.5; v[7] += fz * dy * -0.5; v[8] += fz * dz * -0.5;
+}
+
+/* lj_compute_force per atom (force_op_impl2.hxx L22-78) over the list pairs
+ * with d2 <= rcut^2 (the traversal's rcut_max filter).  Zeroes first
+ * (zero_force_energy), so outputs are the force on each atom, its half-pair
+ * energy sum and its virial. */
+void orc_lj_force(int64_t n, const double* x, const double* y, const double* z,
+                  const int64_t* off, const int32_t* nbr, const int8_t* img, const double L[3],
+                  const orc_lj_params* p, double* fx, double* fy, double* fz, double* ep, double* vir) {
+  const double ecut = orc_lj_energy_cut(p->epsilon, p->sigma, p->rcut);
+  const double rc2 = p->rcut * p->rcut;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < n; ++i) {
+    double _fx = 0., _fy = 0., _fz = 0., _ep = 0., _v[9] = {0};
+    for (int64_t k = off[i]; k < off[i + 1]; ++k) {
+      const int nn[3] = {img[3 * k], img[3 * k + 1], img[3 * k + 2]};
+      double dx, dy, dz;
+      const double d2 = pair_d2(x, y, z, i, nbr[k], nn, L, &dx, &dy, &dz);
+      if (!(d2 <= rc2)) continue;
+      const double r = sqrt(d2);
+      double e, de;
+      orc_lj_pair(p->epsilon, p->sigma, r, &e, &de);
+      e -= ecut;
+      de /= r;
+      const double fex = de * dx, fey = de * dy, fez = de * dz;
+      _fx += fex; _fy += fey; _fz += fez;
+      _ep += .5 * e;
+      add_vir(_v, fex, fey, fez, dx, dy, dz);
+    }
+    fx[i] = _fx; fy[i] = _fy; fz[i] = _fz;
+    if (ep) ep[i] = _ep;
+    if (vir) for (int q = 0; q < 9; ++q) vir[9 * i + q] = _v[q];
+  }
+}
+
+/* lj_multi_force (pair_potential_force_op_multiparam.h L75-118): traversal
+ * filter d2 <= rcut_max^2, then per type pair r <= rcut_pair with that pair's
+ * (eps, sigma) and ecut = e_pair(rcut_pair). */
+void orc_lj_multi_force(int64_t n, const double* x, const double* y, const double* z, const uint8_t* type,
+                        const int64_t* off, const int32_t* nbr, const int8_t* img, const double L[3],
+                        const orc_lj_multi_params* p, double* fx, double* fy, double* fz, double* ep,
+                        double* vir) {
+  const int nt = p->ntypes;
+  double* ecut = (double*)malloc(sizeof(double) * nt * nt);
+  for (int a = 0; a < nt * nt; ++a) ecut[a] = orc_lj_energy_cut(p->epsilon[a], p->sigma[a], p->rcut[a]);
+  const double rc2 = p->rcut_max * p->rcut_max;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < n; ++i) {
+    double _fx = 0., _fy = 0., _fz = 0., _ep = 0., _v[9] = {0};
+    const int ta = type[i];
+    for (int64_t k = off[i]; k < off[i + 1]; ++k) {
+      const int nn[3] = {img[3 * k], img[3 * k + 1], img[3 * k + 2]};
+      double dx, dy, dz;
+      const int64_t j = nbr[k];
+      const double d2 = pair_d2(x, y, z, i, j, nn, L, &dx, &dy, &dz);
+      if (!(d2 <= rc2)) continue;
+      const double r = sqrt(d2);
+      const int pid = ta * nt + type[j];
+      if (r <= p->rcut[pid]) {
+        double e, de;
+        orc_lj_pair(p->epsilon[pid], p->sigma[pid], r, &e, &de);
+        e -= ecut[pid];
+        de /= r;
+        const double fex = de * dx, fey = de * dy, fez = de * dz;
+        _fx += fex; _fy += fey; _fz += fez;
+        _ep += .5 * e;
+        add_vir(_v, fex, fey, fez, dx, dy, dz);
+      }
+    }
+    fx[i] = _fx; fy[i] = _fy; fz[i] = _fz;
+    if (ep) ep[i] = _ep;
+    if (vir) for (int q = 0; q < 9; ++q) vir[9 * i + q] = _v[q];
+  }
+  free(ecut);
+}
+
+/* All-image direct LJ sum (no list, no cells): independent check of the
+ * list-based path.  Returns the total energy (sum of per-atom half-pairs). */
+double orc_lj_direct(int64_t n, const double* x, const double* y, const double* z, const double lo[3],
+                     const double hi[3], const orc_lj_params* p, double* fx, double* fy, double* fz) {
+  const double L[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+  const double ecut = orc_lj_energy_cut(p->epsilon, p->sigma, p->rcut);
+  const double rc2 = p->rcut * p->rcut;
+  double etot = 0.0;
+  int reach[3];
+  for (int d = 0; d < 3; ++d) reach[d] = (int)ceil(p->rcut / L[d]) + 1;
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : etot)
+  for (int64_t i = 0; i < n; ++i) {
+    double _fx = 0., _fy = 0., _fz = 0.;
+    for (int64_t j = 0; j < n; ++j)
+      for (int a = -reach[0]; a <= reach[0]; ++a)
+        for (int b = -reach[1]; b <= reach[1]; ++b)
+          for (int c = -reach[2]; c <= reach[2]; ++c) {
+            if (i == j && a == 0 && b == 0 && c == 0) continue;
+            const int nn[3] = {a, b, c};
+            double dx, dy, dz;
+            const double d2 = pair_d2(x, y, z, i, j, nn, L, &dx, &dy, &dz);
+            if (!(d2 <= rc2)) continue;
+            const double r = sqrt(d2);
+            double e, de;
+            orc_lj_pair(p->epsilon, p->sigma, r, &e, &de);
+            e -= ecut;
+            de /= r;
+            _fx += de * dx; _fy += de * dy; _fz += de * dz;
+            etot += 0.5 * e;
+          }
+    fx[i] = _fx; fy[i] = _fy; fz[i] = _fz;
+  }
+  return etot;
+}
+
+/* ------------------------------------------------------------------------ */
+/* EAM alloy                                                                 */
+/* ------------------------------------------------------------------------ */
+
+/* eam_alloy.cpp L29-58 (LAMMPS array2spline): f[1..n] -> 7 coefficients per
+ * knot; coefficients 0-2 give the derivative, 3-6 the value. spline is
+ * (n+1) x 8 doubles, knot 0 left zero. */
+void orc_eam_spline(int n, double delta, const double* f, double* spline) {
+#define S(m, k) spline[(size_t)(m) * 8 + (k)]
+  memset(spline, 0, sizeof(double) * 8 * (size_t)(n + 1));
+  for (int m = 1; m <= n; m++) S(m, 6) = f[m];
+  S(1, 5) = S(2, 6) - S(1, 6);
+  S(2, 5) = 0.5 * (S(3, 6) - S(1, 6));
+  S(n - 1, 5) = 0.5 * (S(n, 6) - S(n - 2, 6));
+  S(n, 5) = S(n, 6) - S(n - 1, 6);
+  for (int m = 3; m <= n - 2; m++)
+    S(m, 5) = ((S(m - 2, 6) - S(m + 2, 6)) + 8.0 * (S(m + 1, 6) - S(m - 1, 6))) / 12.0;
+  for (int m = 1; m <= n - 1; m++) {
+    S(m, 4) = 3.0 * (S(m + 1, 6) - S(m, 6)) - 2.0 * S(m, 5) - S(m + 1, 5);
+    S(m, 3) = S(m, 5) + S(m + 1, 5) - 2.0 * (S(m + 1, 6) - S(m, 6));
+  }
+  S(n, 4) = 0.0;
+  S(n, 3) = 0.0;
+  for (int m = 1; m <= n; m++) {
+    S(m, 2) = S(m, 5) / delta;
+    S(m, 1) = 2.0 * S(m, 4) / delta;
+    S(m, 0) = 3.0 * S(m, 3) / delta;
+  }
+#undef S
+}
+
+static inline int z2r_index(int a, int b) {
+  /* eam_alloy.h L113-132: irow >= icol, n = irow*(irow+1)/2 + icol */
+  int irow = a > b ? a : b, icol = a > b ? b : a;
+  return irow * (irow + 1) / 2 + icol;
+}
+
+static inline void r_knot(const orc_eam_tables* t, double r, int* m, double* p) {
+  double pp = r * t->rdr + 1.0;
+  int mm = (int)pp;
+  if (mm > t->nr - 1) mm = t->nr - 1;
+  pp -= mm;
+  if (pp > 1.0) pp = 1.0;
+  *m = mm;
+  *p = pp;
+}
+
+/* eam_alloy_rho_noderiv (eam_alloy.h L198-220): density contributed at
+ * distance r by an atom of element `itype` (the first type argument selects
+ * the rhor table; SymRhoOp passes the neighbour's type first, L156). */
+double orc_eam_rho(const orc_eam_tables* t, double r, int itype, int jtype) {
+  (void)jtype;
+  int m;
+  double p;
+  r_knot(t, r, &m, &p);
+  const double* c = t->rhor + ((size_t)itype * (t->nr + 1) + m) * 8;
+  return ((c[3] * p + c[4]) * p + c[5]) * p + c[6];
+}
+
+/* eam_alloy_fEmbed (eam_alloy.h L289-313). */
+void orc_eam_embed_one(const orc_eam_tables* t, double rho, int itype, double* phi, double* fp) {
+  double p = rho * t->rdrho + 1.0;
+  int m = (int)p;
+  if (m > t->nrho - 1) m = t->nrho - 1;
+  if (m < 1) m = 1;
+  p -= m;
+  if (p > 1.0) p = 1.0;
+  const double* c = t->frho + ((size_t)itype * (t->nrho + 1) + m) * 8;
+  double f = (c[0] * p + c[1]) * p + c[2];
+  double e = ((c[3] * p + c[4]) * p + c[5]) * p + c[6];
+  if (rho > t->rhomax) e += f * (rho - t->rhomax);
+  *phi = e * t->conv_frho;
+  *fp = f * t->conv_frho;
+}
+
+/* eam_alloy_mm_force (eam_alloy.h L222-265): fpair such that the force on i
+ * is dr * fpair (dr = r_j - r_i), and the pair energy phi. */
+void orc_eam_pair_force(const orc_eam_tables* t, double r, double fpi, double fpj, int itype, int jtype,
+                        double* fpair, double* phi_out) {
+  int m;
+  double p;
+  r_knot(t, r, &m, &p);
+  const double* ci = t->rhor + ((size_t)itype * (t->nr + 1) + m) * 8;
+  const double rhoip = (ci[0] * p + ci[1]) * p + ci[2];
+  const double* cj = t->rhor + ((size_t)jtype * (t->nr + 1) + m) * 8;
+  const double rhojp = (cj[0] * p + cj[1]) * p + cj[2];
+  const double* c = t->z2r + ((size_t)z2r_index(itype, jtype) * (t->nr + 1) + m) * 8;
+  const double z2p = (c[0] * p + c[1]) * p + c[2];
+  const double z2 = ((c[3] * p + c[4]) * p + c[5]) * p + c[6];
+  const double recip = 1.0 / r;
+  double phi = z2 * recip;
+  const double phip = (z2p * recip - phi * recip) * t->conv_z2r;
+  phi *= t->conv_z2r;
+  const double psip = fpi * rhojp + fpj * rhoip + phip;
+  *fpair = psip * recip;
+  *phi_out = phi;
+}
+
+/* Density pass, SymRhoOp without Newton symmetry (eam_force_op_multimat.h
+ * L123-171): rho_i = sum over list pairs with d2 <= rcut^2 of rho_{t_j}(r). */
+void orc_eam_density(int64_t n, const double* x, const double* y, const double* z, const uint8_t* type,
+                     const int64_t* off, const int32_t* nbr, const int8_t* img, const double L[3],
+                     const orc_eam_tables* t, double rcut, double* rho) {
+  const double rc2 = rcut * rcut;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < n; ++i) {
+    double acc = 0.0;
+    for (int64_t k = off[i]; k < off[i + 1]; ++k) {
+      const int nn[3] = {img[3 * k], img[3 * k + 1], img[3 * k + 2]};
+      double dx, dy, dz;
+      const int64_t j = nbr[k];
+      const double d2 = pair_d2(x, y, z, i, j, nn, L, &dx, &dy, &dz);
+      if (!(d2 <= rc2)) continue;
+      acc += orc_eam_rho(t, sqrt(d2), type[j], type[i]);
+    }
+    rho[i] = 0.0 + acc; /* parallel_memset(0) then += at context stop */
+  }
+}
+
+/* Embedding pass, Rho2EmbOp (eam_force_op_multimat.h L174-197): in place
+ * rho -> F'(rho); ep += F(rho) when ep is given. */
+void orc_eam_embed(int64_t n, const uint8_t* type, const orc_eam_tables* t, double* rho_dEmb, double* ep) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    double phi, fp;
+    orc_eam_embed_one(t, rho_dEmb[i], type[i], &phi, &fp);
+    rho_dEmb[i] = fp;
+    if (ep) ep[i] += phi;
+  }
+}
+
+/* Force pass, SymForceOp without Newton symmetry (eam_force_op_multimat.h
+ * L223-304): f_i = sum dr*fpair; with ep: ep_i += sum phi/2, vir_i += sum
+ * -1/2 (dr*fpair) (x) dr.  Forces are set (zero_force_energy ran before);
+ * ep is accumulated on top of the embedding energy. */
+void orc_eam_force(int64_t n, const double* x, const double* y, const double* z, const uint8_t* type,
+                   const int64_t* off, const int32_t* nbr, const int8_t* img, const double L[3],
+                   const orc_eam_tables* t, double rcut, const double* fp, double* fx, double* fy,
+                   double* fz, double* ep, double* vir) {
+  const double rc2 = rcut * rcut;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < n; ++i) {
+    double _fx = 0., _fy = 0., _fz = 0., _ep = 0., _v[9] = {0};
+    const double fpi = fp[i];
+    const int ti = type[i];
+    for (int64_t k = off[i]; k < off[i + 1]; ++k) {
+      const int nn[3] = {img[3 * k], img[3 * k + 1], img[3 * k + 2]};
+      double dx, dy, dz;
+      const int64_t j = nbr[k];
+      const double d2 = pair_d2(x, y, z, i, j, nn, L, &dx, &dy, &dz);
+      if (!(d2 <= rc2)) continue;
+      double fpair, phi;
+      orc_eam_pair_force(t, sqrt(d2), fpi, fp[j], ti, type[j], &fpair, &phi);
+      const double fex = dx * fpair, fey = dy * fpair, fez = dz * fpair;
+      _fx += fex; _fy += fey; _fz += fez;
+      _ep += .5 * phi;
+      add_vir(_v, fex, fey, fez, dx, dy, dz);
+    }
+    fx[i] = _fx; fy[i] = _fy; fz[i] = _fz;
+    if (ep) ep[i] += _ep;
+    if (vir) for (int q = 0; q < 9; ++q) vir[9 * i + q] = _v[q];
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Integration, accel, thermo                                               */
+/* ------------------------------------------------------------------------ */
+
+/* push_f_v_r: r += v*dt' + a*dt'^2/2, dt' = dt*dt_scale (identity xform;
+ * formula restated in push_vec3_2nd_order_xform_minimization.cpp L33-38). */
+void orc_push_f_v_r(int64_t n, double* x, double* y, double* z, const double* vx, const double* vy,
+                    const double* vz, const double* ax, const double* ay, const double* az, double dt,
+                    double dt_scale) {
+  const double h = dt * dt_scale;
+  const double h2 = h * h * 0.5;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    x[i] += vx[i] * h + ax[i] * h2;
+    y[i] += vy[i] * h + ay[i] * h2;
+    z[i] += vz[i] * h + az[i] * h2;
+  }
+}
+
+/* push_f_v: v += a*dt*dt_scale. */
+void orc_push_f_v(int64_t n, double* vx, double* vy, double* vz, const double* ax, const double* ay,
+                  const double* az, double dt, double dt_scale) {
+  const double h = dt * dt_scale;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    vx[i] += ax[i] * h;
+    vy[i] += ay[i] * h;
+    vz[i] += az[i] * h;
+  }
+}
+
+/* push_f_v_r_xform_minimization, identity-xform branch
+ * (push_vec3_2nd_order_xform_minimization.cpp L116-149): r += a*dt'^2/2.
+ * tolF > 0 additionally clips each acceleration component to [-tolF, tolF]
+ * and writes the clipped value back (the clipping of the same file's
+ * non-identity branch, L174-205); tolF <= 0 is the identity branch as is. */
+void orc_push_min(int64_t n, double* x, double* y, double* z, double* ax, double* ay, double* az,
+                  const uint8_t* type, const double* masses, double dt, double dt_scale, double tolF) {
+  (void)type;
+  (void)masses;
+  const double h = dt * dt_scale;
+  const double h2 = h * h * 0.5;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    if (tolF > 0.0) {
+      if (fabs(ax[i]) > tolF) ax[i] = ax[i] > 0. ? tolF : -tolF;
+      if (fabs(ay[i]) > tolF) ay[i] = ay[i] > 0. ? tolF : -tolF;
+      if (fabs(az[i]) > tolF) az[i] = az[i] > 0. ? tolF : -tolF;
+    }
+    x[i] += ax[i] * h2;
+    y[i] += ay[i] * h2;
+    z[i] += az[i] * h2;
+  }
+}
+
+/* force_to_accel (force_to_accel.cu L42-48): a = f / m[type], in place. */
+void orc_force_to_accel(int64_t n, double* fx, double* fy, double* fz, const uint8_t* type,
+                        const double* masses) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    const double m = masses[type ? type[i] : 0];
+    fx[i] /= m;
+    fy[i] /= m;
+    fz[i] /= m;
+  }
+}
+
+/* simulation_thermodynamic_state (L101-163): the 27 reduced doubles, in the
+ * reference's order: virial(9), ke_tensor(9) = 1/2 sum m v(x)v, momentum(3),
+ * kinetic energy vector(3) = 1/2 sum m v*v, potential energy, mass, count.
+ * Summed in fixed 4096-atom chunks so the result is thread-count independent. */
+void orc_thermo(int64_t n, const double* vx, const double* vy, const double* vz, const double* ep,
+                const double* vir, const uint8_t* type, const double* masses, double out[27]) {
+  const int64_t CH = 4096;
+  const int64_t nch = (n + CH - 1) / CH;
+  double* part = (double*)calloc((size_t)(nch > 0 ? nch : 1) * 26, sizeof(double));
+#pragma omp parallel for schedule(static)
+  for (int64_t c = 0; c < nch; ++c) {
+    double* s = part + 26 * c;
+    const int64_t e = (c + 1) * CH < n ? (c + 1) * CH : n;
+    for (int64_t i = c * CH; i < e; ++i) {
+      const double m = masses[type ? type[i] : 0];
+      const double v[3] = {vx[i], vy[i], vz[i]};
+      if (vir) for (int q = 0; q < 9; ++q) s[q] += vir[9 * i + q];
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) s[9 + 3 * a + b] += v[a] * v[b] * m;
+      for (int a = 0; a < 3; ++a) s[18 + a] += v[a] * m;
+      for (int a = 0; a < 3; ++a) s[21 + a] += v[a] * v[a] * m;
+      if (ep) s[24] += ep[i];
+      s[25] += m;
+    }
+  }
+  for (int q = 0; q < 27; ++q) out[q] = 0.0;
+  for (int64_t c = 0; c < nch; ++c)
+    for (int q = 0; q < 26; ++q) out[q] += part[26 * c + q];
+  for (int q = 9; q < 18; ++q) out[q] *= 0.5;
+  for (int q = 21; q < 24; ++q) out[q] *= 0.5;
+  out[26] = (double)n;
+  free(part);
+}
+
+/* ------------------------------------------------------------------------ */
+/* verlet_nve driver (config_numerical_schemes.msp L23-52)                   */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+  int64_t* off;
+  int32_t* nbr;
+  int8_t* img;
+  int64_t cap;
+} orc_list;
+
+static int list_rebuild(orc_list* l, int64_t n, double* x, double* y, double* z, const uint64_t* id,
+                        const double lo[3], const double hi[3], double R) {
+  if (orc_wrap(n, x, y, z, lo, hi) != 0) return -3;
+  int64_t tot = orc_build_neighbors(n, x, y, z, id, lo, hi, R, l->off, l->cap, l->nbr, l->img);
+  if (tot < 0) return -1;
+  if (tot > l->cap) {
+    free(l->nbr);
+    free(l->img);
+    l->cap = tot + tot / 8 + 64;
+    l->nbr = (int32_t*)malloc(sizeof(int32_t) * (size_t)l->cap);
+    l->img = (int8_t*)malloc(3 * (size_t)l->cap);
+    tot = orc_build_neighbors(n, x, y, z, id, lo, hi, R, l->off, l->cap, l->nbr, l->img);
+  }
+  return 0;
+}
+
+static void compute_pair_forces(int64_t n, const double* x, const double* y, const double* z,
+                                const uint8_t* type, const orc_list* l, const double L[3], int pot_kind,
+                                const void* pot, double* fx, double* fy, double* fz, double* ep) {
+  if (pot_kind == ORC_POT_LJ)
+    orc_lj_force(n, x, y, z, l->off, l->nbr, l->img, L, (const orc_lj_params*)pot, fx, fy, fz, ep, NULL);
+  else
+    orc_lj_multi_force(n, x, y, z, type, l->off, l->nbr, l->img, L, (const orc_lj_multi_params*)pot, fx,
+                       fy, fz, ep, NULL);
+}
+
+int orc_run_nve(int64_t n, double* x, double* y, double* z, double* vx, double* vy, double* vz,
+                double* ax, double* ay, double* az, double* ep, const uint8_t* type, const uint64_t* id,
+                const double* masses, const double lo[3], const double hi[3], int pot_kind,
+                const void* pot, double skin, double dt, int nsteps, int rebuild_every,
+                double* thermo_out) {
+  const double L[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+  double rcut;
+  if (pot_kind == ORC_POT_LJ) rcut = ((const orc_lj_params*)pot)->rcut;
+  else if (pot_kind == ORC_POT_LJ_MULTI) rcut = ((const orc_lj_multi_params*)pot)->rcut_max;
+  else rcut = ((const orc_eam_pot*)pot)->rcut;
+  const double R = rcut + skin;
+  orc_list l = {(int64_t*)malloc(sizeof(int64_t) * (size_t)(n + 1)), NULL, NULL, 0};
+  double* rho = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+  int rc = 0;
+#define FORCES()                                                                                   \
+  do {                                                                                             \
+    if (pot_kind == ORC_POT_EAM) {                                                                 \
+      const orc_eam_pot* ep_ = (const orc_eam_pot*)pot;                                            \
+      orc_eam_density(n, x, y, z, type, l.off, l.nbr, l.img, L, &ep_->t, ep_->rcut, rho);          \
+      for (int64_t i_ = 0; i_ < n; ++i_) ep[i_] = 0.0;                                             \
+      orc_eam_embed(n, type, &ep_->t, rho, ep);                                                    \
+      orc_eam_force(n, x, y, z, type, l.off, l.nbr, l.img, L, &ep_->t, ep_->rcut, rho, ax, ay, az, \
+                    ep, NULL);                                                                     \
+    } else {                                                                                       \
+      compute_pair_forces(n, x, y, z, type, &l, L, pot_kind, pot, ax, ay, az, ep);                \
+    }                                                                                              \
+    orc_force_to_accel(n, ax, ay, az, type, masses);                                               \
+  } while (0)
+
+  if ((rc = list_rebuild(&l, n, x, y, z, id, lo, hi, R)) != 0) goto done;
+  FORCES();
+  if (thermo_out) orc_thermo(n, vx, vy, vz, ep, NULL, type, masses, thermo_out);
+  for (int s = 1; s <= nsteps; ++s) {
+    orc_push_f_v_r(n, x, y, z, vx, vy, vz, ax, ay, az, dt, 1.0);
+    orc_push_f_v(n, vx, vy, vz, ax, ay, az, dt, 0.5);
+    if (rebuild_every > 0 && s % rebuild_every == 0)
+      if ((rc = list_rebuild(&l, n, x, y, z, id, lo, hi, R)) != 0) goto done;
+    FORCES();
+    orc_push_f_v(n, vx, vy, vz, ax, ay, az, dt, 0.5);
+    if (thermo_out) orc_thermo(n, vx, vy, vz, ep, NULL, type, masses, thermo_out + 27 * s);
+  }
+#undef FORCES
+done:
+  free(l.off);
+  free(l.nbr);
+  free(l.img);
+  free(rho);
+  return rc;
+}

@@ -1,0 +1,313 @@
+"""GPU parity tests: the sm_103a kernels, called through the C ABI, against
+the FP64 oracle on the same seeded inputs.
+
+Bars (stated per test):
+  * neighbour pair set inside rcut+skin: bit-exact, in the same per-atom order;
+  * FP64 path: forces / energies / virials within 1e-12 relative of the oracle
+    (same formulas; the GPU contracts multiply-adds in the pair function);
+  * mixed path: force error <= 1e-5 relative RMS, energy <= 1e-6 relative;
+  * standalone push operators: bit-exact.
+"""
+import numpy as np
+import pytest
+
+from exastamp_gb300 import setfl as SF
+from exastamp_gb300 import systems as S
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+MIXED_FORCE_TOL = 1e-5
+
+
+def _jitter(s, sig, seed):
+    rng = np.random.default_rng(seed)
+    for a in (s.x, s.y, s.z):
+        a += rng.normal(0.0, sig, s.n)
+    return s
+
+
+def rel_rms(a, b):
+    return float(np.sqrt(((a - b) ** 2).sum() / max((b ** 2).sum(), 1e-300)))
+
+
+def per_atom_lists(rows):
+    out = {}
+    for r in rows:
+        out.setdefault(int(r[0]), []).append((int(r[1]), int(r[2]), int(r[3]), int(r[4])))
+    return out
+
+
+def oracle_lists(oracle, s, R):
+    x, y, z = s.x.copy(), s.y.copy(), s.z.copy()
+    oracle.wrap(x, y, z, s.lo, s.hi)
+    nl = oracle.build_neighbors(x, y, z, s.id, s.lo, s.hi, R)
+    return per_atom_lists(nl.pairs_with_ids(s.id)), (x, y, z), nl
+
+
+def gpu_ctx(gpu, s, pot, skin, mixed=False, tpa=None, block=None):
+    ctx = gpu.Context(0)
+    ctx.upload_system(s)
+    pot(ctx)
+    ctx.set_skin(skin)
+    ctx.set_precision(mixed)
+    if tpa:
+        ctx.set_launch(tpa, block or 128)
+    return ctx
+
+
+LJ = lambda ctx: ctx.set_lj(1.0, 1.0, 2.5)  # noqa: E731
+
+
+@pytest.mark.parametrize("ncell,sig,tpa", [(3, 0.05, 1), (5, 0.1, 4), (8, 0.02, 8), (2, 0.1, 2)])
+def test_pair_set_bit_exact_lj(gpu, oracle, ncell, sig, tpa):
+    s = _jitter(S.lj_fcc(ncell=ncell, seed=ncell), sig, ncell)
+    ref, _, _ = oracle_lists(oracle, s, 2.8)
+    with gpu_ctx(gpu, s, LJ, 0.3, tpa=tpa) as ctx:
+        ctx.build_neighbors()
+        got = per_atom_lists(ctx.export_pairs())
+    assert got.keys() == ref.keys() or (len(ref) < s.n)
+    assert got == ref
+
+
+def test_pair_set_bit_exact_random_gas_and_small_boxes(gpu, oracle):
+    rng = np.random.default_rng(8)
+    for n, L, R in ((400, 9.0, 2.8), (60, 5.7, 2.8), (12, 3.0, 2.9), (2000, 12.0, 2.8)):
+        x, y, z = (rng.uniform(0, L, n) for _ in range(3))
+        s = S.System(x, y, z, np.zeros(n), np.zeros(n), np.zeros(n), np.zeros(n, np.uint8),
+                     rng.permutation(n).astype(np.uint64), np.zeros(3), np.full(3, L), np.array([1.0]))
+        ref, _, _ = oracle_lists(oracle, s, R)
+        with gpu_ctx(gpu, s, lambda c: c.set_lj(1.0, 1.0, R - 0.3), 0.3) as ctx:
+            ctx.build_neighbors()
+            got = per_atom_lists(ctx.export_pairs())
+        assert got == ref, (n, L)
+
+
+def test_empty_and_single_atom(gpu):
+    for n in (0, 1):
+        s = S.System(*(np.full(n, 3.0) for _ in range(6)), np.zeros(n, np.uint8), np.arange(n, dtype=np.uint64),
+                     np.zeros(3), np.full(3, 10.0), np.array([1.0]))
+        with gpu_ctx(gpu, s, LJ, 0.3) as ctx:
+            ctx.compute_forces()
+            d = ctx.download()
+            assert all(len(v) == n for v in d.values())
+            if n:
+                assert d["ax"][0] == 0.0 and d["ep"][0] == 0.0
+            th = ctx.thermo()
+            assert th[26] == n
+
+
+def _lj_oracle(oracle, s):
+    ref, (x, y, z), nl = oracle_lists(oracle, s, 2.8)
+    fx, fy, fz, ep, vir = oracle.lj_force(x, y, z, nl, s.L, 1.0, 1.0, 2.5)
+    return np.stack([fx, fy, fz], 1), ep, vir
+
+
+@pytest.mark.parametrize("tpa", [1, 2, 4, 8, 16])
+def test_lj_fp64_matches_oracle(gpu, oracle, tpa):
+    s = _jitter(S.lj_fcc(ncell=6, seed=1), 0.04, 1)
+    F, ep, vir = _lj_oracle(oracle, s)
+    with gpu_ctx(gpu, s, LJ, 0.3, tpa=tpa) as ctx:
+        ctx.compute_forces(energy=True, virial=True)
+        d = ctx.download(virial=True)
+    G = np.stack([d["ax"], d["ay"], d["az"]], 1)
+    assert rel_rms(G, F) < FP64_TOL
+    assert np.abs(G - F).max() < 1e-11 * np.abs(F).max()
+    assert np.abs(d["ep"] - ep).max() < FP64_TOL * np.abs(ep).max()
+    assert np.abs(d["vir"] - vir).max() < FP64_TOL * np.abs(vir).max()
+
+
+@pytest.mark.parametrize("tpa", [1, 4, 8])
+def test_lj_mixed_within_tolerance(gpu, oracle, tpa):
+    s = _jitter(S.lj_fcc(ncell=8, seed=2), 0.06, 2)
+    F, ep, vir = _lj_oracle(oracle, s)
+    with gpu_ctx(gpu, s, LJ, 0.3, mixed=True, tpa=tpa) as ctx:
+        ctx.compute_forces(energy=True, virial=True)
+        d = ctx.download(virial=True)
+    G = np.stack([d["ax"], d["ay"], d["az"]], 1)
+    assert rel_rms(G, F) < MIXED_FORCE_TOL
+    assert abs(d["ep"].sum() - ep.sum()) < 1e-6 * abs(ep.sum())
+    assert rel_rms(d["vir"], vir) < 1e-5
+
+
+def test_lj_multi_matches_oracle(gpu, oracle):
+    s = _jitter(S.lj_fcc(ncell=6, seed=3), 0.05, 3)
+    rng = np.random.default_rng(3)
+    s.type = (rng.random(s.n) < 0.2).astype(np.uint8)
+    s.masses = np.array([1.0, 2.0])
+    eps, sig, rc = S.kob_andersen_tables()
+    rcmax = float(rc.max())
+    x, y, z = s.x.copy(), s.y.copy(), s.z.copy()
+    oracle.wrap(x, y, z, s.lo, s.hi)
+    nl = oracle.build_neighbors(x, y, z, s.id, s.lo, s.hi, rcmax + 0.3)
+    fx, fy, fz, ep, vir = oracle.lj_multi_force(x, y, z, s.type, nl, s.L, eps, sig, rc, rcmax)
+    F = np.stack([fx, fy, fz], 1) / s.masses[s.type][:, None]
+    for mixed, tol in ((False, FP64_TOL), (True, MIXED_FORCE_TOL)):
+        with gpu_ctx(gpu, s, lambda c: c.set_lj_multi(eps, sig, rc, 0.0), 0.3, mixed=mixed) as ctx:
+            ctx.compute_forces(energy=True)
+            d = ctx.download()
+        G = np.stack([d["ax"], d["ay"], d["az"]], 1)
+        assert rel_rms(G, F) < tol, mixed
+        assert abs(d["ep"].sum() - ep.sum()) < (1e-12 if not mixed else 1e-6) * abs(ep.sum())
+
+
+def _eam_setup(oracle, ncell=5, displace=0.08, seed=4):
+    cfg = SF.load_cu_params()
+    sf = SF.tabulate(cfg)
+    tab = oracle.EamOracleTables.from_setfl(sf, S.EV, S.EV, rcut=5.0)
+    s = S.eam_cu_fcc(ncell=ncell, displace=displace, seed=seed)
+    return sf, tab, s
+
+
+@pytest.mark.parametrize("tpa", [1, 4, 8])
+def test_eam_fp64_and_mixed_match_oracle(gpu, oracle, tpa):
+    sf, tab, s = _eam_setup(oracle)
+    ref, (x, y, z), nl = oracle_lists(oracle, s, 5.3)
+    fx, fy, fz, ep, vir, fp, rho = oracle.eam_forces(x, y, z, s.type, nl, s.L, tab, 5.0)
+    F = np.stack([fx, fy, fz], 1) / s.masses[0]
+    for mixed, tol in ((False, FP64_TOL), (True, MIXED_FORCE_TOL)):
+        with gpu_ctx(gpu, s, lambda c: c.set_eam_alloy(sf, 5.0, S.EV, S.EV), 0.3, mixed=mixed, tpa=tpa) as ctx:
+            ctx.compute_forces(energy=True, virial=True)
+            d = ctx.download(virial=True)
+            if not mixed:
+                got = per_atom_lists(ctx.export_pairs())
+                assert got == ref
+        G = np.stack([d["ax"], d["ay"], d["az"]], 1)
+        assert rel_rms(G, F) < tol, (mixed, rel_rms(G, F))
+        etol = FP64_TOL if not mixed else 1e-6
+        assert abs(d["ep"].sum() - ep.sum()) < etol * abs(ep.sum())
+        assert rel_rms(d["vir"], vir) < (FP64_TOL if not mixed else 1e-5)
+
+
+def test_eam_setfl_file_path(gpu, oracle, tmp_path):
+    sf, tab, s = _eam_setup(oracle, ncell=4)
+    p = str(tmp_path / "cu.eam.alloy")
+    SF.write_setfl(sf, p)
+    sf2 = SF.read_setfl(p)
+    with gpu_ctx(gpu, s, lambda c: c.load_setfl(p, 5.0, S.EV, S.EV), 0.3) as c1, \
+            gpu_ctx(gpu, s, lambda c: c.set_eam_alloy(sf2, 5.0, S.EV, S.EV), 0.3) as c2:
+        c1.compute_forces()
+        c2.compute_forces()
+        a, b = c1.download(), c2.download()
+    assert np.array_equal(a["ax"], b["ax"]) and np.array_equal(a["ep"], b["ep"])
+
+
+def test_push_operators_bit_exact(gpu, oracle):
+    s = _jitter(S.lj_fcc(ncell=4, seed=5), 0.03, 5)
+    with gpu_ctx(gpu, s, LJ, 0.3) as ctx:
+        ctx.compute_forces()
+        d0 = ctx.download()
+        ctx.push_f_v_r(0.005, 1.0)
+        ctx.push_f_v(0.005, 0.5)
+        d1 = ctx.download()
+        ctx.push_min(0.01, 1.0, 0.5)
+        d2 = ctx.download()
+    st = {k: d0[k].copy() for k in d0}
+    oracle.push_f_v_r(st["x"], st["y"], st["z"], st["vx"], st["vy"], st["vz"], st["ax"], st["ay"], st["az"], 0.005, 1.0)
+    oracle.push_f_v(st["vx"], st["vy"], st["vz"], st["ax"], st["ay"], st["az"], 0.005, 0.5)
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        assert np.array_equal(d1[k], st[k]), k
+    oracle.push_min(st["x"], st["y"], st["z"], st["ax"], st["ay"], st["az"], 0.01, 1.0, 0.5)
+    for k in ("x", "y", "z", "ax", "ay", "az"):
+        assert np.array_equal(d2[k], st[k]), k
+
+
+def test_thermo_matches_oracle(gpu, oracle):
+    s = _jitter(S.lj_fcc(ncell=7, seed=6), 0.03, 6)
+    with gpu_ctx(gpu, s, LJ, 0.3) as ctx:
+        ctx.compute_forces(energy=True, virial=True)
+        d = ctx.download(virial=True)
+        th = ctx.thermo()
+    ref = oracle.thermo(d["vx"], d["vy"], d["vz"], d["ep"], d["vir"], s.type, s.masses)
+    assert np.allclose(th, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+
+
+def _nve_compare(gpu, oracle, s, pot_gpu, pot_kind, pot_orc, skin, dt, nsteps, R, mixed, use_graph=False):
+    st = s.state()
+    th_ref = oracle.run_nve(st, s.masses, s.lo, s.hi, pot_kind, pot_orc, skin, dt, nsteps, R)
+    with gpu_ctx(gpu, s, pot_gpu, skin, mixed=mixed) as ctx:
+        th = ctx.run_nve(nsteps, dt, rebuild_every=R, thermo_every=1 if not use_graph else 2 * R,
+                         use_graph=use_graph)
+        d = ctx.download()
+    return th_ref, th, st, d
+
+
+def test_lj_nve_fp64_tracks_oracle(gpu, oracle):
+    """20 NVE steps, rebuild every 10: FP64 GPU state stays within 1e-10 of
+    the oracle's (rounding differences grow slowly in a chaotic system)."""
+    s = S.lj_fcc(ncell=5, seed=7)
+    th_ref, th, st, d = _nve_compare(gpu, oracle, s, LJ, oracle.POT_LJ, oracle.LJParams(1.0, 1.0, 2.5), 0.3,
+                                     0.005, 20, 10, mixed=False)
+    for k in ("x", "vx", "ax"):
+        assert np.abs(d[k] - st[k]).max() < 1e-10, k
+    assert np.allclose(th, th_ref, rtol=1e-9, atol=1e-9)
+
+
+def test_eam_nve_fp64_tracks_oracle(gpu, oracle):
+    sf, tab, s = _eam_setup(oracle, ncell=4, displace=0.02)
+    th_ref, th, st, d = _nve_compare(gpu, oracle, s, lambda c: c.set_eam_alloy(sf, 5.0, S.EV, S.EV),
+                                     oracle.POT_EAM, tab, 0.3, 1e-3, 20, 10, mixed=False)
+    assert np.abs(d["x"] - st["x"]).max() < 1e-10
+    assert np.allclose(th, th_ref, rtol=1e-9, atol=1e-9 * np.abs(th_ref).max())
+
+
+def test_mixed_nve_energy_drift_lj(gpu, oracle):
+    s = S.lj_fcc(ncell=6, seed=8)
+    with gpu_ctx(gpu, s, LJ, 0.3, mixed=True) as ctx:
+        th = ctx.run_nve(400, 0.005, rebuild_every=10, thermo_every=10)
+    etot = th[:, 21:24].sum(1) + th[:, 24]
+    drift_per_atom = abs(etot[-1] - etot[0]) / s.n
+    assert drift_per_atom < 2e-3
+    assert np.abs(th[:, 18:21]).max() < 1e-6
+
+
+def test_graph_run_equals_stepwise_run(gpu, oracle):
+    s = S.lj_fcc(ncell=5, seed=9)
+    outs = []
+    for use_graph in (False, True):
+        with gpu_ctx(gpu, s, LJ, 0.3, mixed=True) as ctx:
+            ctx.run_nve(65, 0.005, rebuild_every=10, use_graph=use_graph)
+            outs.append(ctx.download())
+    for k in outs[0]:
+        assert np.array_equal(outs[0][k], outs[1][k]), k
+
+
+def test_runs_are_bit_reproducible(gpu):
+    s = S.lj_fcc(ncell=6, seed=10)
+    outs = []
+    for _ in range(2):
+        with gpu_ctx(gpu, s, LJ, 0.3, mixed=True, tpa=4) as ctx:
+            ctx.run_nve(30, 0.005, rebuild_every=10)
+            outs.append(ctx.download())
+    for k in outs[0]:
+        assert np.array_equal(outs[0][k], outs[1][k]), k
+
+
+def test_upload_positions_triggers_rebuild(gpu, oracle):
+    s = _jitter(S.lj_fcc(ncell=5, seed=11), 0.02, 11)
+    with gpu_ctx(gpu, s, LJ, 0.3) as ctx:
+        ctx.compute_forces()
+        # move every atom by 0.2 (> skin/2): the list must be rebuilt
+        x2 = s.x + 0.2
+        ctx.upload_positions(x2, s.y, s.z)
+        ctx.compute_forces()
+        d = ctx.download()
+        got = per_atom_lists(ctx.export_pairs())
+    s2 = s.copy()
+    s2.x = x2
+    F, ep, _ = _lj_oracle(oracle, s2)
+    G = np.stack([d["ax"], d["ay"], d["az"]], 1)
+    assert rel_rms(G, F) < FP64_TOL
+    ref, _, _ = oracle_lists(oracle, s2, 2.8)
+    assert got == ref
+
+
+def test_nonfinite_force_reported(gpu):
+    """Two atoms at the same position: the FP64 path divides by r = 0 and
+    the context reports GBMD_ERR_NONFINITE (no device trap)."""
+    s = S.lj_fcc(ncell=3, seed=12)
+    s.x[1], s.y[1], s.z[1] = s.x[0], s.y[0], s.z[0]
+    with gpu_ctx(gpu, s, LJ, 0.3) as ctx:
+        with pytest.raises(gpu.GbmdError) as e:
+            ctx.run_nve(1, 0.001, rebuild_every=0)
+        assert e.value.code == 6
