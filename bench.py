@@ -71,7 +71,12 @@ def parse():
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--lanes", type=int, default=0, help="lanes per atom (0: autotune)")
     p.add_argument("--block", type=int, default=0)
-    return p.parse_args()
+    p.add_argument("--ncell", type=int, default=0,
+                   help="override the unit cells per edge (small profiling cases of the same workload)")
+    a = p.parse_args()
+    if a.ncell:
+        WORKLOADS[a.workload] = dict(WORKLOADS[a.workload], ncell=a.ncell)
+    return a
 
 
 # ---------------------------------------------------------------------------

@@ -738,7 +738,7 @@ static int one_step(gbmd_context* c, double dt, const StepPlan& p, bool check, d
     launch_thermo(c, true);
     if (thermo_row)
       GBMD_CUDA(c, cudaMemcpyAsync(thermo_row, c->d_thermo, sizeof(double) * 27, cudaMemcpyDeviceToDevice, c->stream));
-    if (!p.last) launch_first_half(c, dt);
+    if (!p.last) launch_first_half_swap(c, dt);
   }
   return GBMD_OK;
 }

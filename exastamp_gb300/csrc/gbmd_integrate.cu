@@ -31,6 +31,7 @@ __device__ __forceinline__ void refresh_gather(const Grid& g, int64_t i, int cp,
 struct PushArgs {
   int64_t n;
   double *x, *y, *z, *vx, *vy, *vz, *ax, *ay, *az;
+  double *xo, *yo, *zo;  // position outputs (== x,y,z in place, or the other buffer)
   const uint8_t* type;
   const int32_t* cellpack;
   float4* pf;
@@ -68,9 +69,9 @@ __global__ void k_first_half(PushArgs P, double h, double h2, double hv) {
   const double x = __dadd_rn(P.x[i], __dadd_rn(__dmul_rn(vx, h), __dmul_rn(ax, h2)));
   const double y = __dadd_rn(P.y[i], __dadd_rn(__dmul_rn(vy, h), __dmul_rn(ay, h2)));
   const double z = __dadd_rn(P.z[i], __dadd_rn(__dmul_rn(vz, h), __dmul_rn(az, h2)));
-  P.x[i] = x;
-  P.y[i] = y;
-  P.z[i] = z;
+  P.xo[i] = x;
+  P.yo[i] = y;
+  P.zo[i] = z;
   P.vx[i] = __dadd_rn(vx, __dmul_rn(ax, hv));
   P.vy[i] = __dadd_rn(vy, __dmul_rn(ay, hv));
   P.vz[i] = __dadd_rn(vz, __dmul_rn(az, hv));
@@ -105,6 +106,7 @@ static PushArgs push_args(gbmd_context* c) {
   P.vx = c->VX(); P.vy = c->VY(); P.vz = c->VZ();
   P.ax = c->AX(); P.ay = c->AY(); P.az = c->AZ();
   P.type = c->TYPE();
+  P.xo = P.x; P.yo = P.y; P.zo = P.z;
   P.cellpack = c->cellpack;
   P.pf = c->POSF();
   P.pd = c->POSD();
@@ -130,6 +132,25 @@ void launch_first_half(gbmd_context* c, double dt) {
   const double h = dt * 1.0;
   const double h2 = h * h * 0.5;
   k_first_half<<<nblk(c->n, 256), 256, 0, c->stream>>>(push_args(c), h, h2, dt * 0.5);
+}
+
+// verlet_first_half writing the new positions (and gather copies) into the
+// other position buffer, then swapping: every step of the runner swaps the
+// position buffers exactly once, whichever path it takes, so a captured
+// chunk of steps always ends on the buffer it started from.
+void launch_first_half_swap(gbmd_context* c, double dt) {
+  if (!c->n) return;
+  PushArgs P = push_args(c);
+  const int o = c->cur ^ 1;
+  P.xo = c->rbuf[o];
+  P.yo = c->rbuf[o] + c->cap;
+  P.zo = c->rbuf[o] + 2 * c->cap;
+  P.pf = c->posf[o];
+  P.pd = c->posd[o];
+  const double h = dt * 1.0;
+  const double h2 = h * h * 0.5;
+  k_first_half<<<nblk(c->n, 256), 256, 0, c->stream>>>(P, h, h2, dt * 0.5);
+  c->cur = o;
 }
 
 void launch_push_min(gbmd_context* c, double dt, double dt_scale, double tolF) {
@@ -197,17 +218,23 @@ __global__ void __launch_bounds__(TH_THREADS) k_thermo_part(ThermoArgs T, double
   }
 }
 
+// one warp per reduced quantity: lane-strided partial sums, then a fixed
+// shuffle tree -- the summation order depends only on the block count
 __global__ void k_thermo_final(const double* __restrict__ part, int nb, int64_t n, double* __restrict__ out) {
-  const int q = threadIdx.x;
+  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (q >= 27) return;
   if (q == 26) {
-    out[26] = (double)n;
+    if (lane == 0) out[26] = (double)n;
     return;
   }
   double v = 0.0;
-  for (int b = 0; b < nb; ++b) v += part[(size_t)b * 26 + q];
-  if ((q >= 9 && q < 18) || (q >= 21 && q < 24)) v *= 0.5;
-  out[q] = v;
+  for (int b = lane; b < nb; b += 32) v += part[(size_t)b * 26 + q];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (lane == 0) {
+    if ((q >= 9 && q < 18) || (q >= 21 && q < 24)) v *= 0.5;
+    out[q] = v;
+  }
 }
 
 void launch_thermo(gbmd_context* c, bool with_virial) {
@@ -220,7 +247,7 @@ void launch_thermo(gbmd_context* c, bool with_virial) {
   for (int t = 0; t < GBMD_MAX_TYPES; ++t) T.mass[t] = t < c->ntypes ? c->mass[t] : 1.0;
   const int nb = thermo_blocks(c->n);
   k_thermo_part<<<nb, TH_THREADS, 0, c->stream>>>(T, c->d_part);
-  k_thermo_final<<<1, 32, 0, c->stream>>>(c->d_part, nb, c->n, c->d_thermo);
+  k_thermo_final<<<1, 27 * 32, 0, c->stream>>>(c->d_part, nb, c->n, c->d_thermo);
 }
 
 }  // namespace gbmd

@@ -220,6 +220,7 @@ void launch_push_f_v_r(gbmd_context* c, double dt, double dt_scale);
 void launch_push_f_v(gbmd_context* c, double dt, double dt_scale);
 void launch_push_min(gbmd_context* c, double dt, double dt_scale, double tolF);
 void launch_first_half(gbmd_context* c, double dt);
+void launch_first_half_swap(gbmd_context* c, double dt);
 void launch_thermo(gbmd_context* c, bool with_virial);
 int thermo_blocks(int64_t n);
 

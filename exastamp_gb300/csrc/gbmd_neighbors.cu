@@ -16,7 +16,8 @@
 //   k_cell_rank   canonical (id, upload index) order per cell   L1-resident
 //   k_gather      permute the FP64 state into cell order        HBM: ~130 B r/w
 //   k_posf        FP32 local + FP64 packed gather copies        HBM: 24 B r, 48 B w
-//   k_build_list  27-cell stencil scan, write entries           HBM: 4 B per entry
+//   k_build_list_cells  warp per home cell over the 27-cell candidates, ballot
+//                 compaction in canonical order                 HBM: 4 B per entry
 #include <cstdio>
 #include <cstring>
 
@@ -251,67 +252,134 @@ __global__ void k_posf(int64_t n, const double* __restrict__ x, const double* __
   pd[i] = make_double4_32a(xi, yi, zi, (double)t);
 }
 
-__global__ void k_build_list(int64_t n, const float4* __restrict__ pf, const double* __restrict__ x,
-                             const double* __restrict__ y, const double* __restrict__ z,
-                             const int32_t* __restrict__ cellpack, const int32_t* __restrict__ cstart,
-                             Grid g, double R2, float R2lo, float R2hi, uint32_t* __restrict__ nbr,
-                             int32_t* __restrict__ nnb, int maxnb, int T, int64_t stride,
-                             int* __restrict__ err) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int cnt = 0;
-  if (i < n) {
-    const int cp = cellpack[i];
-    const int cx = cp & 1023, cy = (cp >> 10) & 1023, cz = cp >> 20;
-    const float4 pi = pf[i];
-    const double xi = x[i], yi = y[i], zi = z[i];
-    for (int dz = -1; dz <= 1; ++dz) {
-      const int nz = image_of(cz, dz, g.nc[2]);
-      const int wz = cz + dz - nz * g.nc[2];
-      const float sz = (float)dz * g.hf[2];
-      const double Sz = (double)nz * g.L[2];
-      for (int dy = -1; dy <= 1; ++dy) {
-        const int ny = image_of(cy, dy, g.nc[1]);
-        const int wy = cy + dy - ny * g.nc[1];
-        const float sy = (float)dy * g.hf[1];
-        const double Sy = (double)ny * g.L[1];
-        for (int dx = -1; dx <= 1; ++dx) {
-          const int nx = image_of(cx, dx, g.nc[0]);
-          const int wx = cx + dx - nx * g.nc[0];
-          const float sx = (float)dx * g.hf[0];
-          const double Sx = (double)nx * g.L[0];
-          const uint32_t code = (uint32_t)(dx + 1) | ((uint32_t)(dy + 1) << 2) | ((uint32_t)(dz + 1) << 4);
-          const int64_t cell = ((int64_t)wz * g.nc[1] + wy) * g.nc[0] + wx;
-          const int beg = cstart[cell], end = cstart[cell + 1];
-          const bool self = (nx | ny | nz) == 0;
-          for (int k = beg; k < end; ++k) {
-            if (self && k == i) continue;
-            const float4 pj = pf[k];
-            const float ddx = (pj.x - pi.x) + sx;
-            const float ddy = (pj.y - pi.y) + sy;
-            const float ddz = (pj.z - pi.z) + sz;
-            const float d2f = ddx * ddx + ddy * ddy + ddz * ddz;
-            bool in;
-            if (d2f > R2hi) in = false;
-            else if (d2f < R2lo) in = true;
-            else {
-              double a, b, c;
-              in = exact_d2(xi, yi, zi, x[k], y[k], z[k], Sx, Sy, Sz, a, b, c) <= R2;
-            }
-            if (in) {
-              if (cnt < maxnb) nbr[nbr_slot(i, cnt, T, stride)] = (uint32_t)k | (code << GBMD_IDX_BITS);
-              ++cnt;
-            }
-          }
+// One warp per home cell.  Lane s < 27 describes stencil cell s (start,
+// count, code, FP32 shift); the 27 candidate ranges are concatenated in
+// stencil order and walked 32 candidates at a time, one per lane, so each
+// candidate position is loaded once per chunk and tested against every home
+// atom of the cell (home positions held one per lane, broadcast by shuffle).
+// A ballot + popc compacts the hits of each home atom in candidate order,
+// which is the canonical order (stencil code, then cell order).
+__global__ void __launch_bounds__(128) k_build_list_cells(
+    int64_t ncells, const float4* __restrict__ pf, const double* __restrict__ x, const double* __restrict__ y,
+    const double* __restrict__ z, const int32_t* __restrict__ cstart, Grid g, double R2, float R2lo, float R2hi,
+    uint32_t* __restrict__ nbr, int32_t* __restrict__ nnb, int maxnb, int T, int64_t stride,
+    int* __restrict__ err) {
+  const int64_t cell = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (cell >= ncells) return;  // uniform per warp
+  const unsigned FULL = 0xffffffffu;
+  const int cx = (int)(cell % g.nc[0]), cy = (int)((cell / g.nc[0]) % g.nc[1]),
+            cz = (int)(cell / ((int64_t)g.nc[0] * g.nc[1]));
+  // stencil cell of this lane
+  int s_start = 0, s_cnt = 0;
+  uint32_t s_code = 0;
+  float s_sx = 0.f, s_sy = 0.f, s_sz = 0.f;
+  if (lane < 27) {
+    const int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
+    const int nx = image_of(cx, dx, g.nc[0]), ny = image_of(cy, dy, g.nc[1]), nz = image_of(cz, dz, g.nc[2]);
+    const int64_t cj = ((int64_t)(cz + dz - nz * g.nc[2]) * g.nc[1] + (cy + dy - ny * g.nc[1])) * g.nc[0] +
+                       (cx + dx - nx * g.nc[0]);
+    s_start = cstart[cj];
+    s_cnt = cstart[cj + 1] - s_start;
+    s_code = (uint32_t)(dx + 1) | ((uint32_t)(dy + 1) << 2) | ((uint32_t)(dz + 1) << 4);
+    s_sx = (float)dx * g.hf[0];
+    s_sy = (float)dy * g.hf[1];
+    s_sz = (float)dz * g.hf[2];
+  }
+  int incl = s_cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int s_pre = incl - s_cnt;  // exclusive prefix of this lane's stencil cell
+  const int total = __shfl_sync(FULL, incl, 26);
+  const int hb = cstart[cell], nh = cstart[cell + 1] - hb;
+  const uint32_t CENTER = 1u | (1u << 2) | (1u << 4);
+  // per-warp shared memory: 32 home positions, 32 counts, 32 x maxnb entries
+  extern __shared__ float4 smem_build[];
+  float4* hpos = smem_build + (size_t)(threadIdx.x >> 5) * (40 + 8 * (size_t)maxnb);
+  int* cnt_s = reinterpret_cast<int*>(hpos + 32);
+  uint32_t* tile = reinterpret_cast<uint32_t*>(hpos + 40);
+  int warp_max = 0;
+  for (int hbatch = 0; hbatch < nh; hbatch += 32) {
+    const int nhb = min(32, nh - hbatch);
+    const bool hv = lane < nhb;
+    const int64_t ih = hb + hbatch + lane;
+    if (hv) hpos[lane] = pf[ih];
+    __syncwarp();
+    int cnt = 0;
+    for (int q0 = 0; q0 < total; q0 += 32) {
+      const int q = q0 + lane;
+      const bool valid = q < total;
+      // stencil cell of candidate q: largest s with s_pre(s) <= q (5-step search)
+      int s = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int t = min(s + step, 26);
+        const int pv = __shfl_sync(FULL, s_pre, t);
+        if (s + step <= 26 && pv <= q) s = t;
+      }
+      const int k = __shfl_sync(FULL, s_start, s) + (q - __shfl_sync(FULL, s_pre, s));
+      const uint32_t code = __shfl_sync(FULL, s_code, s);
+      const float sx = __shfl_sync(FULL, s_sx, s), sy = __shfl_sync(FULL, s_sy, s), sz = __shfl_sync(FULL, s_sz, s);
+      float4 pj = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (valid) pj = pf[k];
+      const float jx = pj.x + sx, jy = pj.y + sy, jz = pj.z + sz;
+      // counts before this chunk: no dependency between the home-atom
+      // iterations below, so they pipeline
+      const int mybase = cnt;
+      unsigned mymask = 0u;
+      for (int hh = 0; hh < nhb; ++hh) {
+        const int64_t i = hb + hbatch + hh;
+        const float4 pi = hpos[hh];
+        const float dx = jx - pi.x;
+        const float dy = jy - pi.y;
+        const float dz = jz - pi.z;
+        const float d2f = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        bool in = valid && !(k == i && code == CENTER) && d2f <= R2hi;
+        if (in && d2f >= R2lo) {
+          const int nxi = image_of(cx, int(code & 3u) - 1, g.nc[0]);
+          const int nyi = image_of(cy, int((code >> 2) & 3u) - 1, g.nc[1]);
+          const int nzi = image_of(cz, int((code >> 4) & 3u) - 1, g.nc[2]);
+          double a, b, cc;
+          in = exact_d2(x[i], y[i], z[i], x[k], y[k], z[k], (double)nxi * g.L[0], (double)nyi * g.L[1],
+                        (double)nzi * g.L[2], a, b, cc) <= R2;
         }
+        const unsigned mask = __ballot_sync(FULL, in);
+        const int base = __shfl_sync(FULL, mybase, hh);
+        if (in) {
+          const int pos = base + __popc(mask & ((1u << lane) - 1u));
+          if (pos < maxnb) tile[hh * maxnb + pos] = (uint32_t)k | (code << GBMD_IDX_BITS);
+        }
+        if (lane == hh) mymask = mask;
+      }
+      cnt += __popc(mymask);
+    }
+    if (hv) {
+      nnb[ih] = cnt;
+      if (cnt > maxnb) atomicOr(&err[ERRW_FLAGS], GBMD_DEVERR_NBR_OVERFLOW);
+    }
+    cnt_s[lane] = hv ? min(cnt, maxnb) : 0;
+    warp_max = max(warp_max, cnt);
+    int bmax = cnt_s[lane];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) bmax = max(bmax, __shfl_xor_sync(FULL, bmax, o));
+    __syncwarp();
+    // coalesced write-out: list row r holds slots r*T..r*T+T-1 of consecutive
+    // atoms contiguously, so the batch's part of a row is nhb*T adjacent words
+    const int64_t row0 = (int64_t)(hb + hbatch) * T;
+    for (int r = 0; r * T < bmax; ++r) {
+      for (int w = lane; w < nhb * T; w += 32) {
+        const int hh = w / T, pos = r * T + (w - hh * T);
+        if (pos < cnt_s[hh]) nbr[(int64_t)r * stride + row0 + w] = tile[hh * maxnb + pos];
       }
     }
-    nnb[i] = cnt;
-    if (cnt > maxnb) atomicOr(&err[ERRW_FLAGS], GBMD_DEVERR_NBR_OVERFLOW);
+    __syncwarp();
   }
-  int m = cnt;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(&err[ERRW_MAXNB], m);
+  for (int o = 16; o > 0; o >>= 1) warp_max = max(warp_max, __shfl_xor_sync(FULL, warp_max, o));
+  if (lane == 0 && warp_max > 0) atomicMax(&err[ERRW_MAXNB], warp_max);
 }
 
 static inline unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
@@ -338,9 +406,17 @@ static int build_list(gbmd_context* c) {
   }
   c->npad = npad;
   GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_MAXNB, 0, sizeof(int), c->stream));
-  k_build_list<<<nblk(c->n, 128), 128, 0, c->stream>>>(c->n, c->POSF(), c->X(), c->Y(), c->Z(), c->cellpack,
-                                                        c->cell_start, c->grid, R2, R2lo, R2hi, c->nbr, c->nnb,
-                                                        c->maxnb, c->tpa, stride, c->d_err);
+  // shared memory per warp: 32 home positions + 32 counts + 32 x maxnb entries
+  const size_t per_warp = 640 + 128 * (size_t)c->maxnb;
+  int W = (int)((96 * 1024) / per_warp);
+  W = W < 1 ? 1 : (W > 4 ? 4 : W);
+  const size_t smem = per_warp * W;
+  if (smem > 227 * 1024) return set_error(c, GBMD_ERR_TOO_LARGE, "neighbour capacity %d per atom too large", c->maxnb);
+  if (smem > 48 * 1024)
+    GBMD_CUDA(c, cudaFuncSetAttribute(k_build_list_cells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_build_list_cells<<<nblk(c->grid.ncells, W), 32 * W, smem, c->stream>>>(
+      c->grid.ncells, c->POSF(), c->X(), c->Y(), c->Z(), c->cell_start, c->grid, R2, R2lo, R2hi, c->nbr, c->nnb,
+      c->maxnb, c->tpa, stride, c->d_err);
   return GBMD_OK;
 }
 

@@ -44,6 +44,9 @@ struct PairArgs {
   int* err;
 };
 
+// Mixed-precision pair kernels (gbmd_mixed.cu); part as in launch_forces.
+int launch_mixed(gbmd_context* c, const PairArgs& A, int part, bool ev);
+
 // Integer image of the stencil cell of `code` seen from home cell (cx,cy,cz).
 __device__ __forceinline__ void image_shift(const Grid& g, int cx, int cy, int cz, uint32_t code,
                                             double& Sx, double& Sy, double& Sz) {

@@ -672,12 +672,12 @@ static int list_rebuild(orc_list* l, int64_t n, double* x, double* y, double* z,
 
 static void compute_pair_forces(int64_t n, const double* x, const double* y, const double* z,
                                 const uint8_t* type, const orc_list* l, const double L[3], int pot_kind,
-                                const void* pot, double* fx, double* fy, double* fz, double* ep) {
+                                const void* pot, double* fx, double* fy, double* fz, double* ep, double* vir) {
   if (pot_kind == ORC_POT_LJ)
-    orc_lj_force(n, x, y, z, l->off, l->nbr, l->img, L, (const orc_lj_params*)pot, fx, fy, fz, ep, NULL);
+    orc_lj_force(n, x, y, z, l->off, l->nbr, l->img, L, (const orc_lj_params*)pot, fx, fy, fz, ep, vir);
   else
     orc_lj_multi_force(n, x, y, z, type, l->off, l->nbr, l->img, L, (const orc_lj_multi_params*)pot, fx,
-                       fy, fz, ep, NULL);
+                       fy, fz, ep, vir);
 }
 
 int orc_run_nve(int64_t n, double* x, double* y, double* z, double* vx, double* vy, double* vz,
@@ -693,6 +693,8 @@ int orc_run_nve(int64_t n, double* x, double* y, double* z, double* vx, double* 
   const double R = rcut + skin;
   orc_list l = {(int64_t*)malloc(sizeof(int64_t) * (size_t)(n + 1)), NULL, NULL, 0};
   double* rho = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+  /* per-atom virial, summed by the thermo reduction (mechanics grid flavor) */
+  double* vir = thermo_out ? (double*)calloc(9 * (size_t)(n > 0 ? n : 1), sizeof(double)) : NULL;
   int rc = 0;
 #define FORCES()                                                                                   \
   do {                                                                                             \
@@ -702,16 +704,16 @@ int orc_run_nve(int64_t n, double* x, double* y, double* z, double* vx, double* 
       for (int64_t i_ = 0; i_ < n; ++i_) ep[i_] = 0.0;                                             \
       orc_eam_embed(n, type, &ep_->t, rho, ep);                                                    \
       orc_eam_force(n, x, y, z, type, l.off, l.nbr, l.img, L, &ep_->t, ep_->rcut, rho, ax, ay, az, \
-                    ep, NULL);                                                                     \
+                    ep, vir);                                                                      \
     } else {                                                                                       \
-      compute_pair_forces(n, x, y, z, type, &l, L, pot_kind, pot, ax, ay, az, ep);                \
+      compute_pair_forces(n, x, y, z, type, &l, L, pot_kind, pot, ax, ay, az, ep, vir);           \
     }                                                                                              \
     orc_force_to_accel(n, ax, ay, az, type, masses);                                               \
   } while (0)
 
   if ((rc = list_rebuild(&l, n, x, y, z, id, lo, hi, R)) != 0) goto done;
   FORCES();
-  if (thermo_out) orc_thermo(n, vx, vy, vz, ep, NULL, type, masses, thermo_out);
+  if (thermo_out) orc_thermo(n, vx, vy, vz, ep, vir, type, masses, thermo_out);
   for (int s = 1; s <= nsteps; ++s) {
     orc_push_f_v_r(n, x, y, z, vx, vy, vz, ax, ay, az, dt, 1.0);
     orc_push_f_v(n, vx, vy, vz, ax, ay, az, dt, 0.5);
@@ -719,7 +721,7 @@ int orc_run_nve(int64_t n, double* x, double* y, double* z, double* vx, double* 
       if ((rc = list_rebuild(&l, n, x, y, z, id, lo, hi, R)) != 0) goto done;
     FORCES();
     orc_push_f_v(n, vx, vy, vz, ax, ay, az, dt, 0.5);
-    if (thermo_out) orc_thermo(n, vx, vy, vz, ep, NULL, type, masses, thermo_out + 27 * s);
+    if (thermo_out) orc_thermo(n, vx, vy, vz, ep, vir, type, masses, thermo_out + 27 * s);
   }
 #undef FORCES
 done:
@@ -727,5 +729,6 @@ done:
   free(l.nbr);
   free(l.img);
   free(rho);
+  free(vir);
   return rc;
 }
