@@ -83,6 +83,7 @@ def lib(path: str = LIB_PATH):
             "gbmd_run_minimize": ([vp, i32, dbl, dbl, i32], i32),
             "gbmd_thermo": ([vp, vp], i32),
             "gbmd_device_state": ([vp] + [vp] * 11, i32),
+            "gbmd_thermo_reduce_noalloc": ([i64, vp, vp, vp, vp, vp, vp, vp, i32, vp, vp], i32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)

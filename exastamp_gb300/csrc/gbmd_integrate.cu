@@ -237,6 +237,23 @@ __global__ void k_thermo_final(const double* __restrict__ part, int nb, int64_t 
   }
 }
 
+// The same two reduction kernels on caller-provided device arrays, with a
+// caller-provided partial buffer of thermo_blocks(n) x 26 doubles.
+void launch_thermo_raw(int64_t n, const double* vx, const double* vy, const double* vz, const double* ep,
+                       const double* vir, const uint8_t* type, const double* mass, int ntypes, double* part,
+                       double* out, cudaStream_t s) {
+  ThermoArgs T;
+  T.n = n;
+  T.vx = vx; T.vy = vy; T.vz = vz;
+  T.ep = ep;
+  T.vir = vir;
+  T.type = type;
+  for (int t = 0; t < GBMD_MAX_TYPES; ++t) T.mass[t] = t < ntypes ? mass[t] : 1.0;
+  const int nb = thermo_blocks(n);
+  k_thermo_part<<<nb, TH_THREADS, 0, s>>>(T, part);
+  k_thermo_final<<<1, 27 * 32, 0, s>>>(part, nb, n, out);
+}
+
 void launch_thermo(gbmd_context* c, bool with_virial) {
   ThermoArgs T;
   T.n = c->n;

@@ -222,6 +222,9 @@ void launch_push_min(gbmd_context* c, double dt, double dt_scale, double tolF);
 void launch_first_half(gbmd_context* c, double dt);
 void launch_first_half_swap(gbmd_context* c, double dt);
 void launch_thermo(gbmd_context* c, bool with_virial);
+void launch_thermo_raw(int64_t n, const double* vx, const double* vy, const double* vz, const double* ep,
+                       const double* vir, const uint8_t* type, const double* mass, int ntypes, double* part,
+                       double* out, cudaStream_t s);
 int thermo_blocks(int64_t n);
 
 }  // namespace gbmd

@@ -189,6 +189,31 @@ int gbmd_run_minimize(gbmd_context* ctx, int nsteps, double dt, double tolF, int
  * particle count, reduced in FP64 on the device. */
 int gbmd_thermo(gbmd_context* ctx, double out[27]);
 
+/* The 27-double thermodynamic reduction of gbmd_thermo on the caller's own
+ * device arrays, without allocating anything.  No counterpart in the
+ * reference: it exists for callers that may not call cudaMalloc -- a plugin
+ * whose device memory must all come from its host framework's pool, code
+ * running while its stream is being captured into a CUDA graph, or a
+ * latency-critical loop that cannot afford the device-wide synchronisation
+ * an allocation can cause.
+ *   vx, vy, vz, ep (may be NULL), vir (n x 9, may be NULL), type: device
+ *   arrays of n atoms; type values must be < ntypes.  masses: HOST array of
+ *   ntypes doubles (ntypes <= 8).  out: DEVICE array of 27 doubles, same
+ *   layout as gbmd_thermo.  stream: cudaStream_t (NULL = default stream).
+ *   The work is enqueued on `stream`; nothing is synchronised.
+ * Scratch: a fixed array of 1184 x 26 doubles (246,272 bytes) inside the
+ * library's device image, present on every GPU that loads the library until
+ * the process exits; every partial it uses is overwritten before it is read,
+ * so no clearing is needed.  All calls on a device share that array: calls
+ * whose kernels overlap on the GPU (different streams, no ordering between
+ * them) race and give wrong sums.  The first call on a device looks the
+ * array's address up (cudaGetSymbolAddress) with that device current; make
+ * that first call before any stream capture.  n > 67,108,864 atoms returns
+ * GBMD_ERR_TOO_LARGE; bad pointers or ntypes return GBMD_ERR_INVALID. */
+int gbmd_thermo_reduce_noalloc(int64_t n, const double* vx, const double* vy, const double* vz,
+                               const double* ep, const double* vir, const uint8_t* type,
+                               const double* masses, int ntypes, double* out, void* stream);
+
 /* Per-kernel timing of one step's kernels with CUDA events on the context
  * stream, averaged over `reps` launches of each (the analogue of onika's
  * per-operator profiling timers, data/config/config_defaults.msp L21-23):
