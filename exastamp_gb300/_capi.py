@@ -271,3 +271,116 @@ class Context:
 
     def synchronize(self):
         self._chk(self._L.gbmd_synchronize(self.h))
+
+
+# --------------------------------------------------------------------------
+# batched replicas (gbmd_batch_*)
+# --------------------------------------------------------------------------
+_BATCH_SIG = {
+    "gbmd_batch_create": (["P(vp)", "i32", "vp"], "i32"),
+    "gbmd_batch_destroy": (["vp"], "i32"),
+    "gbmd_batch_last_error": (["vp"], "cp"),
+    "gbmd_batch_set_eam_alloy": (["vp", "i32", "dbl", "i32", "dbl", "vp", "vp", "vp", "dbl", "dbl", "dbl"], "i32"),
+    "gbmd_batch_set_param_derivatives": (["vp", "i32", "vp", "vp", "vp", "dbl", "dbl"], "i32"),
+    "gbmd_batch_upload": (["vp", "i32", "vp", "vp", "vp", "vp", "vp", "vp"], "i32"),
+    "gbmd_batch_set_targets": (["vp", "vp", "vp", "vp", "vp", "dbl", "dbl"], "i32"),
+    "gbmd_batch_set_launch": (["vp", "i32", "i32"], "i32"),
+    "gbmd_batch_run": (["vp", "i32", "i32", "i32"], "i32"),
+    "gbmd_batch_synchronize": (["vp"], "i32"),
+    "gbmd_batch_download": (["vp", "vp", "vp", "vp", "vp", "vp", "vp", "vp", "vp"], "i32"),
+}
+
+
+def _batch_lib():
+    L = lib()
+    if not getattr(L, "_batch_ready", False):
+        T = {"vp": C.c_void_p, "i32": C.c_int, "dbl": C.c_double, "cp": C.c_char_p,
+             "P(vp)": C.POINTER(C.c_void_p)}
+        for name, (args, res) in _BATCH_SIG.items():
+            fn = getattr(L, name)
+            fn.argtypes = [T[a] for a in args]
+            fn.restype = T[res]
+        L._batch_ready = True
+    return L
+
+
+class Batch:
+    """Many independent periodic eam_alloy replicas, one persistent launch."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        self._L = _batch_lib()
+        h = C.c_void_p()
+        rc = self._L.gbmd_batch_create(C.byref(h), device, stream)
+        if rc != OK:
+            raise GbmdError(rc, "gbmd_batch_create failed")
+        self.h = h
+        self.nrep = 0
+        self.n = 0
+
+    def _chk(self, rc):
+        if rc != OK:
+            raise GbmdError(rc, self._L.gbmd_batch_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.gbmd_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_eam_alloy(self, sf, rcut, conv_z2r=1.0, conv_frho=1.0):
+        frho, rhor, z2r = (np.ascontiguousarray(t[0], np.float64) for t in (sf.frho, sf.rhor, sf.z2r))
+        self._keep_tab = (frho, rhor, z2r)
+        self._chk(self._L.gbmd_batch_set_eam_alloy(self.h, sf.nrho, sf.drho, sf.nr, sf.dr, _p(frho), _p(rhor),
+                                                   _p(z2r), float(rcut), float(conv_z2r), float(conv_frho)))
+
+    def set_param_derivatives(self, J_F, J_f, J_z, conv_z2r=1.0, conv_frho=1.0):
+        J_F, J_f, J_z = (np.ascontiguousarray(a, np.float64) for a in (J_F, J_f, J_z))
+        self._chk(self._L.gbmd_batch_set_param_derivatives(self.h, J_F.shape[0], _p(J_F), _p(J_f), _p(J_z),
+                                                           float(conv_z2r), float(conv_frho)))
+
+    def upload(self, systems):
+        off = np.zeros(len(systems) + 1, np.int64)
+        off[1:] = np.cumsum([s.n for s in systems])
+        lo = np.ascontiguousarray(np.stack([s.lo for s in systems]), np.float64)
+        hi = np.ascontiguousarray(np.stack([s.hi for s in systems]), np.float64)
+        x, y, z = (np.ascontiguousarray(np.concatenate([getattr(s, k) for s in systems]), np.float64)
+                   for k in ("x", "y", "z"))
+        self._chk(self._L.gbmd_batch_upload(self.h, len(systems), _p(off), _p(lo), _p(hi), _p(x), _p(y), _p(z)))
+        self.nrep, self.n, self.offsets = len(systems), int(off[-1]), off
+
+    def set_targets(self, F, E, wF, wE):
+        F = np.ascontiguousarray(F, np.float64).reshape(-1, 3)
+        fx, fy, fz = (np.ascontiguousarray(F[:, k]) for k in range(3))
+        E = np.ascontiguousarray(E, np.float64)
+        self._chk(self._L.gbmd_batch_set_targets(self.h, _p(fx), _p(fy), _p(fz), _p(E), float(wF), float(wE)))
+
+    def set_launch(self, block, stencil):
+        self._chk(self._L.gbmd_batch_set_launch(self.h, int(block), int(stencil)))
+
+    def run(self, adjoint=False, per_replica=False, use_graph=False):
+        self._chk(self._L.gbmd_batch_run(self.h, 1 if adjoint else 0, 1 if per_replica else 0,
+                                         1 if use_graph else 0))
+
+    def synchronize(self):
+        self._chk(self._L.gbmd_batch_synchronize(self.h))
+
+    def download(self):
+        n, r = self.n, self.nrep
+        fx, fy, fz, ep = (np.empty(n) for _ in range(4))
+        e_rep, vir = np.empty(r), np.empty((r, 9))
+        loss, grad = C.c_double(), np.empty(9)
+        self._chk(self._L.gbmd_batch_download(self.h, _p(fx), _p(fy), _p(fz), _p(ep), _p(e_rep), _p(vir),
+                                              C.addressof(loss), _p(grad)))
+        return {"F": np.stack([fx, fy, fz], 1), "ep": ep, "e_rep": e_rep, "vir_rep": vir, "loss": loss.value,
+                "grad": grad}

@@ -166,7 +166,7 @@ static int do_rebuild(gbmd_context* c, bool check) {
 }
 
 // --- EAM spline build (eam_alloy.cpp L29-58, LAMMPS array2spline) ---------
-static void spline7(int n, double delta, const double* f /* 1..n */, double* s /* (n+1) x 8 */) {
+void spline7(int n, double delta, const double* f /* 1..n */, double* s /* (n+1) x 8 */) {
 #define S(m, k) s[(size_t)(m) * 8 + (k)]
   std::memset(s, 0, sizeof(double) * 8 * (size_t)(n + 1));
   for (int m = 1; m <= n; m++) S(m, 6) = f[m];
@@ -489,7 +489,7 @@ int gbmd_set_eam_alloy(gbmd_context* c, int nel, int nrho, double drho, int nr, 
     spline7(nr, dr, f.data(), &c->eam_host_z2r[q * kr * 8]);
   }
   const size_t nd = c->eam_host_frho.size() + c->eam_host_rhor.size() + c->eam_host_z2r.size();
-  const size_t nf = nel * kp + nel * kr + npairs * kr;
+  const size_t nf = nel * kp + nel * kr + npairs * kr + nel * kr;
   cudaFree(c->eam_d);
   cudaFree(c->eam_f);
   c->eam_d = nullptr;
@@ -514,6 +514,12 @@ int gbmd_set_eam_alloy(gbmd_context* c, int nel, int nrho, double drho, int nr, 
   put(c->eam_host_frho, nel, kp, conv_frho);
   put(c->eam_host_rhor, nel, kr, 1.0);
   put(c->eam_host_z2r, npairs, kr, conv_z2r);
+  // rho'(r) = ((3c3 p + 2c4) p + c5) / dr: the force pass reads it as two FMAs
+  for (int e = 0; e < nel; ++e)
+    for (size_t m = 0; m < kr; ++m) {
+      const double* s = &c->eam_host_rhor[(e * kr + m) * 8];
+      hf[o++] = make_float4((float)(3.0 * s[3] / dr), (float)(2.0 * s[4] / dr), (float)(s[5] / dr), 0.f);
+    }
   GBMD_CUDA(c, cudaMemcpy(c->eam_d, hd.data(), sizeof(double) * nd, cudaMemcpyHostToDevice));
   GBMD_CUDA(c, cudaMemcpy(c->eam_f, hf.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice));
   EamDev& E = c->eam;
@@ -534,6 +540,7 @@ int gbmd_set_eam_alloy(gbmd_context* c, int nel, int nrho, double drho, int nr, 
   E.frho4 = c->eam_f;
   E.rhor4 = c->eam_f + nel * kp;
   E.z2r4 = E.rhor4 + nel * kr;
+  E.rhod4 = E.z2r4 + npairs * kr;
   E.rdrf = (float)E.rdr;
   E.rdrhof = (float)E.rdrho;
   E.rhomaxf = (float)E.rhomax;

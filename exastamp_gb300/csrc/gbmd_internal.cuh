@@ -65,6 +65,7 @@ struct EamDev {
   const float4* frho4; // nel x (nrho+1)      F * conv_frho
   const float4* rhor4; // nel x (nr+1)
   const float4* z2r4;  // npairs x (nr+1)      z2r * conv_z2r
+  const float4* rhod4; // nel x (nr+1)         rho' coefficients (3c3, 2c4, c5) / dr
   float rdrf, rdrhof, rhomaxf, rc2f, rc2lo, rc2hi;
 };
 
@@ -195,6 +196,8 @@ struct gbmd_context {
 namespace gbmd {
 
 int set_error(gbmd_context* c, int code, const char* fmt, ...);
+// eam_alloy.cpp L29-58: knot values f[1..n] -> (n+1) x 8 spline coefficients
+void spline7(int n, double delta, const double* f, double* s);
 int check_cuda(gbmd_context* c, cudaError_t e, const char* what);
 int ensure_atom_capacity(gbmd_context* c, int64_t n);
 int sync_error_word(gbmd_context* c);  // copies device error word, returns status

@@ -20,21 +20,9 @@
 
 namespace gbmd {
 
-// {0,1,2} -> -1.f, 0.f, +1.f exactly (small integer through the 2^23 mantissa trick)
-__device__ __forceinline__ float unit_of(uint32_t b) { return __int_as_float(0x4B000000u | b) - 8388609.0f; }
-
 struct GeomF {
   float dx, dy, dz, d2;
 };
-
-__device__ __forceinline__ GeomF geom_f(uint32_t ent, const float4& pj, const float4& pi, const Grid& g) {
-  GeomF r;
-  r.dx = fmaf(unit_of((ent >> 26) & 3u), g.hf[0], pj.x - pi.x);
-  r.dy = fmaf(unit_of((ent >> 28) & 3u), g.hf[1], pj.y - pi.y);
-  r.dz = fmaf(unit_of(ent >> 30), g.hf[2], pj.z - pi.z);
-  r.d2 = fmaf(r.dx, r.dx, fmaf(r.dy, r.dy, r.dz * r.dz));
-  return r;
-}
 
 // Exact FP64 cutoff test of a pair whose FP32 d2 fell in the ambiguous band:
 // d2 <= rc2 and, for per-pair cutoffs, sqrt(d2) <= rc_pair (the reference's
@@ -49,6 +37,62 @@ __device__ __noinline__ bool exact_inside(const double4_32a* __restrict__ posd, 
   const double d2 = exact_d2(di.x, di.y, di.z, dj.x, dj.y, dj.z, Sx, Sy, Sz, a, b, c);
   if (!(d2 <= rc2)) return false;
   return rc_pair <= 0.0 || sqrt(d2) <= rc_pair;
+}
+
+// List-entry prefetch: each thread streams its own list slots through a
+// ring of LIST_RING words in shared memory with cp.async (4 B, L1-cached),
+// LIST_RING - 1 entries ahead of the one being processed.  The slot refilled
+// at iteration `it` is the one consumed at `it - 1`, whose value is already
+// in a register.  Ring layout [slot][thread]: conflict-free.
+constexpr int LIST_RING = 8;
+
+__device__ __forceinline__ void cp_async4(uint32_t* smem, const uint32_t* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_ring() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(LIST_RING - 2) : "memory");
+}
+__device__ __forceinline__ void cp_async_drain() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+static_assert((LIST_RING & (LIST_RING - 1)) == 0, "ring size must be a power of two");
+
+struct ListStream {
+  uint32_t* ring;          // this thread's column: ring[slot * blockDim.x]
+  const uint32_t* p;       // this thread's first list slot, then the next slot to prefetch
+  int64_t stride;
+  int niter;
+  __device__ __forceinline__ void start() {
+#pragma unroll
+    for (int d = 0; d < LIST_RING - 1; ++d) {
+      if (d < niter) cp_async4(ring + d * blockDim.x, p);
+      cp_async_commit();
+      p += stride;
+    }
+  }
+  __device__ __forceinline__ uint32_t next(int it) {
+    cp_async_wait_ring();
+    const unsigned u = (unsigned)it;
+    const uint32_t e = ring[(u & (LIST_RING - 1)) * blockDim.x];
+    if ((int)(u + LIST_RING - 1) < niter) cp_async4(ring + ((u - 1) & (LIST_RING - 1)) * blockDim.x, p);
+    cp_async_commit();
+    p += stride;
+    return e;
+  }
+};
+
+// {0,1,2} -> -1.f, 0.f, +1.f exactly (small integer through the 2^23 mantissa
+// trick); the separation shift is then one FMA per axis.
+__device__ __forceinline__ float unit_of(uint32_t b) { return __int_as_float(0x4B000000u | b) - 8388609.0f; }
+
+__device__ __forceinline__ GeomF geom_f(uint32_t ent, const float4& pj, const float4& pi, const Grid& g) {
+  GeomF r;
+  r.dx = fmaf(unit_of((ent >> 26) & 3u), g.hf[0], pj.x - pi.x);
+  r.dy = fmaf(unit_of((ent >> 28) & 3u), g.hf[1], pj.y - pi.y);
+  r.dz = fmaf(unit_of(ent >> 30), g.hf[2], pj.z - pi.z);
+  r.d2 = fmaf(r.dx, r.dx, fmaf(r.dy, r.dy, r.dz * r.dz));
+  return r;
 }
 
 __device__ __forceinline__ void reduce6(float* v, int T) {
@@ -97,12 +141,12 @@ __global__ void __launch_bounds__(256) k_lj_mixed(PairArgs A, LJF P, const LJPai
   const int ti = __float_as_int(pi.w);
   float fx = 0.f, fy = 0.f, fz = 0.f, cfx = 0.f, cfy = 0.f, cfz = 0.f, e = 0.f, ce = 0.f;
   float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  const uint32_t* p = A.nbr + (size_t)i * T + lane;
-  const int64_t stride = A.stride;
+  __shared__ uint32_t ring_sm[LIST_RING * 256];
+  ListStream ls{ring_sm + threadIdx.x, A.nbr + (size_t)i * T + lane, A.stride, nn > lane ? (nn - lane + T - 1) / T : 0};
+  ls.start();
 #pragma unroll 2
-  for (int k = lane; k < nn; k += T) {
-    const uint32_t ent = __ldg(p);
-    p += stride;
+  for (int it = 0; it < ls.niter; ++it) {
+    const uint32_t ent = ls.next(it);
     const uint32_t j = ent & GBMD_IDX_MASK;
     const float4 pj = __ldg(&A.posf[j]);
     const GeomF G = geom_f(ent, pj, pi, A.g);
@@ -139,6 +183,7 @@ __global__ void __launch_bounds__(256) k_lj_mixed(PairArgs A, LJF P, const LJPai
       v[5] = fmaf(h * G.dy, G.dz, v[5]);
     }
   }
+  cp_async_drain();
   group_reduce_kahan<T>(fx, cfx);
   group_reduce_kahan<T>(fy, cfy);
   group_reduce_kahan<T>(fz, cfz);
@@ -187,12 +232,12 @@ __global__ void __launch_bounds__(256) k_eam_rho_mixed(PairArgs A, EamDev E, flo
   const int nr = E.nr, nr1 = E.nr + 1;
   const float rdr = E.rdrf;
   float rho = 0.f, crho = 0.f;
-  const uint32_t* p = A.nbr + (size_t)i * T + lane;
-  const int64_t stride = A.stride;
+  __shared__ uint32_t ring_sm[LIST_RING * 256];
+  ListStream ls{ring_sm + threadIdx.x, A.nbr + (size_t)i * T + lane, A.stride, nn > lane ? (nn - lane + T - 1) / T : 0};
+  ls.start();
 #pragma unroll 2
-  for (int k = lane; k < nn; k += T) {
-    const uint32_t ent = __ldg(p);
-    p += stride;
+  for (int it = 0; it < ls.niter; ++it) {
+    const uint32_t ent = ls.next(it);
     const uint32_t j = ent & GBMD_IDX_MASK;
     const float4 pj = __ldg(&A.posf[j]);
     const GeomF G = geom_f(ent, pj, pi, A.g);
@@ -204,6 +249,7 @@ __global__ void __launch_bounds__(256) k_eam_rho_mixed(PairArgs A, EamDev E, flo
     const float4 c = __ldg(&E.rhor4[SINGLE ? m : __float_as_int(pj.w) * nr1 + m]);
     kahan_add(rho, crho, in ? spline_val(c, q) : 0.f);
   }
+  cp_async_drain();
   group_reduce_kahan<T>(rho, crho);
   if (live && lane == 0) {
     // Rho2EmbOp / eam_alloy_fEmbed: F'(rho) (and F(rho) on energy steps),
@@ -245,12 +291,16 @@ __global__ void __launch_bounds__(256) k_eam_force_mixed(PairArgs A, EamDev E, c
   const float rdr = E.rdrf;
   float fx = 0.f, fy = 0.f, fz = 0.f, cfx = 0.f, cfy = 0.f, cfz = 0.f, e = 0.f, ce = 0.f;
   float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  const uint32_t* p = A.nbr + (size_t)i * T + lane;
-  const int64_t stride = A.stride;
+  __shared__ uint32_t ring_sm[LIST_RING * 256];
+  ListStream ls{ring_sm + threadIdx.x, A.nbr + (size_t)i * T + lane, A.stride, nn > lane ? (nn - lane + T - 1) / T : 0};
+  ls.start();
+  // the force sums take two pair terms per compensated add: the pair of
+  // terms is rounded once (relative 6e-8 of the larger term), then the sum
+  // is compensated
+  float px = 0.f, py = 0.f, pz = 0.f;
 #pragma unroll 2
-  for (int k = lane; k < nn; k += T) {
-    const uint32_t ent = __ldg(p);
-    p += stride;
+  for (int it = 0; it < ls.niter; ++it) {
+    const uint32_t ent = ls.next(it);
     const uint32_t j = ent & GBMD_IDX_MASK;
     const float4 pj = __ldg(&A.posf[j]);
     const float fpj = __ldg(&fpf[j]);
@@ -262,19 +312,31 @@ __global__ void __launch_bounds__(256) k_eam_force_mixed(PairArgs A, EamDev E, c
     float q;
     const int m = knot_f(r, rdr, nr, q);
     const int tj = __float_as_int(pj.w);
-    const float4 cj = __ldg(&E.rhor4[SINGLE ? m : tj * nr1 + m]);
-    const float rhojp = spline_der(cj, q, rdr);
+    // rho'(r) from the pre-scaled derivative table: (3c3/dr, 2c4/dr, c5/dr)
+    const float4 dj = __ldg(&E.rhod4[SINGLE ? m : tj * nr1 + m]);
+    const float rhojp = fmaf(fmaf(dj.x, q, dj.y), q, dj.z);
     float rhoip = rhojp;
-    if (!SINGLE && ti != tj) rhoip = spline_der(__ldg(&E.rhor4[ti * nr1 + m]), q, rdr);
+    if (!SINGLE && ti != tj) {
+      const float4 di = __ldg(&E.rhod4[ti * nr1 + m]);
+      rhoip = fmaf(fmaf(di.x, q, di.y), q, di.z);
+    }
     const float4 cz = __ldg(&E.z2r4[SINGLE ? m : z2r_index_d(ti, tj) * nr1 + m]);
-    const float z2p = spline_der(cz, q, rdr);
-    const float phi = spline_val(cz, q) * rs;       // z2r tables carry conv_z2r
-    const float phip = (z2p - phi) * rs;
+    const float t1 = fmaf(cz.x, q, cz.y);
+    const float z2 = fmaf(fmaf(t1, q, cz.z), q, cz.w);          // z2r tables carry conv_z2r
+    const float z2d = fmaf(fmaf(cz.x, q, t1 + t1), q, cz.z);     // d z2 / d q
+    const float phi = z2 * rs;
+    const float phip = fmaf(z2d * rdr, rs, -phi * rs);
     const float psip = fmaf(fpi, rhojp, fmaf(fpj, rhoip, phip));
     const float fpair = in ? psip * rs : 0.f;
-    kahan_add(fx, cfx, G.dx * fpair);
-    kahan_add(fy, cfy, G.dy * fpair);
-    kahan_add(fz, cfz, G.dz * fpair);
+    if (it & 1) {
+      kahan_add(fx, cfx, fmaf(G.dx, fpair, px));
+      kahan_add(fy, cfy, fmaf(G.dy, fpair, py));
+      kahan_add(fz, cfz, fmaf(G.dz, fpair, pz));
+    } else {
+      px = G.dx * fpair;
+      py = G.dy * fpair;
+      pz = G.dz * fpair;
+    }
     if (EV) {
       kahan_add(e, ce, in ? 0.5f * phi : 0.f);
       const float h = -0.5f * fpair;
@@ -286,6 +348,12 @@ __global__ void __launch_bounds__(256) k_eam_force_mixed(PairArgs A, EamDev E, c
       v[5] = fmaf(h * G.dy, G.dz, v[5]);
     }
   }
+  if (ls.niter & 1) {  // a last unpaired term
+    kahan_add(fx, cfx, px);
+    kahan_add(fy, cfy, py);
+    kahan_add(fz, cfz, pz);
+  }
+  cp_async_drain();
   group_reduce_kahan<T>(fx, cfx);
   group_reduce_kahan<T>(fy, cfy);
   group_reduce_kahan<T>(fz, cfz);

@@ -252,6 +252,22 @@ __global__ void k_posf(int64_t n, const double* __restrict__ x, const double* __
   pd[i] = make_double4_32a(xi, yi, zi, (double)t);
 }
 
+// FP64 re-test of a candidate whose FP32 d2 fell within 2^-12 of R^2.  Out of
+// line so the compiler cannot predicate it into every iteration of the
+// candidate loop (it runs for ~1e-4 of the candidates).
+__device__ __noinline__ bool exact_within(const double* __restrict__ x, const double* __restrict__ y,
+                                          const double* __restrict__ z, int64_t i, int64_t k, uint32_t code,
+                                          int cx, int cy, int cz, const Grid g, double R2) {
+  const int nxi = image_of(cx, int(code & 3u) - 1, g.nc[0]);
+  const int nyi = image_of(cy, int((code >> 2) & 3u) - 1, g.nc[1]);
+  const int nzi = image_of(cz, int((code >> 4) & 3u) - 1, g.nc[2]);
+  double a, b, c;
+  return exact_d2(x[i], y[i], z[i], x[k], y[k], z[k], (double)nxi * g.L[0], (double)nyi * g.L[1],
+                  (double)nzi * g.L[2], a, b, c) <= R2;
+}
+
+constexpr int BUILD_HB = 16;  // home atoms staged per batch
+
 // One warp per home cell.  Lane s < 27 describes stencil cell s (start,
 // count, code, FP32 shift); the 27 candidate ranges are concatenated in
 // stencil order and walked 32 candidates at a time, one per lane, so each
@@ -296,14 +312,14 @@ __global__ void __launch_bounds__(128) k_build_list_cells(
   const int total = __shfl_sync(FULL, incl, 26);
   const int hb = cstart[cell], nh = cstart[cell + 1] - hb;
   const uint32_t CENTER = 1u | (1u << 2) | (1u << 4);
-  // per-warp shared memory: 32 home positions, 32 counts, 32 x maxnb entries
+  // per-warp shared memory: BUILD_HB home positions, 32 counts, BUILD_HB x maxnb entries
   extern __shared__ float4 smem_build[];
-  float4* hpos = smem_build + (size_t)(threadIdx.x >> 5) * (40 + 8 * (size_t)maxnb);
-  int* cnt_s = reinterpret_cast<int*>(hpos + 32);
-  uint32_t* tile = reinterpret_cast<uint32_t*>(hpos + 40);
+  float4* hpos = smem_build + (size_t)(threadIdx.x >> 5) * (BUILD_HB + 8 + BUILD_HB / 4 * (size_t)maxnb);
+  int* cnt_s = reinterpret_cast<int*>(hpos + BUILD_HB);
+  uint32_t* tile = reinterpret_cast<uint32_t*>(hpos + BUILD_HB + 8);
   int warp_max = 0;
-  for (int hbatch = 0; hbatch < nh; hbatch += 32) {
-    const int nhb = min(32, nh - hbatch);
+  for (int hbatch = 0; hbatch < nh; hbatch += BUILD_HB) {
+    const int nhb = min(BUILD_HB, nh - hbatch);
     const bool hv = lane < nhb;
     const int64_t ih = hb + hbatch + lane;
     if (hv) hpos[lane] = pf[ih];
@@ -330,6 +346,7 @@ __global__ void __launch_bounds__(128) k_build_list_cells(
       // iterations below, so they pipeline
       const int mybase = cnt;
       unsigned mymask = 0u;
+#pragma unroll 4
       for (int hh = 0; hh < nhb; ++hh) {
         const int64_t i = hb + hbatch + hh;
         const float4 pi = hpos[hh];
@@ -337,14 +354,11 @@ __global__ void __launch_bounds__(128) k_build_list_cells(
         const float dy = jy - pi.y;
         const float dz = jz - pi.z;
         const float d2f = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        bool in = valid && !(k == i && code == CENTER) && d2f <= R2hi;
-        if (in && d2f >= R2lo) {
-          const int nxi = image_of(cx, int(code & 3u) - 1, g.nc[0]);
-          const int nyi = image_of(cy, int((code >> 2) & 3u) - 1, g.nc[1]);
-          const int nzi = image_of(cz, int((code >> 4) & 3u) - 1, g.nc[2]);
-          double a, b, cc;
-          in = exact_d2(x[i], y[i], z[i], x[k], y[k], z[k], (double)nxi * g.L[0], (double)nyi * g.L[1],
-                        (double)nzi * g.L[2], a, b, cc) <= R2;
+        const bool keep = (valid && !(k == i && code == CENTER));
+        bool in = keep && d2f < R2lo;
+        const bool band = keep && d2f >= R2lo && d2f <= R2hi;
+        if (__any_sync(FULL, band)) {  // rare: some lane needs the FP64 re-test
+          if (band) in = exact_within(x, y, z, i, k, code, cx, cy, cz, g, R2);
         }
         const unsigned mask = __ballot_sync(FULL, in);
         const int base = __shfl_sync(FULL, mybase, hh);
@@ -406,8 +420,8 @@ static int build_list(gbmd_context* c) {
   }
   c->npad = npad;
   GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_MAXNB, 0, sizeof(int), c->stream));
-  // shared memory per warp: 32 home positions + 32 counts + 32 x maxnb entries
-  const size_t per_warp = 640 + 128 * (size_t)c->maxnb;
+  // shared memory per warp: BUILD_HB home positions + 32 counts + BUILD_HB x maxnb entries
+  const size_t per_warp = 16 * (BUILD_HB + 8) + 4 * BUILD_HB * (size_t)c->maxnb;
   int W = (int)((96 * 1024) / per_warp);
   W = W < 1 ? 1 : (W > 4 ? 4 : W);
   const size_t smem = per_warp * W;

@@ -214,6 +214,44 @@ int gbmd_thermo_reduce_noalloc(int64_t n, const double* vx, const double* vy, co
                                const double* ep, const double* vir, const uint8_t* type,
                                const double* masses, int ntypes, double* out, void* stream);
 
+/* ---- batched replicas ------------------------------------------------------
+ * Many independent periodic single-element eam_alloy systems (<= 2048 atoms
+ * each, every box edge >= rcut) evaluated in one persistent launch: forward
+ * (per-atom forces and energies, per-replica energy and virial) and,
+ * optionally, the gradient of L = wF sum |F - F*|^2 + wE sum (E - E*)^2 with
+ * respect to up to 9 potential parameters.  Forces are in table units x
+ * conv (eV/A with conv = 1), not accelerations.  No reference counterpart
+ * for the batching itself: each replica is the eam_alloy_force operator
+ * (eam_potential_multimat.cu L113-257) on its own periodic domain. */
+typedef struct gbmd_batch gbmd_batch;
+int gbmd_batch_create(gbmd_batch** b, int device, void* stream);
+int gbmd_batch_destroy(gbmd_batch* b);
+const char* gbmd_batch_last_error(const gbmd_batch* b);
+/* single-element setfl tables (F nrho, rho nr, z2r nr knots), as gbmd_set_eam_alloy */
+int gbmd_batch_set_eam_alloy(gbmd_batch* b, int nrho, double drho, int nr, double dr, const double* frho,
+                             const double* rhor, const double* z2r, double rcut, double conv_z2r,
+                             double conv_frho);
+/* d(knot values)/d(parameter): nparam x nrho, nparam x nr, nparam x nr; the
+ * library splines them (the spline map is linear in the knot values). */
+int gbmd_batch_set_param_derivatives(gbmd_batch* b, int nparam, const double* dfrho, const double* drhor,
+                                     const double* dz2r, double conv_z2r, double conv_frho);
+/* offsets: nrep+1 atom offsets; lo, hi: nrep x 3 boxes; x, y, z: all atoms */
+int gbmd_batch_upload(gbmd_batch* b, int nrep, const int64_t* offsets, const double* lo, const double* hi,
+                      const double* x, const double* y, const double* z);
+int gbmd_batch_set_targets(gbmd_batch* b, const double* fx, const double* fy, const double* fz, const double* e,
+                           double wF, double wE);
+/* launch shape (the autotuner's knobs): threads per block (64-512) and the
+ * cell stencil radius (1: cells >= rcut, 2: cells >= rcut/2) */
+int gbmd_batch_set_launch(gbmd_batch* b, int block, int stencil);
+/* per_replica != 0: one launch per replica (the comparison mode);
+ * use_graph != 0: the persistent launch is captured once and replayed */
+int gbmd_batch_run(gbmd_batch* b, int adjoint, int per_replica, int use_graph);
+int gbmd_batch_synchronize(gbmd_batch* b);
+/* any pointer may be NULL; rep_virial is nrep x 9; loss / grad[9] summed
+ * over replicas in replica order */
+int gbmd_batch_download(gbmd_batch* b, double* fx, double* fy, double* fz, double* ep, double* rep_energy,
+                        double* rep_virial, double* loss, double* grad);
+
 /* Per-kernel timing of one step's kernels with CUDA events on the context
  * stream, averaged over `reps` launches of each (the analogue of onika's
  * per-operator profiling timers, data/config/config_defaults.msp L21-23):

@@ -644,6 +644,176 @@ void orc_thermo(int64_t n, const double* vx, const double* vy, const double* vz,
 }
 
 /* ------------------------------------------------------------------------ */
+/* Parameter adjoint of the force-matching + energy loss (single element)    */
+/* ------------------------------------------------------------------------ */
+
+static inline double sp_val(const double* c, double p) { return ((c[3] * p + c[4]) * p + c[5]) * p + c[6]; }
+static inline double sp_der(const double* c, double p) { return (c[0] * p + c[1]) * p + c[2]; }
+
+static inline void rho_knot(const orc_eam_tables* t, double rho, int* m, double* p) {
+  double pp = rho * t->rdrho + 1.0;
+  int mm = (int)pp;
+  if (mm > t->nrho - 1) mm = t->nrho - 1;
+  if (mm < 1) mm = 1;
+  pp -= mm;
+  if (pp > 1.0) pp = 1.0;
+  *m = mm;
+  *p = pp;
+}
+
+/* Forward in the reference's formulas (eam_alloy.h L198-313 with conv = 1),
+ * then the reverse sweep:
+ *   s_ij = gF_i . u_ij                     (dL/dpsi'_ij, psi' = F'_i rho'_ij + F'_j rho'_ij + phi'_ij)
+ *   G_i  = sum_j (s_ij + s_ji) rho'_ij     (dL/dF'_i through the forces)
+ *   lam_i = gE_i F'_i + G_i F''_i          (dL/drho_i)
+ * and every spline evaluation is differentiated with respect to the
+ * parameters by evaluating the same formula on the derivative splines. */
+double orc_eam_loss_grad(int64_t n, const double* x, const double* y, const double* z, const int64_t* off,
+                         const int32_t* nbr, const int8_t* img, const double L[3], const orc_eam_tables* t,
+                         double rcut, const orc_eam_dtables* d, const double* Ft, const double* Et, double wF,
+                         double wE, double* grad, double* F, double* E) {
+  const double rc2 = rcut * rcut;
+  const int np = d->nparam;
+  const size_t kr = (size_t)t->nr + 1, kp = (size_t)t->nrho + 1;
+  double* rho = (double*)calloc((size_t)n + 1, sizeof(double));
+  double* fp = (double*)calloc((size_t)n + 1, sizeof(double));
+  double* fpp = (double*)calloc((size_t)n + 1, sizeof(double));
+  double* f = (double*)calloc(3 * (size_t)n + 1, sizeof(double));
+  double* e = (double*)calloc((size_t)n + 1, sizeof(double));
+  double* gF = (double*)calloc(3 * (size_t)n + 1, sizeof(double));
+  double* gE = (double*)calloc((size_t)n + 1, sizeof(double));
+  double* G = (double*)calloc((size_t)n + 1, sizeof(double));
+  double* gacc = (double*)calloc((size_t)np + 1, sizeof(double));
+#define PAIR_BEGIN                                                               \
+  for (int64_t k = off[i]; k < off[i + 1]; ++k) {                                \
+    const int nn[3] = {img[3 * k], img[3 * k + 1], img[3 * k + 2]};              \
+    double dx, dy, dz;                                                           \
+    const int64_t j = nbr[k];                                                    \
+    const double d2 = pair_d2(x, y, z, i, j, nn, L, &dx, &dy, &dz);              \
+    if (!(d2 <= rc2)) continue;                                                  \
+    const double r = sqrt(d2);                                                   \
+    int m;                                                                       \
+    double p;                                                                    \
+    r_knot(t, r, &m, &p);
+#define PAIR_END }
+  /* forward: density, embedding */
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t i = 0; i < n; ++i) {
+    double acc = 0.0;
+    PAIR_BEGIN
+    acc += sp_val(t->rhor + (size_t)m * 8, p);
+    PAIR_END
+    rho[i] = acc;
+    int mq;
+    double q;
+    rho_knot(t, acc, &mq, &q);
+    const double* c = t->frho + (size_t)mq * 8;
+    double fv = sp_der(c, q), ev = sp_val(c, q);
+    double f2 = (2.0 * c[0] * q + c[1]) * t->rdrho;
+    if (acc > t->rhomax) {
+      ev += fv * (acc - t->rhomax);
+      f2 = 0.0;
+    }
+    fp[i] = fv;
+    fpp[i] = f2;
+    e[i] = ev;
+  }
+  /* forward: forces and pair energies */
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t i = 0; i < n; ++i) {
+    double sx = 0., sy = 0., sz = 0., se = 0.;
+    PAIR_BEGIN
+    const double* cr = t->rhor + (size_t)m * 8;
+    const double* cz = t->z2r + (size_t)m * 8;
+    const double rhop = sp_der(cr, p);
+    const double z2p = sp_der(cz, p), z2 = sp_val(cz, p);
+    const double phi = z2 / r;
+    const double phip = z2p / r - phi / r;
+    const double psip = (fp[i] + fp[j]) * rhop + phip;
+    sx += dx * psip / r;
+    sy += dy * psip / r;
+    sz += dz * psip / r;
+    se += 0.5 * phi;
+    PAIR_END
+    f[3 * i] = sx;
+    f[3 * i + 1] = sy;
+    f[3 * i + 2] = sz;
+    e[i] += se;
+  }
+  /* loss and its gradient with respect to the per-atom outputs */
+  double loss = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    for (int a = 0; a < 3; ++a) {
+      const double df = f[3 * i + a] - Ft[3 * i + a];
+      loss += wF * df * df;
+      gF[3 * i + a] = 2.0 * wF * df;
+    }
+    const double de = e[i] - Et[i];
+    loss += wE * de * de;
+    gE[i] = 2.0 * wE * de;
+  }
+  /* reverse sweep 1: pair terms through phi, phi' and rho'; G_i */
+#pragma omp parallel
+  {
+    double* gl = (double*)calloc((size_t)np + 1, sizeof(double));
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t i = 0; i < n; ++i) {
+      double gi = 0.0;
+      PAIR_BEGIN
+      const double ux = dx / r, uy = dy / r, uz = dz / r;
+      const double sij = gF[3 * i] * ux + gF[3 * i + 1] * uy + gF[3 * i + 2] * uz;
+      const double sji = -(gF[3 * j] * ux + gF[3 * j + 1] * uy + gF[3 * j + 2] * uz);
+      const double rhop = sp_der(t->rhor + (size_t)m * 8, p);
+      gi += (sij + sji) * rhop;
+      const double wv = 0.5 * gE[i] / r - sij / (r * r); /* weight of dz2 */
+      const double wd = sij / r;                         /* weight of dz2' */
+      const double wr = sij * (fp[i] + fp[j]);            /* weight of drho' */
+      for (int q = 0; q < np; ++q) {
+        const double* dz2 = d->dz2r + ((size_t)q * kr + m) * 8;
+        const double* drh = d->drhor + ((size_t)q * kr + m) * 8;
+        gl[q] += wv * sp_val(dz2, p) + wd * sp_der(dz2, p) + wr * sp_der(drh, p);
+      }
+      PAIR_END
+      G[i] = gi;
+    }
+#pragma omp critical
+    for (int q = 0; q < np; ++q) gacc[q] += gl[q];
+    free(gl);
+  }
+  /* reverse sweep 2: embedding terms and rho values through lam_i */
+#pragma omp parallel
+  {
+    double* gl = (double*)calloc((size_t)np + 1, sizeof(double));
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t i = 0; i < n; ++i) {
+      const double lam = gE[i] * fp[i] + G[i] * fpp[i];
+      int mq;
+      double q;
+      rho_knot(t, rho[i], &mq, &q);
+      const double over = rho[i] > t->rhomax ? rho[i] - t->rhomax : 0.0;
+      for (int a = 0; a < np; ++a) {
+        const double* c = d->dfrho + ((size_t)a * kp + mq) * 8;
+        const double dfp = sp_der(c, q);
+        gl[a] += gE[i] * (sp_val(c, q) + dfp * over) + G[i] * dfp;
+      }
+      PAIR_BEGIN
+      for (int a = 0; a < np; ++a) gl[a] += lam * sp_val(d->drhor + ((size_t)a * kr + m) * 8, p);
+      PAIR_END
+    }
+#pragma omp critical
+    for (int a = 0; a < np; ++a) gacc[a] += gl[a];
+    free(gl);
+  }
+#undef PAIR_BEGIN
+#undef PAIR_END
+  for (int q = 0; q < np; ++q) grad[q] += gacc[q];
+  if (F) memcpy(F, f, sizeof(double) * 3 * (size_t)n);
+  if (E) memcpy(E, e, sizeof(double) * (size_t)n);
+  free(rho); free(fp); free(fpp); free(f); free(e); free(gF); free(gE); free(G); free(gacc);
+  return loss;
+}
+
+/* ------------------------------------------------------------------------ */
 /* verlet_nve driver (config_numerical_schemes.msp L23-52)                   */
 /* ------------------------------------------------------------------------ */
 

@@ -109,6 +109,25 @@ void orc_force_to_accel(int64_t n, double* fx, double* fy, double* fz, const uin
 void orc_thermo(int64_t n, const double* vx, const double* vy, const double* vz, const double* ep,
                 const double* vir, const uint8_t* type, const double* masses, double out[27]);
 
+/* Parameter adjoint of the force-matching + energy loss for one single-element
+ * configuration, in eV units (tables with conv = 1):
+ *   L = wF * sum_i |F_i - F*_i|^2 + wE * sum_i (E_i - E*_i)^2
+ * d-tables: for each parameter, the 7-coefficient spline of the derivative of
+ * the tabulated knot values (the spline map is linear in the knot values).
+ * Returns L; adds dL/dtheta into grad[nparam]; writes F (3n, xyz
+ * interleaved) and E (n) when given. */
+typedef struct {
+  int nparam, pad_;
+  const double* dfrho; /* nparam x (nrho+1) x 8 */
+  const double* drhor; /* nparam x (nr+1) x 8 */
+  const double* dz2r;  /* nparam x (nr+1) x 8 */
+} orc_eam_dtables;
+
+double orc_eam_loss_grad(int64_t n, const double* x, const double* y, const double* z, const int64_t* off,
+                         const int32_t* nbr, const int8_t* img, const double L[3], const orc_eam_tables* t,
+                         double rcut, const orc_eam_dtables* d, const double* Ft, const double* Et, double wF,
+                         double wE, double* grad, double* F, double* E);
+
 int orc_run_nve(int64_t n, double* x, double* y, double* z, double* vx, double* vy, double* vz,
                 double* ax, double* ay, double* az, double* ep, const uint8_t* type, const uint64_t* id,
                 const double* masses, const double lo[3], const double hi[3], int pot_kind,

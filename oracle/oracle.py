@@ -100,6 +100,8 @@ def lib():
         L.orc_run_nve.restype = i32
         L.orc_run_nve.argtypes = [i64] + [vp] * 15 + [i32, vp, dbl, dbl, i32, i32, vp]
         L.orc_num_threads.restype = i32
+        L.orc_eam_loss_grad.restype = dbl
+        L.orc_eam_loss_grad.argtypes = [i64, vp, vp, vp, vp, vp, vp, vp, vp, dbl, vp, vp, vp, dbl, dbl, vp, vp, vp]
     return _lib
 
 
@@ -353,3 +355,40 @@ def multi_params(eps, sig, rc, rcut_max):
 
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv))
+
+
+# --------------------------------------------------------------------------
+# parameter adjoint (single-element analytic EAM, eV units)
+# --------------------------------------------------------------------------
+class EamDTables(C.Structure):
+    _fields_ = [("nparam", C.c_int), ("pad_", C.c_int), ("dfrho", C.c_void_p), ("drhor", C.c_void_p),
+                ("dz2r", C.c_void_p)]
+
+
+class EamDerivativeSplines:
+    """Splines of d(knot values)/d(parameter) for every analytic parameter;
+    the spline map is linear, so these are d(spline coefficients)/d(param)."""
+
+    def __init__(self, cfg, params=None):
+        from exastamp_gb300 import setfl as SF
+        J_F, J_f, J_z = SF.table_param_jacobian(cfg, params)
+        _, _, dr, drho = SF.table_grids(cfg)
+        pad = lambda row: np.concatenate([[0.0], row])  # noqa: E731
+        self.dfrho = np.ascontiguousarray(np.stack([eam_spline(pad(r), drho) for r in J_F]))
+        self.drhor = np.ascontiguousarray(np.stack([eam_spline(pad(r), dr) for r in J_f]))
+        self.dz2r = np.ascontiguousarray(np.stack([eam_spline(pad(r), dr) for r in J_z]))
+        self.s = EamDTables(J_F.shape[0], 0, _p(self.dfrho), _p(self.drhor), _p(self.dz2r))
+
+
+def eam_loss_grad(x, y, z, nl, L, tab, rcut, dsp, Ft, Et, wF, wE):
+    """(loss, grad[9], F (n,3), E (n)) for one configuration."""
+    n = len(x)
+    grad = np.zeros(dsp.s.nparam)
+    F = np.zeros((n, 3))
+    E = np.zeros(n)
+    Ft = np.ascontiguousarray(Ft, np.float64).reshape(n, 3)
+    Et = np.ascontiguousarray(Et, np.float64)
+    loss = lib().orc_eam_loss_grad(n, _p(x), _p(y), _p(z), _p(nl.off), _p(nl.nbr), _p(nl.img), _p(_f64(L)),
+                                   tab.tp, float(rcut), C.addressof(dsp.s), _p(Ft), _p(Et), float(wF), float(wE),
+                                   _p(grad), _p(F), _p(E))
+    return float(loss), grad, F, E
