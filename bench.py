@@ -43,6 +43,12 @@ import time
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
+# minimiser that precedes the mixture's NVE run (reduced units): step 0.02
+# and acceleration clip 100, so an atom moves at most 100*0.02^2/2 = 0.02
+# sigma per component per step (the NVE step 0.002 would move overlapping
+# atoms only 2e-4 sigma per step and leave forces that blow the NVE run up)
+MIN_TOLF = 100.0
+MIN_DT = 0.02
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
@@ -52,6 +58,10 @@ WORKLOADS = {
     "lj_fcc_32k": dict(kind="lj", ncell=20, T=1.0, seed=1, rcut=2.5, skin=0.3, dt=0.005,
                        desc="LJ FCC 20^3 cells (32,000 atoms), rho*=0.8442, rc 2.5, skin 0.3, T*=1, "
                             "dt 0.005, NVE, rebuild every 10"),
+    "lj_binary_16m": dict(kind="lj_multi", n=16_777_216, seed=3, rcut=2.5, skin=0.3, dt=0.002, min_steps=200,
+                          desc="LJ A:B 80:20 binary mixture, 16,777,216 atoms, rho 1.2, 64 voids of radius 8 sigma, "
+                               "per-pair cutoff 2.5 sigma_ab, skin 0.3, 200 clipped minimiser steps (step 0.02, "
+                               "clip 100) then NVE dt 0.002, rebuild every 10"),
 }
 
 
@@ -63,19 +73,22 @@ def parse():
     p.add_argument("--impl", default="gbmd", choices=["gbmd", "reference"])
     p.add_argument("--workload", default="eam_cu_4m", choices=sorted(WORKLOADS))
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    p.add_argument("--rebuild-every", type=int, default=10)
+    p.add_argument("--rebuild-every", type=int, default=10,
+                   help="list rebuild interval in steps; -1 rebuilds on the skin/2 displacement trigger")
     p.add_argument("--e2e-steps", type=int, default=20)
     p.add_argument("--fp64-steps", type=int, default=40)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--no-batch", action="store_true", help="skip the batched-replica and adjoint sections")
     p.add_argument("--lanes", type=int, default=0, help="lanes per atom (0: autotune)")
     p.add_argument("--block", type=int, default=0)
     p.add_argument("--ncell", type=int, default=0,
                    help="override the unit cells per edge (small profiling cases of the same workload)")
     a = p.parse_args()
     if a.ncell:
-        WORKLOADS[a.workload] = dict(WORKLOADS[a.workload], ncell=a.ncell)
+        extra = {"n": 4 * a.ncell ** 3} if WORKLOADS[a.workload]["kind"] == "lj_multi" else {}
+        WORKLOADS[a.workload] = dict(WORKLOADS[a.workload], ncell=a.ncell, **extra)
     return a
 
 
@@ -84,6 +97,8 @@ def make_system(w):
     from exastamp_gb300 import systems as S
     if w["kind"] == "eam":
         return S.eam_cu_fcc(ncell=w["ncell"], a=w["a"], T=w["T"], seed=w["seed"])
+    if w["kind"] == "lj_multi":
+        return S.lj_binary_voids(n=w["n"], seed=w["seed"], nvoids=max(1, round(64 * w["n"] / 16_777_216)))
     return S.lj_fcc(ncell=w["ncell"], T=w["T"], seed=w["seed"])
 
 
@@ -92,6 +107,9 @@ def bind_potential(ctx, w):
     if w["kind"] == "eam":
         sf = setfl.tabulate(setfl.load_cu_params())
         ctx.set_eam_alloy(sf, w["rcut"], S.EV, S.EV)
+    elif w["kind"] == "lj_multi":
+        eps, sig, rc = S.kob_andersen_tables()
+        ctx.set_lj_multi(eps, sig, rc, 0.0)
     else:
         ctx.set_lj(1.0, 1.0, w["rcut"])
     ctx.set_skin(w["skin"])
@@ -185,28 +203,46 @@ def barrier(ws):
 
 
 # ---------------------------------------------------------------------------
-def cpu_oracle_rate(w, target_s=12.0, ncell=None):
-    """FP64 OpenMP oracle NVE throughput on a sample of the workload."""
+def oracle_sample(w, O, nc):
+    """A CPU-sized sample of workload `w` (nc FCC cells per edge, or 4 nc^3
+    atoms for the mixture, which is first put through the same clipped
+    minimiser as the GPU run) with the oracle's potential parameters."""
+    from exastamp_gb300 import setfl, systems as S
+    if w["kind"] == "eam":
+        tab = O.EamOracleTables.from_setfl(setfl.tabulate(setfl.load_cu_params()), S.EV, S.EV, rcut=w["rcut"])
+        s = S.eam_cu_fcc(ncell=nc, a=w["a"], T=w["T"], seed=w["seed"])
+        return s, s.state(), O.POT_EAM, tab
+    if w["kind"] == "lj_multi":
+        eps, sig, rc = S.kob_andersen_tables()
+        pot = O.multi_params(eps, sig, rc, float(rc.max()))
+        n = 4 * nc ** 3
+        s = S.lj_binary_voids(n=n, seed=w["seed"], nvoids=max(1, round(64 * n / w["n"])))
+        st = s.state()
+        O.run_minimize(st, s.masses, s.lo, s.hi, O.POT_LJ_MULTI, pot, w["skin"], MIN_DT, MIN_TOLF,
+                       w["min_steps"], 10)
+        return s, st, O.POT_LJ_MULTI, pot
+    s = S.lj_fcc(ncell=nc, T=w["T"], seed=w["seed"])
+    return s, s.state(), O.POT_LJ, O.LJParams(1.0, 1.0, w["rcut"])
+
+
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    from exastamp_gb300 import setfl, systems as S
     O.build()
-    if w["kind"] == "eam":
-        cfg = setfl.load_cu_params()
-        tab = O.EamOracleTables.from_setfl(setfl.tabulate(cfg), S.EV, S.EV, rcut=w["rcut"])
-        pot_kind, pot = O.POT_EAM, tab
-        mk = lambda nc: S.eam_cu_fcc(ncell=nc, a=w["a"], T=w["T"], seed=w["seed"])  # noqa: E731
-    else:
-        pot_kind, pot = O.POT_LJ, O.LJParams(1.0, 1.0, w["rcut"])
-        mk = lambda nc: S.lj_fcc(ncell=nc, T=w["T"], seed=w["seed"])  # noqa: E731
-    nc = ncell or min(w["ncell"], 24 if w["kind"] == "eam" else 20)
-    s = mk(nc)
-    st = s.state()
+    return O
+
+
+def cpu_oracle_rate(w, target_s=12.0, ncell=None):
+    """FP64 OpenMP oracle NVE throughput on a sample of the workload."""
+    O = _oracle()
+    nc = ncell or min(w.get("ncell", 20), 24 if w["kind"] == "eam" else 20)
+    s, st0, pot_kind, pot = oracle_sample(w, O, nc)
+    st = {k: v.copy() for k, v in st0.items()}
     t0 = time.perf_counter()
     O.run_nve(st, s.masses, s.lo, s.hi, pot_kind, pot, w["skin"], w["dt"], 2, 10, thermo=False)
     t_cal = (time.perf_counter() - t0) / 3.0
     steps = int(max(3, min(200, target_s / max(t_cal, 1e-6))))
-    st = s.state()
+    st = {k: v.copy() for k, v in st0.items()}
     t0 = time.perf_counter()
     O.run_nve(st, s.masses, s.lo, s.hi, pot_kind, pot, w["skin"], w["dt"], steps, 10, thermo=False)
     dt = time.perf_counter() - t0
@@ -220,23 +256,14 @@ def run_reference(args, w, ws, rank):
     each step one NVE step of a sample sized so W+K steps fit in minutes."""
     if rank != 0:
         return
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
+    O = _oracle()
     # size the sample: ~150 s for warmup + steps at the calibrated rate
     rate, _ = cpu_oracle_rate(w, target_s=3.0, ncell=8 if w["kind"] == "eam" else 10)
     budget = 150.0
     atoms = rate * budget / max(1, args.steps + args.warmup)
     per = 4
-    nc = int(max(4, min(w["ncell"], round((atoms / per) ** (1.0 / 3.0)))))
-    from exastamp_gb300 import setfl, systems as S
-    if w["kind"] == "eam":
-        tab = O.EamOracleTables.from_setfl(setfl.tabulate(setfl.load_cu_params()), S.EV, S.EV, rcut=w["rcut"])
-        pot_kind, pot = O.POT_EAM, tab
-        s = S.eam_cu_fcc(ncell=nc, a=w["a"], T=w["T"], seed=w["seed"])
-    else:
-        pot_kind, pot = O.POT_LJ, O.LJParams(1.0, 1.0, w["rcut"])
-        s = S.lj_fcc(ncell=nc, T=w["T"], seed=w["seed"])
-    st = s.state()
+    nc = int(max(4, min(w.get("ncell", 64), round((atoms / per) ** (1.0 / 3.0)))))
+    s, st, pot_kind, pot = oracle_sample(w, O, nc)
     O.run_nve(st, s.masses, s.lo, s.hi, pot_kind, pot, w["skin"], w["dt"], args.warmup, args.rebuild_every,
               thermo=False)
     t0 = time.perf_counter()
@@ -244,8 +271,8 @@ def run_reference(args, w, ws, rank):
               thermo=False)
     sec = time.perf_counter() - t0
     value = s.n * args.steps / sec
-    sample = "%d-atom sample (%d^3 FCC cells) of the workload, %d NVE steps, rebuild every %d" % (
-        s.n, nc, args.steps, args.rebuild_every)
+    sample = "%d-atom sample of the workload, %d NVE steps, rebuild every %d" % (
+        s.n, args.steps, args.rebuild_every)
     line = {"impl": "reference", "metric": "atom-timesteps/s", "value": value, "unit": "atom-timesteps/s",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -257,6 +284,75 @@ def run_reference(args, w, ws, rank):
                                      "FP64 OpenMP restatement of its operators"},
             "e2e": {"value": value, "unit": "atom-timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def _time_batch(b, torch, stream, reps, **kw):
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    b.run(**kw)
+    b.synchronize()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(reps):
+        b.run(**kw)
+    ev1.record(stream)
+    b.synchronize()
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / reps
+
+
+def bench_batched(stream, torch):
+    """4,096 independent periodic copper-like replicas (32-2,048 atoms,
+    log-uniform, FCC/BCC, strain <= 3%, 300-1,200 K displacements): forward
+    + parameter adjoint in one persistent launch (CUDA graph), against one
+    launch per replica."""
+    from exastamp_gb300 import _capi, autotune, setfl, systems as S
+    cfg = setfl.load_cu_params()
+    sf = setfl.tabulate(cfg)
+    reps = S.replica_set(nrep=4096, seed=6)
+    n = sum(s.n for s in reps)
+    J_F, J_f, J_z = setfl.table_param_jacobian(cfg)
+    with _capi.Batch(0, stream.cuda_stream) as b:
+        b.set_eam_alloy(sf, 5.0)
+        b.set_param_derivatives(J_F, J_f, J_z)
+        b.upload(reps)
+        b.run()
+        d = b.download()
+        b.set_targets(d["F"] * 1.01, d["ep"] * 1.01, 1.0 / n, 0.1 / n)
+        block, stencil, tun = autotune.tune_batch(b, "replicas4096", adjoint=True)
+        b.set_launch(block, stencil)
+        ms_graph = _time_batch(b, torch, stream, 5, adjoint=True, use_graph=True)
+        ms_fwd = _time_batch(b, torch, stream, 5, adjoint=False, use_graph=True)
+        ms_each = _time_batch(b, torch, stream, 1, adjoint=True, per_replica=True)
+    return {"replicas": len(reps), "atoms": n, "block": block, "stencil": stencil,
+            "ms_forward_adjoint_persistent_graph": ms_graph, "ms_forward_persistent_graph": ms_fwd,
+            "ms_forward_adjoint_one_launch_per_replica": ms_each,
+            "replicas_per_s": len(reps) / (ms_graph * 1e-3), "atom_evaluations_per_s": n / (ms_graph * 1e-3),
+            "speedup_vs_one_launch_per_replica": ms_each / ms_graph, "autotune_ms": tun}
+
+
+def bench_adjoint(stream, torch):
+    """256 copper-like training configurations (4^3 FCC, 5% vacancies, a in
+    [3.5, 3.75] A, Gaussian displacements 0.05-0.15 A), loss = mean |dF|^2 +
+    0.1 mean dE^2 against targets from parameters scaled by U(0.9, 1.1):
+    one forward + adjoint evaluation of the 9 parameter gradients."""
+    from exastamp_gb300 import _capi, setfl, systems as S
+    cfg = setfl.load_cu_params()
+    confs = S.adjoint_training_set(nconf=256, ncell=4, seed=4)
+    rng = np.random.default_rng(5)
+    pert = {k: v * rng.uniform(0.9, 1.1) for k, v in cfg["params"].items()}
+    n = sum(c.n for c in confs)
+    with _capi.Batch(0, stream.cuda_stream) as b:
+        b.set_eam_alloy(setfl.tabulate(cfg, pert), 5.0)
+        b.upload(confs)
+        b.run()
+        t = b.download()
+        b.set_eam_alloy(setfl.tabulate(cfg), 5.0)
+        b.set_param_derivatives(*setfl.table_param_jacobian(cfg))
+        b.set_targets(t["F"], t["ep"], 1.0 / n, 0.1 / n)
+        ms = _time_batch(b, torch, stream, 10, adjoint=True, use_graph=True)
+        g = b.download()
+    return {"configurations": len(confs), "atoms": n, "ms_per_loss_and_gradient": ms, "loss": g["loss"],
+            "grad": dict(zip(setfl.PARAM_NAMES, g["grad"].tolist()))}
 
 
 # ---------------------------------------------------------------------------
@@ -277,6 +373,13 @@ def main():
     ctx = _capi.Context(dev, stream.cuda_stream)
     ctx.upload_system(s)
     bind_potential(ctx, w)
+    t_min = None
+    if w.get("min_steps"):
+        # random positions overlap: clipped minimiser first (FP64 forces)
+        ctx.set_precision(False)
+        t0 = time.perf_counter()
+        ctx.run_minimize(w["min_steps"], MIN_DT, tolF=MIN_TOLF, rebuild_every=args.rebuild_every)
+        t_min = time.perf_counter() - t0
     ctx.set_precision(args.precision == "mixed")
     if args.lanes:
         ctx.set_launch(args.lanes, args.block or 128)
@@ -285,7 +388,9 @@ def main():
         lanes, block, _ = autotune.tune(ctx, key="%s-%s" % (args.workload, args.precision))
         ctx.set_launch(lanes, block)
     R, dt = args.rebuild_every, w["dt"]
-    thermo_every = 2 * R if R > 0 else 0
+    # fixed interval: thermo at the end of each 2R-step graph chunk; with the
+    # displacement trigger (R = -1) every 20 steps
+    thermo_every = 2 * R if R > 0 else (20 if R < 0 else 0)
     # warm-up (also captures the CUDA graph)
     ctx.run_nve(max(args.warmup, 3), dt, R, thermo_every, use_graph=True)
     npairs, maxnb, nc = ctx.neighbor_stats()
@@ -295,28 +400,36 @@ def main():
     with ClockSampler(dev) as clk:
         barrier(ws)
         torch.cuda.synchronize()
+        builds0 = ctx.list_builds()
         ev0.record(stream)
         th = ctx.run_nve(args.steps, dt, R, thermo_every, use_graph=True)
         ev1.record(stream)
         torch.cuda.synchronize()
         barrier(ws)
+        rebuilds = ctx.list_builds() - builds0
     ms = ev0.elapsed_time(ev1)
     ms = dist_max(ms, ws)
     clocks = clk.summary()
     value = s.n * args.steps * ws / (ms * 1e-3)
     etot = th[:, 21:24].sum(1) + th[:, 24]
     drift = (etot[-1] - etot[0]) / s.n / max(args.steps, 1) * 1000.0
-    rebuilds = args.steps // R if R > 0 else 0
     kernels_per_step = 2 if w["kind"] == "eam" else 1
-    gpu_launches = kernels_per_step * args.steps + 9 * rebuilds + 2 * (args.steps // thermo_every if thermo_every else 0)
+    # rebuild chain: wrap/bin, 3 scan kernels, scatter, rank, gather, posf,
+    # list build; with the trigger 14 gated launches every step (displacement
+    # test, 2 fills, the chain, copy-back, reference positions)
+    gpu_launches = kernels_per_step * args.steps + 2 * (args.steps // thermo_every if thermo_every else 0)
+    gpu_launches += 14 * args.steps if R < 0 else 9 * rebuilds
 
     out = {"metric": "atom-timesteps/s", "value": value, "unit": "atom-timesteps/s", "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32-pair/f64-state" if args.precision == "mixed" else "f64",
-           "data": "synthetic (seeded FCC lattice, Maxwell-Boltzmann velocities)",
+           "data": "synthetic (seeded random positions with voids, Maxwell-Boltzmann velocities)"
+           if w["kind"] == "lj_multi" else "synthetic (seeded FCC lattice, Maxwell-Boltzmann velocities)",
            "config": {"workload": args.workload, "description": w["desc"], "atoms": s.n,
-                      "precision": args.precision, "rebuild_every": R, "thermo_every": thermo_every,
+                      "precision": args.precision, "thermo_every": thermo_every,
+                      "rebuild_every": R if R >= 0 else "on displacement > skin/2",
+                      "list_builds_in_timed_region": rebuilds,
                       "neighbours_per_atom": npairs / s.n, "cells": nc.tolist(),
                       "lanes_per_atom": ctx.get_launch()[0], "block": ctx.get_launch()[1],
                       "parallelism": "replicas" if ws > 1 else "single-gpu",
@@ -325,6 +438,9 @@ def main():
                       "cuda_graph": True},
            "gpu_launches": gpu_launches, "clocks": clocks,
            "nve_energy_drift_per_1000_steps_per_atom": drift}
+    if t_min is not None:
+        out["minimiser"] = {"steps": w["min_steps"], "step": MIN_DT, "clip": MIN_TOLF, "precision": "fp64",
+                            "seconds": t_min}
 
     # ---- per-kernel timing for the roofline -------------------------------
     prof = ctx.profile_step(reps=10)
@@ -393,14 +509,18 @@ def main():
                       "ms_per_step": mse / args.e2e_steps,
                       "path": "gbmd_upload_state(pinned r,v,a) + gbmd_run_nve(1) + gbmd_download(r,v,a)"}
 
+    # ---- batched replicas (4,096 EAM systems) and the parameter adjoint --------
+    if not args.no_batch and ws == 1:
+        out["batched_replicas"] = bench_batched(stream, torch)
+        out["parameter_adjoint"] = bench_adjoint(stream, torch)
+
     # ---- CPU baseline (rank 0, N=1) -------------------------------------------
     if not args.no_cpu and ws == 1 and rank == 0:
         rate, info = cpu_oracle_rate(w)
         out["cpu_baseline"] = {"value": rate, "unit": "atom-timesteps/s", "cores": info["threads"],
                                "kind": "port",
-                               "sample": "%d-atom sample (%d^3 FCC cells) of the workload, %d FP64 NVE steps "
-                                         "on the OpenMP oracle (%.1f s)" % (info["atoms"], info["ncell"],
-                                                                            info["steps"], info["seconds"])}
+                               "sample": "%d-atom sample of the workload, %d FP64 NVE steps on the OpenMP "
+                                         "oracle (%.1f s)" % (info["atoms"], info["steps"], info["seconds"])}
     ctx.close()
     if rank == 0:
         print(json.dumps(out), flush=True)

@@ -18,6 +18,7 @@ LIB_PATH = os.path.join(PKG, "libgbmd.so")
 HEADER = os.path.join(ROOT, "include", "gbmd.h")
 
 OK = 0
+REBUILD_ON_DISPLACEMENT = -1  # rebuild_every value of the displacement trigger
 ERR_NAMES = {1: "INVALID", 2: "CUDA", 3: "NO_DEVICE", 4: "NEIGHBOR_OVERFLOW", 5: "LOST_ATOM",
              6: "NONFINITE", 7: "IO", 8: "UNSUPPORTED", 9: "TOO_LARGE"}
 PRECISION_FP64, PRECISION_MIXED = 0, 1
@@ -81,6 +82,7 @@ def lib(path: str = LIB_PATH):
             "gbmd_push_min": ([vp, dbl, dbl, dbl], i32),
             "gbmd_run_nve": ([vp, i32, dbl, i32, i32, vp, i32], i32),
             "gbmd_run_minimize": ([vp, i32, dbl, dbl, i32], i32),
+            "gbmd_list_builds": ([vp, P(i64)], i32),
             "gbmd_thermo": ([vp, vp], i32),
             "gbmd_device_state": ([vp] + [vp] * 11, i32),
             "gbmd_thermo_reduce_noalloc": ([i64, vp, vp, vp, vp, vp, vp, vp, i32, vp, vp], i32),
@@ -263,6 +265,11 @@ class Context:
 
     def run_minimize(self, nsteps, dt, tolF=0.0, rebuild_every=10):
         self._chk(self._L.gbmd_run_minimize(self.h, int(nsteps), float(dt), float(tolF), int(rebuild_every)))
+
+    def list_builds(self):
+        n = C.c_int64(0)
+        self._chk(self._L.gbmd_list_builds(self.h, C.byref(n)))
+        return n.value
 
     def thermo(self):
         out = np.zeros(27)

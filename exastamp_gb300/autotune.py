@@ -49,6 +49,36 @@ def _store(d):
         pass
 
 
+def tune_batch(batch, key: str, blocks=(128, 256, 512), stencils=(1, 2), adjoint=False, reps: int = 3,
+               use_cache: bool = True):
+    """Pick (block, stencil radius) for a gbmd_batch: each candidate runs the
+    persistent launch `reps` times, timed on the host around a synchronize."""
+    import time
+    ck = "%s|batch|%s|%d|%d|%d" % (_gpu_name(), key, batch.nrep, batch.n, int(adjoint))
+    cache = _load() if use_cache else {}
+    if ck in cache:
+        e = cache[ck]
+        return int(e["block"]), int(e["stencil"]), e.get("timings", {})
+    timings, best = {}, None
+    for s in stencils:
+        for b in blocks:
+            batch.set_launch(b, s)
+            batch.run(adjoint=adjoint)
+            batch.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                batch.run(adjoint=adjoint)
+            batch.synchronize()
+            ms = (time.perf_counter() - t0) * 1e3 / reps
+            timings["%dx%d" % (b, s)] = ms
+            if best is None or ms < best[0]:
+                best = (ms, b, s)
+    cache[ck] = {"block": best[1], "stencil": best[2], "timings": timings}
+    if use_cache:
+        _store(cache)
+    return best[1], best[2], timings
+
+
 def tune(ctx, key: str, lanes=LANES, blocks=BLOCKS, reps: int = 3, use_cache: bool = True):
     """Return (lanes, block, timings) for this context's system and potential."""
     n = ctx.n

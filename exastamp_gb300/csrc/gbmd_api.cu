@@ -141,13 +141,28 @@ __global__ void k_iota(int64_t n, int32_t* __restrict__ user, uint64_t* __restri
   if (with_id) id[p] = (uint64_t)p;
 }
 
+// particle_displ_over: flag = 1 when some atom moved more than sqrt(thr2)
+// since the last rebuild; |dr|^2 summed x, y, z without contraction
 __global__ void k_displ_over(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
                              const double* __restrict__ z, const double* __restrict__ rref, int64_t cap,
                              double thr2, int* __restrict__ flag) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= n) return;
-  const double dx = x[p] - rref[p], dy = y[p] - rref[cap + p], dz = z[p] - rref[2 * cap + p];
-  if (dx * dx + dy * dy + dz * dz > thr2) *flag = 1;
+  const double dx = __dsub_rn(x[p], rref[p]), dy = __dsub_rn(y[p], rref[cap + p]),
+               dz = __dsub_rn(z[p], rref[2 * cap + p]);
+  const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  if (d2 > thr2) *flag = 1;
+}
+
+// reference positions after a gated rebuild; block 0 counts the rebuild
+__global__ void k_copy_rref_gated(int64_t n, const double* __restrict__ r, double* __restrict__ rref, int64_t cap,
+                                  const int* __restrict__ gate, int* __restrict__ count) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (!*gate) return;
+  if (p == 0) atomicAdd(count, 1);
+  if (p >= n) return;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) rref[d * cap + p] = r[d * cap + p];
 }
 
 static inline unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
@@ -163,6 +178,33 @@ static int do_rebuild(gbmd_context* c, bool check) {
   int rc = rebuild(c, check);
   if (rc) return rc;
   return copy_rref(c);
+}
+
+// check_and_update_particles of the verlet step (config_move_particles.msp
+// L116-152): the displacement test and the rebuild run on the device, the
+// rebuild kernels gated by its outcome, so nothing waits on the host.
+static int rebuild_if_displaced(gbmd_context* c) {
+  if (c->n == 0) return GBMD_OK;
+  int* gate = c->d_err + ERRW_GATE;
+  const double thr = 0.5 * c->skin;
+  GBMD_CUDA(c, cudaMemsetAsync(gate, 0, sizeof(int), c->stream));
+  k_displ_over<<<nblk(c->n, 256), 256, 0, c->stream>>>(c->n, c->X(), c->Y(), c->Z(), c->rref, c->cap, thr * thr,
+                                                        gate);
+  int rc = rebuild(c, false, gate);
+  if (rc) return rc;
+  k_copy_rref_gated<<<nblk(c->n, 256), 256, 0, c->stream>>>(c->n, c->rbuf[c->cur], c->rref, c->cap, gate,
+                                                             c->d_err + ERRW_REBUILDS);
+  return GBMD_OK;
+}
+
+// folds the device-side rebuild count into list_builds (stream synchronised)
+static int collect_device_rebuilds(gbmd_context* c) {
+  int cnt = 0;
+  GBMD_CUDA(c, cudaMemcpyAsync(&cnt, c->d_err + ERRW_REBUILDS, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_REBUILDS, 0, sizeof(int), c->stream));
+  GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->list_builds += cnt;
+  return GBMD_OK;
 }
 
 // --- EAM spline build (eam_alloy.cpp L29-58, LAMMPS array2spline) ---------
@@ -346,12 +388,13 @@ int gbmd_upload_positions(gbmd_context* c, const double* rx, const double* ry, c
   if (c->list_valid) {
     // particle_displ_over: rebuild when an atom moved more than skin/2 since
     // the last rebuild (config_move_particles.msp L19-22, L116-118)
-    GBMD_CUDA(c, cudaMemsetAsync(c->d_err + 7, 0, sizeof(int), s));
+    GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_DISPL, 0, sizeof(int), s));
     const double thr = 0.5 * c->skin;
-    k_displ_over<<<nblk(n, 256), 256, 0, s>>>(n, c->X(), c->Y(), c->Z(), c->rref, cap, thr * thr, c->d_err + 7);
+    k_displ_over<<<nblk(n, 256), 256, 0, s>>>(n, c->X(), c->Y(), c->Z(), c->rref, cap, thr * thr,
+                                              c->d_err + ERRW_DISPL);
     int rc = sync_error_word(c);
     if (rc) return rc;
-    if (c->h_err[7]) invalidate_list(c);
+    if (c->h_err[ERRW_DISPL]) invalidate_list(c);
     else launch_posf(c);
   }
   return GBMD_OK;
@@ -727,12 +770,13 @@ int gbmd_thermo(gbmd_context* c, double out[27]) {
 // step's first half fused (fuse 2) or, on thermo/last steps, only the second
 // half followed by the thermo reduction and a standalone first half.
 struct StepPlan {
-  bool rebuild, thermo, last;
+  bool rebuild, thermo, last, trigger;
 };
 
 static int one_step(gbmd_context* c, double dt, const StepPlan& p, bool check, double* thermo_row) {
   int rc;
   if (p.rebuild && (rc = do_rebuild(c, check))) return rc;
+  if (p.trigger && (rc = rebuild_if_displaced(c))) return rc;
   ForceFlags f;
   f.energy = p.thermo;
   f.virial = p.thermo;
@@ -750,17 +794,18 @@ static int one_step(gbmd_context* c, double dt, const StepPlan& p, bool check, d
   return GBMD_OK;
 }
 
-// A graph covers two rebuild intervals (2R steps) so that every buffer swap
-// inside it happens an even number of times and the captured pointers are
-// valid again when it is replayed.  With thermo, the reduction is captured at
-// the chunk's last step only (thermo_every == 2R).
-static int capture_graph(gbmd_context* c, double dt, int R, bool thermo_end) {
+// A graph covers G steps: two rebuild intervals (G = 2R) with a fixed
+// interval, or an even G with the displacement trigger (R < 0), so that every
+// buffer swap inside it happens an even number of times and the captured
+// pointers are valid again when it is replayed.  With thermo, the reduction
+// is captured at the chunk's last step only (thermo_every == G).
+static int capture_graph(gbmd_context* c, double dt, int R, int G, bool thermo_end) {
   drop_graph(c);
   cudaGraph_t g;
   GBMD_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   int rc = GBMD_OK;
-  for (int l = 1; l <= 2 * R && rc == GBMD_OK; ++l) {
-    StepPlan p{l % R == 0, thermo_end && l == 2 * R, false};
+  for (int l = 1; l <= G && rc == GBMD_OK; ++l) {
+    StepPlan p{R > 0 && l % R == 0, thermo_end && l == G, false, R < 0};
     rc = one_step(c, dt, p, false, nullptr);
   }
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
@@ -773,6 +818,7 @@ static int capture_graph(gbmd_context* c, double dt, int R, bool thermo_end) {
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return check_cuda(c, e, "cudaGraphInstantiate");
   c->graph_rebuild_every = R;
+  c->graph_chunk = G;
   c->graph_dt = dt;
   c->graph_thermo_end = thermo_end ? 1 : 0;
   c->graph_key_n = c->n;
@@ -783,15 +829,15 @@ static int capture_graph(gbmd_context* c, double dt, int R, bool thermo_end) {
   return GBMD_OK;
 }
 
-static bool graph_matches(const gbmd_context* c, double dt, int R, bool thermo_end) {
-  return c->graph_exec && c->graph_rebuild_every == R && c->graph_dt == dt &&
+static bool graph_matches(const gbmd_context* c, double dt, int R, int G, bool thermo_end) {
+  return c->graph_exec && c->graph_rebuild_every == R && c->graph_chunk == G && c->graph_dt == dt &&
          c->graph_thermo_end == (thermo_end ? 1 : 0) && c->graph_key_n == c->n && c->graph_key_maxnb == c->maxnb &&
          c->graph_key_tpa == c->tpa && c->graph_key_block == c->block && c->graph_key_prec == c->precision;
 }
 
 int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int thermo_every, double* thermo_out,
                  int use_graph) {
-  if (!c || nsteps < 0) return GBMD_ERR_INVALID;
+  if (!c || nsteps < 0 || rebuild_every < GBMD_REBUILD_ON_DISPLACEMENT) return GBMD_ERR_INVALID;
   if (c->pot == GBMD_POT_NONE) return set_error(c, GBMD_ERR_INVALID, "no potential set");
   cudaSetDevice(c->device);
   int rc = ensure_list(c);
@@ -823,22 +869,26 @@ int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int 
   }
   launch_first_half(c, dt);
   const int R = rebuild_every;
-  const bool graph_ok = use_graph && R > 0 && (!want_thermo || thermo_every == 2 * R);
+  const bool trigger = R == GBMD_REBUILD_ON_DISPLACEMENT;
+  // graph chunk length: two rebuild intervals, or with the trigger the thermo
+  // interval when it is even (20 steps without thermo)
+  const int G = trigger ? (want_thermo ? thermo_every : 20) : 2 * R;
+  const bool graph_ok = use_graph && G > 0 && G % 2 == 0 && (!want_thermo || thermo_every == G);
   int s = 1;
   while (s <= nsteps) {
-    // a graph chunk covers steps s..s+2R-1; it starts right after a rebuild
+    // a graph chunk covers steps s..s+G-1; it starts right after a rebuild
     // interval and must end before the last step (which may not fuse the
     // next first half)
-    if (graph_ok && (s - 1) % (2 * R) == 0 && s + 2 * R - 1 < nsteps) {
-      if (!graph_matches(c, dt, R, want_thermo) && (rc = capture_graph(c, dt, R, want_thermo))) return rc;
+    if (graph_ok && (s - 1) % G == 0 && s + G - 1 < nsteps) {
+      if (!graph_matches(c, dt, R, G, want_thermo) && (rc = capture_graph(c, dt, R, G, want_thermo))) return rc;
       GBMD_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
       if (want_thermo)
-        GBMD_CUDA(c, cudaMemcpyAsync(rows + 27 * (size_t)((s + 2 * R - 1) / thermo_every), c->d_thermo,
+        GBMD_CUDA(c, cudaMemcpyAsync(rows + 27 * (size_t)((s + G - 1) / thermo_every), c->d_thermo,
                                      sizeof(double) * 27, cudaMemcpyDeviceToDevice, c->stream));
-      s += 2 * R;
+      s += G;
       continue;
     }
-    StepPlan p{R > 0 && s % R == 0, want_thermo && s % thermo_every == 0, s == nsteps};
+    StepPlan p{R > 0 && s % R == 0, want_thermo && s % thermo_every == 0, s == nsteps, trigger};
     double* row = p.thermo ? rows + 27 * (size_t)(s / thermo_every) : nullptr;
     if ((rc = one_step(c, dt, p, !use_graph, row))) return rc;
     ++s;
@@ -849,22 +899,32 @@ int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int 
   GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
   c->step += nsteps;
   c->forces_valid_step = c->step;
+  if (trigger && (rc = collect_device_rebuilds(c))) return rc;
   return check_device_errors(c);
 }
 
 int gbmd_run_minimize(gbmd_context* c, int nsteps, double dt, double tolF, int rebuild_every) {
-  if (!c || nsteps < 0) return GBMD_ERR_INVALID;
+  if (!c || nsteps < 0 || rebuild_every < GBMD_REBUILD_ON_DISPLACEMENT) return GBMD_ERR_INVALID;
   int rc = ensure_list(c);
   if (rc) return rc;
+  const bool trigger = rebuild_every == GBMD_REBUILD_ON_DISPLACEMENT;
   for (int s = 1; s <= nsteps; ++s) {
     ForceFlags f;
     if ((rc = launch_forces(c, f))) return rc;
     launch_push_min(c, dt, 1.0, tolF);
     if (rebuild_every > 0 && s % rebuild_every == 0 && (rc = do_rebuild(c, true))) return rc;
+    if (trigger && (rc = rebuild_if_displaced(c))) return rc;
   }
   c->forces_valid_step = -1;
   GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (trigger && (rc = collect_device_rebuilds(c))) return rc;
   return check_device_errors(c);
+}
+
+int gbmd_list_builds(const gbmd_context* c, int64_t* count) {
+  if (!c || !count) return GBMD_ERR_INVALID;
+  *count = c->list_builds;
+  return GBMD_OK;
 }
 
 int gbmd_profile_step(gbmd_context* c, int reps, double ms[5]) {

@@ -31,6 +31,9 @@ enum {
   ERRW_LOST = 2,      // atoms found outside the box after the wrap
   ERRW_STEP = 3,      // step index of the first error (-1 none)
   ERRW_BADATOM = 4,   // first offending atom (sorted index)
+  ERRW_REBUILDS = 5,  // displacement-triggered rebuilds run on the device
+  ERRW_GATE = 6,      // this step's displacement trigger (gate of the rebuild chain)
+  ERRW_DISPL = 7,     // displacement check of gbmd_upload_positions
 };
 enum {
   GBMD_DEVERR_NBR_OVERFLOW = 1,
@@ -184,6 +187,7 @@ struct gbmd_context {
   // CUDA graph of a chunk of steps
   cudaGraphExec_t graph_exec = nullptr;
   int graph_rebuild_every = 0;
+  int graph_chunk = 0;
   double graph_dt = 0.0;
   int graph_thermo_end = 0;
   int64_t graph_key_n = -1;
@@ -204,8 +208,10 @@ int sync_error_word(gbmd_context* c);  // copies device error word, returns stat
 
 // neighbours (gbmd_neighbors.cu)
 int grid_dims(const double lo[3], const double hi[3], double R, int nc[3]);
-int rebuild(gbmd_context* c, bool check_capacity);
-void launch_posf(gbmd_context* c);
+// gate: device word; non-null makes every kernel of the chain return at once
+// while it holds 0, and keeps the buffer indices unchanged (see gbmd_neighbors.cu)
+int rebuild(gbmd_context* c, bool check_capacity, const int* gate = nullptr);
+void launch_posf(gbmd_context* c, const int* gate = nullptr);
 int export_pairs(gbmd_context* c, int64_t cap, uint64_t* id_i, uint64_t* id_j, int8_t* img, int64_t* count);
 
 // forces (gbmd_forces.cu)

@@ -18,6 +18,14 @@
 //   k_posf        FP32 local + FP64 packed gather copies        HBM: 24 B r, 48 B w
 //   k_build_list_cells  warp per home cell over the 27-cell candidates, ballot
 //                 compaction in canonical order                 HBM: 4 B per entry
+//
+// Every kernel of the chain takes a `gate` word: when it is non-null and
+// holds 0 the kernel returns at once.  The displacement-triggered step
+// (particle_displ_over, config_move_particles.msp L19-22, L116-118) sets the
+// gate on the device and launches the chain unconditionally, so the decision
+// to rebuild never goes through the host and the chain can sit inside a CUDA
+// graph.  That variant gathers into the spare buffers and copies back, so the
+// buffer parity the captured pointers rely on does not depend on the outcome.
 #include <cstdio>
 #include <cstring>
 
@@ -44,9 +52,9 @@ struct BoxArgs {
 
 __global__ void k_wrap_bin(int64_t n, double* __restrict__ x, double* __restrict__ y,
                            double* __restrict__ z, BoxArgs b, int32_t* __restrict__ cell_of,
-                           int32_t* __restrict__ cell_count, int* __restrict__ err) {
+                           int32_t* __restrict__ cell_count, int* __restrict__ err, const int* __restrict__ gate) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || (gate && !*gate)) return;
   double* r[3] = {x, y, z};
   int c[3];
   bool lost = false;
@@ -103,7 +111,8 @@ __device__ __forceinline__ int block_exclusive(int v, int* smem, int& total) {
 
 // in[0..n) -> out[0..n] exclusive (out[n] = total when this block holds n)
 __global__ void k_scan_block(const int32_t* __restrict__ in, int32_t* __restrict__ out, int64_t n,
-                             int32_t* __restrict__ sums) {
+                             int32_t* __restrict__ sums, const int* __restrict__ gate) {
+  if (gate && !*gate) return;  // uniform per block
   __shared__ int smem[33];
   const int64_t base = (int64_t)blockIdx.x * SCAN_B + (int64_t)threadIdx.x * SCAN_I;
   int it[SCAN_I];
@@ -125,7 +134,8 @@ __global__ void k_scan_block(const int32_t* __restrict__ in, int32_t* __restrict
   if (threadIdx.x == 0) sums[blockIdx.x] = total;
 }
 
-__global__ void k_scan_sums(int32_t* sums, int nb) {
+__global__ void k_scan_sums(int32_t* sums, int nb, const int* __restrict__ gate) {
+  if (gate && !*gate) return;
   __shared__ int smem[33];
   int carry = 0;
   for (int base = 0; base < nb; base += SCAN_B) {
@@ -149,7 +159,9 @@ __global__ void k_scan_sums(int32_t* sums, int nb) {
   }
 }
 
-__global__ void k_scan_add(int32_t* __restrict__ out, int64_t n, const int32_t* __restrict__ sums) {
+__global__ void k_scan_add(int32_t* __restrict__ out, int64_t n, const int32_t* __restrict__ sums,
+                           const int* __restrict__ gate) {
+  if (gate && !*gate) return;
   const int64_t base = (int64_t)blockIdx.x * SCAN_B;
   const int add = sums[blockIdx.x];
   for (int k = threadIdx.x; k < SCAN_B; k += blockDim.x) {
@@ -158,23 +170,23 @@ __global__ void k_scan_add(int32_t* __restrict__ out, int64_t n, const int32_t* 
   }
 }
 
-static int scan(gbmd_context* c, const int32_t* in, int32_t* out, int64_t n) {
+static int scan(gbmd_context* c, const int32_t* in, int32_t* out, int64_t n, const int* gate) {
   const int64_t nb = (n + 1 + SCAN_B - 1) / SCAN_B;
   if (c->scan_cap < nb) {
     if (c->scan_tmp) cudaFree(c->scan_tmp);
     GBMD_CUDA(c, cudaMalloc(&c->scan_tmp, sizeof(int32_t) * nb));
     c->scan_cap = nb;
   }
-  k_scan_block<<<(unsigned)nb, SCAN_T, 0, c->stream>>>(in, out, n, c->scan_tmp);
-  k_scan_sums<<<1, SCAN_T, 0, c->stream>>>(c->scan_tmp, (int)nb);
-  k_scan_add<<<(unsigned)nb, SCAN_T, 0, c->stream>>>(out, n, c->scan_tmp);
+  k_scan_block<<<(unsigned)nb, SCAN_T, 0, c->stream>>>(in, out, n, c->scan_tmp, gate);
+  k_scan_sums<<<1, SCAN_T, 0, c->stream>>>(c->scan_tmp, (int)nb, gate);
+  k_scan_add<<<(unsigned)nb, SCAN_T, 0, c->stream>>>(out, n, c->scan_tmp, gate);
   return GBMD_OK;
 }
 
 __global__ void k_scatter(int64_t n, const int32_t* __restrict__ cell_of, const int32_t* __restrict__ cstart,
-                          int32_t* __restrict__ fill, int32_t* __restrict__ order) {
+                          int32_t* __restrict__ fill, int32_t* __restrict__ order, const int* __restrict__ gate) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || (gate && !*gate)) return;
   const int32_t cl = cell_of[i];
   const int32_t slot = cstart[cl] + atomicAdd(&fill[cl], 1);
   order[slot] = (int32_t)i;
@@ -183,10 +195,10 @@ __global__ void k_scatter(int64_t n, const int32_t* __restrict__ cell_of, const 
 // one warp per cell: rank by (id, upload index) -> src[new] = old
 __global__ void k_cell_rank(int64_t ncells, const int32_t* __restrict__ cstart, const int32_t* __restrict__ order,
                             const uint64_t* __restrict__ id, const int32_t* __restrict__ user,
-                            int32_t* __restrict__ src) {
+                            int32_t* __restrict__ src, const int* __restrict__ gate) {
   const int64_t cell = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (cell >= ncells) return;
+  if (cell >= ncells || (gate && !*gate)) return;
   const int beg = cstart[cell], m = cstart[cell + 1] - beg;
   for (int e = lane; e < m; e += 32) {
     const int32_t a = order[beg + e];
@@ -218,9 +230,9 @@ struct GatherArgs {
 
 __global__ void k_gather(int64_t n, const int32_t* __restrict__ src, GatherArgs g,
                          const int32_t* __restrict__ cell_of, int ncx, int ncy,
-                         int32_t* __restrict__ cellpack) {
+                         int32_t* __restrict__ cellpack, const int* __restrict__ gate) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p >= n) return;
+  if (p >= n || (gate && !*gate)) return;
   const int64_t o = src[p];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
@@ -237,12 +249,38 @@ __global__ void k_gather(int64_t n, const int32_t* __restrict__ src, GatherArgs 
   cellpack[p] = cx | (cy << 10) | (cz << 20);
 }
 
+// gated variant only: the sorted state, gathered into the spare buffers, is
+// copied back so the current buffer index does not change
+__global__ void k_copy_back(int64_t n, GatherArgs g, const int* __restrict__ gate) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n || !*gate) return;
+  double* r0 = const_cast<double*>(g.r0);
+  double* v0 = const_cast<double*>(g.v0);
+  double* a0 = const_cast<double*>(g.a0);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    r0[d * g.cap + p] = g.r1[d * g.cap + p];
+    v0[d * g.cap + p] = g.v1[d * g.cap + p];
+    a0[d * g.cap + p] = g.a1[d * g.cap + p];
+  }
+  const_cast<uint8_t*>(g.t0)[p] = g.t1[p];
+  const_cast<uint64_t*>(g.i0)[p] = g.i1[p];
+  const_cast<int32_t*>(g.u0)[p] = g.u1[p];
+  const_cast<double*>(g.ep0)[p] = g.ep1[p];
+}
+
+__global__ void k_fill_gated(int32_t* __restrict__ p, int64_t n, const int* __restrict__ gate) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n || !*gate) return;
+  p[i] = 0;
+}
+
 __global__ void k_posf(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
                        const double* __restrict__ z, const uint8_t* __restrict__ type,
                        const int32_t* __restrict__ cellpack, Grid g, float4* __restrict__ pf,
-                       double4_32a* __restrict__ pd) {
+                       double4_32a* __restrict__ pd, const int* __restrict__ gate) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || (gate && !*gate)) return;
   const int cp = cellpack[i];
   const double cx = (double)(cp & 1023), cy = (double)((cp >> 10) & 1023), cz = (double)(cp >> 20);
   const double xi = x[i], yi = y[i], zi = z[i];
@@ -266,24 +304,30 @@ __device__ __noinline__ bool exact_within(const double* __restrict__ x, const do
                   (double)nzi * g.L[2], a, b, c) <= R2;
 }
 
-constexpr int BUILD_HB = 16;  // home atoms staged per batch
+constexpr int BUILD_HB = 16;    // home atoms per group (one per half-warp lane)
+constexpr int BUILD_CHUNK = 64; // candidates staged per chunk (two per step)
 
-// One warp per home cell.  Lane s < 27 describes stencil cell s (start,
-// count, code, FP32 shift); the 27 candidate ranges are concatenated in
-// stencil order and walked 32 candidates at a time, one per lane, so each
-// candidate position is loaded once per chunk and tested against every home
-// atom of the cell (home positions held one per lane, broadcast by shuffle).
-// A ballot + popc compacts the hits of each home atom in candidate order,
-// which is the canonical order (stencil code, then cell order).
+// One warp per home cell.  The home atoms are taken 16 at a time; lane l
+// and lane l+16 hold the same home atom.  Lane s < 27 describes stencil cell
+// s (start, count, code, FP32 shift); the 27 candidate ranges are
+// concatenated in stencil order, staged 64 at a time in shared memory
+// (position shifted into the home cell's frame, index and stencil code), and
+// each step tests two consecutive candidates against the 16 home atoms: the
+// low half-warp candidate 2t, the high half-warp candidate 2t+1, both read
+// as shared-memory broadcasts.  The two lanes of a home atom exchange their
+// hits with one shuffle and append them in candidate order, which is the
+// canonical order (stencil code, then cell order), to the atom's row of a
+// shared-memory tile; the tile goes out in coalesced list rows.
 __global__ void __launch_bounds__(128) k_build_list_cells(
     int64_t ncells, const float4* __restrict__ pf, const double* __restrict__ x, const double* __restrict__ y,
     const double* __restrict__ z, const int32_t* __restrict__ cstart, Grid g, double R2, float R2lo, float R2hi,
     uint32_t* __restrict__ nbr, int32_t* __restrict__ nnb, int maxnb, int T, int64_t stride,
-    int* __restrict__ err) {
+    int* __restrict__ err, const int* __restrict__ gate) {
   const int64_t cell = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (cell >= ncells) return;  // uniform per warp
+  if (cell >= ncells || (gate && !*gate)) return;  // uniform per warp
   const unsigned FULL = 0xffffffffu;
+  const int half = lane >> 4, hl = lane & 15;
   const int cx = (int)(cell % g.nc[0]), cy = (int)((cell / g.nc[0]) % g.nc[1]),
             cz = (int)(cell / ((int64_t)g.nc[0] * g.nc[1]));
   // stencil cell of this lane
@@ -311,85 +355,95 @@ __global__ void __launch_bounds__(128) k_build_list_cells(
   const int s_pre = incl - s_cnt;  // exclusive prefix of this lane's stencil cell
   const int total = __shfl_sync(FULL, incl, 26);
   const int hb = cstart[cell], nh = cstart[cell + 1] - hb;
-  const uint32_t CENTER = 1u | (1u << 2) | (1u << 4);
-  // per-warp shared memory: BUILD_HB home positions, 32 counts, BUILD_HB x maxnb entries
+  int tsh = 0;
+  while ((1 << tsh) < T) ++tsh;
+  // per-warp shared memory: 64 staged candidates, 16 counts (padded to 32),
+  // 16 x maxnb tile entries
   extern __shared__ float4 smem_build[];
-  float4* hpos = smem_build + (size_t)(threadIdx.x >> 5) * (BUILD_HB + 8 + BUILD_HB / 4 * (size_t)maxnb);
-  int* cnt_s = reinterpret_cast<int*>(hpos + BUILD_HB);
-  uint32_t* tile = reinterpret_cast<uint32_t*>(hpos + BUILD_HB + 8);
+  float4* stage = smem_build + (size_t)(threadIdx.x >> 5) * (BUILD_CHUNK + 8 + BUILD_HB / 4 * (size_t)maxnb);
+  int* cnt_s = reinterpret_cast<int*>(stage + BUILD_CHUNK);
+  uint32_t* tile = reinterpret_cast<uint32_t*>(stage + BUILD_CHUNK + 8);
+  uint32_t* my_row = tile + hl * maxnb;
+  const float FAR = 1e18f;
   int warp_max = 0;
-  for (int hbatch = 0; hbatch < nh; hbatch += BUILD_HB) {
-    const int nhb = min(BUILD_HB, nh - hbatch);
-    const bool hv = lane < nhb;
-    const int64_t ih = hb + hbatch + lane;
-    if (hv) hpos[lane] = pf[ih];
-    __syncwarp();
+  for (int h0 = 0; h0 < nh; h0 += BUILD_HB) {
+    const int nhb = min(BUILD_HB, nh - h0);
+    const bool hv = hl < nhb;
+    const int i = hb + h0 + hl;
+    float4 pi = make_float4(FAR, FAR, FAR, 0.f);
+    if (hv) pi = pf[i];
     int cnt = 0;
-    for (int q0 = 0; q0 < total; q0 += 32) {
-      const int q = q0 + lane;
-      const bool valid = q < total;
-      // stencil cell of candidate q: largest s with s_pre(s) <= q (5-step search)
-      int s = 0;
+    for (int q0 = 0; q0 < total; q0 += BUILD_CHUNK) {
+      __syncwarp();
 #pragma unroll
-      for (int step = 16; step > 0; step >>= 1) {
-        const int t = min(s + step, 26);
-        const int pv = __shfl_sync(FULL, s_pre, t);
-        if (s + step <= 26 && pv <= q) s = t;
+      for (int r = 0; r < BUILD_CHUNK / 32; ++r) {
+        const int q = q0 + r * 32 + lane;
+        // stencil cell of candidate q: largest s with s_pre(s) <= q (5-step search)
+        int sc = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+          const int t = min(sc + step, 26);
+          const int pv = __shfl_sync(FULL, s_pre, t);
+          if (sc + step <= 26 && pv <= q) sc = t;
+        }
+        const int k = __shfl_sync(FULL, s_start, sc) + (q - __shfl_sync(FULL, s_pre, sc));
+        const uint32_t code = __shfl_sync(FULL, s_code, sc);
+        const float sx = __shfl_sync(FULL, s_sx, sc), sy = __shfl_sync(FULL, s_sy, sc),
+                    sz = __shfl_sync(FULL, s_sz, sc);
+        float4 e = make_float4(FAR, FAR, FAR, __uint_as_float(0xffffffffu));
+        if (q < total) {
+          const float4 pj = pf[k];
+          e = make_float4(pj.x + sx, pj.y + sy, pj.z + sz, __uint_as_float((uint32_t)k | (code << GBMD_IDX_BITS)));
+        }
+        stage[r * 32 + lane] = e;
       }
-      const int k = __shfl_sync(FULL, s_start, s) + (q - __shfl_sync(FULL, s_pre, s));
-      const uint32_t code = __shfl_sync(FULL, s_code, s);
-      const float sx = __shfl_sync(FULL, s_sx, s), sy = __shfl_sync(FULL, s_sy, s), sz = __shfl_sync(FULL, s_sz, s);
-      float4 pj = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (valid) pj = pf[k];
-      const float jx = pj.x + sx, jy = pj.y + sy, jz = pj.z + sz;
-      // counts before this chunk: no dependency between the home-atom
-      // iterations below, so they pipeline
-      const int mybase = cnt;
-      unsigned mymask = 0u;
-#pragma unroll 4
-      for (int hh = 0; hh < nhb; ++hh) {
-        const int64_t i = hb + hbatch + hh;
-        const float4 pi = hpos[hh];
-        const float dx = jx - pi.x;
-        const float dy = jy - pi.y;
-        const float dz = jz - pi.z;
+      __syncwarp();
+      const int m = min(BUILD_CHUNK, total - q0);
+#pragma unroll 2
+      for (int t = 0; t < m; t += 2) {
+        const float4 e = stage[t + half];
+        const uint32_t w = __float_as_uint(e.w);
+        const int k = (int)(w & GBMD_IDX_MASK);
+        const float dx = e.x - pi.x;
+        const float dy = e.y - pi.y;
+        const float dz = e.z - pi.z;
         const float d2f = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const bool keep = (valid && !(k == i && code == CENTER));
+        // an atom never pairs with itself: its images sit at least one box
+        // edge >= R away, so k == i only ever matters in the home cell
+        const bool keep = hv && k != i;
         bool in = keep && d2f < R2lo;
         const bool band = keep && d2f >= R2lo && d2f <= R2hi;
         if (__any_sync(FULL, band)) {  // rare: some lane needs the FP64 re-test
-          if (band) in = exact_within(x, y, z, i, k, code, cx, cy, cz, g, R2);
+          if (band) in = exact_within(x, y, z, i, k, w >> GBMD_IDX_BITS, cx, cy, cz, g, R2);
         }
-        const unsigned mask = __ballot_sync(FULL, in);
-        const int base = __shfl_sync(FULL, mybase, hh);
+        const int other = __shfl_xor_sync(FULL, (int)in, 16);
         if (in) {
-          const int pos = base + __popc(mask & ((1u << lane) - 1u));
-          if (pos < maxnb) tile[hh * maxnb + pos] = (uint32_t)k | (code << GBMD_IDX_BITS);
+          const int pos = cnt + (half ? other : 0);  // candidate 2t goes first
+          if (pos < maxnb) my_row[pos] = w;
         }
-        if (lane == hh) mymask = mask;
+        cnt += (int)in + other;
       }
-      cnt += __popc(mymask);
     }
-    if (hv) {
-      nnb[ih] = cnt;
+    if (hv && half == 0) {
+      nnb[i] = cnt;
       if (cnt > maxnb) atomicOr(&err[ERRW_FLAGS], GBMD_DEVERR_NBR_OVERFLOW);
     }
-    cnt_s[lane] = hv ? min(cnt, maxnb) : 0;
-    warp_max = max(warp_max, cnt);
-    int bmax = cnt_s[lane];
+    if (half == 0) cnt_s[hl] = hv ? min(cnt, maxnb) : 0;
+    warp_max = max(warp_max, hv ? cnt : 0);
+    __syncwarp();
+    int bmax = half == 0 ? cnt_s[hl] : 0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) bmax = max(bmax, __shfl_xor_sync(FULL, bmax, o));
-    __syncwarp();
     // coalesced write-out: list row r holds slots r*T..r*T+T-1 of consecutive
-    // atoms contiguously, so the batch's part of a row is nhb*T adjacent words
-    const int64_t row0 = (int64_t)(hb + hbatch) * T;
+    // atoms contiguously, so the group's part of a row is nhb*T adjacent words
+    const int64_t row0 = (int64_t)(hb + h0) * T;
     for (int r = 0; r * T < bmax; ++r) {
-      for (int w = lane; w < nhb * T; w += 32) {
-        const int hh = w / T, pos = r * T + (w - hh * T);
-        if (pos < cnt_s[hh]) nbr[(int64_t)r * stride + row0 + w] = tile[hh * maxnb + pos];
+      for (int wi = lane; wi < nhb * T; wi += 32) {
+        const int hh = wi >> tsh, pos = r * T + (wi & (T - 1));
+        if (pos < cnt_s[hh]) nbr[(int64_t)r * stride + row0 + wi] = tile[hh * maxnb + pos];
       }
     }
-    __syncwarp();
+    __syncwarp();  // tile and counts are reused by the next group
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) warp_max = max(warp_max, __shfl_xor_sync(FULL, warp_max, o));
@@ -398,13 +452,13 @@ __global__ void __launch_bounds__(128) k_build_list_cells(
 
 static inline unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
 
-void launch_posf(gbmd_context* c) {
+void launch_posf(gbmd_context* c, const int* gate) {
   if (c->n == 0) return;
   k_posf<<<nblk(c->n, 256), 256, 0, c->stream>>>(c->n, c->X(), c->Y(), c->Z(), c->TYPE(), c->cellpack,
-                                                  c->grid, c->POSF(), c->POSD());
+                                                  c->grid, c->POSF(), c->POSD(), gate);
 }
 
-static int build_list(gbmd_context* c) {
+static int build_list(gbmd_context* c, const int* gate) {
   const double R = c->rlist;
   const double R2 = R * R;
   const float R2lo = (float)(R2 * (1.0 - 0x1p-12));
@@ -419,9 +473,9 @@ static int build_list(gbmd_context* c) {
     c->nbr_cap = need;
   }
   c->npad = npad;
-  GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_MAXNB, 0, sizeof(int), c->stream));
-  // shared memory per warp: BUILD_HB home positions + 32 counts + BUILD_HB x maxnb entries
-  const size_t per_warp = 16 * (BUILD_HB + 8) + 4 * BUILD_HB * (size_t)c->maxnb;
+  if (!gate) GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_MAXNB, 0, sizeof(int), c->stream));
+  // shared memory per warp: BUILD_CHUNK staged candidates + 32 counts + BUILD_HB x maxnb entries
+  const size_t per_warp = 16 * (BUILD_CHUNK + 8) + 4 * BUILD_HB * (size_t)c->maxnb;
   int W = (int)((96 * 1024) / per_warp);
   W = W < 1 ? 1 : (W > 4 ? 4 : W);
   const size_t smem = per_warp * W;
@@ -430,11 +484,13 @@ static int build_list(gbmd_context* c) {
     GBMD_CUDA(c, cudaFuncSetAttribute(k_build_list_cells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k_build_list_cells<<<nblk(c->grid.ncells, W), 32 * W, smem, c->stream>>>(
       c->grid.ncells, c->POSF(), c->X(), c->Y(), c->Z(), c->cell_start, c->grid, R2, R2lo, R2hi, c->nbr, c->nnb,
-      c->maxnb, c->tpa, stride, c->d_err);
+      c->maxnb, c->tpa, stride, c->d_err, gate);
   return GBMD_OK;
 }
 
-int rebuild(gbmd_context* c, bool check_capacity) {
+int rebuild(gbmd_context* c, bool check_capacity, const int* gate) {
+  if (gate && (!c->list_valid || !c->grid_valid || c->maxnb <= 0))
+    return set_error(c, GBMD_ERR_INVALID, "gated rebuild needs a built list");
   if (!c->box_set) return set_error(c, GBMD_ERR_INVALID, "box not set");
   if (c->pot == GBMD_POT_NONE) return set_error(c, GBMD_ERR_INVALID, "no potential set");
   if (c->n == 0) {
@@ -476,14 +532,19 @@ int rebuild(gbmd_context* c, bool check_capacity) {
   }
   const int64_t n = c->n;
   cudaStream_t s = c->stream;
-  GBMD_CUDA(c, cudaMemsetAsync(c->cell_fill, 0, sizeof(int32_t) * (g.ncells + 1), s));
-  k_wrap_bin<<<nblk(n, 256), 256, 0, s>>>(n, c->X(), c->Y(), c->Z(), b, c->cell_of, c->cell_fill, c->d_err);
-  int rc = scan(c, c->cell_fill, c->cell_start, g.ncells);
+  auto zero_fill = [&]() -> int {
+    if (gate) k_fill_gated<<<nblk(g.ncells + 1, 256), 256, 0, s>>>(c->cell_fill, g.ncells + 1, gate);
+    else GBMD_CUDA(c, cudaMemsetAsync(c->cell_fill, 0, sizeof(int32_t) * (g.ncells + 1), s));
+    return GBMD_OK;
+  };
+  int rc = zero_fill();
   if (rc) return rc;
-  GBMD_CUDA(c, cudaMemsetAsync(c->cell_fill, 0, sizeof(int32_t) * (g.ncells + 1), s));
-  k_scatter<<<nblk(n, 256), 256, 0, s>>>(n, c->cell_of, c->cell_start, c->cell_fill, c->order);
+  k_wrap_bin<<<nblk(n, 256), 256, 0, s>>>(n, c->X(), c->Y(), c->Z(), b, c->cell_of, c->cell_fill, c->d_err, gate);
+  if ((rc = scan(c, c->cell_fill, c->cell_start, g.ncells, gate))) return rc;
+  if ((rc = zero_fill())) return rc;
+  k_scatter<<<nblk(n, 256), 256, 0, s>>>(n, c->cell_of, c->cell_start, c->cell_fill, c->order, gate);
   k_cell_rank<<<nblk(g.ncells * 32, 256), 256, 0, s>>>(g.ncells, c->cell_start, c->order, c->ID(), c->USER(),
-                                                        c->src);
+                                                        c->src, gate);
   GatherArgs ga;
   const int o = c->cur, os = c->cur_s;
   ga.r0 = c->rbuf[o]; ga.r1 = c->rbuf[o ^ 1];
@@ -494,11 +555,15 @@ int rebuild(gbmd_context* c, bool check_capacity) {
   ga.u0 = c->userb[os]; ga.u1 = c->userb[os ^ 1];
   ga.ep0 = c->ep; ga.ep1 = c->stage;
   ga.cap = c->cap;
-  k_gather<<<nblk(n, 256), 256, 0, s>>>(n, c->src, ga, c->cell_of, g.nc[0], g.nc[1], c->cellpack);
-  GBMD_CUDA(c, cudaMemcpyAsync(c->ep, c->stage, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-  c->cur ^= 1;
-  c->cur_s ^= 1;
-  launch_posf(c);
+  k_gather<<<nblk(n, 256), 256, 0, s>>>(n, c->src, ga, c->cell_of, g.nc[0], g.nc[1], c->cellpack, gate);
+  if (gate) {
+    k_copy_back<<<nblk(n, 256), 256, 0, s>>>(n, ga, gate);
+  } else {
+    GBMD_CUDA(c, cudaMemcpyAsync(c->ep, c->stage, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    c->cur ^= 1;
+    c->cur_s ^= 1;
+  }
+  launch_posf(c, gate);
   if (c->maxnb <= 0) {
     // first estimate: 1.35x the mean count of an ideal gas at this density
     const double V = g.L[0] * g.L[1] * g.L[2];
@@ -506,10 +571,10 @@ int rebuild(gbmd_context* c, bool check_capacity) {
     int m = (int)(mean * 1.35) + 16;
     c->maxnb = ((m + c->tpa - 1) / c->tpa) * c->tpa;
   }
-  rc = build_list(c);
+  rc = build_list(c, gate);
   if (rc) return rc;
   c->list_valid = true;
-  c->list_builds++;
+  if (!gate) c->list_builds++;
   if (check_capacity) {
     rc = sync_error_word(c);
     if (c->h_err[ERRW_FLAGS] & GBMD_DEVERR_LOST_ATOM)
@@ -519,8 +584,8 @@ int rebuild(gbmd_context* c, bool check_capacity) {
     if (maxc > c->maxnb) {
       int m = (int)(maxc * 1.2) + 8;
       c->maxnb = ((m + c->tpa - 1) / c->tpa) * c->tpa;
-      GBMD_CUDA(c, cudaMemsetAsync(c->d_err, 0, sizeof(int) * 8, s));
-      rc = build_list(c);
+      GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_FLAGS, 0, sizeof(int) * 2, s));  // flags, max count
+      rc = build_list(c, nullptr);
       if (rc) return rc;
       rc = sync_error_word(c);
       if (c->h_err[ERRW_FLAGS] & GBMD_DEVERR_NBR_OVERFLOW)

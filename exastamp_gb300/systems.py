@@ -135,10 +135,21 @@ def lj_binary_voids(n: int = 16_777_216, density: float = 1.2, frac_a: float = 0
     while need > 0:
         cand = rng.uniform(0.0, L, (int(need * 1.1) + 16, 3))
         keep = np.ones(len(cand), bool)
+        # only the periodic slab |x - cx| < void_r can hit a void: candidates
+        # sorted by x, each slab is one or two index ranges
+        order = np.argsort(cand[:, 0], kind="stable")
+        xs = cand[order, 0]
         for c in centers:
-            d = cand - c
+            parts = []
+            for a, b in ((c[0] - void_r, c[0] + void_r), (c[0] - void_r + L, c[0] + void_r + L),
+                         (c[0] - void_r - L, c[0] + void_r - L)):
+                a, b = max(a, 0.0), min(b, L)
+                if a < b:
+                    parts.append(order[np.searchsorted(xs, a):np.searchsorted(xs, b, side="right")])
+            sel = np.concatenate(parts)
+            d = cand[sel] - c
             d -= L * np.round(d / L)
-            keep &= (d * d).sum(1) > void_r * void_r
+            keep[sel[(d * d).sum(1) <= void_r * void_r]] = False
         cand = cand[keep][:need]
         out.append(cand)
         need -= len(cand)

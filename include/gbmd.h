@@ -172,15 +172,28 @@ int gbmd_push_f_v(gbmd_context* ctx, double dt, double dt_scale);
  * r += a*dt'^2/2; tolF > 0 clips each acceleration component first. */
 int gbmd_push_min(gbmd_context* ctx, double dt, double dt_scale, double tolF);
 
+/* rebuild_every value: rebuild when some atom moved more than skin/2 since
+ * the last rebuild (particle_displ_over, data/config/config_move_particles.msp
+ * L19-22, L116-118), tested every step on the device. */
+#define GBMD_REBUILD_ON_DISPLACEMENT (-1)
+
 /* verlet_nve for nsteps (config_numerical_schemes.msp L44-52): first half,
- * rebuild every `rebuild_every` steps (0 = never), forces, second half.
+ * rebuild every `rebuild_every` steps (0 = never, GBMD_REBUILD_ON_DISPLACEMENT
+ * = on the displacement trigger), forces, second half.
  * thermo_every > 0 writes the 27-double reduction every thermo_every steps
  * into thermo_out (rows of 27, step 0 first); thermo_out may be NULL.
- * use_graph != 0 captures a rebuild-interval chunk in a CUDA graph. */
+ * use_graph != 0 replays chunks of steps from a CUDA graph: 2*rebuild_every
+ * steps, or with the trigger thermo_every steps when even (20 without
+ * thermo); the remaining steps are launched one by one. */
 int gbmd_run_nve(gbmd_context* ctx, int nsteps, double dt, int rebuild_every, int thermo_every,
                  double* thermo_out, int use_graph);
-/* Minimiser: nsteps of compute forces + push_min (r += a dt^2/2, clipped). */
+/* Minimiser: nsteps of compute forces + push_min (r += a dt^2/2, clipped);
+ * rebuild_every as gbmd_run_nve. */
 int gbmd_run_minimize(gbmd_context* ctx, int nsteps, double dt, double tolF, int rebuild_every);
+/* Number of neighbour-list builds since the context was created, including
+ * the displacement-triggered ones (counted on the device, folded in when
+ * gbmd_run_nve / gbmd_run_minimize return). */
+int gbmd_list_builds(const gbmd_context* ctx, int64_t* count);
 
 /* ---- thermodynamic state ---------------------------------------------------
  * simulation_thermodynamic_state (src/thermo_state/

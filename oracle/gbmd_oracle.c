@@ -850,55 +850,131 @@ static void compute_pair_forces(int64_t n, const double* x, const double* y, con
                        fy, fz, ep, vir);
 }
 
+/* list builds of the last orc_run_nve / orc_run_minimize call */
+static int64_t g_list_builds = 0;
+
+int64_t orc_last_list_builds(void) { return g_list_builds; }
+
+/* particle_displ_over (config_move_particles.msp L19-22, L116-118): 1 when
+ * some atom moved more than skin/2 since rref was taken; |dr|^2 summed x, y,
+ * z in that order (the file is compiled without contraction). */
+static int displ_over(int64_t n, const double* x, const double* y, const double* z, const double* rref,
+                      double skin) {
+  const double thr = 0.5 * skin, thr2 = thr * thr;
+  int over = 0;
+#pragma omp parallel for schedule(static) reduction(| : over)
+  for (int64_t i = 0; i < n; ++i) {
+    const double dx = x[i] - rref[i], dy = y[i] - rref[n + i], dz = z[i] - rref[2 * n + i];
+    if (dx * dx + dy * dy + dz * dz > thr2) over = 1;
+  }
+  return over;
+}
+
+static void take_rref(int64_t n, const double* x, const double* y, const double* z, double* rref) {
+  memcpy(rref, x, sizeof(double) * (size_t)n);
+  memcpy(rref + n, y, sizeof(double) * (size_t)n);
+  memcpy(rref + 2 * n, z, sizeof(double) * (size_t)n);
+}
+
+/* the list update of one step: every `every` steps, or on the displacement
+ * trigger when every == -1 */
+static int maybe_rebuild(orc_list* l, int64_t n, double* x, double* y, double* z, const uint64_t* id,
+                         const double lo[3], const double hi[3], double R, double skin, int every, int s,
+                         double* rref) {
+  int rc = 0;
+  if (every > 0 && s % every == 0) {
+    rc = list_rebuild(l, n, x, y, z, id, lo, hi, R);
+    ++g_list_builds;
+  } else if (every == -1 && displ_over(n, x, y, z, rref, skin)) {
+    rc = list_rebuild(l, n, x, y, z, id, lo, hi, R);
+    take_rref(n, x, y, z, rref);
+    ++g_list_builds;
+  }
+  return rc;
+}
+
+static double pot_rcut(int pot_kind, const void* pot) {
+  if (pot_kind == ORC_POT_LJ) return ((const orc_lj_params*)pot)->rcut;
+  if (pot_kind == ORC_POT_LJ_MULTI) return ((const orc_lj_multi_params*)pot)->rcut_max;
+  return ((const orc_eam_pot*)pot)->rcut;
+}
+
+/* Forces of the bound potential turned into accelerations: the compute_force
+ * node of the step graph (eam_alloy = density, embedding, force passes). */
+static void all_forces(int64_t n, const double* x, const double* y, const double* z, const uint8_t* type,
+                       const orc_list* l, const double L[3], int pot_kind, const void* pot, const double* masses,
+                       double* rho, double* ax, double* ay, double* az, double* ep, double* vir) {
+  if (pot_kind == ORC_POT_EAM) {
+    const orc_eam_pot* p = (const orc_eam_pot*)pot;
+    orc_eam_density(n, x, y, z, type, l->off, l->nbr, l->img, L, &p->t, p->rcut, rho);
+    for (int64_t i = 0; i < n; ++i) ep[i] = 0.0;
+    orc_eam_embed(n, type, &p->t, rho, ep);
+    orc_eam_force(n, x, y, z, type, l->off, l->nbr, l->img, L, &p->t, p->rcut, rho, ax, ay, az, ep, vir);
+  } else {
+    compute_pair_forces(n, x, y, z, type, l, L, pot_kind, pot, ax, ay, az, ep, vir);
+  }
+  orc_force_to_accel(n, ax, ay, az, type, masses);
+}
+
 int orc_run_nve(int64_t n, double* x, double* y, double* z, double* vx, double* vy, double* vz,
                 double* ax, double* ay, double* az, double* ep, const uint8_t* type, const uint64_t* id,
                 const double* masses, const double lo[3], const double hi[3], int pot_kind,
                 const void* pot, double skin, double dt, int nsteps, int rebuild_every,
                 double* thermo_out) {
   const double L[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
-  double rcut;
-  if (pot_kind == ORC_POT_LJ) rcut = ((const orc_lj_params*)pot)->rcut;
-  else if (pot_kind == ORC_POT_LJ_MULTI) rcut = ((const orc_lj_multi_params*)pot)->rcut_max;
-  else rcut = ((const orc_eam_pot*)pot)->rcut;
-  const double R = rcut + skin;
+  const double R = pot_rcut(pot_kind, pot) + skin;
   orc_list l = {(int64_t*)malloc(sizeof(int64_t) * (size_t)(n + 1)), NULL, NULL, 0};
   double* rho = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
   /* per-atom virial, summed by the thermo reduction (mechanics grid flavor) */
   double* vir = thermo_out ? (double*)calloc(9 * (size_t)(n > 0 ? n : 1), sizeof(double)) : NULL;
+  double* rref = (double*)malloc(sizeof(double) * 3 * (size_t)(n > 0 ? n : 1));
   int rc = 0;
-#define FORCES()                                                                                   \
-  do {                                                                                             \
-    if (pot_kind == ORC_POT_EAM) {                                                                 \
-      const orc_eam_pot* ep_ = (const orc_eam_pot*)pot;                                            \
-      orc_eam_density(n, x, y, z, type, l.off, l.nbr, l.img, L, &ep_->t, ep_->rcut, rho);          \
-      for (int64_t i_ = 0; i_ < n; ++i_) ep[i_] = 0.0;                                             \
-      orc_eam_embed(n, type, &ep_->t, rho, ep);                                                    \
-      orc_eam_force(n, x, y, z, type, l.off, l.nbr, l.img, L, &ep_->t, ep_->rcut, rho, ax, ay, az, \
-                    ep, vir);                                                                      \
-    } else {                                                                                       \
-      compute_pair_forces(n, x, y, z, type, &l, L, pot_kind, pot, ax, ay, az, ep, vir);           \
-    }                                                                                              \
-    orc_force_to_accel(n, ax, ay, az, type, masses);                                               \
-  } while (0)
-
+  g_list_builds = 1;
   if ((rc = list_rebuild(&l, n, x, y, z, id, lo, hi, R)) != 0) goto done;
-  FORCES();
+  take_rref(n, x, y, z, rref);
+  all_forces(n, x, y, z, type, &l, L, pot_kind, pot, masses, rho, ax, ay, az, ep, vir);
   if (thermo_out) orc_thermo(n, vx, vy, vz, ep, vir, type, masses, thermo_out);
   for (int s = 1; s <= nsteps; ++s) {
     orc_push_f_v_r(n, x, y, z, vx, vy, vz, ax, ay, az, dt, 1.0);
     orc_push_f_v(n, vx, vy, vz, ax, ay, az, dt, 0.5);
-    if (rebuild_every > 0 && s % rebuild_every == 0)
-      if ((rc = list_rebuild(&l, n, x, y, z, id, lo, hi, R)) != 0) goto done;
-    FORCES();
+    if ((rc = maybe_rebuild(&l, n, x, y, z, id, lo, hi, R, skin, rebuild_every, s, rref)) != 0) goto done;
+    all_forces(n, x, y, z, type, &l, L, pot_kind, pot, masses, rho, ax, ay, az, ep, vir);
     orc_push_f_v(n, vx, vy, vz, ax, ay, az, dt, 0.5);
     if (thermo_out) orc_thermo(n, vx, vy, vz, ep, vir, type, masses, thermo_out + 27 * s);
   }
-#undef FORCES
 done:
   free(l.off);
   free(l.nbr);
   free(l.img);
   free(rho);
   free(vir);
+  free(rref);
+  return rc;
+}
+
+int orc_run_minimize(int64_t n, double* x, double* y, double* z, double* ax, double* ay, double* az,
+                     double* ep, const uint8_t* type, const uint64_t* id, const double* masses,
+                     const double lo[3], const double hi[3], int pot_kind, const void* pot, double skin,
+                     double dt, double tolF, int nsteps, int rebuild_every) {
+  const double L[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+  const double R = pot_rcut(pot_kind, pot) + skin;
+  orc_list l = {(int64_t*)malloc(sizeof(int64_t) * (size_t)(n + 1)), NULL, NULL, 0};
+  double* rho = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+  double* rref = (double*)malloc(sizeof(double) * 3 * (size_t)(n > 0 ? n : 1));
+  int rc = 0;
+  g_list_builds = 1;
+  if ((rc = list_rebuild(&l, n, x, y, z, id, lo, hi, R)) != 0) goto done;
+  take_rref(n, x, y, z, rref);
+  for (int s = 1; s <= nsteps; ++s) {
+    all_forces(n, x, y, z, type, &l, L, pot_kind, pot, masses, rho, ax, ay, az, ep, NULL);
+    orc_push_min(n, x, y, z, ax, ay, az, type, masses, dt, 1.0, tolF);
+    if ((rc = maybe_rebuild(&l, n, x, y, z, id, lo, hi, R, skin, rebuild_every, s, rref)) != 0) goto done;
+  }
+done:
+  free(l.off);
+  free(l.nbr);
+  free(l.img);
+  free(rho);
+  free(rref);
   return rc;
 }

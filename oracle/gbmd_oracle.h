@@ -134,6 +134,19 @@ int orc_run_nve(int64_t n, double* x, double* y, double* z, double* vx, double* 
                 const void* pot, double skin, double dt, int nsteps, int rebuild_every,
                 double* thermo_out);
 
+/* The minimisation graph: forces, clipped push r += a*dt^2/2
+ * (push_vec3_2nd_order_xform_minimization.cpp L116-149), list rebuilt every
+ * rebuild_every steps.  Returns 0, or a negative code as orc_run_nve. */
+int orc_run_minimize(int64_t n, double* x, double* y, double* z, double* ax, double* ay, double* az,
+                     double* ep, const uint8_t* type, const uint64_t* id, const double* masses,
+                     const double lo[3], const double hi[3], int pot_kind, const void* pot, double skin,
+                     double dt, double tolF, int nsteps, int rebuild_every);
+
+/* list builds done by the last orc_run_nve / orc_run_minimize call (the
+ * initial build included); rebuild_every == -1 in either selects the
+ * displacement trigger: rebuild when some atom moved more than skin/2. */
+int64_t orc_last_list_builds(void);
+
 int orc_num_threads(void);
 
 #ifdef __cplusplus

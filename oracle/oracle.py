@@ -99,6 +99,9 @@ def lib():
         L.orc_thermo.argtypes = [i64, vp, vp, vp, vp, vp, vp, vp, vp]
         L.orc_run_nve.restype = i32
         L.orc_run_nve.argtypes = [i64] + [vp] * 15 + [i32, vp, dbl, dbl, i32, i32, vp]
+        L.orc_run_minimize.restype = i32
+        L.orc_run_minimize.argtypes = [i64] + [vp] * 12 + [i32, vp, dbl, dbl, dbl, i32, i32]
+        L.orc_last_list_builds.restype = i64
         L.orc_num_threads.restype = i32
         L.orc_eam_loss_grad.restype = dbl
         L.orc_eam_loss_grad.argtypes = [i64, vp, vp, vp, vp, vp, vp, vp, vp, dbl, vp, vp, vp, dbl, dbl, vp, vp, vp]
@@ -347,6 +350,32 @@ def run_nve(state, masses, lo, hi, pot_kind, pot, skin, dt, nsteps, rebuild_ever
     if rc != 0:
         raise RuntimeError("oracle run_nve failed with code %d" % rc)
     return th
+
+
+def _pot_ptr(pot_kind, pot):
+    if pot_kind == POT_LJ:
+        return C.addressof(pot)
+    if pot_kind == POT_LJ_MULTI:
+        return C.addressof(pot.s)
+    return C.addressof(pot.pot)
+
+
+def run_minimize(state, masses, lo, hi, pot_kind, pot, skin, dt, tolF, nsteps, rebuild_every):
+    """Clipped minimiser (forces, r += a*dt^2/2, rebuild every
+    `rebuild_every`) in place on `state`."""
+    n = len(state["x"])
+    s = state
+    rc = lib().orc_run_minimize(n, _p(s["x"]), _p(s["y"]), _p(s["z"]), _p(s["ax"]), _p(s["ay"]), _p(s["az"]),
+                                _p(s["ep"]), _p(s["type"]), _p(s["id"]), _p(_f64(masses)), _p(_f64(lo)),
+                                _p(_f64(hi)), pot_kind, _pot_ptr(pot_kind, pot), float(skin), float(dt),
+                                float(tolF), int(nsteps), int(rebuild_every))
+    if rc != 0:
+        raise RuntimeError("oracle run_minimize failed with code %d" % rc)
+
+
+def last_list_builds():
+    """List builds of the last run_nve / run_minimize (initial build included)."""
+    return int(lib().orc_last_list_builds())
 
 
 def multi_params(eps, sig, rc, rcut_max):

@@ -236,3 +236,42 @@ def test_oracle_nve_conserves_energy(oracle):
     drift = abs(etot[-1] - etot[0]) / s.n
     assert drift < 2e-3
     assert np.allclose(th[:, 18:21], 0.0, atol=1e-9)
+
+
+def test_oracle_minimiser_lowers_energy_and_clips(oracle):
+    """Clipped minimiser on an overlapping random binary mixture: the
+    potential energy falls and no step moves an atom further than
+    tolF*dt^2/2 per component."""
+    s = S.lj_binary_voids(n=3000, density=1.2, frac_a=0.8, nvoids=1, void_r=2.0, seed=11)
+    eps, sig, rc = S.kob_andersen_tables()
+    prm = oracle.multi_params(eps, sig, rc, float(rc.max()))
+    st = s.state()
+
+    def epot(st):
+        x, y, z = st["x"].copy(), st["y"].copy(), st["z"].copy()
+        oracle.wrap(x, y, z, s.lo, s.hi)
+        nl = oracle.build_neighbors(x, y, z, s.id, s.lo, s.hi, float(rc.max()) + 0.3)
+        return oracle.lj_multi_force(x, y, z, s.type, nl, s.L, eps, sig, rc, float(rc.max()))[3].sum()
+
+    e0 = epot(st)
+    x0 = st["x"].copy()
+    oracle.run_minimize(st, s.masses, s.lo, s.hi, oracle.POT_LJ_MULTI, prm, 0.3, 0.002, 1e3, 1, 0)
+    step = np.abs(st["x"] - x0).max()
+    assert step <= 1e3 * 0.002 ** 2 / 2 * (1 + 1e-12)
+    oracle.run_minimize(st, s.masses, s.lo, s.hi, oracle.POT_LJ_MULTI, prm, 0.3, 0.002, 1e3, 40, 10)
+    assert epot(st) < 0.5 * e0
+
+
+def test_oracle_displacement_trigger(oracle):
+    """Rebuilding on the skin/2 displacement trigger gives the trajectory of
+    rebuilding every step (lists differ only by pairs beyond the cutoff),
+    with far fewer builds."""
+    s = S.lj_fcc(ncell=6, density=0.8442, T=1.5, seed=5)
+    prm = oracle.LJParams(1.0, 1.0, 2.5)
+    st1, st2 = s.state(), s.state()
+    th1 = oracle.run_nve(st1, s.masses, s.lo, s.hi, oracle.POT_LJ, prm, 0.3, 0.005, 150, 1)
+    n1 = oracle.last_list_builds()
+    th2 = oracle.run_nve(st2, s.masses, s.lo, s.hi, oracle.POT_LJ, prm, 0.3, 0.005, 150, -1)
+    n2 = oracle.last_list_builds()
+    assert n1 == 151 and 2 < n2 < 40
+    assert np.allclose(th1, th2, rtol=1e-9, atol=1e-9 * np.abs(th1).max())
