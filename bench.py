@@ -83,6 +83,7 @@ def parse():
     p.add_argument("--no-batch", action="store_true", help="skip the batched-replica and adjoint sections")
     p.add_argument("--lanes", type=int, default=0, help="lanes per atom (0: autotune)")
     p.add_argument("--block", type=int, default=0)
+    p.add_argument("--vec", type=int, default=1, help="list entries per lane per load with --lanes (1 or 4)")
     p.add_argument("--ncell", type=int, default=0,
                    help="override the unit cells per edge (small profiling cases of the same workload)")
     a = p.parse_args()
@@ -374,6 +375,7 @@ def main():
     ctx.upload_system(s)
     bind_potential(ctx, w)
     t_min = None
+    tuned = None
     if w.get("min_steps"):
         # random positions overlap: clipped minimiser first (FP64 forces)
         ctx.set_precision(False)
@@ -382,11 +384,11 @@ def main():
         t_min = time.perf_counter() - t0
     ctx.set_precision(args.precision == "mixed")
     if args.lanes:
-        ctx.set_launch(args.lanes, args.block or 128)
+        ctx.set_launch(args.lanes, args.block or 128, args.vec)
     else:
         from exastamp_gb300 import autotune
-        lanes, block, _ = autotune.tune(ctx, key="%s-%s" % (args.workload, args.precision))
-        ctx.set_launch(lanes, block)
+        lanes, vec, block, tuned = autotune.tune(ctx, key="%s-%s" % (args.workload, args.precision))
+        ctx.set_launch(lanes, block, vec)
     R, dt = args.rebuild_every, w["dt"]
     # fixed interval: thermo at the end of each 2R-step graph chunk; with the
     # displacement trigger (R = -1) every 20 steps
@@ -431,13 +433,16 @@ def main():
                       "rebuild_every": R if R >= 0 else "on displacement > skin/2",
                       "list_builds_in_timed_region": rebuilds,
                       "neighbours_per_atom": npairs / s.n, "cells": nc.tolist(),
-                      "lanes_per_atom": ctx.get_launch()[0], "block": ctx.get_launch()[1],
+                      "lanes_per_atom": ctx.get_launch_ex()[0], "list_entries_per_load": ctx.get_launch_ex()[1],
+                      "block": ctx.get_launch_ex()[2],
                       "parallelism": "replicas" if ws > 1 else "single-gpu",
                       "l2": "inputs larger than L2 (neighbour list %.2f GB)" % (npairs * 4 / 1e9)
                       if npairs * 4 > 129e6 else "inputs resident in L2 (not flushed)",
                       "cuda_graph": True},
            "gpu_launches": gpu_launches, "clocks": clocks,
            "nve_energy_drift_per_1000_steps_per_atom": drift}
+    if tuned:
+        out["autotune_density_plus_pair_ms"] = tuned
     if t_min is not None:
         out["minimiser"] = {"steps": w["min_steps"], "step": MIN_DT, "clip": MIN_TOLF, "precision": "fp64",
                             "seconds": t_min}

@@ -72,6 +72,8 @@ def lib(path: str = LIB_PATH):
             "gbmd_set_precision": ([vp, i32], i32),
             "gbmd_set_launch": ([vp, i32, i32], i32),
             "gbmd_get_launch": ([vp, P(i32), P(i32)], i32),
+            "gbmd_set_launch_ex": ([vp, i32, i32, i32], i32),
+            "gbmd_get_launch_ex": ([vp, P(i32), P(i32), P(i32)], i32),
             "gbmd_set_skin": ([vp, dbl], i32),
             "gbmd_build_neighbors": ([vp], i32),
             "gbmd_export_pairs": ([vp, i64, vp, vp, vp, P(i64)], i32),
@@ -212,13 +214,20 @@ class Context:
     def set_precision(self, mixed: bool):
         self._chk(self._L.gbmd_set_precision(self.h, PRECISION_MIXED if mixed else PRECISION_FP64))
 
-    def set_launch(self, lanes_per_atom, block):
-        self._chk(self._L.gbmd_set_launch(self.h, int(lanes_per_atom), int(block)))
+    def set_launch(self, lanes_per_atom, block, entries_per_load=1):
+        self._chk(self._L.gbmd_set_launch_ex(self.h, int(lanes_per_atom), int(entries_per_load), int(block)))
 
     def get_launch(self):
+        """(lanes per atom, threads per block)."""
         t, b = C.c_int(), C.c_int()
         self._chk(self._L.gbmd_get_launch(self.h, C.byref(t), C.byref(b)))
         return t.value, b.value
+
+    def get_launch_ex(self):
+        """(lanes per atom, list entries per load, threads per block)."""
+        t, v, b = C.c_int(), C.c_int(), C.c_int()
+        self._chk(self._L.gbmd_get_launch_ex(self.h, C.byref(t), C.byref(v), C.byref(b)))
+        return t.value, v.value, b.value
 
     def set_skin(self, skin):
         self._chk(self._L.gbmd_set_skin(self.h, float(skin)))

@@ -2,7 +2,9 @@
 
 The knobs are the lanes that share one atom's neighbour list (1-16; more
 lanes give more parallelism for small systems, fewer lanes avoid the
-per-atom shuffle reduction for large ones) and the threads per block.  Each
+per-atom shuffle reduction for large ones), the list entries each lane reads
+per load (1, or 4 in one 16-byte load with at most 4 lanes) and the threads
+per block.  Each
 candidate is timed with gbmd_profile_step (CUDA events on the context's
 stream, density + final pair kernel) and the fastest is kept.  Results are
 cached in a JSON file keyed by GPU name, workload key and atom count
@@ -14,6 +16,7 @@ import json
 import os
 
 LANES = (1, 2, 4, 8, 16)
+VECS = (1, 4)
 BLOCKS = (128, 256)
 
 
@@ -79,27 +82,31 @@ def tune_batch(batch, key: str, blocks=(128, 256, 512), stencils=(1, 2), adjoint
     return best[1], best[2], timings
 
 
-def tune(ctx, key: str, lanes=LANES, blocks=BLOCKS, reps: int = 3, use_cache: bool = True):
-    """Return (lanes, block, timings) for this context's system and potential."""
+def tune(ctx, key: str, lanes=LANES, blocks=BLOCKS, vecs=VECS, reps: int = 3, use_cache: bool = True):
+    """Return (lanes, entries per load, block, timings) for this context's
+    system and potential."""
     n = ctx.n
-    ck = "%s|%s|%d" % (_gpu_name(), key, n)
+    ck = "%s|%s|%d|v" % (_gpu_name(), key, n)
     cache = _load() if use_cache else {}
     if ck in cache:
         e = cache[ck]
-        return int(e["lanes"]), int(e["block"]), e.get("timings", {})
+        return int(e["lanes"]), int(e["vec"]), int(e["block"]), e.get("timings", {})
     timings = {}
     best = None
     for t in lanes:
-        for b in blocks:
-            if b % t:
+        for v in vecs:
+            if v > 1 and t > 4:
                 continue
-            ctx.set_launch(t, b)
-            prof = ctx.profile_step(reps=reps)
-            ms = prof["density"] + prof["pair"]
-            timings["%dx%d" % (t, b)] = ms
-            if best is None or ms < best[0]:
-                best = (ms, t, b)
-    cache[ck] = {"lanes": best[1], "block": best[2], "timings": timings}
+            for b in blocks:
+                if b % t:
+                    continue
+                ctx.set_launch(t, b, v)
+                prof = ctx.profile_step(reps=reps)
+                ms = prof["density"] + prof["pair"]
+                timings["%dx%dx%d" % (t, v, b)] = ms
+                if best is None or ms < best[0]:
+                    best = (ms, t, v, b)
+    cache[ck] = {"lanes": best[1], "vec": best[2], "block": best[3], "timings": timings}
     if use_cache:
         _store(cache)
-    return best[1], best[2], timings
+    return best[1], best[2], best[3], timings

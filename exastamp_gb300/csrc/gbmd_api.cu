@@ -49,10 +49,12 @@ static void free_atoms(gbmd_context* c) {
   }
   cudaFree(c->ep); cudaFree(c->vir); cudaFree(c->cellpack); cudaFree(c->cell_of);
   cudaFree(c->order); cudaFree(c->src); cudaFree(c->fpf); cudaFree(c->fpd); cudaFree(c->epf);
+  cudaFree(c->pfp);
   cudaFree(c->stage); cudaFree(c->rref); cudaFree(c->nnb); cudaFree(c->d_part);
   c->ep = c->vir = nullptr;
   c->cellpack = c->cell_of = c->order = c->src = nullptr;
   c->fpf = c->epf = nullptr;
+  c->pfp = nullptr;
   c->fpd = c->stage = c->rref = nullptr;
   c->nnb = nullptr;
   c->d_part = nullptr;
@@ -81,6 +83,7 @@ int ensure_atom_capacity(gbmd_context* c, int64_t n) {
   GBMD_CUDA(c, cudaMalloc(&c->src, sizeof(int32_t) * cap));
   GBMD_CUDA(c, cudaMalloc(&c->fpf, sizeof(float) * cap));
   GBMD_CUDA(c, cudaMalloc(&c->epf, sizeof(float) * cap));
+  GBMD_CUDA(c, cudaMalloc(&c->pfp, sizeof(float4) * cap));
   GBMD_CUDA(c, cudaMalloc(&c->fpd, sizeof(double) * cap));
   GBMD_CUDA(c, cudaMalloc(&c->stage, sizeof(double) * 9 * cap));
   GBMD_CUDA(c, cudaMalloc(&c->rref, d3));
@@ -634,15 +637,19 @@ int gbmd_set_precision(gbmd_context* c, int precision) {
   return GBMD_OK;
 }
 
-int gbmd_set_launch(gbmd_context* c, int tpa, int block) {
+int gbmd_set_launch_ex(gbmd_context* c, int tpa, int vec, int block) {
   if (!c) return GBMD_ERR_INVALID;
   if (tpa != 1 && tpa != 2 && tpa != 4 && tpa != 8 && tpa != 16)
     return set_error(c, GBMD_ERR_INVALID, "lanes per atom must be 1,2,4,8 or 16");
+  if (vec != 1 && !(vec == 4 && tpa <= 4))
+    return set_error(c, GBMD_ERR_INVALID, "entries per load must be 1, or 4 with at most 4 lanes per atom");
   if (block < 32 || block > 256 || block % 32 || block % tpa)
     return set_error(c, GBMD_ERR_INVALID, "block must be a multiple of 32 in [32,256]");
-  if (tpa != c->tpa) {
+  if (tpa != c->tpa || vec != c->vec) {
     c->tpa = tpa;
-    if (c->maxnb > 0) c->maxnb = ((c->maxnb + tpa - 1) / tpa) * tpa;
+    c->vec = vec;
+    const int W = list_width(c);
+    if (c->maxnb > 0) c->maxnb = ((c->maxnb + W - 1) / W) * W;
     invalidate_list(c);
   }
   c->block = block;
@@ -650,9 +657,22 @@ int gbmd_set_launch(gbmd_context* c, int tpa, int block) {
   return GBMD_OK;
 }
 
+int gbmd_set_launch(gbmd_context* c, int tpa, int block) {
+  if (!c) return GBMD_ERR_INVALID;
+  return gbmd_set_launch_ex(c, tpa, 1, block);
+}
+
 int gbmd_get_launch(const gbmd_context* c, int* tpa, int* block) {
   if (!c) return GBMD_ERR_INVALID;
   if (tpa) *tpa = c->tpa;
+  if (block) *block = c->block;
+  return GBMD_OK;
+}
+
+int gbmd_get_launch_ex(const gbmd_context* c, int* tpa, int* vec, int* block) {
+  if (!c) return GBMD_ERR_INVALID;
+  if (tpa) *tpa = c->tpa;
+  if (vec) *vec = c->vec;
   if (block) *block = c->block;
   return GBMD_OK;
 }
@@ -802,6 +822,7 @@ static int one_step(gbmd_context* c, double dt, const StepPlan& p, bool check, d
 static int capture_graph(gbmd_context* c, double dt, int R, int G, bool thermo_end) {
   drop_graph(c);
   cudaGraph_t g;
+  const int64_t builds = c->list_builds;  // capturing runs nothing
   GBMD_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   int rc = GBMD_OK;
   for (int l = 1; l <= G && rc == GBMD_OK; ++l) {
@@ -809,6 +830,7 @@ static int capture_graph(gbmd_context* c, double dt, int R, int G, bool thermo_e
     rc = one_step(c, dt, p, false, nullptr);
   }
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  c->list_builds = builds;
   if (rc) {
     if (e == cudaSuccess) cudaGraphDestroy(g);
     return rc;
@@ -824,6 +846,7 @@ static int capture_graph(gbmd_context* c, double dt, int R, int G, bool thermo_e
   c->graph_key_n = c->n;
   c->graph_key_maxnb = c->maxnb;
   c->graph_key_tpa = c->tpa;
+  c->graph_key_vec = c->vec;
   c->graph_key_block = c->block;
   c->graph_key_prec = c->precision;
   return GBMD_OK;
@@ -832,7 +855,8 @@ static int capture_graph(gbmd_context* c, double dt, int R, int G, bool thermo_e
 static bool graph_matches(const gbmd_context* c, double dt, int R, int G, bool thermo_end) {
   return c->graph_exec && c->graph_rebuild_every == R && c->graph_chunk == G && c->graph_dt == dt &&
          c->graph_thermo_end == (thermo_end ? 1 : 0) && c->graph_key_n == c->n && c->graph_key_maxnb == c->maxnb &&
-         c->graph_key_tpa == c->tpa && c->graph_key_block == c->block && c->graph_key_prec == c->precision;
+         c->graph_key_tpa == c->tpa && c->graph_key_vec == c->vec && c->graph_key_block == c->block &&
+         c->graph_key_prec == c->precision;
 }
 
 int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int thermo_every, double* thermo_out,
@@ -882,6 +906,7 @@ int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int 
     if (graph_ok && (s - 1) % G == 0 && s + G - 1 < nsteps) {
       if (!graph_matches(c, dt, R, G, want_thermo) && (rc = capture_graph(c, dt, R, G, want_thermo))) return rc;
       GBMD_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
+      if (R > 0) c->list_builds += G / R;  // replayed rebuilds (trigger ones are counted on the device)
       if (want_thermo)
         GBMD_CUDA(c, cudaMemcpyAsync(rows + 27 * (size_t)((s + G - 1) / thermo_every), c->d_thermo,
                                      sizeof(double) * 27, cudaMemcpyDeviceToDevice, c->stream));

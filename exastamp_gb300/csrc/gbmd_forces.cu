@@ -51,9 +51,9 @@ __global__ void __launch_bounds__(256) k_lj(PairArgs A, LJSingle P, const LJPair
     double4_32a pi = make_double4_32a(0., 0., 0., 0.);
     if (live) pi = A.posd[i];
     ti = (int)pi.w;
-    const uint32_t* p = A.nbr + (size_t)i * T + lane;
-    for (int k = lane; k < nn; k += T, p += A.stride) {
-      const uint32_t ent = __ldg(p);
+    const uint32_t* row = A.nbr + (size_t)i * A.W;
+    for (int k = lane; k < nn; k += T) {
+      const uint32_t ent = __ldg(row + (size_t)(k >> A.wsh) * A.stride + (k & (A.W - 1)));
       const uint32_t j = ent & GBMD_IDX_MASK, code = ent >> GBMD_IDX_BITS;
       const double4_32a pj = A.posd[j];
       double Sx, Sy, Sz, dx, dy, dz;
@@ -126,9 +126,9 @@ __global__ void __launch_bounds__(256) k_eam_rho(PairArgs A, EamDev E, double* _
     double4_32a pi = make_double4_32a(0., 0., 0., 0.);
     if (live) pi = A.posd[i];
     const int ti = (int)pi.w;
-    const uint32_t* p = A.nbr + (size_t)i * T + lane;
-    for (int k = lane; k < nn; k += T, p += A.stride) {
-      const uint32_t ent = __ldg(p);
+    const uint32_t* row = A.nbr + (size_t)i * A.W;
+    for (int k = lane; k < nn; k += T) {
+      const uint32_t ent = __ldg(row + (size_t)(k >> A.wsh) * A.stride + (k & (A.W - 1)));
       const uint32_t j = ent & GBMD_IDX_MASK, code = ent >> GBMD_IDX_BITS;
       const double4_32a pj = A.posd[j];
       double Sx, Sy, Sz, dx, dy, dz;
@@ -183,9 +183,9 @@ __global__ void __launch_bounds__(256) k_eam_force(PairArgs A, EamDev E, const d
       fpi = fpd[i];
     }
     const int ti = (int)pi.w;
-    const uint32_t* p = A.nbr + (size_t)i * T + lane;
-    for (int k = lane; k < nn; k += T, p += A.stride) {
-      const uint32_t ent = __ldg(p);
+    const uint32_t* row = A.nbr + (size_t)i * A.W;
+    for (int k = lane; k < nn; k += T) {
+      const uint32_t ent = __ldg(row + (size_t)(k >> A.wsh) * A.stride + (k & (A.W - 1)));
       const uint32_t j = ent & GBMD_IDX_MASK, code = ent >> GBMD_IDX_BITS;
       const double4_32a pj = A.posd[j];
       double Sx, Sy, Sz, dx, dy, dz;
@@ -239,7 +239,10 @@ __global__ void __launch_bounds__(256) k_eam_force(PairArgs A, EamDev E, const d
 static PairArgs make_args(gbmd_context* c, const ForceFlags& f) {
   PairArgs A;
   A.n = c->n;
-  A.stride = c->npad * c->tpa;
+  A.W = list_width(c);
+  A.wsh = 0;
+  while ((1 << A.wsh) < A.W) ++A.wsh;
+  A.stride = c->npad * A.W;
   A.nbr = c->nbr;
   A.nnb = c->nnb;
   A.maxnb = c->maxnb;

@@ -122,6 +122,7 @@ struct gbmd_context {
   int32_t* order = nullptr;               // scratch: atoms scattered by cell
   int32_t* src = nullptr;                 // scratch: new position -> old position
   float* fpf = nullptr;                   // EAM F'(rho) FP32 (mixed)
+  float4* pfp = nullptr;                  // single-element EAM: FP32 position with F'(rho) in w (mixed)
   double* fpd = nullptr;                  // EAM rho_dEmb FP64
   double* stage = nullptr;                // 9n staging for host<->device reorders
   double* rref = nullptr;                 // 3n positions at the last rebuild (displacement trigger)
@@ -152,8 +153,9 @@ struct gbmd_context {
   uint32_t* nbr = nullptr;
   int32_t* nnb = nullptr;
   int64_t nbr_cap = 0;          // entries allocated
-  int maxnb = 0;                // per-atom capacity (multiple of tpa)
+  int maxnb = 0;                // per-atom capacity (multiple of tpa * vec)
   int tpa = 4;                  // lanes per atom (autotuned)
+  int vec = 1;                  // list entries per lane per load (1 or 4, mixed kernels; autotuned)
   int block = 128;              // threads per block (autotuned)
   double skin = 0.0, rlist = 0.0;
   bool list_valid = false;
@@ -191,7 +193,7 @@ struct gbmd_context {
   double graph_dt = 0.0;
   int graph_thermo_end = 0;
   int64_t graph_key_n = -1;
-  int graph_key_maxnb = -1, graph_key_tpa = -1, graph_key_block = -1, graph_key_prec = -1;
+  int graph_key_maxnb = -1, graph_key_tpa = -1, graph_key_block = -1, graph_key_prec = -1, graph_key_vec = -1;
 };
 
 // ---------------------------------------------------------------------------
@@ -305,6 +307,11 @@ __device__ __forceinline__ double exact_d2(double xi, double yi, double zi, doub
   dz = __dsub_rn(__dadd_rn(zj, sz), zi);
   return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
+
+// Words per list row of one atom: the T lanes of an atom each read `vec`
+// adjacent entries, so row r of atom i holds entries r*W .. r*W+W-1 at
+// nbr[r * npad * W + i * W + ...].
+inline int list_width(const gbmd_context* c) { return c->tpa * c->vec; }
 
 __device__ __forceinline__ size_t nbr_slot(int64_t i, int k, int T, int64_t stride) {
   return (size_t)(k / T) * (size_t)stride + (size_t)i * T + (k % T);

@@ -11,9 +11,12 @@
 // results are converted to FP64 once.  Cutoff membership matches FP64
 // exactly: pairs with FP32 d2 within 2^-12 of rcut^2 are re-tested in FP64.
 //
-// Loop structure (per list entry): one coalesced 4 B list load, one 16 B
-// position gather (plus 4 B F'(rho_j) for the EAM force pass), one 16 B
-// spline-knot gather per table; branch-free except the rare FP64 re-test.
+// Loop structure: each lane reads V list entries with one coalesced load
+// (V = 4: 16 B per lane, streamed past L1 so the gathers keep it), the next
+// row already in flight; per entry one 16 B position gather (single-element
+// EAM force pass: the position carries F'(rho_j) in w), one 16 B spline-knot
+// gather per table; branch-free except the rare FP64 re-test.  The V terms
+// of a row are added in FP32, the row sum goes into the compensated sum.
 // 1/r and r come from one rsqrt; the stencil offset decodes to an exact
 // float in two integer/FP ops per axis.
 #include "gbmd_pair_common.cuh"
@@ -38,49 +41,6 @@ __device__ __noinline__ bool exact_inside(const double4_32a* __restrict__ posd, 
   if (!(d2 <= rc2)) return false;
   return rc_pair <= 0.0 || sqrt(d2) <= rc_pair;
 }
-
-// List-entry prefetch: each thread streams its own list slots through a
-// ring of LIST_RING words in shared memory with cp.async (4 B, L1-cached),
-// LIST_RING - 1 entries ahead of the one being processed.  The slot refilled
-// at iteration `it` is the one consumed at `it - 1`, whose value is already
-// in a register.  Ring layout [slot][thread]: conflict-free.
-constexpr int LIST_RING = 8;
-
-__device__ __forceinline__ void cp_async4(uint32_t* smem, const uint32_t* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_ring() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(LIST_RING - 2) : "memory");
-}
-__device__ __forceinline__ void cp_async_drain() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
-static_assert((LIST_RING & (LIST_RING - 1)) == 0, "ring size must be a power of two");
-
-struct ListStream {
-  uint32_t* ring;          // this thread's column: ring[slot * blockDim.x]
-  const uint32_t* p;       // this thread's first list slot, then the next slot to prefetch
-  int64_t stride;
-  int niter;
-  __device__ __forceinline__ void start() {
-#pragma unroll
-    for (int d = 0; d < LIST_RING - 1; ++d) {
-      if (d < niter) cp_async4(ring + d * blockDim.x, p);
-      cp_async_commit();
-      p += stride;
-    }
-  }
-  __device__ __forceinline__ uint32_t next(int it) {
-    cp_async_wait_ring();
-    const unsigned u = (unsigned)it;
-    const uint32_t e = ring[(u & (LIST_RING - 1)) * blockDim.x];
-    if ((int)(u + LIST_RING - 1) < niter) cp_async4(ring + ((u - 1) & (LIST_RING - 1)) * blockDim.x, p);
-    cp_async_commit();
-    p += stride;
-    return e;
-  }
-};
 
 // {0,1,2} -> -1.f, 0.f, +1.f exactly (small integer through the 2^23 mantissa
 // trick); the separation shift is then one FMA per axis.
@@ -108,6 +68,37 @@ __device__ __forceinline__ void vir9(const float* v, double* o) {
   o[6] = v[4]; o[7] = v[5]; o[8] = v[2];
 }
 
+// The V list entries of lane `lane` in row r of atom i, read with one load
+// that bypasses L1 (each entry is used once per kernel).  Entries at or
+// beyond nn are replaced by a harmless stand-in: j = i seen through the +x
+// stencil offset, a separation of one cell edge (>= rcut + skin), which no
+// cutoff test accepts.
+template <int T, int V>
+struct ListRows {
+  static constexpr int W = T * V;
+  const uint32_t* p;  // nbr + i*W + lane*V
+  int64_t stride;
+  int nrow, k0, nn;
+  uint32_t standin;
+  __device__ __forceinline__ ListRows(const uint32_t* nbr, int64_t i, int lane, int64_t stride_, int nn_)
+      : p(nbr + (size_t)i * W + lane * V), stride(stride_), nn(nn_) {
+    k0 = lane * V;
+    nrow = nn > k0 ? (nn - k0 + W - 1) / W : 0;
+    standin = (uint32_t)i | ((2u | (1u << 2) | (1u << 4)) << GBMD_IDX_BITS);
+  }
+  __device__ __forceinline__ void load(int r, uint32_t (&e)[V]) const {
+    const uint32_t* q = p + (size_t)r * stride;
+    if constexpr (V == 4) {
+      const uint4 u = __ldcs(reinterpret_cast<const uint4*>(q));
+      e[0] = u.x; e[1] = u.y; e[2] = u.z; e[3] = u.w;
+    } else {
+#pragma unroll
+      for (int v = 0; v < V; ++v) e[v] = __ldcs(q + v);
+    }
+  }
+  __device__ __forceinline__ bool valid(int r, int v) const { return r * W + k0 + v < nn; }
+};
+
 // ---------------------------------------------------------------------------
 // Lennard-Jones
 // ---------------------------------------------------------------------------
@@ -116,7 +107,7 @@ struct LJF {
   double rc2, rc;
 };
 
-template <int T, bool EV, bool MULTI>
+template <int T, int V, bool EV, bool MULTI>
 __global__ void __launch_bounds__(256) k_lj_mixed(PairArgs A, LJF P, const LJPair* __restrict__ tab, int ntypes,
                                                   double rcmax2) {
   __shared__ float4 sfa[MULTI ? GBMD_MAX_TYPES * GBMD_MAX_TYPES : 1];   // sig2, eps24, eps4, ecut
@@ -141,49 +132,63 @@ __global__ void __launch_bounds__(256) k_lj_mixed(PairArgs A, LJF P, const LJPai
   const int ti = __float_as_int(pi.w);
   float fx = 0.f, fy = 0.f, fz = 0.f, cfx = 0.f, cfy = 0.f, cfz = 0.f, e = 0.f, ce = 0.f;
   float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  __shared__ uint32_t ring_sm[LIST_RING * 256];
-  ListStream ls{ring_sm + threadIdx.x, A.nbr + (size_t)i * T + lane, A.stride, nn > lane ? (nn - lane + T - 1) / T : 0};
-  ls.start();
-#pragma unroll 2
-  for (int it = 0; it < ls.niter; ++it) {
-    const uint32_t ent = ls.next(it);
-    const uint32_t j = ent & GBMD_IDX_MASK;
-    const float4 pj = __ldg(&A.posf[j]);
-    const GeomF G = geom_f(ent, pj, pi, A.g);
-    float sig2, eps24, eps4, ecut, rlo, rhi;
-    double rcp = 0.0, rc2 = P.rc2;
-    if (MULTI) {
-      const int pid = ti * ntypes + __float_as_int(pj.w);
-      const float4 a = sfa[pid];
-      const float2 b = sfb[pid];
-      sig2 = a.x; eps24 = a.y; eps4 = a.z; ecut = a.w; rlo = b.x; rhi = b.y;
-      rcp = sfr[pid];
-      rc2 = rcmax2;
-    } else {
-      sig2 = P.sig2; eps24 = P.eps24; eps4 = P.eps4; ecut = P.ecut; rlo = P.rc2lo; rhi = P.rc2hi;
+  const ListRows<T, V> L(A.nbr, i, lane, A.stride, nn);
+  uint32_t ent[V], nxt[V];
+  if (L.nrow > 0) L.load(0, ent);
+  for (int r = 0; r < L.nrow; ++r) {
+    if (r + 1 < L.nrow) L.load(r + 1, nxt);
+    float4 pj[V];
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      if (!L.valid(r, q)) ent[q] = L.standin;
+      pj[q] = __ldg(&A.posf[ent[q] & GBMD_IDX_MASK]);
     }
-    bool in = G.d2 < rlo;
-    if (!in && G.d2 <= rhi) in = exact_inside(A.posd, i, j, ent >> GBMD_IDX_BITS, cp, A.g, rc2, rcp);
-    const float r2i = __frcp_rn(G.d2);
-    const float s2 = sig2 * r2i;
-    const float s6 = s2 * s2 * s2;
-    const float s12 = s6 * s6;
-    const float fpair = in ? eps24 * fmaf(2.f, s12, -s6) * r2i : 0.f;  // -(dE/dr)/r
-    kahan_add(fx, cfx, -fpair * G.dx);
-    kahan_add(fy, cfy, -fpair * G.dy);
-    kahan_add(fz, cfz, -fpair * G.dz);
-    if (EV) {
-      kahan_add(e, ce, in ? 0.5f * fmaf(eps4, s12 - s6, -ecut) : 0.f);
-      const float h = 0.5f * fpair;
-      v[0] = fmaf(h * G.dx, G.dx, v[0]);
-      v[1] = fmaf(h * G.dy, G.dy, v[1]);
-      v[2] = fmaf(h * G.dz, G.dz, v[2]);
-      v[3] = fmaf(h * G.dx, G.dy, v[3]);
-      v[4] = fmaf(h * G.dx, G.dz, v[4]);
-      v[5] = fmaf(h * G.dy, G.dz, v[5]);
+    float rx = 0.f, ry = 0.f, rz = 0.f, re = 0.f;
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const uint32_t j = ent[q] & GBMD_IDX_MASK;
+      const GeomF G = geom_f(ent[q], pj[q], pi, A.g);
+      float sig2, eps24, eps4, ecut, rlo, rhi;
+      double rcp = 0.0, rc2 = P.rc2;
+      if (MULTI) {
+        const int pid = ti * ntypes + __float_as_int(pj[q].w);
+        const float4 a = sfa[pid];
+        const float2 b = sfb[pid];
+        sig2 = a.x; eps24 = a.y; eps4 = a.z; ecut = a.w; rlo = b.x; rhi = b.y;
+        rcp = sfr[pid];
+        rc2 = rcmax2;
+      } else {
+        sig2 = P.sig2; eps24 = P.eps24; eps4 = P.eps4; ecut = P.ecut; rlo = P.rc2lo; rhi = P.rc2hi;
+      }
+      bool in = G.d2 < rlo;
+      if (!in && G.d2 <= rhi && L.valid(r, q))
+        in = exact_inside(A.posd, i, j, ent[q] >> GBMD_IDX_BITS, cp, A.g, rc2, rcp);
+      const float r2i = __frcp_rn(G.d2);
+      const float s2 = sig2 * r2i;
+      const float s6 = s2 * s2 * s2;
+      const float s12 = s6 * s6;
+      const float fpair = in ? eps24 * fmaf(2.f, s12, -s6) * r2i : 0.f;  // -(dE/dr)/r
+      rx = fmaf(-fpair, G.dx, rx);
+      ry = fmaf(-fpair, G.dy, ry);
+      rz = fmaf(-fpair, G.dz, rz);
+      if (EV) {
+        re += in ? 0.5f * fmaf(eps4, s12 - s6, -ecut) : 0.f;
+        const float h = 0.5f * fpair;
+        v[0] = fmaf(h * G.dx, G.dx, v[0]);
+        v[1] = fmaf(h * G.dy, G.dy, v[1]);
+        v[2] = fmaf(h * G.dz, G.dz, v[2]);
+        v[3] = fmaf(h * G.dx, G.dy, v[3]);
+        v[4] = fmaf(h * G.dx, G.dz, v[4]);
+        v[5] = fmaf(h * G.dy, G.dz, v[5]);
+      }
     }
+    kahan_add(fx, cfx, rx);
+    kahan_add(fy, cfy, ry);
+    kahan_add(fz, cfz, rz);
+    if (EV) kahan_add(e, ce, re);
+#pragma unroll
+    for (int q = 0; q < V; ++q) ent[q] = nxt[q];
   }
-  cp_async_drain();
   group_reduce_kahan<T>(fx, cfx);
   group_reduce_kahan<T>(fy, cfy);
   group_reduce_kahan<T>(fz, cfz);
@@ -218,9 +223,11 @@ __device__ __forceinline__ float spline_der(const float4& c, float q, float rd) 
   return fmaf(fmaf(3.f * c.x, q, 2.f * c.y), q, c.z) * rd;
 }
 
-template <int T, bool EV, bool SINGLE>
+// Density + embedding.  SINGLE (one element): also writes pfp[i] = (position,
+// F'(rho_i)) so the force pass gathers both in one 16 B load.
+template <int T, int V, bool EV, bool SINGLE>
 __global__ void __launch_bounds__(256) k_eam_rho_mixed(PairArgs A, EamDev E, float* __restrict__ fpf,
-                                                       float* __restrict__ epf) {
+                                                       float* __restrict__ epf, float4* __restrict__ pfp) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t i = gt / T;
   const int lane = (int)(gt % T);
@@ -228,28 +235,39 @@ __global__ void __launch_bounds__(256) k_eam_rho_mixed(PairArgs A, EamDev E, flo
   const int nn = live ? min(A.nnb[i], A.maxnb) : 0;
   const float4 pi = live ? A.posf[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   const int cp = live ? A.cellpack[i] : 0;
-  const int ti = __float_as_int(pi.w);
+  const int ti = SINGLE ? 0 : __float_as_int(pi.w);
   const int nr = E.nr, nr1 = E.nr + 1;
   const float rdr = E.rdrf;
   float rho = 0.f, crho = 0.f;
-  __shared__ uint32_t ring_sm[LIST_RING * 256];
-  ListStream ls{ring_sm + threadIdx.x, A.nbr + (size_t)i * T + lane, A.stride, nn > lane ? (nn - lane + T - 1) / T : 0};
-  ls.start();
-#pragma unroll 2
-  for (int it = 0; it < ls.niter; ++it) {
-    const uint32_t ent = ls.next(it);
-    const uint32_t j = ent & GBMD_IDX_MASK;
-    const float4 pj = __ldg(&A.posf[j]);
-    const GeomF G = geom_f(ent, pj, pi, A.g);
-    bool in = G.d2 < E.rc2lo;
-    if (!in && G.d2 <= E.rc2hi) in = exact_inside(A.posd, i, j, ent >> GBMD_IDX_BITS, cp, A.g, E.rcut2, 0.0);
-    const float r = G.d2 * rsqrtf(G.d2);
-    float q;
-    const int m = knot_f(r, rdr, nr, q);
-    const float4 c = __ldg(&E.rhor4[SINGLE ? m : __float_as_int(pj.w) * nr1 + m]);
-    kahan_add(rho, crho, in ? spline_val(c, q) : 0.f);
+  const ListRows<T, V> L(A.nbr, i, lane, A.stride, nn);
+  uint32_t ent[V], nxt[V];
+  if (L.nrow > 0) L.load(0, ent);
+  for (int r = 0; r < L.nrow; ++r) {
+    if (r + 1 < L.nrow) L.load(r + 1, nxt);
+    float4 pj[V];
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      if (!L.valid(r, q)) ent[q] = L.standin;
+      pj[q] = __ldg(&A.posf[ent[q] & GBMD_IDX_MASK]);
+    }
+    float rr = 0.f;
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const uint32_t j = ent[q] & GBMD_IDX_MASK;
+      const GeomF G = geom_f(ent[q], pj[q], pi, A.g);
+      bool in = G.d2 < E.rc2lo;
+      if (!in && G.d2 <= E.rc2hi && L.valid(r, q))
+        in = exact_inside(A.posd, i, j, ent[q] >> GBMD_IDX_BITS, cp, A.g, E.rcut2, 0.0);
+      const float rd = G.d2 * rsqrtf(G.d2);
+      float t;
+      const int m = knot_f(rd, rdr, nr, t);
+      const float4 c = __ldg(&E.rhor4[SINGLE ? m : __float_as_int(pj[q].w) * nr1 + m]);
+      rr += in ? spline_val(c, t) : 0.f;
+    }
+    kahan_add(rho, crho, rr);
+#pragma unroll
+    for (int q = 0; q < V; ++q) ent[q] = nxt[q];
   }
-  cp_async_drain();
   group_reduce_kahan<T>(rho, crho);
   if (live && lane == 0) {
     // Rho2EmbOp / eam_alloy_fEmbed: F'(rho) (and F(rho) on energy steps),
@@ -262,6 +280,7 @@ __global__ void __launch_bounds__(256) k_eam_rho_mixed(PairArgs A, EamDev E, flo
     const float4 c = __ldg(&E.frho4[(SINGLE ? 0 : ti * (E.nrho + 1)) + m]);
     const float fp = spline_der(c, q, E.rdrhof);
     fpf[i] = fp;
+    if (SINGLE) pfp[i] = make_float4(pi.x, pi.y, pi.z, fp);
     if (EV) {
       float phi = spline_val(c, q);
       if (R > E.rhomaxf) phi = fmaf(fp, R - E.rhomaxf, phi);
@@ -275,9 +294,13 @@ __device__ __forceinline__ int z2r_index_d(int a, int b) {
   return irow * (irow + 1) / 2 + icol;
 }
 
-template <int T, bool EV, bool SINGLE>
+// Force pass: f_i = sum_j u_ij (F'_i rho_j'(r) + F'_j rho_i'(r) + phi'(r)),
+// then force_to_accel and the fused Verlet halves.  SINGLE gathers
+// (position, F'_j) from pfp; otherwise position (type in w) and fpf.
+template <int T, int V, bool EV, bool SINGLE>
 __global__ void __launch_bounds__(256) k_eam_force_mixed(PairArgs A, EamDev E, const float* __restrict__ fpf,
-                                                         const float* __restrict__ epf) {
+                                                         const float* __restrict__ epf,
+                                                         const float4* __restrict__ pfp) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t i = gt / T;
   const int lane = (int)(gt % T);
@@ -286,74 +309,76 @@ __global__ void __launch_bounds__(256) k_eam_force_mixed(PairArgs A, EamDev E, c
   const float4 pi = live ? A.posf[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   const int cp = live ? A.cellpack[i] : 0;
   const float fpi = live ? fpf[i] : 0.f;
-  const int ti = __float_as_int(pi.w);
+  const int ti = SINGLE ? 0 : __float_as_int(pi.w);
   const int nr = E.nr, nr1 = E.nr + 1;
   const float rdr = E.rdrf;
+  const float4* __restrict__ P = SINGLE ? pfp : A.posf;
   float fx = 0.f, fy = 0.f, fz = 0.f, cfx = 0.f, cfy = 0.f, cfz = 0.f, e = 0.f, ce = 0.f;
   float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  __shared__ uint32_t ring_sm[LIST_RING * 256];
-  ListStream ls{ring_sm + threadIdx.x, A.nbr + (size_t)i * T + lane, A.stride, nn > lane ? (nn - lane + T - 1) / T : 0};
-  ls.start();
-  // the force sums take two pair terms per compensated add: the pair of
-  // terms is rounded once (relative 6e-8 of the larger term), then the sum
-  // is compensated
-  float px = 0.f, py = 0.f, pz = 0.f;
-#pragma unroll 2
-  for (int it = 0; it < ls.niter; ++it) {
-    const uint32_t ent = ls.next(it);
-    const uint32_t j = ent & GBMD_IDX_MASK;
-    const float4 pj = __ldg(&A.posf[j]);
-    const float fpj = __ldg(&fpf[j]);
-    const GeomF G = geom_f(ent, pj, pi, A.g);
-    bool in = G.d2 < E.rc2lo;
-    if (!in && G.d2 <= E.rc2hi) in = exact_inside(A.posd, i, j, ent >> GBMD_IDX_BITS, cp, A.g, E.rcut2, 0.0);
-    const float rs = rsqrtf(G.d2);
-    const float r = G.d2 * rs;
-    float q;
-    const int m = knot_f(r, rdr, nr, q);
-    const int tj = __float_as_int(pj.w);
-    // rho'(r) from the pre-scaled derivative table: (3c3/dr, 2c4/dr, c5/dr)
-    const float4 dj = __ldg(&E.rhod4[SINGLE ? m : tj * nr1 + m]);
-    const float rhojp = fmaf(fmaf(dj.x, q, dj.y), q, dj.z);
-    float rhoip = rhojp;
-    if (!SINGLE && ti != tj) {
-      const float4 di = __ldg(&E.rhod4[ti * nr1 + m]);
-      rhoip = fmaf(fmaf(di.x, q, di.y), q, di.z);
+  const ListRows<T, V> L(A.nbr, i, lane, A.stride, nn);
+  uint32_t ent[V], nxt[V];
+  if (L.nrow > 0) L.load(0, ent);
+  for (int r = 0; r < L.nrow; ++r) {
+    if (r + 1 < L.nrow) L.load(r + 1, nxt);
+    float4 pj[V];
+    float fpj[V];
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      if (!L.valid(r, q)) ent[q] = L.standin;
+      const uint32_t j = ent[q] & GBMD_IDX_MASK;
+      pj[q] = __ldg(&P[j]);
+      fpj[q] = SINGLE ? pj[q].w : __ldg(&fpf[j]);
     }
-    const float4 cz = __ldg(&E.z2r4[SINGLE ? m : z2r_index_d(ti, tj) * nr1 + m]);
-    const float t1 = fmaf(cz.x, q, cz.y);
-    const float z2 = fmaf(fmaf(t1, q, cz.z), q, cz.w);          // z2r tables carry conv_z2r
-    const float z2d = fmaf(fmaf(cz.x, q, t1 + t1), q, cz.z);     // d z2 / d q
-    const float phi = z2 * rs;
-    const float phip = fmaf(z2d * rdr, rs, -phi * rs);
-    const float psip = fmaf(fpi, rhojp, fmaf(fpj, rhoip, phip));
-    const float fpair = in ? psip * rs : 0.f;
-    if (it & 1) {
-      kahan_add(fx, cfx, fmaf(G.dx, fpair, px));
-      kahan_add(fy, cfy, fmaf(G.dy, fpair, py));
-      kahan_add(fz, cfz, fmaf(G.dz, fpair, pz));
-    } else {
-      px = G.dx * fpair;
-      py = G.dy * fpair;
-      pz = G.dz * fpair;
+    float rx = 0.f, ry = 0.f, rz = 0.f, re = 0.f;
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const uint32_t j = ent[q] & GBMD_IDX_MASK;
+      const GeomF G = geom_f(ent[q], pj[q], pi, A.g);
+      bool in = G.d2 < E.rc2lo;
+      if (!in && G.d2 <= E.rc2hi && L.valid(r, q))
+        in = exact_inside(A.posd, i, j, ent[q] >> GBMD_IDX_BITS, cp, A.g, E.rcut2, 0.0);
+      const float rs = rsqrtf(G.d2);
+      const float rd = G.d2 * rs;
+      float t;
+      const int m = knot_f(rd, rdr, nr, t);
+      const int tj = SINGLE ? 0 : __float_as_int(pj[q].w);
+      // rho'(r) from the pre-scaled derivative table: (3c3/dr, 2c4/dr, c5/dr)
+      const float4 dj = __ldg(&E.rhod4[SINGLE ? m : tj * nr1 + m]);
+      const float rhojp = fmaf(fmaf(dj.x, t, dj.y), t, dj.z);
+      float rhoip = rhojp;
+      if (!SINGLE && ti != tj) {
+        const float4 di = __ldg(&E.rhod4[ti * nr1 + m]);
+        rhoip = fmaf(fmaf(di.x, t, di.y), t, di.z);
+      }
+      const float4 cz = __ldg(&E.z2r4[SINGLE ? m : z2r_index_d(ti, tj) * nr1 + m]);
+      const float t1 = fmaf(cz.x, t, cz.y);
+      const float z2 = fmaf(fmaf(t1, t, cz.z), t, cz.w);          // z2r tables carry conv_z2r
+      const float z2d = fmaf(fmaf(cz.x, t, t1 + t1), t, cz.z);     // d z2 / d t
+      const float phi = z2 * rs;
+      const float phip = fmaf(z2d * rdr, rs, -phi * rs);
+      const float psip = fmaf(fpi, rhojp, fmaf(fpj[q], rhoip, phip));
+      const float fpair = in ? psip * rs : 0.f;
+      rx = fmaf(G.dx, fpair, rx);
+      ry = fmaf(G.dy, fpair, ry);
+      rz = fmaf(G.dz, fpair, rz);
+      if (EV) {
+        re += in ? 0.5f * phi : 0.f;
+        const float h = -0.5f * fpair;
+        v[0] = fmaf(h * G.dx, G.dx, v[0]);
+        v[1] = fmaf(h * G.dy, G.dy, v[1]);
+        v[2] = fmaf(h * G.dz, G.dz, v[2]);
+        v[3] = fmaf(h * G.dx, G.dy, v[3]);
+        v[4] = fmaf(h * G.dx, G.dz, v[4]);
+        v[5] = fmaf(h * G.dy, G.dz, v[5]);
+      }
     }
-    if (EV) {
-      kahan_add(e, ce, in ? 0.5f * phi : 0.f);
-      const float h = -0.5f * fpair;
-      v[0] = fmaf(h * G.dx, G.dx, v[0]);
-      v[1] = fmaf(h * G.dy, G.dy, v[1]);
-      v[2] = fmaf(h * G.dz, G.dz, v[2]);
-      v[3] = fmaf(h * G.dx, G.dy, v[3]);
-      v[4] = fmaf(h * G.dx, G.dz, v[4]);
-      v[5] = fmaf(h * G.dy, G.dz, v[5]);
-    }
+    kahan_add(fx, cfx, rx);
+    kahan_add(fy, cfy, ry);
+    kahan_add(fz, cfz, rz);
+    if (EV) kahan_add(e, ce, re);
+#pragma unroll
+    for (int q = 0; q < V; ++q) ent[q] = nxt[q];
   }
-  if (ls.niter & 1) {  // a last unpaired term
-    kahan_add(fx, cfx, px);
-    kahan_add(fy, cfy, py);
-    kahan_add(fz, cfz, pz);
-  }
-  cp_async_drain();
   group_reduce_kahan<T>(fx, cfx);
   group_reduce_kahan<T>(fy, cfy);
   group_reduce_kahan<T>(fz, cfz);
@@ -374,8 +399,8 @@ __global__ void __launch_bounds__(256) k_eam_force_mixed(PairArgs A, EamDev E, c
 // ---------------------------------------------------------------------------
 // dispatch
 // ---------------------------------------------------------------------------
-template <int T, bool EV>
-static void launch_mixed_T(gbmd_context* c, const PairArgs& A, int part) {
+template <int T, int V, bool EV>
+static void launch_mixed_TV(gbmd_context* c, const PairArgs& A, int part) {
   const int B = c->block;
   const unsigned grid = (unsigned)((A.n * T + B - 1) / B);
   cudaStream_t s = c->stream;
@@ -383,29 +408,34 @@ static void launch_mixed_T(gbmd_context* c, const PairArgs& A, int part) {
     if (part == 1) return;
     const LJPair& q = c->lj.p[0];
     LJF P{q.sig2f, q.eps24f, q.eps4f, q.ecutf, q.rc2lo, q.rc2hi, q.rc2, q.rc};
-    k_lj_mixed<T, EV, false><<<grid, B, 0, s>>>(A, P, nullptr, 1, c->lj.rcut_max2);
+    k_lj_mixed<T, V, EV, false><<<grid, B, 0, s>>>(A, P, nullptr, 1, c->lj.rcut_max2);
   } else if (c->pot == GBMD_POT_LJ_MULTI) {
     if (part == 1) return;
     LJF P{};
-    k_lj_mixed<T, EV, true><<<grid, B, 0, s>>>(A, P, c->lj_tab_d, c->lj.ntypes, c->lj.rcut_max2);
+    k_lj_mixed<T, V, EV, true><<<grid, B, 0, s>>>(A, P, c->lj_tab_d, c->lj.ntypes, c->lj.rcut_max2);
   } else if (c->eam.nel == 1) {
-    if (part != 2) k_eam_rho_mixed<T, EV, true><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->epf);
-    if (part != 1) k_eam_force_mixed<T, EV, true><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->epf);
+    if (part != 2) k_eam_rho_mixed<T, V, EV, true><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
+    if (part != 1) k_eam_force_mixed<T, V, EV, true><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
   } else {
-    if (part != 2) k_eam_rho_mixed<T, EV, false><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->epf);
-    if (part != 1) k_eam_force_mixed<T, EV, false><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->epf);
+    if (part != 2) k_eam_rho_mixed<T, V, EV, false><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
+    if (part != 1) k_eam_force_mixed<T, V, EV, false><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
   }
 }
 
 template <bool EV>
 static int launch_mixed_E(gbmd_context* c, const PairArgs& A, int part) {
-  switch (c->tpa) {
-    case 1: launch_mixed_T<1, EV>(c, A, part); break;
-    case 2: launch_mixed_T<2, EV>(c, A, part); break;
-    case 4: launch_mixed_T<4, EV>(c, A, part); break;
-    case 8: launch_mixed_T<8, EV>(c, A, part); break;
-    case 16: launch_mixed_T<16, EV>(c, A, part); break;
-    default: return set_error(c, GBMD_ERR_INVALID, "unsupported lanes per atom %d", c->tpa);
+  const int key = c->tpa * 8 + c->vec;
+  switch (key) {
+    case 1 * 8 + 1: launch_mixed_TV<1, 1, EV>(c, A, part); break;
+    case 1 * 8 + 4: launch_mixed_TV<1, 4, EV>(c, A, part); break;
+    case 2 * 8 + 1: launch_mixed_TV<2, 1, EV>(c, A, part); break;
+    case 2 * 8 + 4: launch_mixed_TV<2, 4, EV>(c, A, part); break;
+    case 4 * 8 + 1: launch_mixed_TV<4, 1, EV>(c, A, part); break;
+    case 4 * 8 + 4: launch_mixed_TV<4, 4, EV>(c, A, part); break;
+    case 8 * 8 + 1: launch_mixed_TV<8, 1, EV>(c, A, part); break;
+    case 16 * 8 + 1: launch_mixed_TV<16, 1, EV>(c, A, part); break;
+    default:
+      return set_error(c, GBMD_ERR_INVALID, "unsupported launch: %d lanes x %d entries per atom", c->tpa, c->vec);
   }
   return GBMD_OK;
 }

@@ -342,9 +342,9 @@ __global__ void __launch_bounds__(128) k_build_list_cells(
     s_start = cstart[cj];
     s_cnt = cstart[cj + 1] - s_start;
     s_code = (uint32_t)(dx + 1) | ((uint32_t)(dy + 1) << 2) | ((uint32_t)(dz + 1) << 4);
-    s_sx = (float)dx * g.hf[0];
-    s_sy = (float)dy * g.hf[1];
-    s_sz = (float)dz * g.hf[2];
+    s_sx = __fmul_rn((float)dx, g.hf[0]);
+    s_sy = __fmul_rn((float)dy, g.hf[1]);
+    s_sz = __fmul_rn((float)dz, g.hf[2]);
   }
   int incl = s_cnt;
 #pragma unroll
@@ -373,6 +373,7 @@ __global__ void __launch_bounds__(128) k_build_list_cells(
     float4 pi = make_float4(FAR, FAR, FAR, 0.f);
     if (hv) pi = pf[i];
     int cnt = 0;
+    bool unc = false;
     for (int q0 = 0; q0 < total; q0 += BUILD_CHUNK) {
       __syncwarp();
 #pragma unroll
@@ -393,7 +394,8 @@ __global__ void __launch_bounds__(128) k_build_list_cells(
         float4 e = make_float4(FAR, FAR, FAR, __uint_as_float(0xffffffffu));
         if (q < total) {
           const float4 pj = pf[k];
-          e = make_float4(pj.x + sx, pj.y + sy, pj.z + sz, __uint_as_float((uint32_t)k | (code << GBMD_IDX_BITS)));
+          e = make_float4(__fadd_rn(pj.x, sx), __fadd_rn(pj.y, sy), __fadd_rn(pj.z, sz),
+                          __uint_as_float((uint32_t)k | (code << GBMD_IDX_BITS)));
         }
         stage[r * 32 + lane] = e;
       }
@@ -404,18 +406,16 @@ __global__ void __launch_bounds__(128) k_build_list_cells(
         const float4 e = stage[t + half];
         const uint32_t w = __float_as_uint(e.w);
         const int k = (int)(w & GBMD_IDX_MASK);
-        const float dx = e.x - pi.x;
-        const float dy = e.y - pi.y;
-        const float dz = e.z - pi.z;
-        const float d2f = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const float dx = __fsub_rn(e.x, pi.x);
+        const float dy = __fsub_rn(e.y, pi.y);
+        const float dz = __fsub_rn(e.z, pi.z);
+        const float d2f = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
         // an atom never pairs with itself: its images sit at least one box
-        // edge >= R away, so k == i only ever matters in the home cell
-        const bool keep = hv && k != i;
-        bool in = keep && d2f < R2lo;
-        const bool band = keep && d2f >= R2lo && d2f <= R2hi;
-        if (__any_sync(FULL, band)) {  // rare: some lane needs the FP64 re-test
-          if (band) in = exact_within(x, y, z, i, k, w >> GBMD_IDX_BITS, cx, cy, cz, g, R2);
-        }
+        // edge >= R away, so k == i only ever matters in the home cell.
+        // Candidates inside R^2 (1 + 2^-12) are kept; those in the band
+        // above R^2 (1 - 2^-12) are re-tested in FP64 after the walk.
+        const bool in = hv && k != i && d2f <= R2hi;
+        unc |= in && d2f >= R2lo;
         const int other = __shfl_xor_sync(FULL, (int)in, 16);
         if (in) {
           const int pos = cnt + (half ? other : 0);  // candidate 2t goes first
@@ -423,6 +423,35 @@ __global__ void __launch_bounds__(128) k_build_list_cells(
         }
         cnt += (int)in + other;
       }
+    }
+    // deferred FP64 re-test (about one atom in twenty has a band entry): the
+    // atom's lane in the low half rescans its row, recomputes each entry's
+    // FP32 d2 exactly as above, re-tests the band entries and compacts
+    const bool unc_home = __shfl_xor_sync(FULL, (int)unc, 16) != 0 || unc;
+    if (__any_sync(FULL, unc_home)) {
+      if (half == 0 && hv && unc_home) {
+        const int nkeep = min(cnt, maxnb);
+        int wpos = 0;
+        for (int p = 0; p < nkeep; ++p) {
+          const uint32_t w = my_row[p];
+          const int k = (int)(w & GBMD_IDX_MASK);
+          const uint32_t code = w >> GBMD_IDX_BITS;
+          const float4 pj = pf[k];
+          // the same rounded operations as the staging and the walk
+          const float sx = __fmul_rn((float)((int)(code & 3u) - 1), g.hf[0]);
+          const float sy = __fmul_rn((float)((int)((code >> 2) & 3u) - 1), g.hf[1]);
+          const float sz = __fmul_rn((float)((int)(code >> 4) - 1), g.hf[2]);
+          const float dx = __fsub_rn(__fadd_rn(pj.x, sx), pi.x);
+          const float dy = __fsub_rn(__fadd_rn(pj.y, sy), pi.y);
+          const float dz = __fsub_rn(__fadd_rn(pj.z, sz), pi.z);
+          const float d2f = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
+          bool keepit = true;
+          if (d2f >= R2lo) keepit = exact_within(x, y, z, i, k, code, cx, cy, cz, g, R2);
+          if (keepit) my_row[wpos++] = w;
+        }
+        cnt -= nkeep - wpos;
+      }
+      cnt = __shfl_sync(FULL, cnt, hl);  // the high-half lane takes the corrected count
     }
     if (hv && half == 0) {
       nnb[i] = cnt;
@@ -464,8 +493,9 @@ static int build_list(gbmd_context* c, const int* gate) {
   const float R2lo = (float)(R2 * (1.0 - 0x1p-12));
   const float R2hi = (float)(R2 * (1.0 + 0x1p-12));
   const int64_t npad = ((c->n + 31) / 32) * 32;
-  const int64_t stride = npad * c->tpa;
-  const int64_t need = (int64_t)(c->maxnb / c->tpa) * stride;
+  const int W = list_width(c);
+  const int64_t stride = npad * W;
+  const int64_t need = (int64_t)(c->maxnb / W) * stride;
   if (need > c->nbr_cap) {
     if (c->nbr) cudaFree(c->nbr);
     c->nbr = nullptr;
@@ -476,15 +506,15 @@ static int build_list(gbmd_context* c, const int* gate) {
   if (!gate) GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_MAXNB, 0, sizeof(int), c->stream));
   // shared memory per warp: BUILD_CHUNK staged candidates + 32 counts + BUILD_HB x maxnb entries
   const size_t per_warp = 16 * (BUILD_CHUNK + 8) + 4 * BUILD_HB * (size_t)c->maxnb;
-  int W = (int)((96 * 1024) / per_warp);
-  W = W < 1 ? 1 : (W > 4 ? 4 : W);
-  const size_t smem = per_warp * W;
+  int nw = (int)((96 * 1024) / per_warp);  // warps per block
+  nw = nw < 1 ? 1 : (nw > 4 ? 4 : nw);
+  const size_t smem = per_warp * nw;
   if (smem > 227 * 1024) return set_error(c, GBMD_ERR_TOO_LARGE, "neighbour capacity %d per atom too large", c->maxnb);
   if (smem > 48 * 1024)
     GBMD_CUDA(c, cudaFuncSetAttribute(k_build_list_cells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_build_list_cells<<<nblk(c->grid.ncells, W), 32 * W, smem, c->stream>>>(
+  k_build_list_cells<<<nblk(c->grid.ncells, nw), 32 * nw, smem, c->stream>>>(
       c->grid.ncells, c->POSF(), c->X(), c->Y(), c->Z(), c->cell_start, c->grid, R2, R2lo, R2hi, c->nbr, c->nnb,
-      c->maxnb, c->tpa, stride, c->d_err, gate);
+      c->maxnb, W, stride, c->d_err, gate);
   return GBMD_OK;
 }
 
@@ -569,7 +599,7 @@ int rebuild(gbmd_context* c, bool check_capacity, const int* gate) {
     const double V = g.L[0] * g.L[1] * g.L[2];
     const double mean = (double)n / V * 4.18879020478639 * R * R * R;
     int m = (int)(mean * 1.35) + 16;
-    c->maxnb = ((m + c->tpa - 1) / c->tpa) * c->tpa;
+    c->maxnb = ((m + list_width(c) - 1) / list_width(c)) * list_width(c);
   }
   rc = build_list(c, gate);
   if (rc) return rc;
@@ -583,7 +613,7 @@ int rebuild(gbmd_context* c, bool check_capacity, const int* gate) {
     const int maxc = c->h_err[ERRW_MAXNB];
     if (maxc > c->maxnb) {
       int m = (int)(maxc * 1.2) + 8;
-      c->maxnb = ((m + c->tpa - 1) / c->tpa) * c->tpa;
+      c->maxnb = ((m + list_width(c) - 1) / list_width(c)) * list_width(c);
       GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_FLAGS, 0, sizeof(int) * 2, s));  // flags, max count
       rc = build_list(c, nullptr);
       if (rc) return rc;
@@ -611,7 +641,8 @@ int export_pairs(gbmd_context* c, int64_t cap, uint64_t* id_i, uint64_t* id_j, i
   for (int64_t i = 0; i < n; ++i) total += nnb[i];
   *count = total;
   if (cap < total || !id_i) return GBMD_OK;
-  const int64_t stride = c->npad * c->tpa;
+  const int W = list_width(c);
+  const int64_t stride = c->npad * W;
   std::vector<uint32_t> nb((size_t)c->nbr_cap);
   GBMD_CUDA(c, cudaMemcpy(nb.data(), c->nbr, sizeof(uint32_t) * c->nbr_cap, cudaMemcpyDeviceToHost));
   int64_t row = 0;
@@ -619,7 +650,7 @@ int export_pairs(gbmd_context* c, int64_t cap, uint64_t* id_i, uint64_t* id_j, i
   for (int64_t i = 0; i < n; ++i) {
     const int cx = cp[i] & 1023, cy = (cp[i] >> 10) & 1023, cz = cp[i] >> 20;
     for (int k = 0; k < nnb[i] && k < c->maxnb; ++k) {
-      const uint32_t e = nb[(size_t)(k / c->tpa) * stride + (size_t)i * c->tpa + (k % c->tpa)];
+      const uint32_t e = nb[(size_t)(k / W) * stride + (size_t)i * W + (k % W)];
       const uint32_t j = e & GBMD_IDX_MASK, code = e >> GBMD_IDX_BITS;
       const int d[3] = {int(code & 3) - 1, int((code >> 2) & 3) - 1, int((code >> 4) & 3) - 1};
       const int cc[3] = {cx + d[0], cy + d[1], cz + d[2]};

@@ -1,9 +1,9 @@
 // gbmd_pair_common.cuh -- pieces shared by the pair kernels (LJ, EAM).
 //
-// Thread mapping: T consecutive lanes own one atom i (atoms in cell order);
-// lane l walks list slots l, l+T, ...  The list is stored so that those T
-// slots are adjacent and consecutive atoms are adjacent: one warp reads 128
-// contiguous bytes per iteration.  Per-atom sums are reduced across the T lanes
+// Thread mapping: T consecutive lanes own one atom i (atoms in cell order).
+// The list is stored in rows of W = T*V words per atom (V entries per lane per
+// load), consecutive atoms adjacent: row r of atom i is nbr[r*stride + i*W ..
+// + W), so a warp reads 32*V*4 contiguous bytes per load.  Per-atom sums are reduced across the T lanes
 // with shuffles; lane 0 of the group runs the epilogue.
 //
 // Epilogue (lane 0): a = f/m (force_to_accel), optional ep / virial stores,
@@ -20,7 +20,8 @@ namespace gbmd {
 
 struct PairArgs {
   int64_t n;
-  int64_t stride;             // npad * T
+  int64_t stride;             // npad * W (words per list row)
+  int W, wsh;                 // words per atom per row (lanes x entries per lane), log2 W
   const uint32_t* nbr;
   const int32_t* nnb;
   int maxnb;

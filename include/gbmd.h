@@ -133,10 +133,16 @@ int gbmd_load_setfl(gbmd_context* ctx, const char* path, double rcut, double con
                     double conv_frho);
 
 int gbmd_set_precision(gbmd_context* ctx, int precision);
-/* Lanes per atom (1,2,4,8,16,32) and threads per block for the pair kernels;
- * the autotuner's knobs.  Invalidates the neighbour list layout. */
+/* Lanes per atom (1,2,4,8,16) and threads per block for the pair kernels;
+ * the autotuner's knobs.  Invalidates the neighbour list layout.
+ * gbmd_set_launch keeps one list entry per lane per load. */
 int gbmd_set_launch(gbmd_context* ctx, int lanes_per_atom, int block);
 int gbmd_get_launch(const gbmd_context* ctx, int* lanes_per_atom, int* block);
+/* As gbmd_set_launch, plus the list entries each lane reads per load in the
+ * mixed-precision kernels: 1, or 4 (one 16-byte load; at most 4 lanes per
+ * atom).  The list rows are laid out lanes_per_atom * entries wide. */
+int gbmd_set_launch_ex(gbmd_context* ctx, int lanes_per_atom, int entries_per_load, int block);
+int gbmd_get_launch_ex(const gbmd_context* ctx, int* lanes_per_atom, int* entries_per_load, int* block);
 
 /* ---- neighbour list --------------------------------------------------------
  * chunk_neighbors (exaNBody; config data/config/config_move_particles.msp

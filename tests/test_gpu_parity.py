@@ -45,25 +45,26 @@ def oracle_lists(oracle, s, R):
     return per_atom_lists(nl.pairs_with_ids(s.id)), (x, y, z), nl
 
 
-def gpu_ctx(gpu, s, pot, skin, mixed=False, tpa=None, block=None):
+def gpu_ctx(gpu, s, pot, skin, mixed=False, tpa=None, block=None, vec=1):
     ctx = gpu.Context(0)
     ctx.upload_system(s)
     pot(ctx)
     ctx.set_skin(skin)
     ctx.set_precision(mixed)
     if tpa:
-        ctx.set_launch(tpa, block or 128)
+        ctx.set_launch(tpa, block or 128, vec)
     return ctx
 
 
 LJ = lambda ctx: ctx.set_lj(1.0, 1.0, 2.5)  # noqa: E731
 
 
-@pytest.mark.parametrize("ncell,sig,tpa", [(3, 0.05, 1), (5, 0.1, 4), (8, 0.02, 8), (2, 0.1, 2)])
-def test_pair_set_bit_exact_lj(gpu, oracle, ncell, sig, tpa):
+@pytest.mark.parametrize("ncell,sig,tpa,vec", [(3, 0.05, 1, 1), (5, 0.1, 4, 1), (8, 0.02, 8, 1), (2, 0.1, 2, 1),
+                                               (5, 0.1, 1, 4), (4, 0.05, 2, 4), (6, 0.08, 4, 4)])
+def test_pair_set_bit_exact_lj(gpu, oracle, ncell, sig, tpa, vec):
     s = _jitter(S.lj_fcc(ncell=ncell, seed=ncell), sig, ncell)
     ref, _, _ = oracle_lists(oracle, s, 2.8)
-    with gpu_ctx(gpu, s, LJ, 0.3, tpa=tpa) as ctx:
+    with gpu_ctx(gpu, s, LJ, 0.3, tpa=tpa, vec=vec) as ctx:
         ctx.build_neighbors()
         got = per_atom_lists(ctx.export_pairs())
     assert got.keys() == ref.keys() or (len(ref) < s.n)
@@ -103,11 +104,11 @@ def _lj_oracle(oracle, s):
     return np.stack([fx, fy, fz], 1), ep, vir
 
 
-@pytest.mark.parametrize("tpa", [1, 2, 4, 8, 16])
-def test_lj_fp64_matches_oracle(gpu, oracle, tpa):
+@pytest.mark.parametrize("tpa,vec", [(1, 1), (2, 1), (4, 1), (8, 1), (16, 1), (1, 4), (4, 4)])
+def test_lj_fp64_matches_oracle(gpu, oracle, tpa, vec):
     s = _jitter(S.lj_fcc(ncell=6, seed=1), 0.04, 1)
     F, ep, vir = _lj_oracle(oracle, s)
-    with gpu_ctx(gpu, s, LJ, 0.3, tpa=tpa) as ctx:
+    with gpu_ctx(gpu, s, LJ, 0.3, tpa=tpa, vec=vec) as ctx:
         ctx.compute_forces(energy=True, virial=True)
         d = ctx.download(virial=True)
     G = np.stack([d["ax"], d["ay"], d["az"]], 1)
@@ -117,11 +118,11 @@ def test_lj_fp64_matches_oracle(gpu, oracle, tpa):
     assert np.abs(d["vir"] - vir).max() < FP64_TOL * np.abs(vir).max()
 
 
-@pytest.mark.parametrize("tpa", [1, 4, 8])
-def test_lj_mixed_within_tolerance(gpu, oracle, tpa):
+@pytest.mark.parametrize("tpa,vec", [(1, 1), (4, 1), (8, 1), (1, 4), (2, 4), (4, 4)])
+def test_lj_mixed_within_tolerance(gpu, oracle, tpa, vec):
     s = _jitter(S.lj_fcc(ncell=8, seed=2), 0.06, 2)
     F, ep, vir = _lj_oracle(oracle, s)
-    with gpu_ctx(gpu, s, LJ, 0.3, mixed=True, tpa=tpa) as ctx:
+    with gpu_ctx(gpu, s, LJ, 0.3, mixed=True, tpa=tpa, vec=vec) as ctx:
         ctx.compute_forces(energy=True, virial=True)
         d = ctx.download(virial=True)
     G = np.stack([d["ax"], d["ay"], d["az"]], 1)
@@ -130,7 +131,8 @@ def test_lj_mixed_within_tolerance(gpu, oracle, tpa):
     assert rel_rms(d["vir"], vir) < 1e-5
 
 
-def test_lj_multi_matches_oracle(gpu, oracle):
+@pytest.mark.parametrize("vec", [1, 4])
+def test_lj_multi_matches_oracle(gpu, oracle, vec):
     s = _jitter(S.lj_fcc(ncell=6, seed=3), 0.05, 3)
     rng = np.random.default_rng(3)
     s.type = (rng.random(s.n) < 0.2).astype(np.uint8)
@@ -143,7 +145,7 @@ def test_lj_multi_matches_oracle(gpu, oracle):
     fx, fy, fz, ep, vir = oracle.lj_multi_force(x, y, z, s.type, nl, s.L, eps, sig, rc, rcmax)
     F = np.stack([fx, fy, fz], 1) / s.masses[s.type][:, None]
     for mixed, tol in ((False, FP64_TOL), (True, MIXED_FORCE_TOL)):
-        with gpu_ctx(gpu, s, lambda c: c.set_lj_multi(eps, sig, rc, 0.0), 0.3, mixed=mixed) as ctx:
+        with gpu_ctx(gpu, s, lambda c: c.set_lj_multi(eps, sig, rc, 0.0), 0.3, mixed=mixed, tpa=1, vec=vec) as ctx:
             ctx.compute_forces(energy=True)
             d = ctx.download()
         G = np.stack([d["ax"], d["ay"], d["az"]], 1)
@@ -159,14 +161,15 @@ def _eam_setup(oracle, ncell=5, displace=0.08, seed=4):
     return sf, tab, s
 
 
-@pytest.mark.parametrize("tpa", [1, 4, 8])
-def test_eam_fp64_and_mixed_match_oracle(gpu, oracle, tpa):
+@pytest.mark.parametrize("tpa,vec", [(1, 1), (4, 1), (8, 1), (1, 4), (2, 4)])
+def test_eam_fp64_and_mixed_match_oracle(gpu, oracle, tpa, vec):
     sf, tab, s = _eam_setup(oracle)
     ref, (x, y, z), nl = oracle_lists(oracle, s, 5.3)
     fx, fy, fz, ep, vir, fp, rho = oracle.eam_forces(x, y, z, s.type, nl, s.L, tab, 5.0)
     F = np.stack([fx, fy, fz], 1) / s.masses[0]
     for mixed, tol in ((False, FP64_TOL), (True, MIXED_FORCE_TOL)):
-        with gpu_ctx(gpu, s, lambda c: c.set_eam_alloy(sf, 5.0, S.EV, S.EV), 0.3, mixed=mixed, tpa=tpa) as ctx:
+        with gpu_ctx(gpu, s, lambda c: c.set_eam_alloy(sf, 5.0, S.EV, S.EV), 0.3, mixed=mixed, tpa=tpa,
+                     vec=vec) as ctx:
             ctx.compute_forces(energy=True, virial=True)
             d = ctx.download(virial=True)
             if not mixed:
@@ -176,6 +179,40 @@ def test_eam_fp64_and_mixed_match_oracle(gpu, oracle, tpa):
         assert rel_rms(G, F) < tol, (mixed, rel_rms(G, F))
         etol = FP64_TOL if not mixed else 1e-6
         assert abs(d["ep"].sum() - ep.sum()) < etol * abs(ep.sum())
+        assert rel_rms(d["vir"], vir) < (FP64_TOL if not mixed else 1e-5)
+
+
+def _two_element_setfl():
+    """Cu-like element 0 and a stiffer, larger element 1 (A x1.1, re x1.03),
+    cross pair z2r = mean of the two; same knot grids."""
+    cfg = SF.load_cu_params()
+    a = SF.tabulate(cfg)
+    b = SF.tabulate(cfg, {"A": cfg["params"]["A"] * 1.1, "re": cfg["params"]["re"] * 1.03})
+    return SF.Setfl(["Cu", "Xx"], [29, 30], [a.masses[0], 1.1 * a.masses[0]], [a.a0[0], a.a0[0]],
+                    [a.structs[0], a.structs[0]], a.nrho, a.drho, a.nr, a.dr, a.rcut,
+                    [a.frho[0], b.frho[0]], [a.rhor[0], b.rhor[0]],
+                    [a.z2r[0], 0.5 * (a.z2r[0] + b.z2r[0]), b.z2r[0]])
+
+
+@pytest.mark.parametrize("vec", [1, 4])
+def test_eam_two_elements_match_oracle(gpu, oracle, vec):
+    sf = _two_element_setfl()
+    tab = oracle.EamOracleTables.from_setfl(sf, S.EV, S.EV, rcut=5.0)
+    s = S.eam_cu_fcc(ncell=5, displace=0.08, seed=14)
+    rng = np.random.default_rng(14)
+    s.type = (rng.random(s.n) < 0.3).astype(np.uint8)
+    s.masses = np.array(sf.masses)
+    _, (x, y, z), nl = oracle_lists(oracle, s, 5.3)
+    fx, fy, fz, ep, vir, fp, rho = oracle.eam_forces(x, y, z, s.type, nl, s.L, tab, 5.0)
+    F = np.stack([fx, fy, fz], 1) / s.masses[s.type][:, None]
+    for mixed, tol in ((False, FP64_TOL), (True, MIXED_FORCE_TOL)):
+        with gpu_ctx(gpu, s, lambda c: c.set_eam_alloy(sf, 5.0, S.EV, S.EV), 0.3, mixed=mixed, tpa=1,
+                     vec=vec) as ctx:
+            ctx.compute_forces(energy=True, virial=True)
+            d = ctx.download(virial=True)
+        G = np.stack([d["ax"], d["ay"], d["az"]], 1)
+        assert rel_rms(G, F) < tol, (mixed, rel_rms(G, F))
+        assert abs(d["ep"].sum() - ep.sum()) < (FP64_TOL if not mixed else 1e-6) * abs(ep.sum())
         assert rel_rms(d["vir"], vir) < (FP64_TOL if not mixed else 1e-5)
 
 

@@ -79,3 +79,17 @@ def test_trigger_minimiser_matches_oracle(gpu, oracle):
     for k in ("x", "y", "z"):
         dd = np.abs(d[k] - st[k])
         assert np.minimum(dd, s.L[0] - dd).max() < 1e-8, k
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_fixed_interval_build_count(gpu, use_graph):
+    s = S.lj_fcc(ncell=8, density=0.8442, T=1.0, seed=6)
+    with gpu.Context(0) as ctx:
+        ctx.upload_system(s)
+        ctx.set_lj(1.0, 1.0, 2.5)
+        ctx.set_skin(0.3)
+        ctx.set_precision(True)
+        ctx.build_neighbors()
+        b0 = ctx.list_builds()
+        ctx.run_nve(101, 0.005, rebuild_every=10, thermo_every=20, use_graph=use_graph)
+        assert ctx.list_builds() - b0 == 10
