@@ -535,7 +535,11 @@ int gbmd_set_eam_alloy(gbmd_context* c, int nel, int nrho, double drho, int nr, 
     spline7(nr, dr, f.data(), &c->eam_host_z2r[q * kr * 8]);
   }
   const size_t nd = c->eam_host_frho.size() + c->eam_host_rhor.size() + c->eam_host_z2r.size();
-  const size_t nf = nel * kp + nel * kr + npairs * kr + nel * kr;
+  // FP32 tables, then (one element) rho' and z2r interleaved per knot, starting
+  // on a 32-byte boundary so a knot's two float4 share one sector
+  const size_t nf0 = nel * kp + nel * kr + npairs * kr + nel * kr;
+  const size_t fz_off = (nf0 + 1) & ~(size_t)1;
+  const size_t nf = nel == 1 ? fz_off + 2 * kr : nf0;
   cudaFree(c->eam_d);
   cudaFree(c->eam_f);
   c->eam_d = nullptr;
@@ -566,6 +570,11 @@ int gbmd_set_eam_alloy(gbmd_context* c, int nel, int nrho, double drho, int nr, 
       const double* s = &c->eam_host_rhor[(e * kr + m) * 8];
       hf[o++] = make_float4((float)(3.0 * s[3] / dr), (float)(2.0 * s[4] / dr), (float)(s[5] / dr), 0.f);
     }
+  if (nel == 1)
+    for (size_t m = 0; m < kr; ++m) {
+      hf[fz_off + 2 * m] = hf[nel * kp + nel * kr + npairs * kr + m];  // rho' coefficients
+      hf[fz_off + 2 * m + 1] = hf[nel * kp + nel * kr + m];           // z2r coefficients
+    }
   GBMD_CUDA(c, cudaMemcpy(c->eam_d, hd.data(), sizeof(double) * nd, cudaMemcpyHostToDevice));
   GBMD_CUDA(c, cudaMemcpy(c->eam_f, hf.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice));
   EamDev& E = c->eam;
@@ -587,6 +596,7 @@ int gbmd_set_eam_alloy(gbmd_context* c, int nel, int nrho, double drho, int nr, 
   E.rhor4 = c->eam_f + nel * kp;
   E.z2r4 = E.rhor4 + nel * kr;
   E.rhod4 = E.z2r4 + npairs * kr;
+  E.fz8 = nel == 1 ? c->eam_f + fz_off : nullptr;
   E.rdrf = (float)E.rdr;
   E.rdrhof = (float)E.rdrho;
   E.rhomaxf = (float)E.rhomax;

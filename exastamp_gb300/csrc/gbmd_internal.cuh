@@ -69,6 +69,7 @@ struct EamDev {
   const float4* rhor4; // nel x (nr+1)
   const float4* z2r4;  // npairs x (nr+1)      z2r * conv_z2r
   const float4* rhod4; // nel x (nr+1)         rho' coefficients (3c3, 2c4, c5) / dr
+  const float4* fz8;   // one element: (nr+1) x {rhod4, z2r4}, 32-byte aligned knots
   float rdrf, rdrhof, rhomaxf, rc2f, rc2lo, rc2hi;
 };
 

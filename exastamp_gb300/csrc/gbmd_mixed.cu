@@ -289,6 +289,14 @@ __global__ void __launch_bounds__(256) k_eam_rho_mixed(PairArgs A, EamDev E, flo
   }
 }
 
+// One 32-byte load of a knot's two float4 (rho' and z2r coefficients of the
+// interleaved one-element table; the address is 32-byte aligned).
+__device__ __forceinline__ void ldg_knot_pair(const float4* p, float4& a, float4& b) {
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(p));
+}
+
 __device__ __forceinline__ int z2r_index_d(int a, int b) {
   const int irow = a > b ? a : b, icol = a > b ? b : a;
   return irow * (irow + 1) / 2 + icol;
@@ -342,15 +350,21 @@ __global__ void __launch_bounds__(256) k_eam_force_mixed(PairArgs A, EamDev E, c
       float t;
       const int m = knot_f(rd, rdr, nr, t);
       const int tj = SINGLE ? 0 : __float_as_int(pj[q].w);
-      // rho'(r) from the pre-scaled derivative table: (3c3/dr, 2c4/dr, c5/dr)
-      const float4 dj = __ldg(&E.rhod4[SINGLE ? m : tj * nr1 + m]);
+      // rho'(r) from the pre-scaled derivative table: (3c3/dr, 2c4/dr, c5/dr);
+      // one element: rho' and z2r knots interleaved, read in one 32 B load
+      float4 dj, cz;
+      if (SINGLE) {
+        ldg_knot_pair(&E.fz8[2 * m], dj, cz);
+      } else {
+        dj = __ldg(&E.rhod4[tj * nr1 + m]);
+        cz = __ldg(&E.z2r4[z2r_index_d(ti, tj) * nr1 + m]);
+      }
       const float rhojp = fmaf(fmaf(dj.x, t, dj.y), t, dj.z);
       float rhoip = rhojp;
       if (!SINGLE && ti != tj) {
         const float4 di = __ldg(&E.rhod4[ti * nr1 + m]);
         rhoip = fmaf(fmaf(di.x, t, di.y), t, di.z);
       }
-      const float4 cz = __ldg(&E.z2r4[SINGLE ? m : z2r_index_d(ti, tj) * nr1 + m]);
       const float t1 = fmaf(cz.x, t, cz.y);
       const float z2 = fmaf(fmaf(t1, t, cz.z), t, cz.w);          // z2r tables carry conv_z2r
       const float z2d = fmaf(fmaf(cz.x, t, t1 + t1), t, cz.z);     // d z2 / d t
