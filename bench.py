@@ -233,7 +233,7 @@ def _oracle():
     return O
 
 
-def cpu_oracle_rate(w, target_s=12.0, ncell=None):
+def cpu_oracle_rate(w, target_s=15.0, ncell=None):
     """FP64 OpenMP oracle NVE throughput on a sample of the workload."""
     O = _oracle()
     nc = ncell or min(w.get("ncell", 20), 24 if w["kind"] == "eam" else 20)
@@ -242,7 +242,7 @@ def cpu_oracle_rate(w, target_s=12.0, ncell=None):
     t0 = time.perf_counter()
     O.run_nve(st, s.masses, s.lo, s.hi, pot_kind, pot, w["skin"], w["dt"], 2, 10, thermo=False)
     t_cal = (time.perf_counter() - t0) / 3.0
-    steps = int(max(3, min(200, target_s / max(t_cal, 1e-6))))
+    steps = int(max(3, min(5000, target_s / max(t_cal, 1e-6))))
     st = {k: v.copy() for k, v in st0.items()}
     t0 = time.perf_counter()
     O.run_nve(st, s.masses, s.lo, s.hi, pot_kind, pot, w["skin"], w["dt"], steps, 10, thermo=False)

@@ -155,9 +155,9 @@ struct gbmd_context {
   int32_t* nnb = nullptr;
   int64_t nbr_cap = 0;          // entries allocated
   int maxnb = 0;                // per-atom capacity (multiple of tpa * vec)
-  int tpa = 4;                  // lanes per atom (autotuned)
-  int vec = 1;                  // list entries per lane per load (1 or 4, mixed kernels; autotuned)
-  int block = 128;              // threads per block (autotuned)
+  int tpa = 1;                  // lanes per atom (autotuned; default = the GB300 optimum)
+  int vec = 4;                  // list entries per lane per load (1 or 4, mixed kernels; autotuned)
+  int block = 256;              // threads per block (autotuned)
   double skin = 0.0, rlist = 0.0;
   bool list_valid = false;
   int64_t list_builds = 0;

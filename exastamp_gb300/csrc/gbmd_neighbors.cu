@@ -304,30 +304,30 @@ __device__ __noinline__ bool exact_within(const double* __restrict__ x, const do
                   (double)nzi * g.L[2], a, b, c) <= R2;
 }
 
-constexpr int BUILD_HB = 16;    // home atoms per group (one per half-warp lane)
-constexpr int BUILD_CHUNK = 64; // candidates staged per chunk (two per step)
+constexpr int BUILD_CHUNK = 64;  // candidates staged per chunk
+constexpr int BUILD_WARPS = 4;   // warps per block
 
-// One warp per home cell.  The home atoms are taken 16 at a time; lane l
-// and lane l+16 hold the same home atom.  Lane s < 27 describes stencil cell
-// s (start, count, code, FP32 shift); the 27 candidate ranges are
-// concatenated in stencil order, staged 64 at a time in shared memory
-// (position shifted into the home cell's frame, index and stencil code), and
-// each step tests two consecutive candidates against the 16 home atoms: the
-// low half-warp candidate 2t, the high half-warp candidate 2t+1, both read
-// as shared-memory broadcasts.  The two lanes of a home atom exchange their
-// hits with one shuffle and append them in candidate order, which is the
-// canonical order (stencil code, then cell order), to the atom's row of a
-// shared-memory tile; the tile goes out in coalesced list rows.
-__global__ void __launch_bounds__(128) k_build_list_cells(
+// One warp per home cell; each lane holds one home atom (32 at a time).  Lane
+// s < 27 describes stencil cell s (start, count, code, FP32 shift); the 27
+// candidate ranges are concatenated in stencil order and staged 64 at a time
+// in shared memory (position shifted into the home cell's frame, index and
+// stencil code).  Every step all lanes test the same candidate, read as a
+// shared-memory broadcast, against their own home atom and append hits in
+// candidate order -- the canonical order (stencil code, then cell order) --
+// straight to the atom's list row.  The walk keeps every candidate with FP32
+// d2 <= R^2 (1 + 2^-12) and only flags the atom when one lies above
+// R^2 (1 - 2^-12); flagged atoms (a few per cent) then rescan their row with
+// the same rounded FP32 operations, re-test those entries in FP64 and
+// compact, so the walk itself has no call and no divergent branch.
+__global__ void __launch_bounds__(BUILD_WARPS * 32) k_build_list_cells(
     int64_t ncells, const float4* __restrict__ pf, const double* __restrict__ x, const double* __restrict__ y,
     const double* __restrict__ z, const int32_t* __restrict__ cstart, Grid g, double R2, float R2lo, float R2hi,
-    uint32_t* __restrict__ nbr, int32_t* __restrict__ nnb, int maxnb, int T, int64_t stride,
+    uint32_t* __restrict__ nbr, int32_t* __restrict__ nnb, int maxnb, int W, int64_t stride,
     int* __restrict__ err, const int* __restrict__ gate) {
   const int64_t cell = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (cell >= ncells || (gate && !*gate)) return;  // uniform per warp
   const unsigned FULL = 0xffffffffu;
-  const int half = lane >> 4, hl = lane & 15;
   const int cx = (int)(cell % g.nc[0]), cy = (int)((cell / g.nc[0]) % g.nc[1]),
             cz = (int)(cell / ((int64_t)g.nc[0] * g.nc[1]));
   // stencil cell of this lane
@@ -355,23 +355,18 @@ __global__ void __launch_bounds__(128) k_build_list_cells(
   const int s_pre = incl - s_cnt;  // exclusive prefix of this lane's stencil cell
   const int total = __shfl_sync(FULL, incl, 26);
   const int hb = cstart[cell], nh = cstart[cell + 1] - hb;
-  int tsh = 0;
-  while ((1 << tsh) < T) ++tsh;
-  // per-warp shared memory: 64 staged candidates, 16 counts (padded to 32),
-  // 16 x maxnb tile entries
-  extern __shared__ float4 smem_build[];
-  float4* stage = smem_build + (size_t)(threadIdx.x >> 5) * (BUILD_CHUNK + 8 + BUILD_HB / 4 * (size_t)maxnb);
-  int* cnt_s = reinterpret_cast<int*>(stage + BUILD_CHUNK);
-  uint32_t* tile = reinterpret_cast<uint32_t*>(stage + BUILD_CHUNK + 8);
-  uint32_t* my_row = tile + hl * maxnb;
+  int wsh = 0;
+  while ((1 << wsh) < W) ++wsh;
+  __shared__ float4 stage_all[BUILD_WARPS][BUILD_CHUNK];
+  float4* stage = stage_all[threadIdx.x >> 5];
   const float FAR = 1e18f;
   int warp_max = 0;
-  for (int h0 = 0; h0 < nh; h0 += BUILD_HB) {
-    const int nhb = min(BUILD_HB, nh - h0);
-    const bool hv = hl < nhb;
-    const int i = hb + h0 + hl;
+  for (int h0 = 0; h0 < nh; h0 += 32) {
+    const bool hv = h0 + lane < nh;
+    const int i = hb + h0 + lane;
     float4 pi = make_float4(FAR, FAR, FAR, 0.f);
     if (hv) pi = pf[i];
+    uint32_t* row = nbr + (size_t)i * W;  // slot k at row[(k >> wsh) * stride + (k & (W - 1))]
     int cnt = 0;
     bool unc = false;
     for (int q0 = 0; q0 < total; q0 += BUILD_CHUNK) {
@@ -401,78 +396,55 @@ __global__ void __launch_bounds__(128) k_build_list_cells(
       }
       __syncwarp();
       const int m = min(BUILD_CHUNK, total - q0);
-#pragma unroll 2
-      for (int t = 0; t < m; t += 2) {
-        const float4 e = stage[t + half];
+#pragma unroll 4
+      for (int t = 0; t < m; ++t) {
+        const float4 e = stage[t];
         const uint32_t w = __float_as_uint(e.w);
-        const int k = (int)(w & GBMD_IDX_MASK);
         const float dx = __fsub_rn(e.x, pi.x);
         const float dy = __fsub_rn(e.y, pi.y);
         const float dz = __fsub_rn(e.z, pi.z);
         const float d2f = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
         // an atom never pairs with itself: its images sit at least one box
-        // edge >= R away, so k == i only ever matters in the home cell.
-        // Candidates inside R^2 (1 + 2^-12) are kept; those in the band
-        // above R^2 (1 - 2^-12) are re-tested in FP64 after the walk.
-        const bool in = hv && k != i && d2f <= R2hi;
+        // edge >= R away, so k == i only ever matters in the home cell
+        const bool in = hv && (int)(w & GBMD_IDX_MASK) != i && d2f <= R2hi;
         unc |= in && d2f >= R2lo;
-        const int other = __shfl_xor_sync(FULL, (int)in, 16);
         if (in) {
-          const int pos = cnt + (half ? other : 0);  // candidate 2t goes first
-          if (pos < maxnb) my_row[pos] = w;
+          if (cnt < maxnb) row[(size_t)(cnt >> wsh) * stride + (cnt & (W - 1))] = w;
+          ++cnt;
         }
-        cnt += (int)in + other;
       }
     }
-    // deferred FP64 re-test (about one atom in twenty has a band entry): the
-    // atom's lane in the low half rescans its row, recomputes each entry's
-    // FP32 d2 exactly as above, re-tests the band entries and compacts
-    const bool unc_home = __shfl_xor_sync(FULL, (int)unc, 16) != 0 || unc;
-    if (__any_sync(FULL, unc_home)) {
-      if (half == 0 && hv && unc_home) {
-        const int nkeep = min(cnt, maxnb);
-        int wpos = 0;
-        for (int p = 0; p < nkeep; ++p) {
-          const uint32_t w = my_row[p];
-          const int k = (int)(w & GBMD_IDX_MASK);
-          const uint32_t code = w >> GBMD_IDX_BITS;
-          const float4 pj = pf[k];
-          // the same rounded operations as the staging and the walk
-          const float sx = __fmul_rn((float)((int)(code & 3u) - 1), g.hf[0]);
-          const float sy = __fmul_rn((float)((int)((code >> 2) & 3u) - 1), g.hf[1]);
-          const float sz = __fmul_rn((float)((int)(code >> 4) - 1), g.hf[2]);
-          const float dx = __fsub_rn(__fadd_rn(pj.x, sx), pi.x);
-          const float dy = __fsub_rn(__fadd_rn(pj.y, sy), pi.y);
-          const float dz = __fsub_rn(__fadd_rn(pj.z, sz), pi.z);
-          const float d2f = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
-          bool keepit = true;
-          if (d2f >= R2lo) keepit = exact_within(x, y, z, i, k, code, cx, cy, cz, g, R2);
-          if (keepit) my_row[wpos++] = w;
+    // deferred FP64 re-test of the band entries, row compacted in place
+    if (unc) {
+      const int nkeep = min(cnt, maxnb);
+      int wpos = 0;
+      for (int p = 0; p < nkeep; ++p) {
+        const uint32_t w = row[(size_t)(p >> wsh) * stride + (p & (W - 1))];
+        const int k = (int)(w & GBMD_IDX_MASK);
+        const uint32_t code = w >> GBMD_IDX_BITS;
+        const float4 pj = pf[k];
+        // the same rounded operations as the staging and the walk
+        const float sx = __fmul_rn((float)((int)(code & 3u) - 1), g.hf[0]);
+        const float sy = __fmul_rn((float)((int)((code >> 2) & 3u) - 1), g.hf[1]);
+        const float sz = __fmul_rn((float)((int)(code >> 4) - 1), g.hf[2]);
+        const float dx = __fsub_rn(__fadd_rn(pj.x, sx), pi.x);
+        const float dy = __fsub_rn(__fadd_rn(pj.y, sy), pi.y);
+        const float dz = __fsub_rn(__fadd_rn(pj.z, sz), pi.z);
+        const float d2f = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
+        bool keepit = true;
+        if (d2f >= R2lo) keepit = exact_within(x, y, z, i, k, code, cx, cy, cz, g, R2);
+        if (keepit) {
+          row[(size_t)(wpos >> wsh) * stride + (wpos & (W - 1))] = w;
+          ++wpos;
         }
-        cnt -= nkeep - wpos;
       }
-      cnt = __shfl_sync(FULL, cnt, hl);  // the high-half lane takes the corrected count
+      cnt -= nkeep - wpos;
     }
-    if (hv && half == 0) {
+    if (hv) {
       nnb[i] = cnt;
       if (cnt > maxnb) atomicOr(&err[ERRW_FLAGS], GBMD_DEVERR_NBR_OVERFLOW);
+      warp_max = max(warp_max, cnt);
     }
-    if (half == 0) cnt_s[hl] = hv ? min(cnt, maxnb) : 0;
-    warp_max = max(warp_max, hv ? cnt : 0);
-    __syncwarp();
-    int bmax = half == 0 ? cnt_s[hl] : 0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) bmax = max(bmax, __shfl_xor_sync(FULL, bmax, o));
-    // coalesced write-out: list row r holds slots r*T..r*T+T-1 of consecutive
-    // atoms contiguously, so the group's part of a row is nhb*T adjacent words
-    const int64_t row0 = (int64_t)(hb + h0) * T;
-    for (int r = 0; r * T < bmax; ++r) {
-      for (int wi = lane; wi < nhb * T; wi += 32) {
-        const int hh = wi >> tsh, pos = r * T + (wi & (T - 1));
-        if (pos < cnt_s[hh]) nbr[(int64_t)r * stride + row0 + wi] = tile[hh * maxnb + pos];
-      }
-    }
-    __syncwarp();  // tile and counts are reused by the next group
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) warp_max = max(warp_max, __shfl_xor_sync(FULL, warp_max, o));
@@ -504,15 +476,7 @@ static int build_list(gbmd_context* c, const int* gate) {
   }
   c->npad = npad;
   if (!gate) GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_MAXNB, 0, sizeof(int), c->stream));
-  // shared memory per warp: BUILD_CHUNK staged candidates + 32 counts + BUILD_HB x maxnb entries
-  const size_t per_warp = 16 * (BUILD_CHUNK + 8) + 4 * BUILD_HB * (size_t)c->maxnb;
-  int nw = (int)((96 * 1024) / per_warp);  // warps per block
-  nw = nw < 1 ? 1 : (nw > 4 ? 4 : nw);
-  const size_t smem = per_warp * nw;
-  if (smem > 227 * 1024) return set_error(c, GBMD_ERR_TOO_LARGE, "neighbour capacity %d per atom too large", c->maxnb);
-  if (smem > 48 * 1024)
-    GBMD_CUDA(c, cudaFuncSetAttribute(k_build_list_cells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_build_list_cells<<<nblk(c->grid.ncells, nw), 32 * nw, smem, c->stream>>>(
+  k_build_list_cells<<<nblk(c->grid.ncells, BUILD_WARPS), 32 * BUILD_WARPS, 0, c->stream>>>(
       c->grid.ncells, c->POSF(), c->X(), c->Y(), c->Z(), c->cell_start, c->grid, R2, R2lo, R2hi, c->nbr, c->nnb,
       c->maxnb, W, stride, c->d_err, gate);
   return GBMD_OK;
