@@ -84,6 +84,7 @@ def lib(path: str = LIB_PATH):
             "gbmd_push_min": ([vp, dbl, dbl, dbl], i32),
             "gbmd_run_nve": ([vp, i32, dbl, i32, i32, vp, i32], i32),
             "gbmd_run_minimize": ([vp, i32, dbl, dbl, i32], i32),
+            "gbmd_set_eam_johnson": ([vp, vp, dbl], i32),
             "gbmd_list_builds": ([vp, P(i64)], i32),
             "gbmd_thermo": ([vp, vp], i32),
             "gbmd_device_state": ([vp] + [vp] * 11, i32),
@@ -274,6 +275,13 @@ class Context:
 
     def run_minimize(self, nsteps, dt, tolF=0.0, rebuild_every=10):
         self._chk(self._L.gbmd_run_minimize(self.h, int(nsteps), float(dt), float(tolF), int(rebuild_every)))
+
+    def set_eam_johnson(self, params, rcut):
+        """johnson_force: params = 19 values in EamJohnsonParameters order."""
+        p = _f64(params)
+        if p.shape != (19,):
+            raise ValueError("johnson_force takes 19 parameters")
+        self._chk(self._L.gbmd_set_eam_johnson(self.h, _p(p), float(rcut)))
 
     def list_builds(self):
         n = C.c_int64(0)

@@ -118,6 +118,7 @@ static void set_rlist(gbmd_context* c, double rcut_max) {
 static double pot_rcut_max(const gbmd_context* c) {
   if (c->pot == GBMD_POT_LJ || c->pot == GBMD_POT_LJ_MULTI) return c->lj.rcut_max;
   if (c->pot == GBMD_POT_EAM_ALLOY) return c->eam.rcut;
+  if (c->pot == GBMD_POT_EAM_JOHNSON) return c->ej.rcut;
   return 0.0;
 }
 
@@ -635,6 +636,37 @@ int gbmd_load_setfl(gbmd_context* c, const char* path, double rcut, double conv_
   if (!in) return set_error(c, GBMD_ERR_IO, "truncated setfl file %s", path);
   return gbmd_set_eam_alloy(c, nel, nrho, drho, nr, dr, frho.data(), rhor.data(), z2r.data(),
                             rcut > 0 ? rcut : rc, conv_z2r, conv_frho);
+}
+
+// johnson_force parameters (johnson.h L28-49), see gbmd_johnson.cu
+int gbmd_set_eam_johnson(gbmd_context* c, const double params[19], double rcut) {
+  if (!c || !params || !(rcut > 0.0)) return GBMD_ERR_INVALID;
+  gbmd::JohnsonDev P{};
+  const double* q = params;
+  P.re = q[0]; P.fe = q[1]; P.rhoe = q[2]; P.alpha = q[3]; P.beta = q[4]; P.A = q[5]; P.B = q[6];
+  P.kappa = q[7]; P.lambda = q[8]; P.Fn0 = q[9]; P.Fn1 = q[10]; P.Fn2 = q[11]; P.Fn3 = q[12];
+  P.F0 = q[13]; P.F1 = q[14]; P.F2 = q[15]; P.F3 = q[16]; P.Fo = q[17]; P.eta = q[18];
+  for (int k = 0; k < 19; ++k)
+    if (!std::isfinite(q[k])) return set_error(c, GBMD_ERR_INVALID, "johnson parameter %d not finite", k);
+  if (!(P.re > 0.0) || !(P.rhoe > 0.0)) return set_error(c, GBMD_ERR_INVALID, "re and rhoe must be > 0");
+  P.rcut = rcut;
+  P.rcut2 = rcut * rcut;
+  P.ref = (float)P.re;
+  P.ire_f = (float)(1.0 / P.re);
+  P.fef = (float)P.fe;
+  P.alphaf = (float)P.alpha;
+  P.betaf = (float)P.beta;
+  P.Af = (float)P.A;
+  P.Bf = (float)P.B;
+  P.kappaf = (float)P.kappa;
+  P.lambdaf = (float)P.lambda;
+  P.rc2lo = (float)(P.rcut2 * (1.0 - 0x1p-12));
+  P.rc2hi = (float)(P.rcut2 * (1.0 + 0x1p-12));
+  c->ej = P;
+  c->pot = GBMD_POT_EAM_JOHNSON;
+  c->forces_valid_step = -1;
+  set_rlist(c, rcut);
+  return GBMD_OK;
 }
 
 int gbmd_set_precision(gbmd_context* c, int precision) {

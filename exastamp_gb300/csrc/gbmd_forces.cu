@@ -326,7 +326,8 @@ int launch_forces(gbmd_context* c, const ForceFlags& f) {
   const bool mixed = c->precision == GBMD_PRECISION_MIXED;
   const int part = f.part;
   int rc;
-  if (mixed) rc = launch_mixed(c, A, part, ev);
+  if (c->pot == GBMD_POT_EAM_JOHNSON) rc = launch_johnson(c, A, part, ev, mixed);
+  else if (mixed) rc = launch_mixed(c, A, part, ev);
   else rc = ev ? launch_fp64<true>(c, A, part) : launch_fp64<false>(c, A, part);
   if (rc) return rc;
   if (f.fuse == FUSE_PUSH2_PUSH1 && part != 1) c->cur ^= 1;

@@ -73,6 +73,14 @@ struct EamDev {
   float rdrf, rdrhof, rhomaxf, rc2f, rc2lo, rc2hi;
 };
 
+// johnson_force parameters (EamJohnsonParameters order) in FP64 and FP32.
+struct JohnsonDev {
+  double re, fe, rhoe, alpha, beta, A, B, kappa, lambda, Fn0, Fn1, Fn2, Fn3, F0, F1, F2, F3, Fo, eta;
+  double rcut, rcut2;
+  float ref, ire_f, fef, alphaf, betaf, Af, Bf, kappaf, lambdaf;
+  float rc2lo, rc2hi;
+};
+
 struct Grid {
   int nc[3];
   double h[3], L[3], lo[3];
@@ -165,6 +173,7 @@ struct gbmd_context {
 
   // potential
   int pot = GBMD_POT_NONE;
+  gbmd::JohnsonDev ej{};
   gbmd::LJTable lj{};
   gbmd::EamDev eam{};
   double* eam_d = nullptr;      // device FP64 tables (one allocation)

@@ -307,18 +307,161 @@ __device__ __noinline__ bool exact_within(const double* __restrict__ x, const do
 constexpr int BUILD_CHUNK = 64;  // candidates staged per chunk
 constexpr int BUILD_WARPS = 4;   // warps per block
 
-// One warp per home cell; each lane holds one home atom (32 at a time).  Lane
-// s < 27 describes stencil cell s (start, count, code, FP32 shift); the 27
-// candidate ranges are concatenated in stencil order and staged 64 at a time
-// in shared memory (position shifted into the home cell's frame, index and
-// stencil code).  Every step all lanes test the same candidate, read as a
-// shared-memory broadcast, against their own home atom and append hits in
-// candidate order -- the canonical order (stencil code, then cell order) --
-// straight to the atom's list row.  The walk keeps every candidate with FP32
-// d2 <= R^2 (1 + 2^-12) and only flags the atom when one lies above
-// R^2 (1 - 2^-12); flagged atoms (a few per cent) then rescan their row with
-// the same rounded FP32 operations, re-test those entries in FP64 and
-// compact, so the walk itself has no call and no divergent branch.
+// Per-warp state of the candidate walk shared by both groupings.
+struct BuildCell {
+  int cx, cy, cz, total, hb, nh;
+  int s_start, s_pre;
+  uint32_t s_code;
+  float s_sx, s_sy, s_sz;
+};
+
+// Stage candidates q0 .. q0+63 (position shifted into the home cell's frame,
+// index | stencil code << 26) into this warp's shared-memory buffer.
+__device__ __forceinline__ void build_stage(const BuildCell& B, const float4* __restrict__ pf, int q0,
+                                            float4* stage, int lane) {
+  const unsigned FULL = 0xffffffffu;
+  const float FAR = 1e18f;
+#pragma unroll
+  for (int r = 0; r < BUILD_CHUNK / 32; ++r) {
+    const int q = q0 + r * 32 + lane;
+    // stencil cell of candidate q: largest s with s_pre(s) <= q (5-step search)
+    int sc = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+      const int t = min(sc + step, 26);
+      const int pv = __shfl_sync(FULL, B.s_pre, t);
+      if (sc + step <= 26 && pv <= q) sc = t;
+    }
+    const int k = __shfl_sync(FULL, B.s_start, sc) + (q - __shfl_sync(FULL, B.s_pre, sc));
+    const uint32_t code = __shfl_sync(FULL, B.s_code, sc);
+    const float sx = __shfl_sync(FULL, B.s_sx, sc), sy = __shfl_sync(FULL, B.s_sy, sc),
+                sz = __shfl_sync(FULL, B.s_sz, sc);
+    float4 e = make_float4(FAR, FAR, FAR, __uint_as_float(0xffffffffu));
+    if (q < B.total) {
+      const float4 pj = pf[k];
+      e = make_float4(__fadd_rn(pj.x, sx), __fadd_rn(pj.y, sy), __fadd_rn(pj.z, sz),
+                      __uint_as_float((uint32_t)k | (code << GBMD_IDX_BITS)));
+    }
+    stage[r * 32 + lane] = e;
+  }
+}
+
+// Deferred FP64 re-test of an atom's band entries: recompute each entry's
+// FP32 d2 with the rounded operations of the staging and the walk, re-test
+// the band ones and compact the row in place.  Returns the entries dropped.
+__device__ __noinline__ int build_retest_row(uint32_t* row, int nkeep, int wsh, int W, int64_t stride,
+                                             const float4* __restrict__ pf, float4 pi, const double* __restrict__ x,
+                                             const double* __restrict__ y, const double* __restrict__ z, int i,
+                                             int cx, int cy, int cz, const Grid g, double R2, float R2lo) {
+  int wpos = 0;
+  for (int p = 0; p < nkeep; ++p) {
+    const uint32_t w = row[(size_t)(p >> wsh) * stride + (p & (W - 1))];
+    const int k = (int)(w & GBMD_IDX_MASK);
+    const uint32_t code = w >> GBMD_IDX_BITS;
+    const float4 pj = pf[k];
+    const float sx = __fmul_rn((float)((int)(code & 3u) - 1), g.hf[0]);
+    const float sy = __fmul_rn((float)((int)((code >> 2) & 3u) - 1), g.hf[1]);
+    const float sz = __fmul_rn((float)((int)(code >> 4) - 1), g.hf[2]);
+    const float dx = __fsub_rn(__fadd_rn(pj.x, sx), pi.x);
+    const float dy = __fsub_rn(__fadd_rn(pj.y, sy), pi.y);
+    const float dz = __fsub_rn(__fadd_rn(pj.z, sz), pi.z);
+    const float d2f = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
+    bool keepit = true;
+    if (d2f >= R2lo) keepit = exact_within(x, y, z, i, k, code, cx, cy, cz, g, R2);
+    if (keepit) {
+      row[(size_t)(wpos >> wsh) * stride + (wpos & (W - 1))] = w;
+      ++wpos;
+    }
+  }
+  return nkeep - wpos;
+}
+
+// The walk for home groups of G atoms: G = 32, one home atom per lane and one
+// candidate per step; G = 16, lanes l and l+16 hold the same home atom and a
+// step tests candidates 2t (low half) and 2t+1 (high half), the two lanes
+// exchanging their hit with one shuffle so both append in candidate order.
+template <int G>
+__device__ __forceinline__ int build_walk(const BuildCell& B, const float4* __restrict__ pf,
+                                          const double* __restrict__ x, const double* __restrict__ y,
+                                          const double* __restrict__ z, const Grid& g, double R2, float R2lo,
+                                          float R2hi, uint32_t* __restrict__ nbr, int32_t* __restrict__ nnb,
+                                          int maxnb, int W, int wsh, int64_t stride, int* __restrict__ err,
+                                          float4* stage, int lane) {
+  const unsigned FULL = 0xffffffffu;
+  const float FAR = 1e18f;
+  const int half = G == 16 ? (lane >> 4) : 0;
+  const int hl = G == 16 ? (lane & 15) : lane;
+  int warp_max = 0;
+  for (int h0 = 0; h0 < B.nh; h0 += G) {
+    const bool hv = h0 + hl < B.nh;
+    const int i = B.hb + h0 + hl;
+    float4 pi = make_float4(FAR, FAR, FAR, 0.f);
+    if (hv) pi = pf[i];
+    uint32_t* row = nbr + (size_t)i * W;  // slot k at row[(k >> wsh) * stride + (k & (W - 1))]
+    int cnt = 0;
+    bool unc = false;
+    for (int q0 = 0; q0 < B.total; q0 += BUILD_CHUNK) {
+      __syncwarp();
+      build_stage(B, pf, q0, stage, lane);
+      __syncwarp();
+      const int m = min(BUILD_CHUNK, B.total - q0);
+#pragma unroll 4
+      for (int t = 0; t < m; t += (G == 16 ? 2 : 1)) {
+        const float4 e = stage[t + half];
+        const uint32_t w = __float_as_uint(e.w);
+        const float dx = __fsub_rn(e.x, pi.x);
+        const float dy = __fsub_rn(e.y, pi.y);
+        const float dz = __fsub_rn(e.z, pi.z);
+        const float d2f = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
+        // an atom never pairs with itself: its images sit at least one box
+        // edge >= R away, so k == i only ever matters in the home cell.
+        // Keep d2 <= R^2 (1 + 2^-12); flag the atom when d2 >= R^2 (1 - 2^-12).
+        const bool in = hv && (int)(w & GBMD_IDX_MASK) != i && d2f <= R2hi;
+        unc |= in && d2f >= R2lo;
+        if (G == 16) {
+          const int other = __shfl_xor_sync(FULL, (int)in, 16);
+          if (in) {
+            const int pos = cnt + (half ? other : 0);  // candidate 2t goes first
+            if (pos < maxnb) row[(size_t)(pos >> wsh) * stride + (pos & (W - 1))] = w;
+          }
+          cnt += (int)in + other;
+        } else if (in) {
+          if (cnt < maxnb) row[(size_t)(cnt >> wsh) * stride + (cnt & (W - 1))] = w;
+          ++cnt;
+        }
+      }
+    }
+    if (G == 16) {
+      unc = unc || __shfl_xor_sync(FULL, (int)unc, 16) != 0;
+      __syncwarp();  // the high-half lanes' entries are visible to the low half
+      if (half == 0 && unc) cnt -= build_retest_row(row, min(cnt, maxnb), wsh, W, stride, pf, pi, x, y, z, i,
+                                                    B.cx, B.cy, B.cz, g, R2, R2lo);
+      cnt = __shfl_sync(FULL, cnt, hl);  // the high-half lane takes the corrected count
+    } else if (unc) {
+      cnt -= build_retest_row(row, min(cnt, maxnb), wsh, W, stride, pf, pi, x, y, z, i, B.cx, B.cy, B.cz, g,
+                              R2, R2lo);
+    }
+    if (hv && half == 0) {
+      nnb[i] = cnt;
+      if (cnt > maxnb) atomicOr(&err[ERRW_FLAGS], GBMD_DEVERR_NBR_OVERFLOW);
+      warp_max = max(warp_max, cnt);
+    }
+  }
+  return warp_max;
+}
+
+// One warp per home cell.  Lane s < 27 describes stencil cell s (start,
+// count, code, FP32 shift); the 27 candidate ranges are concatenated in
+// stencil order and staged 64 at a time in shared memory, every candidate is
+// read as a shared-memory broadcast and tested against the home atoms held
+// in the lanes, hits are appended in candidate order -- the canonical order
+// (stencil code, then cell order) -- straight to the atoms' list rows.  Cells
+// of at most 16 atoms use the 16-atom grouping (two candidates per step),
+// fuller cells the 32-atom one.  The walk keeps every candidate with FP32
+// d2 <= R^2 (1 + 2^-12) and flags the atom when one lies above
+// R^2 (1 - 2^-12); flagged atoms (a few per cent) rescan their row, re-test
+// those entries in FP64 and compact, so the walk has no call and no
+// divergent branch.
 __global__ void __launch_bounds__(BUILD_WARPS * 32) k_build_list_cells(
     int64_t ncells, const float4* __restrict__ pf, const double* __restrict__ x, const double* __restrict__ y,
     const double* __restrict__ z, const int32_t* __restrict__ cstart, Grid g, double R2, float R2lo, float R2hi,
@@ -328,23 +471,26 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32) k_build_list_cells(
   const int lane = threadIdx.x & 31;
   if (cell >= ncells || (gate && !*gate)) return;  // uniform per warp
   const unsigned FULL = 0xffffffffu;
-  const int cx = (int)(cell % g.nc[0]), cy = (int)((cell / g.nc[0]) % g.nc[1]),
-            cz = (int)(cell / ((int64_t)g.nc[0] * g.nc[1]));
+  BuildCell B;
+  B.cx = (int)(cell % g.nc[0]);
+  B.cy = (int)((cell / g.nc[0]) % g.nc[1]);
+  B.cz = (int)(cell / ((int64_t)g.nc[0] * g.nc[1]));
   // stencil cell of this lane
-  int s_start = 0, s_cnt = 0;
-  uint32_t s_code = 0;
-  float s_sx = 0.f, s_sy = 0.f, s_sz = 0.f;
+  int s_cnt = 0;
+  B.s_start = 0;
+  B.s_code = 0;
+  B.s_sx = B.s_sy = B.s_sz = 0.f;
   if (lane < 27) {
     const int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
-    const int nx = image_of(cx, dx, g.nc[0]), ny = image_of(cy, dy, g.nc[1]), nz = image_of(cz, dz, g.nc[2]);
-    const int64_t cj = ((int64_t)(cz + dz - nz * g.nc[2]) * g.nc[1] + (cy + dy - ny * g.nc[1])) * g.nc[0] +
-                       (cx + dx - nx * g.nc[0]);
-    s_start = cstart[cj];
-    s_cnt = cstart[cj + 1] - s_start;
-    s_code = (uint32_t)(dx + 1) | ((uint32_t)(dy + 1) << 2) | ((uint32_t)(dz + 1) << 4);
-    s_sx = __fmul_rn((float)dx, g.hf[0]);
-    s_sy = __fmul_rn((float)dy, g.hf[1]);
-    s_sz = __fmul_rn((float)dz, g.hf[2]);
+    const int nx = image_of(B.cx, dx, g.nc[0]), ny = image_of(B.cy, dy, g.nc[1]), nz = image_of(B.cz, dz, g.nc[2]);
+    const int64_t cj = ((int64_t)(B.cz + dz - nz * g.nc[2]) * g.nc[1] + (B.cy + dy - ny * g.nc[1])) * g.nc[0] +
+                       (B.cx + dx - nx * g.nc[0]);
+    B.s_start = cstart[cj];
+    s_cnt = cstart[cj + 1] - B.s_start;
+    B.s_code = (uint32_t)(dx + 1) | ((uint32_t)(dy + 1) << 2) | ((uint32_t)(dz + 1) << 4);
+    B.s_sx = __fmul_rn((float)dx, g.hf[0]);
+    B.s_sy = __fmul_rn((float)dy, g.hf[1]);
+    B.s_sz = __fmul_rn((float)dz, g.hf[2]);
   }
   int incl = s_cnt;
 #pragma unroll
@@ -352,100 +498,19 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32) k_build_list_cells(
     const int t = __shfl_up_sync(FULL, incl, o);
     if (lane >= o) incl += t;
   }
-  const int s_pre = incl - s_cnt;  // exclusive prefix of this lane's stencil cell
-  const int total = __shfl_sync(FULL, incl, 26);
-  const int hb = cstart[cell], nh = cstart[cell + 1] - hb;
+  B.s_pre = incl - s_cnt;  // exclusive prefix of this lane's stencil cell
+  B.total = __shfl_sync(FULL, incl, 26);
+  B.hb = cstart[cell];
+  B.nh = cstart[cell + 1] - B.hb;
   int wsh = 0;
   while ((1 << wsh) < W) ++wsh;
   __shared__ float4 stage_all[BUILD_WARPS][BUILD_CHUNK];
   float4* stage = stage_all[threadIdx.x >> 5];
-  const float FAR = 1e18f;
-  int warp_max = 0;
-  for (int h0 = 0; h0 < nh; h0 += 32) {
-    const bool hv = h0 + lane < nh;
-    const int i = hb + h0 + lane;
-    float4 pi = make_float4(FAR, FAR, FAR, 0.f);
-    if (hv) pi = pf[i];
-    uint32_t* row = nbr + (size_t)i * W;  // slot k at row[(k >> wsh) * stride + (k & (W - 1))]
-    int cnt = 0;
-    bool unc = false;
-    for (int q0 = 0; q0 < total; q0 += BUILD_CHUNK) {
-      __syncwarp();
-#pragma unroll
-      for (int r = 0; r < BUILD_CHUNK / 32; ++r) {
-        const int q = q0 + r * 32 + lane;
-        // stencil cell of candidate q: largest s with s_pre(s) <= q (5-step search)
-        int sc = 0;
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1) {
-          const int t = min(sc + step, 26);
-          const int pv = __shfl_sync(FULL, s_pre, t);
-          if (sc + step <= 26 && pv <= q) sc = t;
-        }
-        const int k = __shfl_sync(FULL, s_start, sc) + (q - __shfl_sync(FULL, s_pre, sc));
-        const uint32_t code = __shfl_sync(FULL, s_code, sc);
-        const float sx = __shfl_sync(FULL, s_sx, sc), sy = __shfl_sync(FULL, s_sy, sc),
-                    sz = __shfl_sync(FULL, s_sz, sc);
-        float4 e = make_float4(FAR, FAR, FAR, __uint_as_float(0xffffffffu));
-        if (q < total) {
-          const float4 pj = pf[k];
-          e = make_float4(__fadd_rn(pj.x, sx), __fadd_rn(pj.y, sy), __fadd_rn(pj.z, sz),
-                          __uint_as_float((uint32_t)k | (code << GBMD_IDX_BITS)));
-        }
-        stage[r * 32 + lane] = e;
-      }
-      __syncwarp();
-      const int m = min(BUILD_CHUNK, total - q0);
-#pragma unroll 4
-      for (int t = 0; t < m; ++t) {
-        const float4 e = stage[t];
-        const uint32_t w = __float_as_uint(e.w);
-        const float dx = __fsub_rn(e.x, pi.x);
-        const float dy = __fsub_rn(e.y, pi.y);
-        const float dz = __fsub_rn(e.z, pi.z);
-        const float d2f = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
-        // an atom never pairs with itself: its images sit at least one box
-        // edge >= R away, so k == i only ever matters in the home cell
-        const bool in = hv && (int)(w & GBMD_IDX_MASK) != i && d2f <= R2hi;
-        unc |= in && d2f >= R2lo;
-        if (in) {
-          if (cnt < maxnb) row[(size_t)(cnt >> wsh) * stride + (cnt & (W - 1))] = w;
-          ++cnt;
-        }
-      }
-    }
-    // deferred FP64 re-test of the band entries, row compacted in place
-    if (unc) {
-      const int nkeep = min(cnt, maxnb);
-      int wpos = 0;
-      for (int p = 0; p < nkeep; ++p) {
-        const uint32_t w = row[(size_t)(p >> wsh) * stride + (p & (W - 1))];
-        const int k = (int)(w & GBMD_IDX_MASK);
-        const uint32_t code = w >> GBMD_IDX_BITS;
-        const float4 pj = pf[k];
-        // the same rounded operations as the staging and the walk
-        const float sx = __fmul_rn((float)((int)(code & 3u) - 1), g.hf[0]);
-        const float sy = __fmul_rn((float)((int)((code >> 2) & 3u) - 1), g.hf[1]);
-        const float sz = __fmul_rn((float)((int)(code >> 4) - 1), g.hf[2]);
-        const float dx = __fsub_rn(__fadd_rn(pj.x, sx), pi.x);
-        const float dy = __fsub_rn(__fadd_rn(pj.y, sy), pi.y);
-        const float dz = __fsub_rn(__fadd_rn(pj.z, sz), pi.z);
-        const float d2f = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
-        bool keepit = true;
-        if (d2f >= R2lo) keepit = exact_within(x, y, z, i, k, code, cx, cy, cz, g, R2);
-        if (keepit) {
-          row[(size_t)(wpos >> wsh) * stride + (wpos & (W - 1))] = w;
-          ++wpos;
-        }
-      }
-      cnt -= nkeep - wpos;
-    }
-    if (hv) {
-      nnb[i] = cnt;
-      if (cnt > maxnb) atomicOr(&err[ERRW_FLAGS], GBMD_DEVERR_NBR_OVERFLOW);
-      warp_max = max(warp_max, cnt);
-    }
-  }
+  int warp_max;
+  if (B.nh <= 16)
+    warp_max = build_walk<16>(B, pf, x, y, z, g, R2, R2lo, R2hi, nbr, nnb, maxnb, W, wsh, stride, err, stage, lane);
+  else
+    warp_max = build_walk<32>(B, pf, x, y, z, g, R2, R2lo, R2hi, nbr, nnb, maxnb, W, wsh, stride, err, stage, lane);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) warp_max = max(warp_max, __shfl_xor_sync(FULL, warp_max, o));
   if (lane == 0 && warp_max > 0) atomicMax(&err[ERRW_MAXNB], warp_max);

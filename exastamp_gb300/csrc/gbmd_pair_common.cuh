@@ -47,6 +47,8 @@ struct PairArgs {
 
 // Mixed-precision pair kernels (gbmd_mixed.cu); part as in launch_forces.
 int launch_mixed(gbmd_context* c, const PairArgs& A, int part, bool ev);
+// johnson_force kernels, both precisions (gbmd_johnson.cu).
+int launch_johnson(gbmd_context* c, const PairArgs& A, int part, bool ev, bool mixed);
 
 // Integer image of the stencil cell of `code` seen from home cell (cx,cy,cz).
 __device__ __forceinline__ void image_shift(const Grid& g, int cx, int cy, int cz, uint32_t code,

@@ -26,6 +26,7 @@
 #include <exanb/core/make_grid_variant_operator.h>
 #include <exaStamp/particle_species/particle_specie.h>
 #include <exaStamp/unit_system.h>
+#include "johnson.h"  // src/potential/eam_potentials/johnson (EamJohnsonParameters + its YAML decoder)
 
 #include <gbmd.h>
 
@@ -91,7 +92,7 @@ void gather(const GridT& grid, Staging& s) {
 
 template <class GridT>
 class Gb300ForceNode : public OperatorNode {
-  ADD_SLOT(std::string, potential, INPUT, REQUIRED, DocString{"lj, lj_multi or eam_alloy"});
+  ADD_SLOT(std::string, potential, INPUT, REQUIRED, DocString{"lj, eam_alloy or johnson"});
   ADD_SLOT(double, rcut, INPUT, REQUIRED);
   ADD_SLOT(double, rcut_max, INPUT_OUTPUT, 0.0);
   ADD_SLOT(double, ghost_dist_max, INPUT_OUTPUT, 0.0);
@@ -99,6 +100,8 @@ class Gb300ForceNode : public OperatorNode {
   ADD_SLOT(double, epsilon, INPUT, 0.0);
   ADD_SLOT(double, sigma, INPUT, 0.0);
   ADD_SLOT(std::string, setfl_file, INPUT, std::string{}, DocString{"eam_alloy parameter file"});
+  ADD_SLOT(EamJohnsonParameters, johnson_parameters, INPUT, OPTIONAL,
+           DocString{"johnson parameters (johnson.h L28-49), as the johnson_force slot `parameters`"});
   ADD_SLOT(std::string, precision, INPUT, std::string{"mixed"}, DocString{"mixed or fp64"});
   ADD_SLOT(bool, trigger_thermo_state, INPUT, OPTIONAL);
   ADD_SLOT(bool, compute_virial, INPUT, false);
@@ -113,7 +116,8 @@ class Gb300ForceNode : public OperatorNode {
  public:
   inline void execute() override final {
     *rcut_max = std::max(*rcut, *rcut_max);
-    if (*potential == "eam_alloy") *ghost_dist_max = std::max(*ghost_dist_max, 2.0 * (*rcut));
+    if (*potential == "eam_alloy" || *potential == "johnson")
+      *ghost_dist_max = std::max(*ghost_dist_max, 2.0 * (*rcut));
     if (grid->number_of_cells() == 0) return;  // pre-initialisation pass publishing rcut_max
     if (!m_ctx) {
       gbmd_context* c = nullptr;
@@ -134,7 +138,13 @@ class Gb300ForceNode : public OperatorNode {
                      gbmd_load_setfl(c, onika::data_file_path(*setfl_file).c_str(), *rcut,
                                      EXASTAMP_CONST_QUANTITY(1. * eV * ang), EXASTAMP_CONST_QUANTITY(1.0 * eV)),
                      "gbmd_load_setfl");
-      else
+      else if (*potential == "johnson") {
+        if (!johnson_parameters.has_value()) fatal_error() << "gb300: johnson needs johnson_parameters" << std::endl;
+        const EamJohnsonParameters& q = *johnson_parameters;
+        const double jp[19] = {q.re, q.fe, q.rhoe, q.alpha, q.beta, q.A,   q.B,  q.kappa, q.lambda, q.Fn0,
+                               q.Fn1, q.Fn2, q.Fn3, q.F0, q.F1, q.F2, q.F3, q.Fo, q.eta};
+        gb300::check(c, gbmd_set_eam_johnson(c, jp, *rcut), "gbmd_set_eam_johnson");
+      } else
         fatal_error() << "gb300: unsupported potential " << *potential << std::endl;
       gb300::check(c, gbmd_set_skin(c, *rcut_inc), "gbmd_set_skin");
       gb300::check(c, gbmd_set_precision(c, *precision == "fp64" ? GBMD_PRECISION_FP64 : GBMD_PRECISION_MIXED),

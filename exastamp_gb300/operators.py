@@ -42,16 +42,20 @@ class OperatorError(RuntimeError):
 
 
 def quantity(v) -> float:
-    """'3.4 ang' / '0.0104 eV' / 2.5 -> float in internal units."""
+    """'3.4 ang' / '0.0104 eV' / '3.08 eV/ang' / 2.5 -> float in internal units."""
     if isinstance(v, (int, float)):
         return float(v)
-    m = re.fullmatch(r"\s*([-+0-9.eE]+)\s*([A-Za-z]*)\s*", str(v))
+    m = re.fullmatch(r"\s*([-+0-9.eE]+)\s*([A-Za-z]*)\s*(?:/\s*([A-Za-z]+))?\s*", str(v))
     if not m:
         raise OperatorError("cannot parse quantity %r" % (v,))
-    val, unit = float(m.group(1)), m.group(2)
-    if unit and unit not in _UNIT:
-        raise OperatorError("unsupported unit %r" % unit)
-    return val * (_UNIT[unit] if unit else 1.0)
+    val, unit, per = float(m.group(1)), m.group(2), m.group(3)
+    for u in (unit, per):
+        if u and u not in _UNIT:
+            raise OperatorError("unsupported unit %r" % u)
+    f = _UNIT[unit] if unit else 1.0
+    if per:
+        f /= _UNIT[per]
+    return val * f
 
 
 @dataclass
@@ -222,6 +226,31 @@ class eam_alloy_force(Operator):
             raise OperatorError("eam_symmetry (Newton-3 scatter) is not offered; the full-list path is used")
         rcut = quantity(self.slots["rcut"])
         sim.ctx.set_eam_alloy(sf, rcut, EV * 1.0, EV)
+        sim.rcut_max = max(sim.rcut_max, rcut)
+        sim.ghost_dist_max = max(sim.ghost_dist_max, 2.0 * rcut)
+
+    def execute(self, sim: Simulation, energy=True, virial=False):
+        sim.ctx.compute_forces(energy=energy, virial=virial)
+
+
+class johnson_force(Operator):
+    """The mono-material analytic EAM operator (eam_potential.cu L69-193 with
+    johnson.h L28-176): both passes in one call.  `parameters` holds the 19
+    EamJohnsonParameters entries as quantities, converted as the reference's
+    YAML decoder does (every entry through its unit)."""
+    name = "johnson_force"
+    required = ("rcut", "parameters")
+
+    def bind(self, sim: Simulation):
+        from .systems import JOHNSON_PARAM_NAMES
+        p = self.slots["parameters"]
+        missing = [k for k in JOHNSON_PARAM_NAMES if k not in p]
+        if missing:
+            raise OperatorError("johnson_force: missing parameters %s" % ", ".join(missing))
+        if len(sim.species) > 1:
+            raise OperatorError("johnson_force: single material potential, %d species declared" % len(sim.species))
+        rcut = quantity(self.slots["rcut"])
+        sim.ctx.set_eam_johnson(np.array([quantity(p[k]) for k in JOHNSON_PARAM_NAMES]), rcut)
         sim.rcut_max = max(sim.rcut_max, rcut)
         sim.ghost_dist_max = max(sim.ghost_dist_max, 2.0 * rcut)
 

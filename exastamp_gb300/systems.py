@@ -123,6 +123,40 @@ def eam_cu_fcc(ncell: int = 100, a: float = 3.615, T: float = 300.0, seed: int =
                  {"kind": "eam_cu_fcc", "ncell": ncell, "a": a, "T": T, "seed": seed})
 
 
+# johnson_force parameter order (EamJohnsonParameters, johnson.h L28-49)
+JOHNSON_PARAM_NAMES = ("re", "fe", "rhoe", "alpha", "beta", "A", "B", "kappa", "lambda", "Fn0", "Fn1", "Fn2",
+                       "Fn3", "F0", "F1", "F2", "F3", "Fo", "eta")
+
+
+def johnson_ta_params(conv: float = EV) -> np.ndarray:
+    """The Ta parameter set of the reference's johnson_force regression case
+    (data/regression_new/potentials/eam/eam_johnson/single_specy.msp L6-27),
+    as the 19-vector of gbmd_set_eam_johnson: re in angstrom, energies (A, B,
+    Fn*, F*, Fo) and fe, rhoe (eV/angstrom there) multiplied by `conv`; alpha,
+    beta, kappa, lambda and eta dimensionless (the run file tags eta with eV,
+    but it is an exponent)."""
+    v = dict(re=2.860082, fe=3.08634, rhoe=33.787168, alpha=8.489528, beta=4.527748, A=0.611679, B=1.032101,
+             kappa=0.176977, lambda_=0.353954, Fn0=-5.103845, Fn1=-0.405524, Fn2=1.112997, Fn3=-3.585325,
+             F0=-5.14, F1=0.0, F2=1.640098, F3=0.221375, Fo=-5.141526, eta=0.848843)
+    v["lambda"] = v.pop("lambda_")
+    scaled = {"fe", "rhoe", "A", "B", "Fn0", "Fn1", "Fn2", "Fn3", "F0", "F1", "F2", "F3", "Fo"}
+    return np.array([v[k] * (conv if k in scaled else 1.0) for k in JOHNSON_PARAM_NAMES])
+
+
+def ta_bcc(ncell: int = 20, a: float = 3.3, T: float = 300.0, noise: float = 0.05, seed: int = 7,
+           mass: float = 180.95) -> System:
+    """BCC tantalum as in the johnson_force regression case (20^3 cells of
+    3.3 angstrom, positions shifted 0.01 angstrom, Gaussian noise 0.05
+    angstrom; seeded here)."""
+    pos, lo, hi = lattice(ncell, ncell, ncell, a, BCC_BASIS)
+    rng = np.random.default_rng(seed)
+    pos = pos + 0.01 + rng.normal(0.0, noise, pos.shape)
+    pos = lo + np.mod(pos - lo, hi - lo)
+    v = maxwell_boltzmann(np.full(len(pos), mass), T, KB_METAL, rng)
+    return _make(pos, lo, hi, np.zeros(len(pos)), np.array([mass]), v,
+                 {"kind": "ta_bcc", "ncell": ncell, "a": a, "T": T, "seed": seed})
+
+
 def lj_binary_voids(n: int = 16_777_216, density: float = 1.2, frac_a: float = 0.8, nvoids: int = 64,
                     void_r: float = 8.0, T: float = 1.0, seed: int = 3, min_dist: float = 0.0) -> System:
     """Uneven-density LJ A/B mixture: uniform random positions at `density`

@@ -57,7 +57,8 @@ enum gbmd_potential {
   GBMD_POT_NONE = 0,
   GBMD_POT_LJ = 1,          /* lj_compute_force */
   GBMD_POT_LJ_MULTI = 2,    /* lj_multi_force */
-  GBMD_POT_EAM_ALLOY = 3    /* eam_alloy_force (rho, rho2emb, force passes) */
+  GBMD_POT_EAM_ALLOY = 3,   /* eam_alloy_force (rho, rho2emb, force passes) */
+  GBMD_POT_EAM_JOHNSON = 4  /* johnson_force: analytic single-element EAM, 2 passes */
 };
 
 enum gbmd_force_flags {
@@ -129,6 +130,15 @@ int gbmd_set_eam_alloy(gbmd_context* ctx, int nelements, int nrho, double drho, 
                        const double* frho, const double* rhor, const double* z2r, double rcut,
                        double conv_z2r, double conv_frho);
 /* eam_alloy_init: read a setfl (.eam.alloy) file (eam_alloy.cpp L66-201). */
+/* johnson_force (src/potential/eam_potentials/johnson/johnson.h L28-176 with
+ * the mono-material 2-pass template src/potential/eam_potential_template/
+ * eam_potential.cu L69-193, eam_force_op_singlemat.h L39-171): analytic
+ * phi(r), rho(r), F(rho) of one element.  params[19] in the order of
+ * EamJohnsonParameters: re, fe, rhoe, alpha, beta, A, B, kappa, lambda, Fn0,
+ * Fn1, Fn2, Fn3, F0, F1, F2, F3, Fo, eta, already in the caller's units
+ * (energies in the energy unit, re in the length unit; alpha, beta, kappa,
+ * lambda and eta dimensionless).  Every atom must be of type 0. */
+int gbmd_set_eam_johnson(gbmd_context* ctx, const double params[19], double rcut);
 int gbmd_load_setfl(gbmd_context* ctx, const char* path, double rcut, double conv_z2r,
                     double conv_frho);
 

@@ -543,6 +543,110 @@ void orc_eam_force(int64_t n, const double* x, const double* y, const double* z,
 }
 
 /* ------------------------------------------------------------------------ */
+/* johnson_force: analytic single-element EAM                               */
+/* ------------------------------------------------------------------------ */
+
+/* One c1/(1 + (x-c)^20) term and its r-derivative (johnson.h L55-94). */
+static void ej_term(double pre, double k, double x, double c, double ire, double* v, double* dv) {
+  const double c1 = pre * exp(-k * (x - 1.));
+  const double c2 = x - c;
+  const double c3 = pow(c2, 20.);
+  const double den = 1. + c3;
+  const double dnum = -k * c1;
+  const double dden = 20. * c3 / c2;
+  *v += c1 / den;
+  *dv += ire * (dnum * den - c1 * dden) / (den * den);
+}
+
+/* eam_johnson_phi (johnson.h L55-94) */
+void orc_ej_phi(const orc_johnson_params* p, double r, double* phi, double* dphi) {
+  const double x = r / p->re, ire = 1. / p->re;
+  *phi = 0.;
+  *dphi = 0.;
+  ej_term(p->A, p->alpha, x, p->kappa, ire, phi, dphi);
+  ej_term(-p->B, p->beta, x, p->lambda, ire, phi, dphi);
+}
+
+/* eam_johnson_rho (johnson.h L101-118) */
+void orc_ej_rho(const orc_johnson_params* p, double r, double* rho, double* drho) {
+  const double x = r / p->re, ire = 1. / p->re;
+  *rho = 0.;
+  *drho = 0.;
+  ej_term(p->fe, p->beta, x, p->lambda, ire, rho, drho);
+}
+
+/* eam_johnson_fEmbed (johnson.h L125-176): three branches split at
+ * 0.85 rhoe and 1.15 rhoe. */
+void orc_ej_embed(const orc_johnson_params* p, double rho, double* f, double* df) {
+  const double rhon = 0.85 * p->rhoe, rho0 = 1.15 * p->rhoe;
+  if (rho < rhon) {
+    const double t = rho / rhon - 1.;
+    *f = p->Fn0 + p->Fn1 * t + p->Fn2 * (t * t) + p->Fn3 * (t * (t * t));
+    *df = (p->Fn1 + 2. * p->Fn2 * t + 3. * p->Fn3 * (t * t)) * (1. / rhon);
+  } else if (rho < rho0) {
+    const double t = rho * (1. / p->rhoe) - 1.;
+    *f = p->F0 + p->F1 * t + p->F2 * (t * t) + p->F3 * (t * (t * t));
+    *df = (p->F1 + 2. * p->F2 * t + 3. * p->F3 * (t * t)) * (1. / p->rhoe);
+  } else {
+    const double s = rho * (1. / p->rhoe);
+    const double se = pow(s, p->eta);
+    const double lse = log(se);
+    *f = p->Fo * (1. - lse) * se;
+    *df = (-p->eta * se + (1. - lse) * p->eta * se) * (p->Fo * (1. / p->rhoe) / s);
+  }
+}
+
+/* The two passes of the mono-material template (eam_potential.cu L125-170):
+ * EmbOp (eam_force_op_singlemat.h L39-84): rho_i, ep_i = F(rho_i), F'_i;
+ * ForceOp (L86-171): de = (rho'(F'_i + F'_j) + phi')/r, f_i += de*dr,
+ * ep_i += phi/2, vir_i += -1/2 f (x) dr.  fp receives F'. */
+void orc_ej_forces(int64_t n, const double* x, const double* y, const double* z, const int64_t* off,
+                   const int32_t* nbr, const int8_t* img, const double L[3], const orc_johnson_params* p,
+                   double rcut, double* fp, double* fx, double* fy, double* fz, double* ep, double* vir) {
+  const double rc2 = rcut * rcut;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < n; ++i) {
+    double rho = 0.;
+    for (int64_t k = off[i]; k < off[i + 1]; ++k) {
+      const int nn[3] = {img[3 * k], img[3 * k + 1], img[3 * k + 2]};
+      double dx, dy, dz;
+      const double d2 = pair_d2(x, y, z, i, nbr[k], nn, L, &dx, &dy, &dz);
+      if (!(d2 <= rc2)) continue;
+      double v, dv;
+      orc_ej_rho(p, sqrt(d2), &v, &dv);
+      rho += v;
+    }
+    double f, df;
+    orc_ej_embed(p, rho, &f, &df);
+    fp[i] = df;
+    if (ep) ep[i] = f;
+  }
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < n; ++i) {
+    double _fx = 0., _fy = 0., _fz = 0., _ep = 0., _v[9] = {0};
+    for (int64_t k = off[i]; k < off[i + 1]; ++k) {
+      const int nn[3] = {img[3 * k], img[3 * k + 1], img[3 * k + 2]};
+      double dx, dy, dz;
+      const int64_t j = nbr[k];
+      const double d2 = pair_d2(x, y, z, i, j, nn, L, &dx, &dy, &dz);
+      if (!(d2 <= rc2)) continue;
+      const double r = sqrt(d2);
+      double rh, drh, ph, dph;
+      orc_ej_rho(p, r, &rh, &drh);
+      orc_ej_phi(p, r, &ph, &dph);
+      const double de = (drh * (fp[i] + fp[j]) + dph) / r;
+      const double fex = de * dx, fey = de * dy, fez = de * dz;
+      _fx += fex; _fy += fey; _fz += fez;
+      _ep += .5 * ph;
+      add_vir(_v, fex, fey, fez, dx, dy, dz);
+    }
+    fx[i] = _fx; fy[i] = _fy; fz[i] = _fz;
+    if (ep) ep[i] += _ep;
+    if (vir) for (int q = 0; q < 9; ++q) vir[9 * i + q] = _v[q];
+  }
+}
+
+/* ------------------------------------------------------------------------ */
 /* Integration, accel, thermo                                               */
 /* ------------------------------------------------------------------------ */
 
@@ -896,6 +1000,7 @@ static int maybe_rebuild(orc_list* l, int64_t n, double* x, double* y, double* z
 static double pot_rcut(int pot_kind, const void* pot) {
   if (pot_kind == ORC_POT_LJ) return ((const orc_lj_params*)pot)->rcut;
   if (pot_kind == ORC_POT_LJ_MULTI) return ((const orc_lj_multi_params*)pot)->rcut_max;
+  if (pot_kind == ORC_POT_EAM_JOHNSON) return ((const orc_johnson_pot*)pot)->rcut;
   return ((const orc_eam_pot*)pot)->rcut;
 }
 
@@ -904,7 +1009,10 @@ static double pot_rcut(int pot_kind, const void* pot) {
 static void all_forces(int64_t n, const double* x, const double* y, const double* z, const uint8_t* type,
                        const orc_list* l, const double L[3], int pot_kind, const void* pot, const double* masses,
                        double* rho, double* ax, double* ay, double* az, double* ep, double* vir) {
-  if (pot_kind == ORC_POT_EAM) {
+  if (pot_kind == ORC_POT_EAM_JOHNSON) {
+    const orc_johnson_pot* p = (const orc_johnson_pot*)pot;
+    orc_ej_forces(n, x, y, z, l->off, l->nbr, l->img, L, &p->p, p->rcut, rho, ax, ay, az, ep, vir);
+  } else if (pot_kind == ORC_POT_EAM) {
     const orc_eam_pot* p = (const orc_eam_pot*)pot;
     orc_eam_density(n, x, y, z, type, l->off, l->nbr, l->img, L, &p->t, p->rcut, rho);
     for (int64_t i = 0; i < n; ++i) ep[i] = 0.0;

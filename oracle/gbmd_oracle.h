@@ -48,7 +48,17 @@ typedef struct {
 } orc_eam_pot;
 
 /* Kinds for orc_run_nve */
-enum { ORC_POT_LJ = 0, ORC_POT_LJ_MULTI = 1, ORC_POT_EAM = 2 };
+enum { ORC_POT_LJ = 0, ORC_POT_LJ_MULTI = 1, ORC_POT_EAM = 2, ORC_POT_EAM_JOHNSON = 3 };
+
+/* johnson_force parameters, EamJohnsonParameters order (johnson.h L28-49) */
+typedef struct {
+  double re, fe, rhoe, alpha, beta, A, B, kappa, lambda, Fn0, Fn1, Fn2, Fn3, F0, F1, F2, F3, Fo, eta;
+} orc_johnson_params;
+
+typedef struct {
+  orc_johnson_params p;
+  double rcut;
+} orc_johnson_pot;
 
 typedef struct {
   double epsilon, sigma, rcut;
@@ -146,6 +156,14 @@ int orc_run_minimize(int64_t n, double* x, double* y, double* z, double* ax, dou
  * initial build included); rebuild_every == -1 in either selects the
  * displacement trigger: rebuild when some atom moved more than skin/2. */
 int64_t orc_last_list_builds(void);
+
+void orc_ej_phi(const orc_johnson_params* p, double r, double* phi, double* dphi);
+void orc_ej_rho(const orc_johnson_params* p, double r, double* rho, double* drho);
+void orc_ej_embed(const orc_johnson_params* p, double rho, double* f, double* df);
+/* Both passes of johnson_force over a CSR list; fp receives F'(rho_i). */
+void orc_ej_forces(int64_t n, const double* x, const double* y, const double* z, const int64_t* off,
+                   const int32_t* nbr, const int8_t* img, const double L[3], const orc_johnson_params* p,
+                   double rcut, double* fp, double* fx, double* fy, double* fz, double* ep, double* vir);
 
 int orc_num_threads(void);
 

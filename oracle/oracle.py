@@ -58,7 +58,23 @@ class LJMultiParams(C.Structure):
                 ("sigma", C.c_void_p), ("rcut", C.c_void_p), ("rcut_max", C.c_double)]
 
 
-POT_LJ, POT_LJ_MULTI, POT_EAM = 0, 1, 2
+POT_LJ, POT_LJ_MULTI, POT_EAM, POT_EAM_JOHNSON = 0, 1, 2, 3
+
+
+class JohnsonParams(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("re", "fe", "rhoe", "alpha", "beta", "A", "B", "kappa", "lambda_",
+                                          "Fn0", "Fn1", "Fn2", "Fn3", "F0", "F1", "F2", "F3", "Fo", "eta")]
+
+
+class JohnsonPot(C.Structure):
+    _fields_ = [("p", JohnsonParams), ("rcut", C.c_double)]
+
+
+class Johnson:
+    """johnson_force parameters (19-vector, EamJohnsonParameters order) + rcut."""
+
+    def __init__(self, params, rcut):
+        self.pot = JohnsonPot(JohnsonParams(*[float(v) for v in params]), float(rcut))
 
 _lib = None
 
@@ -102,6 +118,11 @@ def lib():
         L.orc_run_minimize.restype = i32
         L.orc_run_minimize.argtypes = [i64] + [vp] * 12 + [i32, vp, dbl, dbl, dbl, i32, i32]
         L.orc_last_list_builds.restype = i64
+        L.orc_ej_forces.restype = None
+        L.orc_ej_forces.argtypes = [i64] + [vp] * 7 + [vp, dbl] + [vp] * 6
+        for f in ("orc_ej_phi", "orc_ej_rho", "orc_ej_embed"):
+            getattr(L, f).restype = None
+            getattr(L, f).argtypes = [vp, dbl, vp, vp]
         L.orc_num_threads.restype = i32
         L.orc_eam_loss_grad.restype = dbl
         L.orc_eam_loss_grad.argtypes = [i64, vp, vp, vp, vp, vp, vp, vp, vp, dbl, vp, vp, vp, dbl, dbl, vp, vp, vp]
@@ -213,6 +234,23 @@ class _Multi:
         self.eps, self.sig, self.rc = _f64(eps), _f64(sig), _f64(rc)
         self.s = LJMultiParams(self.eps.shape[0], 0, _p(self.eps), _p(self.sig), _p(self.rc),
                                float(rcut_max))
+
+
+def ej_function(name, pot, arg):
+    """(value, derivative) of orc_ej_phi / orc_ej_rho / orc_ej_embed."""
+    a, b = C.c_double(), C.c_double()
+    getattr(lib(), "orc_ej_" + name)(C.addressof(pot.pot.p), float(arg), C.addressof(a), C.addressof(b))
+    return a.value, b.value
+
+
+def ej_forces(x, y, z, nl, L, pot, virial=True):
+    """johnson_force, both passes: returns (fx, fy, fz, ep, vir, F')."""
+    n = len(x)
+    fx, fy, fz, ep, v = _outs(n, virial)
+    fp = np.zeros(n)
+    lib().orc_ej_forces(n, _p(x), _p(y), _p(z), _p(nl.off), _p(nl.nbr), _p(nl.img), _p(_f64(L)),
+                        C.addressof(pot.pot.p), pot.pot.rcut, _p(fp), _p(fx), _p(fy), _p(fz), _p(ep), _p(v))
+    return fx, fy, fz, ep, v, fp
 
 
 def lj_multi_force(x, y, z, types, nl, L, eps, sig, rc, rcut_max, virial=True):

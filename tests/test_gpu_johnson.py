@@ -1,0 +1,66 @@
+"""johnson_force (analytic single-element EAM, johnson.h L28-176 with the
+mono-material two-pass template) on the GPU against the oracle, on the Ta
+BCC system of the reference's regression case (parameters from
+eam_johnson/single_specy.msp, rcut 6.1 A, skin 1.0 A, noise 0.05 A).
+Tolerances: FP64 1e-12 relative RMS force, mixed 1e-5."""
+import numpy as np
+import pytest
+
+from exastamp_gb300 import systems as S
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+MIXED_TOL = 1e-5
+
+
+def _rel(a, b):
+    return float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))
+
+
+def _oracle_forces(oracle, s, pot):
+    x, y, z = s.x.copy(), s.y.copy(), s.z.copy()
+    oracle.wrap(x, y, z, s.lo, s.hi)
+    nl = oracle.build_neighbors(x, y, z, s.id, s.lo, s.hi, 7.1)
+    fx, fy, fz, ep, vir, fp = oracle.ej_forces(x, y, z, nl, s.L, pot)
+    return np.stack([fx, fy, fz], 1) / s.masses[0], ep, vir
+
+
+@pytest.mark.parametrize("tpa,vec", [(1, 1), (1, 4), (4, 1)])
+def test_johnson_forces_match_oracle(gpu, oracle, tpa, vec):
+    s = S.ta_bcc(ncell=8, seed=21)
+    params = S.johnson_ta_params()
+    pot = oracle.Johnson(params, 6.1)
+    F, ep, vir = _oracle_forces(oracle, s, pot)
+    for mixed, tol in ((False, FP64_TOL), (True, MIXED_TOL)):
+        with gpu.Context(0) as ctx:
+            ctx.upload_system(s)
+            ctx.set_eam_johnson(params, 6.1)
+            ctx.set_skin(1.0)
+            ctx.set_precision(mixed)
+            ctx.set_launch(tpa, 128, vec)
+            ctx.compute_forces(energy=True, virial=True)
+            d = ctx.download(virial=True)
+        G = np.stack([d["ax"], d["ay"], d["az"]], 1)
+        assert _rel(G, F) < tol, (mixed, _rel(G, F))
+        assert abs(d["ep"].sum() - ep.sum()) < (FP64_TOL if not mixed else 1e-6) * abs(ep.sum())
+        assert _rel(d["vir"], vir) < (FP64_TOL if not mixed else 1e-5)
+
+
+def test_johnson_nve_tracks_oracle(gpu, oracle):
+    s = S.ta_bcc(ncell=6, seed=22)
+    params = S.johnson_ta_params()
+    pot = oracle.Johnson(params, 6.1)
+    st = s.state()
+    th_ref = oracle.run_nve(st, s.masses, s.lo, s.hi, oracle.POT_EAM_JOHNSON, pot, 1.0, 1e-3, 20, 10)
+    with gpu.Context(0) as ctx:
+        ctx.upload_system(s)
+        ctx.set_eam_johnson(params, 6.1)
+        ctx.set_skin(1.0)
+        ctx.set_precision(False)
+        th = ctx.run_nve(20, 1e-3, rebuild_every=10, thermo_every=1)
+        d = ctx.download(("x", "y", "z"))
+    assert np.allclose(th, th_ref, rtol=1e-10, atol=1e-10 * np.abs(th_ref).max())
+    for k in ("x", "y", "z"):
+        dd = np.abs(d[k] - st[k])
+        assert np.minimum(dd, s.L[0] - dd).max() < 1e-10, k

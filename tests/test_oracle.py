@@ -275,3 +275,50 @@ def test_oracle_displacement_trigger(oracle):
     n2 = oracle.last_list_builds()
     assert n1 == 151 and 2 < n2 < 40
     assert np.allclose(th1, th2, rtol=1e-9, atol=1e-9 * np.abs(th1).max())
+
+
+def _ej(oracle):
+    return oracle.Johnson(S.johnson_ta_params(), 6.1)
+
+
+def test_johnson_functions_derivatives(oracle):
+    """eam_johnson_phi / rho / fEmbed: the returned derivatives match central
+    differences, the embedding in all three density branches."""
+    pot = _ej(oracle)
+    h = 1e-6
+    for name, args in (("phi", [2.4, 2.86, 3.3, 4.1, 5.5]), ("rho", [2.4, 2.86, 3.3, 4.1, 5.5])):
+        for r in args:
+            v, dv = oracle.ej_function(name, pot, r)
+            fd = (oracle.ej_function(name, pot, r + h)[0] - oracle.ej_function(name, pot, r - h)[0]) / (2 * h)
+            assert abs(dv - fd) <= 1e-6 * max(1.0, abs(dv)), (name, r, dv, fd)
+    rhoe = S.johnson_ta_params()[2]
+    for frac in (0.5, 0.84, 1.0, 1.1, 1.3, 1.6):
+        rho = frac * rhoe
+        v, dv = oracle.ej_function("embed", pot, rho)
+        hh = 1e-6 * rhoe
+        fd = (oracle.ej_function("embed", pot, rho + hh)[0] - oracle.ej_function("embed", pot, rho - hh)[0]) / (2 * hh)
+        assert abs(dv - fd) <= 1e-6 * max(1.0, abs(dv)), (frac, dv, fd)
+
+
+def test_johnson_forces_are_energy_gradient(oracle):
+    s = S.ta_bcc(ncell=4, noise=0.08, seed=3)
+    pot = _ej(oracle)
+
+    def energy_forces(x, y, z):
+        x, y, z = x.copy(), y.copy(), z.copy()
+        oracle.wrap(x, y, z, s.lo, s.hi)
+        nl = oracle.build_neighbors(x, y, z, s.id, s.lo, s.hi, 7.1)
+        fx, fy, fz, ep, _, _ = oracle.ej_forces(x, y, z, nl, s.L, pot)
+        return ep.sum(), np.stack([fx, fy, fz], 1)
+
+    E0, F = energy_forces(s.x, s.y, s.z)
+    h = 1e-5
+    for i in (0, 17, 63):
+        for d, arr in enumerate((s.x, s.y, s.z)):
+            p, m = arr.copy(), arr.copy()
+            p[i] += h
+            m[i] -= h
+            args_p = [p if q == d else (s.x, s.y, s.z)[q] for q in range(3)]
+            args_m = [m if q == d else (s.x, s.y, s.z)[q] for q in range(3)]
+            fd = -(energy_forces(*args_p)[0] - energy_forces(*args_m)[0]) / (2 * h)
+            assert abs(fd - F[i, d]) < 1e-6 * np.abs(F).max(), (i, d, fd, F[i, d])
