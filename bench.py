@@ -48,6 +48,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 # sigma per component per step (the NVE step 0.002 would move overlapping
 # atoms only 2e-4 sigma per step and leave forces that blow the NVE run up)
 MIN_TOLF = 100.0
+# measured DRAM traffic of the force kernel per atom (see roofline.traffic)
+EAM_FORCE_DRAM_BYTES_PER_ATOM = (273.772288e6 + 51.000832e6) / 864000.0
 MIN_DT = 0.02
 sys.path.insert(0, ROOT)
 
@@ -459,11 +461,18 @@ def main():
     alg_bytes = per_atom * s.n
     t_pair = prof["pair"] * 1e-3
     achieved = alg_bytes / t_pair / 1e9
+    traffic, traffic_src = None, None
+    if w["kind"] == "eam" and args.precision == "mixed":
+        # DRAM bytes per atom of k_eam_force_mixed from one ncu capture of the
+        # same kernel on the 864,000-atom case (60^3 cells), scaled by atoms
+        traffic = EAM_FORCE_DRAM_BYTES_PER_ATOM * s.n
+        traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_eam_force_mixed<1,4> on the "
+                       "864,000-atom case (273.8 + 51.0 MB), scaled to %d atoms" % s.n)
     out["roofline"] = {"kernel": "k_eam_force (mixed, fused Verlet halves)" if w["kind"] == "eam" else "k_lj",
                        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                        "frac": achieved / peak, "peak_source": peak_kind,
                        "algorithmic_bytes_per_launch": alg_bytes, "bytes_per_atom": per_atom,
-                       "traffic": None, "kernel_ms": prof}
+                       "traffic": traffic, "traffic_source": traffic_src, "kernel_ms": prof}
 
     # ---- FP64 comparison ----------------------------------------------------
     if not args.no_fp64 and ws == 1:

@@ -131,11 +131,26 @@ __global__ void k_to_user(int64_t n, const double* __restrict__ src, const int32
   for (int q = 0; q < width; ++q) dst[u * width + q] = src[p * width + q];
 }
 
-__global__ void k_from_user(int64_t n, const double* __restrict__ src, const int32_t* __restrict__ user,
-                            double* __restrict__ dst) {
+// up to 9 arrays in one launch: dst_k[p] = stage[k * cap + user[p]]
+struct Arrays9 {
+  double* a[9];
+};
+
+__global__ void k_from_user_multi(int64_t n, int64_t cap, const double* __restrict__ stage,
+                                  const int32_t* __restrict__ user, Arrays9 dst, int count) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= n) return;
-  dst[p] = src[user[p]];
+  const int64_t u = user[p];
+  for (int k = 0; k < count; ++k) dst.a[k][p] = stage[k * cap + u];
+}
+
+// stage[k * cap + user[p]] = src_k[p]
+__global__ void k_to_user_multi(int64_t n, int64_t cap, Arrays9 src, const int32_t* __restrict__ user,
+                                double* __restrict__ stage, int count) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int64_t u = user[p];
+  for (int k = 0; k < count; ++k) stage[k * cap + u] = src.a[k][p];
 }
 
 __global__ void k_iota(int64_t n, int32_t* __restrict__ user, uint64_t* __restrict__ id, int with_id) {
@@ -170,6 +185,34 @@ __global__ void k_copy_rref_gated(int64_t n, const double* __restrict__ r, doubl
 }
 
 static inline unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+
+// Host<->device copies of up to 9 arrays of n doubles between host[k] and
+// stage[k * cap], spread over the context's stream and two copy streams so
+// several copy engines run at once; ordered after the work already on the
+// stream and before the work issued after this call.
+static int staged_copies(gbmd_context* c, double* const* host, int count, bool to_device) {
+  if (!c->copy_stream[0]) {
+    for (int k = 0; k < 2; ++k) {
+      GBMD_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream[k], cudaStreamNonBlocking));
+      GBMD_CUDA(c, cudaEventCreateWithFlags(&c->copy_join[k], cudaEventDisableTiming));
+    }
+    GBMD_CUDA(c, cudaEventCreateWithFlags(&c->copy_fork, cudaEventDisableTiming));
+  }
+  const size_t bytes = sizeof(double) * (size_t)c->n;
+  GBMD_CUDA(c, cudaEventRecord(c->copy_fork, c->stream));
+  for (int k = 0; k < 2; ++k) GBMD_CUDA(c, cudaStreamWaitEvent(c->copy_stream[k], c->copy_fork, 0));
+  for (int k = 0; k < count; ++k) {
+    cudaStream_t st = k % 3 == 0 ? c->stream : c->copy_stream[k % 3 - 1];
+    double* dev = c->stage + (size_t)k * c->cap;
+    if (to_device) GBMD_CUDA(c, cudaMemcpyAsync(dev, host[k], bytes, cudaMemcpyHostToDevice, st));
+    else GBMD_CUDA(c, cudaMemcpyAsync(host[k], dev, bytes, cudaMemcpyDeviceToHost, st));
+  }
+  for (int k = 0; k < 2; ++k) {
+    GBMD_CUDA(c, cudaEventRecord(c->copy_join[k], c->copy_stream[k]));
+    GBMD_CUDA(c, cudaStreamWaitEvent(c->stream, c->copy_join[k], 0));
+  }
+  return GBMD_OK;
+}
 
 static int copy_rref(gbmd_context* c) {
   for (int d = 0; d < 3; ++d)
@@ -255,6 +298,9 @@ int gbmd_create(gbmd_context** out, int device, void* stream) {
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GBMD_ERR_NO_DEVICE;
   if (device < 0 || device >= ndev) return GBMD_ERR_INVALID;
+  // a non-sticky error left by earlier, unrelated runtime calls (a failed
+  // allocation, say) would otherwise surface in this context's first check
+  (void)cudaGetLastError();
   gbmd_context* c = new gbmd_context();
   c->device = device;
   if (cudaSetDevice(device) != cudaSuccess) {
@@ -294,6 +340,11 @@ int gbmd_destroy(gbmd_context* c) {
   cudaFree(c->d_err); cudaFree(c->d_thermo); cudaFree(c->d_rows);
   if (c->h_err) cudaFreeHost(c->h_err);
   if (c->h_thermo) cudaFreeHost(c->h_thermo);
+  for (int k = 0; k < 2; ++k) {
+    if (c->copy_stream[k]) cudaStreamDestroy(c->copy_stream[k]);
+    if (c->copy_join[k]) cudaEventDestroy(c->copy_join[k]);
+  }
+  if (c->copy_fork) cudaEventDestroy(c->copy_fork);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return GBMD_OK;
@@ -371,52 +422,62 @@ int gbmd_upload_atoms(gbmd_context* c, int64_t n, const double* rx, const double
   return GBMD_OK;
 }
 
+// Copy r (and v, a when given) from host arrays in upload order into the
+// cell-sorted device state: one batch of copies, one permutation kernel.
+static int upload_arrays(gbmd_context* c, const double* const* host, double* const* dev, int count) {
+  const int64_t n = c->n;
+  int rc = staged_copies(c, const_cast<double* const*>(host), count, true);
+  if (rc) return rc;
+  Arrays9 d{};
+  for (int k = 0; k < count; ++k) d.a[k] = dev[k];
+  k_from_user_multi<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->cap, c->stage, c->USER(), d, count);
+  return GBMD_OK;
+}
+
+// particle_displ_over after new positions: rebuild when an atom moved more
+// than skin/2 since the last rebuild (config_move_particles.msp L19-22,
+// L116-118), otherwise refresh the FP32/FP64 gather copies.
+static int after_new_positions(gbmd_context* c) {
+  c->forces_valid_step = -1;
+  if (!c->list_valid) return GBMD_OK;
+  cudaStream_t s = c->stream;
+  GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_DISPL, 0, sizeof(int), s));
+  const double thr = 0.5 * c->skin;
+  k_displ_over<<<nblk(c->n, 256), 256, 0, s>>>(c->n, c->X(), c->Y(), c->Z(), c->rref, c->cap, thr * thr,
+                                               c->d_err + ERRW_DISPL);
+  int rc = sync_error_word(c);
+  if (rc) return rc;
+  if (c->h_err[ERRW_DISPL]) invalidate_list(c);
+  else launch_posf(c);
+  return GBMD_OK;
+}
+
 int gbmd_upload_positions(gbmd_context* c, const double* rx, const double* ry, const double* rz,
                           const double* vx, const double* vy, const double* vz) {
   if (!c || !rx || !ry || !rz) return GBMD_ERR_INVALID;
-  const int64_t n = c->n, cap = c->cap;
-  if (n == 0) return GBMD_OK;
-  cudaStream_t s = c->stream;
-  const double* r[3] = {rx, ry, rz};
-  const double* v[3] = {vx, vy, vz};
-  for (int d = 0; d < 3; ++d) {
-    GBMD_CUDA(c, cudaMemcpyAsync(c->stage + d * cap, r[d], sizeof(double) * n, cudaMemcpyHostToDevice, s));
-    k_from_user<<<nblk(n, 256), 256, 0, s>>>(n, c->stage + d * cap, c->USER(), c->rbuf[c->cur] + d * cap);
-  }
-  if (vx && vy && vz)
-    for (int d = 0; d < 3; ++d) {
-      GBMD_CUDA(c, cudaMemcpyAsync(c->stage + d * cap, v[d], sizeof(double) * n, cudaMemcpyHostToDevice, s));
-      k_from_user<<<nblk(n, 256), 256, 0, s>>>(n, c->stage + d * cap, c->USER(), c->vbuf[c->cur_s] + d * cap);
-    }
-  c->forces_valid_step = -1;
-  if (c->list_valid) {
-    // particle_displ_over: rebuild when an atom moved more than skin/2 since
-    // the last rebuild (config_move_particles.msp L19-22, L116-118)
-    GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_DISPL, 0, sizeof(int), s));
-    const double thr = 0.5 * c->skin;
-    k_displ_over<<<nblk(n, 256), 256, 0, s>>>(n, c->X(), c->Y(), c->Z(), c->rref, cap, thr * thr,
-                                              c->d_err + ERRW_DISPL);
-    int rc = sync_error_word(c);
-    if (rc) return rc;
-    if (c->h_err[ERRW_DISPL]) invalidate_list(c);
-    else launch_posf(c);
-  }
-  return GBMD_OK;
+  const int64_t cap = c->cap;
+  if (c->n == 0) return GBMD_OK;
+  const bool with_v = vx && vy && vz;
+  const double* host[6] = {rx, ry, rz, vx, vy, vz};
+  double* dev[6] = {c->rbuf[c->cur], c->rbuf[c->cur] + cap, c->rbuf[c->cur] + 2 * cap,
+                    c->vbuf[c->cur_s], c->vbuf[c->cur_s] + cap, c->vbuf[c->cur_s] + 2 * cap};
+  int rc = upload_arrays(c, host, dev, with_v ? 6 : 3);
+  if (rc) return rc;
+  return after_new_positions(c);
 }
 
 int gbmd_upload_state(gbmd_context* c, const double* rx, const double* ry, const double* rz, const double* vx,
                       const double* vy, const double* vz, const double* ax, const double* ay, const double* az) {
-  if (!c || !vx || !vy || !vz || !ax || !ay || !az) return GBMD_ERR_INVALID;
-  int rc = gbmd_upload_positions(c, rx, ry, rz, vx, vy, vz);
+  if (!c || !rx || !ry || !rz || !vx || !vy || !vz || !ax || !ay || !az) return GBMD_ERR_INVALID;
+  const int64_t cap = c->cap;
+  if (c->n == 0) return GBMD_OK;
+  const double* host[9] = {rx, ry, rz, vx, vy, vz, ax, ay, az};
+  double* dev[9] = {c->rbuf[c->cur], c->rbuf[c->cur] + cap, c->rbuf[c->cur] + 2 * cap,
+                    c->vbuf[c->cur_s], c->vbuf[c->cur_s] + cap, c->vbuf[c->cur_s] + 2 * cap,
+                    c->abuf[c->cur_s], c->abuf[c->cur_s] + cap, c->abuf[c->cur_s] + 2 * cap};
+  int rc = upload_arrays(c, host, dev, 9);
   if (rc) return rc;
-  const int64_t n = c->n, cap = c->cap;
-  if (n == 0) return GBMD_OK;
-  cudaStream_t s = c->stream;
-  const double* a[3] = {ax, ay, az};
-  for (int d = 0; d < 3; ++d) {
-    GBMD_CUDA(c, cudaMemcpyAsync(c->stage + d * cap, a[d], sizeof(double) * n, cudaMemcpyHostToDevice, s));
-    k_from_user<<<nblk(n, 256), 256, 0, s>>>(n, c->stage + d * cap, c->USER(), c->abuf[c->cur_s] + d * cap);
-  }
+  if ((rc = after_new_positions(c))) return rc;
   c->forces_valid_step = c->step;
   return GBMD_OK;
 }
@@ -434,7 +495,22 @@ int gbmd_download(gbmd_context* c, double* rx, double* ry, double* rz, double* v
   } f[11] = {{rx, c->X(), 1}, {ry, c->Y(), 1}, {rz, c->Z(), 1}, {vx, c->VX(), 1}, {vy, c->VY(), 1},
              {vz, c->VZ(), 1}, {ax, c->AX(), 1}, {ay, c->AY(), 1}, {az, c->AZ(), 1}, {ep, c->ep, 1},
              {vir, c->vir, 9}};
-  for (int k = 0; k < 11; ++k) {
+  // r, v, a: one un-permutation kernel into separate staging slots, then the
+  // copies over several copy streams; ep and vir one by one
+  Arrays9 src{};
+  double* host[9];
+  int count = 0;
+  for (int k = 0; k < 9; ++k)
+    if (f[k].host) {
+      src.a[count] = const_cast<double*>(f[k].dev);
+      host[count++] = f[k].host;
+    }
+  if (count) {
+    k_to_user_multi<<<nblk(n, 256), 256, 0, s>>>(n, c->cap, src, c->USER(), c->stage, count);
+    int rc = staged_copies(c, host, count, false);
+    if (rc) return rc;
+  }
+  for (int k = 9; k < 11; ++k) {
     if (!f[k].host) continue;
     if (!f[k].dev) {
       std::memset(f[k].host, 0, sizeof(double) * n * f[k].width);

@@ -98,6 +98,10 @@ struct StepParams {
 struct gbmd_context {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // copy streams for host<->device staging (created lazily), forked from and
+  // joined back into `stream` with events
+  cudaStream_t copy_stream[2] = {nullptr, nullptr};
+  cudaEvent_t copy_fork = nullptr, copy_join[2] = {nullptr, nullptr};
   bool own_stream = false;
   std::string err;
 

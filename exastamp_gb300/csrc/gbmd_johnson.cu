@@ -259,7 +259,9 @@ __global__ void __launch_bounds__(256) k_ej_force_mixed(PairArgs A, JohnsonDev P
   const float fpi = live ? fpf[i] : 0.f;
   const int ti = __float_as_int(pi.w);
   float fx = 0.f, fy = 0.f, fz = 0.f, cfx = 0.f, cfy = 0.f, cfz = 0.f, e = 0.f, ce = 0.f;
-  float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  // virial: compensated too (its diagonal is a small difference of large
+  // attractive and repulsive terms in this potential)
+  float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, cv[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   const uint32_t* row = A.nbr + (size_t)i * A.W;
   for (int k = lane; k < nn; k += T) {
     const uint32_t ent = __ldcs(row + (size_t)(k >> A.wsh) * A.stride + (k & (A.W - 1)));
@@ -281,12 +283,12 @@ __global__ void __launch_bounds__(256) k_ej_force_mixed(PairArgs A, JohnsonDev P
     if (EV) {
       kahan_add(e, ce, G.in ? 0.5f * ph : 0.f);
       const float h = -0.5f * de;
-      v[0] = fmaf(h * G.dx, G.dx, v[0]);
-      v[1] = fmaf(h * G.dy, G.dy, v[1]);
-      v[2] = fmaf(h * G.dz, G.dz, v[2]);
-      v[3] = fmaf(h * G.dx, G.dy, v[3]);
-      v[4] = fmaf(h * G.dx, G.dz, v[4]);
-      v[5] = fmaf(h * G.dy, G.dz, v[5]);
+      kahan_add(v[0], cv[0], h * G.dx * G.dx);
+      kahan_add(v[1], cv[1], h * G.dy * G.dy);
+      kahan_add(v[2], cv[2], h * G.dz * G.dz);
+      kahan_add(v[3], cv[3], h * G.dx * G.dy);
+      kahan_add(v[4], cv[4], h * G.dx * G.dz);
+      kahan_add(v[5], cv[5], h * G.dy * G.dz);
     }
   }
   group_reduce_kahan<T>(fx, cfx);
@@ -295,8 +297,10 @@ __global__ void __launch_bounds__(256) k_ej_force_mixed(PairArgs A, JohnsonDev P
   if (EV) {
     group_reduce_kahan<T>(e, ce);
 #pragma unroll
-    for (int q = 0; q < 6; ++q)
-      for (int off = T / 2; off > 0; off >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], off);
+    for (int q = 0; q < 6; ++q) {
+      group_reduce_kahan<T>(v[q], cv[q]);
+      v[q] -= cv[q];
+    }
   }
   if (live && lane == 0) {
     const float im = A.inv_massf[ti];

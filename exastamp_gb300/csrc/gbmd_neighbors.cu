@@ -432,7 +432,9 @@ __device__ __forceinline__ int build_walk(const BuildCell& B, const float4* __re
       }
     }
     if (G == 16) {
-      unc = unc || __shfl_xor_sync(FULL, (int)unc, 16) != 0;
+      // the shuffle runs on every lane (a short-circuit here would skip it)
+      const int partner_unc = __shfl_xor_sync(FULL, (int)unc, 16);
+      unc = unc || partner_unc != 0;
       __syncwarp();  // the high-half lanes' entries are visible to the low half
       if (half == 0 && unc) cnt -= build_retest_row(row, min(cnt, maxnb), wsh, W, stride, pf, pi, x, y, z, i,
                                                     B.cx, B.cy, B.cz, g, R2, R2lo);

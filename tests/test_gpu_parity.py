@@ -361,3 +361,19 @@ def test_nonfinite_force_reported(gpu):
         with pytest.raises(gpu.GbmdError) as e:
             ctx.run_nve(1, 0.001, rebuild_every=0)
         assert e.value.code == 6
+
+
+def test_upload_state_download_round_trip(gpu):
+    """r, v, a through gbmd_upload_state and back through gbmd_download, in
+    the caller's order, bit for bit (batched staging copies + permutation)."""
+    s = _jitter(S.lj_fcc(ncell=7, seed=31), 0.05, 31)
+    rng = np.random.default_rng(31)
+    with gpu_ctx(gpu, s, LJ, 0.3, mixed=True) as ctx:
+        ctx.run_nve(12, 0.005, rebuild_every=5)
+        d = ctx.download(("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az"))
+        new = {k: d[k] + (rng.normal(0.0, 1e-3, s.n) if k[0] != "x" and k[0] != "y" and k[0] != "z" else 0.0)
+               for k in d}
+        ctx.upload_state(*(new[k] for k in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az")))
+        back = ctx.download(("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az"))
+    for k in new:
+        assert np.array_equal(back[k], new[k]), k
