@@ -86,6 +86,8 @@ def parse():
     p.add_argument("--lanes", type=int, default=0, help="lanes per atom (0: autotune)")
     p.add_argument("--block", type=int, default=0)
     p.add_argument("--vec", type=int, default=1, help="list entries per lane per load with --lanes (1 or 4)")
+    p.add_argument("--no-staging", action="store_true",
+                   help="with --lanes 1 --vec 4: gather neighbour positions instead of staging them")
     p.add_argument("--ncell", type=int, default=0,
                    help="override the unit cells per edge (small profiling cases of the same workload)")
     a = p.parse_args()
@@ -387,6 +389,7 @@ def main():
     ctx.set_precision(args.precision == "mixed")
     if args.lanes:
         ctx.set_launch(args.lanes, args.block or 128, args.vec)
+        ctx.set_neighbor_staging(not args.no_staging)
     else:
         from exastamp_gb300 import autotune
         lanes, vec, block, tuned = autotune.tune(ctx, key="%s-%s" % (args.workload, args.precision))
@@ -436,7 +439,7 @@ def main():
                       "list_builds_in_timed_region": rebuilds,
                       "neighbours_per_atom": npairs / s.n, "cells": nc.tolist(),
                       "lanes_per_atom": ctx.get_launch_ex()[0], "list_entries_per_load": ctx.get_launch_ex()[1],
-                      "block": ctx.get_launch_ex()[2],
+                      "block": ctx.get_launch_ex()[2], "staged_neighbour_positions": ctx.get_neighbor_staging(),
                       "parallelism": "replicas" if ws > 1 else "single-gpu",
                       "l2": "inputs larger than L2 (neighbour list %.2f GB)" % (npairs * 4 / 1e9)
                       if npairs * 4 > 129e6 else "inputs resident in L2 (not flushed)",

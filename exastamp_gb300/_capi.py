@@ -73,6 +73,8 @@ def lib(path: str = LIB_PATH):
             "gbmd_set_launch": ([vp, i32, i32], i32),
             "gbmd_get_launch": ([vp, P(i32), P(i32)], i32),
             "gbmd_set_launch_ex": ([vp, i32, i32, i32], i32),
+            "gbmd_set_neighbor_staging": ([vp, i32], i32),
+            "gbmd_get_neighbor_staging": ([vp, P(i32)], i32),
             "gbmd_get_launch_ex": ([vp, P(i32), P(i32), P(i32)], i32),
             "gbmd_set_skin": ([vp, dbl], i32),
             "gbmd_build_neighbors": ([vp], i32),
@@ -223,6 +225,14 @@ class Context:
         t, b = C.c_int(), C.c_int()
         self._chk(self._L.gbmd_get_launch(self.h, C.byref(t), C.byref(b)))
         return t.value, b.value
+
+    def set_neighbor_staging(self, enable):
+        self._chk(self._L.gbmd_set_neighbor_staging(self.h, 1 if enable else 0))
+
+    def get_neighbor_staging(self):
+        e = C.c_int()
+        self._chk(self._L.gbmd_get_neighbor_staging(self.h, C.byref(e)))
+        return bool(e.value)
 
     def get_launch_ex(self):
         """(lanes per atom, list entries per load, threads per block)."""

@@ -3,8 +3,9 @@
 The knobs are the lanes that share one atom's neighbour list (1-16; more
 lanes give more parallelism for small systems, fewer lanes avoid the
 per-atom shuffle reduction for large ones), the list entries each lane reads
-per load (1, or 4 in one 16-byte load with at most 4 lanes) and the threads
-per block.  Each
+per load (1, or 4 in one 16-byte load with at most 4 lanes), whether
+neighbour positions come from shared-memory staging (1 lane x 4 entries) and
+the threads per block.  tune() leaves the staging choice set on the context.  Each
 candidate is timed with gbmd_profile_step (CUDA events on the context's
 stream, density + final pair kernel) and the fastest is kept.  Results are
 cached in a JSON file keyed by GPU name, workload key and atom count
@@ -86,10 +87,11 @@ def tune(ctx, key: str, lanes=LANES, blocks=BLOCKS, vecs=VECS, reps: int = 3, us
     """Return (lanes, entries per load, block, timings) for this context's
     system and potential."""
     n = ctx.n
-    ck = "%s|%s|%d|v" % (_gpu_name(), key, n)
+    ck = "%s|%s|%d|vs" % (_gpu_name(), key, n)
     cache = _load() if use_cache else {}
     if ck in cache:
         e = cache[ck]
+        ctx.set_neighbor_staging(bool(e.get("staged", True)))
         return int(e["lanes"]), int(e["vec"]), int(e["block"]), e.get("timings", {})
     timings = {}
     best = None
@@ -100,13 +102,17 @@ def tune(ctx, key: str, lanes=LANES, blocks=BLOCKS, vecs=VECS, reps: int = 3, us
             for b in blocks:
                 if b % t:
                     continue
-                ctx.set_launch(t, b, v)
-                prof = ctx.profile_step(reps=reps)
-                ms = prof["density"] + prof["pair"]
-                timings["%dx%dx%d" % (t, v, b)] = ms
-                if best is None or ms < best[0]:
-                    best = (ms, t, v, b)
-    cache[ck] = {"lanes": best[1], "vec": best[2], "block": best[3], "timings": timings}
+                # shared-memory staging of neighbour positions exists for 1 lane x 4 entries
+                for staged in ((False, True) if (t == 1 and v == 4) else (False,)):
+                    ctx.set_launch(t, b, v)
+                    ctx.set_neighbor_staging(staged)
+                    prof = ctx.profile_step(reps=reps)
+                    ms = prof["density"] + prof["pair"]
+                    timings["%dx%dx%d%s" % (t, v, b, "s" if staged else "")] = ms
+                    if best is None or ms < best[0]:
+                        best = (ms, t, v, b, staged)
+    cache[ck] = {"lanes": best[1], "vec": best[2], "block": best[3], "staged": best[4], "timings": timings}
     if use_cache:
         _store(cache)
+    ctx.set_neighbor_staging(best[4])
     return best[1], best[2], best[3], timings

@@ -787,6 +787,21 @@ int gbmd_get_launch(const gbmd_context* c, int* tpa, int* block) {
   return GBMD_OK;
 }
 
+int gbmd_set_neighbor_staging(gbmd_context* c, int enable) {
+  if (!c) return GBMD_ERR_INVALID;
+  if (c->staged != (enable != 0)) {
+    c->staged = enable != 0;
+    drop_graph(c);
+  }
+  return GBMD_OK;
+}
+
+int gbmd_get_neighbor_staging(const gbmd_context* c, int* enabled) {
+  if (!c || !enabled) return GBMD_ERR_INVALID;
+  *enabled = c->staged ? 1 : 0;
+  return GBMD_OK;
+}
+
 int gbmd_get_launch_ex(const gbmd_context* c, int* tpa, int* vec, int* block) {
   if (!c) return GBMD_ERR_INVALID;
   if (tpa) *tpa = c->tpa;
@@ -965,6 +980,7 @@ static int capture_graph(gbmd_context* c, double dt, int R, int G, bool thermo_e
   c->graph_key_maxnb = c->maxnb;
   c->graph_key_tpa = c->tpa;
   c->graph_key_vec = c->vec;
+  c->graph_key_staged = c->staged ? 1 : 0;
   c->graph_key_block = c->block;
   c->graph_key_prec = c->precision;
   return GBMD_OK;
@@ -974,6 +990,7 @@ static bool graph_matches(const gbmd_context* c, double dt, int R, int G, bool t
   return c->graph_exec && c->graph_rebuild_every == R && c->graph_chunk == G && c->graph_dt == dt &&
          c->graph_thermo_end == (thermo_end ? 1 : 0) && c->graph_key_n == c->n && c->graph_key_maxnb == c->maxnb &&
          c->graph_key_tpa == c->tpa && c->graph_key_vec == c->vec && c->graph_key_block == c->block &&
+         c->graph_key_staged == (c->staged ? 1 : 0) &&
          c->graph_key_prec == c->precision;
 }
 

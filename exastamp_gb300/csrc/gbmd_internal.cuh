@@ -169,6 +169,7 @@ struct gbmd_context {
   int maxnb = 0;                // per-atom capacity (multiple of tpa * vec)
   int tpa = 1;                  // lanes per atom (autotuned; default = the GB300 optimum)
   int vec = 4;                  // list entries per lane per load (1 or 4, mixed kernels; autotuned)
+  bool staged = true;           // 1 lane x 4 entries: neighbour positions from shared memory
   int block = 256;              // threads per block (autotuned)
   double skin = 0.0, rlist = 0.0;
   bool list_valid = false;
@@ -207,7 +208,8 @@ struct gbmd_context {
   double graph_dt = 0.0;
   int graph_thermo_end = 0;
   int64_t graph_key_n = -1;
-  int graph_key_maxnb = -1, graph_key_tpa = -1, graph_key_block = -1, graph_key_prec = -1, graph_key_vec = -1;
+  int graph_key_maxnb = -1, graph_key_tpa = -1, graph_key_block = -1, graph_key_prec = -1, graph_key_vec = -1,
+      graph_key_staged = -1;
 };
 
 // ---------------------------------------------------------------------------

@@ -100,6 +100,86 @@ struct ListRows {
 };
 
 // ---------------------------------------------------------------------------
+// Neighbour-position sources.  GlobalFetch gathers position j from the
+// cell-sorted array; StagedFetch reads it from the block's shared-memory copy
+// of the cells around its home cells (see stage_cells): the list entry's
+// stencil row (dy, dz) picks one of nine staged row segments, each at most
+// two contiguous global ranges (a row wraps at most once in x).
+// ---------------------------------------------------------------------------
+struct GlobalFetch {
+  const float4* __restrict__ P;
+  __device__ __forceinline__ float4 operator()(uint32_t ent, uint32_t j) const { return __ldg(&P[j]); }
+};
+
+struct StagedFetch {
+  const float4* pos;   // staged positions (shared memory)
+  const int4* rows;    // 16 entries by (dy+1) | (dz+1) << 2: {delta0, g1, n1, delta1}
+  __device__ __forceinline__ float4 operator()(uint32_t ent, uint32_t j) const {
+    const int4 t = rows[(ent >> 28) & 15u];
+    const int jj = (int)j;
+    const int slot = jj - ((unsigned)(jj - t.y) < (unsigned)t.z ? t.w : t.x);
+    return pos[slot];
+  }
+};
+
+// Stage, for the block's K home cells (x0 .. x0+K-1 of row (y, z), taken
+// from blockIdx), the positions of every atom of the cells x0-1 .. x0+K in
+// the nine rows (y+dy, z+dz) into `pos` and the translation table into
+// `rows`; a0 / a1 receive the block's home atom range.  Returns false (then
+// the block gathers from global memory) when they exceed `cap` atoms.
+__device__ bool stage_cells(const Grid& g, const int32_t* __restrict__ cstart, const float4* __restrict__ src,
+                            int K, int cap, float4* pos, int4* rows, int* sh, int64_t& a0, int64_t& a1) {
+  const int ncx = g.nc[0], ncy = g.nc[1], ncz = g.nc[2];
+  const int x0 = blockIdx.x * K, y = blockIdx.y, z = blockIdx.z;
+  const int x1 = min(x0 + K, ncx);  // exclusive
+  const int64_t rowbase = ((int64_t)z * ncy + y) * ncx;
+  a0 = cstart[rowbase + x0];
+  a1 = cstart[rowbase + x1];
+  // sh[0..35]: per row s = 0..8, global start / count of range A and B
+  if (threadIdx.x < 9) {
+    const int s = threadIdx.x, dy = s % 3 - 1, dz = s / 3 - 1;
+    const int yy = (y + dy + ncy) % ncy, zz = (z + dz + ncz) % ncz;
+    const int64_t rb = ((int64_t)zz * ncy + yy) * ncx;
+    int la = 0, ha = ncx - 1, lb = 0, hb = -1;  // inclusive cell ranges; B empty
+    if (ncx > x1 - x0 + 2) {
+      const int xs = x0 - 1, xe = x1;
+      if (xs < 0) { la = ncx - 1; ha = ncx - 1; lb = 0; hb = xe; }
+      else if (xe >= ncx) { la = xs; ha = ncx - 1; lb = 0; hb = 0; }
+      else { la = xs; ha = xe; }
+    }
+    const int ga = cstart[rb + la], na = cstart[rb + ha + 1] - ga;
+    const int gb = hb >= lb ? cstart[rb + lb] : 0, nb = hb >= lb ? cstart[rb + hb + 1] - gb : 0;
+    sh[4 * s] = ga; sh[4 * s + 1] = na; sh[4 * s + 2] = gb; sh[4 * s + 3] = nb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int off = 0;
+    for (int q = 0; q < 16; ++q) rows[q] = make_int4(0, 0, 0, 0);
+    for (int s = 0; s < 9; ++s) {
+      const int ga = sh[4 * s], na = sh[4 * s + 1], gb = sh[4 * s + 2], nb = sh[4 * s + 3];
+      const int oa = off, ob = off + na;
+      off += na + nb;
+      const int key = (s % 3) | ((s / 3) << 2);
+      rows[key] = make_int4(ga - oa, gb, nb, gb - ob);
+      sh[36 + 2 * s] = oa;
+      sh[36 + 2 * s + 1] = ob;
+    }
+    sh[54] = off;
+  }
+  __syncthreads();
+  const int total = sh[54];
+  if (total > cap) return false;  // uniform
+  for (int s = 0; s < 9; ++s) {
+    const int ga = sh[4 * s], na = sh[4 * s + 1], gb = sh[4 * s + 2], nb = sh[4 * s + 3];
+    const int oa = sh[36 + 2 * s], ob = sh[36 + 2 * s + 1];
+    for (int t = threadIdx.x; t < na; t += blockDim.x) pos[oa + t] = __ldg(&src[ga + t]);
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) pos[ob + t] = __ldg(&src[gb + t]);
+  }
+  __syncthreads();
+  return true;
+}
+
+// ---------------------------------------------------------------------------
 // Lennard-Jones
 // ---------------------------------------------------------------------------
 struct LJF {
@@ -107,25 +187,25 @@ struct LJF {
   double rc2, rc;
 };
 
-template <int T, int V, bool EV, bool MULTI>
-__global__ void __launch_bounds__(256) k_lj_mixed(PairArgs A, LJF P, const LJPair* __restrict__ tab, int ntypes,
-                                                  double rcmax2) {
-  __shared__ float4 sfa[MULTI ? GBMD_MAX_TYPES * GBMD_MAX_TYPES : 1];   // sig2, eps24, eps4, ecut
-  __shared__ float2 sfb[MULTI ? GBMD_MAX_TYPES * GBMD_MAX_TYPES : 1];   // rc2lo, rc2hi
-  __shared__ double sfr[MULTI ? GBMD_MAX_TYPES * GBMD_MAX_TYPES : 1];   // rc
-  if (MULTI) {
-    for (int q = threadIdx.x; q < ntypes * ntypes; q += blockDim.x) {
-      const LJPair& p = tab[q];
-      sfa[q] = make_float4(p.sig2f, p.eps24f, p.eps4f, p.ecutf);
-      sfb[q] = make_float2(p.rc2lo, p.rc2hi);
-      sfr[q] = p.rc;
-    }
-    __syncthreads();
+struct LJTabSmem {
+  float4 a[GBMD_MAX_TYPES * GBMD_MAX_TYPES];   // sig2, eps24, eps4, ecut
+  float2 b[GBMD_MAX_TYPES * GBMD_MAX_TYPES];   // rc2lo, rc2hi
+  double r[GBMD_MAX_TYPES * GBMD_MAX_TYPES];   // rc
+};
+
+__device__ __forceinline__ void lj_load_table(LJTabSmem& t, const LJPair* __restrict__ tab, int ntypes) {
+  for (int q = threadIdx.x; q < ntypes * ntypes; q += blockDim.x) {
+    const LJPair& p = tab[q];
+    t.a[q] = make_float4(p.sig2f, p.eps24f, p.eps4f, p.ecutf);
+    t.b[q] = make_float2(p.rc2lo, p.rc2hi);
+    t.r[q] = p.rc;
   }
-  const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = gt / T;
-  const int lane = (int)(gt % T);
-  const bool live = i < A.n;
+  __syncthreads();
+}
+
+template <int T, int V, bool EV, bool MULTI, class Fetch>
+__device__ __forceinline__ void lj_atom(const PairArgs& A, const LJF& P, const LJTabSmem& tab, int ntypes,
+                                        double rcmax2, int64_t i, int lane, bool live, const Fetch& fetch) {
   const int nn = live ? min(A.nnb[i], A.maxnb) : 0;
   const float4 pi = live ? A.posf[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   const int cp = live ? A.cellpack[i] : 0;
@@ -141,7 +221,7 @@ __global__ void __launch_bounds__(256) k_lj_mixed(PairArgs A, LJF P, const LJPai
 #pragma unroll
     for (int q = 0; q < V; ++q) {
       if (!L.valid(r, q)) ent[q] = L.standin;
-      pj[q] = __ldg(&A.posf[ent[q] & GBMD_IDX_MASK]);
+      pj[q] = fetch(ent[q], ent[q] & GBMD_IDX_MASK);
     }
     float rx = 0.f, ry = 0.f, rz = 0.f, re = 0.f;
 #pragma unroll
@@ -152,10 +232,10 @@ __global__ void __launch_bounds__(256) k_lj_mixed(PairArgs A, LJF P, const LJPai
       double rcp = 0.0, rc2 = P.rc2;
       if (MULTI) {
         const int pid = ti * ntypes + __float_as_int(pj[q].w);
-        const float4 a = sfa[pid];
-        const float2 b = sfb[pid];
+        const float4 a = tab.a[pid];
+        const float2 b = tab.b[pid];
         sig2 = a.x; eps24 = a.y; eps4 = a.z; ecut = a.w; rlo = b.x; rhi = b.y;
-        rcp = sfr[pid];
+        rcp = tab.r[pid];
         rc2 = rcmax2;
       } else {
         sig2 = P.sig2; eps24 = P.eps24; eps4 = P.eps4; ecut = P.ecut; rlo = P.rc2lo; rhi = P.rc2hi;
@@ -205,6 +285,35 @@ __global__ void __launch_bounds__(256) k_lj_mixed(PairArgs A, LJF P, const LJPai
   }
 }
 
+template <int T, int V, bool EV, bool MULTI>
+__global__ void __launch_bounds__(256) k_lj_mixed(PairArgs A, LJF P, const LJPair* __restrict__ tab, int ntypes,
+                                                  double rcmax2) {
+  __shared__ LJTabSmem t;
+  if (MULTI) lj_load_table(t, tab, ntypes);
+  const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i = gt / T;
+  lj_atom<T, V, EV, MULTI>(A, P, t, ntypes, rcmax2, i, (int)(gt % T), i < A.n, GlobalFetch{A.posf});
+}
+
+// One lane per atom, 4 entries per load, neighbour positions from the
+// block's staged cells.
+template <bool EV, bool MULTI>
+__global__ void __launch_bounds__(256) k_lj_staged(PairArgs A, LJF P, const LJPair* __restrict__ tab, int ntypes,
+                                                   double rcmax2, const int32_t* __restrict__ cstart, int K,
+                                                   int cap) {
+  __shared__ LJTabSmem t;
+  __shared__ int4 rows[16];
+  __shared__ int sh[56];
+  extern __shared__ float4 staged_pos[];
+  if (MULTI) lj_load_table(t, tab, ntypes);
+  int64_t a0, a1;
+  const bool ok = stage_cells(A.g, cstart, A.posf, K, cap, staged_pos, rows, sh, a0, a1);
+  for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+    if (ok) lj_atom<1, 4, EV, MULTI>(A, P, t, ntypes, rcmax2, i, 0, true, StagedFetch{staged_pos, rows});
+    else lj_atom<1, 4, EV, MULTI>(A, P, t, ntypes, rcmax2, i, 0, true, GlobalFetch{A.posf});
+  }
+}
+
 // ---------------------------------------------------------------------------
 // eam_alloy
 // ---------------------------------------------------------------------------
@@ -225,13 +334,10 @@ __device__ __forceinline__ float spline_der(const float4& c, float q, float rd) 
 
 // Density + embedding.  SINGLE (one element): also writes pfp[i] = (position,
 // F'(rho_i)) so the force pass gathers both in one 16 B load.
-template <int T, int V, bool EV, bool SINGLE>
-__global__ void __launch_bounds__(256) k_eam_rho_mixed(PairArgs A, EamDev E, float* __restrict__ fpf,
-                                                       float* __restrict__ epf, float4* __restrict__ pfp) {
-  const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = gt / T;
-  const int lane = (int)(gt % T);
-  const bool live = i < A.n;
+template <int T, int V, bool EV, bool SINGLE, class Fetch>
+__device__ __forceinline__ void eam_rho_atom(const PairArgs& A, const EamDev& E, float* __restrict__ fpf,
+                                             float* __restrict__ epf, float4* __restrict__ pfp, int64_t i,
+                                             int lane, bool live, const Fetch& fetch) {
   const int nn = live ? min(A.nnb[i], A.maxnb) : 0;
   const float4 pi = live ? A.posf[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   const int cp = live ? A.cellpack[i] : 0;
@@ -248,7 +354,7 @@ __global__ void __launch_bounds__(256) k_eam_rho_mixed(PairArgs A, EamDev E, flo
 #pragma unroll
     for (int q = 0; q < V; ++q) {
       if (!L.valid(r, q)) ent[q] = L.standin;
-      pj[q] = __ldg(&A.posf[ent[q] & GBMD_IDX_MASK]);
+      pj[q] = fetch(ent[q], ent[q] & GBMD_IDX_MASK);
     }
     float rr = 0.f;
 #pragma unroll
@@ -289,6 +395,29 @@ __global__ void __launch_bounds__(256) k_eam_rho_mixed(PairArgs A, EamDev E, flo
   }
 }
 
+template <int T, int V, bool EV, bool SINGLE>
+__global__ void __launch_bounds__(256) k_eam_rho_mixed(PairArgs A, EamDev E, float* __restrict__ fpf,
+                                                       float* __restrict__ epf, float4* __restrict__ pfp) {
+  const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i = gt / T;
+  eam_rho_atom<T, V, EV, SINGLE>(A, E, fpf, epf, pfp, i, (int)(gt % T), i < A.n, GlobalFetch{A.posf});
+}
+
+template <bool EV>
+__global__ void __launch_bounds__(256) k_eam_rho_staged(PairArgs A, EamDev E, float* __restrict__ fpf,
+                                                        float* __restrict__ epf, float4* __restrict__ pfp,
+                                                        const int32_t* __restrict__ cstart, int K, int cap) {
+  __shared__ int4 rows[16];
+  __shared__ int sh[56];
+  extern __shared__ float4 staged_pos[];
+  int64_t a0, a1;
+  const bool ok = stage_cells(A.g, cstart, A.posf, K, cap, staged_pos, rows, sh, a0, a1);
+  for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+    if (ok) eam_rho_atom<1, 4, EV, true>(A, E, fpf, epf, pfp, i, 0, true, StagedFetch{staged_pos, rows});
+    else eam_rho_atom<1, 4, EV, true>(A, E, fpf, epf, pfp, i, 0, true, GlobalFetch{A.posf});
+  }
+}
+
 // One 32-byte load of a knot's two float4 (rho' and z2r coefficients of the
 // interleaved one-element table; the address is 32-byte aligned).
 __device__ __forceinline__ void ldg_knot_pair(const float4* p, float4& a, float4& b) {
@@ -303,16 +432,12 @@ __device__ __forceinline__ int z2r_index_d(int a, int b) {
 }
 
 // Force pass: f_i = sum_j u_ij (F'_i rho_j'(r) + F'_j rho_i'(r) + phi'(r)),
-// then force_to_accel and the fused Verlet halves.  SINGLE gathers
-// (position, F'_j) from pfp; otherwise position (type in w) and fpf.
-template <int T, int V, bool EV, bool SINGLE>
-__global__ void __launch_bounds__(256) k_eam_force_mixed(PairArgs A, EamDev E, const float* __restrict__ fpf,
-                                                         const float* __restrict__ epf,
-                                                         const float4* __restrict__ pfp) {
-  const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = gt / T;
-  const int lane = (int)(gt % T);
-  const bool live = i < A.n;
+// then force_to_accel and the fused Verlet halves.  SINGLE reads (position,
+// F'_j) through `fetch` from pfp; otherwise position (type in w) and fpf.
+template <int T, int V, bool EV, bool SINGLE, class Fetch>
+__device__ __forceinline__ void eam_force_atom(const PairArgs& A, const EamDev& E, const float* __restrict__ fpf,
+                                               const float* __restrict__ epf, int64_t i, int lane, bool live,
+                                               const Fetch& fetch) {
   const int nn = live ? min(A.nnb[i], A.maxnb) : 0;
   const float4 pi = live ? A.posf[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   const int cp = live ? A.cellpack[i] : 0;
@@ -320,7 +445,6 @@ __global__ void __launch_bounds__(256) k_eam_force_mixed(PairArgs A, EamDev E, c
   const int ti = SINGLE ? 0 : __float_as_int(pi.w);
   const int nr = E.nr, nr1 = E.nr + 1;
   const float rdr = E.rdrf;
-  const float4* __restrict__ P = SINGLE ? pfp : A.posf;
   float fx = 0.f, fy = 0.f, fz = 0.f, cfx = 0.f, cfy = 0.f, cfz = 0.f, e = 0.f, ce = 0.f;
   float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   const ListRows<T, V> L(A.nbr, i, lane, A.stride, nn);
@@ -334,7 +458,7 @@ __global__ void __launch_bounds__(256) k_eam_force_mixed(PairArgs A, EamDev E, c
     for (int q = 0; q < V; ++q) {
       if (!L.valid(r, q)) ent[q] = L.standin;
       const uint32_t j = ent[q] & GBMD_IDX_MASK;
-      pj[q] = __ldg(&P[j]);
+      pj[q] = fetch(ent[q], j);
       fpj[q] = SINGLE ? pj[q].w : __ldg(&fpf[j]);
     }
     float rx = 0.f, ry = 0.f, rz = 0.f, re = 0.f;
@@ -410,6 +534,32 @@ __global__ void __launch_bounds__(256) k_eam_force_mixed(PairArgs A, EamDev E, c
   }
 }
 
+template <int T, int V, bool EV, bool SINGLE>
+__global__ void __launch_bounds__(256) k_eam_force_mixed(PairArgs A, EamDev E, const float* __restrict__ fpf,
+                                                         const float* __restrict__ epf,
+                                                         const float4* __restrict__ pfp) {
+  const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i = gt / T;
+  eam_force_atom<T, V, EV, SINGLE>(A, E, fpf, epf, i, (int)(gt % T), i < A.n,
+                                   GlobalFetch{SINGLE ? pfp : A.posf});
+}
+
+template <bool EV>
+__global__ void __launch_bounds__(256) k_eam_force_staged(PairArgs A, EamDev E, const float* __restrict__ fpf,
+                                                          const float* __restrict__ epf,
+                                                          const float4* __restrict__ pfp,
+                                                          const int32_t* __restrict__ cstart, int K, int cap) {
+  __shared__ int4 rows[16];
+  __shared__ int sh[56];
+  extern __shared__ float4 staged_pos[];
+  int64_t a0, a1;
+  const bool ok = stage_cells(A.g, cstart, pfp, K, cap, staged_pos, rows, sh, a0, a1);
+  for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+    if (ok) eam_force_atom<1, 4, EV, true>(A, E, fpf, epf, i, 0, true, StagedFetch{staged_pos, rows});
+    else eam_force_atom<1, 4, EV, true>(A, E, fpf, epf, i, 0, true, GlobalFetch{pfp});
+  }
+}
+
 // ---------------------------------------------------------------------------
 // dispatch
 // ---------------------------------------------------------------------------
@@ -436,8 +586,53 @@ static void launch_mixed_TV(gbmd_context* c, const PairArgs& A, int part) {
   }
 }
 
+// Staged launch (one lane per atom, 4 entries per load): blocks of K home
+// cells along x; K gives about 0.8 * block atoms per block, and the staged
+// capacity is 1.4 times the mean neighbourhood of (K+2) x 3 x 3 cells (a
+// denser block falls back to global gathers).
+template <bool EV>
+static bool launch_staged(gbmd_context* c, const PairArgs& A, int part) {
+  const bool lj = c->pot == GBMD_POT_LJ || c->pot == GBMD_POT_LJ_MULTI;
+  if (!lj && !(c->pot == GBMD_POT_EAM_ALLOY && c->eam.nel == 1)) return false;
+  const Grid& g = c->grid;
+  const double per_cell = (double)A.n / (double)g.ncells;
+  const int B = c->block;
+  int K = (int)(0.8 * B / (per_cell > 0.5 ? per_cell : 0.5));
+  K = K < 1 ? 1 : (K > g.nc[0] ? g.nc[0] : K);
+  int cap = (int)(1.4 * per_cell * 9 * (K + 2)) + 64;
+  const int max_cap = (200 * 1024) / (int)sizeof(float4);
+  if (cap > max_cap) cap = max_cap;
+  const size_t smem = (size_t)cap * sizeof(float4);
+  const dim3 grid((unsigned)((g.nc[0] + K - 1) / K), (unsigned)g.nc[1], (unsigned)g.nc[2]);
+  cudaStream_t s = c->stream;
+  if (c->pot == GBMD_POT_LJ) {
+    if (part == 1) return true;
+    const LJPair& q = c->lj.p[0];
+    LJF P{q.sig2f, q.eps24f, q.eps4f, q.ecutf, q.rc2lo, q.rc2hi, q.rc2, q.rc};
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_lj_staged<EV, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_lj_staged<EV, false><<<grid, B, smem, s>>>(A, P, nullptr, 1, c->lj.rcut_max2, c->cell_start, K, cap);
+  } else if (c->pot == GBMD_POT_LJ_MULTI) {
+    if (part == 1) return true;
+    LJF P{};
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_lj_staged<EV, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_lj_staged<EV, true><<<grid, B, smem, s>>>(A, P, c->lj_tab_d, c->lj.ntypes, c->lj.rcut_max2, c->cell_start,
+                                                 K, cap);
+  } else {
+    if (smem > 48 * 1024) {
+      cudaFuncSetAttribute(k_eam_rho_staged<EV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(k_eam_force_staged<EV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
+    if (part != 2)
+      k_eam_rho_staged<EV><<<grid, B, smem, s>>>(A, c->eam, c->fpf, c->epf, c->pfp, c->cell_start, K, cap);
+    if (part != 1)
+      k_eam_force_staged<EV><<<grid, B, smem, s>>>(A, c->eam, c->fpf, c->epf, c->pfp, c->cell_start, K, cap);
+  }
+  return true;
+}
+
 template <bool EV>
 static int launch_mixed_E(gbmd_context* c, const PairArgs& A, int part) {
+  if (c->staged && c->tpa == 1 && c->vec == 4 && launch_staged<EV>(c, A, part)) return GBMD_OK;
   const int key = c->tpa * 8 + c->vec;
   switch (key) {
     case 1 * 8 + 1: launch_mixed_TV<1, 1, EV>(c, A, part); break;

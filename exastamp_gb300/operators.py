@@ -107,6 +107,15 @@ class ThermodynamicState:
     def total_energy(self):
         return float(self.kinetic_energy.sum()) + self.potential_energy
 
+    @property
+    def temperature_scal(self):
+        return float(self.temperature.sum()) / 3.0
+
+    @property
+    def full_stress_tensor(self):
+        """(virial + kinetic tensor) / volume (thermodynamic_state.h L71-87)."""
+        return (self.virial + self.ke_tensor) / self.volume
+
 
 class Simulation:
     """The grid + domain + species slots shared by the operators, backed by
@@ -118,12 +127,14 @@ class Simulation:
         self.rcut_max = 0.0
         self.ghost_dist_max = 0.0
         self.volume = 0.0
+        self.lo = self.hi = np.zeros(3)
         self.mixed = False
         if system is not None:
             self.load(system)
 
     def load(self, s):
         self.ctx.upload_system(s)
+        self.lo, self.hi = np.asarray(s.lo, float), np.asarray(s.hi, float)
         self.volume = float(np.prod(s.hi - s.lo))
         if not self.species:
             self.species = ["T%d" % t for t in range(len(s.masses))]
@@ -300,6 +311,56 @@ class simulation_thermodynamic_state(Operator):
         return ThermodynamicState(sim.ctx.thermo(), sim.volume)
 
 
+# dump_thermodynamic_state (src/io/dump_thermodynamic_state.cpp L55-120): the
+# column set, header and number formats of the reference's
+# thermodynamic_state.csv, so runs can be diffed against reference logs.
+# Conversion factors from the internal system (angstrom, dalton, picosecond)
+# built from CODATA 2018 constants as the reference does (L58-64).
+_ATOMIC_MASS = 1.66053906660e-27
+_BOLTZMANN = 1.380649e-23
+_ELEMENTARY_CHARGE = 1.602176634e-19
+THERMO_CONV_TEMPERATURE = 1.0e4 * _ATOMIC_MASS / _BOLTZMANN
+THERMO_CONV_ENERGY = 1.0e4 * _ATOMIC_MASS / _ELEMENTARY_CHARGE
+THERMO_CONV_PRESSURE = 1.0e4 * _ATOMIC_MASS * 1e30
+THERMO_CONV_DENSITY = _ATOMIC_MASS * 1e3 * 1e24
+THERMO_HEADER = ("# Step     Time (ps)     Particles  Tot. E. (eV/part)  Kin. E. (eV/part)  Pot. E. (eV/part)  "
+                 "Temp. (K) Pxx Pyy Pzz Pxy Pxz Pyz (Pa) A/B/C (ang)    alpha/beta/gamma (deg)     Vol. (ang^3)  "
+                 "Rho (g/cm^3)")
+_THERMO_FMT = ("%9d % .6e %13d  % .10e  % .10e  % .10e  % 9.12f  % 9.12f  % 9.12f  % 9.12f  % 9.12f  % 9.12f "
+               "% 9.12f % 12.12f % 12.12f % 12.12f % 9.12f % 9.12f % 9.12f % 16.12f % 13.12f ")
+
+
+class dump_thermodynamic_state(Operator):
+    """Appends one line per call (the header first when print_header) to
+    `thermostate_file`; cubic boxes (identity xform), so the cell angles are
+    90 degrees."""
+    name = "dump_thermodynamic_state"
+
+    def format_line(self, sim: "Simulation", st: ThermodynamicState, timestep: int, physical_time: float) -> str:
+        n = st.particle_count
+        P = st.full_stress_tensor * THERMO_CONV_PRESSURE
+        lo, hi = np.asarray(sim.lo, float), np.asarray(sim.hi, float)
+        A, B, C = (float(v) for v in (hi - lo))
+        vol = st.volume
+        return _THERMO_FMT % (
+            timestep, physical_time, n,
+            st.total_energy / n * THERMO_CONV_ENERGY,
+            float(st.kinetic_energy.sum()) / n * THERMO_CONV_ENERGY,
+            st.potential_energy / n * THERMO_CONV_ENERGY,
+            st.temperature_scal / n * THERMO_CONV_TEMPERATURE,
+            P[0, 0], P[1, 1], P[2, 2], P[0, 1], P[0, 2], P[1, 2],
+            A, B, C, 90.0, 90.0, 90.0, vol, THERMO_CONV_DENSITY * st.mass / vol)
+
+    def execute(self, sim: "Simulation", st: ThermodynamicState, timestep: int, physical_time: float = 0.0):
+        path = self.slots.get("thermostate_file", "thermodynamic_state.csv")
+        line = self.format_line(sim, st, timestep, physical_time)
+        with open(path, "a") as fh:
+            if self.slots.get("print_header", True):
+                fh.write(THERMO_HEADER + "\n")
+            fh.write(line + "\n")
+        return line
+
+
 def verlet_nve(sim: Simulation, nsteps: int, dt: float, rebuild_every: int = 10, thermo_every: int = 0,
                use_graph: bool = False):
     """The verlet_nve graph (config_numerical_schemes.msp L44-52) run on the
@@ -309,7 +370,7 @@ def verlet_nve(sim: Simulation, nsteps: int, dt: float, rebuild_every: int = 10,
 
 
 FORCE_OPERATORS = {"lj_compute_force": lj_compute_force, "lj_multi_force": lj_multi_force,
-                   "eam_alloy_force": eam_alloy_force}
+                   "eam_alloy_force": eam_alloy_force, "johnson_force": johnson_force}
 
 
 def compute_force_from_config(cfg: dict) -> Operator:

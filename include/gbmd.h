@@ -153,6 +153,13 @@ int gbmd_get_launch(const gbmd_context* ctx, int* lanes_per_atom, int* block);
  * atom).  The list rows are laid out lanes_per_atom * entries wide. */
 int gbmd_set_launch_ex(gbmd_context* ctx, int lanes_per_atom, int entries_per_load, int block);
 int gbmd_get_launch_ex(const gbmd_context* ctx, int* lanes_per_atom, int* entries_per_load, int* block);
+/* With one lane per atom and 4 entries per load, the mixed-precision pair
+ * kernels can run one block per run of home cells along x and read
+ * neighbour positions from a shared-memory copy of the surrounding cells
+ * instead of gathering them (enable = 1, the default); results are the same
+ * bit for bit. */
+int gbmd_set_neighbor_staging(gbmd_context* ctx, int enable);
+int gbmd_get_neighbor_staging(const gbmd_context* ctx, int* enabled);
 
 /* ---- neighbour list --------------------------------------------------------
  * chunk_neighbors (exaNBody; config data/config/config_move_particles.msp

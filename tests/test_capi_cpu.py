@@ -62,3 +62,32 @@ def test_header_is_plain_c():
     hdr = os.path.join(os.path.dirname(os.path.dirname(__file__)), "include", "gbmd.h")
     r = subprocess.run(["gcc", "-std=c99", "-fsyntax-only", "-x", "c", hdr], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_dump_thermodynamic_state_columns(oracle, tmp_path):
+    """The thermo CSV line: 21 columns in the reference's order and formats,
+    total = kinetic + potential per particle, temperature from the kinetic
+    energy without the centre-of-mass term, cubic-box geometry."""
+    import types
+
+    import numpy as np
+
+    from exastamp_gb300 import operators as O
+    from exastamp_gb300 import systems as S
+
+    s = S.eam_cu_fcc(ncell=3, T=300.0, seed=5)
+    th = oracle.thermo(s.vx, s.vy, s.vz, np.full(s.n, -3.0 * S.EV), np.zeros((s.n, 9)), s.type, s.masses)
+    vol = float(np.prod(s.hi - s.lo))
+    st = O.ThermodynamicState(th, vol)
+    sim = types.SimpleNamespace(lo=s.lo, hi=s.hi, volume=vol)
+    op = O.dump_thermodynamic_state(thermostate_file=str(tmp_path / "thermo.csv"))
+    line = op.execute(sim, st, timestep=10, physical_time=0.01)
+    text = (tmp_path / "thermo.csv").read_text().splitlines()
+    assert text[0] == O.THERMO_HEADER and text[1] == line
+    cols = [float(v) for v in line.split()]
+    assert len(cols) == 21 and cols[0] == 10 and cols[2] == s.n
+    assert abs(cols[3] - (cols[4] + cols[5])) < 1e-9 * abs(cols[3])
+    assert abs(cols[5] + 3.0) < 1e-9
+    assert abs(cols[6] - 300.0) < 30.0  # Maxwell-Boltzmann draw of 108 atoms
+    assert cols[13:16] == [float(s.hi[0] - s.lo[0])] * 3 and cols[16:19] == [90.0] * 3
+    assert abs(cols[20] - O.THERMO_CONV_DENSITY * s.masses[0] * s.n / vol) < 1e-9
