@@ -524,7 +524,8 @@ def main():
         out["e2e"] = {"value": n * args.e2e_steps * ws / (mse * 1e-3), "unit": "atom-timesteps/s",
                       "h2d_bytes_per_step": 72 * n, "d2h_bytes_per_step": 72 * n, "steps": args.e2e_steps,
                       "ms_per_step": mse / args.e2e_steps,
-                      "path": "gbmd_upload_state(pinned r,v,a) + gbmd_run_nve(1) + gbmd_download(r,v,a)"}
+                      "path": "gbmd_upload_state(pinned r,v,a; skin/2 displacement test) + gbmd_run_nve(1) + "
+                              "gbmd_download(pinned r,v,a)"}
 
     # ---- batched replicas (4,096 EAM systems) and the parameter adjoint --------
     if not args.no_batch and ws == 1:

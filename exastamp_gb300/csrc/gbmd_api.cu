@@ -153,6 +153,42 @@ __global__ void k_to_user_multi(int64_t n, int64_t cap, Arrays9 src, const int32
   for (int k = 0; k < count; ++k) stage[k * cap + u] = src.a[k][p];
 }
 
+// inv[user[p]] = p: caller index -> cell-sorted index
+__global__ void k_invert_user(int64_t n, const int32_t* __restrict__ user, int32_t* __restrict__ inv) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  inv[user[p]] = (int32_t)p;
+}
+
+// Page-locked caller arrays read / written by the kernel itself over the
+// host link, walked in the caller's order (consecutive threads, consecutive
+// host addresses); the device side is the scattered one.
+__global__ void k_host_to_state(int64_t n, const int32_t* __restrict__ inv, Arrays9 host, Arrays9 dev, int count) {
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (u >= n) return;
+  const int64_t p = inv[u];
+  double v[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k)
+    if (k < count) v[k] = host.a[k][u];
+#pragma unroll
+  for (int k = 0; k < 9; ++k)
+    if (k < count) dev.a[k][p] = v[k];
+}
+
+__global__ void k_state_to_host(int64_t n, const int32_t* __restrict__ inv, Arrays9 dev, Arrays9 host, int count) {
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (u >= n) return;
+  const int64_t p = inv[u];
+  double v[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k)
+    if (k < count) v[k] = dev.a[k][p];
+#pragma unroll
+  for (int k = 0; k < 9; ++k)
+    if (k < count) host.a[k][u] = v[k];
+}
+
 __global__ void k_iota(int64_t n, int32_t* __restrict__ user, uint64_t* __restrict__ id, int with_id) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= n) return;
@@ -424,12 +460,38 @@ int gbmd_upload_atoms(gbmd_context* c, int64_t n, const double* rx, const double
 
 // Copy r (and v, a when given) from host arrays in upload order into the
 // cell-sorted device state: one batch of copies, one permutation kernel.
+// Device addresses of caller arrays the GPU can access directly (page-locked
+// or managed memory); false when any of them is ordinary pageable memory.
+static bool device_accessible(const double* const* host, int count, Arrays9& out) {
+  for (int k = 0; k < count; ++k) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host[k]) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return false;
+    }
+    if ((a.type != cudaMemoryTypeHost && a.type != cudaMemoryTypeManaged) || !a.devicePointer) return false;
+    out.a[k] = static_cast<double*>(a.devicePointer);
+  }
+  return true;
+}
+
+static int32_t* inverse_user(gbmd_context* c) {
+  int32_t* inv = reinterpret_cast<int32_t*>(c->stage + 8 * c->cap);  // the last staging slot
+  k_invert_user<<<nblk(c->n, 256), 256, 0, c->stream>>>(c->n, c->USER(), inv);
+  return inv;
+}
+
 static int upload_arrays(gbmd_context* c, const double* const* host, double* const* dev, int count) {
   const int64_t n = c->n;
+  Arrays9 hd{}, d{};
+  for (int k = 0; k < count; ++k) d.a[k] = dev[k];
+  if (device_accessible(host, count, hd)) {
+    const int32_t* inv = inverse_user(c);
+    k_host_to_state<<<nblk(n, 256), 256, 0, c->stream>>>(n, inv, hd, d, count);
+    return GBMD_OK;
+  }
   int rc = staged_copies(c, const_cast<double* const*>(host), count, true);
   if (rc) return rc;
-  Arrays9 d{};
-  for (int k = 0; k < count; ++k) d.a[k] = dev[k];
   k_from_user_multi<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->cap, c->stage, c->USER(), d, count);
   return GBMD_OK;
 }
@@ -439,7 +501,11 @@ static int upload_arrays(gbmd_context* c, const double* const* host, double* con
 // L116-118), otherwise refresh the FP32/FP64 gather copies.
 static int after_new_positions(gbmd_context* c) {
   c->forces_valid_step = -1;
-  if (!c->list_valid) return GBMD_OK;
+  if (!c->list_valid) {
+    // the caller may reuse its arrays once the upload returns
+    GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
+    return GBMD_OK;
+  }
   cudaStream_t s = c->stream;
   GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_DISPL, 0, sizeof(int), s));
   const double thr = 0.5 * c->skin;
@@ -505,7 +571,11 @@ int gbmd_download(gbmd_context* c, double* rx, double* ry, double* rz, double* v
       src.a[count] = const_cast<double*>(f[k].dev);
       host[count++] = f[k].host;
     }
-  if (count) {
+  Arrays9 hd{};
+  if (count && device_accessible(host, count, hd)) {
+    const int32_t* inv = inverse_user(c);
+    k_state_to_host<<<nblk(n, 256), 256, 0, s>>>(n, inv, src, hd, count);
+  } else if (count) {
     k_to_user_multi<<<nblk(n, 256), 256, 0, s>>>(n, c->cap, src, c->USER(), c->stage, count);
     int rc = staged_copies(c, host, count, false);
     if (rc) return rc;

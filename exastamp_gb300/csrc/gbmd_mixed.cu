@@ -169,12 +169,20 @@ __device__ bool stage_cells(const Grid& g, const int32_t* __restrict__ cstart, c
   __syncthreads();
   const int total = sh[54];
   if (total > cap) return false;  // uniform
-  for (int s = 0; s < 9; ++s) {
-    const int ga = sh[4 * s], na = sh[4 * s + 1], gb = sh[4 * s + 2], nb = sh[4 * s + 3];
-    const int oa = sh[36 + 2 * s], ob = sh[36 + 2 * s + 1];
-    for (int t = threadIdx.x; t < na; t += blockDim.x) pos[oa + t] = __ldg(&src[ga + t]);
-    for (int t = threadIdx.x; t < nb; t += blockDim.x) pos[ob + t] = __ldg(&src[gb + t]);
+  // all copies in flight at once: slot u belongs to the last segment starting
+  // at or before it (18 segments A0 B0 A1 B1 ... in staging order)
+  for (int u = threadIdx.x; u < total; u += blockDim.x) {
+    int seg = 0;
+#pragma unroll
+    for (int q = 1; q < 18; ++q)
+      if (sh[36 + q] <= u) seg = q;
+    const int s = seg >> 1, b = seg & 1;
+    const int g0 = sh[4 * s + 2 * b];
+    const float4* from = &src[g0 + (u - sh[36 + seg])];
+    const unsigned to = (unsigned)__cvta_generic_to_shared(&pos[u]);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(to), "l"(from) : "memory");
   }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
   __syncthreads();
   return true;
 }
