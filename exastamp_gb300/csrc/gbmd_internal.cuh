@@ -169,7 +169,7 @@ struct gbmd_context {
   int maxnb = 0;                // per-atom capacity (multiple of tpa * vec)
   int tpa = 1;                  // lanes per atom (autotuned; default = the GB300 optimum)
   int vec = 4;                  // list entries per lane per load (1 or 4, mixed kernels; autotuned)
-  bool staged = true;           // 1 lane x 4 entries: neighbour positions from shared memory
+  bool staged = false;          // 1 lane x 4 entries: neighbour positions from shared memory
   int block = 256;              // threads per block (autotuned)
   double skin = 0.0, rlist = 0.0;
   bool list_valid = false;

@@ -156,8 +156,8 @@ int gbmd_get_launch_ex(const gbmd_context* ctx, int* lanes_per_atom, int* entrie
 /* With one lane per atom and 4 entries per load, the mixed-precision pair
  * kernels can run one block per run of home cells along x and read
  * neighbour positions from a shared-memory copy of the surrounding cells
- * instead of gathering them (enable = 1, the default); results are the same
- * bit for bit. */
+ * instead of gathering them (enable = 1; default 0, the gathers are faster
+ * on GB300); results are the same bit for bit. */
 int gbmd_set_neighbor_staging(gbmd_context* ctx, int enable);
 int gbmd_get_neighbor_staging(const gbmd_context* ctx, int* enabled);
 
