@@ -393,7 +393,6 @@ def main():
     else:
         from exastamp_gb300 import autotune
         lanes, vec, block, tuned = autotune.tune(ctx, key="%s-%s" % (args.workload, args.precision))
-        ctx.set_launch(lanes, block, vec)
     R, dt = args.rebuild_every, w["dt"]
     # fixed interval: thermo at the end of each 2R-step graph chunk; with the
     # displacement trigger (R = -1) every 20 steps
@@ -439,7 +438,8 @@ def main():
                       "list_builds_in_timed_region": rebuilds,
                       "neighbours_per_atom": npairs / s.n, "cells": nc.tolist(),
                       "lanes_per_atom": ctx.get_launch_ex()[0], "list_entries_per_load": ctx.get_launch_ex()[1],
-                      "block": ctx.get_launch_ex()[2], "staged_neighbour_positions": ctx.get_neighbor_staging(),
+                      "block": ctx.get_launch_ex()[2], "density_block": ctx.get_density_block(),
+                      "staged_neighbour_positions": ctx.get_neighbor_staging(),
                       "parallelism": "replicas" if ws > 1 else "single-gpu",
                       "l2": "inputs larger than L2 (neighbour list %.2f GB)" % (npairs * 4 / 1e9)
                       if npairs * 4 > 129e6 else "inputs resident in L2 (not flushed)",

@@ -74,6 +74,8 @@ def lib(path: str = LIB_PATH):
             "gbmd_get_launch": ([vp, P(i32), P(i32)], i32),
             "gbmd_set_launch_ex": ([vp, i32, i32, i32], i32),
             "gbmd_set_neighbor_staging": ([vp, i32], i32),
+            "gbmd_set_density_block": ([vp, i32], i32),
+            "gbmd_get_density_block": ([vp, P(i32)], i32),
             "gbmd_get_neighbor_staging": ([vp, P(i32)], i32),
             "gbmd_get_launch_ex": ([vp, P(i32), P(i32), P(i32)], i32),
             "gbmd_set_skin": ([vp, dbl], i32),
@@ -87,6 +89,7 @@ def lib(path: str = LIB_PATH):
             "gbmd_run_nve": ([vp, i32, dbl, i32, i32, vp, i32], i32),
             "gbmd_run_minimize": ([vp, i32, dbl, dbl, i32], i32),
             "gbmd_set_eam_johnson": ([vp, vp, dbl], i32),
+            "gbmd_lj_loss_grad": ([vp, vp, vp, vp, vp, dbl, dbl, P(dbl), vp], i32),
             "gbmd_list_builds": ([vp, P(i64)], i32),
             "gbmd_thermo": ([vp, vp], i32),
             "gbmd_device_state": ([vp] + [vp] * 11, i32),
@@ -226,6 +229,15 @@ class Context:
         self._chk(self._L.gbmd_get_launch(self.h, C.byref(t), C.byref(b)))
         return t.value, b.value
 
+    def set_density_block(self, block):
+        """Threads per block of the EAM density kernels (0 = the pair kernels')."""
+        self._chk(self._L.gbmd_set_density_block(self.h, int(block)))
+
+    def get_density_block(self):
+        b = C.c_int()
+        self._chk(self._L.gbmd_get_density_block(self.h, C.byref(b)))
+        return b.value
+
     def set_neighbor_staging(self, enable):
         self._chk(self._L.gbmd_set_neighbor_staging(self.h, 1 if enable else 0))
 
@@ -292,6 +304,18 @@ class Context:
         if p.shape != (19,):
             raise ValueError("johnson_force takes 19 parameters")
         self._chk(self._L.gbmd_set_eam_johnson(self.h, _p(p), float(rcut)))
+
+    def lj_loss_grad(self, f_target, e_target, w_force, w_energy):
+        """Force-matching + energy loss of lj_compute_force and its gradient
+        with respect to (epsilon, sigma); f_target (n, 3) forces, e_target (n,)
+        per-atom energies, both in upload order."""
+        ft = np.asarray(f_target, dtype=np.float64)
+        fx, fy, fz = (np.ascontiguousarray(ft[:, d]) for d in range(3))
+        et = _f64(e_target)
+        loss, g = C.c_double(), np.zeros(2)
+        self._chk(self._L.gbmd_lj_loss_grad(self.h, _p(fx), _p(fy), _p(fz), _p(et), float(w_force), float(w_energy),
+                                            C.byref(loss), _p(g)))
+        return loss.value, g
 
     def list_builds(self):
         n = C.c_int64(0)

@@ -18,7 +18,7 @@ import os
 
 LANES = (1, 2, 4, 8, 16)
 VECS = (1, 4)
-BLOCKS = (128, 256)
+BLOCKS = (64, 128, 256)
 
 
 def _cache_path():
@@ -85,13 +85,17 @@ def tune_batch(batch, key: str, blocks=(128, 256, 512), stencils=(1, 2), adjoint
 
 def tune(ctx, key: str, lanes=LANES, blocks=BLOCKS, vecs=VECS, reps: int = 3, use_cache: bool = True):
     """Return (lanes, entries per load, block, timings) for this context's
-    system and potential."""
+    system and potential and leave the chosen shape set on the context: the
+    pair-kernel block, the density-kernel block (chosen separately, the two
+    kernels being independent) and the staging switch."""
     n = ctx.n
-    ck = "%s|%s|%d|vs" % (_gpu_name(), key, n)
+    ck = "%s|%s|%d|vsd" % (_gpu_name(), key, n)
     cache = _load() if use_cache else {}
     if ck in cache:
         e = cache[ck]
-        ctx.set_neighbor_staging(bool(e.get("staged", True)))
+        ctx.set_launch(int(e["lanes"]), int(e["block"]), int(e["vec"]))
+        ctx.set_neighbor_staging(bool(e.get("staged", False)))
+        ctx.set_density_block(int(e.get("density_block", 0)))
         return int(e["lanes"]), int(e["vec"]), int(e["block"]), e.get("timings", {})
     timings = {}
     best = None
@@ -99,20 +103,28 @@ def tune(ctx, key: str, lanes=LANES, blocks=BLOCKS, vecs=VECS, reps: int = 3, us
         for v in vecs:
             if v > 1 and t > 4:
                 continue
-            for b in blocks:
-                if b % t:
-                    continue
-                # shared-memory staging of neighbour positions exists for 1 lane x 4 entries
-                for staged in ((False, True) if (t == 1 and v == 4) else (False,)):
+            # shared-memory staging of neighbour positions exists for 1 lane x 4 entries
+            for staged in ((False, True) if (t == 1 and v == 4) else (False,)):
+                dens, pair = {}, {}
+                for b in blocks:
+                    if b % t:
+                        continue
                     ctx.set_launch(t, b, v)
+                    ctx.set_density_block(0)
                     ctx.set_neighbor_staging(staged)
                     prof = ctx.profile_step(reps=reps)
-                    ms = prof["density"] + prof["pair"]
-                    timings["%dx%dx%d%s" % (t, v, b, "s" if staged else "")] = ms
-                    if best is None or ms < best[0]:
-                        best = (ms, t, v, b, staged)
-    cache[ck] = {"lanes": best[1], "vec": best[2], "block": best[3], "staged": best[4], "timings": timings}
+                    dens[b], pair[b] = prof["density"], prof["pair"]
+                    timings["%dx%dx%d%s" % (t, v, b, "s" if staged else "")] = [prof["density"], prof["pair"]]
+                bd = min(dens, key=dens.get)
+                bp = min(pair, key=pair.get)
+                ms = dens[bd] + pair[bp]
+                if best is None or ms < best[0]:
+                    best = (ms, t, v, bp, staged, bd)
+    _, t, v, bp, staged, bd = best
+    cache[ck] = {"lanes": t, "vec": v, "block": bp, "staged": staged, "density_block": bd, "timings": timings}
     if use_cache:
         _store(cache)
-    ctx.set_neighbor_staging(best[4])
-    return best[1], best[2], best[3], timings
+    ctx.set_launch(t, bp, v)
+    ctx.set_neighbor_staging(staged)
+    ctx.set_density_block(bd)
+    return t, v, bp, timings

@@ -14,7 +14,7 @@
 #include <fstream>
 #include <sstream>
 
-#include "gbmd_internal.cuh"
+#include "gbmd_pair_common.cuh"
 
 namespace gbmd {
 
@@ -373,7 +373,7 @@ int gbmd_destroy(gbmd_context* c) {
   free_atoms(c);
   cudaFree(c->cell_start); cudaFree(c->cell_fill); cudaFree(c->scan_tmp); cudaFree(c->nbr);
   cudaFree(c->eam_d); cudaFree(c->eam_f); cudaFree(c->lj_tab_d);
-  cudaFree(c->d_err); cudaFree(c->d_thermo); cudaFree(c->d_rows);
+  cudaFree(c->d_err); cudaFree(c->d_thermo); cudaFree(c->d_rows); cudaFree(c->adj_scratch);
   if (c->h_err) cudaFreeHost(c->h_err);
   if (c->h_thermo) cudaFreeHost(c->h_thermo);
   for (int k = 0; k < 2; ++k) {
@@ -841,6 +841,7 @@ int gbmd_set_launch_ex(gbmd_context* c, int tpa, int vec, int block) {
     invalidate_list(c);
   }
   c->block = block;
+  if (c->block_rho % tpa) c->block_rho = 0;  // follow `block` until set again
   drop_graph(c);
   return GBMD_OK;
 }
@@ -854,6 +855,21 @@ int gbmd_get_launch(const gbmd_context* c, int* tpa, int* block) {
   if (!c) return GBMD_ERR_INVALID;
   if (tpa) *tpa = c->tpa;
   if (block) *block = c->block;
+  return GBMD_OK;
+}
+
+int gbmd_set_density_block(gbmd_context* c, int block) {
+  if (!c) return GBMD_ERR_INVALID;
+  if (block != 0 && (block < 32 || block > 256 || block % 32 || block % c->tpa))
+    return set_error(c, GBMD_ERR_INVALID, "density block must be 0 or a multiple of 32 in [32,256]");
+  c->block_rho = block;
+  drop_graph(c);
+  return GBMD_OK;
+}
+
+int gbmd_get_density_block(const gbmd_context* c, int* block) {
+  if (!c || !block) return GBMD_ERR_INVALID;
+  *block = c->block_rho ? c->block_rho : c->block;
   return GBMD_OK;
 }
 
@@ -1052,6 +1068,7 @@ static int capture_graph(gbmd_context* c, double dt, int R, int G, bool thermo_e
   c->graph_key_vec = c->vec;
   c->graph_key_staged = c->staged ? 1 : 0;
   c->graph_key_block = c->block;
+  c->graph_key_block_rho = c->block_rho;
   c->graph_key_prec = c->precision;
   return GBMD_OK;
 }
@@ -1060,6 +1077,7 @@ static bool graph_matches(const gbmd_context* c, double dt, int R, int G, bool t
   return c->graph_exec && c->graph_rebuild_every == R && c->graph_chunk == G && c->graph_dt == dt &&
          c->graph_thermo_end == (thermo_end ? 1 : 0) && c->graph_key_n == c->n && c->graph_key_maxnb == c->maxnb &&
          c->graph_key_tpa == c->tpa && c->graph_key_vec == c->vec && c->graph_key_block == c->block &&
+         c->graph_key_block_rho == c->block_rho &&
          c->graph_key_staged == (c->staged ? 1 : 0) &&
          c->graph_key_prec == c->precision;
 }
@@ -1148,6 +1166,44 @@ int gbmd_run_minimize(gbmd_context* c, int nsteps, double dt, double tolF, int r
   c->forces_valid_step = -1;
   GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
   if (trigger && (rc = collect_device_rebuilds(c))) return rc;
+  return check_device_errors(c);
+}
+
+// lj_compute_force parameter adjoint (gbmd_adjoint_lj.cu): forces and
+// energies of the current state, the loss against caller-order targets and
+// its gradient with respect to (epsilon, sigma).
+int gbmd_lj_loss_grad(gbmd_context* c, const double* fx_target, const double* fy_target, const double* fz_target,
+                      const double* e_target, double w_force, double w_energy, double* loss, double grad[2]) {
+  if (!c || !fx_target || !fy_target || !fz_target || !e_target || !loss || !grad) return GBMD_ERR_INVALID;
+  if (c->pot != GBMD_POT_LJ) return set_error(c, GBMD_ERR_INVALID, "the LJ adjoint needs lj_compute_force");
+  const int64_t n = c->n;
+  if (n == 0) {
+    *loss = grad[0] = grad[1] = 0.0;
+    return GBMD_OK;
+  }
+  int rc = gbmd_compute_forces(c, GBMD_FORCE_ENERGY);
+  if (rc) return rc;
+  const int64_t need = 7 * n + 3 * 592 + 3;
+  if (need > c->adj_cap) {
+    cudaFree(c->adj_scratch);
+    c->adj_scratch = nullptr;
+    GBMD_CUDA(c, cudaMalloc(&c->adj_scratch, sizeof(double) * need));
+    c->adj_cap = need;
+  }
+  double* t = c->adj_scratch;
+  const double* host[4] = {fx_target, fy_target, fz_target, e_target};
+  double* dev[4] = {t, t + n, t + 2 * n, t + 3 * n};
+  if ((rc = upload_arrays(c, host, dev, 4))) return rc;
+  ForceFlags f;
+  const PairArgs A = make_args(c, f);
+  const double* tg[4] = {dev[0], dev[1], dev[2], dev[3]};
+  if ((rc = launch_lj_loss_grad(c, A, tg, w_force, w_energy, t + 4 * n))) return rc;
+  GBMD_CUDA(c, cudaMemcpyAsync(c->h_thermo, t + 7 * n + 3 * 592, sizeof(double) * 3, cudaMemcpyDeviceToHost,
+                               c->stream));
+  GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
+  *loss = c->h_thermo[0];
+  grad[0] = c->h_thermo[1];
+  grad[1] = c->h_thermo[2];
   return check_device_errors(c);
 }
 

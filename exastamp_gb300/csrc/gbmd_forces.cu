@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(256) k_eam_force(PairArgs A, EamDev E, const d
 // ---------------------------------------------------------------------------
 // host dispatch
 // ---------------------------------------------------------------------------
-static PairArgs make_args(gbmd_context* c, const ForceFlags& f) {
+PairArgs make_args(gbmd_context* c, const ForceFlags& f) {
   PairArgs A;
   A.n = c->n;
   A.W = list_width(c);

@@ -136,6 +136,8 @@ struct gbmd_context {
   int32_t* src = nullptr;                 // scratch: new position -> old position
   float* fpf = nullptr;                   // EAM F'(rho) FP32 (mixed)
   float4* pfp = nullptr;                  // single-element EAM: FP32 position with F'(rho) in w (mixed)
+  double* adj_scratch = nullptr;          // LJ adjoint: targets + per-atom terms (lazily allocated)
+  int64_t adj_cap = 0;
   double* fpd = nullptr;                  // EAM rho_dEmb FP64
   double* stage = nullptr;                // 9n staging for host<->device reorders
   double* rref = nullptr;                 // 3n positions at the last rebuild (displacement trigger)
@@ -170,7 +172,8 @@ struct gbmd_context {
   int tpa = 1;                  // lanes per atom (autotuned; default = the GB300 optimum)
   int vec = 4;                  // list entries per lane per load (1 or 4, mixed kernels; autotuned)
   bool staged = false;          // 1 lane x 4 entries: neighbour positions from shared memory
-  int block = 256;              // threads per block (autotuned)
+  int block = 256;              // threads per block of the pair / force kernels (autotuned)
+  int block_rho = 128;          // threads per block of the EAM density kernels (autotuned; 0 = block)
   double skin = 0.0, rlist = 0.0;
   bool list_valid = false;
   int64_t list_builds = 0;
@@ -209,7 +212,7 @@ struct gbmd_context {
   int graph_thermo_end = 0;
   int64_t graph_key_n = -1;
   int graph_key_maxnb = -1, graph_key_tpa = -1, graph_key_block = -1, graph_key_prec = -1, graph_key_vec = -1,
-      graph_key_staged = -1;
+      graph_key_staged = -1, graph_key_block_rho = -1;
 };
 
 // ---------------------------------------------------------------------------

@@ -89,8 +89,10 @@ struct ListRows {
   __device__ __forceinline__ void load(int r, uint32_t (&e)[V]) const {
     const uint32_t* q = p + (size_t)r * stride;
     if constexpr (V == 4) {
-      const uint4 u = __ldcs(reinterpret_cast<const uint4*>(q));
-      e[0] = u.x; e[1] = u.y; e[2] = u.z; e[3] = u.w;
+      // read once per kernel: keep it out of L1, which serves the gathers
+      asm("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+          : "=r"(e[0]), "=r"(e[1]), "=r"(e[2]), "=r"(e[3])
+          : "l"(q));
     } else {
 #pragma unroll
       for (int v = 0; v < V; ++v) e[v] = __ldcs(q + v);
@@ -108,7 +110,13 @@ struct ListRows {
 // ---------------------------------------------------------------------------
 struct GlobalFetch {
   const float4* __restrict__ P;
-  __device__ __forceinline__ float4 operator()(uint32_t ent, uint32_t j) const { return __ldg(&P[j]); }
+  __device__ __forceinline__ float4 operator()(uint32_t ent, uint32_t j) const {
+    float4 v;
+    asm("ld.global.nc.L1::evict_last.v4.f32 {%0,%1,%2,%3}, [%4];"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "l"(P + j));
+    return v;
+  }
 };
 
 struct StagedFetch {
@@ -575,6 +583,8 @@ template <int T, int V, bool EV>
 static void launch_mixed_TV(gbmd_context* c, const PairArgs& A, int part) {
   const int B = c->block;
   const unsigned grid = (unsigned)((A.n * T + B - 1) / B);
+  const int Bd = c->block_rho ? c->block_rho : B;  // density kernels
+  const unsigned gridd = (unsigned)((A.n * T + Bd - 1) / Bd);
   cudaStream_t s = c->stream;
   if (c->pot == GBMD_POT_LJ) {
     if (part == 1) return;
@@ -586,10 +596,10 @@ static void launch_mixed_TV(gbmd_context* c, const PairArgs& A, int part) {
     LJF P{};
     k_lj_mixed<T, V, EV, true><<<grid, B, 0, s>>>(A, P, c->lj_tab_d, c->lj.ntypes, c->lj.rcut_max2);
   } else if (c->eam.nel == 1) {
-    if (part != 2) k_eam_rho_mixed<T, V, EV, true><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
+    if (part != 2) k_eam_rho_mixed<T, V, EV, true><<<gridd, Bd, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
     if (part != 1) k_eam_force_mixed<T, V, EV, true><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
   } else {
-    if (part != 2) k_eam_rho_mixed<T, V, EV, false><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
+    if (part != 2) k_eam_rho_mixed<T, V, EV, false><<<gridd, Bd, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
     if (part != 1) k_eam_force_mixed<T, V, EV, false><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
   }
 }

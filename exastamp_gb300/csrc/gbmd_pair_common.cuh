@@ -47,6 +47,13 @@ struct PairArgs {
 
 // Mixed-precision pair kernels (gbmd_mixed.cu); part as in launch_forces.
 int launch_mixed(gbmd_context* c, const PairArgs& A, int part, bool ev);
+// Pair-kernel arguments for the context's current buffers (gbmd_forces.cu).
+PairArgs make_args(gbmd_context* c, const ForceFlags& f);
+// lj_compute_force parameter adjoint (gbmd_adjoint_lj.cu): targets are
+// cell-sorted device arrays fx, fy, fz, e; scratch holds 3n + 1779 doubles and
+// receives (loss, dL/deps, dL/dsigma) at its end.
+int launch_lj_loss_grad(gbmd_context* c, const PairArgs& A, const double* const targets[4], double wF, double wE,
+                        double* scratch);
 // johnson_force kernels, both precisions (gbmd_johnson.cu).
 int launch_johnson(gbmd_context* c, const PairArgs& A, int part, bool ev, bool mixed);
 

@@ -153,6 +153,11 @@ int gbmd_get_launch(const gbmd_context* ctx, int* lanes_per_atom, int* block);
  * atom).  The list rows are laid out lanes_per_atom * entries wide. */
 int gbmd_set_launch_ex(gbmd_context* ctx, int lanes_per_atom, int entries_per_load, int block);
 int gbmd_get_launch_ex(const gbmd_context* ctx, int* lanes_per_atom, int* entries_per_load, int* block);
+/* Threads per block of the EAM density kernels (0 = the pair kernels'
+ * block).  On GB300 the density pass prefers smaller blocks than the force
+ * pass (4 M-atom Cu: 128 vs 256); the autotuner sets both. */
+int gbmd_set_density_block(gbmd_context* ctx, int block);
+int gbmd_get_density_block(const gbmd_context* ctx, int* block);
 /* With one lane per atom and 4 entries per load, the mixed-precision pair
  * kernels can run one block per run of home cells along x and read
  * neighbour positions from a shared-memory copy of the surrounding cells
@@ -213,6 +218,15 @@ int gbmd_run_nve(gbmd_context* ctx, int nsteps, double dt, int rebuild_every, in
 /* Minimiser: nsteps of compute forces + push_min (r += a dt^2/2, clipped);
  * rebuild_every as gbmd_run_nve. */
 int gbmd_run_minimize(gbmd_context* ctx, int nsteps, double dt, double tolF, int rebuild_every);
+/* Parameter adjoint of lj_compute_force (no reference counterpart: the
+ * reference has no gradients).  Computes forces and per-atom energies of the
+ * current state (precision as set), the force-matching + energy loss
+ *   L = w_force sum_i |F_i - F*_i|^2 + w_energy sum_i (E_i - E*_i)^2
+ * against host targets in upload order (F = m a, E = per-atom energy), and
+ * dL/d(epsilon, sigma) with every pair term recomputed in FP64.  grad[2]. */
+int gbmd_lj_loss_grad(gbmd_context* ctx, const double* fx_target, const double* fy_target, const double* fz_target,
+                      const double* e_target, double w_force, double w_energy, double* loss, double grad[2]);
+
 /* Number of neighbour-list builds since the context was created, including
  * the displacement-triggered ones (counted on the device, folded in when
  * gbmd_run_nve / gbmd_run_minimize return). */

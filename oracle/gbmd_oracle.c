@@ -542,6 +542,66 @@ void orc_eam_force(int64_t n, const double* x, const double* y, const double* z,
   }
 }
 
+/* Force-matching + energy loss of lj_compute_force and its gradient with
+ * respect to (epsilon, sigma):
+ *   L = wF sum_i |F_i - F*_i|^2 + wE sum_i (E_i - E*_i)^2,
+ *   F_i = sum_j g(r) d_ij with g = (de/dr)/r, d_ij = r_j - r_i,
+ *   E_i = 1/2 sum_j (e(r) - e(rc)),
+ * so dL/dtheta = sum_i 2wF (F_i - F*_i) . sum_j dg/dtheta d_ij
+ *                + 2wE (E_i - E*_i) 1/2 sum_j (de/dtheta - de(rc)/dtheta),
+ * with de/deps = e/eps, de/dsigma = 4 eps (12 s^12 - 6 s^6)/sigma, s = sigma/r
+ * (lennard_jones.h L41-50).  Forces and energies are recomputed here. */
+double orc_lj_loss_grad(int64_t n, const double* x, const double* y, const double* z, const int64_t* off,
+                        const int32_t* nbr, const int8_t* img, const double L[3], const orc_lj_params* p,
+                        const double* fxt, const double* fyt, const double* fzt, const double* et, double wF,
+                        double wE, double grad[2]) {
+  const double eps = p->epsilon, sig = p->sigma, rc2 = p->rcut * p->rcut;
+  const double ecut = orc_lj_energy_cut(eps, sig, p->rcut);
+  const double sc = sig / p->rcut, sc6 = sc * sc * sc * sc * sc * sc, sc12 = sc6 * sc6;
+  const double decut_deps = ecut / eps, decut_dsig = 4. * eps * (12. * sc12 - 6. * sc6) / sig;
+  double loss = 0., ge = 0., gs = 0.;
+#pragma omp parallel for schedule(static) reduction(+ : loss, ge, gs)
+  for (int64_t i = 0; i < n; ++i) {
+    double F[3] = {0., 0., 0.}, E = 0.;
+    for (int64_t k = off[i]; k < off[i + 1]; ++k) {
+      const int nn[3] = {img[3 * k], img[3 * k + 1], img[3 * k + 2]};
+      double dx, dy, dz;
+      const double d2 = pair_d2(x, y, z, i, nbr[k], nn, L, &dx, &dy, &dz);
+      if (!(d2 <= rc2)) continue;
+      const double r = sqrt(d2);
+      double e, de;
+      orc_lj_pair(eps, sig, r, &e, &de);
+      const double g = de / r;
+      F[0] += g * dx; F[1] += g * dy; F[2] += g * dz;
+      E += .5 * (e - ecut);
+    }
+    const double dF[3] = {F[0] - fxt[i], F[1] - fyt[i], F[2] - fzt[i]};
+    const double dE = E - et[i];
+    loss += wF * (dF[0] * dF[0] + dF[1] * dF[1] + dF[2] * dF[2]) + wE * dE * dE;
+    double gi_e = 0., gi_s = 0.;
+    for (int64_t k = off[i]; k < off[i + 1]; ++k) {
+      const int nn[3] = {img[3 * k], img[3 * k + 1], img[3 * k + 2]};
+      double dx, dy, dz;
+      const double d2 = pair_d2(x, y, z, i, nbr[k], nn, L, &dx, &dy, &dz);
+      if (!(d2 <= rc2)) continue;
+      const double r = sqrt(d2);
+      const double s = sig / r, s2 = s * s, s6 = s2 * s2 * s2, s12 = s6 * s6;
+      const double e = 4. * eps * (s12 - s6);
+      const double g = -24. * eps * (2. * s12 - s6) / d2;             /* (de/dr)/r */
+      const double dg_deps = g / eps;
+      const double dg_dsig = -24. * eps * (24. * s12 - 6. * s6) / (d2 * sig);
+      const double proj = dF[0] * dx + dF[1] * dy + dF[2] * dz;
+      gi_e += 2. * wF * proj * dg_deps + wE * dE * (e / eps - decut_deps);
+      gi_s += 2. * wF * proj * dg_dsig + wE * dE * (4. * eps * (12. * s12 - 6. * s6) / sig - decut_dsig);
+    }
+    ge += gi_e;
+    gs += gi_s;
+  }
+  grad[0] = ge;
+  grad[1] = gs;
+  return loss;
+}
+
 /* ------------------------------------------------------------------------ */
 /* johnson_force: analytic single-element EAM                               */
 /* ------------------------------------------------------------------------ */

@@ -165,6 +165,13 @@ void orc_ej_forces(int64_t n, const double* x, const double* y, const double* z,
                    const int32_t* nbr, const int8_t* img, const double L[3], const orc_johnson_params* p,
                    double rcut, double* fp, double* fx, double* fy, double* fz, double* ep, double* vir);
 
+/* lj_compute_force force-matching + energy loss and d(loss)/d(epsilon, sigma)
+ * (targets: forces and per-atom energies); returns the loss. */
+double orc_lj_loss_grad(int64_t n, const double* x, const double* y, const double* z, const int64_t* off,
+                        const int32_t* nbr, const int8_t* img, const double L[3], const orc_lj_params* p,
+                        const double* fxt, const double* fyt, const double* fzt, const double* et, double wF,
+                        double wE, double grad[2]);
+
 int orc_num_threads(void);
 
 #ifdef __cplusplus

@@ -118,6 +118,8 @@ def lib():
         L.orc_run_minimize.restype = i32
         L.orc_run_minimize.argtypes = [i64] + [vp] * 12 + [i32, vp, dbl, dbl, dbl, i32, i32]
         L.orc_last_list_builds.restype = i64
+        L.orc_lj_loss_grad.restype = dbl
+        L.orc_lj_loss_grad.argtypes = [i64] + [vp] * 7 + [vp] + [vp] * 4 + [dbl, dbl, vp]
         L.orc_ej_forces.restype = None
         L.orc_ej_forces.argtypes = [i64] + [vp] * 7 + [vp, dbl] + [vp] * 6
         for f in ("orc_ej_phi", "orc_ej_rho", "orc_ej_embed"):
@@ -234,6 +236,20 @@ class _Multi:
         self.eps, self.sig, self.rc = _f64(eps), _f64(sig), _f64(rc)
         self.s = LJMultiParams(self.eps.shape[0], 0, _p(self.eps), _p(self.sig), _p(self.rc),
                                float(rcut_max))
+
+
+def lj_loss_grad(x, y, z, nl, L, eps, sigma, rcut, ft, et, wF, wE):
+    """lj_compute_force force-matching + energy loss and its gradient with
+    respect to (epsilon, sigma); ft (n, 3) target forces, et (n,) energies."""
+    n = len(x)
+    prm = LJParams(eps, sigma, rcut)
+    ft = np.ascontiguousarray(ft, dtype=np.float64)
+    fx, fy, fz = (np.ascontiguousarray(ft[:, d]) for d in range(3))
+    g = np.zeros(2)
+    loss = lib().orc_lj_loss_grad(n, _p(x), _p(y), _p(z), _p(nl.off), _p(nl.nbr), _p(nl.img), _p(_f64(L)),
+                                  C.addressof(prm), _p(fx), _p(fy), _p(fz), _p(_f64(et)), float(wF), float(wE),
+                                  _p(g))
+    return loss, g
 
 
 def ej_function(name, pot, arg):

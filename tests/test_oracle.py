@@ -322,3 +322,26 @@ def test_johnson_forces_are_energy_gradient(oracle):
             args_m = [m if q == d else (s.x, s.y, s.z)[q] for q in range(3)]
             fd = -(energy_forces(*args_p)[0] - energy_forces(*args_m)[0]) / (2 * h)
             assert abs(fd - F[i, d]) < 1e-6 * np.abs(F).max(), (i, d, fd, F[i, d])
+
+
+def test_lj_loss_gradient_matches_finite_differences(oracle):
+    """d(loss)/d(epsilon, sigma) of the force-matching + energy loss against
+    central differences of the oracle's own loss (relative 1e-6)."""
+    s = S.lj_fcc(ncell=4, density=0.8442, T=1.0, seed=9)
+    rng = np.random.default_rng(9)
+    x, y, z = (a + rng.normal(0.0, 0.05, s.n) for a in (s.x, s.y, s.z))
+    oracle.wrap(x, y, z, s.lo, s.hi)
+    nl = oracle.build_neighbors(x, y, z, s.id, s.lo, s.hi, 2.8)
+    fx, fy, fz, ep, _ = oracle.lj_force(x, y, z, nl, s.L, 1.1, 0.97, 2.5)
+    ft, et = np.stack([fx, fy, fz], 1), ep
+    wF, wE = 1.0 / s.n, 0.1 / s.n
+    loss, g = oracle.lj_loss_grad(x, y, z, nl, s.L, 1.0, 1.0, 2.5, ft, et, wF, wE)
+    assert loss > 0
+    h = 1e-6
+    for k in range(2):
+        p, m = [1.0, 1.0], [1.0, 1.0]
+        p[k] += h
+        m[k] -= h
+        fd = (oracle.lj_loss_grad(x, y, z, nl, s.L, p[0], p[1], 2.5, ft, et, wF, wE)[0]
+              - oracle.lj_loss_grad(x, y, z, nl, s.L, m[0], m[1], 2.5, ft, et, wF, wE)[0]) / (2 * h)
+        assert abs(fd - g[k]) < 1e-6 * max(abs(fd), 1e-12), (k, fd, g[k])
