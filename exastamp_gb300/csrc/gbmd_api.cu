@@ -875,6 +875,9 @@ int gbmd_get_density_block(const gbmd_context* c, int* block) {
 
 int gbmd_set_neighbor_staging(gbmd_context* c, int enable) {
   if (!c) return GBMD_ERR_INVALID;
+  cudaSetDevice(c->device);
+  if (enable && configure_staged_kernels() != GBMD_OK)
+    return set_error(c, GBMD_ERR_CUDA, "cannot raise the shared-memory limit of the staged kernels");
   if (c->staged != (enable != 0)) {
     c->staged = enable != 0;
     drop_graph(c);

@@ -608,6 +608,27 @@ static void launch_mixed_TV(gbmd_context* c, const PairArgs& A, int part) {
 // cells along x; K gives about 0.8 * block atoms per block, and the staged
 // capacity is 1.4 times the mean neighbourhood of (K+2) x 3 x 3 cells (a
 // denser block falls back to global gathers).
+// Raise the dynamic shared-memory limit of the staged kernels once, outside
+// any stream capture (the attribute is per kernel, not per launch).
+static constexpr int STAGED_MAX_SMEM = 200 * 1024;
+
+int configure_staged_kernels() {
+  cudaError_t e = cudaSuccess;
+  auto set = [&](const void* f) {
+    const cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, STAGED_MAX_SMEM);
+    if (r != cudaSuccess) e = r;
+  };
+  set((const void*)k_lj_staged<false, false>);
+  set((const void*)k_lj_staged<true, false>);
+  set((const void*)k_lj_staged<false, true>);
+  set((const void*)k_lj_staged<true, true>);
+  set((const void*)k_eam_rho_staged<false>);
+  set((const void*)k_eam_rho_staged<true>);
+  set((const void*)k_eam_force_staged<false>);
+  set((const void*)k_eam_force_staged<true>);
+  return e == cudaSuccess ? GBMD_OK : GBMD_ERR_CUDA;
+}
+
 template <bool EV>
 static bool launch_staged(gbmd_context* c, const PairArgs& A, int part) {
   const bool lj = c->pot == GBMD_POT_LJ || c->pot == GBMD_POT_LJ_MULTI;
@@ -618,7 +639,7 @@ static bool launch_staged(gbmd_context* c, const PairArgs& A, int part) {
   int K = (int)(0.8 * B / (per_cell > 0.5 ? per_cell : 0.5));
   K = K < 1 ? 1 : (K > g.nc[0] ? g.nc[0] : K);
   int cap = (int)(1.4 * per_cell * 9 * (K + 2)) + 64;
-  const int max_cap = (200 * 1024) / (int)sizeof(float4);
+  const int max_cap = STAGED_MAX_SMEM / (int)sizeof(float4);
   if (cap > max_cap) cap = max_cap;
   const size_t smem = (size_t)cap * sizeof(float4);
   const dim3 grid((unsigned)((g.nc[0] + K - 1) / K), (unsigned)g.nc[1], (unsigned)g.nc[2]);
@@ -627,19 +648,13 @@ static bool launch_staged(gbmd_context* c, const PairArgs& A, int part) {
     if (part == 1) return true;
     const LJPair& q = c->lj.p[0];
     LJF P{q.sig2f, q.eps24f, q.eps4f, q.ecutf, q.rc2lo, q.rc2hi, q.rc2, q.rc};
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_lj_staged<EV, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_lj_staged<EV, false><<<grid, B, smem, s>>>(A, P, nullptr, 1, c->lj.rcut_max2, c->cell_start, K, cap);
   } else if (c->pot == GBMD_POT_LJ_MULTI) {
     if (part == 1) return true;
     LJF P{};
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_lj_staged<EV, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_lj_staged<EV, true><<<grid, B, smem, s>>>(A, P, c->lj_tab_d, c->lj.ntypes, c->lj.rcut_max2, c->cell_start,
                                                  K, cap);
   } else {
-    if (smem > 48 * 1024) {
-      cudaFuncSetAttribute(k_eam_rho_staged<EV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      cudaFuncSetAttribute(k_eam_force_staged<EV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    }
     if (part != 2)
       k_eam_rho_staged<EV><<<grid, B, smem, s>>>(A, c->eam, c->fpf, c->epf, c->pfp, c->cell_start, K, cap);
     if (part != 1)

@@ -405,7 +405,7 @@ __device__ __forceinline__ int build_walk(const BuildCell& B, const float4* __re
       build_stage(B, pf, q0, stage, lane);
       __syncwarp();
       const int m = min(BUILD_CHUNK, B.total - q0);
-#pragma unroll 4
+#pragma unroll 8
       for (int t = 0; t < m; t += (G == 16 ? 2 : 1)) {
         const float4 e = stage[t + half];
         const uint32_t w = __float_as_uint(e.w);
@@ -418,16 +418,18 @@ __device__ __forceinline__ int build_walk(const BuildCell& B, const float4* __re
         // Keep d2 <= R^2 (1 + 2^-12); flag the atom when d2 >= R^2 (1 - 2^-12).
         const bool in = hv && (int)(w & GBMD_IDX_MASK) != i && d2f <= R2hi;
         unc |= in && d2f >= R2lo;
+        // the slot address is formed on every step and only the store is
+        // conditional, so the walk stays one straight-line block
         if (G == 16) {
           const int other = __shfl_xor_sync(FULL, (int)in, 16);
-          if (in) {
-            const int pos = cnt + (half ? other : 0);  // candidate 2t goes first
-            if (pos < maxnb) row[(size_t)(pos >> wsh) * stride + (pos & (W - 1))] = w;
-          }
+          const int pos = cnt + (half & other);  // candidate 2t goes first
+          uint32_t* dst = row + (size_t)(pos >> wsh) * stride + (pos & (W - 1));
+          if (in && pos < maxnb) *dst = w;
           cnt += (int)in + other;
-        } else if (in) {
-          if (cnt < maxnb) row[(size_t)(cnt >> wsh) * stride + (cnt & (W - 1))] = w;
-          ++cnt;
+        } else {
+          uint32_t* dst = row + (size_t)(cnt >> wsh) * stride + (cnt & (W - 1));
+          if (in && cnt < maxnb) *dst = w;
+          cnt += (int)in;
         }
       }
     }

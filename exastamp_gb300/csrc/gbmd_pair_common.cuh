@@ -47,6 +47,9 @@ struct PairArgs {
 
 // Mixed-precision pair kernels (gbmd_mixed.cu); part as in launch_forces.
 int launch_mixed(gbmd_context* c, const PairArgs& A, int part, bool ev);
+// Raises the shared-memory limit of the staged pair kernels (gbmd_mixed.cu);
+// called when staging is switched on, never during a stream capture.
+int configure_staged_kernels();
 // Pair-kernel arguments for the context's current buffers (gbmd_forces.cu).
 PairArgs make_args(gbmd_context* c, const ForceFlags& f);
 // lj_compute_force parameter adjoint (gbmd_adjoint_lj.cu): targets are

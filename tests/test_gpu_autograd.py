@@ -46,7 +46,10 @@ def test_lj_autograd_gradient(gpu, oracle, mixed):
             fd[k] = (float(LJLoss.apply(pp, ctx, 2.5, Ft, Et, wF, wE))
                      - float(LJLoss.apply(pm, ctx, 2.5, Ft, Et, wF, wE))) / (2 * h)
     loss_ref, g_ref = oracle.lj_loss_grad(x, y, z, nl, s.L, 1.0, 1.0, 2.5, Ft, Et, wF, wE)
-    assert np.all(np.abs(g - fd) < 1e-4 * np.abs(fd)), (g, fd)
+    # FP64: 1e-4 (the adjoint target); mixed: the forward's FP32 forces put
+    # ~1e-7 relative noise on the loss, i.e. ~1e-4 on differences over h = 1e-4
+    fd_tol = 1e-4 if not mixed else 1e-3
+    assert np.all(np.abs(g - fd) < fd_tol * np.abs(fd)), (g, fd)
     tol = 1e-9 if not mixed else 1e-4
     assert np.all(np.abs(g - g_ref) < tol * np.abs(g_ref)), (g, g_ref)
     assert abs(float(loss) - loss_ref) < (1e-9 if not mixed else 1e-4) * loss_ref
