@@ -521,7 +521,18 @@ def main():
         wall = time.perf_counter() - t0
         mse = ev0.elapsed_time(ev1)
         mse = dist_max(max(mse, wall * 1e3), ws)
+        # split of one step: upload alone, download alone (host wall clock)
+        keys9 = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az")
+        t0 = time.perf_counter()
+        for _ in range(3):
+            ctx._chk(L.gbmd_upload_state(ctx.h, *[ptr(k) for k in keys9]))
+        up_ms = (time.perf_counter() - t0) * 1e3 / 3
+        t0 = time.perf_counter()
+        for _ in range(3):
+            ctx._chk(L.gbmd_download(ctx.h, *[ptr(k) for k in keys9], None, None))
+        down_ms = (time.perf_counter() - t0) * 1e3 / 3
         out["e2e"] = {"value": n * args.e2e_steps * ws / (mse * 1e-3), "unit": "atom-timesteps/s",
+                      "upload_ms": up_ms, "download_ms": down_ms,
                       "h2d_bytes_per_step": 72 * n, "d2h_bytes_per_step": 72 * n, "steps": args.e2e_steps,
                       "ms_per_step": mse / args.e2e_steps,
                       "path": "gbmd_upload_state(pinned r,v,a; skin/2 displacement test) + gbmd_run_nve(1) + "
