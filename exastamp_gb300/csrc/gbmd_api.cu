@@ -1227,6 +1227,19 @@ int gbmd_profile_step(gbmd_context* c, int reps, double ms[5]) {
   GBMD_CUDA(c, cudaEventCreate(&e0));
   GBMD_CUDA(c, cudaEventCreate(&e1));
   for (int k = 0; k < 5; ++k) {
+    // one untimed pass first (a kernel's first launch also loads its module);
+    // the fused pair kernel swaps the position buffers, so it runs twice
+    for (int w = 0; w < (k == 2 ? 2 : 1) && rc == GBMD_OK; ++w) {
+      ForceFlags f;
+      f.sp.dt = f.sp.dth = f.sp.dt2h = 0.0;
+      switch (k) {
+        case 0: rc = do_rebuild(c, false); break;
+        case 1: f.part = 1; rc = launch_forces(c, f); break;
+        case 2: f.part = 2; f.fuse = FUSE_PUSH2_PUSH1; rc = launch_forces(c, f); break;
+        case 3: launch_first_half(c, 0.0); break;
+        case 4: launch_thermo(c, true); break;
+      }
+    }
     float acc = 0.f;
     for (int r = 0; r < reps && rc == GBMD_OK; ++r) {
       cudaEventRecord(e0, c->stream);

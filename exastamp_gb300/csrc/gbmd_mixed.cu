@@ -302,7 +302,7 @@ __device__ __forceinline__ void lj_atom(const PairArgs& A, const LJF& P, const L
 }
 
 template <int T, int V, bool EV, bool MULTI>
-__global__ void __launch_bounds__(256) k_lj_mixed(PairArgs A, LJF P, const LJPair* __restrict__ tab, int ntypes,
+__global__ void __launch_bounds__(256, 4) k_lj_mixed(PairArgs A, LJF P, const LJPair* __restrict__ tab, int ntypes,
                                                   double rcmax2) {
   __shared__ LJTabSmem t;
   if (MULTI) lj_load_table(t, tab, ntypes);
@@ -551,7 +551,7 @@ __device__ __forceinline__ void eam_force_atom(const PairArgs& A, const EamDev& 
 }
 
 template <int T, int V, bool EV, bool SINGLE>
-__global__ void __launch_bounds__(256) k_eam_force_mixed(PairArgs A, EamDev E, const float* __restrict__ fpf,
+__global__ void __launch_bounds__(256, 4) k_eam_force_mixed(PairArgs A, EamDev E, const float* __restrict__ fpf,
                                                          const float* __restrict__ epf,
                                                          const float4* __restrict__ pfp) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
