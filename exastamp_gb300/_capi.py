@@ -87,6 +87,7 @@ def lib(path: str = LIB_PATH):
             "gbmd_push_f_v": ([vp, dbl, dbl], i32),
             "gbmd_push_min": ([vp, dbl, dbl, dbl], i32),
             "gbmd_run_nve": ([vp, i32, dbl, i32, i32, vp, i32], i32),
+            "gbmd_run_nve_host": ([vp, i32, dbl, i32] + [vp] * 9, i32),
             "gbmd_run_minimize": ([vp, i32, dbl, dbl, i32], i32),
             "gbmd_set_eam_johnson": ([vp, vp, dbl], i32),
             "gbmd_lj_loss_grad": ([vp, vp, vp, vp, vp, dbl, dbl, P(dbl), vp], i32),
@@ -294,6 +295,17 @@ class Context:
         self._chk(self._L.gbmd_run_nve(self.h, int(nsteps), float(dt), int(rebuild_every), int(thermo_every),
                                        _p(out) if rows else None, 1 if use_graph else 0))
         return out[:rows] if rows else None
+
+    def run_nve_host(self, state, nsteps, dt, rebuild_every=10):
+        """gbmd_run_nve_host on a dict of 9 contiguous float64 arrays (x, y, z,
+        vx, vy, vz, ax, ay, az), updated in place."""
+        keys = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az")
+        for k in keys:
+            a = state[k]
+            if a.dtype != np.float64 or not a.flags.c_contiguous or len(a) != self.n:
+                raise ValueError("%s: need a contiguous float64 array of n atoms" % k)
+        self._chk(self._L.gbmd_run_nve_host(self.h, int(nsteps), float(dt), int(rebuild_every),
+                                            *[state[k].ctypes.data for k in keys]))
 
     def run_minimize(self, nsteps, dt, tolF=0.0, rebuild_every=10):
         self._chk(self._L.gbmd_run_minimize(self.h, int(nsteps), float(dt), float(tolF), int(rebuild_every)))

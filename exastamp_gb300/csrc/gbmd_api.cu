@@ -50,7 +50,8 @@ static void free_atoms(gbmd_context* c) {
   cudaFree(c->ep); cudaFree(c->vir); cudaFree(c->cellpack); cudaFree(c->cell_of);
   cudaFree(c->order); cudaFree(c->src); cudaFree(c->fpf); cudaFree(c->fpd); cudaFree(c->epf);
   cudaFree(c->pfp);
-  cudaFree(c->stage); cudaFree(c->rref); cudaFree(c->nnb); cudaFree(c->d_part);
+  cudaFree(c->stage); cudaFree(c->rref); cudaFree(c->nnb); cudaFree(c->d_part); cudaFree(c->stage_r);
+  c->stage_r = nullptr;
   c->ep = c->vir = nullptr;
   c->cellpack = c->cell_of = c->order = c->src = nullptr;
   c->fpf = c->epf = nullptr;
@@ -226,7 +227,7 @@ static inline unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / 
 // stage[k * cap], spread over the context's stream and two copy streams so
 // several copy engines run at once; ordered after the work already on the
 // stream and before the work issued after this call.
-static int staged_copies(gbmd_context* c, double* const* host, int count, bool to_device) {
+static int ensure_copy_streams(gbmd_context* c) {
   if (!c->copy_stream[0]) {
     for (int k = 0; k < 2; ++k) {
       GBMD_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream[k], cudaStreamNonBlocking));
@@ -234,6 +235,12 @@ static int staged_copies(gbmd_context* c, double* const* host, int count, bool t
     }
     GBMD_CUDA(c, cudaEventCreateWithFlags(&c->copy_fork, cudaEventDisableTiming));
   }
+  return GBMD_OK;
+}
+
+static int staged_copies(gbmd_context* c, double* const* host, int count, bool to_device) {
+  int rc = ensure_copy_streams(c);
+  if (rc) return rc;
   const size_t bytes = sizeof(double) * (size_t)c->n;
   GBMD_CUDA(c, cudaEventRecord(c->copy_fork, c->stream));
   for (int k = 0; k < 2; ++k) GBMD_CUDA(c, cudaStreamWaitEvent(c->copy_stream[k], c->copy_fork, 0));
@@ -247,6 +254,30 @@ static int staged_copies(gbmd_context* c, double* const* host, int count, bool t
     GBMD_CUDA(c, cudaEventRecord(c->copy_join[k], c->copy_stream[k]));
     GBMD_CUDA(c, cudaStreamWaitEvent(c->stream, c->copy_join[k], 0));
   }
+  return GBMD_OK;
+}
+
+// Positions of the last step of gbmd_run_nve_host, final once its first half
+// and any rebuild (which wraps them) have run: gathered into caller order on
+// the main stream, then copied to the caller's arrays on a copy stream while
+// the force pass runs; copy_join[0] marks the end.
+static int download_r_async(gbmd_context* c) {
+  const int64_t n = c->n;
+  if (!c->stage_r) GBMD_CUDA(c, cudaMalloc(&c->stage_r, sizeof(double) * 3 * c->cap));
+  int rc = ensure_copy_streams(c);
+  if (rc) return rc;
+  Arrays9 src{};
+  src.a[0] = c->X();
+  src.a[1] = c->Y();
+  src.a[2] = c->Z();
+  k_to_user_multi<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->cap, src, c->USER(), c->stage_r, 3);
+  GBMD_CUDA(c, cudaEventRecord(c->copy_fork, c->stream));
+  GBMD_CUDA(c, cudaStreamWaitEvent(c->copy_stream[0], c->copy_fork, 0));
+  c->r_copy_pending = true;
+  for (int k = 0; k < 3; ++k)
+    GBMD_CUDA(c, cudaMemcpyAsync(c->host_r_out[k], c->stage_r + (size_t)k * c->cap, sizeof(double) * n,
+                                 cudaMemcpyDeviceToHost, c->copy_stream[0]));
+  GBMD_CUDA(c, cudaEventRecord(c->copy_join[0], c->copy_stream[0]));
   return GBMD_OK;
 }
 
@@ -1019,6 +1050,8 @@ static int one_step(gbmd_context* c, double dt, const StepPlan& p, bool check, d
   int rc;
   if (p.rebuild && (rc = do_rebuild(c, check))) return rc;
   if (p.trigger && (rc = rebuild_if_displaced(c))) return rc;
+  // gbmd_run_nve_host: the positions are final (and wrapped by a rebuild) here
+  if (p.last && c->host_r_out[0] && (rc = download_r_async(c))) return rc;
   ForceFlags f;
   f.energy = p.thermo;
   f.virial = p.thermo;
@@ -1152,6 +1185,28 @@ int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int 
   c->forces_valid_step = c->step;
   if (trigger && (rc = collect_device_rebuilds(c))) return rc;
   return check_device_errors(c);
+}
+
+int gbmd_run_nve_host(gbmd_context* c, int nsteps, double dt, int rebuild_every, double* rx, double* ry, double* rz,
+                      double* vx, double* vy, double* vz, double* ax, double* ay, double* az) {
+  if (!c || nsteps < 1 || !rx || !ry || !rz || !vx || !vy || !vz || !ax || !ay || !az) return GBMD_ERR_INVALID;
+  int rc = gbmd_upload_state(c, rx, ry, rz, vx, vy, vz, ax, ay, az);
+  if (rc) return rc;
+  if (c->n == 0) return GBMD_OK;
+  c->host_r_out[0] = rx;
+  c->host_r_out[1] = ry;
+  c->host_r_out[2] = rz;
+  c->r_copy_pending = false;
+  rc = gbmd_run_nve(c, nsteps, dt, rebuild_every, 0, nullptr, 0);
+  c->host_r_out[0] = c->host_r_out[1] = c->host_r_out[2] = nullptr;
+  if (rc == GBMD_OK) rc = gbmd_download(c, nullptr, nullptr, nullptr, vx, vy, vz, ax, ay, az, nullptr, nullptr);
+  if (c->r_copy_pending) {
+    // the caller's r arrays are written until this copy ends, error or not
+    c->r_copy_pending = false;
+    const cudaError_t e = cudaEventSynchronize(c->copy_join[0]);
+    if (rc == GBMD_OK && e != cudaSuccess) rc = check_cuda(c, e, "position copy");
+  }
+  return rc;
 }
 
 int gbmd_run_minimize(gbmd_context* c, int nsteps, double dt, double tolF, int rebuild_every) {

@@ -100,6 +100,9 @@ struct gbmd_context {
   cudaStream_t stream = nullptr;
   // copy streams for host<->device staging (created lazily), forked from and
   // joined back into `stream` with events
+  double* stage_r = nullptr;    // 3 x cap: r in caller order, copied out during a force pass
+  double* host_r_out[3] = {nullptr, nullptr, nullptr};  // gbmd_run_nve_host's r arrays
+  bool r_copy_pending = false;  // copy_join[0] marks the end of that copy
   cudaStream_t copy_stream[2] = {nullptr, nullptr};
   cudaEvent_t copy_fork = nullptr, copy_join[2] = {nullptr, nullptr};
   bool own_stream = false;

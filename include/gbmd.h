@@ -215,6 +215,14 @@ int gbmd_push_min(gbmd_context* ctx, double dt, double dt_scale, double tolF);
  * thermo); the remaining steps are launched one by one. */
 int gbmd_run_nve(gbmd_context* ctx, int nsteps, double dt, int rebuild_every, int thermo_every,
                  double* thermo_out, int use_graph);
+/* verlet_nve on a state held in host arrays (the caller's grid, in upload
+ * order): gbmd_upload_state(r, v, a) (the skin/2 displacement test decides
+ * a rebuild), gbmd_run_nve(nsteps, no thermo, no graph), then r, v, a are
+ * written back.  The positions of the last step are final after its first
+ * half and go back to the host while its force pass runs; v and a follow.
+ * Page-locked arrays are fastest.  Returns once every array is written. */
+int gbmd_run_nve_host(gbmd_context* ctx, int nsteps, double dt, int rebuild_every, double* rx, double* ry,
+                      double* rz, double* vx, double* vy, double* vz, double* ax, double* ay, double* az);
 /* Minimiser: nsteps of compute forces + push_min (r += a dt^2/2, clipped);
  * rebuild_every as gbmd_run_nve. */
 int gbmd_run_minimize(gbmd_context* ctx, int nsteps, double dt, double tolF, int rebuild_every);

@@ -433,3 +433,29 @@ def test_pinned_host_arrays_round_trip(gpu):
     for k in keys:
         assert np.array_equal(out[k], pinned[k]), k
         assert np.array_equal(back[k], pinned[k]), k
+
+
+@pytest.mark.parametrize("pinned,nsteps,R", [(True, 1, 10), (True, 5, 1), (False, 3, 2)])
+def test_run_nve_host_matches_separate_calls(gpu, pinned, nsteps, R):
+    """gbmd_run_nve_host (positions copied back during the last force pass)
+    gives the state of upload_state + run_nve + download bit for bit, also
+    when the last step rebuilds the list (R = 1) and for pageable arrays."""
+    torch = pytest.importorskip("torch")
+    s = _jitter(S.lj_fcc(ncell=7, seed=33), 0.05, 33)
+    keys = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az")
+    # two contexts with the same history, so the same rebuild decisions
+    with gpu_ctx(gpu, s, LJ, 0.3, mixed=True) as ctx:
+        ctx.run_nve(7, 0.005, rebuild_every=5)
+        start = ctx.download(keys)
+        ctx.upload_state(*(start[k] for k in keys))
+        ctx.run_nve(nsteps, 0.005, rebuild_every=R)
+        ref = ctx.download(keys)
+    with gpu_ctx(gpu, s, LJ, 0.3, mixed=True) as ctx:
+        ctx.run_nve(7, 0.005, rebuild_every=5)
+        st = {}
+        for k in keys:
+            st[k] = torch.empty(s.n, dtype=torch.float64, pin_memory=True).numpy() if pinned else np.empty(s.n)
+            st[k][:] = start[k]
+        ctx.run_nve_host(st, nsteps, 0.005, rebuild_every=R)
+    for k in keys:
+        assert np.array_equal(st[k], ref[k]), k
