@@ -7,11 +7,14 @@
 // Everything a replica needs lives in shared memory: its cell-sorted FP32
 // cell-relative positions, cell ranges, F'(rho), the loss gradients with
 // respect to its per-atom forces and energies, and the adjoint
-// intermediates.  Pairs are found on the fly from the (2S+1)^3 cells around
-// each atom (S = 1 with cells >= rcut, or S = 2 with cells >= rcut/2; the
-// autotuner picks S and the block size), with the same FP32 screen + FP64
-// re-test of the ambiguous band as the main path, so the in-cutoff pair set
-// is the FP64 one.  Pair arithmetic is FP32 with compensated force and
+// intermediates.  Pairs are found once per replica from the (2S+1)^3 cells
+// around each atom (S = 1 with cells >= rcut, or S = 2 with cells >= rcut/2;
+// the autotuner picks S and the block size), with the same FP32 screen +
+// FP64 re-test of the ambiguous band as the main path, so the in-cutoff pair
+// set is the FP64 one; they go to a pair list in the block's own global
+// scratch (128 entries per atom, slot-major), which the density, force and
+// adjoint passes read.  A replica with a fuller atom walks the cells in
+// every pass instead, with the same order and arithmetic.  Pair arithmetic is FP32 with compensated force and
 // density sums; per-replica sums (energy, virial, loss, gradient) are FP64
 // and written to the replica's own row, so results do not depend on which
 // block ran which replica.
@@ -37,6 +40,8 @@ namespace {
 
 constexpr int BMAX_ATOMS = 2048;
 constexpr int BMAX_CELLS = 1024;
+constexpr int NBL_MAX = 128;                          // pair-list entries per atom
+constexpr size_t NBL_REGION = (size_t)BMAX_ATOMS * NBL_MAX;  // entries per block
 constexpr int BMAX_PARAMS = 9;
 constexpr int REP_ROW = 20;  // epot, virial[9], loss, grad[9]
 
@@ -65,6 +70,7 @@ struct BatchArgs {
   double wF, wE;
   const float4 *dz2r4, *drhor4, *dfrho4;  // [k][knot] for the listed parameters
   int nz2, nrh, nfr;
+  uint32_t* nbl;  // NBL_REGION entries per block: the current replica's pair list
   int pz2[BMAX_PARAMS], prh[BMAX_PARAMS], pfr[BMAX_PARAMS];
 };
 
@@ -79,8 +85,10 @@ struct SmemLayout {
   float eemb[BMAX_ATOMS];   // F(rho) by slot
   float rho[BMAX_ATOMS];    // rho by slot
   float G[BMAX_ATOMS];      // adjoint G by slot
+  int nnb[BMAX_ATOMS];      // pair-list length by slot
   double red[32][REP_ROW];  // block reduction
   int rep;
+  int list_ok;              // every atom's pairs fit in the list
 };
 
 struct RepGeom {
@@ -129,7 +137,18 @@ __device__ __forceinline__ int knot(float t, int nmax, float& q) {
   return m;
 }
 
-// Visit every in-cutoff neighbour of slot s: fn(k, dx, dy, dz, d2).
+// FP32 separation of a candidate (position shifted by its cell offset) and
+// its square: the one expression every pass and the list build use.
+__device__ __forceinline__ float pair_d2(const float4& pi, const float4& pj, float sx, float sy, float sz,
+                                         float& ddx, float& ddy, float& ddz) {
+  ddx = (pj.x - pi.x) + sx;
+  ddy = (pj.y - pi.y) + sy;
+  ddz = (pj.z - pi.z) + sz;
+  return fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz));
+}
+
+// Visit every in-cutoff neighbour of slot s from the cells around it:
+// fn(k, dx, dy, dz, d2, code), code = the cell offset (dx+S) | (dy+S) << 3 | (dz+S) << 6.
 template <class Fn>
 __device__ __forceinline__ void for_pairs(const BatchArgs& A, const RepGeom& g, const SmemLayout& sm, int s, Fn fn) {
   const int ai = sm.order[s];
@@ -146,17 +165,64 @@ __device__ __forceinline__ void for_pairs(const BatchArgs& A, const RepGeom& g, 
         const int cj = (wz * g.nc[1] + wy) * g.nc[0] + wx;
         const float sx = (float)dx * g.hf[0], sy = (float)dy * g.hf[1], sz = (float)dz * g.hf[2];
         const bool self_cell = (dx | dy | dz) == 0;
+        const uint32_t code = (uint32_t)(dx + S) | ((uint32_t)(dy + S) << 3) | ((uint32_t)(dz + S) << 6);
         for (int k = sm.cstart[cj]; k < sm.cstart[cj + 1]; ++k) {
           if (self_cell && k == s) continue;
           const float4 pj = sm.pos[k];
-          const float ddx = (pj.x - pi.x) + sx, ddy = (pj.y - pi.y) + sy, ddz = (pj.z - pi.z) + sz;
-          const float d2 = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz));
+          float ddx, ddy, ddz;
+          const float d2 = pair_d2(pi, pj, sx, sy, sz, ddx, ddy, ddz);
           if (d2 > A.rc2hi) continue;
           if (d2 >= A.rc2lo && !batch_exact(A, g, ai, sm.order[k], nx, ny, nz)) continue;
-          fn(k, ddx, ddy, ddz, d2);
+          fn(k, ddx, ddy, ddz, d2, code);
         }
       }
     }
+  }
+}
+
+// The same neighbours, in the same order and with the same FP32 arithmetic,
+// from the replica's pair list (entry: slot k | code << 11, slot-major).
+template <class Fn>
+__device__ __forceinline__ void for_list(const RepGeom& g, const SmemLayout& sm, const uint32_t* __restrict__ nbl,
+                                         int n, int S, int s, Fn fn) {
+  const float4 pi = sm.pos[s];
+  const int cnt = sm.nnb[s];
+  for (int q = 0; q < cnt; ++q) {
+    const uint32_t e = nbl[(size_t)q * n + s];
+    const int k = (int)(e & 2047u);
+    const int dx = (int)((e >> 11) & 7u) - S, dy = (int)((e >> 14) & 7u) - S, dz = (int)((e >> 17) & 7u) - S;
+    const float sx = (float)dx * g.hf[0], sy = (float)dy * g.hf[1], sz = (float)dz * g.hf[2];
+    const float4 pj = sm.pos[k];
+    float ddx, ddy, ddz;
+    const float d2 = pair_d2(pi, pj, sx, sy, sz, ddx, ddy, ddz);
+    fn(k, ddx, ddy, ddz, d2);
+  }
+}
+
+// fn(k, dx, dy, dz, d2) over the neighbours of slot s: from the list when
+// every atom's pairs fit in it, else from the cells.
+template <class Fn>
+__device__ __forceinline__ void visit(const BatchArgs& A, const RepGeom& g, const SmemLayout& sm,
+                                      const uint32_t* nbl, int n, int s, Fn fn) {
+  if (sm.list_ok)
+    for_list(g, sm, nbl, n, A.S, s, fn);
+  else
+    for_pairs(A, g, sm, s, [&](int k, float dx, float dy, float dz, float d2, uint32_t) { fn(k, dx, dy, dz, d2); });
+}
+
+// The replica's pair list, one thread per atom walking the cells as
+// for_pairs does (same FP32 screen and FP64 band re-test, same order).  A
+// warp-per-cell walk with shared-memory broadcasts measured slower here: a
+// replica of a few hundred atoms has too few cells to keep 16 warps busy.
+__device__ void build_list(const BatchArgs& A, const RepGeom& g, SmemLayout& sm, uint32_t* __restrict__ nbl, int n) {
+  for (int s = threadIdx.x; s < n; s += blockDim.x) {
+    int cnt = 0;
+    for_pairs(A, g, sm, s, [&](int k, float, float, float, float, uint32_t code) {
+      if (cnt < NBL_MAX) nbl[(size_t)cnt * n + s] = (uint32_t)k | (code << 11);
+      ++cnt;
+    });
+    sm.nnb[s] = cnt;
+    if (cnt > NBL_MAX) sm.list_ok = 0;
   }
 }
 
@@ -177,7 +243,7 @@ __device__ void block_reduce_row(SmemLayout& sm, double* v, int nv, double* out)
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(512) k_batch(BatchArgs A) {
+__global__ void __launch_bounds__(512, 1) k_batch(BatchArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemLayout& sm = *reinterpret_cast<SmemLayout*>(smem_raw);
   const int t = threadIdx.x, B = blockDim.x;
@@ -291,11 +357,17 @@ __global__ void __launch_bounds__(512) k_batch(BatchArgs A) {
       }
       sm.pos[s] = make_float4(lp[0], lp[1], lp[2], __int_as_float(a));
     }
+    if (t == 0) sm.list_ok = 1;
+    __syncthreads();
+    // ---- pair list: one walk over the cells (FP32 screen, FP64 band
+    // re-test), then every pass below reads the list
+    uint32_t* nbl = A.nbl + (A.single >= 0 ? (size_t)0 : (size_t)blockIdx.x * NBL_REGION);
+    build_list(A, g, sm, nbl, n);
     __syncthreads();
     // ---- density + embedding
     for (int s = t; s < n; s += B) {
       float acc = 0.f, comp = 0.f;
-      for_pairs(A, g, sm, s, [&](int k, float dx, float dy, float dz, float d2) {
+      visit(A, g, sm, nbl, n, s, [&](int k, float dx, float dy, float dz, float d2) {
         const float rr = d2 * rsqrtf(d2);
         float q;
         const int m = knot(fmaf(rr, A.rdr, 1.f), A.nr - 1, q);
@@ -322,7 +394,7 @@ __global__ void __launch_bounds__(512) k_batch(BatchArgs A) {
       float fx = 0.f, fy = 0.f, fz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f, ee = 0.f, ce = 0.f;
       float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       const float fpi = sm.fp[s];
-      for_pairs(A, g, sm, s, [&](int k, float dx, float dy, float dz, float d2) {
+      visit(A, g, sm, nbl, n, s, [&](int k, float dx, float dy, float dz, float d2) {
         const float rs = rsqrtf(d2), rr = d2 * rs;
         float q;
         const int m = knot(fmaf(rr, A.rdr, 1.f), A.nr - 1, q);
@@ -372,7 +444,7 @@ __global__ void __launch_bounds__(512) k_batch(BatchArgs A) {
         const float4 gi = sm.gfe[s];
         const float fpi = sm.fp[s];
         float Gs = 0.f;
-        for_pairs(A, g, sm, s, [&](int k, float dx, float dy, float dz, float d2) {
+        visit(A, g, sm, nbl, n, s, [&](int k, float dx, float dy, float dz, float d2) {
           const float rs = rsqrtf(d2), rr = d2 * rs;
           float q;
           const int m = knot(fmaf(rr, A.rdr, 1.f), A.nr - 1, q);
@@ -416,7 +488,7 @@ __global__ void __launch_bounds__(512) k_batch(BatchArgs A) {
           const float dfp = sdq(dc, q) * A.rdrho;
           acc_rep[11 + A.pfr[p]] += (double)fmaf(gi.w, sval(dc, q) + (over ? dfp * (R - A.rhomax) : 0.f), Gs * dfp);
         }
-        for_pairs(A, g, sm, s, [&](int k, float dx, float dy, float dz, float d2) {
+        visit(A, g, sm, nbl, n, s, [&](int k, float dx, float dy, float dz, float d2) {
           const float rr = d2 * rsqrtf(d2);
           float qq;
           const int mm = knot(fmaf(rr, A.rdr, 1.f), A.nr - 1, qq);
@@ -452,6 +524,8 @@ struct gbmd_batch {
   BatchArgs a{};
   bool have_pot = false, have_targets = false;
   int block = 256, S = 1;
+  uint32_t* nbl = nullptr;  // pair-list scratch, NBL_REGION entries per resident block
+  size_t nbl_regions = 0;
   cudaGraphExec_t graph = nullptr;
   int graph_adjoint = -1;
 };
@@ -545,6 +619,7 @@ int gbmd_batch_destroy(gbmd_batch* b) {
   cudaFree(b->d_err);
   cudaFree(b->tab);
   cudaFree(b->dtab);
+  cudaFree(b->nbl);
   if (b->own_stream) cudaStreamDestroy(b->stream);
   delete b;
   return GBMD_OK;
@@ -710,6 +785,26 @@ int gbmd_batch_set_launch(gbmd_batch* b, int block, int stencil) {
   return GBMD_OK;
 }
 
+// blocks of the persistent launch: as many as fit on the device at once
+static int persistent_grid(gbmd_batch* b) {
+  int dev_sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, b->device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, b->block, smem_bytes());
+  return std::max(1, std::min(b->nrep, dev_sms * std::max(per_sm, 1)));
+}
+
+// pair-list scratch for `regions` blocks (allocated outside any capture)
+static int ensure_nbl(gbmd_batch* b, int regions) {
+  if ((size_t)regions <= b->nbl_regions) return GBMD_OK;
+  drop_graph(b);
+  cudaFree(b->nbl);
+  b->nbl = nullptr;
+  b->nbl_regions = 0;
+  BCUDA(b, cudaMalloc(&b->nbl, sizeof(uint32_t) * NBL_REGION * (size_t)regions));
+  b->nbl_regions = (size_t)regions;
+  return GBMD_OK;
+}
+
 static int batch_launch(gbmd_batch* b, int adjoint, int per_replica) {
   BatchArgs A = b->a;
   A.nrep = b->nrep;
@@ -726,6 +821,7 @@ static int batch_launch(gbmd_batch* b, int adjoint, int per_replica) {
   A.S = b->S;
   A.adjoint = adjoint;
   A.Ftx = b->Ftx; A.Fty = b->Fty; A.Ftz = b->Ftz; A.Et = b->Et;
+  A.nbl = b->nbl;
   const size_t smem = smem_bytes();
   if (per_replica) {
     for (int r = 0; r < b->nrep; ++r) {
@@ -733,11 +829,8 @@ static int batch_launch(gbmd_batch* b, int adjoint, int per_replica) {
       k_batch<<<1, b->block, smem, b->stream>>>(A);
     }
   } else {
-    int dev_sms = 0;
-    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, b->device);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, b->block, smem);
-    const int grid = std::max(1, std::min(b->nrep, dev_sms * std::max(per_sm, 1)));
+    const int grid = persistent_grid(b);
+    if ((size_t)grid > b->nbl_regions) return berr(b, GBMD_ERR_INVALID, "pair-list scratch not sized");
     A.single = -1;
     BCUDA(b, cudaMemsetAsync(b->queue, 0, sizeof(int), b->stream));
     k_batch<<<grid, b->block, smem, b->stream>>>(A);
@@ -751,6 +844,10 @@ int gbmd_batch_run(gbmd_batch* b, int adjoint, int per_replica, int use_graph) {
   if (adjoint && (!b->have_targets || b->a.nz2 + b->a.nrh + b->a.nfr == 0))
     return berr(b, GBMD_ERR_INVALID, "adjoint needs targets and parameter derivatives");
   cudaSetDevice(b->device);
+  {
+    const int rc = ensure_nbl(b, per_replica ? 1 : persistent_grid(b));
+    if (rc) return rc;
+  }
   if (use_graph && !per_replica) {
     if (!b->graph || b->graph_adjoint != adjoint) {
       drop_graph(b);

@@ -59,6 +59,34 @@ def test_batch_forward_matches_oracle(gpu, oracle, cu, stencil):
     assert np.sqrt(((d["vir_rep"] - V) ** 2).sum() / (V ** 2).sum()) < 1e-5
 
 
+def test_batch_dense_replica_walks_the_cells(gpu, oracle, cu):
+    """A replica compressed so far that its atoms have more pairs than the
+    per-atom list holds (128) is evaluated from the cells instead; both kinds
+    of replica in one launch match the oracle."""
+    cfg, sf = cu
+    reps = _replicas(6, seed=35)
+    pos, lo, hi = S.lattice(4, 4, 4, 2.45, S.FCC_BASIS)
+    rng = np.random.default_rng(35)
+    pos = pos + rng.normal(0.0, 0.03, pos.shape)
+    reps.insert(2, S._make(pos, lo, hi, np.zeros(len(pos)), np.array([63.546]), np.zeros_like(pos), {}))
+    tab = oracle.EamOracleTables.from_setfl(sf, 1.0, 1.0, rcut=5.0)
+    F, E, V = _oracle_forward(oracle, reps, tab)
+    x, y, z = reps[2].x.copy(), reps[2].y.copy(), reps[2].z.copy()
+    oracle.wrap(x, y, z, reps[2].lo, reps[2].hi)
+    nl = oracle.build_neighbors(x, y, z, reps[2].id, reps[2].lo, reps[2].hi, 5.0)
+    assert np.diff(nl.off).max() > 128
+    with gpu.Batch(0) as b:
+        b.set_eam_alloy(sf, 5.0)
+        b.upload(reps)
+        b.run()
+        d = b.download()
+    err = np.sqrt(((d["F"] - F) ** 2).sum() / (F ** 2).sum())
+    assert err < 1e-5, err
+    # the dense replica sums ~140 strongly repulsive pair energies per atom
+    # (+15 eV per atom) in FP32: 2e-6 relative
+    assert np.abs(d["ep"] - E).max() < 2e-6 * np.abs(E).max()
+
+
 def test_batch_launch_modes_are_identical(gpu, cu):
     cfg, sf = cu
     reps = _replicas(40, seed=32, nmax=800)
