@@ -388,8 +388,12 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs A) {
     }
     __syncthreads();
     // ---- forces, energies, virial; loss residuals
+    // per-thread sums: energy, virial, loss (static indices) and the
+    // parameter gradient by parameter slot
     double acc_rep[REP_ROW];
+    double acc_par[BMAX_PARAMS];
     for (int q = 0; q < REP_ROW; ++q) acc_rep[q] = 0.0;
+    for (int q = 0; q < BMAX_PARAMS; ++q) acc_par[q] = 0.0;
     for (int s = t; s < n; s += B) {
       float fx = 0.f, fy = 0.f, fz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f, ee = 0.f, ce = 0.f;
       float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -444,6 +448,11 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs A) {
         const float4 gi = sm.gfe[s];
         const float fpi = sm.fp[s];
         float Gs = 0.f;
+        // this atom's parameter terms, FP32 over its pairs (static indices:
+        // registers), folded into the FP64 per-thread sums once per atom
+        float gz[BMAX_PARAMS], gr[BMAX_PARAMS];
+#pragma unroll
+        for (int p = 0; p < BMAX_PARAMS; ++p) gz[p] = gr[p] = 0.f;
         visit(A, g, sm, nbl, n, s, [&](int k, float dx, float dy, float dz, float d2) {
           const float rs = rsqrtf(d2), rr = d2 * rs;
           float q;
@@ -458,16 +467,24 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs A) {
           const float wv = (0.5f * gi.w - sij * rs) * rs;  // weight of dz2
           const float wd = sij * rs * A.rdr;              // weight of dz2/dq
           const float wr = sij * (fpi + sm.fp[k]) * A.rdr; // weight of drho/dq
-          for (int p = 0; p < A.nz2; ++p) {
-            const float4 c = A.dz2r4[(size_t)p * (A.nr + 1) + m];
-            acc_rep[11 + A.pz2[p]] += (double)fmaf(wv, sval(c, q), wd * sdq(c, q));
-          }
-          for (int p = 0; p < A.nrh; ++p) {
-            const float4 c = A.drhor4[(size_t)p * (A.nr + 1) + m];
-            acc_rep[11 + A.prh[p]] += (double)(wr * sdq(c, q));
+#pragma unroll
+          for (int p = 0; p < BMAX_PARAMS; ++p) {
+            if (p < A.nz2) {
+              const float4 c = A.dz2r4[(size_t)p * (A.nr + 1) + m];
+              gz[p] += fmaf(wv, sval(c, q), wd * sdq(c, q));
+            }
+            if (p < A.nrh) {
+              const float4 c = A.drhor4[(size_t)p * (A.nr + 1) + m];
+              gr[p] = fmaf(wr, sdq(c, q), gr[p]);
+            }
           }
         });
         sm.G[s] = Gs;
+#pragma unroll
+        for (int p = 0; p < BMAX_PARAMS; ++p) {
+          if (p < A.nz2) acc_par[A.pz2[p]] += (double)gz[p];
+          if (p < A.nrh) acc_par[A.prh[p]] += (double)gr[p];
+        }
       }
       __syncthreads();
       // ---- adjoint sweep 2: embedding terms and lam_i * drho
@@ -486,18 +503,28 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs A) {
         for (int p = 0; p < A.nfr; ++p) {
           const float4 dc = A.dfrho4[(size_t)p * (A.nrho + 1) + m];
           const float dfp = sdq(dc, q) * A.rdrho;
-          acc_rep[11 + A.pfr[p]] += (double)fmaf(gi.w, sval(dc, q) + (over ? dfp * (R - A.rhomax) : 0.f), Gs * dfp);
+          acc_par[A.pfr[p]] += (double)fmaf(gi.w, sval(dc, q) + (over ? dfp * (R - A.rhomax) : 0.f), Gs * dfp);
         }
+        // lam_i * sum_j drho(r_ij): the pair sums in FP32, lam once per atom
+        float gd[BMAX_PARAMS];
+#pragma unroll
+        for (int p = 0; p < BMAX_PARAMS; ++p) gd[p] = 0.f;
         visit(A, g, sm, nbl, n, s, [&](int k, float dx, float dy, float dz, float d2) {
           const float rr = d2 * rsqrtf(d2);
           float qq;
           const int mm = knot(fmaf(rr, A.rdr, 1.f), A.nr - 1, qq);
-          for (int p = 0; p < A.nrh; ++p)
-            acc_rep[11 + A.prh[p]] += (double)(lam * sval(A.drhor4[(size_t)p * (A.nr + 1) + mm], qq));
+#pragma unroll
+          for (int p = 0; p < BMAX_PARAMS; ++p)
+            if (p < A.nrh) gd[p] += sval(A.drhor4[(size_t)p * (A.nr + 1) + mm], qq);
         });
+#pragma unroll
+        for (int p = 0; p < BMAX_PARAMS; ++p)
+          if (p < A.nrh) acc_par[A.prh[p]] += (double)(lam * gd[p]);
       }
     }
     __syncthreads();
+#pragma unroll
+    for (int q = 0; q < BMAX_PARAMS; ++q) acc_rep[11 + q] = acc_par[q];
     block_reduce_row(sm, acc_rep, REP_ROW, row);
   }
 }
