@@ -257,30 +257,6 @@ static int staged_copies(gbmd_context* c, double* const* host, int count, bool t
   return GBMD_OK;
 }
 
-// Positions of the last step of gbmd_run_nve_host, final once its first half
-// and any rebuild (which wraps them) have run: gathered into caller order on
-// the main stream, then copied to the caller's arrays on a copy stream while
-// the force pass runs; copy_join[0] marks the end.
-static int download_r_async(gbmd_context* c) {
-  const int64_t n = c->n;
-  if (!c->stage_r) GBMD_CUDA(c, cudaMalloc(&c->stage_r, sizeof(double) * 3 * c->cap));
-  int rc = ensure_copy_streams(c);
-  if (rc) return rc;
-  Arrays9 src{};
-  src.a[0] = c->X();
-  src.a[1] = c->Y();
-  src.a[2] = c->Z();
-  k_to_user_multi<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->cap, src, c->USER(), c->stage_r, 3);
-  GBMD_CUDA(c, cudaEventRecord(c->copy_fork, c->stream));
-  GBMD_CUDA(c, cudaStreamWaitEvent(c->copy_stream[0], c->copy_fork, 0));
-  c->r_copy_pending = true;
-  for (int k = 0; k < 3; ++k)
-    GBMD_CUDA(c, cudaMemcpyAsync(c->host_r_out[k], c->stage_r + (size_t)k * c->cap, sizeof(double) * n,
-                                 cudaMemcpyDeviceToHost, c->copy_stream[0]));
-  GBMD_CUDA(c, cudaEventRecord(c->copy_join[0], c->copy_stream[0]));
-  return GBMD_OK;
-}
-
 static int copy_rref(gbmd_context* c) {
   for (int d = 0; d < 3; ++d)
     GBMD_CUDA(c, cudaMemcpyAsync(c->rref + d * c->cap, c->rbuf[c->cur] + d * c->cap, sizeof(double) * c->n,
@@ -511,6 +487,34 @@ static int32_t* inverse_user(gbmd_context* c) {
   k_invert_user<<<nblk(c->n, 256), 256, 0, c->stream>>>(c->n, c->USER(), inv);
   return inv;
 }
+
+// Positions of the last step of gbmd_run_nve_host, final once its first half
+// and any rebuild (which wraps them) have run: gathered into caller order on
+// the main stream, then copied to the caller's arrays on a copy stream while
+// the force pass runs; copy_join[0] marks the end.
+static int download_r_async(gbmd_context* c) {
+  const int64_t n = c->n;
+  if (!c->stage_r) GBMD_CUDA(c, cudaMalloc(&c->stage_r, sizeof(double) * 3 * c->cap));
+  int rc = ensure_copy_streams(c);
+  if (rc) return rc;
+  Arrays9 src{}, dst{};
+  for (int k = 0; k < 3; ++k) dst.a[k] = c->stage_r + (size_t)k * c->cap;
+  src.a[0] = c->X();
+  src.a[1] = c->Y();
+  src.a[2] = c->Z();
+  // gathered by caller index (coalesced writes; the reads are the scattered side)
+  const int32_t* inv = inverse_user(c);
+  k_state_to_host<<<nblk(n, 256), 256, 0, c->stream>>>(n, inv, src, dst, 3);
+  GBMD_CUDA(c, cudaEventRecord(c->copy_fork, c->stream));
+  GBMD_CUDA(c, cudaStreamWaitEvent(c->copy_stream[0], c->copy_fork, 0));
+  c->r_copy_pending = true;
+  for (int k = 0; k < 3; ++k)
+    GBMD_CUDA(c, cudaMemcpyAsync(c->host_r_out[k], c->stage_r + (size_t)k * c->cap, sizeof(double) * n,
+                                 cudaMemcpyDeviceToHost, c->copy_stream[0]));
+  GBMD_CUDA(c, cudaEventRecord(c->copy_join[0], c->copy_stream[0]));
+  return GBMD_OK;
+}
+
 
 static int upload_arrays(gbmd_context* c, const double* const* host, double* const* dev, int count) {
   const int64_t n = c->n;
