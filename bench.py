@@ -89,6 +89,8 @@ def parse():
     p.add_argument("--vec", type=int, default=1, help="list entries per lane per load with --lanes (1 or 4)")
     p.add_argument("--staging", action="store_true",
                    help="with --lanes 1 --vec 4: stage neighbour positions in shared memory")
+    p.add_argument("--ref-seconds", type=float, default=150.0,
+                   help="--impl reference: CPU seconds the warm-up + timed steps of the sample should take")
     p.add_argument("--thermalise", type=int, default=100,
                    help="untimed NVE steps from the lattice before the launch shape is tuned (lattice workloads)")
     p.add_argument("--ncell", type=int, default=0,
@@ -265,9 +267,9 @@ def run_reference(args, w, ws, rank):
     if rank != 0:
         return
     O = _oracle()
-    # size the sample: ~150 s for warmup + steps at the calibrated rate
-    rate, _ = cpu_oracle_rate(w, target_s=3.0, ncell=8 if w["kind"] == "eam" else 10)
-    budget = 150.0
+    # size the sample: --ref-seconds (150 s) for warmup + steps at the calibrated rate
+    rate, _ = cpu_oracle_rate(w, target_s=min(3.0, args.ref_seconds), ncell=8 if w["kind"] == "eam" else 10)
+    budget = args.ref_seconds
     atoms = rate * budget / max(1, args.steps + args.warmup)
     per = 4
     nc = int(max(4, min(w.get("ncell", 64), round((atoms / per) ** (1.0 / 3.0)))))
