@@ -316,11 +316,17 @@ struct BuildCell {
 };
 
 // Stage candidates q0 .. q0+63 (position shifted into the home cell's frame,
-// index | stencil code << 26) into this warp's shared-memory buffer.
-__device__ __forceinline__ void build_stage(const BuildCell& B, const float4* __restrict__ pf, int q0,
-                                            float4* stage, int lane) {
+// index | stencil code << 26) into this warp's shared-memory buffer, keeping
+// in order only those within reach of the home group's bounding box
+// [blo, bhi] (box distance^2 <= R2keep); the rest cannot pair with any home
+// atom of the group (about a quarter of the candidates: the far parts of the
+// edge and corner cells).  Returns the number kept; stage[kept] is a sentinel.
+__device__ __forceinline__ int build_stage(const BuildCell& B, const float4* __restrict__ pf, int q0,
+                                           float4* stage, int lane, const float3& blo, const float3& bhi,
+                                           float R2keep) {
   const unsigned FULL = 0xffffffffu;
   const float FAR = 1e18f;
+  int kept = 0;
 #pragma unroll
   for (int r = 0; r < BUILD_CHUNK / 32; ++r) {
     const int q = q0 + r * 32 + lane;
@@ -337,13 +343,22 @@ __device__ __forceinline__ void build_stage(const BuildCell& B, const float4* __
     const float sx = __shfl_sync(FULL, B.s_sx, sc), sy = __shfl_sync(FULL, B.s_sy, sc),
                 sz = __shfl_sync(FULL, B.s_sz, sc);
     float4 e = make_float4(FAR, FAR, FAR, __uint_as_float(0xffffffffu));
+    bool keep = false;
     if (q < B.total) {
       const float4 pj = pf[k];
       e = make_float4(__fadd_rn(pj.x, sx), __fadd_rn(pj.y, sy), __fadd_rn(pj.z, sz),
                       __uint_as_float((uint32_t)k | (code << GBMD_IDX_BITS)));
+      const float bx = fmaxf(0.f, fmaxf(blo.x - e.x, e.x - bhi.x));
+      const float by = fmaxf(0.f, fmaxf(blo.y - e.y, e.y - bhi.y));
+      const float bz = fmaxf(0.f, fmaxf(blo.z - e.z, e.z - bhi.z));
+      keep = fmaf(bx, bx, fmaf(by, by, bz * bz)) <= R2keep;
     }
-    stage[r * 32 + lane] = e;
+    const unsigned km = __ballot_sync(FULL, keep);
+    if (keep) stage[kept + __popc(km & ((1u << lane) - 1u))] = e;
+    kept += __popc(km);
   }
+  if (lane == 0) stage[kept] = make_float4(FAR, FAR, FAR, __uint_as_float(0xffffffffu));
+  return kept;
 }
 
 // Deferred FP64 re-test of an atom's band entries: recompute each entry's
@@ -391,20 +406,34 @@ __device__ __forceinline__ int build_walk(const BuildCell& B, const float4* __re
   const float FAR = 1e18f;
   const int half = G == 16 ? (lane >> 4) : 0;
   const int hl = G == 16 ? (lane & 15) : lane;
+  // box distance bound with a margin far above the FP32 rounding of the
+  // walk's d2, so no candidate the walk would keep is dropped
+  const float R2keep = R2hi * (1.0f + 0x1p-10f);
   int warp_max = 0;
   for (int h0 = 0; h0 < B.nh; h0 += G) {
     const bool hv = h0 + hl < B.nh;
     const int i = B.hb + h0 + hl;
     float4 pi = make_float4(FAR, FAR, FAR, 0.f);
     if (hv) pi = pf[i];
+    // bounding box of the group's home atoms (cell frame)
+    float3 blo = make_float3(hv ? pi.x : FAR, hv ? pi.y : FAR, hv ? pi.z : FAR);
+    float3 bhi = make_float3(hv ? pi.x : -FAR, hv ? pi.y : -FAR, hv ? pi.z : -FAR);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      blo.x = fminf(blo.x, __shfl_xor_sync(FULL, blo.x, o));
+      blo.y = fminf(blo.y, __shfl_xor_sync(FULL, blo.y, o));
+      blo.z = fminf(blo.z, __shfl_xor_sync(FULL, blo.z, o));
+      bhi.x = fmaxf(bhi.x, __shfl_xor_sync(FULL, bhi.x, o));
+      bhi.y = fmaxf(bhi.y, __shfl_xor_sync(FULL, bhi.y, o));
+      bhi.z = fmaxf(bhi.z, __shfl_xor_sync(FULL, bhi.z, o));
+    }
     uint32_t* row = nbr + (size_t)i * W;  // slot k at row[(k >> wsh) * stride + (k & (W - 1))]
     int cnt = 0;
     bool unc = false;
     for (int q0 = 0; q0 < B.total; q0 += BUILD_CHUNK) {
       __syncwarp();
-      build_stage(B, pf, q0, stage, lane);
+      const int m = build_stage(B, pf, q0, stage, lane, blo, bhi, R2keep);
       __syncwarp();
-      const int m = min(BUILD_CHUNK, B.total - q0);
 #pragma unroll 8
       for (int t = 0; t < m; t += (G == 16 ? 2 : 1)) {
         const float4 e = stage[t + half];
@@ -508,7 +537,7 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32) k_build_list_cells(
   B.nh = cstart[cell + 1] - B.hb;
   int wsh = 0;
   while ((1 << wsh) < W) ++wsh;
-  __shared__ float4 stage_all[BUILD_WARPS][BUILD_CHUNK];
+  __shared__ float4 stage_all[BUILD_WARPS][BUILD_CHUNK + 1];
   float4* stage = stage_all[threadIdx.x >> 5];
   int warp_max;
   if (B.nh <= 16)
