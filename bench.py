@@ -410,8 +410,10 @@ def main():
     # fixed interval: thermo at the end of each 2R-step graph chunk; with the
     # displacement trigger (R = -1) every 20 steps
     thermo_every = 2 * R if R > 0 else (20 if R < 0 else 0)
-    # warm-up (also captures the CUDA graph)
-    ctx.run_nve(max(args.warmup, 3), dt, R, thermo_every, use_graph=True)
+    # warm-up: at least W steps, and one graph chunk plus a step so that the
+    # CUDA graph is captured here rather than inside the timed region
+    warm = max(args.warmup, 3, thermo_every + 1)
+    ctx.run_nve(warm, dt, R, thermo_every, use_graph=True)
     npairs, maxnb, nc = ctx.neighbor_stats()
 
     # ---- timed region: K steps, device resident --------------------------
@@ -449,6 +451,7 @@ def main():
                       "precision": args.precision, "thermo_every": thermo_every,
                       "rebuild_every": R if R >= 0 else "on displacement > skin/2",
                       "list_builds_in_timed_region": rebuilds,
+                      "warmup_steps_run": warm,
                       "neighbours_per_atom": npairs / s.n, "cells": nc.tolist(),
                       "lanes_per_atom": ctx.get_launch_ex()[0], "list_entries_per_load": ctx.get_launch_ex()[1],
                       "block": ctx.get_launch_ex()[2], "density_block": ctx.get_density_block(),

@@ -200,6 +200,24 @@ __global__ void k_cell_rank(int64_t ncells, const int32_t* __restrict__ cstart, 
   const int lane = threadIdx.x & 31;
   if (cell >= ncells || (gate && !*gate)) return;
   const int beg = cstart[cell], m = cstart[cell + 1] - beg;
+  if (m <= 32) {
+    // keys in registers, compared through shuffles
+    int32_t a = 0, ua = 0;
+    uint64_t ka = 0;
+    if (lane < m) {
+      a = order[beg + lane];
+      ka = id[a];
+      ua = user[a];
+    }
+    int rank = 0;
+    for (int f = 0; f < m; ++f) {
+      const uint64_t kb = __shfl_sync(0xffffffffu, ka, f);
+      const int32_t ub = __shfl_sync(0xffffffffu, ua, f);
+      rank += (kb < ka) || (kb == ka && ub < ua);
+    }
+    if (lane < m) src[beg + rank] = a;
+    return;
+  }
   for (int e = lane; e < m; e += 32) {
     const int32_t a = order[beg + e];
     const uint64_t ka = id[a];
