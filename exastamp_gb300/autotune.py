@@ -46,9 +46,10 @@ def _store(d):
     p = _cache_path()
     try:
         os.makedirs(os.path.dirname(p), exist_ok=True)
-        with open(p + ".tmp", "w") as fh:
+        tmp = "%s.%d.tmp" % (p, os.getpid())  # one per process: ranks may store at once
+        with open(tmp, "w") as fh:
             json.dump(d, fh, indent=1)
-        os.replace(p + ".tmp", p)
+        os.replace(tmp, p)
     except OSError:
         pass
 
