@@ -328,12 +328,13 @@ def bench_batched(stream, torch):
         b.run()
         d = b.download()
         b.set_targets(d["F"] * 1.01, d["ep"] * 1.01, 1.0 / n, 0.1 / n)
-        block, stencil, tun = autotune.tune_batch(b, "replicas4096", adjoint=True)
-        b.set_launch(block, stencil)
+        block, stencil, small_block, tun = autotune.tune_batch(b, "replicas4096", adjoint=True)
         ms_graph = _time_batch(b, torch, stream, 5, adjoint=True, use_graph=True)
         ms_fwd = _time_batch(b, torch, stream, 5, adjoint=False, use_graph=True)
         ms_each = _time_batch(b, torch, stream, 1, adjoint=True, per_replica=True)
     return {"replicas": len(reps), "atoms": n, "block": block, "stencil": stencil,
+            "small_replica_block": small_block,
+            "replicas_over_512_atoms": sum(1 for s in reps if s.n > 512),
             "ms_forward_adjoint_persistent_graph": ms_graph, "ms_forward_persistent_graph": ms_fwd,
             "ms_forward_adjoint_one_launch_per_replica": ms_each,
             "replicas_per_s": len(reps) / (ms_graph * 1e-3), "atom_evaluations_per_s": n / (ms_graph * 1e-3),

@@ -355,6 +355,7 @@ _BATCH_SIG = {
     "gbmd_batch_upload": (["vp", "i32", "vp", "vp", "vp", "vp", "vp", "vp"], "i32"),
     "gbmd_batch_set_targets": (["vp", "vp", "vp", "vp", "vp", "dbl", "dbl"], "i32"),
     "gbmd_batch_set_launch": (["vp", "i32", "i32"], "i32"),
+    "gbmd_batch_set_small_block": (["vp", "i32"], "i32"),
     "gbmd_batch_run": (["vp", "i32", "i32", "i32"], "i32"),
     "gbmd_batch_synchronize": (["vp"], "i32"),
     "gbmd_batch_download": (["vp", "vp", "vp", "vp", "vp", "vp", "vp", "vp", "vp"], "i32"),
@@ -437,6 +438,10 @@ class Batch:
 
     def set_launch(self, block, stencil):
         self._chk(self._L.gbmd_batch_set_launch(self.h, int(block), int(stencil)))
+
+    def set_small_block(self, block):
+        """Threads per block of the kernel for replicas of at most 512 atoms."""
+        self._chk(self._L.gbmd_batch_set_small_block(self.h, int(block)))
 
     def run(self, adjoint=False, per_replica=False, use_graph=False):
         self._chk(self._L.gbmd_batch_run(self.h, 1 if adjoint else 0, 1 if per_replica else 0,

@@ -54,34 +54,54 @@ def _store(d):
         pass
 
 
-def tune_batch(batch, key: str, blocks=(128, 256, 512), stencils=(1, 2), adjoint=False, reps: int = 3,
-               use_cache: bool = True):
-    """Pick (block, stencil radius) for a gbmd_batch: each candidate runs the
-    persistent launch `reps` times, timed on the host around a synchronize."""
+def tune_batch(batch, key: str, blocks=(128, 256, 512), stencils=(1, 2), small_blocks=(64, 128, 256),
+               adjoint=False, reps: int = 3, use_cache: bool = True):
+    """Pick (block, stencil radius, small-replica block) for a gbmd_batch:
+    each candidate runs the persistent launch `reps` times, timed on the host
+    around a synchronize; the small-replica kernel's block is tried last, with
+    the best (block, stencil).  Leaves the choice set on the batch and returns
+    (block, stencil, small_block, timings)."""
     import time
-    ck = "%s|batch|%s|%d|%d|%d" % (_gpu_name(), key, batch.nrep, batch.n, int(adjoint))
+
+    def timed():
+        batch.run(adjoint=adjoint)
+        batch.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            batch.run(adjoint=adjoint)
+        batch.synchronize()
+        return (time.perf_counter() - t0) * 1e3 / reps
+
+    ck = "%s|batch2|%s|%d|%d|%d" % (_gpu_name(), key, batch.nrep, batch.n, int(adjoint))
     cache = _load() if use_cache else {}
     if ck in cache:
         e = cache[ck]
-        return int(e["block"]), int(e["stencil"]), e.get("timings", {})
+        batch.set_launch(int(e["block"]), int(e["stencil"]))
+        batch.set_small_block(int(e["small_block"]))
+        return int(e["block"]), int(e["stencil"]), int(e["small_block"]), e.get("timings", {})
     timings, best = {}, None
+    batch.set_small_block(128)
     for s in stencils:
         for b in blocks:
             batch.set_launch(b, s)
-            batch.run(adjoint=adjoint)
-            batch.synchronize()
-            t0 = time.perf_counter()
-            for _ in range(reps):
-                batch.run(adjoint=adjoint)
-            batch.synchronize()
-            ms = (time.perf_counter() - t0) * 1e3 / reps
+            ms = timed()
             timings["%dx%d" % (b, s)] = ms
             if best is None or ms < best[0]:
                 best = (ms, b, s)
-    cache[ck] = {"block": best[1], "stencil": best[2], "timings": timings}
+    _, b, s = best
+    batch.set_launch(b, s)
+    best_small = None
+    for sb in small_blocks:
+        batch.set_small_block(sb)
+        ms = timed()
+        timings["%dx%d small %d" % (b, s, sb)] = ms
+        if best_small is None or ms < best_small[0]:
+            best_small = (ms, sb)
+    batch.set_small_block(best_small[1])
+    cache[ck] = {"block": b, "stencil": s, "small_block": best_small[1], "timings": timings}
     if use_cache:
         _store(cache)
-    return best[1], best[2], timings
+    return b, s, best_small[1], timings
 
 
 def tune(ctx, key: str, lanes=LANES, blocks=BLOCKS, vecs=VECS, reps: int = 3, use_cache: bool = True):

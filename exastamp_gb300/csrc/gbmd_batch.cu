@@ -38,10 +38,11 @@
 
 namespace {
 
-constexpr int BMAX_ATOMS = 2048;
+constexpr int BMAX_ATOMS = 2048;   // largest replica
 constexpr int BMAX_CELLS = 1024;
-constexpr int NBL_MAX = 128;                          // pair-list entries per atom
-constexpr size_t NBL_REGION = (size_t)BMAX_ATOMS * NBL_MAX;  // entries per block
+constexpr int SMALL_ATOMS = 512;   // replicas up to this size run in the small-block kernel
+constexpr int SMALL_CELLS = 512;
+constexpr int NBL_MAX = 128;       // pair-list entries per atom
 constexpr int BMAX_PARAMS = 9;
 constexpr int REP_ROW = 20;  // epot, virial[9], loss, grad[9]
 
@@ -70,22 +71,24 @@ struct BatchArgs {
   double wF, wE;
   const float4 *dz2r4, *drhor4, *dfrho4;  // [k][knot] for the listed parameters
   int nz2, nrh, nfr;
-  uint32_t* nbl;  // NBL_REGION entries per block: the current replica's pair list
+  uint32_t* nbl;  // MAXA * NBL_MAX entries per block: the current replica's pair list
   int pz2[BMAX_PARAMS], prh[BMAX_PARAMS], pfr[BMAX_PARAMS];
 };
 
-struct SmemLayout {
-  float4 pos[BMAX_ATOMS];   // cell-relative FP32 position, w = local atom index bits
-  float4 gfe[BMAX_ATOMS];   // adjoint: dL/dF (xyz) and dL/dE (w)
-  int cstart[BMAX_CELLS + 1];
-  int cfill[BMAX_CELLS];
-  int cellof[BMAX_ATOMS];   // by local atom index
-  int order[BMAX_ATOMS];    // slot -> local atom index
-  float fp[BMAX_ATOMS];     // F'(rho) by slot
-  float eemb[BMAX_ATOMS];   // F(rho) by slot
-  float rho[BMAX_ATOMS];    // rho by slot
-  float G[BMAX_ATOMS];      // adjoint G by slot
-  int nnb[BMAX_ATOMS];      // pair-list length by slot
+// Shared memory of one block: a replica of up to MAXA atoms in MAXC cells.
+template <int MAXA, int MAXC>
+struct SmemT {
+  float4 pos[MAXA];   // cell-relative FP32 position, w = local atom index bits
+  float4 gfe[MAXA];   // adjoint: dL/dF (xyz) and dL/dE (w)
+  int cstart[MAXC + 1];
+  int cfill[MAXC];
+  int cellof[MAXA];   // by local atom index
+  int order[MAXA];    // slot -> local atom index
+  float fp[MAXA];     // F'(rho) by slot
+  float eemb[MAXA];   // F(rho) by slot
+  float rho[MAXA];    // rho by slot
+  float G[MAXA];      // adjoint G by slot
+  int nnb[MAXA];      // pair-list length by slot
   double red[32][REP_ROW];  // block reduction
   int rep;
   int list_ok;              // every atom's pairs fit in the list
@@ -149,8 +152,8 @@ __device__ __forceinline__ float pair_d2(const float4& pi, const float4& pj, flo
 
 // Visit every in-cutoff neighbour of slot s from the cells around it:
 // fn(k, dx, dy, dz, d2, code), code = the cell offset (dx+S) | (dy+S) << 3 | (dz+S) << 6.
-template <class Fn>
-__device__ __forceinline__ void for_pairs(const BatchArgs& A, const RepGeom& g, const SmemLayout& sm, int s, Fn fn) {
+template <class SM, class Fn>
+__device__ __forceinline__ void for_pairs(const BatchArgs& A, const RepGeom& g, const SM& sm, int s, Fn fn) {
   const int ai = sm.order[s];
   const int c = sm.cellof[ai];
   const int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
@@ -182,8 +185,8 @@ __device__ __forceinline__ void for_pairs(const BatchArgs& A, const RepGeom& g, 
 
 // The same neighbours, in the same order and with the same FP32 arithmetic,
 // from the replica's pair list (entry: slot k | code << 11, slot-major).
-template <class Fn>
-__device__ __forceinline__ void for_list(const RepGeom& g, const SmemLayout& sm, const uint32_t* __restrict__ nbl,
+template <class SM, class Fn>
+__device__ __forceinline__ void for_list(const RepGeom& g, const SM& sm, const uint32_t* __restrict__ nbl,
                                          int n, int S, int s, Fn fn) {
   const float4 pi = sm.pos[s];
   const int cnt = sm.nnb[s];
@@ -201,8 +204,8 @@ __device__ __forceinline__ void for_list(const RepGeom& g, const SmemLayout& sm,
 
 // fn(k, dx, dy, dz, d2) over the neighbours of slot s: from the list when
 // every atom's pairs fit in it, else from the cells.
-template <class Fn>
-__device__ __forceinline__ void visit(const BatchArgs& A, const RepGeom& g, const SmemLayout& sm,
+template <class SM, class Fn>
+__device__ __forceinline__ void visit(const BatchArgs& A, const RepGeom& g, const SM& sm,
                                       const uint32_t* nbl, int n, int s, Fn fn) {
   if (sm.list_ok)
     for_list(g, sm, nbl, n, A.S, s, fn);
@@ -214,7 +217,8 @@ __device__ __forceinline__ void visit(const BatchArgs& A, const RepGeom& g, cons
 // for_pairs does (same FP32 screen and FP64 band re-test, same order).  A
 // warp-per-cell walk with shared-memory broadcasts measured slower here: a
 // replica of a few hundred atoms has too few cells to keep 16 warps busy.
-__device__ void build_list(const BatchArgs& A, const RepGeom& g, SmemLayout& sm, uint32_t* __restrict__ nbl, int n) {
+template <class SM>
+__device__ void build_list(const BatchArgs& A, const RepGeom& g, SM& sm, uint32_t* __restrict__ nbl, int n) {
   for (int s = threadIdx.x; s < n; s += blockDim.x) {
     int cnt = 0;
     for_pairs(A, g, sm, s, [&](int k, float, float, float, float, uint32_t code) {
@@ -226,7 +230,8 @@ __device__ void build_list(const BatchArgs& A, const RepGeom& g, SmemLayout& sm,
   }
 }
 
-__device__ void block_reduce_row(SmemLayout& sm, double* v, int nv, double* out) {
+template <class SM>
+__device__ void block_reduce_row(SM& sm, double* v, int nv, double* out) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int q = 0; q < nv; ++q) {
     double a = v[q];
@@ -243,9 +248,11 @@ __device__ void block_reduce_row(SmemLayout& sm, double* v, int nv, double* out)
   __syncthreads();
 }
 
+template <int MAXA, int MAXC>
 __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemLayout& sm = *reinterpret_cast<SmemLayout*>(smem_raw);
+  using SM = SmemT<MAXA, MAXC>;
+  SM& sm = *reinterpret_cast<SM*>(smem_raw);
   const int t = threadIdx.x, B = blockDim.x;
   // Persistent mode: take queue tickets until they run past nrep (each block
   // takes at most nrep + 1 tickets).  Single mode: exactly one replica.
@@ -267,7 +274,7 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs A) {
       int q = (int)floor(g.L[d] / cell_min);
       g.nc[d] = q < A.S ? A.S : q;
     }
-    while ((int64_t)g.nc[0] * g.nc[1] * g.nc[2] > BMAX_CELLS) {  // coarser cells still cover rcut
+    while ((int64_t)g.nc[0] * g.nc[1] * g.nc[2] > MAXC) {  // coarser cells still cover rcut
       int dm = 0;
       for (int d = 1; d < 3; ++d)
         if (g.nc[d] > g.nc[dm]) dm = d;
@@ -280,7 +287,7 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs A) {
       g.hf[d] = (float)g.h[d];
     }
     double* row = A.rep + (size_t)r * REP_ROW;
-    if (g.n > BMAX_ATOMS || g.L[0] < A.rcut || g.L[1] < A.rcut || g.L[2] < A.rcut) {
+    if (g.n > MAXA || g.L[0] < A.rcut || g.L[1] < A.rcut || g.L[2] < A.rcut) {
       if (t == 0) {
         atomicOr(&A.err[0], 16);
         for (int q = 0; q < REP_ROW; ++q) row[q] = __longlong_as_double(0x7ff8000000000000ll);
@@ -361,7 +368,7 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs A) {
     __syncthreads();
     // ---- pair list: one walk over the cells (FP32 screen, FP64 band
     // re-test), then every pass below reads the list
-    uint32_t* nbl = A.nbl + (A.single >= 0 ? (size_t)0 : (size_t)blockIdx.x * NBL_REGION);
+    uint32_t* nbl = A.nbl + (A.single >= 0 ? (size_t)0 : (size_t)blockIdx.x * MAXA * NBL_MAX);
     build_list(A, g, sm, nbl, n);
     __syncthreads();
     // ---- density + embedding
@@ -551,8 +558,13 @@ struct gbmd_batch {
   BatchArgs a{};
   bool have_pot = false, have_targets = false;
   int block = 256, S = 1;
-  uint32_t* nbl = nullptr;  // pair-list scratch, NBL_REGION entries per resident block
+  int small_block = 128;         // threads per block of the small-replica kernel
+  int nbig = 0;                  // replicas of more than SMALL_ATOMS atoms (first in `order`)
+  std::vector<int> rep_atoms;    // atoms per replica (host copy)
+  uint32_t* nbl = nullptr;       // pair-list scratch of the large-replica kernel's blocks
   size_t nbl_regions = 0;
+  uint32_t* nbl_small = nullptr; // and of the small-replica kernel's blocks
+  size_t nbl_small_regions = 0;
   cudaGraphExec_t graph = nullptr;
   int graph_adjoint = -1;
 };
@@ -600,7 +612,10 @@ void table_f4(int n, double delta, const double* vals, double scale, std::vector
                               (float)(s[m * 8 + 5] * scale), (float)(s[m * 8 + 6] * scale)));
 }
 
-size_t smem_bytes() { return sizeof(SmemLayout); }
+constexpr size_t SMEM_BIG = sizeof(SmemT<BMAX_ATOMS, BMAX_CELLS>);
+constexpr size_t SMEM_SMALL = sizeof(SmemT<SMALL_ATOMS, SMALL_CELLS>);
+auto* const K_BIG = &k_batch<BMAX_ATOMS, BMAX_CELLS>;
+auto* const K_SMALL = &k_batch<SMALL_ATOMS, SMALL_CELLS>;
 
 }  // namespace
 
@@ -624,9 +639,10 @@ int gbmd_batch_create(gbmd_batch** out, int device, void* stream) {
     }
     b->own_stream = true;
   }
-  if (cudaMalloc(&b->queue, sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_err, sizeof(int) * 4) != cudaSuccess ||
+  if (cudaMalloc(&b->queue, sizeof(int) * 2) != cudaSuccess || cudaMalloc(&b->d_err, sizeof(int) * 4) != cudaSuccess ||
       cudaMemset(b->d_err, 0, sizeof(int) * 4) != cudaSuccess ||
-      cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes()) != cudaSuccess) {
+      cudaFuncSetAttribute(K_BIG, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BIG) != cudaSuccess ||
+      cudaFuncSetAttribute(K_SMALL, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_SMALL) != cudaSuccess) {
     cudaFree(b->queue);
     cudaFree(b->d_err);
     delete b;
@@ -647,6 +663,7 @@ int gbmd_batch_destroy(gbmd_batch* b) {
   cudaFree(b->tab);
   cudaFree(b->dtab);
   cudaFree(b->nbl);
+  cudaFree(b->nbl_small);
   if (b->own_stream) cudaStreamDestroy(b->stream);
   delete b;
   return GBMD_OK;
@@ -767,6 +784,12 @@ int gbmd_batch_upload(gbmd_batch* b, int nrep, const int64_t* offsets, const dou
   std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) {
     return offsets[a + 1] - offsets[a] > offsets[c + 1] - offsets[c];
   });
+  b->rep_atoms.resize(nrep);
+  b->nbig = 0;
+  for (int r = 0; r < nrep; ++r) {
+    b->rep_atoms[r] = (int)(offsets[r + 1] - offsets[r]);
+    if (b->rep_atoms[r] > SMALL_ATOMS) ++b->nbig;
+  }
   const size_t nb = sizeof(double) * (size_t)(n > 0 ? n : 1);
   BCUDA(b, cudaMalloc(&b->off, sizeof(int64_t) * (nrep + 1)));
   BCUDA(b, cudaMalloc(&b->lo, sizeof(double) * 3 * nrep));
@@ -803,6 +826,13 @@ int gbmd_batch_set_targets(gbmd_batch* b, const double* fx, const double* fy, co
   return GBMD_OK;
 }
 
+int gbmd_batch_set_small_block(gbmd_batch* b, int block) {
+  if (!b || block < 64 || block > 256 || block % 32) return berr(b, GBMD_ERR_INVALID, "small block in [64,256], multiple of 32");
+  b->small_block = block;
+  drop_graph(b);
+  return GBMD_OK;
+}
+
 int gbmd_batch_set_launch(gbmd_batch* b, int block, int stencil) {
   if (!b || block < 64 || block > 512 || block % 32 || (stencil != 1 && stencil != 2))
     return berr(b, GBMD_ERR_INVALID, "block in [64,512] (multiple of 32), stencil 1 or 2");
@@ -812,26 +842,45 @@ int gbmd_batch_set_launch(gbmd_batch* b, int block, int stencil) {
   return GBMD_OK;
 }
 
-// blocks of the persistent launch: as many as fit on the device at once
-static int persistent_grid(gbmd_batch* b) {
+// Blocks of a persistent launch: as many as fit on the device at once, at
+// most one per replica of its queue.  big: the large-replica kernel (the
+// autotuned block), else the small-replica kernel (b->small_block threads).
+static int persistent_grid(gbmd_batch* b, bool big) {
   int dev_sms = 0, per_sm = 0;
   cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, b->device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, b->block, smem_bytes());
-  return std::max(1, std::min(b->nrep, dev_sms * std::max(per_sm, 1)));
+  if (big)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, K_BIG, b->block, SMEM_BIG);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, K_SMALL, b->small_block, SMEM_SMALL);
+  const int nq = big ? b->nbig : b->nrep - b->nbig;
+  return std::max(1, std::min(nq, dev_sms * std::max(per_sm, 1)));
 }
 
-// pair-list scratch for `regions` blocks (allocated outside any capture)
-static int ensure_nbl(gbmd_batch* b, int regions) {
-  if ((size_t)regions <= b->nbl_regions) return GBMD_OK;
-  drop_graph(b);
-  cudaFree(b->nbl);
-  b->nbl = nullptr;
-  b->nbl_regions = 0;
-  BCUDA(b, cudaMalloc(&b->nbl, sizeof(uint32_t) * NBL_REGION * (size_t)regions));
-  b->nbl_regions = (size_t)regions;
+// pair-list scratch for `regions` blocks of each kernel (allocated outside any capture)
+static int ensure_nbl(gbmd_batch* b, int regions, int small_regions) {
+  if ((size_t)regions > b->nbl_regions) {
+    drop_graph(b);
+    cudaFree(b->nbl);
+    b->nbl = nullptr;
+    b->nbl_regions = 0;
+    BCUDA(b, cudaMalloc(&b->nbl, sizeof(uint32_t) * BMAX_ATOMS * NBL_MAX * (size_t)regions));
+    b->nbl_regions = (size_t)regions;
+  }
+  if ((size_t)small_regions > b->nbl_small_regions) {
+    drop_graph(b);
+    cudaFree(b->nbl_small);
+    b->nbl_small = nullptr;
+    b->nbl_small_regions = 0;
+    BCUDA(b, cudaMalloc(&b->nbl_small, sizeof(uint32_t) * SMALL_ATOMS * NBL_MAX * (size_t)small_regions));
+    b->nbl_small_regions = (size_t)small_regions;
+  }
   return GBMD_OK;
 }
 
+// Replicas of more than SMALL_ATOMS atoms run in the large-replica kernel
+// (one block of up to 512 threads and 136 KB of shared memory per SM), the
+// rest in the small-replica kernel (64-256 threads, 36 KB, several blocks per
+// SM); each takes its replicas from its own queue, largest first.
 static int batch_launch(gbmd_batch* b, int adjoint, int per_replica) {
   BatchArgs A = b->a;
   A.nrep = b->nrep;
@@ -848,19 +897,38 @@ static int batch_launch(gbmd_batch* b, int adjoint, int per_replica) {
   A.S = b->S;
   A.adjoint = adjoint;
   A.Ftx = b->Ftx; A.Fty = b->Fty; A.Ftz = b->Ftz; A.Et = b->Et;
-  A.nbl = b->nbl;
-  const size_t smem = smem_bytes();
   if (per_replica) {
     for (int r = 0; r < b->nrep; ++r) {
       A.single = r;
-      k_batch<<<1, b->block, smem, b->stream>>>(A);
+      if (b->rep_atoms[r] > SMALL_ATOMS) {
+        A.nbl = b->nbl;
+        K_BIG<<<1, b->block, SMEM_BIG, b->stream>>>(A);
+      } else {
+        A.nbl = b->nbl_small;
+        K_SMALL<<<1, b->small_block, SMEM_SMALL, b->stream>>>(A);
+      }
     }
   } else {
-    const int grid = persistent_grid(b);
-    if ((size_t)grid > b->nbl_regions) return berr(b, GBMD_ERR_INVALID, "pair-list scratch not sized");
     A.single = -1;
-    BCUDA(b, cudaMemsetAsync(b->queue, 0, sizeof(int), b->stream));
-    k_batch<<<grid, b->block, smem, b->stream>>>(A);
+    BCUDA(b, cudaMemsetAsync(b->queue, 0, sizeof(int) * 2, b->stream));
+    if (b->nbig > 0) {
+      const int grid = persistent_grid(b, true);
+      if ((size_t)grid > b->nbl_regions) return berr(b, GBMD_ERR_INVALID, "pair-list scratch not sized");
+      BatchArgs Ab = A;
+      Ab.nrep = b->nbig;
+      Ab.nbl = b->nbl;
+      K_BIG<<<grid, b->block, SMEM_BIG, b->stream>>>(Ab);
+    }
+    if (b->nrep > b->nbig) {
+      const int grid = persistent_grid(b, false);
+      if ((size_t)grid > b->nbl_small_regions) return berr(b, GBMD_ERR_INVALID, "pair-list scratch not sized");
+      BatchArgs As = A;
+      As.nrep = b->nrep - b->nbig;
+      As.order = b->order + b->nbig;
+      As.queue = b->queue + 1;
+      As.nbl = b->nbl_small;
+      K_SMALL<<<grid, b->small_block, SMEM_SMALL, b->stream>>>(As);
+    }
   }
   BCUDA(b, cudaGetLastError());
   return GBMD_OK;
@@ -872,7 +940,9 @@ int gbmd_batch_run(gbmd_batch* b, int adjoint, int per_replica, int use_graph) {
     return berr(b, GBMD_ERR_INVALID, "adjoint needs targets and parameter derivatives");
   cudaSetDevice(b->device);
   {
-    const int rc = ensure_nbl(b, per_replica ? 1 : persistent_grid(b));
+    const int rc = per_replica ? ensure_nbl(b, 1, 1)
+                               : ensure_nbl(b, b->nbig > 0 ? persistent_grid(b, true) : 0,
+                                            b->nrep > b->nbig ? persistent_grid(b, false) : 0);
     if (rc) return rc;
   }
   if (use_graph && !per_replica) {

@@ -301,6 +301,9 @@ int gbmd_batch_set_targets(gbmd_batch* b, const double* fx, const double* fy, co
 /* launch shape (the autotuner's knobs): threads per block (64-512) and the
  * cell stencil radius (1: cells >= rcut, 2: cells >= rcut/2) */
 int gbmd_batch_set_launch(gbmd_batch* b, int block, int stencil);
+/* Replicas of at most 512 atoms run in a second kernel with smaller blocks
+ * (several per SM): its threads per block, 64-256 (default 128). */
+int gbmd_batch_set_small_block(gbmd_batch* b, int block);
 /* per_replica != 0: one launch per replica (the comparison mode);
  * use_graph != 0: the persistent launch is captured once and replayed */
 int gbmd_batch_run(gbmd_batch* b, int adjoint, int per_replica, int use_graph);
