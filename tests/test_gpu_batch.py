@@ -39,10 +39,13 @@ def cu():
     return cfg, SF.tabulate(cfg)
 
 
-@pytest.mark.parametrize("stencil", [1, 2])
-def test_batch_forward_matches_oracle(gpu, oracle, cu, stencil):
+@pytest.mark.parametrize("stencil,nmax", [(1, 400), (2, 400), (1, 1500), (2, 1500)])
+def test_batch_forward_matches_oracle(gpu, oracle, cu, stencil, nmax):
+    """nmax 400: only the small-replica kernel; 1500: both kernels."""
     cfg, sf = cu
-    reps = _replicas(24, seed=31)
+    reps = _replicas(24, seed=31, nmax=nmax)
+    if nmax > 512:
+        assert any(s.n > 512 for s in reps) and any(s.n <= 512 for s in reps)
     tab = oracle.EamOracleTables.from_setfl(sf, 1.0, 1.0, rcut=5.0)
     F, E, V = _oracle_forward(oracle, reps, tab)
     with gpu.Batch(0) as b:
@@ -104,8 +107,8 @@ def test_batch_launch_modes_are_identical(gpu, cu):
         assert np.array_equal(o["vir_rep"], outs[0]["vir_rep"])
 
 
-def _adjoint_problem(oracle, cfg, nconf=6, seed=4):
-    confs = S.adjoint_training_set(nconf=nconf, ncell=4, seed=seed)
+def _adjoint_problem(oracle, cfg, nconf=6, seed=4, ncell=4):
+    confs = S.adjoint_training_set(nconf=nconf, ncell=ncell, seed=seed)
     rng = np.random.default_rng(5)
     pert = {k: v * rng.uniform(0.9, 1.1) for k, v in cfg["params"].items()}
     tab_t = oracle.EamOracleTables.from_setfl(SF.tabulate(cfg, pert), 1.0, 1.0, rcut=5.0)
@@ -113,9 +116,13 @@ def _adjoint_problem(oracle, cfg, nconf=6, seed=4):
     return confs, Ft, Et
 
 
-def test_batch_adjoint_matches_fp64_oracle_gradient(gpu, oracle, cu):
+@pytest.mark.parametrize("ncell", [4, 6])
+def test_batch_adjoint_matches_fp64_oracle_gradient(gpu, oracle, cu, ncell):
+    """ncell 4: 243-atom configurations (small-replica kernel); 6: ~820 atoms
+    (large-replica kernel)."""
     cfg, sf = cu
-    confs, Ft, Et = _adjoint_problem(oracle, cfg)
+    confs, Ft, Et = _adjoint_problem(oracle, cfg, nconf=6 if ncell == 4 else 3, ncell=ncell)
+    assert all((c.n > 512) == (ncell == 6) for c in confs)
     ntot = sum(c.n for c in confs)
     wF, wE = 1.0 / ntot, 0.1 / ntot
     # FP64 oracle loss and gradient
