@@ -4,15 +4,21 @@
 // Built as an exaStamp plugin (onika_add_plugin, as in
 // src/potential/pair_potential_template/CMakeLists.txt L54-59) when onika and
 // exaNBody are available; it is not compiled in this repository, which has
-// neither.  Operator:
+// neither.  Operators (drop-ins for the compute_force slot):
 //
-//   gb300_force   drop-in for lj_compute_force / eam_alloy_force in the
-//                 compute_force slot (slot `potential`: lj or eam_alloy)
+//   gb300_lj_force         lj_compute_force  (pair_potential_impl.hxx L104-121)
+//   gb300_lj_multi_force   lj_multi_force    (pair_potential_force_op_multiparam.h L249-284)
+//   gb300_eam_alloy_force  eam_alloy_force   (eam_potential_multimat.cu L88-109)
+//   gb300_johnson_force    johnson_force     (johnson.h, eam_potential.cu L69-193)
+//   gb300_force            any of them, chosen by the slot `potential`
 //
-// It keeps the reference slots (pair_potential_impl.hxx
-// L104-121, eam_potential_multimat.cu L88-109): rcut, rcut_max, parameters,
-// ghost_dist_max, grid, domain, species, trigger_thermo_state,
-// compute_virial.  Each execute() copies the inner-cell particles
+// Each keeps its reference operator's slot names and meaning (parameters,
+// rcut, rcut_max, ghost_dist_max, chunk_neighbors, species, grid, domain,
+// trigger_thermo_state, compute_virial, the eam_* pass flags), plus rcut_inc
+// (the neighbour skin, global.rcut_inc) and precision (mixed or fp64).
+// Slots that only steer the reference's own traversal (chunk_neighbors,
+// ghost, compact_nbh_weight, enable_pair_weights) are accepted and unused:
+// the library keeps its own list, rebuilt on the skin/2 displacement test.  Each execute() copies the inner-cell particles
 // (rx,ry,rz,vx,vy,vz,type,id) into the GPU context, runs zero_force_energy +
 // compute_force + force_to_accel on the device, and writes forces f = m*a,
 // ep and virial back into the cells, so the graph's own force_to_accel and
@@ -24,8 +30,12 @@
 #include <exanb/core/domain.h>
 #include <exanb/core/grid.h>
 #include <exanb/core/make_grid_variant_operator.h>
+#include <exanb/particle_neighbors/chunk_neighbors.h>
 #include <exaStamp/particle_species/particle_specie.h>
+#include <exaStamp/potential/pair_potentials/lennard_jones/lennard_jones.h>  // LennardJonesParms + YAML
 #include <exaStamp/unit_system.h>
+#include <onika/physics/units.h>
+#include <yaml-cpp/yaml.h>
 #include "johnson.h"  // src/potential/eam_potentials/johnson (EamJohnsonParameters + its YAML decoder)
 
 #include <gbmd.h>
@@ -88,7 +98,293 @@ void gather(const GridT& grid, Staging& s) {
   s.vir.resize(9 * s.n);
 }
 
+inline gbmd_context* make_context(const Domain& domain, const ParticleSpecies& species) {
+  gbmd_context* c = nullptr;
+  if (gbmd_create(&c, 0, parallel_execution_context()->gpu_stream()) != GBMD_OK)
+    fatal_error() << "gb300: no GPU context" << std::endl;
+  const Vec3d lo = domain.bounds().bmin, hi = domain.bounds().bmax;
+  const double blo[3] = {lo.x, lo.y, lo.z}, bhi[3] = {hi.x, hi.y, hi.z};
+  const int per[3] = {domain.periodic_boundary_x(), domain.periodic_boundary_y(), domain.periodic_boundary_z()};
+  check(c, gbmd_set_box(c, blo, bhi, per), "gbmd_set_box");
+  std::vector<double> m(species.size());
+  for (size_t t = 0; t < m.size(); ++t) m[t] = species.at(t).m_mass;
+  check(c, gbmd_set_species(c, (int)m.size(), m.data()), "gbmd_set_species");
+  return c;
+}
+
+inline void finish_setup(gbmd_context* c, double skin, const std::string& precision) {
+  check(c, gbmd_set_skin(c, skin), "gbmd_set_skin");
+  check(c, gbmd_set_precision(c, precision == "fp64" ? GBMD_PRECISION_FP64 : GBMD_PRECISION_MIXED),
+        "gbmd_set_precision");
+}
+
+// One compute_force call: the inner cells' particles into the context
+// (all of them when the count changed, else positions only: the library's
+// skin/2 displacement test decides a rebuild), zero_force_energy +
+// compute_force + force_to_accel on the device, then f = m a and ep back into
+// the cells (the graph's force_to_accel runs next).
+template <class GridT>
+void compute_and_store(gbmd_context* c, GridT& grid, const ParticleSpecies& species, Staging& s, size_t& uploaded,
+                       bool energy, bool virial) {
+  gather(grid, s);
+  if (s.n != uploaded) {
+    check(c, gbmd_upload_atoms(c, (int64_t)s.n, s.rx.data(), s.ry.data(), s.rz.data(), s.vx.data(), s.vy.data(),
+                               s.vz.data(), s.type.data(), s.id.data()),
+          "gbmd_upload_atoms");
+    uploaded = s.n;
+  } else {
+    check(c, gbmd_upload_positions(c, s.rx.data(), s.ry.data(), s.rz.data(), nullptr, nullptr, nullptr),
+          "gbmd_upload_positions");
+  }
+  check(c, gbmd_compute_forces(c, (energy ? GBMD_FORCE_ENERGY : 0) | (virial ? GBMD_FORCE_VIRIAL : 0)),
+        "gbmd_compute_forces");
+  check(c, gbmd_download(c, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, s.ax.data(), s.ay.data(),
+                         s.az.data(), energy ? s.ep.data() : nullptr, virial ? s.vir.data() : nullptr),
+        "gbmd_download");
+  auto cells = grid.cells();
+  for (size_t k = 0; k < s.n; ++k) {
+    const size_t cc = s.cell_of[k], p = s.slot_of[k];
+    const double m = species.at(s.type[k]).m_mass;
+    cells[cc][field::fx][p] = s.ax[k] * m;
+    cells[cc][field::fy][p] = s.ay[k] * m;
+    cells[cc][field::fz][p] = s.az[k] * m;
+    if (energy) cells[cc][field::ep][p] = s.ep[k];
+  }
+}
+
+// `parameters` of eam_alloy_force: the setfl file, as a scalar or {file: ...}
+// (eam_alloy.cpp L66-84).
+struct SetflRef {
+  std::string file;
+};
+
+// `parameters` of lj_multi_force: [{type_a, type_b, rcut, parameters:
+// {epsilon, sigma}}, ...] (pair_potential_force_op_multiparam.h L249-284).
+struct LJPairEntry {
+  std::string type_a, type_b;
+  double rcut = 0.0;
+  LennardJonesParms p;
+};
+struct LJPairList {
+  std::vector<LJPairEntry> pairs;
+};
+
 }  // namespace gb300
+}  // namespace exaStamp
+
+namespace YAML {
+template <>
+struct convert<exaStamp::gb300::SetflRef> {
+  static bool decode(const Node& node, exaStamp::gb300::SetflRef& v) {
+    if (node.IsScalar()) v.file = node.as<std::string>();
+    else if (node.IsMap() && node["file"]) v.file = node["file"].as<std::string>();
+    else return false;
+    return true;
+  }
+};
+template <>
+struct convert<exaStamp::gb300::LJPairList> {
+  static bool decode(const Node& node, exaStamp::gb300::LJPairList& v) {
+    if (!node.IsSequence()) return false;
+    for (auto pp : node) {
+      if (!pp.IsMap() || !pp["type_a"] || !pp["type_b"] || !pp["rcut"] || !pp["parameters"]) return false;
+      exaStamp::gb300::LJPairEntry e;
+      e.type_a = pp["type_a"].as<std::string>();
+      e.type_b = pp["type_b"].as<std::string>();
+      e.rcut = pp["rcut"].as<onika::physics::Quantity>().convert();
+      e.p = pp["parameters"].as<exaStamp::LennardJonesParms>();
+      v.pairs.push_back(e);
+    }
+    return true;
+  }
+};
+}  // namespace YAML
+
+namespace exaStamp {
+
+using StringVector = std::vector<std::string>;
+
+// lj_compute_force (pair_potential_impl.hxx L104-121): one species pair,
+// energy shifted by e(rcut) as the reference does (L373-377).
+template <class GridT>
+class Gb300LJForceNode : public OperatorNode {
+  ADD_SLOT(LennardJonesParms, parameters, INPUT, LennardJonesParms{});
+  ADD_SLOT(double, rcut, INPUT, REQUIRED);
+  ADD_SLOT(double, rcut_max, INPUT_OUTPUT, 0.0);
+  ADD_SLOT(exanb::GridChunkNeighbors, chunk_neighbors, INPUT, exanb::GridChunkNeighbors{}, DocString{"unused"});
+  ADD_SLOT(ParticleSpecies, species, INPUT, REQUIRED);
+  ADD_SLOT(std::string, type, INPUT, OPTIONAL);
+  ADD_SLOT(bool, ghost, INPUT, false);
+  ADD_SLOT(GridT, grid, INPUT_OUTPUT);
+  ADD_SLOT(Domain, domain, INPUT, REQUIRED);
+  ADD_SLOT(bool, trigger_thermo_state, INPUT, OPTIONAL);
+  ADD_SLOT(bool, compute_virial, INPUT, false);
+  ADD_SLOT(double, rcut_inc, INPUT, 1.0, DocString{"neighbour skin (global.rcut_inc)"});
+  ADD_SLOT(std::string, precision, INPUT, std::string{"mixed"}, DocString{"mixed or fp64"});
+  gb300::ContextPtr m_ctx;
+  gb300::Staging m_stage;
+  size_t m_uploaded = 0;
+
+ public:
+  inline void execute() override final {
+    *rcut_max = std::max(*rcut, *rcut_max);
+    if (grid->number_of_cells() == 0) return;
+    if (!m_ctx) {
+      gbmd_context* c = gb300::make_context(*domain, *species);
+      m_ctx.reset(c);
+      gb300::check(c, gbmd_set_lj(c, parameters->epsilon, parameters->sigma, *rcut), "gbmd_set_lj");
+      gb300::finish_setup(c, *rcut_inc, *precision);
+    }
+    const bool energy = trigger_thermo_state.has_value() && *trigger_thermo_state;
+    gb300::compute_and_store(m_ctx.get(), *grid, *species, m_stage, m_uploaded, energy, energy && *compute_virial);
+  }
+};
+
+// lj_multi_force (pair_potential_force_op_multiparam.h L57-118): per
+// species-pair (epsilon, sigma, rcut); pairs not listed take
+// common_parameters with the operator's rcut, or do not interact.
+template <class GridT>
+class Gb300LJMultiForceNode : public OperatorNode {
+  ADD_SLOT(LennardJonesParms, common_parameters, INPUT, OPTIONAL);
+  ADD_SLOT(gb300::LJPairList, parameters, INPUT, REQUIRED);
+  ADD_SLOT(double, rcut, INPUT, REQUIRED);
+  ADD_SLOT(double, rcut_max, INPUT_OUTPUT, 0.0);
+  ADD_SLOT(exanb::GridChunkNeighbors, chunk_neighbors, INPUT, exanb::GridChunkNeighbors{}, DocString{"unused"});
+  ADD_SLOT(ParticleSpecies, species, INPUT, REQUIRED);
+  ADD_SLOT(GridT, grid, INPUT_OUTPUT);
+  ADD_SLOT(Domain, domain, INPUT, REQUIRED);
+  ADD_SLOT(bool, trigger_thermo_state, INPUT, OPTIONAL);
+  ADD_SLOT(bool, compute_virial, INPUT, false);
+  ADD_SLOT(double, rcut_inc, INPUT, 1.0, DocString{"neighbour skin (global.rcut_inc)"});
+  ADD_SLOT(std::string, precision, INPUT, std::string{"mixed"}, DocString{"mixed or fp64"});
+  gb300::ContextPtr m_ctx;
+  gb300::Staging m_stage;
+  size_t m_uploaded = 0;
+
+ public:
+  inline void execute() override final {
+    double rmax = *rcut;
+    for (const auto& e : parameters->pairs) rmax = std::max(rmax, e.rcut);
+    *rcut_max = std::max(rmax, *rcut_max);
+    if (grid->number_of_cells() == 0) return;
+    if (!m_ctx) {
+      gbmd_context* c = gb300::make_context(*domain, *species);
+      m_ctx.reset(c);
+      const int nt = (int)species->size();
+      std::vector<double> eps(nt * nt, 0.0), sig(nt * nt, 1.0), rc(nt * nt, 0.0);
+      if (common_parameters.has_value())
+        for (int k = 0; k < nt * nt; ++k) {
+          eps[k] = common_parameters->epsilon;
+          sig[k] = common_parameters->sigma;
+          rc[k] = *rcut;
+        }
+      auto type_of = [&](const std::string& name) {
+        for (int t = 0; t < nt; ++t)
+          if (species->at(t).name() == name) return t;
+        fatal_error() << "gb300: unknown species " << name << std::endl;
+        return -1;
+      };
+      for (const auto& e : parameters->pairs) {
+        const int a = type_of(e.type_a), b = type_of(e.type_b);
+        for (int k : {a * nt + b, b * nt + a}) {
+          eps[k] = e.p.epsilon;
+          sig[k] = e.p.sigma;
+          rc[k] = e.rcut;
+        }
+      }
+      gb300::check(c, gbmd_set_lj_multi(c, nt, eps.data(), sig.data(), rc.data(), *rcut), "gbmd_set_lj_multi");
+      gb300::finish_setup(c, *rcut_inc, *precision);
+    }
+    const bool energy = trigger_thermo_state.has_value() && *trigger_thermo_state;
+    gb300::compute_and_store(m_ctx.get(), *grid, *species, m_stage, m_uploaded, energy, energy && *compute_virial);
+  }
+};
+
+// eam_alloy_force (eam_potential_multimat.cu L88-109): the three passes in
+// one call; the split-pass and Newton-3 forms are not offered.
+template <class GridT>
+class Gb300EamAlloyForceNode : public OperatorNode {
+  ADD_SLOT(ParticleSpecies, species, INPUT, REQUIRED);
+  ADD_SLOT(gb300::SetflRef, parameters, INPUT, REQUIRED, DocString{"setfl file (scalar or {file: ...})"});
+  ADD_SLOT(StringVector, types, INPUT, StringVector{});
+  ADD_SLOT(double, rcut, INPUT, REQUIRED);
+  ADD_SLOT(double, rcut_max, INPUT_OUTPUT, 0.0);
+  ADD_SLOT(double, ghost_dist_max, INPUT_OUTPUT, 0.0);
+  ADD_SLOT(exanb::GridChunkNeighbors, chunk_neighbors, INPUT, exanb::GridChunkNeighbors{}, DocString{"unused"});
+  ADD_SLOT(GridT, grid, INPUT_OUTPUT);
+  ADD_SLOT(Domain, domain, INPUT, REQUIRED);
+  ADD_SLOT(bool, trigger_thermo_state, INPUT, OPTIONAL);
+  ADD_SLOT(bool, compute_virial, INPUT, false);
+  ADD_SLOT(bool, eam_rho, INPUT, true);
+  ADD_SLOT(bool, eam_rho2emb, INPUT, true);
+  ADD_SLOT(bool, eam_ghost, INPUT, true);
+  ADD_SLOT(bool, eam_force, INPUT, true);
+  ADD_SLOT(bool, eam_symmetry, INPUT, false);
+  ADD_SLOT(double, rcut_inc, INPUT, 1.0, DocString{"neighbour skin (global.rcut_inc)"});
+  ADD_SLOT(std::string, precision, INPUT, std::string{"mixed"}, DocString{"mixed or fp64"});
+  gb300::ContextPtr m_ctx;
+  gb300::Staging m_stage;
+  size_t m_uploaded = 0;
+
+ public:
+  inline void execute() override final {
+    *rcut_max = std::max(*rcut, *rcut_max);
+    *ghost_dist_max = std::max(*ghost_dist_max, 2.0 * (*rcut));
+    if (grid->number_of_cells() == 0) return;
+    if (!(*eam_rho && *eam_rho2emb && *eam_force) || *eam_symmetry)
+      fatal_error() << "gb300_eam_alloy_force: only the fused three-pass full-list form is offered" << std::endl;
+    if (!m_ctx) {
+      gbmd_context* c = gb300::make_context(*domain, *species);
+      m_ctx.reset(c);
+      gb300::check(c,
+                   gbmd_load_setfl(c, onika::data_file_path(parameters->file).c_str(), *rcut,
+                                   EXASTAMP_CONST_QUANTITY(1. * eV * ang), EXASTAMP_CONST_QUANTITY(1.0 * eV)),
+                   "gbmd_load_setfl");
+      gb300::finish_setup(c, *rcut_inc, *precision);
+    }
+    const bool energy = trigger_thermo_state.has_value() && *trigger_thermo_state;
+    gb300::compute_and_store(m_ctx.get(), *grid, *species, m_stage, m_uploaded, energy, energy && *compute_virial);
+  }
+};
+
+// johnson_force (johnson.h L28-176 through the mono-material two-pass
+// template, eam_potential.cu L69-193).
+template <class GridT>
+class Gb300JohnsonForceNode : public OperatorNode {
+  ADD_SLOT(EamJohnsonParameters, parameters, INPUT, REQUIRED);
+  ADD_SLOT(double, rcut, INPUT, REQUIRED);
+  ADD_SLOT(double, rcut_max, INPUT_OUTPUT, 0.0);
+  ADD_SLOT(double, ghost_dist_max, INPUT_OUTPUT, 0.0);
+  ADD_SLOT(exanb::GridChunkNeighbors, chunk_neighbors, INPUT, exanb::GridChunkNeighbors{}, DocString{"unused"});
+  ADD_SLOT(ParticleSpecies, species, INPUT, REQUIRED);
+  ADD_SLOT(GridT, grid, INPUT_OUTPUT);
+  ADD_SLOT(Domain, domain, INPUT, REQUIRED);
+  ADD_SLOT(bool, trigger_thermo_state, INPUT, OPTIONAL);
+  ADD_SLOT(bool, compute_virial, INPUT, false);
+  ADD_SLOT(double, rcut_inc, INPUT, 1.0, DocString{"neighbour skin (global.rcut_inc)"});
+  ADD_SLOT(std::string, precision, INPUT, std::string{"mixed"}, DocString{"mixed or fp64"});
+  gb300::ContextPtr m_ctx;
+  gb300::Staging m_stage;
+  size_t m_uploaded = 0;
+
+ public:
+  inline void execute() override final {
+    *rcut_max = std::max(*rcut, *rcut_max);
+    *ghost_dist_max = std::max(*ghost_dist_max, 2.0 * (*rcut));
+    if (grid->number_of_cells() == 0) return;
+    if (!m_ctx) {
+      gbmd_context* c = gb300::make_context(*domain, *species);
+      m_ctx.reset(c);
+      const EamJohnsonParameters& q = *parameters;
+      const double jp[19] = {q.re, q.fe, q.rhoe, q.alpha, q.beta, q.A,   q.B,  q.kappa, q.lambda, q.Fn0,
+                             q.Fn1, q.Fn2, q.Fn3, q.F0, q.F1, q.F2, q.F3, q.Fo, q.eta};
+      gb300::check(c, gbmd_set_eam_johnson(c, jp, *rcut), "gbmd_set_eam_johnson");
+      gb300::finish_setup(c, *rcut_inc, *precision);
+    }
+    const bool energy = trigger_thermo_state.has_value() && *trigger_thermo_state;
+    gb300::compute_and_store(m_ctx.get(), *grid, *species, m_stage, m_uploaded, energy, energy && *compute_virial);
+  }
+};
 
 template <class GridT>
 class Gb300ForceNode : public OperatorNode {
@@ -120,17 +416,8 @@ class Gb300ForceNode : public OperatorNode {
       *ghost_dist_max = std::max(*ghost_dist_max, 2.0 * (*rcut));
     if (grid->number_of_cells() == 0) return;  // pre-initialisation pass publishing rcut_max
     if (!m_ctx) {
-      gbmd_context* c = nullptr;
-      if (gbmd_create(&c, 0, parallel_execution_context()->gpu_stream()) != GBMD_OK)
-        fatal_error() << "gb300: no GPU context" << std::endl;
+      gbmd_context* c = gb300::make_context(*domain, *species);
       m_ctx.reset(c);
-      const Vec3d lo = domain->bounds().bmin, hi = domain->bounds().bmax;
-      const double blo[3] = {lo.x, lo.y, lo.z}, bhi[3] = {hi.x, hi.y, hi.z};
-      const int per[3] = {domain->periodic_boundary_x(), domain->periodic_boundary_y(), domain->periodic_boundary_z()};
-      gb300::check(c, gbmd_set_box(c, blo, bhi, per), "gbmd_set_box");
-      std::vector<double> m(species->size());
-      for (size_t t = 0; t < m.size(); ++t) m[t] = species->at(t).m_mass;
-      gb300::check(c, gbmd_set_species(c, (int)m.size(), m.data()), "gbmd_set_species");
       if (*potential == "lj")
         gb300::check(c, gbmd_set_lj(c, *epsilon, *sigma, *rcut), "gbmd_set_lj");
       else if (*potential == "eam_alloy")
@@ -146,46 +433,34 @@ class Gb300ForceNode : public OperatorNode {
         gb300::check(c, gbmd_set_eam_johnson(c, jp, *rcut), "gbmd_set_eam_johnson");
       } else
         fatal_error() << "gb300: unsupported potential " << *potential << std::endl;
-      gb300::check(c, gbmd_set_skin(c, *rcut_inc), "gbmd_set_skin");
-      gb300::check(c, gbmd_set_precision(c, *precision == "fp64" ? GBMD_PRECISION_FP64 : GBMD_PRECISION_MIXED),
-                   "gbmd_set_precision");
-    }
-    gbmd_context* c = m_ctx.get();
-    gb300::Staging& s = m_stage;
-    gb300::gather(*grid, s);
-    if (s.n != m_uploaded) {
-      gb300::check(c, gbmd_upload_atoms(c, (int64_t)s.n, s.rx.data(), s.ry.data(), s.rz.data(), s.vx.data(),
-                                        s.vy.data(), s.vz.data(), s.type.data(), s.id.data()),
-                   "gbmd_upload_atoms");
-      m_uploaded = s.n;
-    } else {
-      gb300::check(c, gbmd_upload_positions(c, s.rx.data(), s.ry.data(), s.rz.data(), nullptr, nullptr, nullptr),
-                   "gbmd_upload_positions");
+      gb300::finish_setup(c, *rcut_inc, *precision);
     }
     const bool energy = trigger_thermo_state.has_value() && *trigger_thermo_state;
-    const bool virial = energy && *compute_virial;
-    gb300::check(c, gbmd_compute_forces(c, (energy ? GBMD_FORCE_ENERGY : 0) | (virial ? GBMD_FORCE_VIRIAL : 0)),
-                 "gbmd_compute_forces");
-    gb300::check(c, gbmd_download(c, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, s.ax.data(), s.ay.data(),
-                                  s.az.data(), energy ? s.ep.data() : nullptr, virial ? s.vir.data() : nullptr),
-                 "gbmd_download");
-    auto cells = grid->cells();
-    for (size_t k = 0; k < s.n; ++k) {
-      const size_t cc = s.cell_of[k], p = s.slot_of[k];
-      const double m = species->at(s.type[k]).m_mass;
-      cells[cc][field::fx][p] = s.ax[k] * m;  // force_to_accel runs next in the graph
-      cells[cc][field::fy][p] = s.ay[k] * m;
-      cells[cc][field::fz][p] = s.az[k] * m;
-      if (energy) cells[cc][field::ep][p] = s.ep[k];
-    }
+    gb300::compute_and_store(m_ctx.get(), *grid, *species, m_stage, m_uploaded, energy, energy && *compute_virial);
   }
 };
 
 template <class GridT>
 using Gb300ForceNodeTmpl = Gb300ForceNode<GridT>;
 
+template <class GridT>
+using Gb300LJForceTmpl = Gb300LJForceNode<GridT>;
+template <class GridT>
+using Gb300LJMultiForceTmpl = Gb300LJMultiForceNode<GridT>;
+template <class GridT>
+using Gb300EamAlloyForceTmpl = Gb300EamAlloyForceNode<GridT>;
+template <class GridT>
+using Gb300JohnsonForceTmpl = Gb300JohnsonForceNode<GridT>;
+
 ONIKA_AUTORUN_INIT(gb300_md_ops) {
   OperatorNodeFactory::instance()->register_factory("gb300_force", make_grid_variant_operator<Gb300ForceNodeTmpl>);
+  OperatorNodeFactory::instance()->register_factory("gb300_lj_force", make_grid_variant_operator<Gb300LJForceTmpl>);
+  OperatorNodeFactory::instance()->register_factory("gb300_lj_multi_force",
+                                                    make_grid_variant_operator<Gb300LJMultiForceTmpl>);
+  OperatorNodeFactory::instance()->register_factory("gb300_eam_alloy_force",
+                                                    make_grid_variant_operator<Gb300EamAlloyForceTmpl>);
+  OperatorNodeFactory::instance()->register_factory("gb300_johnson_force",
+                                                    make_grid_variant_operator<Gb300JohnsonForceTmpl>);
 }
 
 }  // namespace exaStamp
