@@ -245,21 +245,23 @@ __device__ __forceinline__ void lj_atom(const PairArgs& A, const LJF& P, const L
       const uint32_t j = ent[q] & GBMD_IDX_MASK;
       const GeomF G = geom_f(ent[q], pj[q], pi, A.g);
       float sig2, eps24, eps4, ecut, rlo, rhi;
-      double rcp = 0.0, rc2 = P.rc2;
+      int pid = 0;
       if (MULTI) {
-        const int pid = ti * ntypes + __float_as_int(pj[q].w);
+        pid = ti * ntypes + __float_as_int(pj[q].w);
         const float4 a = tab.a[pid];
         const float2 b = tab.b[pid];
         sig2 = a.x; eps24 = a.y; eps4 = a.z; ecut = a.w; rlo = b.x; rhi = b.y;
-        rcp = tab.r[pid];
-        rc2 = rcmax2;
       } else {
         sig2 = P.sig2; eps24 = P.eps24; eps4 = P.eps4; ecut = P.ecut; rlo = P.rc2lo; rhi = P.rc2hi;
       }
       bool in = G.d2 < rlo;
-      if (!in && G.d2 <= rhi && L.valid(r, q))
-        in = exact_inside(A.posd, i, j, ent[q] >> GBMD_IDX_BITS, cp, A.g, rc2, rcp);
-      const float r2i = __frcp_rn(G.d2);
+      if (!in && G.d2 <= rhi && L.valid(r, q))  // rare: the FP64 per-pair cutoff only here
+        in = exact_inside(A.posd, i, j, ent[q] >> GBMD_IDX_BITS, cp, A.g, MULTI ? rcmax2 : P.rc2,
+                          MULTI ? tab.r[pid] : 0.0);
+      // hardware reciprocal (within 1 ulp): the pair term's error budget is
+      // ~1e-7 relative against a 1e-5 force tolerance
+      float r2i;
+      asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r2i) : "f"(G.d2));
       const float s2 = sig2 * r2i;
       const float s6 = s2 * s2 * s2;
       const float s12 = s6 * s6;
