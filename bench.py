@@ -436,10 +436,18 @@ def main():
     etot = th[:, 21:24].sum(1) + th[:, 24]
     drift = (etot[-1] - etot[0]) / s.n / max(args.steps, 1) * 1000.0
     kernels_per_step = 2 if w["kind"] == "eam" else 1
-    # rebuild chain: wrap/bin, 3 scan kernels, scatter, rank, gather, posf,
-    # list build; with the trigger 14 gated launches every step (displacement
-    # test, 2 fills, the chain, copy-back, reference positions)
-    gpu_launches = kernels_per_step * args.steps + 2 * (args.steps // thermo_every if thermo_every else 0)
+    # Launches of the timed gbmd_run_nve call: the pair kernel(s) once per
+    # step and once more for the energies of step 0; the thermo reduction (2)
+    # at step 0 and every thermo_every steps; the standalone first half at
+    # the start and after every thermo step but the last; the rebuild chain
+    # (wrap/bin, 3 scan kernels, scatter, rank, gather, posf, list build) per
+    # rebuild, or with the trigger 14 gated launches every step (displacement
+    # test, 2 fills, the chain, copy-back, reference positions).
+    n_thermo = args.steps // thermo_every if thermo_every else 0
+    last_is_thermo = bool(thermo_every) and args.steps % thermo_every == 0
+    gpu_launches = kernels_per_step * (args.steps + (1 if thermo_every else 0))
+    gpu_launches += 2 * (n_thermo + (1 if thermo_every else 0))
+    gpu_launches += 1 + n_thermo - (1 if last_is_thermo else 0)
     gpu_launches += 14 * args.steps if R < 0 else 9 * rebuilds
 
     out = {"metric": "atom-timesteps/s", "value": value, "unit": "atom-timesteps/s", "n_gpus": ws,
