@@ -459,3 +459,54 @@ def test_run_nve_host_matches_separate_calls(gpu, pinned, nsteps, R):
         ctx.run_nve_host(st, nsteps, 0.005, rebuild_every=R)
     for k in keys:
         assert np.array_equal(st[k], ref[k]), k
+
+
+def test_upload_argument_errors(gpu):
+    """The reference aborts on bad input; the ABI returns a status and the
+    context stays usable: too many atoms (checked before any array is read),
+    a type outside the species table, a negative count."""
+    x = np.zeros(4)
+    with gpu.Context(0) as ctx:
+        ctx.set_box(np.zeros(3), np.full(3, 10.0))
+        ctx.set_species(np.array([1.0]))
+        L, h, p = ctx._L, ctx.h, x.ctypes.data
+        assert L.gbmd_upload_atoms(h, (1 << 26) + 1, p, p, p, None, None, None, None, None) == 9
+        bad = np.array([0, 1, 0, 0], np.uint8)
+        assert L.gbmd_upload_atoms(h, 4, p, p, p, None, None, None, bad.ctypes.data, None) == 1
+        assert L.gbmd_upload_atoms(h, -1, p, p, p, None, None, None, None, None) == 1
+        s = _jitter(S.lj_fcc(ncell=3, seed=2), 0.05, 2)
+        ctx.upload_system(s)
+        ctx.set_lj(1.0, 1.0, 2.5)
+        ctx.set_skin(0.3)
+        ctx.compute_forces()
+        assert np.isfinite(ctx.download(("ax",))["ax"]).all()
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_list_regrows_for_a_dense_cluster(gpu, oracle, mixed):
+    """A dense FCC cluster in a dilute gas: the first per-atom capacity is
+    sized from the mean density, the cluster's atoms overflow it, the list is
+    regrown and rebuilt; the pair set stays bit-exact and the forces match."""
+    rng = np.random.default_rng(21)
+    L = 24.0
+    pos, _, _ = S.lattice(5, 5, 5, 1.5874, S.FCC_BASIS)   # 500 atoms at rho ~1.0
+    pos = pos + 8.0
+    gas = rng.uniform(0, L, (300, 3))
+    gas = gas[np.any((gas < 6.5) | (gas > 17.5), axis=1)]   # outside the cluster's cube
+    P = np.concatenate([pos, gas])
+    n = len(P)
+    s = S.System(*(np.ascontiguousarray(P[:, k]) for k in range(3)), np.zeros(n), np.zeros(n), np.zeros(n),
+                 np.zeros(n, np.uint8), rng.permutation(n).astype(np.uint64), np.zeros(3), np.full(3, L),
+                 np.array([1.0]))
+    s = _jitter(s, 0.03, 21)
+    ref, (x, y, z), nl = oracle_lists(oracle, s, 2.8)
+    assert max(len(v) for v in ref.values()) > 1.35 * 4.18879 * 2.8 ** 3 * n / L ** 3 + 16
+    fx, fy, fz, ep, _ = oracle.lj_force(x, y, z, nl, s.L, 1.0, 1.0, 2.5)
+    F = np.stack([fx, fy, fz], 1)
+    with gpu_ctx(gpu, s, LJ, 0.3, mixed=mixed) as ctx:
+        ctx.compute_forces(energy=True)
+        got = per_atom_lists(ctx.export_pairs())
+        d = ctx.download(("ax", "ay", "az"))
+    assert got == ref
+    G = np.stack([d["ax"], d["ay"], d["az"]], 1)
+    assert rel_rms(G, F) < (FP64_TOL if not mixed else MIXED_FORCE_TOL)
