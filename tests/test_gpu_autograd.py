@@ -52,7 +52,7 @@ def test_lj_autograd_gradient(gpu, oracle, mixed):
     assert np.all(np.abs(g - fd) < fd_tol * np.abs(fd)), (g, fd)
     tol = 1e-9 if not mixed else 1e-4
     assert np.all(np.abs(g - g_ref) < tol * np.abs(g_ref)), (g, g_ref)
-    assert abs(float(loss) - loss_ref) < (1e-9 if not mixed else 1e-4) * loss_ref
+    assert abs(float(loss.detach()) - loss_ref) < (1e-9 if not mixed else 1e-4) * loss_ref
 
 
 def test_eam_autograd_gradient(gpu, oracle):
