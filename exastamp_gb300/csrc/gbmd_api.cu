@@ -210,15 +210,15 @@ __global__ void k_displ_over(int64_t n, const double* __restrict__ x, const doub
   if (d2 > thr2) *flag = 1;
 }
 
-// reference positions after a gated rebuild; block 0 counts the rebuild
+// reference positions after a gated rebuild; thread 0 counts the rebuild
 __global__ void k_copy_rref_gated(int64_t n, const double* __restrict__ r, double* __restrict__ rref, int64_t cap,
                                   const int* __restrict__ gate, int* __restrict__ count) {
-  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (!*gate) return;
-  if (p == 0) atomicAdd(count, 1);
-  if (p >= n) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(count, 1);
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
 #pragma unroll
-  for (int d = 0; d < 3; ++d) rref[d * cap + p] = r[d * cap + p];
+    for (int d = 0; d < 3; ++d) rref[d * cap + p] = r[d * cap + p];
+  }
 }
 
 static inline unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
@@ -282,8 +282,8 @@ static int rebuild_if_displaced(gbmd_context* c) {
                                                         gate);
   int rc = rebuild(c, false, gate);
   if (rc) return rc;
-  k_copy_rref_gated<<<nblk(c->n, 256), 256, 0, c->stream>>>(c->n, c->rbuf[c->cur], c->rref, c->cap, gate,
-                                                             c->d_err + ERRW_REBUILDS);
+  k_copy_rref_gated<<<chain_blocks(c, c->n, 256, gate, 8), 256, 0, c->stream>>>(c->n, c->rbuf[c->cur], c->rref,
+                                                                                c->cap, gate, c->d_err + ERRW_REBUILDS);
   return GBMD_OK;
 }
 
@@ -362,7 +362,8 @@ int gbmd_create(gbmd_context** out, int device, void* stream) {
   if (cudaMalloc(&c->d_err, sizeof(int) * 8) != cudaSuccess ||
       cudaMallocHost(&c->h_err, sizeof(int) * 8) != cudaSuccess ||
       cudaMalloc(&c->d_thermo, sizeof(double) * 27) != cudaSuccess ||
-      cudaMallocHost(&c->h_thermo, sizeof(double) * 27) != cudaSuccess) {
+      cudaMallocHost(&c->h_thermo, sizeof(double) * 27) != cudaSuccess ||
+      cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
     gbmd_destroy(c);
     return GBMD_ERR_CUDA;
   }

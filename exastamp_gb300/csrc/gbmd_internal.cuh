@@ -100,6 +100,7 @@ struct gbmd_context {
   cudaStream_t stream = nullptr;
   // copy streams for host<->device staging (created lazily), forked from and
   // joined back into `stream` with events
+  int nsm = 0;                  // SMs of the device
   double* stage_r = nullptr;    // 3 x cap: r in caller order, copied out during a force pass
   double* host_r_out[3] = {nullptr, nullptr, nullptr};  // gbmd_run_nve_host's r arrays
   bool r_copy_pending = false;  // copy_join[0] marks the end of that copy
@@ -236,6 +237,9 @@ int grid_dims(const double lo[3], const double hi[3], double R, int nc[3]);
 // while it holds 0, and keeps the buffer indices unchanged (see gbmd_neighbors.cu)
 int rebuild(gbmd_context* c, bool check_capacity, const int* gate = nullptr);
 void launch_posf(gbmd_context* c, const int* gate = nullptr);
+// blocks for a rebuild-chain kernel over `items` (per_block per block): all
+// of them ungated, at most per_sm per SM when gated (grid-stride kernels)
+unsigned chain_blocks(const gbmd_context* c, int64_t items, int per_block, const int* gate, int per_sm);
 int export_pairs(gbmd_context* c, int64_t cap, uint64_t* id_i, uint64_t* id_j, int8_t* img, int64_t* count);
 
 // forces (gbmd_forces.cu)

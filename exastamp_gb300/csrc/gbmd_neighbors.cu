@@ -53,8 +53,8 @@ struct BoxArgs {
 __global__ void k_wrap_bin(int64_t n, double* __restrict__ x, double* __restrict__ y,
                            double* __restrict__ z, BoxArgs b, int32_t* __restrict__ cell_of,
                            int32_t* __restrict__ cell_count, int* __restrict__ err, const int* __restrict__ gate) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n || (gate && !*gate)) return;
+  if (gate && !*gate) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
   double* r[3] = {x, y, z};
   int c[3];
   bool lost = false;
@@ -76,6 +76,7 @@ __global__ void k_wrap_bin(int64_t n, double* __restrict__ x, double* __restrict
   const int32_t lin = (int32_t)(((int64_t)c[2] * b.nc[1] + c[1]) * b.nc[0] + c[0]);
   cell_of[i] = lin;
   atomicAdd(&cell_count[lin], 1);
+  }
 }
 
 // --- exclusive scan (256 threads x 8 items per block) ----------------------
@@ -185,20 +186,22 @@ static int scan(gbmd_context* c, const int32_t* in, int32_t* out, int64_t n, con
 
 __global__ void k_scatter(int64_t n, const int32_t* __restrict__ cell_of, const int32_t* __restrict__ cstart,
                           int32_t* __restrict__ fill, int32_t* __restrict__ order, const int* __restrict__ gate) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n || (gate && !*gate)) return;
-  const int32_t cl = cell_of[i];
-  const int32_t slot = cstart[cl] + atomicAdd(&fill[cl], 1);
-  order[slot] = (int32_t)i;
+  if (gate && !*gate) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t cl = cell_of[i];
+    const int32_t slot = cstart[cl] + atomicAdd(&fill[cl], 1);
+    order[slot] = (int32_t)i;
+  }
 }
 
 // one warp per cell: rank by (id, upload index) -> src[new] = old
 __global__ void k_cell_rank(int64_t ncells, const int32_t* __restrict__ cstart, const int32_t* __restrict__ order,
                             const uint64_t* __restrict__ id, const int32_t* __restrict__ user,
                             int32_t* __restrict__ src, const int* __restrict__ gate) {
-  const int64_t cell = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (cell >= ncells || (gate && !*gate)) return;
+  if (gate && !*gate) return;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t cell = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; cell < ncells; cell += warps) {
   const int beg = cstart[cell], m = cstart[cell + 1] - beg;
   if (m <= 32) {
     // keys in registers, compared through shuffles
@@ -216,7 +219,7 @@ __global__ void k_cell_rank(int64_t ncells, const int32_t* __restrict__ cstart, 
       rank += (kb < ka) || (kb == ka && ub < ua);
     }
     if (lane < m) src[beg + rank] = a;
-    return;
+    continue;
   }
   for (int e = lane; e < m; e += 32) {
     const int32_t a = order[beg + e];
@@ -229,6 +232,7 @@ __global__ void k_cell_rank(int64_t ncells, const int32_t* __restrict__ cstart, 
       rank += (kb < ka) || (kb == ka && user[b] < ua);
     }
     src[beg + rank] = a;
+  }
   }
 }
 
@@ -249,8 +253,8 @@ struct GatherArgs {
 __global__ void k_gather(int64_t n, const int32_t* __restrict__ src, GatherArgs g,
                          const int32_t* __restrict__ cell_of, int ncx, int ncy,
                          int32_t* __restrict__ cellpack, const int* __restrict__ gate) {
-  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p >= n || (gate && !*gate)) return;
+  if (gate && !*gate) return;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
   const int64_t o = src[p];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
@@ -265,13 +269,14 @@ __global__ void k_gather(int64_t n, const int32_t* __restrict__ src, GatherArgs 
   const int32_t lin = cell_of[o];
   const int cx = lin % ncx, cy = (lin / ncx) % ncy, cz = lin / (ncx * ncy);
   cellpack[p] = cx | (cy << 10) | (cz << 20);
+  }
 }
 
 // gated variant only: the sorted state, gathered into the spare buffers, is
 // copied back so the current buffer index does not change
 __global__ void k_copy_back(int64_t n, GatherArgs g, const int* __restrict__ gate) {
-  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p >= n || !*gate) return;
+  if (!*gate) return;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
   double* r0 = const_cast<double*>(g.r0);
   double* v0 = const_cast<double*>(g.v0);
   double* a0 = const_cast<double*>(g.a0);
@@ -285,20 +290,20 @@ __global__ void k_copy_back(int64_t n, GatherArgs g, const int* __restrict__ gat
   const_cast<uint64_t*>(g.i0)[p] = g.i1[p];
   const_cast<int32_t*>(g.u0)[p] = g.u1[p];
   const_cast<double*>(g.ep0)[p] = g.ep1[p];
+  }
 }
 
 __global__ void k_fill_gated(int32_t* __restrict__ p, int64_t n, const int* __restrict__ gate) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n || !*gate) return;
-  p[i] = 0;
+  if (!*gate) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = 0;
 }
 
 __global__ void k_posf(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
                        const double* __restrict__ z, const uint8_t* __restrict__ type,
                        const int32_t* __restrict__ cellpack, Grid g, float4* __restrict__ pf,
                        double4_32a* __restrict__ pd, const int* __restrict__ gate) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n || (gate && !*gate)) return;
+  if (gate && !*gate) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
   const int cp = cellpack[i];
   const double cx = (double)(cp & 1023), cy = (double)((cp >> 10) & 1023), cz = (double)(cp >> 20);
   const double xi = x[i], yi = y[i], zi = z[i];
@@ -306,6 +311,7 @@ __global__ void k_posf(int64_t n, const double* __restrict__ x, const double* __
   pf[i] = make_float4((float)(xi - cx * g.h[0] - g.lo[0]), (float)(yi - cy * g.h[1] - g.lo[1]),
                       (float)(zi - cz * g.h[2] - g.lo[2]), __int_as_float(t));
   pd[i] = make_double4_32a(xi, yi, zi, (double)t);
+  }
 }
 
 // FP64 re-test of a candidate whose FP32 d2 fell within 2^-12 of R^2.  Out of
@@ -513,15 +519,23 @@ __device__ __forceinline__ int build_walk(const BuildCell& B, const float4* __re
 // R^2 (1 - 2^-12); flagged atoms (a few per cent) rescan their row, re-test
 // those entries in FP64 and compact, so the walk has no call and no
 // divergent branch.
+template <bool LOOP>
 __global__ void __launch_bounds__(BUILD_WARPS * 32) k_build_list_cells(
     int64_t ncells, const float4* __restrict__ pf, const double* __restrict__ x, const double* __restrict__ y,
     const double* __restrict__ z, const int32_t* __restrict__ cstart, Grid g, double R2, float R2lo, float R2hi,
     uint32_t* __restrict__ nbr, int32_t* __restrict__ nnb, int maxnb, int W, int64_t stride,
     int* __restrict__ err, const int* __restrict__ gate) {
-  const int64_t cell = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (cell >= ncells || (gate && !*gate)) return;  // uniform per warp
+  if (gate && !*gate) return;
   const unsigned FULL = 0xffffffffu;
+  __shared__ float4 stage_all[BUILD_WARPS][BUILD_CHUNK + 1];
+  float4* stage = stage_all[threadIdx.x >> 5];
+  int wsh = 0;
+  while ((1 << wsh) < W) ++wsh;
+  // one cell per warp (LOOP: and per iteration, striding over the cells;
+  // used by the gated launch with its capped grid)
+  const int64_t warps = LOOP ? (int64_t)gridDim.x * (blockDim.x >> 5) : ncells;
+  for (int64_t cell = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); cell < ncells; cell += warps) {
   BuildCell B;
   B.cx = (int)(cell % g.nc[0]);
   B.cy = (int)((cell / g.nc[0]) % g.nc[1]);
@@ -553,10 +567,6 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32) k_build_list_cells(
   B.total = __shfl_sync(FULL, incl, 26);
   B.hb = cstart[cell];
   B.nh = cstart[cell + 1] - B.hb;
-  int wsh = 0;
-  while ((1 << wsh) < W) ++wsh;
-  __shared__ float4 stage_all[BUILD_WARPS][BUILD_CHUNK + 1];
-  float4* stage = stage_all[threadIdx.x >> 5];
   int warp_max;
   if (B.nh <= 16)
     warp_max = build_walk<16>(B, pf, x, y, z, g, R2, R2lo, R2hi, nbr, nnb, maxnb, W, wsh, stride, err, stage, lane);
@@ -565,14 +575,29 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32) k_build_list_cells(
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) warp_max = max(warp_max, __shfl_xor_sync(FULL, warp_max, o));
   if (lane == 0 && warp_max > 0) atomicMax(&err[ERRW_MAXNB], warp_max);
+  __syncwarp();  // the next cell restages this warp's buffer
+  }
 }
 
 static inline unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
 
+// Blocks of a rebuild-chain launch.  Ungated launches cover the data once;
+// gated ones (launched every step, mostly to find the gate closed) get at most
+// per_sm blocks per SM (no more than fit at once) and stride over the data,
+// so a closed gate costs a few microseconds instead of a full grid of empty
+// blocks.
+unsigned chain_blocks(const gbmd_context* c, int64_t items, int per_block, const int* gate, int per_sm) {
+  const unsigned full = nblk(items, per_block);
+  if (!gate) return full;
+  const unsigned cap = (unsigned)(per_sm * (c->nsm > 0 ? c->nsm : 1));
+  return full < cap ? full : cap;
+}
+
 void launch_posf(gbmd_context* c, const int* gate) {
   if (c->n == 0) return;
-  k_posf<<<nblk(c->n, 256), 256, 0, c->stream>>>(c->n, c->X(), c->Y(), c->Z(), c->TYPE(), c->cellpack,
-                                                  c->grid, c->POSF(), c->POSD(), gate);
+  k_posf<<<chain_blocks(c, c->n, 256, gate, 8), 256, 0, c->stream>>>(c->n, c->X(), c->Y(), c->Z(), c->TYPE(),
+                                                                   c->cellpack, c->grid, c->POSF(), c->POSD(),
+                                                                   gate);
 }
 
 static int build_list(gbmd_context* c, const int* gate) {
@@ -592,9 +617,15 @@ static int build_list(gbmd_context* c, const int* gate) {
   }
   c->npad = npad;
   if (!gate) GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_MAXNB, 0, sizeof(int), c->stream));
-  k_build_list_cells<<<nblk(c->grid.ncells, BUILD_WARPS), 32 * BUILD_WARPS, 0, c->stream>>>(
-      c->grid.ncells, c->POSF(), c->X(), c->Y(), c->Z(), c->cell_start, c->grid, R2, R2lo, R2hi, c->nbr, c->nnb,
-      c->maxnb, W, stride, c->d_err, gate);
+  if (gate)  // capped grid striding over the cells (five blocks per SM fit)
+    k_build_list_cells<true><<<chain_blocks(c, c->grid.ncells, BUILD_WARPS, gate, 5), 32 * BUILD_WARPS, 0,
+                                c->stream>>>(c->grid.ncells, c->POSF(), c->X(), c->Y(), c->Z(), c->cell_start,
+                                             c->grid, R2, R2lo, R2hi, c->nbr, c->nnb, c->maxnb, W, stride,
+                                             c->d_err, gate);
+  else
+    k_build_list_cells<false><<<nblk(c->grid.ncells, BUILD_WARPS), 32 * BUILD_WARPS, 0, c->stream>>>(
+        c->grid.ncells, c->POSF(), c->X(), c->Y(), c->Z(), c->cell_start, c->grid, R2, R2lo, R2hi, c->nbr, c->nnb,
+        c->maxnb, W, stride, c->d_err, nullptr);
   return GBMD_OK;
 }
 
@@ -643,17 +674,20 @@ int rebuild(gbmd_context* c, bool check_capacity, const int* gate) {
   const int64_t n = c->n;
   cudaStream_t s = c->stream;
   auto zero_fill = [&]() -> int {
-    if (gate) k_fill_gated<<<nblk(g.ncells + 1, 256), 256, 0, s>>>(c->cell_fill, g.ncells + 1, gate);
+    if (gate) k_fill_gated<<<chain_blocks(c, g.ncells + 1, 256, gate, 8), 256, 0, s>>>(c->cell_fill, g.ncells + 1, gate);
     else GBMD_CUDA(c, cudaMemsetAsync(c->cell_fill, 0, sizeof(int32_t) * (g.ncells + 1), s));
     return GBMD_OK;
   };
   int rc = zero_fill();
   if (rc) return rc;
-  k_wrap_bin<<<nblk(n, 256), 256, 0, s>>>(n, c->X(), c->Y(), c->Z(), b, c->cell_of, c->cell_fill, c->d_err, gate);
+  k_wrap_bin<<<chain_blocks(c, n, 256, gate, 8), 256, 0, s>>>(n, c->X(), c->Y(), c->Z(), b, c->cell_of, c->cell_fill,
+                                                            c->d_err, gate);
   if ((rc = scan(c, c->cell_fill, c->cell_start, g.ncells, gate))) return rc;
   if ((rc = zero_fill())) return rc;
-  k_scatter<<<nblk(n, 256), 256, 0, s>>>(n, c->cell_of, c->cell_start, c->cell_fill, c->order, gate);
-  k_cell_rank<<<nblk(g.ncells * 32, 256), 256, 0, s>>>(g.ncells, c->cell_start, c->order, c->ID(), c->USER(),
+  k_scatter<<<chain_blocks(c, n, 256, gate, 8), 256, 0, s>>>(n, c->cell_of, c->cell_start, c->cell_fill, c->order,
+                                                           gate);
+  k_cell_rank<<<chain_blocks(c, g.ncells * 32, 256, gate, 8), 256, 0, s>>>(g.ncells, c->cell_start, c->order, c->ID(),
+                                                                       c->USER(),
                                                         c->src, gate);
   GatherArgs ga;
   const int o = c->cur, os = c->cur_s;
@@ -665,9 +699,10 @@ int rebuild(gbmd_context* c, bool check_capacity, const int* gate) {
   ga.u0 = c->userb[os]; ga.u1 = c->userb[os ^ 1];
   ga.ep0 = c->ep; ga.ep1 = c->stage;
   ga.cap = c->cap;
-  k_gather<<<nblk(n, 256), 256, 0, s>>>(n, c->src, ga, c->cell_of, g.nc[0], g.nc[1], c->cellpack, gate);
+  k_gather<<<chain_blocks(c, n, 256, gate, 8), 256, 0, s>>>(n, c->src, ga, c->cell_of, g.nc[0], g.nc[1], c->cellpack,
+                                                          gate);
   if (gate) {
-    k_copy_back<<<nblk(n, 256), 256, 0, s>>>(n, ga, gate);
+    k_copy_back<<<chain_blocks(c, n, 256, gate, 8), 256, 0, s>>>(n, ga, gate);
   } else {
     GBMD_CUDA(c, cudaMemcpyAsync(c->ep, c->stage, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
     c->cur ^= 1;
