@@ -51,6 +51,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 MIN_TOLF = 100.0
 # measured DRAM traffic of the force kernel per atom (see roofline.traffic)
 EAM_FORCE_DRAM_BYTES_PER_ATOM = (273.772288e6 + 51.000832e6) / 864000.0
+# the same for k_lj_mixed on the 864,000-atom LJ mixture (lj_binary_16m --ncell 60)
+LJ_MULTI_PAIR_DRAM_BYTES_PER_ATOM = (474.028544e6 + 51.887872e6) / 864000.0
 MIN_DT = 0.02
 sys.path.insert(0, ROOT)
 
@@ -499,6 +501,10 @@ def main():
         traffic = EAM_FORCE_DRAM_BYTES_PER_ATOM * s.n
         traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_eam_force_mixed<1,4> on the "
                        "864,000-atom case (273.8 + 51.0 MB), scaled to %d atoms" % s.n)
+    elif w["kind"] == "lj_multi" and args.precision == "mixed":
+        traffic = LJ_MULTI_PAIR_DRAM_BYTES_PER_ATOM * s.n
+        traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_lj_mixed<1,4,multi> on the "
+                       "864,000-atom mixture (474.0 + 51.9 MB), scaled to %d atoms" % s.n)
     out["roofline"] = {"kernel": "k_eam_force (mixed, fused Verlet halves)" if w["kind"] == "eam" else "k_lj",
                        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                        "frac": achieved / peak, "peak_source": peak_kind,
