@@ -273,6 +273,11 @@ static int do_rebuild(gbmd_context* c, bool check) {
 // check_and_update_particles of the verlet step (config_move_particles.msp
 // L116-152): the displacement test and the rebuild run on the device, the
 // rebuild kernels gated by its outcome, so nothing waits on the host.
+// the device-side decision of a captured step, handed to its conditional node
+__global__ void k_set_conditional(cudaGraphConditionalHandle h, const int* __restrict__ gate) {
+  cudaGraphSetConditional(h, *gate ? 1u : 0u);
+}
+
 static int rebuild_if_displaced(gbmd_context* c) {
   if (c->n == 0) return GBMD_OK;
   int* gate = c->d_err + ERRW_GATE;
@@ -280,10 +285,53 @@ static int rebuild_if_displaced(gbmd_context* c) {
   GBMD_CUDA(c, cudaMemsetAsync(gate, 0, sizeof(int), c->stream));
   k_displ_over<<<nblk(c->n, 256), 256, 0, c->stream>>>(c->n, c->X(), c->Y(), c->Z(), c->rref, c->cap, thr * thr,
                                                         gate);
+  if (!c->capturing) {
+    // launched step by step: the chain's kernels check the gate themselves
+    int rc = rebuild(c, false, gate);
+    if (rc) return rc;
+    k_copy_rref_gated<<<chain_blocks(c, c->n, 256, gate, 8), 256, 0, c->stream>>>(
+        c->n, c->rbuf[c->cur], c->rref, c->cap, gate, c->d_err + ERRW_REBUILDS);
+    return GBMD_OK;
+  }
+  // Inside a graph capture the chain goes into the body of an IF conditional
+  // node that the device opens only when the gate is set, so a step without
+  // a rebuild launches none of it.  The body keeps the gated variant's
+  // semantics (spare buffers, copy back) so the graph's buffer indices do not
+  // depend on the outcome.
+  cudaStreamCaptureStatus st;
+  cudaGraph_t graph;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  GBMD_CUDA(c, cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &graph, nullptr, nullptr, nullptr));
+  cudaGraphConditionalHandle h;
+  GBMD_CUDA(c, cudaGraphConditionalHandleCreate(&h, graph, 0, 0));
+  k_set_conditional<<<1, 1, 0, c->stream>>>(h, gate);
+  GBMD_CUDA(c, cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &graph, &deps, nullptr, &ndeps));
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeIf;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  GBMD_CUDA(c, cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &np));
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  if (!c->cond_stream) GBMD_CUDA(c, cudaStreamCreateWithFlags(&c->cond_stream, cudaStreamNonBlocking));
+  GBMD_CUDA(c, cudaStreamBeginCaptureToGraph(c->cond_stream, body, nullptr, nullptr, 0,
+                                             cudaStreamCaptureModeThreadLocal));
+  cudaStream_t main_stream = c->stream;
+  c->stream = c->cond_stream;
+  c->full_chain_grids = true;
   int rc = rebuild(c, false, gate);
+  if (rc == GBMD_OK)
+    k_copy_rref_gated<<<nblk(c->n, 256), 256, 0, c->stream>>>(c->n, c->rbuf[c->cur], c->rref, c->cap, gate,
+                                                               c->d_err + ERRW_REBUILDS);
+  c->full_chain_grids = false;
+  c->stream = main_stream;
+  cudaGraph_t body_out = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(c->cond_stream, &body_out);
   if (rc) return rc;
-  k_copy_rref_gated<<<chain_blocks(c, c->n, 256, gate, 8), 256, 0, c->stream>>>(c->n, c->rbuf[c->cur], c->rref,
-                                                                                c->cap, gate, c->d_err + ERRW_REBUILDS);
+  if (e != cudaSuccess) return check_cuda(c, e, "conditional body capture");
+  GBMD_CUDA(c, cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
   return GBMD_OK;
 }
 
@@ -389,6 +437,7 @@ int gbmd_destroy(gbmd_context* c) {
     if (c->copy_join[k]) cudaEventDestroy(c->copy_join[k]);
   }
   if (c->copy_fork) cudaEventDestroy(c->copy_fork);
+  if (c->cond_stream) cudaStreamDestroy(c->cond_stream);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return GBMD_OK;
@@ -1085,10 +1134,12 @@ static int capture_graph(gbmd_context* c, double dt, int R, int G, bool thermo_e
   const int64_t builds = c->list_builds;  // capturing runs nothing
   GBMD_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   int rc = GBMD_OK;
+  c->capturing = true;
   for (int l = 1; l <= G && rc == GBMD_OK; ++l) {
     StepPlan p{R > 0 && l % R == 0, thermo_end && l == G, false, R < 0};
     rc = one_step(c, dt, p, false, nullptr);
   }
+  c->capturing = false;
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
   c->list_builds = builds;
   if (rc) {

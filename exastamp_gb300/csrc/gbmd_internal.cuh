@@ -101,6 +101,9 @@ struct gbmd_context {
   // copy streams for host<->device staging (created lazily), forked from and
   // joined back into `stream` with events
   int nsm = 0;                  // SMs of the device
+  bool capturing = false;       // a gbmd_run_nve graph is being captured
+  bool full_chain_grids = false;  // gated rebuild chain captured into a conditional body
+  cudaStream_t cond_stream = nullptr;  // captures the conditional rebuild body
   double* stage_r = nullptr;    // 3 x cap: r in caller order, copied out during a force pass
   double* host_r_out[3] = {nullptr, nullptr, nullptr};  // gbmd_run_nve_host's r arrays
   bool r_copy_pending = false;  // copy_join[0] marks the end of that copy

@@ -588,7 +588,7 @@ static inline unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / 
 // blocks.
 unsigned chain_blocks(const gbmd_context* c, int64_t items, int per_block, const int* gate, int per_sm) {
   const unsigned full = nblk(items, per_block);
-  if (!gate) return full;
+  if (!gate || c->full_chain_grids) return full;
   const unsigned cap = (unsigned)(per_sm * (c->nsm > 0 ? c->nsm : 1));
   return full < cap ? full : cap;
 }
@@ -617,7 +617,7 @@ static int build_list(gbmd_context* c, const int* gate) {
   }
   c->npad = npad;
   if (!gate) GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_MAXNB, 0, sizeof(int), c->stream));
-  if (gate)  // capped grid striding over the cells (five blocks per SM fit)
+  if (gate && !c->full_chain_grids)  // capped grid striding over the cells (five blocks per SM fit)
     k_build_list_cells<true><<<chain_blocks(c, c->grid.ncells, BUILD_WARPS, gate, 5), 32 * BUILD_WARPS, 0,
                                 c->stream>>>(c->grid.ncells, c->POSF(), c->X(), c->Y(), c->Z(), c->cell_start,
                                              c->grid, R2, R2lo, R2hi, c->nbr, c->nnb, c->maxnb, W, stride,
@@ -625,7 +625,7 @@ static int build_list(gbmd_context* c, const int* gate) {
   else
     k_build_list_cells<false><<<nblk(c->grid.ncells, BUILD_WARPS), 32 * BUILD_WARPS, 0, c->stream>>>(
         c->grid.ncells, c->POSF(), c->X(), c->Y(), c->Z(), c->cell_start, c->grid, R2, R2lo, R2hi, c->nbr, c->nnb,
-        c->maxnb, W, stride, c->d_err, nullptr);
+        c->maxnb, W, stride, c->d_err, gate);
   return GBMD_OK;
 }
 
