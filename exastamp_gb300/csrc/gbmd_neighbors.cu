@@ -75,7 +75,10 @@ __global__ void k_wrap_bin(int64_t n, double* __restrict__ x, double* __restrict
   }
   const int32_t lin = (int32_t)(((int64_t)c[2] * b.nc[1] + c[1]) * b.nc[0] + c[0]);
   cell_of[i] = lin;
-  atomicAdd(&cell_count[lin], 1);
+  // atoms stay cell-sorted between rebuilds, so a warp's 32 atoms fall into
+  // a few cells: one atomic per cell and warp
+  const unsigned peers = __match_any_sync(__activemask(), lin);
+  if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&cell_count[lin], __popc(peers));
   }
 }
 
@@ -187,10 +190,17 @@ static int scan(gbmd_context* c, const int32_t* in, int32_t* out, int64_t n, con
 __global__ void k_scatter(int64_t n, const int32_t* __restrict__ cell_of, const int32_t* __restrict__ cstart,
                           int32_t* __restrict__ fill, int32_t* __restrict__ order, const int* __restrict__ gate) {
   if (gate && !*gate) return;
+  const int lane = threadIdx.x & 31;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int32_t cl = cell_of[i];
-    const int32_t slot = cstart[cl] + atomicAdd(&fill[cl], 1);
-    order[slot] = (int32_t)i;
+    // one atomic per cell and warp; the order inside a cell is fixed later
+    // by k_cell_rank, so any slot assignment will do
+    const unsigned peers = __match_any_sync(__activemask(), cl);
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&fill[cl], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    order[cstart[cl] + base + __popc(peers & ((1u << lane) - 1u))] = (int32_t)i;
   }
 }
 
