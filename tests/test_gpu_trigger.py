@@ -17,23 +17,28 @@ pytestmark = pytest.mark.gpu
 TRIGGER = -1
 
 
-def test_trigger_fp64_lj_matches_oracle(gpu, oracle):
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_trigger_fp64_lj_matches_oracle(gpu, oracle, use_graph):
+    """Step by step (gated kernels) and in CUDA-graph chunks of 10 steps (the
+    rebuild chain in a conditional node set on the device)."""
     s = S.lj_fcc(ncell=10, density=0.8442, T=1.5, seed=5)
     st = s.state()
     th_ref = oracle.run_nve(st, s.masses, s.lo, s.hi, oracle.POT_LJ, oracle.LJParams(1.0, 1.0, 2.5), 0.3, 0.005,
                             150, TRIGGER)
     builds_ref = oracle.last_list_builds()
+    every = 10 if use_graph else 1
     with gpu.Context(0) as ctx:
         ctx.upload_system(s)
         ctx.set_lj(1.0, 1.0, 2.5)
         ctx.set_skin(0.3)
         ctx.set_precision(False)
         b0 = ctx.list_builds()
-        th = ctx.run_nve(150, 0.005, rebuild_every=TRIGGER, thermo_every=1)
+        th = ctx.run_nve(150, 0.005, rebuild_every=TRIGGER, thermo_every=every, use_graph=use_graph)
         builds = ctx.list_builds() - b0
         d = ctx.download(("x", "y", "z"))
     assert 2 < builds_ref < 60
     assert builds == builds_ref
+    th_ref = th_ref[::every]
     assert np.allclose(th, th_ref, rtol=1e-9, atol=1e-9 * np.abs(th_ref).max())
     for k in ("x", "y", "z"):
         dd = np.abs(d[k] - st[k])
