@@ -559,6 +559,8 @@ struct gbmd_batch {
   bool have_pot = false, have_targets = false;
   int block = 256, S = 1;
   int small_block = 128;         // threads per block of the small-replica kernel
+  cudaStream_t side = nullptr;   // runs the small-replica kernel beside the large one
+  cudaEvent_t fork = nullptr, join = nullptr;
   int nbig = 0;                  // replicas of more than SMALL_ATOMS atoms (first in `order`)
   std::vector<int> rep_atoms;    // atoms per replica (host copy)
   uint32_t* nbl = nullptr;       // pair-list scratch of the large-replica kernel's blocks
@@ -642,9 +644,16 @@ int gbmd_batch_create(gbmd_batch** out, int device, void* stream) {
   if (cudaMalloc(&b->queue, sizeof(int) * 2) != cudaSuccess || cudaMalloc(&b->d_err, sizeof(int) * 4) != cudaSuccess ||
       cudaMemset(b->d_err, 0, sizeof(int) * 4) != cudaSuccess ||
       cudaFuncSetAttribute(K_BIG, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BIG) != cudaSuccess ||
-      cudaFuncSetAttribute(K_SMALL, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_SMALL) != cudaSuccess) {
+      cudaFuncSetAttribute(K_SMALL, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_SMALL) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess) {
     cudaFree(b->queue);
     cudaFree(b->d_err);
+    if (b->side) cudaStreamDestroy(b->side);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->join) cudaEventDestroy(b->join);
+    if (b->own_stream) cudaStreamDestroy(b->stream);
     delete b;
     return GBMD_ERR_CUDA;
   }
@@ -664,6 +673,9 @@ int gbmd_batch_destroy(gbmd_batch* b) {
   cudaFree(b->dtab);
   cudaFree(b->nbl);
   cudaFree(b->nbl_small);
+  if (b->side) cudaStreamDestroy(b->side);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
   if (b->own_stream) cudaStreamDestroy(b->stream);
   delete b;
   return GBMD_OK;
@@ -911,6 +923,13 @@ static int batch_launch(gbmd_batch* b, int adjoint, int per_replica) {
   } else {
     A.single = -1;
     BCUDA(b, cudaMemsetAsync(b->queue, 0, sizeof(int) * 2, b->stream));
+    // the two size classes on two streams, so the small-replica blocks take
+    // over SMs as the large-replica kernel's blocks run out of work
+    const bool both = b->nbig > 0 && b->nrep > b->nbig;
+    if (both) {
+      BCUDA(b, cudaEventRecord(b->fork, b->stream));
+      BCUDA(b, cudaStreamWaitEvent(b->side, b->fork, 0));
+    }
     if (b->nbig > 0) {
       const int grid = persistent_grid(b, true);
       if ((size_t)grid > b->nbl_regions) return berr(b, GBMD_ERR_INVALID, "pair-list scratch not sized");
@@ -927,7 +946,11 @@ static int batch_launch(gbmd_batch* b, int adjoint, int per_replica) {
       As.order = b->order + b->nbig;
       As.queue = b->queue + 1;
       As.nbl = b->nbl_small;
-      K_SMALL<<<grid, b->small_block, SMEM_SMALL, b->stream>>>(As);
+      K_SMALL<<<grid, b->small_block, SMEM_SMALL, both ? b->side : b->stream>>>(As);
+    }
+    if (both) {
+      BCUDA(b, cudaEventRecord(b->join, b->side));
+      BCUDA(b, cudaStreamWaitEvent(b->stream, b->join, 0));
     }
   }
   BCUDA(b, cudaGetLastError());
