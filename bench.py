@@ -91,6 +91,8 @@ def parse():
     p.add_argument("--vec", type=int, default=1, help="list entries per lane per load with --lanes (1 or 4)")
     p.add_argument("--staging", action="store_true",
                    help="with --lanes 1 --vec 4: stage neighbour positions in shared memory")
+    p.add_argument("--newton3", action="store_true",
+                   help="LJ workloads with --lanes 1 --vec 4: half list + scattered reaction forces")
     p.add_argument("--ref-seconds", type=float, default=150.0,
                    help="--impl reference: CPU seconds the warm-up + timed steps of the sample should take")
     p.add_argument("--thermalise", type=int, default=100,
@@ -406,6 +408,7 @@ def main():
     if args.lanes:
         ctx.set_launch(args.lanes, args.block or 128, args.vec)
         ctx.set_neighbor_staging(args.staging)
+        ctx.set_newton3(args.newton3)
     else:
         from exastamp_gb300 import autotune
         lanes, vec, block, tuned = autotune.tune(ctx, key="%s-%s" % (args.workload, args.precision))
@@ -437,7 +440,8 @@ def main():
     value = s.n * args.steps * ws / (ms * 1e-3)
     etot = th[:, 21:24].sum(1) + th[:, 24]
     drift = (etot[-1] - etot[0]) / s.n / max(args.steps, 1) * 1000.0
-    kernels_per_step = 2 if w["kind"] == "eam" else 1
+    # EAM: density + force; Newton-3 LJ: half-list pair pass + epilogue
+    kernels_per_step = 2 if w["kind"] == "eam" or args.newton3 else 1
     # Launches of the timed gbmd_run_nve call: the pair kernel(s) once per
     # step and once more for the energies of step 0; the thermo reduction (2)
     # at step 0 and every thermo_every steps; the standalone first half at
@@ -467,6 +471,7 @@ def main():
                       "lanes_per_atom": ctx.get_launch_ex()[0], "list_entries_per_load": ctx.get_launch_ex()[1],
                       "block": ctx.get_launch_ex()[2], "density_block": ctx.get_density_block(),
                       "staged_neighbour_positions": ctx.get_neighbor_staging(),
+                      "newton3_half_list": ctx.get_newton3(),
                       "parallelism": "replicas" if ws > 1 else "single-gpu",
                       "l2": "inputs larger than L2 (neighbour list %.2f GB)" % (npairs * 4 / 1e9)
                       if npairs * 4 > 129e6 else "inputs resident in L2 (not flushed)",

@@ -74,6 +74,8 @@ def lib(path: str = LIB_PATH):
             "gbmd_get_launch": ([vp, P(i32), P(i32)], i32),
             "gbmd_set_launch_ex": ([vp, i32, i32, i32], i32),
             "gbmd_set_neighbor_staging": ([vp, i32], i32),
+            "gbmd_set_newton3": ([vp, i32], i32),
+            "gbmd_get_newton3": ([vp, P(i32)], i32),
             "gbmd_set_density_block": ([vp, i32], i32),
             "gbmd_get_density_block": ([vp, P(i32)], i32),
             "gbmd_get_neighbor_staging": ([vp, P(i32)], i32),
@@ -245,6 +247,15 @@ class Context:
     def get_neighbor_staging(self):
         e = C.c_int()
         self._chk(self._L.gbmd_get_neighbor_staging(self.h, C.byref(e)))
+        return bool(e.value)
+
+    def set_newton3(self, enable):
+        """Half list + scattered reaction forces (LJ, mixed precision)."""
+        self._chk(self._L.gbmd_set_newton3(self.h, 1 if enable else 0))
+
+    def get_newton3(self):
+        e = C.c_int()
+        self._chk(self._L.gbmd_get_newton3(self.h, C.byref(e)))
         return bool(e.value)
 
     def get_launch_ex(self):

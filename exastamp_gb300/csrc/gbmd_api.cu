@@ -51,7 +51,9 @@ static void free_atoms(gbmd_context* c) {
   cudaFree(c->order); cudaFree(c->src); cudaFree(c->fpf); cudaFree(c->fpd); cudaFree(c->epf);
   cudaFree(c->pfp);
   cudaFree(c->stage); cudaFree(c->rref); cudaFree(c->nnb); cudaFree(c->d_part); cudaFree(c->stage_r);
+  cudaFree(c->h3acc);
   c->stage_r = nullptr;
+  c->h3acc = nullptr;
   c->ep = c->vir = nullptr;
   c->cellpack = c->cell_of = c->order = c->src = nullptr;
   c->fpf = c->epf = nullptr;
@@ -91,6 +93,11 @@ int ensure_atom_capacity(gbmd_context* c, int64_t n) {
   GBMD_CUDA(c, cudaMalloc(&c->nnb, sizeof(int32_t) * cap));
   GBMD_CUDA(c, cudaMalloc(&c->d_part, sizeof(double) * 26 * thermo_blocks(cap)));
   c->cap = cap;
+  if (c->newton3) {
+    // zeroed once; the Newton-3 epilogue clears each atom's slots after reading them
+    GBMD_CUDA(c, cudaMalloc(&c->h3acc, sizeof(float4) * 3 * cap));
+    GBMD_CUDA(c, cudaMemset(c->h3acc, 0, sizeof(float4) * 3 * cap));
+  }
   c->cur = c->cur_s = 0;
   return GBMD_OK;
 }
@@ -970,6 +977,26 @@ int gbmd_set_neighbor_staging(gbmd_context* c, int enable) {
   return GBMD_OK;
 }
 
+int gbmd_set_newton3(gbmd_context* c, int enable) {
+  if (!c) return GBMD_ERR_INVALID;
+  cudaSetDevice(c->device);
+  if ((enable != 0) == c->newton3) return GBMD_OK;
+  if (enable && c->cap > 0 && !c->h3acc) {
+    GBMD_CUDA(c, cudaMalloc(&c->h3acc, sizeof(float4) * 3 * c->cap));
+    GBMD_CUDA(c, cudaMemset(c->h3acc, 0, sizeof(float4) * 3 * c->cap));
+  }
+  c->newton3 = enable != 0;
+  c->list_valid = false;  // the half and the full list differ
+  drop_graph(c);
+  return GBMD_OK;
+}
+
+int gbmd_get_newton3(const gbmd_context* c, int* enabled) {
+  if (!c || !enabled) return GBMD_ERR_INVALID;
+  *enabled = c->newton3 ? 1 : 0;
+  return GBMD_OK;
+}
+
 int gbmd_get_neighbor_staging(const gbmd_context* c, int* enabled) {
   if (!c || !enabled) return GBMD_ERR_INVALID;
   *enabled = c->staged ? 1 : 0;
@@ -1290,6 +1317,7 @@ int gbmd_lj_loss_grad(gbmd_context* c, const double* fx_target, const double* fy
                       const double* e_target, double w_force, double w_energy, double* loss, double grad[2]) {
   if (!c || !fx_target || !fy_target || !fz_target || !e_target || !loss || !grad) return GBMD_ERR_INVALID;
   if (c->pot != GBMD_POT_LJ) return set_error(c, GBMD_ERR_INVALID, "the LJ adjoint needs lj_compute_force");
+  if (c->newton3) return set_error(c, GBMD_ERR_UNSUPPORTED, "the LJ adjoint reads the full list (switch Newton-3 off)");
   const int64_t n = c->n;
   if (n == 0) {
     *loss = grad[0] = grad[1] = 0.0;

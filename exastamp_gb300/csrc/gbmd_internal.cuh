@@ -179,6 +179,8 @@ struct gbmd_context {
   int tpa = 1;                  // lanes per atom (autotuned; default = the GB300 optimum)
   int vec = 4;                  // list entries per lane per load (1 or 4, mixed kernels; autotuned)
   bool staged = false;          // 1 lane x 4 entries: neighbour positions from shared memory
+  bool newton3 = false;         // half list (j > i in cell order) + scattered reaction forces (LJ, mixed)
+  float4* h3acc = nullptr;      // Newton-3 accumulators, 3 float4 per atom: (f, ep), virial xx yy zz xy, xz yz
   int block = 256;              // threads per block of the pair / force kernels (autotuned)
   int block_rho = 128;          // threads per block of the EAM density kernels (autotuned; 0 = block)
   double skin = 0.0, rlist = 0.0;

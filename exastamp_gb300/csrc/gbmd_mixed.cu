@@ -579,6 +579,143 @@ __global__ void __launch_bounds__(256) k_eam_force_staged(PairArgs A, EamDev E, 
 }
 
 // ---------------------------------------------------------------------------
+// Newton-3 LJ (lj_compute_force_symetric, pair_potential_singlemat_symetric.cpp
+// L230-320): every unordered pair once, from the half list (j after i in cell
+// order).  The pair's force, half its energy and half its virial go to i's
+// register sums and -- the force negated -- to j's accumulators through
+// float4 / float2 atomic additions (the reference takes a spin lock on j);
+// i's own sums are added to its accumulators once at the end, since other
+// threads add to them as well.  The accumulators are three planes of `cap`
+// float4: (f, ep), (vxx, vyy, vzz, vxy), (vxz, vyz).  k_h3_epilogue turns
+// them into the acceleration (and the fused Verlet half steps) and clears
+// them for the next pass.  The atomic order varies from run to run, so the
+// result is not bit-reproducible (the full-list kernels are).
+// ---------------------------------------------------------------------------
+template <bool EV, bool MULTI>
+__global__ void __launch_bounds__(256) k_lj_half(PairArgs A, LJF P, const LJPair* __restrict__ tab, int ntypes,
+                                                 double rcmax2, float4* __restrict__ acc, int64_t cap) {
+  __shared__ LJTabSmem tb;
+  if (MULTI) lj_load_table(tb, tab, ntypes);
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= A.n) return;
+  float4* acc1 = acc + cap;
+  float4* acc2 = acc + 2 * cap;
+  const int nn = min(A.nnb[i], A.maxnb);
+  const float4 pi = A.posf[i];
+  const int cp = A.cellpack[i];
+  const int ti = __float_as_int(pi.w);
+  float fx = 0.f, fy = 0.f, fz = 0.f, cfx = 0.f, cfy = 0.f, cfz = 0.f, e = 0.f, ce = 0.f;
+  float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  const ListRows<1, 4> L(A.nbr, i, 0, A.stride, nn);
+  const GlobalFetch fetch{A.posf};
+  uint32_t ent[4], nxt[4];
+  if (L.nrow > 0) L.load(0, ent);
+  for (int r = 0; r < L.nrow; ++r) {
+    if (r + 1 < L.nrow) L.load(r + 1, nxt);
+    float4 pj[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (!L.valid(r, q)) ent[q] = L.standin;
+      pj[q] = fetch(ent[q], ent[q] & GBMD_IDX_MASK);
+    }
+    float rx = 0.f, ry = 0.f, rz = 0.f, re = 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t j = ent[q] & GBMD_IDX_MASK;
+      const GeomF G = geom_f(ent[q], pj[q], pi, A.g);
+      float sig2, eps24, eps4, ecut, rlo, rhi;
+      int pid = 0;
+      if (MULTI) {
+        pid = ti * ntypes + __float_as_int(pj[q].w);
+        const float4 a = tb.a[pid];
+        const float2 b = tb.b[pid];
+        sig2 = a.x; eps24 = a.y; eps4 = a.z; ecut = a.w; rlo = b.x; rhi = b.y;
+      } else {
+        sig2 = P.sig2; eps24 = P.eps24; eps4 = P.eps4; ecut = P.ecut; rlo = P.rc2lo; rhi = P.rc2hi;
+      }
+      bool in = G.d2 < rlo;
+      if (!in && G.d2 <= rhi && L.valid(r, q))
+        in = exact_inside(A.posd, i, j, ent[q] >> GBMD_IDX_BITS, cp, A.g, MULTI ? rcmax2 : P.rc2,
+                          MULTI ? tb.r[pid] : 0.0);
+      float r2i;
+      asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r2i) : "f"(G.d2));
+      const float s2 = sig2 * r2i;
+      const float s6 = s2 * s2 * s2;
+      const float s12 = s6 * s6;
+      const float fpair = eps24 * fmaf(2.f, s12, -s6) * r2i;  // -(dE/dr)/r
+      if (in) {
+        const float gx = fpair * G.dx, gy = fpair * G.dy, gz = fpair * G.dz;
+        rx -= gx;
+        ry -= gy;
+        rz -= gz;
+        if (EV) {
+          const float eh = 0.5f * fmaf(eps4, s12 - s6, -ecut);
+          const float h = 0.5f * fpair;
+          const float w0 = h * G.dx * G.dx, w1 = h * G.dy * G.dy, w2 = h * G.dz * G.dz;
+          const float w3 = h * G.dx * G.dy, w4 = h * G.dx * G.dz, w5 = h * G.dy * G.dz;
+          re += eh;
+          v[0] += w0; v[1] += w1; v[2] += w2; v[3] += w3; v[4] += w4; v[5] += w5;
+          atomicAdd(acc + j, make_float4(gx, gy, gz, eh));
+          atomicAdd(acc1 + j, make_float4(w0, w1, w2, w3));
+          atomicAdd(reinterpret_cast<float2*>(acc2 + j), make_float2(w4, w5));
+        } else {
+          atomicAdd(acc + j, make_float4(gx, gy, gz, 0.f));
+        }
+      }
+    }
+    kahan_add(fx, cfx, rx);
+    kahan_add(fy, cfy, ry);
+    kahan_add(fz, cfz, rz);
+    if (EV) kahan_add(e, ce, re);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ent[q] = nxt[q];
+  }
+  atomicAdd(acc + i, make_float4(fx - cfx, fy - cfy, fz - cfz, EV ? e - ce : 0.f));
+  if (EV) {
+    atomicAdd(acc1 + i, make_float4(v[0], v[1], v[2], v[3]));
+    atomicAdd(reinterpret_cast<float2*>(acc2 + i), make_float2(v[4], v[5]));
+  }
+}
+
+template <bool EV>
+__global__ void __launch_bounds__(256) k_h3_epilogue(PairArgs A, float4* __restrict__ acc, int64_t cap) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= A.n) return;
+  const float4 f = acc[i];
+  acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int t = __float_as_int(A.posf[i].w);
+  const float im = A.inv_massf[t];
+  double o[9];
+  if (EV) {
+    const float4 w = acc[cap + i];
+    const float4 u = acc[2 * cap + i];
+    acc[cap + i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    acc[2 * cap + i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float v[6] = {w.x, w.y, w.z, w.w, u.x, u.y};
+    vir9(v, o);
+  }
+  atom_epilogue<true>(A, i, t, 0., 0., 0., f.x * im, f.y * im, f.z * im, EV ? (double)f.w : 0.0, EV ? o : nullptr);
+}
+
+template <bool EV>
+static int launch_newton3(gbmd_context* c, const PairArgs& A, int part) {
+  if (part == 1 || A.n == 0) return GBMD_OK;
+  const int B = 256;
+  const unsigned grid = (unsigned)((A.n + B - 1) / B);
+  cudaStream_t s = c->stream;
+  if (c->pot == GBMD_POT_LJ) {
+    const LJPair& q = c->lj.p[0];
+    LJF P{q.sig2f, q.eps24f, q.eps4f, q.ecutf, q.rc2lo, q.rc2hi, q.rc2, q.rc};
+    k_lj_half<EV, false><<<grid, B, 0, s>>>(A, P, nullptr, 1, c->lj.rcut_max2, c->h3acc, c->cap);
+  } else {
+    LJF P{};
+    k_lj_half<EV, true><<<grid, B, 0, s>>>(A, P, c->lj_tab_d, c->lj.ntypes, c->lj.rcut_max2, c->h3acc, c->cap);
+  }
+  k_h3_epilogue<EV><<<grid, B, 0, s>>>(A, c->h3acc, c->cap);
+  return GBMD_OK;
+}
+
+// ---------------------------------------------------------------------------
 // dispatch
 // ---------------------------------------------------------------------------
 template <int T, int V, bool EV>
@@ -667,6 +804,12 @@ static bool launch_staged(gbmd_context* c, const PairArgs& A, int part) {
 
 template <bool EV>
 static int launch_mixed_E(gbmd_context* c, const PairArgs& A, int part) {
+  if (c->newton3) {
+    // the half list is laid out as one lane x 4 entries per load
+    if (c->tpa != 1 || c->vec != 4)
+      return set_error(c, GBMD_ERR_UNSUPPORTED, "Newton-3 half lists need the 1 lane x 4 entries launch");
+    return launch_newton3<EV>(c, A, part);
+  }
   if (c->staged && c->tpa == 1 && c->vec == 4 && launch_staged<EV>(c, A, part)) return GBMD_OK;
   const int key = c->tpa * 8 + c->vec;
   switch (key) {

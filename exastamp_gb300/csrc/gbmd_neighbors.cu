@@ -429,7 +429,9 @@ __device__ __noinline__ int build_retest_row(uint32_t* row, int nkeep, int wsh, 
 // candidate per step; G = 16, lanes l and l+16 hold the same home atom and a
 // step tests candidates 2t (low half) and 2t+1 (high half), the two lanes
 // exchanging their hit with one shuffle so both append in candidate order.
-template <int G>
+// HALF keeps only candidates after the home atom in cell order (k > i): each
+// unordered pair once, for the Newton-3 force kernels.
+template <int G, bool HALF>
 __device__ __forceinline__ int build_walk(const BuildCell& B, const float4* __restrict__ pf,
                                           const double* __restrict__ x, const double* __restrict__ y,
                                           const double* __restrict__ z, const Grid& g, double R2, float R2lo,
@@ -479,7 +481,8 @@ __device__ __forceinline__ int build_walk(const BuildCell& B, const float4* __re
         // an atom never pairs with itself: its images sit at least one box
         // edge >= R away, so k == i only ever matters in the home cell.
         // Keep d2 <= R^2 (1 + 2^-12); flag the atom when d2 >= R^2 (1 - 2^-12).
-        const bool in = hv && (int)(w & GBMD_IDX_MASK) != i && d2f <= R2hi;
+        const int k = (int)(w & GBMD_IDX_MASK);
+        const bool in = hv && (HALF ? k > i : k != i) && d2f <= R2hi;
         unc |= in && d2f >= R2lo;
         // the slot address is formed on every step and only the store is
         // conditional, so the walk stays one straight-line block
@@ -529,7 +532,7 @@ __device__ __forceinline__ int build_walk(const BuildCell& B, const float4* __re
 // R^2 (1 - 2^-12); flagged atoms (a few per cent) rescan their row, re-test
 // those entries in FP64 and compact, so the walk has no call and no
 // divergent branch.
-template <bool LOOP>
+template <bool LOOP, bool HALF>
 __global__ void __launch_bounds__(BUILD_WARPS * 32) k_build_list_cells(
     int64_t ncells, const float4* __restrict__ pf, const double* __restrict__ x, const double* __restrict__ y,
     const double* __restrict__ z, const int32_t* __restrict__ cstart, Grid g, double R2, float R2lo, float R2hi,
@@ -579,9 +582,9 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32) k_build_list_cells(
   B.nh = cstart[cell + 1] - B.hb;
   int warp_max;
   if (B.nh <= 16)
-    warp_max = build_walk<16>(B, pf, x, y, z, g, R2, R2lo, R2hi, nbr, nnb, maxnb, W, wsh, stride, err, stage, lane);
+    warp_max = build_walk<16, HALF>(B, pf, x, y, z, g, R2, R2lo, R2hi, nbr, nnb, maxnb, W, wsh, stride, err, stage, lane);
   else
-    warp_max = build_walk<32>(B, pf, x, y, z, g, R2, R2lo, R2hi, nbr, nnb, maxnb, W, wsh, stride, err, stage, lane);
+    warp_max = build_walk<32, HALF>(B, pf, x, y, z, g, R2, R2lo, R2hi, nbr, nnb, maxnb, W, wsh, stride, err, stage, lane);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) warp_max = max(warp_max, __shfl_xor_sync(FULL, warp_max, o));
   if (lane == 0 && warp_max > 0) atomicMax(&err[ERRW_MAXNB], warp_max);
@@ -627,15 +630,13 @@ static int build_list(gbmd_context* c, const int* gate) {
   }
   c->npad = npad;
   if (!gate) GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_MAXNB, 0, sizeof(int), c->stream));
-  if (gate && !c->full_chain_grids)  // capped grid striding over the cells (five blocks per SM fit)
-    k_build_list_cells<true><<<chain_blocks(c, c->grid.ncells, BUILD_WARPS, gate, 5), 32 * BUILD_WARPS, 0,
-                                c->stream>>>(c->grid.ncells, c->POSF(), c->X(), c->Y(), c->Z(), c->cell_start,
-                                             c->grid, R2, R2lo, R2hi, c->nbr, c->nnb, c->maxnb, W, stride,
-                                             c->d_err, gate);
-  else
-    k_build_list_cells<false><<<nblk(c->grid.ncells, BUILD_WARPS), 32 * BUILD_WARPS, 0, c->stream>>>(
-        c->grid.ncells, c->POSF(), c->X(), c->Y(), c->Z(), c->cell_start, c->grid, R2, R2lo, R2hi, c->nbr, c->nnb,
-        c->maxnb, W, stride, c->d_err, gate);
+  const bool loop = gate && !c->full_chain_grids;  // capped grid striding over the cells (five blocks per SM fit)
+  const unsigned blocks = loop ? chain_blocks(c, c->grid.ncells, BUILD_WARPS, gate, 5) : nblk(c->grid.ncells, BUILD_WARPS);
+  auto kern = loop ? (c->newton3 ? k_build_list_cells<true, true> : k_build_list_cells<true, false>)
+                   : (c->newton3 ? k_build_list_cells<false, true> : k_build_list_cells<false, false>);
+  kern<<<blocks, 32 * BUILD_WARPS, 0, c->stream>>>(c->grid.ncells, c->POSF(), c->X(), c->Y(), c->Z(), c->cell_start,
+                                                  c->grid, R2, R2lo, R2hi, c->nbr, c->nnb, c->maxnb, W, stride,
+                                                  c->d_err, gate);
   return GBMD_OK;
 }
 

@@ -165,6 +165,16 @@ int gbmd_get_density_block(const gbmd_context* ctx, int* block);
  * on GB300); results are the same bit for bit. */
 int gbmd_set_neighbor_staging(gbmd_context* ctx, int enable);
 int gbmd_get_neighbor_staging(const gbmd_context* ctx, int* enabled);
+/* Newton-3 mode (lj_compute_force_symetric,
+ * src/potential/pair_potential_template/pair_potential_singlemat_symetric.cpp
+ * L44, L230-320): the list keeps each unordered pair once (j after i in
+ * cell order) and the LJ kernels add the reaction force, half the pair
+ * energy and half the pair virial to j with FP32 atomics.  LJ potentials in
+ * mixed precision with the 1 lane x 4 entries launch only; other set-ups
+ * return GBMD_ERR_UNSUPPORTED at the force call.  Results are not
+ * bit-reproducible from run to run (atomic order).  Default 0. */
+int gbmd_set_newton3(gbmd_context* ctx, int enable);
+int gbmd_get_newton3(const gbmd_context* ctx, int* enabled);
 
 /* ---- neighbour list --------------------------------------------------------
  * chunk_neighbors (exaNBody; config data/config/config_move_particles.msp

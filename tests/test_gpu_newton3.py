@@ -1,0 +1,152 @@
+"""Newton-3 mode (lj_compute_force_symetric): half list + scattered reaction
+forces, called through the C ABI, against the FP64 oracle.
+
+Bars: the half list holds each pair of the full list exactly once (bit-exact
+pair set after mirroring); forces within 1e-5 relative RMS (the mixed
+tolerance), total energy within 1e-6 relative, virial within 1e-5 relative
+RMS; an NVE run stays close to the full-list run; the set-ups without a
+Newton-3 kernel answer GBMD_ERR_UNSUPPORTED.
+"""
+import numpy as np
+import pytest
+
+from exastamp_gb300 import systems as S
+from exastamp_gb300 import setfl as SF
+
+from test_gpu_parity import LJ, _jitter, _lj_oracle, gpu_ctx, rel_rms
+
+pytestmark = pytest.mark.gpu
+
+MIXED_FORCE_TOL = 1e-5
+UNSUPPORTED = 8  # GBMD_ERR_UNSUPPORTED
+
+
+def _n3_ctx(gpu, s, pot, skin=0.3):
+    ctx = gpu_ctx(gpu, s, pot, skin, mixed=True, tpa=1, block=256, vec=4)
+    ctx.set_newton3(True)
+    assert ctx.get_newton3()
+    return ctx
+
+
+@pytest.mark.parametrize("ncell,sig", [(3, 0.05), (6, 0.1), (2, 0.1)])
+def test_half_list_mirrors_to_full_list(gpu, ncell, sig):
+    s = _jitter(S.lj_fcc(ncell=ncell, seed=ncell), sig, ncell)
+    with gpu_ctx(gpu, s, LJ, 0.3, mixed=True, tpa=1, block=256, vec=4) as ctx:
+        ctx.build_neighbors()
+        full = {tuple(int(v) for v in r) for r in ctx.export_pairs()}
+    with _n3_ctx(gpu, s, LJ) as ctx:
+        ctx.build_neighbors()
+        rows = [tuple(int(v) for v in r) for r in ctx.export_pairs()]
+    half = set(rows)
+    assert len(half) == len(rows)
+    mirror = {(j, i, -a, -b, -c) for (i, j, a, b, c) in half}
+    assert not (half & mirror)
+    assert half | mirror == full
+    assert 2 * len(half) == len(full)
+
+
+@pytest.mark.parametrize("ncell,sig", [(8, 0.06), (3, 0.08)])
+def test_lj_newton3_matches_oracle(gpu, oracle, ncell, sig):
+    s = _jitter(S.lj_fcc(ncell=ncell, seed=2), sig, 2)
+    F, ep, vir = _lj_oracle(oracle, s)
+    with _n3_ctx(gpu, s, LJ) as ctx:
+        for _ in range(2):  # the second call sees the accumulators cleared by the first
+            ctx.compute_forces(energy=True, virial=True)
+            d = ctx.download(virial=True)
+            G = np.stack([d["ax"], d["ay"], d["az"]], 1)
+            assert rel_rms(G, F) < MIXED_FORCE_TOL
+            assert abs(d["ep"].sum() - ep.sum()) < 1e-6 * abs(ep.sum())
+            assert rel_rms(d["ep"], ep) < 1e-5
+            assert rel_rms(d["vir"], vir) < 1e-5
+        ctx.compute_forces()  # no energy: forces only
+        d = ctx.download()
+        assert rel_rms(np.stack([d["ax"], d["ay"], d["az"]], 1), F) < MIXED_FORCE_TOL
+
+
+def test_lj_multi_newton3_matches_oracle(gpu, oracle):
+    s = _jitter(S.lj_fcc(ncell=6, seed=3), 0.05, 3)
+    rng = np.random.default_rng(3)
+    s.type = (rng.random(s.n) < 0.2).astype(np.uint8)
+    s.masses = np.array([1.0, 2.0])
+    eps, sig, rc = S.kob_andersen_tables()
+    rcmax = float(rc.max())
+    x, y, z = s.x.copy(), s.y.copy(), s.z.copy()
+    oracle.wrap(x, y, z, s.lo, s.hi)
+    nl = oracle.build_neighbors(x, y, z, s.id, s.lo, s.hi, rcmax + 0.3)
+    fx, fy, fz, ep, vir = oracle.lj_multi_force(x, y, z, s.type, nl, s.L, eps, sig, rc, rcmax)
+    F = np.stack([fx, fy, fz], 1) / s.masses[s.type][:, None]
+    with _n3_ctx(gpu, s, lambda c: c.set_lj_multi(eps, sig, rc, 0.0)) as ctx:
+        ctx.compute_forces(energy=True, virial=True)
+        d = ctx.download(virial=True)
+    G = np.stack([d["ax"], d["ay"], d["az"]], 1)
+    assert rel_rms(G, F) < MIXED_FORCE_TOL
+    assert abs(d["ep"].sum() - ep.sum()) < 1e-6 * abs(ep.sum())
+    assert rel_rms(d["vir"], vir) < 1e-5
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_newton3_nve_tracks_full_list(gpu, use_graph):
+    """40 NVE steps with rebuilds every 10 (fused Verlet epilogue, graph
+    replay): positions stay within 1e-6 of the full-list run, the energy is
+    conserved as well, and the momentum stays ~0 (pairwise equal and opposite
+    forces up to FP32 rounding)."""
+    s = S.lj_fcc(ncell=6, seed=8)
+    out = {}
+    for n3 in (False, True):
+        with gpu_ctx(gpu, s, LJ, 0.3, mixed=True, tpa=1, block=256, vec=4) as ctx:
+            ctx.set_newton3(n3)
+            th = ctx.run_nve(40, 0.005, rebuild_every=10, thermo_every=20 if use_graph else 10,
+                             use_graph=use_graph)
+            out[n3] = (th, ctx.download())
+    (th0, d0), (th1, d1) = out[False], out[True]
+    for k in ("x", "y", "z", "vx"):
+        assert np.abs(d1[k] - d0[k]).max() < 1e-6, k
+    e0 = th0[:, 21:24].sum(1) + th0[:, 24]
+    e1 = th1[:, 21:24].sum(1) + th1[:, 24]
+    assert np.abs(e1 - e0).max() < 1e-6 * np.abs(e0).max()
+    assert np.abs(th1[:, 18:21]).max() < 1e-5
+
+
+def test_newton3_displacement_trigger(gpu):
+    s = S.lj_fcc(ncell=6, seed=9)
+    with gpu_ctx(gpu, s, LJ, 0.3, mixed=True, tpa=1, block=256, vec=4) as ctx:
+        ctx.set_newton3(True)
+        ctx.run_nve(30, 0.005, rebuild_every=-1, thermo_every=10)
+        d1 = ctx.download()
+    with gpu_ctx(gpu, s, LJ, 0.3, mixed=True, tpa=1, block=256, vec=4) as ctx:
+        ctx.run_nve(30, 0.005, rebuild_every=-1, thermo_every=10)
+        d0 = ctx.download()
+    assert np.abs(d1["x"] - d0["x"]).max() < 1e-6
+
+
+def test_newton3_unsupported_setups(gpu):
+    s = _jitter(S.lj_fcc(ncell=4, seed=5), 0.05, 5)
+    # FP64 precision
+    with gpu_ctx(gpu, s, LJ, 0.3, mixed=False, tpa=1, block=256, vec=4) as ctx:
+        ctx.set_newton3(True)
+        with pytest.raises(gpu.GbmdError) as e:
+            ctx.compute_forces()
+        assert e.value.code == UNSUPPORTED
+    # another launch layout
+    with gpu_ctx(gpu, s, LJ, 0.3, mixed=True, tpa=4, block=128, vec=1) as ctx:
+        ctx.set_newton3(True)
+        with pytest.raises(gpu.GbmdError) as e:
+            ctx.compute_forces()
+        assert e.value.code == UNSUPPORTED
+    # EAM
+    sf = SF.tabulate(SF.load_cu_params())
+    c = S.eam_cu_fcc(ncell=4, displace=0.05, seed=4)
+    with gpu_ctx(gpu, c, lambda k: k.set_eam_alloy(sf, 5.0, S.EV, S.EV), 0.3, mixed=True, tpa=1, block=256,
+                 vec=4) as ctx:
+        ctx.set_newton3(True)
+        with pytest.raises(gpu.GbmdError) as e:
+            ctx.compute_forces()
+        assert e.value.code == UNSUPPORTED
+    # switching back gives the full-list result again
+    with _n3_ctx(gpu, s, LJ) as ctx:
+        ctx.compute_forces(energy=True)
+        d1 = ctx.download()
+        ctx.set_newton3(False)
+        ctx.compute_forces(energy=True)
+        d0 = ctx.download()
+    assert rel_rms(d1["ax"], d0["ax"]) < MIXED_FORCE_TOL
