@@ -7,6 +7,8 @@
 // neither.  Operators (drop-ins for the compute_force slot):
 //
 //   gb300_lj_force         lj_compute_force  (pair_potential_impl.hxx L104-121)
+//   gb300_lj_force_symetric lj_compute_force_symetric (pair_potential_singlemat_symetric.cpp L335-346):
+//                          the same with the Newton-3 half list (gbmd_set_newton3)
 //   gb300_lj_multi_force   lj_multi_force    (pair_potential_force_op_multiparam.h L249-284)
 //   gb300_eam_alloy_force  eam_alloy_force   (eam_potential_multimat.cu L88-109)
 //   gb300_johnson_force    johnson_force     (johnson.h, eam_potential.cu L69-193)
@@ -205,8 +207,11 @@ namespace exaStamp {
 using StringVector = std::vector<std::string>;
 
 // lj_compute_force (pair_potential_impl.hxx L104-121): one species pair,
-// energy shifted by e(rcut) as the reference does (L373-377).
-template <class GridT>
+// energy shifted by e(rcut) as the reference does (L373-377).  SYM: the
+// lj_compute_force_symetric slots (pair_potential_singlemat_symetric.cpp
+// L335-346; particle_locks accepted and unused: the library scatters the
+// reaction forces with atomics) on the Newton-3 half list.
+template <class GridT, bool SYM = false>
 class Gb300LJForceNode : public OperatorNode {
   ADD_SLOT(LennardJonesParms, parameters, INPUT, LennardJonesParms{});
   ADD_SLOT(double, rcut, INPUT, REQUIRED);
@@ -221,6 +226,7 @@ class Gb300LJForceNode : public OperatorNode {
   ADD_SLOT(bool, compute_virial, INPUT, false);
   ADD_SLOT(double, rcut_inc, INPUT, 1.0, DocString{"neighbour skin (global.rcut_inc)"});
   ADD_SLOT(std::string, precision, INPUT, std::string{"mixed"}, DocString{"mixed or fp64"});
+  ADD_SLOT(GridParticleLocks, particle_locks, INPUT, OPTIONAL, DocString{"unused (atomic scatter)"});
   gb300::ContextPtr m_ctx;
   gb300::Staging m_stage;
   size_t m_uploaded = 0;
@@ -234,6 +240,11 @@ class Gb300LJForceNode : public OperatorNode {
       m_ctx.reset(c);
       gb300::check(c, gbmd_set_lj(c, parameters->epsilon, parameters->sigma, *rcut), "gbmd_set_lj");
       gb300::finish_setup(c, *rcut_inc, *precision);
+      if (SYM) {
+        // the half-list kernel: mixed precision, one lane x 4 entries per load
+        gb300::check(c, gbmd_set_launch_ex(c, 1, 4, 256), "gbmd_set_launch_ex");
+        gb300::check(c, gbmd_set_newton3(c, 1), "gbmd_set_newton3");
+      }
     }
     const bool energy = trigger_thermo_state.has_value() && *trigger_thermo_state;
     gb300::compute_and_store(m_ctx.get(), *grid, *species, m_stage, m_uploaded, energy, energy && *compute_virial);
@@ -446,6 +457,8 @@ using Gb300ForceNodeTmpl = Gb300ForceNode<GridT>;
 template <class GridT>
 using Gb300LJForceTmpl = Gb300LJForceNode<GridT>;
 template <class GridT>
+using Gb300LJForceSymTmpl = Gb300LJForceNode<GridT, true>;
+template <class GridT>
 using Gb300LJMultiForceTmpl = Gb300LJMultiForceNode<GridT>;
 template <class GridT>
 using Gb300EamAlloyForceTmpl = Gb300EamAlloyForceNode<GridT>;
@@ -455,6 +468,8 @@ using Gb300JohnsonForceTmpl = Gb300JohnsonForceNode<GridT>;
 ONIKA_AUTORUN_INIT(gb300_md_ops) {
   OperatorNodeFactory::instance()->register_factory("gb300_force", make_grid_variant_operator<Gb300ForceNodeTmpl>);
   OperatorNodeFactory::instance()->register_factory("gb300_lj_force", make_grid_variant_operator<Gb300LJForceTmpl>);
+  OperatorNodeFactory::instance()->register_factory("gb300_lj_force_symetric",
+                                                    make_grid_variant_operator<Gb300LJForceSymTmpl>);
   OperatorNodeFactory::instance()->register_factory("gb300_lj_multi_force",
                                                     make_grid_variant_operator<Gb300LJMultiForceTmpl>);
   OperatorNodeFactory::instance()->register_factory("gb300_eam_alloy_force",

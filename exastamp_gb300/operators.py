@@ -181,6 +181,21 @@ class lj_compute_force(Operator):
         sim.ctx.compute_forces(energy=energy, virial=virial)
 
 
+class lj_compute_force_symetric(lj_compute_force):
+    """lj_compute_force_symetric (pair_potential_singlemat_symetric.cpp L44,
+    slots L335-346): lj_compute_force on the Newton-3 half list.  The
+    reference scatters the reaction force under per-particle spin locks
+    (`particle_locks`, accepted and unused here); the library adds it with
+    FP32 atomics.  Mixed precision with one lane x 4 entries per load."""
+    name = "lj_compute_force_symetric"
+
+    def bind(self, sim: Simulation):
+        super().bind(sim)
+        sim.set_precision(True)
+        sim.ctx.set_launch(1, 256, 4)
+        sim.ctx.set_newton3(True)
+
+
 class lj_multi_force(Operator):
     name = "lj_multi_force"
     required = ("rcut",)
@@ -369,7 +384,8 @@ def verlet_nve(sim: Simulation, nsteps: int, dt: float, rebuild_every: int = 10,
     return sim.ctx.run_nve(nsteps, dt, rebuild_every, thermo_every, use_graph)
 
 
-FORCE_OPERATORS = {"lj_compute_force": lj_compute_force, "lj_multi_force": lj_multi_force,
+FORCE_OPERATORS = {"lj_compute_force": lj_compute_force, "lj_compute_force_symetric": lj_compute_force_symetric,
+                   "lj_multi_force": lj_multi_force,
                    "eam_alloy_force": eam_alloy_force, "johnson_force": johnson_force}
 
 

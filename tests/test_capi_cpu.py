@@ -55,6 +55,9 @@ def test_required_slots_raise():
                                        "lj_compute_force": {"rcut": "2.5 ang",
                                                             "parameters": {"epsilon": 1.0, "sigma": 1.0}}})
     assert isinstance(op, OP.lj_compute_force)
+    op = OP.compute_force_from_config({"compute_force": "lj_compute_force_symetric",
+                                       "lj_compute_force_symetric": {"rcut": 2.5}})
+    assert isinstance(op, OP.lj_compute_force_symetric) and op.name == "lj_compute_force_symetric"
 
 
 def test_header_is_plain_c():

@@ -150,3 +150,28 @@ def test_newton3_unsupported_setups(gpu):
         ctx.compute_forces(energy=True)
         d0 = ctx.download()
     assert rel_rms(d1["ax"], d0["ax"]) < MIXED_FORCE_TOL
+
+
+def test_symetric_operator_matches_lj_compute_force(gpu, oracle):
+    """The operator mirror: a run file binding lj_compute_force_symetric to
+    compute_force gives the lj_compute_force result (within the mixed
+    tolerance) on the Newton-3 path."""
+    from exastamp_gb300 import operators as OP
+    s = _jitter(S.lj_fcc(ncell=5, seed=6), 0.05, 6)
+    F, ep, _ = _lj_oracle(oracle, s)
+    cfg = {"compute_force": "lj_compute_force_symetric",
+           "lj_compute_force_symetric": {"rcut": 2.5, "parameters": {"epsilon": 1.0, "sigma": 1.0}}}
+    sim = OP.Simulation(s)
+    try:
+        op = OP.compute_force_from_config(cfg)
+        assert isinstance(op, OP.lj_compute_force_symetric)
+        op.bind(sim)
+        OP.chunk_neighbors().bind(sim, 0.3)
+        op.execute(sim, energy=True)
+        assert sim.ctx.get_newton3()
+        d = sim.ctx.download()
+    finally:
+        sim.ctx.close()
+    G = np.stack([d["ax"], d["ay"], d["az"]], 1)
+    assert rel_rms(G, F) < MIXED_FORCE_TOL
+    assert abs(d["ep"].sum() - ep.sum()) < 1e-6 * abs(ep.sum())
