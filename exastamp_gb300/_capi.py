@@ -24,6 +24,7 @@ ERR_NAMES = {1: "INVALID", 2: "CUDA", 3: "NO_DEVICE", 4: "NEIGHBOR_OVERFLOW", 5:
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 POT_NONE, POT_LJ, POT_LJ_MULTI, POT_EAM_ALLOY = 0, 1, 2, 3
 FORCE_ENERGY, FORCE_VIRIAL = 1, 2
+FORCE_PASS_DENSITY, FORCE_PASS_FORCE = 4, 8  # split EAM passes (eam_rho + eam_rho2emb / eam_force)
 
 
 class GbmdError(RuntimeError):
@@ -287,8 +288,11 @@ class Context:
         self._chk(self._L.gbmd_neighbor_stats(self.h, C.byref(npairs), C.byref(maxnb), _p(nc)))
         return npairs.value, maxnb.value, nc
 
-    def compute_forces(self, energy=True, virial=False):
+    def compute_forces(self, energy=True, virial=False, passes="all"):
+        """passes: "all", "density" (EAM density + embedding only) or "force"
+        (the final pair pass from the kept F'(rho))."""
         flags = (FORCE_ENERGY if energy else 0) | (FORCE_VIRIAL if virial else 0)
+        flags |= {"all": 0, "density": FORCE_PASS_DENSITY, "force": FORCE_PASS_FORCE}[passes]
         self._chk(self._L.gbmd_compute_forces(self.h, flags))
 
     def push_f_v_r(self, dt, dt_scale=1.0):

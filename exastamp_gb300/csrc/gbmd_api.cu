@@ -109,7 +109,7 @@ static void drop_graph(gbmd_context* c) {
 
 static void invalidate_list(gbmd_context* c) {
   c->list_valid = false;
-  c->forces_valid_step = -1;
+  c->forces_valid_step = c->rho_valid_step = -1;
   drop_graph(c);
 }
 
@@ -592,7 +592,7 @@ static int upload_arrays(gbmd_context* c, const double* const* host, double* con
 // than skin/2 since the last rebuild (config_move_particles.msp L19-22,
 // L116-118), otherwise refresh the FP32/FP64 gather copies.
 static int after_new_positions(gbmd_context* c) {
-  c->forces_valid_step = -1;
+  c->forces_valid_step = c->rho_valid_step = -1;
   if (!c->list_valid) {
     // the caller may reuse its arrays once the upload returns
     GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -902,7 +902,7 @@ int gbmd_set_eam_johnson(gbmd_context* c, const double params[19], double rcut) 
   P.rc2hi = (float)(P.rcut2 * (1.0 + 0x1p-12));
   c->ej = P;
   c->pot = GBMD_POT_EAM_JOHNSON;
-  c->forces_valid_step = -1;
+  c->forces_valid_step = c->rho_valid_step = -1;
   set_rlist(c, rcut);
   return GBMD_OK;
 }
@@ -911,7 +911,7 @@ int gbmd_set_precision(gbmd_context* c, int precision) {
   if (!c || (precision != GBMD_PRECISION_FP64 && precision != GBMD_PRECISION_MIXED)) return GBMD_ERR_INVALID;
   if (c->precision != precision) {
     c->precision = precision;
-    c->forces_valid_step = -1;
+    c->forces_valid_step = c->rho_valid_step = -1;
     drop_graph(c);
   }
   return GBMD_OK;
@@ -1022,7 +1022,7 @@ int gbmd_build_neighbors(gbmd_context* c) {
   if (!c) return GBMD_ERR_INVALID;
   int rc = do_rebuild(c, true);
   if (rc) return rc;
-  c->forces_valid_step = -1;
+  c->forces_valid_step = c->rho_valid_step = -1;
   return GBMD_OK;
 }
 
@@ -1080,6 +1080,26 @@ int gbmd_compute_forces(gbmd_context* c, int flags) {
   f.virial = (flags & GBMD_FORCE_VIRIAL) != 0;
   if (f.virial && (rc = ensure_virial(c))) return rc;
   f.fuse = FUSE_NONE;
+  const int passes = flags & (GBMD_FORCE_PASS_DENSITY | GBMD_FORCE_PASS_FORCE);
+  const bool eam = c->pot == GBMD_POT_EAM_ALLOY || c->pot == GBMD_POT_EAM_JOHNSON;
+  if (passes == GBMD_FORCE_PASS_DENSITY) {
+    // eam_rho (+ eam_rho2emb): F'(rho) kept in the context for the force pass
+    f.part = 1;
+    if ((rc = launch_forces(c, f))) return rc;
+    GBMD_CUDA(c, cudaGetLastError());
+    c->rho_valid_step = c->step;
+    c->rho_builds = c->list_builds;
+    c->rho_ev = f.energy || f.virial;
+    return GBMD_OK;
+  }
+  if (passes == GBMD_FORCE_PASS_FORCE && eam) {
+    // eam_force alone: needs the density pass on these positions and this list
+    if (c->rho_valid_step != c->step || c->rho_builds != c->list_builds)
+      return set_error(c, GBMD_ERR_INVALID, "the EAM force pass needs a density pass on the same positions");
+    if ((f.energy || f.virial) && !c->rho_ev)
+      return set_error(c, GBMD_ERR_INVALID, "energies: run the density pass with GBMD_FORCE_ENERGY");
+    f.part = 2;
+  }
   rc = launch_forces(c, f);
   if (rc) return rc;
   GBMD_CUDA(c, cudaGetLastError());
@@ -1090,7 +1110,7 @@ int gbmd_compute_forces(gbmd_context* c, int flags) {
 int gbmd_push_f_v_r(gbmd_context* c, double dt, double dt_scale) {
   if (!c) return GBMD_ERR_INVALID;
   launch_push_f_v_r(c, dt, dt_scale);
-  c->forces_valid_step = -1;
+  c->forces_valid_step = c->rho_valid_step = -1;
   GBMD_CUDA(c, cudaGetLastError());
   return GBMD_OK;
 }
@@ -1105,7 +1125,7 @@ int gbmd_push_f_v(gbmd_context* c, double dt, double dt_scale) {
 int gbmd_push_min(gbmd_context* c, double dt, double dt_scale, double tolF) {
   if (!c) return GBMD_ERR_INVALID;
   launch_push_min(c, dt, dt_scale, tolF);
-  c->forces_valid_step = -1;
+  c->forces_valid_step = c->rho_valid_step = -1;
   GBMD_CUDA(c, cudaGetLastError());
   return GBMD_OK;
 }
@@ -1304,7 +1324,7 @@ int gbmd_run_minimize(gbmd_context* c, int nsteps, double dt, double tolF, int r
     if (rebuild_every > 0 && s % rebuild_every == 0 && (rc = do_rebuild(c, true))) return rc;
     if (trigger && (rc = rebuild_if_displaced(c))) return rc;
   }
-  c->forces_valid_step = -1;
+  c->forces_valid_step = c->rho_valid_step = -1;
   GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
   if (trigger && (rc = collect_device_rebuilds(c))) return rc;
   return check_device_errors(c);
@@ -1409,7 +1429,7 @@ int gbmd_profile_step(gbmd_context* c, int reps, double ms[5]) {
   cudaEventDestroy(e1);
   if (rc) return rc;
   GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
-  c->forces_valid_step = -1;
+  c->forces_valid_step = c->rho_valid_step = -1;
   return check_device_errors(c);
 }
 

@@ -228,9 +228,18 @@ class lj_multi_force(Operator):
 
 
 class eam_alloy_force(Operator):
-    """eam_rho, eam_rho2emb and eam_force in one call (eam_ghost single-pass
-    mode: the whole periodic system lives on one GPU, so no halo refresh of
-    rho_dEmb is needed between passes)."""
+    """eam_rho, eam_rho2emb and eam_force (eam_potential_multimat.cu
+    L101-104, L186-232): by default all three in one call (eam_ghost
+    single-pass mode: the whole periodic system lives on one GPU, so no halo
+    refresh of rho_dEmb is needed between passes).  The split run-file form
+    (multi_species_nosym_cs4.msp L8-16: one eam_alloy_force per pass) maps
+    onto the library's density pass, which also applies the embedding, and
+    its force pass:
+
+      eam_rho (with or without eam_rho2emb)  -> density + embedding pass
+      eam_rho2emb alone                      -> nothing (already applied)
+      eam_force alone                        -> force pass from the kept F'(rho)
+    """
     name = "eam_alloy_force"
     required = ("rcut", "parameters")
 
@@ -245,18 +254,29 @@ class eam_alloy_force(Operator):
             raise OperatorError("setfl file has %d elements, %d species declared" % (sf.nelements, len(sim.species)))
         if sf.nelements > 7:
             raise OperatorError("Maximum number of elements is 7")
-        for flag in ("eam_rho", "eam_rho2emb", "eam_force"):
-            if not self.slots.get(flag, True):
-                raise OperatorError("%s: split-pass execution is not offered; the three passes run fused" % flag)
+        rho, emb, frc = (bool(self.slots.get(k, True)) for k in ("eam_rho", "eam_rho2emb", "eam_force"))
+        if rho and frc:
+            self.passes = "all" if emb else None
+        elif rho:
+            self.passes = "density"
+        elif frc:
+            self.passes = "force" if not emb else None
+        else:
+            self.passes = "none"
+        if self.passes is None:
+            raise OperatorError("eam_rho2emb %s with eam_rho and eam_force both %s: the embedding runs with "
+                                "the density pass" % (emb, rho))
         if self.slots.get("eam_symmetry", False):
             raise OperatorError("eam_symmetry (Newton-3 scatter) is not offered; the full-list path is used")
         rcut = quantity(self.slots["rcut"])
         sim.ctx.set_eam_alloy(sf, rcut, EV * 1.0, EV)
         sim.rcut_max = max(sim.rcut_max, rcut)
-        sim.ghost_dist_max = max(sim.ghost_dist_max, 2.0 * rcut)
+        if (rho or frc) and self.slots.get("eam_ghost", True):
+            sim.ghost_dist_max = max(sim.ghost_dist_max, 2.0 * rcut)
 
     def execute(self, sim: Simulation, energy=True, virial=False):
-        sim.ctx.compute_forces(energy=energy, virial=virial)
+        if self.passes != "none":
+            sim.ctx.compute_forces(energy=energy, virial=virial, passes=self.passes)
 
 
 class johnson_force(Operator):

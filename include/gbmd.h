@@ -63,7 +63,18 @@ enum gbmd_potential {
 
 enum gbmd_force_flags {
   GBMD_FORCE_ENERGY = 1,    /* per-atom ep (trigger_thermo_state) */
-  GBMD_FORCE_VIRIAL = 2     /* per-atom virial tensor (compute_virial) */
+  GBMD_FORCE_VIRIAL = 2,    /* per-atom virial tensor (compute_virial) */
+  /* Split EAM passes (eam_alloy_force with eam_rho / eam_rho2emb / eam_force,
+   * src/potential/eam_potential_template/eam_potential_multimat.cu L101-104,
+   * L186-232).  Neither or both bits: every pass.  DENSITY alone: density +
+   * embedding (F'(rho) kept in the context; the embedding energy too with
+   * GBMD_FORCE_ENERGY).  FORCE alone: the final pair pass from the kept
+   * F'(rho); for EAM it needs a DENSITY call on the same positions and list
+   * (GBMD_ERR_INVALID otherwise), and energies need that call to have had
+   * GBMD_FORCE_ENERGY.  Pair potentials have no density pass: DENSITY
+   * alone does nothing and FORCE alone is the whole evaluation. */
+  GBMD_FORCE_PASS_DENSITY = 4,
+  GBMD_FORCE_PASS_FORCE = 8
 };
 
 /* ---- context --------------------------------------------------------------
