@@ -52,6 +52,8 @@ static void free_atoms(gbmd_context* c) {
   cudaFree(c->pfp);
   cudaFree(c->stage); cudaFree(c->rref); cudaFree(c->nnb); cudaFree(c->d_part); cudaFree(c->stage_r);
   cudaFree(c->h3acc);
+  cudaFree(c->epd);
+  c->epd = nullptr;
   c->stage_r = nullptr;
   c->h3acc = nullptr;
   c->ep = c->vir = nullptr;
@@ -80,6 +82,7 @@ int ensure_atom_capacity(gbmd_context* c, int64_t n) {
     GBMD_CUDA(c, cudaMalloc(&c->userb[b], sizeof(int32_t) * cap));
   }
   GBMD_CUDA(c, cudaMalloc(&c->ep, sizeof(double) * cap));
+  GBMD_CUDA(c, cudaMalloc(&c->epd, sizeof(double) * cap));
   GBMD_CUDA(c, cudaMalloc(&c->cellpack, sizeof(int32_t) * cap));
   GBMD_CUDA(c, cudaMalloc(&c->cell_of, sizeof(int32_t) * cap));
   GBMD_CUDA(c, cudaMalloc(&c->order, sizeof(int32_t) * cap));

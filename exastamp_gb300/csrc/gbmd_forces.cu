@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(256) k_eam_rho(PairArgs A, EamDev E, double* _
       phi *= E.conv_frho;
       fp *= E.conv_frho;
       fpd[i] = fp;
-      if (EV) A.ep[i] = phi;
+      if (EV) A.ep_emb[i] = phi;
     }
   }
 }
@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(256) k_eam_force(PairArgs A, EamDev E, const d
       for (int q = 0; q < 9; ++q) v[q] = group_reduce_d<T>(v[q]);
     }
     if (live && lane == 0) {
-      const double epv = EV ? A.ep[i] + e : 0.0;
+      const double epv = EV ? A.ep_emb[i] + e : 0.0;
       atom_epilogue<false>(A, i, ti, fx, fy, fz, 0.f, 0.f, 0.f, epv, EV ? v : nullptr);
     }
   }
@@ -262,6 +262,7 @@ PairArgs make_args(gbmd_context* c, const ForceFlags& f) {
   A.vx = c->VX(); A.vy = c->VY(); A.vz = c->VZ();
   A.ax = c->AX(); A.ay = c->AY(); A.az = c->AZ();
   A.ep = c->ep;
+  A.ep_emb = c->epd;
   A.vir = c->vir;
   A.type = c->TYPE();
   for (int t = 0; t < GBMD_MAX_TYPES; ++t) {

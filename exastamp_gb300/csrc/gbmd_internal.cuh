@@ -136,6 +136,7 @@ struct gbmd_context {
   int cur = 0;                            // which of r/posf/posd is current
   int cur_s = 0;                          // which of v/a/type/id/user is current
   double* ep = nullptr;
+  double* epd = nullptr;                  // FP64 EAM embedding energies (density pass -> force pass)
   double* vir = nullptr;                  // 9n, allocated when virials are requested
   int32_t* cellpack = nullptr;            // home cell at the last rebuild
   int32_t* cell_of = nullptr;             // scratch: linear cell per atom (pre-sort order)

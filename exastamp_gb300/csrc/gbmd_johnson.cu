@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(256) k_ej_rho(PairArgs A, JohnsonDev P, double
     double f, df;
     ej_embed_d(P, rho, f, df);
     fpd[i] = df;
-    if (EV) A.ep[i] = f;
+    if (EV) A.ep_emb[i] = f;
   }
 }
 
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(256) k_ej_force(PairArgs A, JohnsonDev P, cons
     for (int q = 0; q < 9; ++q) v[q] = group_reduce_d<T>(v[q]);
   }
   if (live && lane == 0) {
-    const double epv = EV ? A.ep[i] + e : 0.0;
+    const double epv = EV ? A.ep_emb[i] + e : 0.0;
     atom_epilogue<false>(A, i, ti, fx, fy, fz, 0.f, 0.f, 0.f, epv, EV ? v : nullptr);
   }
 }

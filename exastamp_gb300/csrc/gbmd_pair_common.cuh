@@ -35,6 +35,7 @@ struct PairArgs {
   double4_32a* posd_o;
   double *vx, *vy, *vz, *ax, *ay, *az;
   double* ep;
+  double* ep_emb;             // FP64 EAM: embedding energy F(rho_i) from the density pass
   double* vir;
   const uint8_t* type;
   double mass[GBMD_MAX_TYPES];
