@@ -447,14 +447,21 @@ def main():
     # at step 0 and every thermo_every steps; the standalone first half at
     # the start and after every thermo step but the last; the rebuild chain
     # (wrap/bin, 3 scan kernels, scatter, rank, gather, posf, list build) per
-    # rebuild, or with the trigger 14 gated launches every step (displacement
-    # test, 2 fills, the chain, copy-back, reference positions).
+    # rebuild.  With the trigger the kernels that move the atoms test them, and
+    # a graph step launches the conditional's setter, plus the 13-kernel
+    # rebuild body (2 fills, the chain, copy-back, reference positions) when
+    # the gate opens; the steps after the last whole graph chunk run the 13
+    # gated launches every step.
     n_thermo = args.steps // thermo_every if thermo_every else 0
     last_is_thermo = bool(thermo_every) and args.steps % thermo_every == 0
     gpu_launches = kernels_per_step * (args.steps + (1 if thermo_every else 0))
     gpu_launches += 2 * (n_thermo + (1 if thermo_every else 0))
     gpu_launches += 1 + n_thermo - (1 if last_is_thermo else 0)
-    gpu_launches += 14 * args.steps if R < 0 else 9 * rebuilds
+    if R < 0:
+        n_graph = ((args.steps - 1) // thermo_every) * thermo_every
+        gpu_launches += n_graph + 13 * rebuilds + 13 * (args.steps - n_graph)
+    else:
+        gpu_launches += 9 * rebuilds
 
     out = {"metric": "atom-timesteps/s", "value": value, "unit": "atom-timesteps/s", "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,

@@ -292,15 +292,21 @@ static int rebuild_if_displaced(gbmd_context* c) {
   if (c->n == 0) return GBMD_OK;
   int* gate = c->d_err + ERRW_GATE;
   const double thr = 0.5 * c->skin;
-  GBMD_CUDA(c, cudaMemsetAsync(gate, 0, sizeof(int), c->stream));
-  k_displ_over<<<nblk(c->n, 256), 256, 0, c->stream>>>(c->n, c->X(), c->Y(), c->Z(), c->rref, c->cap, thr * thr,
-                                                        gate);
+  if (!c->fused_trigger) {
+    GBMD_CUDA(c, cudaMemsetAsync(gate, 0, sizeof(int), c->stream));
+    k_displ_over<<<nblk(c->n, 256), 256, 0, c->stream>>>(c->n, c->X(), c->Y(), c->Z(), c->rref, c->cap, thr * thr,
+                                                          gate);
+  }
+  // fused_trigger: the kernel that moved the atoms (the force pass's fused
+  // first half, or k_first_half) has already tested them and raised the gate;
+  // it is cleared once the chain has read it, for the next such kernel
   if (!c->capturing) {
     // launched step by step: the chain's kernels check the gate themselves
     int rc = rebuild(c, false, gate);
     if (rc) return rc;
     k_copy_rref_gated<<<chain_blocks(c, c->n, 256, gate, 8), 256, 0, c->stream>>>(
         c->n, c->rbuf[c->cur], c->rref, c->cap, gate, c->d_err + ERRW_REBUILDS);
+    if (c->fused_trigger) GBMD_CUDA(c, cudaMemsetAsync(gate, 0, sizeof(int), c->stream));
     return GBMD_OK;
   }
   // Inside a graph capture the chain goes into the body of an IF conditional
@@ -342,6 +348,7 @@ static int rebuild_if_displaced(gbmd_context* c) {
   if (rc) return rc;
   if (e != cudaSuccess) return check_cuda(c, e, "conditional body capture");
   GBMD_CUDA(c, cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  if (c->fused_trigger) GBMD_CUDA(c, cudaMemsetAsync(gate, 0, sizeof(int), c->stream));
   return GBMD_OK;
 }
 
@@ -1150,6 +1157,13 @@ struct StepPlan {
   bool rebuild, thermo, last, trigger;
 };
 
+// Sets the context's fused-trigger mode for the lifetime of one run_nve.
+struct FusedTriggerScope {
+  gbmd_context* c;
+  FusedTriggerScope(gbmd_context* ctx, bool on) : c(ctx) { c->fused_trigger = on; }
+  ~FusedTriggerScope() { c->fused_trigger = false; }
+};
+
 static int one_step(gbmd_context* c, double dt, const StepPlan& p, bool check, double* thermo_row) {
   int rc;
   if (p.rebuild && (rc = do_rebuild(c, check))) return rc;
@@ -1256,9 +1270,15 @@ int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int 
     GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
     return check_device_errors(c);
   }
-  launch_first_half(c, dt);
   const int R = rebuild_every;
   const bool trigger = R == GBMD_REBUILD_ON_DISPLACEMENT;
+  // with the trigger, each kernel that moves the atoms tests them as it
+  // writes them (the force pass's fused first half, k_first_half), so the
+  // decision is ready when the next step starts and no separate test kernel
+  // runs; the gate starts cleared
+  if (trigger) GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_GATE, 0, sizeof(int), c->stream));
+  const FusedTriggerScope fused(c, trigger);
+  launch_first_half(c, dt);
   // graph chunk length: two rebuild intervals, or with the trigger the thermo
   // interval when it is even (20 steps without thermo)
   const int G = trigger ? (want_thermo ? thermo_every : 20) : 2 * R;

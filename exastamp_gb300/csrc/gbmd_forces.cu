@@ -270,6 +270,11 @@ PairArgs make_args(gbmd_context* c, const ForceFlags& f) {
     A.inv_massf[t] = (float)(1.0 / A.mass[t]);
   }
   A.fuse = f.fuse;
+  const bool test = c->fused_trigger && f.fuse == FUSE_PUSH2_PUSH1;
+  A.gate = test ? c->d_err + ERRW_GATE : nullptr;
+  A.rref = c->rref;
+  A.rcap = c->cap;
+  A.thr2 = (0.5 * c->skin) * (0.5 * c->skin);
   A.want_energy = f.energy ? 1 : 0;
   A.want_virial = f.virial ? 1 : 0;
   A.dt = f.sp.dt;

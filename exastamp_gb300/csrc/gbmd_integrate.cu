@@ -38,6 +38,10 @@ struct PushArgs {
   double4_32a* pd;
   Grid g;
   int refresh;
+  int* gate;  // k_first_half under the displacement trigger (else null)
+  const double* rref;
+  int64_t rcap;
+  double thr2;
 };
 
 __global__ void k_push_f_v_r(PushArgs P, double h, double h2) {
@@ -76,6 +80,7 @@ __global__ void k_first_half(PushArgs P, double h, double h2, double hv) {
   P.vy[i] = __dadd_rn(vy, __dmul_rn(ay, hv));
   P.vz[i] = __dadd_rn(vz, __dmul_rn(az, hv));
   if (P.refresh) refresh_gather(P.g, i, P.cellpack[i], P.type[i], x, y, z, P.pf, P.pd);
+  if (P.gate) displacement_test(P.gate, P.rref, P.rcap, P.thr2, i, x, y, z);
 }
 
 __global__ void k_push_min(PushArgs P, double h2, double tolF) {
@@ -112,6 +117,10 @@ static PushArgs push_args(gbmd_context* c) {
   P.pd = c->POSD();
   P.g = c->grid;
   P.refresh = c->list_valid ? 1 : 0;
+  P.gate = c->fused_trigger ? c->d_err + ERRW_GATE : nullptr;
+  P.rref = c->rref;
+  P.rcap = c->cap;
+  P.thr2 = (0.5 * c->skin) * (0.5 * c->skin);
   return P;
 }
 

@@ -180,6 +180,7 @@ struct gbmd_context {
   int tpa = 1;                  // lanes per atom (autotuned; default = the GB300 optimum)
   int vec = 4;                  // list entries per lane per load (1 or 4, mixed kernels; autotuned)
   bool staged = false;          // 1 lane x 4 entries: neighbour positions from shared memory
+  bool fused_trigger = false;   // run_nve with the displacement trigger: kernels that move atoms test them
   bool newton3 = false;         // half list (j > i in cell order) + scattered reaction forces (LJ, mixed)
   float4* h3acc = nullptr;      // Newton-3 accumulators, 3 float4 per atom: (f, ep), virial xx yy zz xy, xz yz
   int block = 256;              // threads per block of the pair / force kernels (autotuned)
@@ -283,6 +284,16 @@ int thermo_blocks(int64_t n);
     cudaError_t e_ = (call);                                \
     if (e_ != cudaSuccess) return gbmd::check_cuda((c), e_, #call); \
   } while (0)
+
+// particle_displ_over for one atom at its new position: raise the gate when
+// it moved more than sqrt(thr2) since the last rebuild (|dr|^2 summed x, y, z
+// without contraction, as the standalone test kernel does).
+__device__ __forceinline__ void displacement_test(int* gate, const double* __restrict__ rref, int64_t cap,
+                                                  double thr2, int64_t i, double x, double y, double z) {
+  const double dx = __dsub_rn(x, rref[i]), dy = __dsub_rn(y, rref[cap + i]), dz = __dsub_rn(z, rref[2 * cap + i]);
+  const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  if (d2 > thr2) *gate = 1;
+}
 
 __device__ __forceinline__ void kahan_add(float& s, float& comp, float v) {
   const float y = v - comp;

@@ -41,6 +41,10 @@ struct PairArgs {
   double mass[GBMD_MAX_TYPES];
   float inv_massf[GBMD_MAX_TYPES];
   int fuse;
+  int* gate;                  // fuse 2 with the displacement trigger: set when an atom moved > skin/2
+  const double* rref;         // positions at the last rebuild (3 planes of rcap)
+  int64_t rcap;
+  double thr2;                // (skin/2)^2
   int want_energy, want_virial;
   double dt, dth, dt2h;
   int* err;
@@ -119,6 +123,7 @@ __device__ __forceinline__ void atom_epilogue(const PairArgs& A, int64_t i, int 
       A.xo[i] = x;
       A.yo[i] = y;
       A.zo[i] = z;
+      if (A.gate) displacement_test(A.gate, A.rref, A.rcap, A.thr2, i, x, y, z);
       int cx, cy, cz;
       unpack_cell(A.cellpack[i], cx, cy, cz);
       A.posf_o[i] = make_float4((float)(x - (double)cx * A.g.h[0] - A.g.lo[0]),
