@@ -94,6 +94,7 @@ def lib(path: str = LIB_PATH):
             "gbmd_run_minimize": ([vp, i32, dbl, dbl, i32], i32),
             "gbmd_set_eam_johnson": ([vp, vp, dbl], i32),
             "gbmd_lj_loss_grad": ([vp, vp, vp, vp, vp, dbl, dbl, P(dbl), vp], i32),
+            "gbmd_lj_multi_loss_grad": ([vp, vp, vp, vp, vp, dbl, dbl, P(dbl), vp, vp], i32),
             "gbmd_list_builds": ([vp, P(i64)], i32),
             "gbmd_thermo": ([vp, vp], i32),
             "gbmd_device_state": ([vp] + [vp] * 11, i32),
@@ -210,6 +211,7 @@ class Context:
     def set_lj_multi(self, eps, sig, rc, rcut_common=0.0):
         eps, sig, rc = _f64(eps), _f64(sig), _f64(rc)
         self._chk(self._L.gbmd_set_lj_multi(self.h, eps.shape[0], _p(eps), _p(sig), _p(rc), float(rcut_common)))
+        self._lj_ntypes = int(eps.shape[0])
 
     def set_eam_alloy(self, sf, rcut, conv_z2r, conv_frho):
         frho = np.ascontiguousarray(np.stack(sf.frho), np.float64)
@@ -343,6 +345,21 @@ class Context:
         self._chk(self._L.gbmd_lj_loss_grad(self.h, _p(fx), _p(fy), _p(fz), _p(et), float(w_force), float(w_energy),
                                             C.byref(loss), _p(g)))
         return loss.value, g
+
+    def lj_multi_loss_grad(self, f_target, e_target, w_force, w_energy):
+        """The same loss for lj_multi_force; returns (loss, dL/deps, dL/dsigma)
+        with the gradients as symmetric ntypes x ntypes arrays (one parameter
+        per unordered species pair)."""
+        ft = np.asarray(f_target, dtype=np.float64)
+        fx, fy, fz = (np.ascontiguousarray(ft[:, d]) for d in range(3))
+        et = _f64(e_target)
+        nt = getattr(self, "_lj_ntypes", 0)
+        if not nt:
+            raise GbmdError(1, "set_lj_multi first")
+        loss, ge, gs = C.c_double(), np.zeros((nt, nt)), np.zeros((nt, nt))
+        self._chk(self._L.gbmd_lj_multi_loss_grad(self.h, _p(fx), _p(fy), _p(fz), _p(et), float(w_force),
+                                                  float(w_energy), C.byref(loss), _p(ge), _p(gs)))
+        return loss.value, ge, gs
 
     def list_builds(self):
         n = C.c_int64(0)

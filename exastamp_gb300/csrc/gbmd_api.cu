@@ -5,6 +5,7 @@
 // into the compute_force / verlet_first_half / verlet_second_half /
 // update_particle_neighbors slots (data/config/config_numerical_schemes.msp
 // L8-52, data/config/config_move_particles.msp L54-68).
+#include <vector>
 #include <cerrno>
 #include <cmath>
 #include <cstdarg>
@@ -1389,6 +1390,55 @@ int gbmd_lj_loss_grad(gbmd_context* c, const double* fx_target, const double* fy
   *loss = c->h_thermo[0];
   grad[0] = c->h_thermo[1];
   grad[1] = c->h_thermo[2];
+  return check_device_errors(c);
+}
+
+int gbmd_lj_multi_loss_grad(gbmd_context* c, const double* fx_target, const double* fy_target,
+                            const double* fz_target, const double* e_target, double w_force, double w_energy,
+                            double* loss, double* grad_eps, double* grad_sigma) {
+  if (!c || !fx_target || !fy_target || !fz_target || !e_target || !loss || !grad_eps || !grad_sigma)
+    return GBMD_ERR_INVALID;
+  if (c->pot != GBMD_POT_LJ_MULTI) return set_error(c, GBMD_ERR_INVALID, "the LJ-mixture adjoint needs lj_multi_force");
+  if (c->newton3) return set_error(c, GBMD_ERR_UNSUPPORTED, "the LJ adjoint reads the full list (switch Newton-3 off)");
+  const int nt = c->lj.ntypes;
+  const int64_t n = c->n;
+  if (n == 0) {
+    *loss = 0.0;
+    for (int q = 0; q < nt * nt; ++q) grad_eps[q] = grad_sigma[q] = 0.0;
+    return GBMD_OK;
+  }
+  int rc = gbmd_compute_forces(c, GBMD_FORCE_ENERGY);
+  if (rc) return rc;
+  const int K = 1 + nt * (nt + 1);  // loss + 2 per unordered type pair
+  const size_t args_words = (gbmd::lj_multi_adj_args_size() + sizeof(double) - 1) / sizeof(double);
+  const int64_t need = 4 * n + (int64_t)K * n + (int64_t)K * 593 + (int64_t)args_words;
+  if (need > c->adj_cap) {
+    cudaFree(c->adj_scratch);
+    c->adj_scratch = nullptr;
+    GBMD_CUDA(c, cudaMalloc(&c->adj_scratch, sizeof(double) * need));
+    c->adj_cap = need;
+  }
+  double* t = c->adj_scratch;
+  const double* host[4] = {fx_target, fy_target, fz_target, e_target};
+  double* dev[4] = {t, t + n, t + 2 * n, t + 3 * n};
+  if ((rc = upload_arrays(c, host, dev, 4))) return rc;
+  ForceFlags f;
+  const PairArgs A = make_args(c, f);
+  const double* tg[4] = {dev[0], dev[1], dev[2], dev[3]};
+  double* scratch = t + 4 * n;
+  void* args_dev = scratch + (size_t)K * n + (size_t)K * 593;
+  int nu = 0;
+  if ((rc = launch_lj_multi_loss_grad(c, A, tg, w_force, w_energy, args_dev, scratch, &nu))) return rc;
+  std::vector<double> h(K);
+  GBMD_CUDA(c, cudaMemcpy(h.data(), scratch + (size_t)K * n + (size_t)K * 592, sizeof(double) * K,
+                          cudaMemcpyDeviceToHost));
+  *loss = h[0];
+  int u = 0;
+  for (int a = 0; a < nt; ++a)
+    for (int b = a; b < nt; ++b, ++u) {
+      grad_eps[a * nt + b] = grad_eps[b * nt + a] = h[1 + u];
+      grad_sigma[a * nt + b] = grad_sigma[b * nt + a] = h[1 + nu + u];
+    }
   return check_device_errors(c);
 }
 

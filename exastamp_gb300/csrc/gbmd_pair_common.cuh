@@ -60,6 +60,12 @@ PairArgs make_args(gbmd_context* c, const ForceFlags& f);
 // lj_compute_force parameter adjoint (gbmd_adjoint_lj.cu): targets are
 // cell-sorted device arrays fx, fy, fz, e; scratch holds 3n + 1779 doubles and
 // receives (loss, dL/deps, dL/dsigma) at its end.
+// lj_multi_force adjoint (gbmd_adjoint_lj.cu): args_dev holds
+// lj_multi_adj_args_size() bytes; scratch K n + K * 593 doubles with
+// K = 1 + 2 nu (nu unordered type pairs, returned), sums at its end.
+int launch_lj_multi_loss_grad(gbmd_context* c, const PairArgs& A, const double* const targets[4], double wF,
+                              double wE, void* args_dev, double* scratch, int* nu_out);
+size_t lj_multi_adj_args_size();
 int launch_lj_loss_grad(gbmd_context* c, const PairArgs& A, const double* const targets[4], double wF, double wE,
                         double* scratch);
 // johnson_force kernels, both precisions (gbmd_johnson.cu).

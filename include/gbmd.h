@@ -255,6 +255,13 @@ int gbmd_run_minimize(gbmd_context* ctx, int nsteps, double dt, double tolF, int
  * dL/d(epsilon, sigma) with every pair term recomputed in FP64.  grad[2]. */
 int gbmd_lj_loss_grad(gbmd_context* ctx, const double* fx_target, const double* fy_target, const double* fz_target,
                       const double* e_target, double w_force, double w_energy, double* loss, double grad[2]);
+/* The same loss for lj_multi_force: gradients with respect to each species
+ * pair's (epsilon, sigma), the (a,b) and (b,a) table entries being one
+ * parameter.  grad_eps and grad_sigma receive ntypes x ntypes row-major
+ * (symmetric) arrays. */
+int gbmd_lj_multi_loss_grad(gbmd_context* ctx, const double* fx_target, const double* fy_target,
+                            const double* fz_target, const double* e_target, double w_force, double w_energy,
+                            double* loss, double* grad_eps, double* grad_sigma);
 
 /* Number of neighbour-list builds since the context was created, including
  * the displacement-triggered ones (counted on the device, folded in when
