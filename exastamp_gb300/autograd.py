@@ -1,8 +1,14 @@
-"""torch.autograd.Function bindings of the two parameter adjoints.
+"""torch.autograd.Function bindings of the parameter adjoints.
 
 * ``LJLoss.apply(params, context, rcut, f_target, e_target, w_force,
   w_energy)`` -- params = tensor [epsilon, sigma]; one system held by a
   ``_capi.Context`` (gbmd_lj_loss_grad).
+* ``LJMultiLoss.apply(eps, sigma, context, rc, f_target, e_target, w_force,
+  w_energy)`` -- eps, sigma = symmetric (ntypes, ntypes) tensors, rc the
+  per-pair cutoffs (lj_multi_force; gbmd_lj_multi_loss_grad).  An (a, b)
+  entry and its (b, a) mirror are one parameter of the potential; backward
+  gives each of them half of that parameter's derivative (a != b), so a
+  symmetric parametrisation (e.g. U + U.T) receives the exact gradient.
 * ``EamLoss.apply(params, batch, cfg, rcut, f_target, e_target, w_force,
   w_energy)`` -- params = tensor of the 9 analytic parameters in
   ``setfl.PARAM_NAMES`` order; the configurations held by a ``_capi.Batch``
@@ -37,6 +43,25 @@ class LJLoss(torch.autograd.Function):
     def backward(ctx, g_out):
         (g,) = ctx.saved_tensors
         return g_out * g, None, None, None, None, None, None
+
+
+class LJMultiLoss(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, eps, sigma, context, rc, f_target, e_target, w_force, w_energy):
+        e = eps.detach().to("cpu", torch.float64).numpy()
+        sg = sigma.detach().to("cpu", torch.float64).numpy()
+        if not (np.array_equal(e, e.T) and np.array_equal(sg, sg.T)):
+            raise ValueError("eps and sigma must be symmetric")
+        context.set_lj_multi(e, sg, np.asarray(rc, dtype=np.float64), 0.0)
+        loss, ge, gs = context.lj_multi_loss_grad(f_target, e_target, w_force, w_energy)
+        half = np.where(np.eye(len(e), dtype=bool), 1.0, 0.5)
+        ctx.save_for_backward(torch.as_tensor(ge * half, dtype=eps.dtype), torch.as_tensor(gs * half, dtype=eps.dtype))
+        return torch.as_tensor(loss, dtype=eps.dtype)
+
+    @staticmethod
+    def backward(ctx, g_out):
+        ge, gs = ctx.saved_tensors
+        return g_out * ge, g_out * gs, None, None, None, None, None, None
 
 
 class EamLoss(torch.autograd.Function):

@@ -149,3 +149,41 @@ def test_lj_multi_loss_gradient(gpu, oracle):
     su = lambda m: m[0, 0] + m[0, 1] + m[1, 1]  # noqa: E731  (one entry per unordered pair)
     assert abs(su(ge2) - g1[0]) < 1e-9 * abs(g1[0])
     assert abs(su(gs2) - g1[1]) < 1e-9 * abs(g1[1])
+
+
+def test_lj_multi_autograd_symmetric_parametrisation(gpu):
+    """LJMultiLoss through a symmetric parametrisation (upper triangle ->
+    U + U.T - diag): torch's gradient equals the adjoint's per-pair one."""
+    from exastamp_gb300.autograd import LJMultiLoss
+    s = S.lj_fcc(ncell=4, seed=32)
+    rng = np.random.default_rng(32)
+    for a in (s.x, s.y, s.z):
+        a += rng.normal(0.0, 0.05, s.n)
+    s.type = (rng.random(s.n) < 0.3).astype(np.uint8)
+    s.masses = np.array([1.0, 1.5])
+    eps, sig, rc = S.kob_andersen_tables()
+    wF, wE = 1.0 / s.n, 0.1 / s.n
+    with gpu.Context(0) as ctx:
+        ctx.upload_system(s)
+        ctx.set_skin(0.3)
+        ctx.set_precision(False)
+        ctx.set_lj_multi(eps * 0.95, sig * 1.02, rc, 0.0)
+        ctx.compute_forces(energy=True)
+        d = ctx.download()
+        Ft = np.stack([d["ax"], d["ay"], d["az"]], 1) * s.masses[s.type][:, None]
+        Et = d["ep"].copy()
+        iu = np.triu_indices(2)
+        ue = torch.tensor(eps[iu], dtype=torch.float64, requires_grad=True)
+        us = torch.tensor(sig[iu], dtype=torch.float64, requires_grad=True)
+
+        def sym(u):
+            m = torch.zeros(2, 2, dtype=torch.float64)
+            m = m.index_put((torch.tensor(iu[0]), torch.tensor(iu[1])), u)
+            return m + m.T - torch.diag(torch.diag(m))
+
+        loss = LJMultiLoss.apply(sym(ue), sym(us), ctx, rc, Ft, Et, wF, wE)
+        loss.backward()
+        ref_loss, ge, gs = ctx.lj_multi_loss_grad(Ft, Et, wF, wE)
+    assert abs(float(loss.detach()) - ref_loss) < 1e-12 * ref_loss
+    assert np.allclose(ue.grad.numpy(), ge[iu], rtol=1e-12, atol=0)
+    assert np.allclose(us.grad.numpy(), gs[iu], rtol=1e-12, atol=0)
