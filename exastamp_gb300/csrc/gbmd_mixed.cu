@@ -592,7 +592,7 @@ __global__ void __launch_bounds__(256) k_eam_force_staged(PairArgs A, EamDev E, 
 // result is not bit-reproducible (the full-list kernels are).
 // ---------------------------------------------------------------------------
 template <bool EV, bool MULTI>
-__global__ void __launch_bounds__(256) k_lj_half(PairArgs A, LJF P, const LJPair* __restrict__ tab, int ntypes,
+__global__ void __launch_bounds__(256, EV ? 1 : 4) k_lj_half(PairArgs A, LJF P, const LJPair* __restrict__ tab, int ntypes,
                                                  double rcmax2, float4* __restrict__ acc, int64_t cap) {
   __shared__ LJTabSmem tb;
   if (MULTI) lj_load_table(tb, tab, ntypes);
