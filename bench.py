@@ -291,7 +291,7 @@ def run_reference(args, w, ws, rank):
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded FCC lattice, Maxwell-Boltzmann velocities)",
-            "config": {"workload": args.workload, "description": w["desc"], "sample_atoms": s.n},
+            "config": {"workload": args.workload, "description": w["desc"], "atoms": s.n},
             "cpu_baseline": {"value": value, "unit": "atom-timesteps/s", "cores": O.num_threads(),
                              "kind": "port", "sample": sample,
                              "note": "reference unbuildable here (needs onika, exaNBody, yaml-cpp, MPI); "

@@ -29,11 +29,13 @@
 //   dL/dtheta = sum_i [gE_i dF + G_i dF'] + sum_ij [ (gE_i/2r - s_ij/r^2) dz2
 //               + (s_ij/r) dz2' + s_ij (F'_i + F'_j) drho' + lam_i drho ]
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstring>
 #include <numeric>
 #include <vector>
 
+#include "gbmd_batch_grid.h"
 #include "gbmd_internal.cuh"
 
 namespace {
@@ -270,17 +272,8 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs A) {
       g.lo[d] = A.lo[3 * r + d];
       g.L[d] = A.L[3 * r + d];
       g.hi[d] = A.hi[3 * r + d];
-      const double cell_min = A.rcut / A.S * (1.0 + 0x1p-40);
-      int q = (int)floor(g.L[d] / cell_min);
-      g.nc[d] = q < A.S ? A.S : q;
     }
-    while ((int64_t)g.nc[0] * g.nc[1] * g.nc[2] > MAXC) {  // coarser cells still cover rcut
-      int dm = 0;
-      for (int d = 1; d < 3; ++d)
-        if (g.nc[d] > g.nc[dm]) dm = d;
-      g.nc[dm] -= 1;
-    }
-    g.ncells = g.nc[0] * g.nc[1] * g.nc[2];
+    g.ncells = gbmd::batch_grid_dims(g.L, A.rcut, A.S, MAXC, g.nc);
     for (int d = 0; d < 3; ++d) {
       g.h[d] = g.L[d] / g.nc[d];
       g.inv_h[d] = (double)g.nc[d] / g.L[d];
@@ -778,8 +771,8 @@ int gbmd_batch_upload(gbmd_batch* b, int nrep, const int64_t* offsets, const dou
     const int64_t m = offsets[r + 1] - offsets[r];
     if (m < 0) return berr(b, GBMD_ERR_INVALID, "offsets must be non-decreasing");
     if (m > BMAX_ATOMS) return berr(b, GBMD_ERR_TOO_LARGE, "replica %d has %lld atoms (max %d)", r, (long long)m, BMAX_ATOMS);
-    for (int d = 0; d < 3; ++d)
-      if (!(hi[3 * r + d] > lo[3 * r + d])) return berr(b, GBMD_ERR_INVALID, "replica %d: empty box", r);
+    if (!gbmd::batch_box_ok(lo + 3 * r, hi + 3 * r))
+      return berr(b, GBMD_ERR_INVALID, "replica %d: empty or non-finite box", r);
   }
   cudaSetDevice(b->device);
   cudaStreamSynchronize(b->stream);

@@ -171,9 +171,6 @@ void launch_push_min(gbmd_context* c, double dt, double dt_scale, double tolF) {
 // --------------------------------------------------------------------------
 // thermodynamic reduction
 // --------------------------------------------------------------------------
-constexpr int TH_THREADS = 256;
-constexpr int TH_MAX_BLOCKS = 1184;  // 8 x 148; fixed so the sum order is fixed
-
 int thermo_blocks(int64_t n) {
   int64_t b = (n + TH_THREADS - 1) / TH_THREADS;
   if (b < 1) b = 1;
@@ -185,6 +182,7 @@ struct ThermoArgs {
   int64_t n;
   const double *vx, *vy, *vz, *ep, *vir;
   const uint8_t* type;
+  int ntypes;
   double mass[GBMD_MAX_TYPES];
 };
 
@@ -193,7 +191,10 @@ __global__ void __launch_bounds__(TH_THREADS) k_thermo_part(ThermoArgs T, double
 #pragma unroll
   for (int q = 0; q < 26; ++q) s[q] = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < T.n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double m = T.mass[T.type[i]];
+    // a type outside [0, ntypes) has no mass: it makes the mass-weighted
+    // sums NaN instead of reading past the table
+    const unsigned ti = T.type[i];
+    const double m = ti < (unsigned)T.ntypes ? T.mass[ti] : __longlong_as_double(0x7ff8000000000000ll);
     const double v[3] = {T.vx[i], T.vy[i], T.vz[i]};
     if (T.vir) {
 #pragma unroll
@@ -257,6 +258,7 @@ void launch_thermo_raw(int64_t n, const double* vx, const double* vy, const doub
   T.ep = ep;
   T.vir = vir;
   T.type = type;
+  T.ntypes = ntypes;
   for (int t = 0; t < GBMD_MAX_TYPES; ++t) T.mass[t] = t < ntypes ? mass[t] : 1.0;
   const int nb = thermo_blocks(n);
   k_thermo_part<<<nb, TH_THREADS, 0, s>>>(T, part);
@@ -270,6 +272,7 @@ void launch_thermo(gbmd_context* c, bool with_virial) {
   T.ep = c->ep;
   T.vir = (with_virial && c->vir) ? c->vir : nullptr;
   T.type = c->TYPE();
+  T.ntypes = c->ntypes > 0 ? c->ntypes : GBMD_MAX_TYPES;
   for (int t = 0; t < GBMD_MAX_TYPES; ++t) T.mass[t] = t < c->ntypes ? c->mass[t] : 1.0;
   const int nb = thermo_blocks(c->n);
   k_thermo_part<<<nb, TH_THREADS, 0, c->stream>>>(T, c->d_part);

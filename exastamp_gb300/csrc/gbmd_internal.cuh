@@ -272,6 +272,12 @@ void launch_thermo(gbmd_context* c, bool with_virial);
 void launch_thermo_raw(int64_t n, const double* vx, const double* vy, const double* vz, const double* ep,
                        const double* vir, const uint8_t* type, const double* mass, int ntypes, double* part,
                        double* out, cudaStream_t s);
+// The thermodynamic reduction runs TH_THREADS-thread blocks, at most
+// TH_MAX_BLOCKS of them (about eight per SM): a fixed cap, so the summation
+// order depends on the atom count only, and the partial buffer of any call
+// holds at most TH_MAX_BLOCKS x 26 doubles.
+constexpr int TH_THREADS = 256;
+constexpr int TH_MAX_BLOCKS = 1184;
 int thermo_blocks(int64_t n);
 
 }  // namespace gbmd

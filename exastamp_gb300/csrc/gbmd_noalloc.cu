@@ -10,38 +10,29 @@
 // acceptable.  gbmd_thermo_reduce_noalloc() runs the same two reduction
 // kernels on the caller's device arrays and uses, as scratch, a fixed array
 // in this library's own device image instead of an allocation.
-#include <mutex>
-
 #include "gbmd_internal.cuh"
 
 namespace {
 
-// One row of 26 partial sums per reduction block; the reduction never uses
-// more than this many blocks (thermo_blocks() caps the grid at 1184), so the
-// scratch is 1184 x 26 doubles = 246,272 bytes on every device that loads
-// the library, held until the process exits.
-constexpr int kScratchRows = 1184;
-constexpr int kMaxDevices = 64;
+// One row of 26 partial sums per reduction block.  The reduction never uses
+// more than TH_MAX_BLOCKS blocks, so the scratch is TH_MAX_BLOCKS x 26
+// doubles (1184 x 26 = 246,272 bytes) on every device that loads the
+// library, held until the process exits.
+constexpr int kScratchRows = gbmd::TH_MAX_BLOCKS;
+static_assert(kScratchRows >= gbmd::TH_MAX_BLOCKS, "thermo scratch smaller than the reduction grid");
 
 static __device__ __align__(256) double g_thermo_scratch[kScratchRows * 26];
 
-std::mutex g_setup_mutex;
-double* g_scratch_on_device[kMaxDevices] = {nullptr};
-
-// Device address of the scratch array for the current device, looked up
-// once per device with that device current.
+// Device address of the scratch array in the current device's context.  It
+// is looked up on every call (a host-side table lookup that allocates
+// nothing), so it stays right when the context has been torn down and
+// re-created in between, e.g. after cudaDeviceReset, where a cached address
+// would point into the old module.
 int scratch_for_current_device(double** out) {
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess) return GBMD_ERR_CUDA;
-  if (dev < 0 || dev >= kMaxDevices) return GBMD_ERR_UNSUPPORTED;
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_on_device[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_thermo_scratch);
-    if (e != cudaSuccess || !p) return GBMD_ERR_CUDA;
-    g_scratch_on_device[dev] = static_cast<double*>(p);
-  }
-  *out = g_scratch_on_device[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_thermo_scratch);
+  if (e != cudaSuccess || !p) return GBMD_ERR_CUDA;
+  *out = static_cast<double*>(p);
   return GBMD_OK;
 }
 
@@ -54,7 +45,6 @@ extern "C" int gbmd_thermo_reduce_noalloc(int64_t n, const double* vx, const dou
   if (n > GBMD_MAX_ATOMS) return GBMD_ERR_TOO_LARGE;
   if (ntypes < 1 || ntypes > GBMD_MAX_TYPES || !masses || !out) return GBMD_ERR_INVALID;
   if (n > 0 && (!vx || !vy || !vz || !type)) return GBMD_ERR_INVALID;
-  if (gbmd::thermo_blocks(n) > kScratchRows) return GBMD_ERR_TOO_LARGE;
   double* scratch = nullptr;
   const int rc = scratch_for_current_device(&scratch);
   if (rc != GBMD_OK) return rc;

@@ -283,7 +283,9 @@ int gbmd_thermo(gbmd_context* ctx, double out[27]);
  * latency-critical loop that cannot afford the device-wide synchronisation
  * an allocation can cause.
  *   vx, vy, vz, ep (may be NULL), vir (n x 9, may be NULL), type: device
- *   arrays of n atoms; type values must be < ntypes.  masses: HOST array of
+ *   arrays of n atoms; type values must be < ntypes (an atom of another
+ *   type is checked on the device and turns the mass-weighted sums --
+ *   out[9..23] and out[25] -- into NaN).  masses: HOST array of
  *   ntypes doubles (ntypes <= 8).  out: DEVICE array of 27 doubles, same
  *   layout as gbmd_thermo.  stream: cudaStream_t (NULL = default stream).
  *   The work is enqueued on `stream`; nothing is synchronised.
@@ -292,9 +294,11 @@ int gbmd_thermo(gbmd_context* ctx, double out[27]);
  * the process exits; every partial it uses is overwritten before it is read,
  * so no clearing is needed.  All calls on a device share that array: calls
  * whose kernels overlap on the GPU (different streams, no ordering between
- * them) race and give wrong sums.  The first call on a device looks the
- * array's address up (cudaGetSymbolAddress) with that device current; make
- * that first call before any stream capture.  n > 67,108,864 atoms returns
+ * them) race and give wrong sums.  Every call looks the array's address up
+ * (cudaGetSymbolAddress, no allocation) with the caller's device current,
+ * so the address stays valid across a cudaDeviceReset; the first call on a
+ * device also loads the library's device code there, so make that first
+ * call before any stream capture.  n > 67,108,864 atoms returns
  * GBMD_ERR_TOO_LARGE; bad pointers or ntypes return GBMD_ERR_INVALID. */
 int gbmd_thermo_reduce_noalloc(int64_t n, const double* vx, const double* vy, const double* vz,
                                const double* ep, const double* vir, const uint8_t* type,

@@ -19,7 +19,9 @@ from exastamp_gb300 import setfl
 
 import golden_setfl as G
 
-REF = os.environ.get("EXASTAMP_ROOT", "/root/reference")
+# the exaStamp source tree, when readable (set EXASTAMP_ROOT to check the
+# fixture against the original files)
+REF = os.environ.get("EXASTAMP_ROOT", "")
 
 
 def oracle_lattice(oracle, sf, case, a):
@@ -50,7 +52,7 @@ def test_oracle_lattice_known_answers(oracle, k):
         assert abs(P0) < 1e-8, P0
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "data", "potentials")),
+@pytest.mark.skipif(not REF or not os.path.isdir(os.path.join(REF, "data", "potentials")),
                     reason="exaStamp sources not present")
 def test_fixture_matches_exastamp_files(oracle):
     """The committed windows are the files' own values, and a lattice
