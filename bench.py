@@ -64,9 +64,10 @@ WORKLOADS = {
                        desc="LJ FCC 20^3 cells (32,000 atoms), rho*=0.8442, rc 2.5, skin 0.3, T*=1, "
                             "dt 0.005, NVE, rebuild every 10"),
     "lj_binary_16m": dict(kind="lj_multi", n=16_777_216, seed=3, rcut=2.5, skin=0.3, dt=0.002, min_steps=200,
+                          min_fp64_steps=20,
                           desc="LJ A:B 80:20 binary mixture, 16,777,216 atoms, rho 1.2, 64 voids of radius 8 sigma, "
                                "per-pair cutoff 2.5 sigma_ab, skin 0.3, 200 clipped minimiser steps (step 0.02, "
-                               "clip 100) then NVE dt 0.002, rebuild every 10"),
+                               "clip 100; the first 20 in FP64, the rest mixed) then NVE dt 0.002, rebuild every 10"),
 }
 
 
@@ -99,6 +100,12 @@ def parse():
                    help="untimed NVE steps from the lattice before the launch shape is tuned (lattice workloads)")
     p.add_argument("--ncell", type=int, default=0,
                    help="override the unit cells per edge (small profiling cases of the same workload)")
+    p.add_argument("--no-mixture", action="store_true",
+                   help="skip the 16.7 M-atom LJ mixture section of the default run")
+    p.add_argument("--no-drift", action="store_true",
+                   help="skip the 1,000-step mixed / 200-step FP64 NVE drift section")
+    p.add_argument("--no-oracle-check", action="store_true",
+                   help="skip the force error against the FP64 oracle at the benchmarked state")
     a = p.parse_args()
     if a.ncell:
         extra = {"n": 4 * a.ncell ** 3} if WORKLOADS[a.workload]["kind"] == "lj_multi" else {}
@@ -370,20 +377,173 @@ def bench_adjoint(stream, torch):
             "grad": dict(zip(setfl.PARAM_NAMES, g["grad"].tolist()))}
 
 
+
+
 # ---------------------------------------------------------------------------
-def main():
-    args = parse()
-    w = WORKLOADS[args.workload]
-    ws, rank, local = dist_setup(args)
-    if args.impl == "reference":
-        run_reference(args, w, ws, rank)
-        return
-    import torch
+KEYS9 = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az")
+
+
+def _etot(th):
+    """Total energy (kinetic + potential) of each thermo row."""
+    return th[:, 21:24].sum(1) + th[:, 24]
+
+
+def _drift(th, every, n):
+    """Energy drift per atom per 1,000 steps: end minus start, and the slope
+    of a least-squares line through the thermo rows (every `every` steps)."""
+    e = _etot(th)
+    t = np.arange(len(e)) * float(every)
+    slope = float(np.polyfit(t, e, 1)[0]) if len(e) > 2 else float("nan")
+    steps = t[-1] if len(t) > 1 else 1.0
+    return {"end_minus_start": float(e[-1] - e[0]) / n / steps * 1000.0, "fit": slope / n * 1000.0,
+            "steps": int(steps), "thermo_every": every}
+
+
+def _rel_rms(a, b):
+    return float(np.sqrt(((a - b) ** 2).sum() / max((b ** 2).sum(), 1e-300)))
+
+
+def oracle_force_check(ctx, s, w, sample):
+    """Relative RMS error of the GPU's mixed and FP64 forces against the FP64
+    oracle at the context's current state.  EAM: every atom (the density
+    pass needs all of them).  Pair potentials: the first `sample` atoms of
+    a seeded permutation (their lists built among all atoms)."""
+    O = _oracle()
+    d = ctx.download(("x", "y", "z"))
+    ctx.set_precision(True)
+    ctx.compute_forces(energy=False)
+    am = ctx.download(("ax", "ay", "az"))
+    ctx.set_precision(False)
+    ctx.compute_forces(energy=False)
+    a64 = ctx.download(("ax", "ay", "az"))
+    ctx.set_precision(True)
+    x, y, z = d["x"].copy(), d["y"].copy(), d["z"].copy()
+    O.wrap(x, y, z, s.lo, s.hi)
+    t0 = time.perf_counter()
+    if w["kind"] == "eam":
+        from exastamp_gb300 import setfl, systems as S
+        tab = O.EamOracleTables.from_setfl(setfl.tabulate(setfl.load_cu_params()), S.EV, S.EV, rcut=w["rcut"])
+        nl = O.build_neighbors(x, y, z, s.id, s.lo, s.hi, w["rcut"] + w["skin"])
+        fx, fy, fz, _, _, _, _ = O.eam_forces(x, y, z, s.type, nl, s.L, tab, w["rcut"], virial=False)
+        sel = np.arange(s.n)
+        F = np.stack([fx, fy, fz], 1) / s.masses[s.type][:, None]
+        how = "all %d atoms" % s.n
+    else:
+        from exastamp_gb300 import systems as S
+        perm = np.random.default_rng(7).permutation(s.n)
+        m = min(sample, s.n)
+        sel = perm[:m]
+        xp, yp, zp = x[perm], y[perm], z[perm]
+        ids, types = s.id[perm], np.ascontiguousarray(s.type[perm])
+        eps, sig, rc = S.kob_andersen_tables()
+        rcmax = float(rc.max())
+        nl = O.build_neighbors_first(xp, yp, zp, ids, s.lo, s.hi, rcmax + w["skin"], m)
+        fx, fy, fz, _, _ = O.lj_multi_force(xp, yp, zp, types, nl, s.L, eps, sig, rc, rcmax, virial=False)
+        F = np.stack([fx, fy, fz], 1) / s.masses[types[:m]][:, None]
+        how = "%d atoms of %d (seeded sample; their lists built among all atoms)" % (m, s.n)
+    t_orc = time.perf_counter() - t0
+    M = np.stack([am[k][sel] for k in ("ax", "ay", "az")], 1)
+    G = np.stack([a64[k][sel] for k in ("ax", "ay", "az")], 1)
+    return {"force_rel_rms_error_mixed_vs_oracle": _rel_rms(M, F),
+            "force_rel_rms_error_fp64_vs_oracle": _rel_rms(G, F),
+            "oracle_atoms": how, "oracle_seconds": t_orc, "oracle_threads": O.num_threads()}
+
+
+def nve_drift(ctx, s, w, R, mixed_steps, fp64_steps):
+    """From one saved state: mixed_steps NVE steps in mixed precision, then
+    fp64_steps from the same state through the plain-FP64 kernels (thermo
+    every 20 steps); drifts per atom per 1,000 steps in internal units and
+    in eV (EAM) or epsilon (LJ)."""
+    from exastamp_gb300 import systems as S
+    st = ctx.download(KEYS9)
+    unit = S.EV if w["kind"] == "eam" else 1.0
+    out = {"unit": "eV per atom per 1000 steps" if w["kind"] == "eam" else "epsilon per atom per 1000 steps"}
+    for name, mixed, nsteps in (("mixed", True, mixed_steps), ("fp64", False, fp64_steps)):
+        ctx.upload_state(*(st[k] for k in KEYS9))
+        ctx.set_precision(mixed)
+        t0 = time.perf_counter()
+        th = ctx.run_nve(nsteps, w["dt"], R, 20, use_graph=True)
+        ctx.synchronize()
+        dd = _drift(th, 20, s.n)
+        out[name] = {"steps": nsteps, "seconds": time.perf_counter() - t0,
+                     "drift_end_minus_start": dd["end_minus_start"] / unit, "drift_fit": dd["fit"] / unit}
+        if mixed and nsteps >= fp64_steps:
+            dd2 = _drift(th[: fp64_steps // 20 + 1], 20, s.n)
+            out["mixed_first_%d_steps" % fp64_steps] = {"drift_end_minus_start": dd2["end_minus_start"] / unit,
+                                                         "drift_fit": dd2["fit"] / unit}
+    ctx.upload_state(*(st[k] for k in KEYS9))
+    ctx.set_precision(True)
+    return out
+
+
+def e2e_section(ctx, s, w, R, steps, ws, torch, stream):
+    """The same step through the C ABI with the grid state in pinned host
+    arrays: gbmd_run_nve_host per step, copies inside the timed region."""
+    n = s.n
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pin = lambda: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()  # noqa: E731
+    host = {k: pin() for k in KEYS9}
+    d = ctx.download(KEYS9)
+    for k in host:
+        host[k][:] = d[k]
+    L = ctx._L
+    ptr = lambda k: host[k].ctypes.data  # noqa: E731
+    start = {k: host[k].copy() for k in KEYS9}
+    dt = w["dt"]
+    # untimed: the first host-step call allocates its position staging buffer
+    ctx._chk(L.gbmd_run_nve_host(ctx.h, 1, dt, R, *[ptr(k) for k in KEYS9]))
+
+    def loop(host_call):
+        """K steps from the same state, list freshly built: (CUDA-event ms,
+        wall ms, list builds)."""
+        for k in KEYS9:
+            host[k][:] = start[k]
+        ctx.upload_state(*(host[k] for k in KEYS9))
+        ctx.build_neighbors()
+        b0 = ctx.list_builds()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            if host_call:
+                ctx._chk(L.gbmd_run_nve_host(ctx.h, 1, dt, R, *[ptr(k) for k in KEYS9]))
+            else:
+                ctx._chk(L.gbmd_upload_state(ctx.h, *[ptr(k) for k in KEYS9]))
+                ctx._chk(L.gbmd_run_nve(ctx.h, 1, dt, R, 0, None, 0))
+                ctx._chk(L.gbmd_download(ctx.h, *[ptr(k) for k in KEYS9], None, None))
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        return ev0.elapsed_time(ev1), wall * 1e3, ctx.list_builds() - b0
+
+    sep_ms, sep_wall, _ = loop(False)   # the same step as three calls, for comparison
+    mse, wall_ms, builds = loop(True)
+    mse = dist_max(max(mse, wall_ms), ws)
+    sep_ms = max(sep_ms, sep_wall)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        ctx._chk(L.gbmd_upload_state(ctx.h, *[ptr(k) for k in KEYS9]))
+    up_ms = (time.perf_counter() - t0) * 1e3 / 3
+    t0 = time.perf_counter()
+    for _ in range(3):
+        ctx._chk(L.gbmd_download(ctx.h, *[ptr(k) for k in KEYS9], None, None))
+    down_ms = (time.perf_counter() - t0) * 1e3 / 3
+    return {"value": n * steps * ws / (mse * 1e-3), "unit": "atom-timesteps/s",
+            "upload_ms": up_ms, "download_ms": down_ms,
+            "h2d_bytes_per_step": 72 * n, "d2h_bytes_per_step": 72 * n, "steps": steps,
+            "ms_per_step": mse / steps, "ms_per_step_as_three_calls": sep_ms / steps,
+            "list_builds": builds,
+            "path": "gbmd_run_nve_host(1 step; pinned r,v,a uploaded, skin/2 displacement test, "
+                    "r copied back during the force pass, then v,a)"}
+
+
+def measure(args, w, ws, dev, stream, torch, *, steps, fp64_steps, e2e_steps, drift_steps, oracle_sample,
+            name):
+    """One workload on one GPU: the device-resident timed region (value), the
+    roofline of its final pair kernel, and the optional sections (FP64
+    comparison, oracle force check, NVE drift, e2e).  Returns the fields of
+    the JSON line."""
     from exastamp_gb300 import _capi
-    assert torch.cuda.is_available(), "bench.py needs a GPU (no CPU fallback)"
-    dev = local if ws > 1 else 0
-    torch.cuda.set_device(dev)
-    stream = torch.cuda.Stream(device=dev)
     s = make_system(w)
     ctx = _capi.Context(dev, stream.cuda_stream)
     ctx.upload_system(s)
@@ -391,10 +551,15 @@ def main():
     t_min = None
     tuned = None
     if w.get("min_steps"):
-        # random positions overlap: clipped minimiser first (FP64 forces)
-        ctx.set_precision(False)
+        # random positions overlap: the first steps of the clipped minimiser
+        # in FP64 (separations far below sigma), the rest in mixed precision
         t0 = time.perf_counter()
-        ctx.run_minimize(w["min_steps"], MIN_DT, tolF=MIN_TOLF, rebuild_every=args.rebuild_every)
+        ctx.set_precision(False)
+        ctx.run_minimize(w["min_fp64_steps"], MIN_DT, tolF=MIN_TOLF, rebuild_every=args.rebuild_every)
+        ctx.set_precision(True)
+        ctx.run_minimize(w["min_steps"] - w["min_fp64_steps"], MIN_DT, tolF=MIN_TOLF,
+                         rebuild_every=args.rebuild_every)
+        ctx.synchronize()
         t_min = time.perf_counter() - t0
     ctx.set_precision(args.precision == "mixed")
     t_therm = None
@@ -411,7 +576,7 @@ def main():
         ctx.set_newton3(args.newton3)
     else:
         from exastamp_gb300 import autotune
-        lanes, vec, block, tuned = autotune.tune(ctx, key="%s-%s" % (args.workload, args.precision))
+        lanes, vec, block, tuned = autotune.tune(ctx, key="%s-%s" % (name, args.precision))
     R, dt = args.rebuild_every, w["dt"]
     # fixed interval: thermo at the end of each 2R-step graph chunk; with the
     # displacement trigger (R = -1) every 20 steps
@@ -429,7 +594,7 @@ def main():
         torch.cuda.synchronize()
         builds0 = ctx.list_builds()
         ev0.record(stream)
-        th = ctx.run_nve(args.steps, dt, R, thermo_every, use_graph=True)
+        th = ctx.run_nve(steps, dt, R, thermo_every, use_graph=True)
         ev1.record(stream)
         torch.cuda.synchronize()
         barrier(ws)
@@ -437,9 +602,7 @@ def main():
     ms = ev0.elapsed_time(ev1)
     ms = dist_max(ms, ws)
     clocks = clk.summary()
-    value = s.n * args.steps * ws / (ms * 1e-3)
-    etot = th[:, 21:24].sum(1) + th[:, 24]
-    drift = (etot[-1] - etot[0]) / s.n / max(args.steps, 1) * 1000.0
+    value = s.n * steps * ws / (ms * 1e-3)
     # EAM: density + force; Newton-3 LJ: half-list pair pass + epilogue
     kernels_per_step = 2 if w["kind"] == "eam" or args.newton3 else 1
     # Launches of the timed gbmd_run_nve call: the pair kernel(s) once per
@@ -452,24 +615,24 @@ def main():
     # rebuild body (2 fills, the chain, copy-back, reference positions) when
     # the gate opens; the steps after the last whole graph chunk run the 13
     # gated launches every step.
-    n_thermo = args.steps // thermo_every if thermo_every else 0
-    last_is_thermo = bool(thermo_every) and args.steps % thermo_every == 0
-    gpu_launches = kernels_per_step * (args.steps + (1 if thermo_every else 0))
+    n_thermo = steps // thermo_every if thermo_every else 0
+    last_is_thermo = bool(thermo_every) and steps % thermo_every == 0
+    gpu_launches = kernels_per_step * (steps + (1 if thermo_every else 0))
     gpu_launches += 2 * (n_thermo + (1 if thermo_every else 0))
     gpu_launches += 1 + n_thermo - (1 if last_is_thermo else 0)
     if R < 0:
-        n_graph = ((args.steps - 1) // thermo_every) * thermo_every
-        gpu_launches += n_graph + 13 * rebuilds + 13 * (args.steps - n_graph)
+        n_graph = ((steps - 1) // thermo_every) * thermo_every
+        gpu_launches += n_graph + 13 * rebuilds + 13 * (steps - n_graph)
     else:
         gpu_launches += 9 * rebuilds
 
     out = {"metric": "atom-timesteps/s", "value": value, "unit": "atom-timesteps/s", "n_gpus": ws,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+           "steps": steps, "warmup": args.warmup, "ms_per_step": ms / steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32-pair/f64-state" if args.precision == "mixed" else "f64",
            "data": "synthetic (seeded random positions with voids, Maxwell-Boltzmann velocities)"
            if w["kind"] == "lj_multi" else "synthetic (seeded FCC lattice, Maxwell-Boltzmann velocities)",
-           "config": {"workload": args.workload, "description": w["desc"], "atoms": s.n,
+           "config": {"workload": name, "description": w["desc"], "atoms": s.n,
                       "precision": args.precision, "thermo_every": thermo_every,
                       "rebuild_every": R if R >= 0 else "on displacement > skin/2",
                       "list_builds_in_timed_region": rebuilds,
@@ -484,14 +647,16 @@ def main():
                       if npairs * 4 > 129e6 else "inputs resident in L2 (not flushed)",
                       "cuda_graph": True},
            "gpu_launches": gpu_launches, "clocks": clocks,
-           "nve_energy_drift_per_1000_steps_per_atom": drift}
+           "nve_energy_drift_per_1000_steps_per_atom_timed_region": _drift(th, thermo_every, s.n)["end_minus_start"]
+           if thermo_every else None}
     if tuned:
         out["autotune_density_plus_pair_ms"] = tuned
     if t_therm is not None:
         out["thermalisation"] = {"steps": args.thermalise, "seconds": t_therm,
                                  "note": "untimed NVE steps from the lattice before tuning and warm-up"}
     if t_min is not None:
-        out["minimiser"] = {"steps": w["min_steps"], "step": MIN_DT, "clip": MIN_TOLF, "precision": "fp64",
+        out["minimiser"] = {"steps": w["min_steps"], "step": MIN_DT, "clip": MIN_TOLF,
+                            "precision": "fp64 for the first %d steps, then mixed" % w["min_fp64_steps"],
                             "seconds": t_min}
 
     # ---- per-kernel timing for the roofline -------------------------------
@@ -523,86 +688,61 @@ def main():
                        "algorithmic_bytes_per_launch": alg_bytes, "bytes_per_atom": per_atom,
                        "traffic": traffic, "traffic_source": traffic_src, "kernel_ms": prof}
 
+    single = ws == 1
+    # ---- accuracy against the FP64 oracle at the benchmarked state ----------
+    if single and not args.no_oracle_check and args.precision == "mixed":
+        out["accuracy"] = oracle_force_check(ctx, s, w, oracle_sample)
+
     # ---- FP64 comparison ----------------------------------------------------
-    if not args.no_fp64 and ws == 1:
+    if single and not args.no_fp64:
+        st = ctx.download(KEYS9)
         d_mixed = ctx.download(("ax", "ay", "az"))
         ctx.set_precision(False)
         ctx.compute_forces(energy=False)
         d64 = ctx.download(("ax", "ay", "az"))
         A = np.stack([d_mixed[k] for k in ("ax", "ay", "az")], 1)
         B = np.stack([d64[k] for k in ("ax", "ay", "az")], 1)
-        ferr = float(np.sqrt(((A - B) ** 2).sum() / (B ** 2).sum()))
+        ferr = _rel_rms(A, B)
         ctx.run_nve(3, dt, R, 0, use_graph=False)
         torch.cuda.synchronize()
         ev0.record(stream)
-        ctx.run_nve(args.fp64_steps, dt, R, 0, use_graph=True)
+        ctx.run_nve(fp64_steps, dt, R, 0, use_graph=True)
         ev1.record(stream)
         torch.cuda.synchronize()
         ms64 = ev0.elapsed_time(ev1)
-        v64 = s.n * args.fp64_steps / (ms64 * 1e-3)
-        out["fp64"] = {"value": v64, "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps,
+        v64 = s.n * fp64_steps / (ms64 * 1e-3)
+        out["fp64"] = {"value": v64, "ms_per_step": ms64 / fp64_steps, "steps": fp64_steps,
                        "mixed_over_fp64": value / v64, "force_rel_rms_error_mixed_vs_fp64": ferr}
+        ctx.upload_state(*(st[k] for k in KEYS9))
         ctx.set_precision(args.precision == "mixed")
+
+    # ---- NVE energy drift, mixed vs FP64 from one state -----------------------
+    if single and not args.no_drift and drift_steps:
+        out["nve_drift"] = nve_drift(ctx, s, w, R, *drift_steps)
 
     # ---- end-to-end through the C ABI with host buffers -----------------------
     if not args.no_e2e:
-        n = s.n
-        pin = lambda: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()  # noqa: E731
-        host = {k: pin() for k in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az")}
-        d = ctx.download(tuple(host))
-        for k in host:
-            host[k][:] = d[k]
-        L = ctx._L
-        ptr = lambda k: host[k].ctypes.data  # noqa: E731
-        keys9 = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az")
-        start = {k: host[k].copy() for k in keys9}
-        # untimed: the first host-step call allocates its position staging buffer
-        ctx._chk(L.gbmd_run_nve_host(ctx.h, 1, dt, R, *[ptr(k) for k in keys9]))
+        out["e2e"] = e2e_section(ctx, s, w, R, e2e_steps, ws, torch, stream)
+    ctx.close()
+    return out
 
-        def e2e_loop(host_call):
-            """K steps from the same state, list freshly built: (CUDA-event ms,
-            wall ms, list builds)."""
-            for k in keys9:
-                host[k][:] = start[k]
-            ctx.upload_state(*(host[k] for k in keys9))
-            ctx.build_neighbors()
-            b0 = ctx.list_builds()
-            torch.cuda.synchronize()
-            ev0.record(stream)
-            t0 = time.perf_counter()
-            for _ in range(args.e2e_steps):
-                if host_call:
-                    ctx._chk(L.gbmd_run_nve_host(ctx.h, 1, dt, R, *[ptr(k) for k in keys9]))
-                else:
-                    ctx._chk(L.gbmd_upload_state(ctx.h, *[ptr(k) for k in keys9]))
-                    ctx._chk(L.gbmd_run_nve(ctx.h, 1, dt, R, 0, None, 0))
-                    ctx._chk(L.gbmd_download(ctx.h, *[ptr(k) for k in keys9], None, None))
-            ev1.record(stream)
-            torch.cuda.synchronize()
-            wall = time.perf_counter() - t0
-            return ev0.elapsed_time(ev1), wall * 1e3, ctx.list_builds() - b0
 
-        sep_ms, sep_wall, _ = e2e_loop(False)   # the same step as three calls, for comparison
-        mse, wall_ms, e2e_builds = e2e_loop(True)
-        mse = dist_max(max(mse, wall_ms), ws)
-        sep_ms = max(sep_ms, sep_wall)
-        # split of one step: upload alone, download alone (host wall clock)
-        t0 = time.perf_counter()
-        for _ in range(3):
-            ctx._chk(L.gbmd_upload_state(ctx.h, *[ptr(k) for k in keys9]))
-        up_ms = (time.perf_counter() - t0) * 1e3 / 3
-        t0 = time.perf_counter()
-        for _ in range(3):
-            ctx._chk(L.gbmd_download(ctx.h, *[ptr(k) for k in keys9], None, None))
-        down_ms = (time.perf_counter() - t0) * 1e3 / 3
-        out["e2e"] = {"value": n * args.e2e_steps * ws / (mse * 1e-3), "unit": "atom-timesteps/s",
-                      "upload_ms": up_ms, "download_ms": down_ms,
-                      "h2d_bytes_per_step": 72 * n, "d2h_bytes_per_step": 72 * n, "steps": args.e2e_steps,
-                      "ms_per_step": mse / args.e2e_steps,
-                      "ms_per_step_as_three_calls": sep_ms / args.e2e_steps,
-                      "list_builds": e2e_builds,
-                      "path": "gbmd_run_nve_host(1 step; pinned r,v,a uploaded, skin/2 displacement test, "
-                              "r copied back during the force pass, then v,a)"}
+def main():
+    args = parse()
+    w = WORKLOADS[args.workload]
+    ws, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, w, ws, rank)
+        return
+    import torch
+    assert torch.cuda.is_available(), "bench.py needs a GPU (no CPU fallback)"
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    eam = w["kind"] == "eam"
+    out = measure(args, w, ws, dev, stream, torch, steps=args.steps, fp64_steps=args.fp64_steps,
+                  e2e_steps=args.e2e_steps, drift_steps=(1000, 200) if eam else (500, 50),
+                  oracle_sample=65536, name=args.workload)
 
     # ---- batched replicas (4,096 EAM systems) and the parameter adjoint --------
     if not args.no_batch and ws == 1:
@@ -616,7 +756,22 @@ def main():
                                "kind": "port",
                                "sample": "%d-atom sample of the workload, %d FP64 NVE steps on the OpenMP "
                                          "oracle (%.1f s)" % (info["atoms"], info["steps"], info["seconds"])}
-    ctx.close()
+
+    # ---- the 16.7 M-atom LJ binary mixture, in the same line -------------------
+    if eam and not args.no_mixture and not args.ncell and ws == 1:
+        wm = WORKLOADS["lj_binary_16m"]
+        mix = measure(args, wm, ws, dev, stream, torch, steps=args.steps, fp64_steps=10, e2e_steps=10,
+                      drift_steps=(500, 50), oracle_sample=65536, name="lj_binary_16m")
+        if not args.no_cpu and rank == 0:
+            rate, info = cpu_oracle_rate(wm, target_s=8.0)
+            mix["cpu_baseline"] = {"value": rate, "unit": "atom-timesteps/s", "cores": info["threads"],
+                                   "kind": "port",
+                                   "sample": "%d-atom sample of the workload (minimised first), %d FP64 NVE "
+                                             "steps on the OpenMP oracle (%.1f s)"
+                                             % (info["atoms"], info["steps"], info["seconds"])}
+        for k in ("metric", "unit", "n_gpus", "steps", "warmup", "higher_is_better", "scaling", "vs_baseline"):
+            mix.pop(k, None)
+        out["lj_mixture"] = mix
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:

@@ -284,6 +284,19 @@ class Context:
         self._chk(self._L.gbmd_export_pairs(self.h, n, _p(a), _p(b), _p(img), C.byref(cnt)))
         return np.column_stack([a[:n].astype(np.int64), b[:n].astype(np.int64), img[:n].astype(np.int64)])
 
+    def export_pairs_raw(self):
+        """The exported pair set as three arrays (id_i, id_j: uint64; image:
+        n x 3 int8), without the int64 stacking of export_pairs (for lists of
+        hundreds of millions of pairs)."""
+        cnt = C.c_int64()
+        self._chk(self._L.gbmd_export_pairs(self.h, 0, None, None, None, C.byref(cnt)))
+        n = cnt.value
+        a = np.empty(max(n, 1), np.uint64)
+        b = np.empty(max(n, 1), np.uint64)
+        img = np.empty((max(n, 1), 3), np.int8)
+        self._chk(self._L.gbmd_export_pairs(self.h, n, _p(a), _p(b), _p(img), C.byref(cnt)))
+        return a[:n], b[:n], img[:n]
+
     def neighbor_stats(self):
         npairs, maxnb = C.c_int64(), C.c_int()
         nc = np.zeros(3, np.int32)

@@ -197,18 +197,27 @@ static int64_t visit_atom(const orc_grid* g, int64_t i, const double* x, const d
 int64_t orc_build_neighbors(int64_t n, const double* x, const double* y, const double* z,
                             const uint64_t* id, const double lo[3], const double hi[3], double R,
                             int64_t* offsets, int64_t cap, int32_t* nbr, int8_t* img) {
+  return orc_build_neighbors_first(n, n, x, y, z, id, lo, hi, R, offsets, cap, nbr, img);
+}
+
+/* The same list for the first nlist atoms only (their neighbours taken among
+ * all n): a bounded sample of a large system's pair set. */
+int64_t orc_build_neighbors_first(int64_t n, int64_t nlist, const double* x, const double* y, const double* z,
+                                  const uint64_t* id, const double lo[3], const double hi[3], double R,
+                                  int64_t* offsets, int64_t cap, int32_t* nbr, int8_t* img) {
+  if (nlist < 0 || nlist > n) return -1;
   orc_grid g;
   if (grid_build(&g, n, x, y, z, id, lo, hi, R) != 0) return -1;
   const double L[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
   const double R2 = R * R;
 #pragma omp parallel for schedule(dynamic, 64)
-  for (int64_t i = 0; i < n; ++i) offsets[i + 1] = visit_atom(&g, i, x, y, z, L, R2, NULL, NULL);
+  for (int64_t i = 0; i < nlist; ++i) offsets[i + 1] = visit_atom(&g, i, x, y, z, L, R2, NULL, NULL);
   offsets[0] = 0;
-  for (int64_t i = 0; i < n; ++i) offsets[i + 1] += offsets[i];
-  const int64_t total = offsets[n];
+  for (int64_t i = 0; i < nlist; ++i) offsets[i + 1] += offsets[i];
+  const int64_t total = offsets[nlist];
   if (nbr && total <= cap) {
 #pragma omp parallel for schedule(dynamic, 64)
-    for (int64_t i = 0; i < n; ++i) visit_atom(&g, i, x, y, z, L, R2, nbr + offsets[i], img + 3 * offsets[i]);
+    for (int64_t i = 0; i < nlist; ++i) visit_atom(&g, i, x, y, z, L, R2, nbr + offsets[i], img + 3 * offsets[i]);
   }
   grid_free(&g);
   return total;

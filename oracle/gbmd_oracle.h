@@ -77,6 +77,9 @@ int64_t orc_wrap(int64_t n, double* x, double* y, double* z, const double lo[3],
 int64_t orc_build_neighbors(int64_t n, const double* x, const double* y, const double* z,
                             const uint64_t* id, const double lo[3], const double hi[3], double R,
                             int64_t* offsets, int64_t cap, int32_t* nbr, int8_t* img);
+int64_t orc_build_neighbors_first(int64_t n, int64_t nlist, const double* x, const double* y, const double* z,
+                                  const uint64_t* id, const double lo[3], const double hi[3], double R,
+                                  int64_t* offsets, int64_t cap, int32_t* nbr, int8_t* img);
 int64_t orc_brute_pairs(int64_t n, const double* x, const double* y, const double* z,
                         const double lo[3], const double hi[3], double R, int64_t cap,
                         int32_t* pi, int32_t* pj, int8_t* img);

@@ -90,6 +90,8 @@ def lib():
         L.orc_wrap.argtypes = [i64, vp, vp, vp, vp, vp]
         L.orc_build_neighbors.restype = i64
         L.orc_build_neighbors.argtypes = [i64, vp, vp, vp, vp, vp, vp, dbl, vp, i64, vp, vp]
+        L.orc_build_neighbors_first.restype = i64
+        L.orc_build_neighbors_first.argtypes = [i64, i64, vp, vp, vp, vp, vp, vp, dbl, vp, i64, vp, vp]
         L.orc_brute_pairs.restype = i64
         L.orc_brute_pairs.argtypes = [i64, vp, vp, vp, vp, vp, dbl, i64, vp, vp, vp]
         L.orc_lj_energy_cut.restype = dbl
@@ -195,6 +197,25 @@ def build_neighbors(x, y, z, ids, lo, hi, R) -> NeighborList:
     return NeighborList(off, nbr[:tot], img[:tot])
 
 
+def build_neighbors_first(x, y, z, ids, lo, hi, R, nlist) -> NeighborList:
+    """The lists of the first nlist atoms only (neighbours among all atoms):
+    a bounded sample of a large system's pair set."""
+    n = len(x)
+    lo, hi = _f64(lo), _f64(hi)
+    ids = np.ascontiguousarray(ids, dtype=np.uint64)
+    off = np.zeros(nlist + 1, dtype=np.int64)
+    tot = lib().orc_build_neighbors_first(n, nlist, _p(x), _p(y), _p(z), _p(ids), _p(lo), _p(hi), float(R),
+                                          _p(off), 0, None, None)
+    if tot < 0:
+        raise ValueError("neighbour build failed (box thinner than radius?)")
+    nbr = np.zeros(max(tot, 1), dtype=np.int32)
+    img = np.zeros((max(tot, 1), 3), dtype=np.int8)
+    tot2 = lib().orc_build_neighbors_first(n, nlist, _p(x), _p(y), _p(z), _p(ids), _p(lo), _p(hi), float(R),
+                                           _p(off), tot, _p(nbr), _p(img))
+    assert tot2 == tot
+    return NeighborList(off, nbr[:tot], img[:tot])
+
+
 def brute_pairs(x, y, z, lo, hi, R):
     n = len(x)
     lo, hi = _f64(lo), _f64(hi)
@@ -223,7 +244,7 @@ def _outs(n, vir):
 
 
 def lj_force(x, y, z, nl, L, eps, sigma, rcut, virial=True):
-    n = len(x)
+    n = len(nl.off) - 1
     fx, fy, fz, ep, v = _outs(n, virial)
     prm = LJParams(eps, sigma, rcut)
     lib().orc_lj_force(n, _p(x), _p(y), _p(z), _p(nl.off), _p(nl.nbr), _p(nl.img), _p(_f64(L)),
@@ -270,7 +291,9 @@ def ej_forces(x, y, z, nl, L, pot, virial=True):
 
 
 def lj_multi_force(x, y, z, types, nl, L, eps, sig, rc, rcut_max, virial=True):
-    n = len(x)
+    """Forces of the atoms the list covers: all of them, or the first
+    len(nl.off) - 1 for a build_neighbors_first list."""
+    n = len(nl.off) - 1
     m = _Multi(eps, sig, rc, rcut_max)
     fx, fy, fz, ep, v = _outs(n, virial)
     types = np.ascontiguousarray(types, dtype=np.uint8)

@@ -1,0 +1,115 @@
+"""Parity at the benchmarked sizes: the sm_103a path, through the C ABI,
+against the FP64 oracle on the headline systems themselves.
+
+* eam_alloy copper-like FCC 100^3 cells, 4,000,000 atoms (the benchmark
+  workload: 5,000-point splines, rcut 5.0 A, skin 0.3 A, 300 K), after 100
+  mixed-precision NVE steps of 1 fs from the lattice.  The 68^3-cell grid
+  puts the 26-bit atom index and the 10-bit cell packing near their limits.
+* Lennard-Jones A:B 80:20 mixture at rho 1.2 with voids of radius 8 sigma,
+  2,097,152 atoms (the 16.7 M-atom workload at 1/8 of the volume, same
+  density and void fraction), after the 200-step clipped minimiser.
+
+Bars, as in the small-box parity tests:
+  * neighbour pair set inside rcut + skin: bit-exact, in the same per-atom order
+    (the oracle is eam_force_op_multimat.h / atom_neighbors_stats.cpp's pair
+    decode, restated in oracle/gbmd_oracle.c);
+  * FP64 path: forces, per-atom energies and virials within 1e-12 relative;
+  * mixed path: relative RMS force error <= 1e-5 against the oracle (not
+    against the GPU's own FP64 path), total energy within 1e-6.
+"""
+import numpy as np
+import pytest
+
+from exastamp_gb300 import setfl as SF
+from exastamp_gb300 import systems as S
+
+from pairset_compare import assert_same_pair_sets
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+MIXED_FORCE_TOL = 1e-5
+
+
+def rel_rms(a, b):
+    return float(np.sqrt(((a - b) ** 2).sum() / max((b ** 2).sum(), 1e-300)))
+
+
+def _state_arrays(d):
+    return d["x"].copy(), d["y"].copy(), d["z"].copy()
+
+
+def test_eam_cu_4m_atoms_after_100_steps(gpu, oracle):
+    sf = SF.tabulate(SF.load_cu_params())
+    tab = oracle.EamOracleTables.from_setfl(sf, S.EV, S.EV, rcut=5.0)
+    s = S.eam_cu_fcc(ncell=100, a=3.615, T=300.0, seed=2)
+    assert s.n == 4_000_000
+    with gpu.Context(0) as ctx:
+        ctx.upload_system(s)
+        ctx.set_eam_alloy(sf, 5.0, S.EV, S.EV)
+        ctx.set_skin(0.3)
+        ctx.set_precision(True)
+        ctx.run_nve(100, 1e-3, 10, 0, use_graph=True)
+        d = ctx.download(("x", "y", "z"))
+        ctx.build_neighbors()
+        rows = ctx.export_pairs_raw()
+        ctx.compute_forces(energy=True, virial=True)
+        dm = ctx.download(("ax", "ay", "az", "ep"), virial=True)
+        ctx.set_precision(False)
+        ctx.compute_forces(energy=True, virial=True)
+        d64 = ctx.download(("ax", "ay", "az", "ep"), virial=True)
+    x, y, z = _state_arrays(d)
+    oracle.wrap(x, y, z, s.lo, s.hi)
+    nl = oracle.build_neighbors(x, y, z, s.id, s.lo, s.hi, 5.3)
+    assert_same_pair_sets(rows, nl, s.id)
+    del rows
+    fx, fy, fz, ep, vir, _, _ = oracle.eam_forces(x, y, z, s.type, nl, s.L, tab, 5.0)
+    F = np.stack([fx, fy, fz], 1) / s.masses[0]
+    del nl
+    G = np.stack([d64["ax"], d64["ay"], d64["az"]], 1)
+    assert rel_rms(G, F) < FP64_TOL
+    assert np.abs(G - F).max() < 1e-11 * np.abs(F).max()
+    assert np.abs(d64["ep"] - ep).max() < FP64_TOL * np.abs(ep).max()
+    assert np.abs(d64["vir"] - vir).max() < FP64_TOL * np.abs(vir).max()
+    M = np.stack([dm["ax"], dm["ay"], dm["az"]], 1)
+    err = rel_rms(M, F)
+    assert err < MIXED_FORCE_TOL, err
+    assert abs(dm["ep"].sum() - ep.sum()) < 1e-6 * abs(ep.sum())
+    assert rel_rms(dm["vir"], vir) < 1e-5
+
+
+def test_lj_mixture_2m_atoms_after_minimiser(gpu, oracle):
+    n = 2_097_152
+    s = S.lj_binary_voids(n=n, seed=3, nvoids=8)
+    eps, sig, rc = S.kob_andersen_tables()
+    rcmax = float(rc.max())
+    with gpu.Context(0) as ctx:
+        ctx.upload_system(s)
+        ctx.set_lj_multi(eps, sig, rc, 0.0)
+        ctx.set_skin(0.3)
+        ctx.set_precision(False)
+        ctx.run_minimize(200, 0.02, tolF=100.0, rebuild_every=10)
+        d = ctx.download(("x", "y", "z"))
+        ctx.build_neighbors()
+        rows = ctx.export_pairs_raw()
+        ctx.compute_forces(energy=True, virial=True)
+        d64 = ctx.download(("ax", "ay", "az", "ep"), virial=True)
+        ctx.set_precision(True)
+        ctx.compute_forces(energy=True, virial=True)
+        dm = ctx.download(("ax", "ay", "az", "ep"), virial=True)
+    x, y, z = _state_arrays(d)
+    oracle.wrap(x, y, z, s.lo, s.hi)
+    nl = oracle.build_neighbors(x, y, z, s.id, s.lo, s.hi, rcmax + 0.3)
+    assert_same_pair_sets(rows, nl, s.id)
+    del rows
+    fx, fy, fz, ep, vir = oracle.lj_multi_force(x, y, z, s.type, nl, s.L, eps, sig, rc, rcmax)
+    F = np.stack([fx, fy, fz], 1) / s.masses[s.type][:, None]
+    del nl
+    G = np.stack([d64["ax"], d64["ay"], d64["az"]], 1)
+    assert rel_rms(G, F) < FP64_TOL
+    assert np.abs(d64["ep"] - ep).max() < FP64_TOL * np.abs(ep).max()
+    assert np.abs(d64["vir"] - vir).max() < FP64_TOL * np.abs(vir).max()
+    M = np.stack([dm["ax"], dm["ay"], dm["az"]], 1)
+    err = rel_rms(M, F)
+    assert err < MIXED_FORCE_TOL, err
+    assert abs(dm["ep"].sum() - ep.sum()) < 1e-6 * abs(ep.sum())

@@ -345,3 +345,25 @@ def test_lj_loss_gradient_matches_finite_differences(oracle):
         fd = (oracle.lj_loss_grad(x, y, z, nl, s.L, p[0], p[1], 2.5, ft, et, wF, wE)[0]
               - oracle.lj_loss_grad(x, y, z, nl, s.L, m[0], m[1], 2.5, ft, et, wF, wE)[0]) / (2 * h)
         assert abs(fd - g[k]) < 1e-6 * max(abs(fd), 1e-12), (k, fd, g[k])
+
+
+def test_build_neighbors_first_matches_full_list(oracle):
+    """The lists of the first m atoms (neighbours among all) are the full
+    build's lists of those atoms, and the LJ-mixture forces of those atoms
+    from them are the full evaluation's."""
+    from exastamp_gb300 import systems as S
+    s = S.lj_binary_voids(n=4000, seed=9, nvoids=1, void_r=2.0)
+    eps, sig, rc = S.kob_andersen_tables()
+    rcmax = float(rc.max())
+    x, y, z = s.x.copy(), s.y.copy(), s.z.copy()
+    oracle.wrap(x, y, z, s.lo, s.hi)
+    full = oracle.build_neighbors(x, y, z, s.id, s.lo, s.hi, rcmax + 0.3)
+    m = 700
+    part = oracle.build_neighbors_first(x, y, z, s.id, s.lo, s.hi, rcmax + 0.3, m)
+    assert np.array_equal(part.off, full.off[: m + 1])
+    assert np.array_equal(part.nbr, full.nbr[: full.off[m]])
+    assert np.array_equal(part.img, full.img[: full.off[m]])
+    ff = oracle.lj_multi_force(x, y, z, s.type, full, s.L, eps, sig, rc, rcmax)
+    fp = oracle.lj_multi_force(x, y, z, s.type, part, s.L, eps, sig, rc, rcmax)
+    for a, b in zip(ff[:4], fp[:4]):
+        assert np.array_equal(a[:m], b)
