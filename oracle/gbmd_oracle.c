@@ -278,6 +278,34 @@ static inline void add_vir(double* v, double fx, double fy, double fz, double dx
   v[6] += fz * dx * -0.5; v[7] += fz * dy * -0.5; v[8] += fz * dz * -0.5;
 }
 
+/* One in-cutoff pair of lj_compute_force's per-atom loop
+ * (force_op_impl2.hxx L33-68): e -= ecut, de /= r, fe = de * dr, f += fe,
+ * ep += e / 2, virial += (fe x dr) * -1/2.  acc = {fx, fy, fz, ep, vir[9]}. */
+static inline void lj_accumulate(double epsilon, double sigma, double ecut, double dx, double dy, double dz,
+                                 double d2, double* acc) {
+  const double r = sqrt(d2);
+  double e, de;
+  orc_lj_pair(epsilon, sigma, r, &e, &de);
+  e -= ecut;
+  de /= r;
+  const double fex = de * dx, fey = de * dy, fez = de * dz;
+  acc[0] += fex; acc[1] += fey; acc[2] += fez;
+  acc[3] += .5 * e;
+  add_vir(acc + 4, fex, fey, fez, dx, dy, dz);
+}
+
+/* force_op_impl2.hxx L22-78 on one atom's pair buffer (drx, dry, drz, d2 of
+ * its n in-cutoff neighbours, as the reference's ComputePairBuffer2 holds
+ * them): out = {ep, fx, fy, fz, vir[9]}, each summed in buffer order. */
+void orc_lj_atom_buffer(double epsilon, double sigma, double ecut, int n, const double* drx, const double* dry,
+                        const double* drz, const double* d2, double* out) {
+  double acc[13] = {0};
+  for (int k = 0; k < n; ++k) lj_accumulate(epsilon, sigma, ecut, drx[k], dry[k], drz[k], d2[k], acc);
+  out[0] = acc[3];
+  out[1] = acc[0]; out[2] = acc[1]; out[3] = acc[2];
+  for (int q = 0; q < 9; ++q) out[4 + q] = acc[4 + q];
+}
+
 /* lj_compute_force per atom (force_op_impl2.hxx L22-78) over the list pairs
  * with d2 <= rcut^2 (the traversal's rcut_max filter).  Zeroes first
  * (zero_force_energy), so outputs are the force on each atom, its half-pair
@@ -289,25 +317,17 @@ void orc_lj_force(int64_t n, const double* x, const double* y, const double* z,
   const double rc2 = p->rcut * p->rcut;
 #pragma omp parallel for schedule(dynamic, 256)
   for (int64_t i = 0; i < n; ++i) {
-    double _fx = 0., _fy = 0., _fz = 0., _ep = 0., _v[9] = {0};
+    double acc[13] = {0};
     for (int64_t k = off[i]; k < off[i + 1]; ++k) {
       const int nn[3] = {img[3 * k], img[3 * k + 1], img[3 * k + 2]};
       double dx, dy, dz;
       const double d2 = pair_d2(x, y, z, i, nbr[k], nn, L, &dx, &dy, &dz);
       if (!(d2 <= rc2)) continue;
-      const double r = sqrt(d2);
-      double e, de;
-      orc_lj_pair(p->epsilon, p->sigma, r, &e, &de);
-      e -= ecut;
-      de /= r;
-      const double fex = de * dx, fey = de * dy, fez = de * dz;
-      _fx += fex; _fy += fey; _fz += fez;
-      _ep += .5 * e;
-      add_vir(_v, fex, fey, fez, dx, dy, dz);
+      lj_accumulate(p->epsilon, p->sigma, ecut, dx, dy, dz, d2, acc);
     }
-    fx[i] = _fx; fy[i] = _fy; fz[i] = _fz;
-    if (ep) ep[i] = _ep;
-    if (vir) for (int q = 0; q < 9; ++q) vir[9 * i + q] = _v[q];
+    fx[i] = acc[0]; fy[i] = acc[1]; fz[i] = acc[2];
+    if (ep) ep[i] = acc[3];
+    if (vir) for (int q = 0; q < 9; ++q) vir[9 * i + q] = acc[4 + q];
   }
 }
 
@@ -324,7 +344,7 @@ void orc_lj_multi_force(int64_t n, const double* x, const double* y, const doubl
   const double rc2 = p->rcut_max * p->rcut_max;
 #pragma omp parallel for schedule(dynamic, 256)
   for (int64_t i = 0; i < n; ++i) {
-    double _fx = 0., _fy = 0., _fz = 0., _ep = 0., _v[9] = {0};
+    double acc[13] = {0};
     const int ta = type[i];
     for (int64_t k = off[i]; k < off[i + 1]; ++k) {
       const int nn[3] = {img[3 * k], img[3 * k + 1], img[3 * k + 2]};
@@ -332,22 +352,12 @@ void orc_lj_multi_force(int64_t n, const double* x, const double* y, const doubl
       const int64_t j = nbr[k];
       const double d2 = pair_d2(x, y, z, i, j, nn, L, &dx, &dy, &dz);
       if (!(d2 <= rc2)) continue;
-      const double r = sqrt(d2);
       const int pid = ta * nt + type[j];
-      if (r <= p->rcut[pid]) {
-        double e, de;
-        orc_lj_pair(p->epsilon[pid], p->sigma[pid], r, &e, &de);
-        e -= ecut[pid];
-        de /= r;
-        const double fex = de * dx, fey = de * dy, fez = de * dz;
-        _fx += fex; _fy += fey; _fz += fez;
-        _ep += .5 * e;
-        add_vir(_v, fex, fey, fez, dx, dy, dz);
-      }
+      if (sqrt(d2) <= p->rcut[pid]) lj_accumulate(p->epsilon[pid], p->sigma[pid], ecut[pid], dx, dy, dz, d2, acc);
     }
-    fx[i] = _fx; fy[i] = _fy; fz[i] = _fz;
-    if (ep) ep[i] = _ep;
-    if (vir) for (int q = 0; q < 9; ++q) vir[9 * i + q] = _v[q];
+    fx[i] = acc[0]; fy[i] = acc[1]; fz[i] = acc[2];
+    if (ep) ep[i] = acc[3];
+    if (vir) for (int q = 0; q < 9; ++q) vir[9 * i + q] = acc[4 + q];
   }
   free(ecut);
 }

@@ -86,6 +86,8 @@ int64_t orc_brute_pairs(int64_t n, const double* x, const double* y, const doubl
 
 double orc_lj_energy_cut(double epsilon, double sigma, double rcut);
 void orc_lj_pair(double epsilon, double sigma, double r, double* e, double* de);
+void orc_lj_atom_buffer(double epsilon, double sigma, double ecut, int n, const double* drx, const double* dry,
+                        const double* drz, const double* d2, double* out);
 void orc_lj_force(int64_t n, const double* x, const double* y, const double* z,
                   const int64_t* off, const int32_t* nbr, const int8_t* img, const double L[3],
                   const orc_lj_params* p, double* fx, double* fy, double* fz, double* ep, double* vir);

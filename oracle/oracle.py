@@ -97,6 +97,7 @@ def lib():
         L.orc_lj_energy_cut.restype = dbl
         L.orc_lj_energy_cut.argtypes = [dbl, dbl, dbl]
         L.orc_lj_pair.argtypes = [dbl, dbl, dbl, vp, vp]
+        L.orc_lj_atom_buffer.argtypes = [dbl, dbl, dbl, i32, vp, vp, vp, vp, vp]
         L.orc_lj_force.argtypes = [i64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.orc_lj_multi_force.argtypes = [i64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.orc_lj_direct.restype = dbl
@@ -235,6 +236,15 @@ def lj_pair(eps, sigma, r):
 
 def lj_energy_cut(eps, sigma, rcut):
     return float(lib().orc_lj_energy_cut(float(eps), float(sigma), float(rcut)))
+
+
+def lj_atom_buffer(eps, sigma, ecut, drx, dry, drz, d2):
+    """One atom of lj_compute_force over its pair buffer (in-cutoff pairs):
+    {ep, fx, fy, fz, vir[9]} (force_op_impl2.hxx L22-78)."""
+    arrs = [_f64(a) for a in (drx, dry, drz, d2)]
+    out = np.zeros(13)
+    lib().orc_lj_atom_buffer(float(eps), float(sigma), float(ecut), len(arrs[0]), *[_p(a) for a in arrs], _p(out))
+    return out
 
 
 def _outs(n, vir):
