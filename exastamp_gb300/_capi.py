@@ -83,6 +83,7 @@ def lib(path: str = LIB_PATH):
             "gbmd_get_launch_ex": ([vp, P(i32), P(i32), P(i32)], i32),
             "gbmd_set_skin": ([vp, dbl], i32),
             "gbmd_build_neighbors": ([vp], i32),
+            "gbmd_update_neighbors": ([vp, P(i32)], i32),
             "gbmd_export_pairs": ([vp, i64, vp, vp, vp, P(i64)], i32),
             "gbmd_neighbor_stats": ([vp, P(i64), P(i32), vp], i32),
             "gbmd_compute_forces": ([vp, i32], i32),
@@ -283,6 +284,13 @@ class Context:
         img = np.empty((max(n, 1), 3), np.int8)
         self._chk(self._L.gbmd_export_pairs(self.h, n, _p(a), _p(b), _p(img), C.byref(cnt)))
         return np.column_stack([a[:n].astype(np.int64), b[:n].astype(np.int64), img[:n].astype(np.int64)])
+
+    def update_neighbors(self) -> bool:
+        """check_and_update_particles: rebuild when some atom moved more than
+        skin/2 since the last rebuild; returns whether it rebuilt."""
+        r = C.c_int()
+        self._chk(self._L.gbmd_update_neighbors(self.h, C.byref(r)))
+        return bool(r.value)
 
     def export_pairs_raw(self):
         """The exported pair set as three arrays (id_i, id_j: uint64; image:

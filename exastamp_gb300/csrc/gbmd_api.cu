@@ -1037,6 +1037,30 @@ int gbmd_build_neighbors(gbmd_context* c) {
   return GBMD_OK;
 }
 
+int gbmd_update_neighbors(gbmd_context* c, int* rebuilt) {
+  if (!c) return GBMD_ERR_INVALID;
+  if (rebuilt) *rebuilt = 0;
+  cudaSetDevice(c->device);
+  if (c->n == 0) return GBMD_OK;
+  if (c->list_valid) {
+    // trigger_move_particles = particle_displ_over: one device test, its
+    // outcome read back so a rebuild can regrow the list on overflow
+    cudaStream_t s = c->stream;
+    GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_DISPL, 0, sizeof(int), s));
+    const double thr = 0.5 * c->skin;
+    k_displ_over<<<nblk(c->n, 256), 256, 0, s>>>(c->n, c->X(), c->Y(), c->Z(), c->rref, c->cap, thr * thr,
+                                                 c->d_err + ERRW_DISPL);
+    int rc = sync_error_word(c);
+    if (rc) return rc;
+    if (!c->h_err[ERRW_DISPL]) return GBMD_OK;
+  }
+  int rc = do_rebuild(c, true);
+  if (rc) return rc;
+  c->forces_valid_step = c->rho_valid_step = -1;
+  if (rebuilt) *rebuilt = 1;
+  return GBMD_OK;
+}
+
 int gbmd_export_pairs(gbmd_context* c, int64_t cap, uint64_t* id_i, uint64_t* id_j, int8_t* img, int64_t* count) {
   if (!c || !count) return GBMD_ERR_INVALID;
   return export_pairs(c, cap, id_i, id_j, img, count);

@@ -2,30 +2,42 @@
 // (include/gbmd.h) into exaStamp's operator slots.
 //
 // Built as an exaStamp plugin (onika_add_plugin, as in
-// src/potential/pair_potential_template/CMakeLists.txt L54-59) when onika and
-// exaNBody are available; it is not compiled in this repository, which has
-// neither.  Operators (drop-ins for the compute_force slot):
+// src/potential/pair_potential_template/CMakeLists.txt L54-59) where onika
+// and exaNBody are installed.  This repository has neither: it checks the
+// file against stand-in headers of the API it uses (tests/onika_stub, a
+// syntax and instantiation check) and runs the host logic, which lives in
+// gb300_bridge.h, over a fake grid on the GPU (tests/onika_bridge).
 //
-//   gb300_lj_force         lj_compute_force  (pair_potential_impl.hxx L104-121)
-//   gb300_lj_force_symetric lj_compute_force_symetric (pair_potential_singlemat_symetric.cpp L335-346):
-//                          the same with the Newton-3 half list (gbmd_set_newton3)
-//   gb300_lj_multi_force   lj_multi_force    (pair_potential_force_op_multiparam.h L249-284)
-//   gb300_eam_alloy_force  eam_alloy_force   (eam_potential_multimat.cu L88-109)
-//   gb300_johnson_force    johnson_force     (johnson.h, eam_potential.cu L69-193)
-//   gb300_force            any of them, chosen by the slot `potential`
+// Force operators (drop-ins for the compute_force slot):
+//   gb300_lj_force          lj_compute_force  (pair_potential_impl.hxx L104-121)
+//   gb300_lj_force_symetric lj_compute_force_symetric (pair_potential_singlemat_symetric.cpp
+//                           L335-346): the same forces; the half list is opt-in (half_list)
+//   gb300_lj_multi_force    lj_multi_force    (pair_potential_force_op_multiparam.h L249-284)
+//   gb300_eam_alloy_force   eam_alloy_force   (eam_potential_multimat.cu L88-109), with the
+//                           eam_rho / eam_rho2emb / eam_force split as separate instances
+//   gb300_johnson_force     johnson_force     (johnson.h, eam_potential.cu L69-193)
+//   gb300_force             any of them, chosen by the slot `potential`
+// Whole-step operators (config_numerical_schemes.msp L23-28, L44-52;
+// config_move_particles.msp L116-152):
+//   gb300_push_f_v_r        push_f_v_r of verlet_first_half
+//   gb300_push_f_v          push_f_v of verlet_first_half / verlet_second_half
+//   gb300_neighbors         check_and_update_particles (displacement trigger + rebuild)
+//   gb300_sync_grid         the device state back into the grid (before thermo or dumps)
 //
-// Each keeps its reference operator's slot names and meaning (parameters,
-// rcut, rcut_max, ghost_dist_max, chunk_neighbors, species, grid, domain,
+// All of them share one gb300::Session (device context, upload layout)
+// through the slot gb300_session.  With only a force operator bound, each
+// call copies the inner particles in and f = m a, ep and the virial out
+// (re-uploading every field when move_particles changed the particle order,
+// positions only otherwise); with the whole-step operators bound the state
+// stays on the device (see gb300_bridge.h).  Each force operator keeps its
+// reference operator's slot names and meaning (parameters, rcut, rcut_max,
+// ghost_dist_max, chunk_neighbors, species, grid, domain,
 // trigger_thermo_state, compute_virial, the eam_* pass flags), plus rcut_inc
 // (the neighbour skin, global.rcut_inc) and precision (mixed or fp64).
 // Slots that only steer the reference's own traversal (chunk_neighbors,
-// ghost, compact_nbh_weight, enable_pair_weights) are accepted and unused:
-// the library keeps its own list, rebuilt on the skin/2 displacement test.  Each execute() copies the inner-cell particles
-// (rx,ry,rz,vx,vy,vz,type,id) into the GPU context, runs zero_force_energy +
-// compute_force + force_to_accel on the device, and writes forces f = m*a,
-// ep and virial back into the cells, so the graph's own force_to_accel and
-// push operators keep working unchanged.  Errors become fatal_error(), like
-// the reference operators.
+// ghost, compact_nbh_weight, enable_pair_weights, particle_locks) are
+// accepted and unused.  Library errors become fatal_error(), like the
+// reference operators'.
 #include <onika/scg/operator.h>
 #include <onika/scg/operator_factory.h>
 #include <onika/scg/operator_slot.h>
@@ -42,6 +54,8 @@
 
 #include <gbmd.h>
 
+#include "gb300_bridge.h"
+
 #include <memory>
 #include <string>
 #include <vector>
@@ -49,109 +63,123 @@
 namespace exaStamp {
 using namespace exanb;
 
-namespace gb300 {
+namespace gb300_ops {
 
-struct ContextDeleter {
-  void operator()(gbmd_context* c) const { gbmd_destroy(c); }
+using gb300::Field;
+
+// The onika grid seen through gb300_bridge.h's grid-view interface: the
+// inner cells in grid order, the particle fields by (cell, slot).
+template <class GridT>
+class GridView {
+ public:
+  GridView(GridT& grid, const ParticleSpecies& species) : m_grid(grid), m_species(species) {
+    const IJK dims = grid.dimension();
+    const ssize_t gl = grid.ghost_layers();
+    GRID_FOR_BEGIN(dims - 2 * gl, _, loc) { m_inner.push_back(grid_ijk_to_index(dims, loc + gl)); }
+    GRID_FOR_END
+  }
+  size_t inner_cells() const { return m_inner.size(); }
+  size_t cell_index(size_t k) const { return m_inner[k]; }
+  size_t cell_size(size_t c) const { return m_grid.cells()[c].size(); }
+  double get(size_t c, Field f, size_t p) const {
+    auto cells = m_grid.cells();
+    switch (f) {
+      case gb300::RX: return cells[c][field::rx][p];
+      case gb300::RY: return cells[c][field::ry][p];
+      case gb300::RZ: return cells[c][field::rz][p];
+      case gb300::VX: return cells[c][field::vx][p];
+      case gb300::VY: return cells[c][field::vy][p];
+      case gb300::VZ: return cells[c][field::vz][p];
+      case gb300::FX: return cells[c][field::fx][p];
+      case gb300::FY: return cells[c][field::fy][p];
+      case gb300::FZ: return cells[c][field::fz][p];
+      default: return cells[c][field::ep][p];
+    }
+  }
+  void set(size_t c, Field f, size_t p, double v) {
+    auto cells = m_grid.cells();
+    switch (f) {
+      case gb300::RX: cells[c][field::rx][p] = v; break;
+      case gb300::RY: cells[c][field::ry][p] = v; break;
+      case gb300::RZ: cells[c][field::rz][p] = v; break;
+      case gb300::VX: cells[c][field::vx][p] = v; break;
+      case gb300::VY: cells[c][field::vy][p] = v; break;
+      case gb300::VZ: cells[c][field::vz][p] = v; break;
+      case gb300::FX: cells[c][field::fx][p] = v; break;
+      case gb300::FY: cells[c][field::fy][p] = v; break;
+      case gb300::FZ: cells[c][field::fz][p] = v; break;
+      default: cells[c][field::ep][p] = v; break;
+    }
+  }
+  uint8_t type(size_t c, size_t p) const { return m_grid.cells()[c][field::type][p]; }
+  uint64_t id(size_t c, size_t p) const { return m_grid.cells()[c][field::id][p]; }
+  // grid_flavor_multimat_mechanics carries the virial (grid_flavor.cpp L56-84)
+  static constexpr bool kVirial = GridHasField<GridT, field::_virial>::value;
+  bool has_virial() const { return kVirial; }
+  void set_virial(size_t c, size_t p, const double v[9]) {
+    if constexpr (kVirial) {
+      Mat3d& m = m_grid.cells()[c][field::virial][p];
+      m.m11 = v[0]; m.m12 = v[1]; m.m13 = v[2];
+      m.m21 = v[3]; m.m22 = v[4]; m.m23 = v[5];
+      m.m31 = v[6]; m.m32 = v[7]; m.m33 = v[8];
+    }
+  }
+  double mass(int t) const { return m_species.at(t).m_mass; }
+
+ private:
+  GridT& m_grid;
+  const ParticleSpecies& m_species;
+  std::vector<size_t> m_inner;
 };
-using ContextPtr = std::unique_ptr<gbmd_context, ContextDeleter>;
 
-inline void check(gbmd_context* c, int rc, const char* what) {
+// The shared session, created on first use with the domain and species.
+inline gb300::Session& session_for(gb300::SessionPtr& ptr, const Domain& domain, const ParticleSpecies& species) {
+  if (!ptr) ptr = std::make_shared<gb300::Session>();
+  if (!ptr->ctx) {
+    const Vec3d lo = domain.bounds().bmin, hi = domain.bounds().bmax;
+    const double blo[3] = {lo.x, lo.y, lo.z}, bhi[3] = {hi.x, hi.y, hi.z};
+    const int per[3] = {domain.periodic_boundary_x(), domain.periodic_boundary_y(), domain.periodic_boundary_z()};
+    if (!domain.xform_is_identity())
+      fatal_error() << "gb300: only orthorhombic domains (identity xform) are supported" << std::endl;
+    std::vector<double> m(species.size());
+    for (size_t t = 0; t < m.size(); ++t) m[t] = species.at(t).m_mass;
+    try {
+      gb300::ensure_context(*ptr, parallel_execution_context()->gpu_stream(), blo, bhi, per, m);
+    } catch (const gb300::Error& e) {
+      fatal_error() << "gb300: " << e.what() << std::endl;
+    }
+  }
+  return *ptr;
+}
+
+// A library status as the reference operators report errors.
+inline void ok(gbmd_context* c, int rc, const char* what) {
   if (rc != GBMD_OK) fatal_error() << what << " failed: " << gbmd_last_error(c) << std::endl;
 }
 
-// Host staging of the inner cells' particles in a fixed (cell, slot) order.
-struct Staging {
-  std::vector<double> rx, ry, rz, vx, vy, vz, ax, ay, az, ep, vir;
-  std::vector<uint8_t> type;
-  std::vector<uint64_t> id;
-  std::vector<size_t> cell_of, slot_of;
-  size_t n = 0;
-};
+inline void finish_setup(gb300::Session& s, double skin, const std::string& precision) {
+  ok(s.ctx, gbmd_set_skin(s.ctx, skin), "gbmd_set_skin");
+  ok(s.ctx, gbmd_set_precision(s.ctx, precision == "fp64" ? GBMD_PRECISION_FP64 : GBMD_PRECISION_MIXED),
+               "gbmd_set_precision");
+  s.potential_set = true;
+}
 
+// Runs fn(), turning library errors into fatal_error().
+template <class Fn>
+void guarded(const char* op, Fn&& fn) {
+  try {
+    fn();
+  } catch (const gb300::Error& e) {
+    fatal_error() << op << ": " << e.what() << std::endl;
+  }
+}
+
+// One compute_force call of a force operator (per call or resident).
 template <class GridT>
-void gather(const GridT& grid, Staging& s) {
-  auto cells = grid.cells();
-  const IJK dims = grid.dimension();
-  const ssize_t gl = grid.ghost_layers();
-  s = Staging{};
-  GRID_FOR_BEGIN(dims - 2 * gl, _, loc) {
-    const size_t c = grid_ijk_to_index(dims, loc + gl);
-    const size_t np = cells[c].size();
-    for (size_t p = 0; p < np; ++p) {
-      s.rx.push_back(cells[c][field::rx][p]);
-      s.ry.push_back(cells[c][field::ry][p]);
-      s.rz.push_back(cells[c][field::rz][p]);
-      s.vx.push_back(cells[c][field::vx][p]);
-      s.vy.push_back(cells[c][field::vy][p]);
-      s.vz.push_back(cells[c][field::vz][p]);
-      s.type.push_back(cells[c][field::type][p]);
-      s.id.push_back(cells[c][field::id][p]);
-      s.cell_of.push_back(c);
-      s.slot_of.push_back(p);
-    }
-  }
-  GRID_FOR_END
-  s.n = s.rx.size();
-  s.ax.resize(s.n);
-  s.ay.resize(s.n);
-  s.az.resize(s.n);
-  s.ep.resize(s.n);
-  s.vir.resize(9 * s.n);
-}
-
-inline gbmd_context* make_context(const Domain& domain, const ParticleSpecies& species) {
-  gbmd_context* c = nullptr;
-  if (gbmd_create(&c, 0, parallel_execution_context()->gpu_stream()) != GBMD_OK)
-    fatal_error() << "gb300: no GPU context" << std::endl;
-  const Vec3d lo = domain.bounds().bmin, hi = domain.bounds().bmax;
-  const double blo[3] = {lo.x, lo.y, lo.z}, bhi[3] = {hi.x, hi.y, hi.z};
-  const int per[3] = {domain.periodic_boundary_x(), domain.periodic_boundary_y(), domain.periodic_boundary_z()};
-  check(c, gbmd_set_box(c, blo, bhi, per), "gbmd_set_box");
-  std::vector<double> m(species.size());
-  for (size_t t = 0; t < m.size(); ++t) m[t] = species.at(t).m_mass;
-  check(c, gbmd_set_species(c, (int)m.size(), m.data()), "gbmd_set_species");
-  return c;
-}
-
-inline void finish_setup(gbmd_context* c, double skin, const std::string& precision) {
-  check(c, gbmd_set_skin(c, skin), "gbmd_set_skin");
-  check(c, gbmd_set_precision(c, precision == "fp64" ? GBMD_PRECISION_FP64 : GBMD_PRECISION_MIXED),
-        "gbmd_set_precision");
-}
-
-// One compute_force call: the inner cells' particles into the context
-// (all of them when the count changed, else positions only: the library's
-// skin/2 displacement test decides a rebuild), zero_force_energy +
-// compute_force + force_to_accel on the device, then f = m a and ep back into
-// the cells (the graph's force_to_accel runs next).
-template <class GridT>
-void compute_and_store(gbmd_context* c, GridT& grid, const ParticleSpecies& species, Staging& s, size_t& uploaded,
-                       bool energy, bool virial) {
-  gather(grid, s);
-  if (s.n != uploaded) {
-    check(c, gbmd_upload_atoms(c, (int64_t)s.n, s.rx.data(), s.ry.data(), s.rz.data(), s.vx.data(), s.vy.data(),
-                               s.vz.data(), s.type.data(), s.id.data()),
-          "gbmd_upload_atoms");
-    uploaded = s.n;
-  } else {
-    check(c, gbmd_upload_positions(c, s.rx.data(), s.ry.data(), s.rz.data(), nullptr, nullptr, nullptr),
-          "gbmd_upload_positions");
-  }
-  check(c, gbmd_compute_forces(c, (energy ? GBMD_FORCE_ENERGY : 0) | (virial ? GBMD_FORCE_VIRIAL : 0)),
-        "gbmd_compute_forces");
-  check(c, gbmd_download(c, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, s.ax.data(), s.ay.data(),
-                         s.az.data(), energy ? s.ep.data() : nullptr, virial ? s.vir.data() : nullptr),
-        "gbmd_download");
-  auto cells = grid.cells();
-  for (size_t k = 0; k < s.n; ++k) {
-    const size_t cc = s.cell_of[k], p = s.slot_of[k];
-    const double m = species.at(s.type[k]).m_mass;
-    cells[cc][field::fx][p] = s.ax[k] * m;
-    cells[cc][field::fy][p] = s.ay[k] * m;
-    cells[cc][field::fz][p] = s.az[k] * m;
-    if (energy) cells[cc][field::ep][p] = s.ep[k];
-  }
+void compute_force_call(const char* op, gb300::Session& s, GridT& grid, const ParticleSpecies& species, bool energy,
+                        bool virial, int passes) {
+  GridView<GridT> view(grid, species);
+  guarded(op, [&] { gb300::compute_forces(s, view, energy, virial, passes); });
 }
 
 // `parameters` of eam_alloy_force: the setfl file, as a scalar or {file: ...}
@@ -171,13 +199,13 @@ struct LJPairList {
   std::vector<LJPairEntry> pairs;
 };
 
-}  // namespace gb300
+}  // namespace gb300_ops
 }  // namespace exaStamp
 
 namespace YAML {
 template <>
-struct convert<exaStamp::gb300::SetflRef> {
-  static bool decode(const Node& node, exaStamp::gb300::SetflRef& v) {
+struct convert<exaStamp::gb300_ops::SetflRef> {
+  static bool decode(const Node& node, exaStamp::gb300_ops::SetflRef& v) {
     if (node.IsScalar()) v.file = node.as<std::string>();
     else if (node.IsMap() && node["file"]) v.file = node["file"].as<std::string>();
     else return false;
@@ -185,12 +213,12 @@ struct convert<exaStamp::gb300::SetflRef> {
   }
 };
 template <>
-struct convert<exaStamp::gb300::LJPairList> {
-  static bool decode(const Node& node, exaStamp::gb300::LJPairList& v) {
+struct convert<exaStamp::gb300_ops::LJPairList> {
+  static bool decode(const Node& node, exaStamp::gb300_ops::LJPairList& v) {
     if (!node.IsSequence()) return false;
     for (auto pp : node) {
       if (!pp.IsMap() || !pp["type_a"] || !pp["type_b"] || !pp["rcut"] || !pp["parameters"]) return false;
-      exaStamp::gb300::LJPairEntry e;
+      exaStamp::gb300_ops::LJPairEntry e;
       e.type_a = pp["type_a"].as<std::string>();
       e.type_b = pp["type_b"].as<std::string>();
       e.rcut = pp["rcut"].as<onika::physics::Quantity>().convert();
@@ -205,12 +233,19 @@ struct convert<exaStamp::gb300::LJPairList> {
 namespace exaStamp {
 
 using StringVector = std::vector<std::string>;
+using gb300_ops::compute_force_call;
+using gb300_ops::finish_setup;
+using gb300_ops::session_for;
+
+#define GB300_SESSION_SLOT \
+  ADD_SLOT(gb300::SessionPtr, gb300_session, INPUT_OUTPUT, gb300::SessionPtr{}, DocString{"shared GPU context"})
 
 // lj_compute_force (pair_potential_impl.hxx L104-121): one species pair,
 // energy shifted by e(rcut) as the reference does (L373-377).  SYM: the
 // lj_compute_force_symetric slots (pair_potential_singlemat_symetric.cpp
-// L335-346; particle_locks accepted and unused: the library scatters the
-// reaction forces with atomics) on the Newton-3 half list.
+// L335-346; particle_locks accepted and unused).  The forces are the same;
+// the library's full list is faster on GB300 and deterministic, so the
+// Newton-3 half list (atomic reaction forces) is opt-in through half_list.
 template <class GridT, bool SYM = false>
 class Gb300LJForceNode : public OperatorNode {
   ADD_SLOT(LennardJonesParms, parameters, INPUT, LennardJonesParms{});
@@ -226,28 +261,26 @@ class Gb300LJForceNode : public OperatorNode {
   ADD_SLOT(bool, compute_virial, INPUT, false);
   ADD_SLOT(double, rcut_inc, INPUT, 1.0, DocString{"neighbour skin (global.rcut_inc)"});
   ADD_SLOT(std::string, precision, INPUT, std::string{"mixed"}, DocString{"mixed or fp64"});
-  ADD_SLOT(GridParticleLocks, particle_locks, INPUT, OPTIONAL, DocString{"unused (atomic scatter)"});
-  gb300::ContextPtr m_ctx;
-  gb300::Staging m_stage;
-  size_t m_uploaded = 0;
+  ADD_SLOT(bool, half_list, INPUT, false, DocString{"Newton-3 half list with atomic reaction forces"});
+  ADD_SLOT(GridParticleLocks, particle_locks, INPUT, OPTIONAL, DocString{"unused"});
+  GB300_SESSION_SLOT;
 
  public:
   inline void execute() override final {
     *rcut_max = std::max(*rcut, *rcut_max);
     if (grid->number_of_cells() == 0) return;
-    if (!m_ctx) {
-      gbmd_context* c = gb300::make_context(*domain, *species);
-      m_ctx.reset(c);
-      gb300::check(c, gbmd_set_lj(c, parameters->epsilon, parameters->sigma, *rcut), "gbmd_set_lj");
-      gb300::finish_setup(c, *rcut_inc, *precision);
-      if (SYM) {
+    gb300::Session& s = session_for(*gb300_session, *domain, *species);
+    if (!s.potential_set) {
+      gb300_ops::ok(s.ctx, gbmd_set_lj(s.ctx, parameters->epsilon, parameters->sigma, *rcut), "gbmd_set_lj");
+      finish_setup(s, *rcut_inc, *precision);
+      if (SYM && *half_list) {
         // the half-list kernel: mixed precision, one lane x 4 entries per load
-        gb300::check(c, gbmd_set_launch_ex(c, 1, 4, 256), "gbmd_set_launch_ex");
-        gb300::check(c, gbmd_set_newton3(c, 1), "gbmd_set_newton3");
+        gb300_ops::ok(s.ctx, gbmd_set_launch_ex(s.ctx, 1, 4, 256), "gbmd_set_launch_ex");
+        gb300_ops::ok(s.ctx, gbmd_set_newton3(s.ctx, 1), "gbmd_set_newton3");
       }
     }
     const bool energy = trigger_thermo_state.has_value() && *trigger_thermo_state;
-    gb300::compute_and_store(m_ctx.get(), *grid, *species, m_stage, m_uploaded, energy, energy && *compute_virial);
+    compute_force_call("gb300_lj_force", s, *grid, *species, energy, energy && *compute_virial, 0);
   }
 };
 
@@ -257,7 +290,7 @@ class Gb300LJForceNode : public OperatorNode {
 template <class GridT>
 class Gb300LJMultiForceNode : public OperatorNode {
   ADD_SLOT(LennardJonesParms, common_parameters, INPUT, OPTIONAL);
-  ADD_SLOT(gb300::LJPairList, parameters, INPUT, REQUIRED);
+  ADD_SLOT(gb300_ops::LJPairList, parameters, INPUT, REQUIRED);
   ADD_SLOT(double, rcut, INPUT, REQUIRED);
   ADD_SLOT(double, rcut_max, INPUT_OUTPUT, 0.0);
   ADD_SLOT(exanb::GridChunkNeighbors, chunk_neighbors, INPUT, exanb::GridChunkNeighbors{}, DocString{"unused"});
@@ -268,9 +301,7 @@ class Gb300LJMultiForceNode : public OperatorNode {
   ADD_SLOT(bool, compute_virial, INPUT, false);
   ADD_SLOT(double, rcut_inc, INPUT, 1.0, DocString{"neighbour skin (global.rcut_inc)"});
   ADD_SLOT(std::string, precision, INPUT, std::string{"mixed"}, DocString{"mixed or fp64"});
-  gb300::ContextPtr m_ctx;
-  gb300::Staging m_stage;
-  size_t m_uploaded = 0;
+  GB300_SESSION_SLOT;
 
  public:
   inline void execute() override final {
@@ -278,9 +309,8 @@ class Gb300LJMultiForceNode : public OperatorNode {
     for (const auto& e : parameters->pairs) rmax = std::max(rmax, e.rcut);
     *rcut_max = std::max(rmax, *rcut_max);
     if (grid->number_of_cells() == 0) return;
-    if (!m_ctx) {
-      gbmd_context* c = gb300::make_context(*domain, *species);
-      m_ctx.reset(c);
+    gb300::Session& s = session_for(*gb300_session, *domain, *species);
+    if (!s.potential_set) {
       const int nt = (int)species->size();
       std::vector<double> eps(nt * nt, 0.0), sig(nt * nt, 1.0), rc(nt * nt, 0.0);
       if (common_parameters.has_value())
@@ -303,20 +333,28 @@ class Gb300LJMultiForceNode : public OperatorNode {
           rc[k] = e.rcut;
         }
       }
-      gb300::check(c, gbmd_set_lj_multi(c, nt, eps.data(), sig.data(), rc.data(), *rcut), "gbmd_set_lj_multi");
-      gb300::finish_setup(c, *rcut_inc, *precision);
+      gb300_ops::ok(s.ctx, gbmd_set_lj_multi(s.ctx, nt, eps.data(), sig.data(), rc.data(), *rcut),
+                   "gbmd_set_lj_multi");
+      finish_setup(s, *rcut_inc, *precision);
     }
     const bool energy = trigger_thermo_state.has_value() && *trigger_thermo_state;
-    gb300::compute_and_store(m_ctx.get(), *grid, *species, m_stage, m_uploaded, energy, energy && *compute_virial);
+    compute_force_call("gb300_lj_multi_force", s, *grid, *species, energy, energy && *compute_virial, 0);
   }
 };
 
-// eam_alloy_force (eam_potential_multimat.cu L88-109): the three passes in
-// one call; the split-pass and Newton-3 forms are not offered.
+// eam_alloy_force (eam_potential_multimat.cu L88-109).  The passes follow
+// the eam_* flags (L101-105, L186-232): all three in one call, or split
+// over operator instances as in baseline_single_specy.yaml L41-54 --
+// eam_rho (density + embedding, F'(rho) kept on the device), eam_rho2emb
+// alone (nothing left to do: the embedding ran with the density), eam_force
+// (the force pass from the kept F'(rho), on the same positions).  The
+// instances share the device context through gb300_session.  eam_ghost is
+// accepted (there are no ghost cells on the device).  eam_symmetry (Newton-3)
+// is refused: the library has no half-list EAM kernels.
 template <class GridT>
 class Gb300EamAlloyForceNode : public OperatorNode {
   ADD_SLOT(ParticleSpecies, species, INPUT, REQUIRED);
-  ADD_SLOT(gb300::SetflRef, parameters, INPUT, REQUIRED, DocString{"setfl file (scalar or {file: ...})"});
+  ADD_SLOT(gb300_ops::SetflRef, parameters, INPUT, REQUIRED, DocString{"setfl file (scalar or {file: ...})"});
   ADD_SLOT(StringVector, types, INPUT, StringVector{});
   ADD_SLOT(double, rcut, INPUT, REQUIRED);
   ADD_SLOT(double, rcut_max, INPUT_OUTPUT, 0.0);
@@ -333,28 +371,29 @@ class Gb300EamAlloyForceNode : public OperatorNode {
   ADD_SLOT(bool, eam_symmetry, INPUT, false);
   ADD_SLOT(double, rcut_inc, INPUT, 1.0, DocString{"neighbour skin (global.rcut_inc)"});
   ADD_SLOT(std::string, precision, INPUT, std::string{"mixed"}, DocString{"mixed or fp64"});
-  gb300::ContextPtr m_ctx;
-  gb300::Staging m_stage;
-  size_t m_uploaded = 0;
+  GB300_SESSION_SLOT;
 
  public:
   inline void execute() override final {
     *rcut_max = std::max(*rcut, *rcut_max);
     *ghost_dist_max = std::max(*ghost_dist_max, 2.0 * (*rcut));
     if (grid->number_of_cells() == 0) return;
-    if (!(*eam_rho && *eam_rho2emb && *eam_force) || *eam_symmetry)
-      fatal_error() << "gb300_eam_alloy_force: only the fused three-pass full-list form is offered" << std::endl;
-    if (!m_ctx) {
-      gbmd_context* c = gb300::make_context(*domain, *species);
-      m_ctx.reset(c);
-      gb300::check(c,
-                   gbmd_load_setfl(c, onika::data_file_path(parameters->file).c_str(), *rcut,
+    if (*eam_symmetry) fatal_error() << "gb300_eam_alloy_force: eam_symmetry is not offered" << std::endl;
+    const int passes = (*eam_rho && *eam_force) ? 0
+                       : *eam_rho               ? GBMD_FORCE_PASS_DENSITY
+                       : *eam_force             ? GBMD_FORCE_PASS_FORCE
+                                                : -1;
+    if (passes < 0) return;  // eam_rho2emb alone: the embedding already ran with the density
+    gb300::Session& s = session_for(*gb300_session, *domain, *species);
+    if (!s.potential_set) {
+      gb300_ops::ok(s.ctx,
+                   gbmd_load_setfl(s.ctx, onika::data_file_path(parameters->file).c_str(), *rcut,
                                    EXASTAMP_CONST_QUANTITY(1. * eV * ang), EXASTAMP_CONST_QUANTITY(1.0 * eV)),
                    "gbmd_load_setfl");
-      gb300::finish_setup(c, *rcut_inc, *precision);
+      finish_setup(s, *rcut_inc, *precision);
     }
     const bool energy = trigger_thermo_state.has_value() && *trigger_thermo_state;
-    gb300::compute_and_store(m_ctx.get(), *grid, *species, m_stage, m_uploaded, energy, energy && *compute_virial);
+    compute_force_call("gb300_eam_alloy_force", s, *grid, *species, energy, energy && *compute_virial, passes);
   }
 };
 
@@ -374,26 +413,23 @@ class Gb300JohnsonForceNode : public OperatorNode {
   ADD_SLOT(bool, compute_virial, INPUT, false);
   ADD_SLOT(double, rcut_inc, INPUT, 1.0, DocString{"neighbour skin (global.rcut_inc)"});
   ADD_SLOT(std::string, precision, INPUT, std::string{"mixed"}, DocString{"mixed or fp64"});
-  gb300::ContextPtr m_ctx;
-  gb300::Staging m_stage;
-  size_t m_uploaded = 0;
+  GB300_SESSION_SLOT;
 
  public:
   inline void execute() override final {
     *rcut_max = std::max(*rcut, *rcut_max);
     *ghost_dist_max = std::max(*ghost_dist_max, 2.0 * (*rcut));
     if (grid->number_of_cells() == 0) return;
-    if (!m_ctx) {
-      gbmd_context* c = gb300::make_context(*domain, *species);
-      m_ctx.reset(c);
+    gb300::Session& s = session_for(*gb300_session, *domain, *species);
+    if (!s.potential_set) {
       const EamJohnsonParameters& q = *parameters;
       const double jp[19] = {q.re, q.fe, q.rhoe, q.alpha, q.beta, q.A,   q.B,  q.kappa, q.lambda, q.Fn0,
                              q.Fn1, q.Fn2, q.Fn3, q.F0, q.F1, q.F2, q.F3, q.Fo, q.eta};
-      gb300::check(c, gbmd_set_eam_johnson(c, jp, *rcut), "gbmd_set_eam_johnson");
-      gb300::finish_setup(c, *rcut_inc, *precision);
+      gb300_ops::ok(s.ctx, gbmd_set_eam_johnson(s.ctx, jp, *rcut), "gbmd_set_eam_johnson");
+      finish_setup(s, *rcut_inc, *precision);
     }
     const bool energy = trigger_thermo_state.has_value() && *trigger_thermo_state;
-    gb300::compute_and_store(m_ctx.get(), *grid, *species, m_stage, m_uploaded, energy, energy && *compute_virial);
+    compute_force_call("gb300_johnson_force", s, *grid, *species, energy, energy && *compute_virial, 0);
   }
 };
 
@@ -415,10 +451,7 @@ class Gb300ForceNode : public OperatorNode {
   ADD_SLOT(GridT, grid, INPUT_OUTPUT);
   ADD_SLOT(Domain, domain, INPUT, REQUIRED);
   ADD_SLOT(ParticleSpecies, species, INPUT, REQUIRED);
-
-  gb300::ContextPtr m_ctx;
-  gb300::Staging m_stage;
-  size_t m_uploaded = 0;
+  GB300_SESSION_SLOT;
 
  public:
   inline void execute() override final {
@@ -426,14 +459,13 @@ class Gb300ForceNode : public OperatorNode {
     if (*potential == "eam_alloy" || *potential == "johnson")
       *ghost_dist_max = std::max(*ghost_dist_max, 2.0 * (*rcut));
     if (grid->number_of_cells() == 0) return;  // pre-initialisation pass publishing rcut_max
-    if (!m_ctx) {
-      gbmd_context* c = gb300::make_context(*domain, *species);
-      m_ctx.reset(c);
+    gb300::Session& s = session_for(*gb300_session, *domain, *species);
+    if (!s.potential_set) {
       if (*potential == "lj")
-        gb300::check(c, gbmd_set_lj(c, *epsilon, *sigma, *rcut), "gbmd_set_lj");
+        gb300_ops::ok(s.ctx, gbmd_set_lj(s.ctx, *epsilon, *sigma, *rcut), "gbmd_set_lj");
       else if (*potential == "eam_alloy")
-        gb300::check(c,
-                     gbmd_load_setfl(c, onika::data_file_path(*setfl_file).c_str(), *rcut,
+        gb300_ops::ok(s.ctx,
+                     gbmd_load_setfl(s.ctx, onika::data_file_path(*setfl_file).c_str(), *rcut,
                                      EXASTAMP_CONST_QUANTITY(1. * eV * ang), EXASTAMP_CONST_QUANTITY(1.0 * eV)),
                      "gbmd_load_setfl");
       else if (*potential == "johnson") {
@@ -441,19 +473,90 @@ class Gb300ForceNode : public OperatorNode {
         const EamJohnsonParameters& q = *johnson_parameters;
         const double jp[19] = {q.re, q.fe, q.rhoe, q.alpha, q.beta, q.A,   q.B,  q.kappa, q.lambda, q.Fn0,
                                q.Fn1, q.Fn2, q.Fn3, q.F0, q.F1, q.F2, q.F3, q.Fo, q.eta};
-        gb300::check(c, gbmd_set_eam_johnson(c, jp, *rcut), "gbmd_set_eam_johnson");
+        gb300_ops::ok(s.ctx, gbmd_set_eam_johnson(s.ctx, jp, *rcut), "gbmd_set_eam_johnson");
       } else
         fatal_error() << "gb300: unsupported potential " << *potential << std::endl;
-      gb300::finish_setup(c, *rcut_inc, *precision);
+      finish_setup(s, *rcut_inc, *precision);
     }
     const bool energy = trigger_thermo_state.has_value() && *trigger_thermo_state;
-    gb300::compute_and_store(m_ctx.get(), *grid, *species, m_stage, m_uploaded, energy, energy && *compute_virial);
+    compute_force_call("gb300_force", s, *grid, *species, energy, energy && *compute_virial, 0);
+  }
+};
+
+// push_f_v_r / push_f_v (exaNBody push operators, scheduled by
+// config_numerical_schemes.msp L23-28; formula
+// push_vec3_2nd_order_xform_minimization.cpp L33-38) on the device's copy of
+// the state: r += v dt' + a dt'^2 / 2 (R) or v += a dt' (V), dt' = dt dt_scale.
+// xform_mode is accepted for orthorhombic domains (identity xform) only.
+template <class GridT, bool R>
+class Gb300PushNode : public OperatorNode {
+  ADD_SLOT(GridT, grid, INPUT_OUTPUT);
+  ADD_SLOT(double, dt, INPUT, REQUIRED);
+  ADD_SLOT(double, dt_scale, INPUT, REQUIRED);
+  ADD_SLOT(std::string, xform_mode, INPUT, std::string{"INV_XFORM"});
+  ADD_SLOT(Domain, domain, INPUT, REQUIRED);
+  ADD_SLOT(ParticleSpecies, species, INPUT, REQUIRED);
+  GB300_SESSION_SLOT;
+
+ public:
+  inline void execute() override final {
+    if (grid->number_of_cells() == 0) return;
+    gb300::Session& s = session_for(*gb300_session, *domain, *species);
+    gb300_ops::GridView<GridT> view(*grid, *species);
+    gb300_ops::guarded(R ? "gb300_push_f_v_r" : "gb300_push_f_v", [&] {
+      if (R) gb300::push_f_v_r(s, view, *dt, *dt_scale);
+      else gb300::push_f_v(s, view, *dt, *dt_scale);
+    });
+  }
+};
+
+// check_and_update_particles (config_move_particles.msp L116-152) on the
+// device's copy: trigger_move_particles (particle_displ_over against skin/2,
+// L19-22) and the full update (wrap, rebin, neighbour list) when it fires.
+// The outcome is published in trigger_move_particles for the graph's other
+// operators (load balancing logs, counters).
+template <class GridT>
+class Gb300NeighborsNode : public OperatorNode {
+  ADD_SLOT(GridT, grid, INPUT_OUTPUT);
+  ADD_SLOT(Domain, domain, INPUT, REQUIRED);
+  ADD_SLOT(ParticleSpecies, species, INPUT, REQUIRED);
+  ADD_SLOT(bool, trigger_move_particles, OUTPUT);
+  GB300_SESSION_SLOT;
+
+ public:
+  inline void execute() override final {
+    if (grid->number_of_cells() == 0) return;
+    gb300::Session& s = session_for(*gb300_session, *domain, *species);
+    gb300_ops::GridView<GridT> view(*grid, *species);
+    bool rebuilt = false;
+    gb300_ops::guarded("gb300_neighbors", [&] { rebuilt = gb300::update_neighbors(s, view); });
+    *trigger_move_particles = rebuilt;
+  }
+};
+
+// The device state back into the grid (whole-step runs): r, v, the
+// accelerations into the f fields, and, on thermo steps, ep and the virial.
+// Bound before the operators that read the grid (thermodynamic state, dumps).
+template <class GridT>
+class Gb300SyncGridNode : public OperatorNode {
+  ADD_SLOT(GridT, grid, INPUT_OUTPUT);
+  ADD_SLOT(ParticleSpecies, species, INPUT, REQUIRED);
+  ADD_SLOT(bool, trigger_thermo_state, INPUT, OPTIONAL);
+  ADD_SLOT(bool, compute_virial, INPUT, false);
+  GB300_SESSION_SLOT;
+
+ public:
+  inline void execute() override final {
+    if (!*gb300_session || grid->number_of_cells() == 0) return;
+    const bool energy = trigger_thermo_state.has_value() && *trigger_thermo_state;
+    gb300_ops::GridView<GridT> view(*grid, *species);
+    gb300_ops::guarded("gb300_sync_grid",
+                       [&] { gb300::sync_grid(**gb300_session, view, energy, energy && *compute_virial); });
   }
 };
 
 template <class GridT>
 using Gb300ForceNodeTmpl = Gb300ForceNode<GridT>;
-
 template <class GridT>
 using Gb300LJForceTmpl = Gb300LJForceNode<GridT>;
 template <class GridT>
@@ -464,6 +567,14 @@ template <class GridT>
 using Gb300EamAlloyForceTmpl = Gb300EamAlloyForceNode<GridT>;
 template <class GridT>
 using Gb300JohnsonForceTmpl = Gb300JohnsonForceNode<GridT>;
+template <class GridT>
+using Gb300PushFVRTmpl = Gb300PushNode<GridT, true>;
+template <class GridT>
+using Gb300PushFVTmpl = Gb300PushNode<GridT, false>;
+template <class GridT>
+using Gb300NeighborsTmpl = Gb300NeighborsNode<GridT>;
+template <class GridT>
+using Gb300SyncGridTmpl = Gb300SyncGridNode<GridT>;
 
 ONIKA_AUTORUN_INIT(gb300_md_ops) {
   OperatorNodeFactory::instance()->register_factory("gb300_force", make_grid_variant_operator<Gb300ForceNodeTmpl>);
@@ -476,6 +587,10 @@ ONIKA_AUTORUN_INIT(gb300_md_ops) {
                                                     make_grid_variant_operator<Gb300EamAlloyForceTmpl>);
   OperatorNodeFactory::instance()->register_factory("gb300_johnson_force",
                                                     make_grid_variant_operator<Gb300JohnsonForceTmpl>);
+  OperatorNodeFactory::instance()->register_factory("gb300_push_f_v_r", make_grid_variant_operator<Gb300PushFVRTmpl>);
+  OperatorNodeFactory::instance()->register_factory("gb300_push_f_v", make_grid_variant_operator<Gb300PushFVTmpl>);
+  OperatorNodeFactory::instance()->register_factory("gb300_neighbors", make_grid_variant_operator<Gb300NeighborsTmpl>);
+  OperatorNodeFactory::instance()->register_factory("gb300_sync_grid", make_grid_variant_operator<Gb300SyncGridTmpl>);
 }
 
 }  // namespace exaStamp

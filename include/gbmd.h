@@ -197,6 +197,14 @@ int gbmd_get_newton3(const gbmd_context* ctx, int* enabled);
  * contraction. */
 int gbmd_set_skin(gbmd_context* ctx, double skin);
 int gbmd_build_neighbors(gbmd_context* ctx);
+/* check_and_update_particles (data/config/config_move_particles.msp L116-152:
+ * trigger_move_particles = particle_displ_over, L19-22, then the full update
+ * when it fires): the skin/2 displacement test of the current positions
+ * against those of the last rebuild, on the device, and a rebuild (wrap,
+ * rebin, list, regrown on overflow) when some atom moved farther; builds the
+ * list when there is none.  rebuilt (may be NULL) receives 1 when it did.
+ * Synchronises the stream (the test's outcome is read back). */
+int gbmd_update_neighbors(gbmd_context* ctx, int* rebuilt);
 /* Export the list as (id_i, id_j, n_x, n_y, n_z) rows, rows of one atom in
  * list order, atoms in cell-sorted order. count receives the number of rows
  * (call with cap 0 to size). */
