@@ -696,6 +696,8 @@ def measure(args, w, ws, dev, stream, torch, *, steps, fp64_steps, e2e_steps, dr
     # ---- FP64 comparison ----------------------------------------------------
     if single and not args.no_fp64:
         st = ctx.download(KEYS9)
+        ctx.set_precision(args.precision == "mixed")
+        ctx.compute_forces(energy=False)
         d_mixed = ctx.download(("ax", "ay", "az"))
         ctx.set_precision(False)
         ctx.compute_forces(energy=False)

@@ -1301,9 +1301,13 @@ int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int 
   // writes them (the force pass's fused first half, k_first_half), so the
   // decision is ready when the next step starts and no separate test kernel
   // runs; the gate starts cleared
+  // gbmd_run_nve_host may have applied step 1's first half (and any rebuild
+  // it called for) while reading the state in
+  const bool pushed = c->first_half_done;
+  c->first_half_done = false;
   if (trigger) GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_GATE, 0, sizeof(int), c->stream));
   const FusedTriggerScope fused(c, trigger);
-  launch_first_half(c, dt);
+  if (!pushed) launch_first_half(c, dt);
   // graph chunk length: two rebuild intervals, or with the trigger the thermo
   // interval when it is even (20 steps without thermo)
   const int G = trigger ? (want_thermo ? thermo_every : 20) : 2 * R;
@@ -1341,14 +1345,43 @@ int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int 
 int gbmd_run_nve_host(gbmd_context* c, int nsteps, double dt, int rebuild_every, double* rx, double* ry, double* rz,
                       double* vx, double* vy, double* vz, double* ax, double* ay, double* az) {
   if (!c || nsteps < 1 || !rx || !ry || !rz || !vx || !vy || !vz || !ax || !ay || !az) return GBMD_ERR_INVALID;
-  int rc = gbmd_upload_state(c, rx, ry, rz, vx, vy, vz, ax, ay, az);
-  if (rc) return rc;
+  if (c->pot == GBMD_POT_NONE) return set_error(c, GBMD_ERR_INVALID, "no potential set");
+  cudaSetDevice(c->device);
+  int rc;
+  const double* host[9] = {rx, ry, rz, vx, vy, vz, ax, ay, az};
+  Arrays9 hd{};
+  if (c->n > 0 && c->list_valid && c->grid_valid && device_accessible(host, 9, hd)) {
+    // page-locked arrays with a list in place: the state is read in with
+    // step 1's first half applied (no separate push kernel) and the skin/2
+    // test of the pushed positions -- check_and_update_particles after
+    // verlet_first_half -- decides a rebuild, which can regrow the list; the
+    // given accelerations are the forces of the given positions
+    GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_GATE, 0, sizeof(int), c->stream));
+    const double* hdev[9];
+    for (int k = 0; k < 9; ++k) hdev[k] = hd.a[k];
+    {
+      const FusedTriggerScope gate(c, true);
+      launch_host_first_half(c, hdev, inverse_user(c), dt);
+    }
+    if ((rc = sync_error_word(c))) return rc;
+    if (c->h_err[ERRW_GATE]) {
+      GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_GATE, 0, sizeof(int), c->stream));
+      if ((rc = do_rebuild(c, true))) return rc;
+    }
+    c->forces_valid_step = c->step;
+    c->rho_valid_step = -1;
+    c->first_half_done = true;
+  } else {
+    rc = gbmd_upload_state(c, rx, ry, rz, vx, vy, vz, ax, ay, az);
+    if (rc) return rc;
+  }
   if (c->n == 0) return GBMD_OK;
   c->host_r_out[0] = rx;
   c->host_r_out[1] = ry;
   c->host_r_out[2] = rz;
   c->r_copy_pending = false;
   rc = gbmd_run_nve(c, nsteps, dt, rebuild_every, 0, nullptr, 0);
+  c->first_half_done = false;
   c->host_r_out[0] = c->host_r_out[1] = c->host_r_out[2] = nullptr;
   if (rc == GBMD_OK) rc = gbmd_download(c, nullptr, nullptr, nullptr, vx, vy, vz, ax, ay, az, nullptr, nullptr);
   if (c->r_copy_pending) {

@@ -162,6 +162,49 @@ void launch_first_half_swap(gbmd_context* c, double dt) {
   c->cur = o;
 }
 
+// gbmd_run_nve_host's upload fused with verlet_first_half: the caller's
+// page-locked r, v, a (caller order, read over the host link by consecutive
+// threads) are pushed by the first half -- the formulas of k_first_half --
+// and written into the cell-sorted state in place (r', v', and a as given),
+// with the gather copies refreshed and the skin/2 displacement test taken on
+// r', as check_and_update_particles does after verlet_first_half.
+struct HostState9 {
+  const double* a[9];
+};
+
+__global__ void k_host_first_half(PushArgs P, HostState9 H, const int32_t* __restrict__ inv, double h, double h2,
+                                  double hv) {
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (u >= P.n) return;
+  double q[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) q[k] = H.a[k][u];
+  const int64_t i = inv[u];
+  const double x = __dadd_rn(q[0], __dadd_rn(__dmul_rn(q[3], h), __dmul_rn(q[6], h2)));
+  const double y = __dadd_rn(q[1], __dadd_rn(__dmul_rn(q[4], h), __dmul_rn(q[7], h2)));
+  const double z = __dadd_rn(q[2], __dadd_rn(__dmul_rn(q[5], h), __dmul_rn(q[8], h2)));
+  P.xo[i] = x;
+  P.yo[i] = y;
+  P.zo[i] = z;
+  P.vx[i] = __dadd_rn(q[3], __dmul_rn(q[6], hv));
+  P.vy[i] = __dadd_rn(q[4], __dmul_rn(q[7], hv));
+  P.vz[i] = __dadd_rn(q[5], __dmul_rn(q[8], hv));
+  P.ax[i] = q[6];
+  P.ay[i] = q[7];
+  P.az[i] = q[8];
+  if (P.refresh) refresh_gather(P.g, i, P.cellpack[i], P.type[i], x, y, z, P.pf, P.pd);
+  if (P.gate) displacement_test(P.gate, P.rref, P.rcap, P.thr2, i, x, y, z);
+}
+
+void launch_host_first_half(gbmd_context* c, const double* const host[9], const int32_t* inv, double dt) {
+  if (!c->n) return;
+  HostState9 H;
+  for (int k = 0; k < 9; ++k) H.a[k] = host[k];
+  const double h = dt * 1.0;
+  const double h2 = h * h * 0.5;
+  k_host_first_half<<<nblk(c->n, 256), 256, 0, c->stream>>>(push_args(c), H, inv, h, h2, dt * 0.5);
+}
+
 void launch_push_min(gbmd_context* c, double dt, double dt_scale, double tolF) {
   if (!c->n) return;
   const double h = dt * dt_scale;

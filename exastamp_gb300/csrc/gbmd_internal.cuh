@@ -181,6 +181,7 @@ struct gbmd_context {
   int vec = 4;                  // list entries per lane per load (1 or 4, mixed kernels; autotuned)
   bool staged = false;          // 1 lane x 4 entries: neighbour positions from shared memory
   bool fused_trigger = false;   // run_nve with the displacement trigger: kernels that move atoms test them
+  bool first_half_done = false; // gbmd_run_nve_host pushed the first half while reading the state in
   bool newton3 = false;         // half list (j > i in cell order) + scattered reaction forces (LJ, mixed)
   float4* h3acc = nullptr;      // Newton-3 accumulators, 3 float4 per atom: (f, ep), virial xx yy zz xy, xz yz
   int block = 256;              // threads per block of the pair / force kernels (autotuned)
@@ -268,6 +269,9 @@ void launch_push_f_v(gbmd_context* c, double dt, double dt_scale);
 void launch_push_min(gbmd_context* c, double dt, double dt_scale, double tolF);
 void launch_first_half(gbmd_context* c, double dt);
 void launch_first_half_swap(gbmd_context* c, double dt);
+// host: device addresses of page-locked caller arrays r, v, a (caller order);
+// inv: caller index -> cell-sorted index
+void launch_host_first_half(gbmd_context* c, const double* const host[9], const int32_t* inv, double dt);
 void launch_thermo(gbmd_context* c, bool with_virial);
 void launch_thermo_raw(int64_t n, const double* vx, const double* vy, const double* vz, const double* ep,
                        const double* vir, const uint8_t* type, const double* mass, int ntypes, double* part,

@@ -55,6 +55,38 @@ __device__ __forceinline__ GeomF geom_f(uint32_t ent, const float4& pj, const fl
   return r;
 }
 
+// Two list entries at once in packed FP32 (sm_100 float2 arithmetic: one
+// instruction per pair of lanes' worth of FADD / FMUL / FFMA).  Each half is
+// geom_f of its entry, operation for operation: (p_j - p_i) is p_j + (-p_i),
+// which rounds identically.  npi = (-p_i) in both halves of each axis.
+struct GeomF2 {
+  float2 dx, dy, dz, d2;
+};
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+__device__ __forceinline__ GeomF2 geom_f2(uint32_t ea, uint32_t eb, const float4& pa, const float4& pb,
+                                          const float2& npx, const float2& npy, const float2& npz, const float2& hx,
+                                          const float2& hy, const float2& hz) {
+  GeomF2 r;
+  r.dx = __ffma2_rn(f2(unit_of((ea >> 26) & 3u), unit_of((eb >> 26) & 3u)), hx, __fadd2_rn(f2(pa.x, pb.x), npx));
+  r.dy = __ffma2_rn(f2(unit_of((ea >> 28) & 3u), unit_of((eb >> 28) & 3u)), hy, __fadd2_rn(f2(pa.y, pb.y), npy));
+  r.dz = __ffma2_rn(f2(unit_of(ea >> 30), unit_of(eb >> 30)), hz, __fadd2_rn(f2(pa.z, pb.z), npz));
+  r.d2 = __ffma2_rn(r.dx, r.dx, __ffma2_rn(r.dy, r.dy, __fmul2_rn(r.dz, r.dz)));
+  return r;
+}
+
+// The per-atom constants of geom_f2: -p_i and the cell edges, packed.
+struct PairFrame {
+  float2 npx, npy, npz, hx, hy, hz;
+  __device__ __forceinline__ PairFrame(const float4& pi, const Grid& g)
+      : npx(f2(-pi.x, -pi.x)), npy(f2(-pi.y, -pi.y)), npz(f2(-pi.z, -pi.z)), hx(f2(g.hf[0], g.hf[0])),
+        hy(f2(g.hf[1], g.hf[1])), hz(f2(g.hf[2], g.hf[2])) {}
+  __device__ __forceinline__ GeomF2 geom(uint32_t ea, uint32_t eb, const float4& pa, const float4& pb) const {
+    return geom_f2(ea, eb, pa, pb, npx, npy, npz, hx, hy, hz);
+  }
+};
+
 __device__ __forceinline__ void reduce6(float* v, int T) {
   for (int off = T / 2; off > 0; off >>= 1)
 #pragma unroll
@@ -363,6 +395,7 @@ __device__ __forceinline__ void eam_rho_atom(const PairArgs& A, const EamDev& E,
   const int nr = E.nr, nr1 = E.nr + 1;
   const float rdr = E.rdrf;
   float rho = 0.f, crho = 0.f;
+  const PairFrame PF(pi, A.g);
   const ListRows<T, V> L(A.nbr, i, lane, A.stride, nn);
   uint32_t ent[V], nxt[V];
   if (L.nrow > 0) L.load(0, ent);
@@ -375,18 +408,45 @@ __device__ __forceinline__ void eam_rho_atom(const PairArgs& A, const EamDev& E,
       pj[q] = fetch(ent[q], ent[q] & GBMD_IDX_MASK);
     }
     float rr = 0.f;
+    if constexpr (V == 4) {
+      // entries (0, 1) and (2, 3) in packed FP32; the rows' partial sums
+      // stay packed until the row is added to the compensated sum
+      float2 rr2 = f2(0.f, 0.f);
 #pragma unroll
-    for (int q = 0; q < V; ++q) {
-      const uint32_t j = ent[q] & GBMD_IDX_MASK;
-      const GeomF G = geom_f(ent[q], pj[q], pi, A.g);
-      bool in = G.d2 < E.rc2lo;
-      if (!in && G.d2 <= E.rc2hi && L.valid(r, q))
-        in = exact_inside(A.posd, i, j, ent[q] >> GBMD_IDX_BITS, cp, A.g, E.rcut2, 0.0);
-      const float rd = G.d2 * rsqrtf(G.d2);
-      float t;
-      const int m = knot_f(rd, rdr, nr, t);
-      const float4 c = __ldg(&E.rhor4[SINGLE ? m : __float_as_int(pj[q].w) * nr1 + m]);
-      rr += in ? spline_val(c, t) : 0.f;
+      for (int q = 0; q < V; q += 2) {
+        const GeomF2 G = PF.geom(ent[q], ent[q + 1], pj[q], pj[q + 1]);
+        bool ina = G.d2.x < E.rc2lo, inb = G.d2.y < E.rc2lo;
+        if (!ina && G.d2.x <= E.rc2hi && L.valid(r, q))
+          ina = exact_inside(A.posd, i, ent[q] & GBMD_IDX_MASK, ent[q] >> GBMD_IDX_BITS, cp, A.g, E.rcut2, 0.0);
+        if (!inb && G.d2.y <= E.rc2hi && L.valid(r, q + 1))
+          inb = exact_inside(A.posd, i, ent[q + 1] & GBMD_IDX_MASK, ent[q + 1] >> GBMD_IDX_BITS, cp, A.g, E.rcut2,
+                             0.0);
+        const float2 rd = __fmul2_rn(G.d2, f2(rsqrtf(G.d2.x), rsqrtf(G.d2.y)));
+        const float2 tt = __ffma2_rn(rd, f2(rdr, rdr), f2(1.0f, 1.0f));
+        const int ma = min((int)tt.x, nr - 1), mb = min((int)tt.y, nr - 1);
+        const float2 qq0 = __fadd2_rn(tt, f2(-(float)ma, -(float)mb));
+        const float2 qq = f2(fminf(qq0.x, 1.0f), fminf(qq0.y, 1.0f));
+        const float4 ca = __ldg(&E.rhor4[SINGLE ? ma : __float_as_int(pj[q].w) * nr1 + ma]);
+        const float4 cb = __ldg(&E.rhor4[SINGLE ? mb : __float_as_int(pj[q + 1].w) * nr1 + mb]);
+        const float2 val = __ffma2_rn(__ffma2_rn(__ffma2_rn(f2(ca.x, cb.x), qq, f2(ca.y, cb.y)), qq, f2(ca.z, cb.z)),
+                                      qq, f2(ca.w, cb.w));
+        rr2 = __fadd2_rn(rr2, f2(ina ? val.x : 0.f, inb ? val.y : 0.f));
+      }
+      rr = rr2.x + rr2.y;
+    } else {
+#pragma unroll
+      for (int q = 0; q < V; ++q) {
+        const uint32_t j = ent[q] & GBMD_IDX_MASK;
+        const GeomF G = geom_f(ent[q], pj[q], pi, A.g);
+        bool in = G.d2 < E.rc2lo;
+        if (!in && G.d2 <= E.rc2hi && L.valid(r, q))
+          in = exact_inside(A.posd, i, j, ent[q] >> GBMD_IDX_BITS, cp, A.g, E.rcut2, 0.0);
+        const float rd = G.d2 * rsqrtf(G.d2);
+        float t;
+        const int m = knot_f(rd, rdr, nr, t);
+        const float4 c = __ldg(&E.rhor4[SINGLE ? m : __float_as_int(pj[q].w) * nr1 + m]);
+        rr += in ? spline_val(c, t) : 0.f;
+      }
     }
     kahan_add(rho, crho, rr);
 #pragma unroll

@@ -425,22 +425,12 @@ __device__ __noinline__ int build_retest_row(uint32_t* row, int nkeep, int wsh, 
   return nkeep - wpos;
 }
 
-// The walk for home groups of G atoms, two phases per staged chunk of up to
-// 64 candidates.  Test phase: each lane holds a home atom (G = 32; it tests
-// every candidate of the chunk), or lanes l and l+16 hold the same home atom
-// and test the even and the odd candidates (G = 16, two candidates per
-// step).  A test is a shared-memory broadcast, the FP32 d2 of the walk and a
-// predicated bit-set in the lane's hit mask; the chunk's unused slots hold
-// far-away sentinels, so the steps run in unguarded blocks of eight.  Emit
-// phase: each lane writes its hits, in candidate order (the canonical
-// order: stencil code, then cell order), straight to its atom's list row;
-// with G = 16 the two lanes of an atom interleave, each adding the partner's
-// hits before its own candidate (one popcount).  Candidates with FP32
-// d2 <= R^2 (1 + 2^-12) are kept; an atom with one above R^2 (1 - 2^-12) is
-// flagged, and after the walk rescans its row, re-tests those entries in
-// FP64 and compacts (build_retest_row).  HALF keeps only candidates after
-// the home atom in cell order (k > i): each unordered pair once, for the
-// Newton-3 force kernels.
+// The walk for home groups of G atoms: G = 32, one home atom per lane and one
+// candidate per step; G = 16, lanes l and l+16 hold the same home atom and a
+// step tests candidates 2t (low half) and 2t+1 (high half), the two lanes
+// exchanging their hit with one shuffle so both append in candidate order.
+// HALF keeps only candidates after the home atom in cell order (k > i): each
+// unordered pair once, for the Newton-3 force kernels.
 template <int G, bool HALF>
 __device__ __forceinline__ int build_walk(const BuildCell& B, const float4* __restrict__ pf,
                                           const double* __restrict__ x, const double* __restrict__ y,
@@ -459,8 +449,7 @@ __device__ __forceinline__ int build_walk(const BuildCell& B, const float4* __re
   for (int h0 = 0; h0 < B.nh; h0 += G) {
     const bool hv = h0 + hl < B.nh;
     const int i = B.hb + h0 + hl;
-    // an idle lane sits at -FAR: nothing, sentinels included, is in reach
-    float4 pi = make_float4(-FAR, -FAR, -FAR, 0.f);
+    float4 pi = make_float4(FAR, FAR, FAR, 0.f);
     if (hv) pi = pf[i];
     // bounding box of the group's home atoms (cell frame)
     float3 blo = make_float3(hv ? pi.x : FAR, hv ? pi.y : FAR, hv ? pi.z : FAR);
@@ -474,69 +463,40 @@ __device__ __forceinline__ int build_walk(const BuildCell& B, const float4* __re
       bhi.y = fmaxf(bhi.y, __shfl_xor_sync(FULL, bhi.y, o));
       bhi.z = fmaxf(bhi.z, __shfl_xor_sync(FULL, bhi.z, o));
     }
-    // the home atom itself, seen from its own cell (stencil code 21 = (0,0,0))
-    const uint32_t self_w = (uint32_t)i | (21u << GBMD_IDX_BITS);
     uint32_t* row = nbr + (size_t)i * W;  // slot k at row[(k >> wsh) * stride + (k & (W - 1))]
     int cnt = 0;
     bool unc = false;
     for (int q0 = 0; q0 < B.total; q0 += BUILD_CHUNK) {
       __syncwarp();
       const int m = build_stage(B, pf, q0, stage, lane, blo, bhi, R2keep);
-      // sentinels in every slot the unguarded steps may read
-      for (int p = m + 1 + lane; p < BUILD_CHUNK; p += 32)
-        stage[p] = make_float4(FAR, FAR, FAR, __uint_as_float(0xffffffffu));
       __syncwarp();
-      // ---- test phase: hit masks --------------------------------------------
-      uint32_t mlo = 0, mhi = 0;
-      const int steps = G == 16 ? (m + 1) >> 1 : m;
-      for (int t0 = 0; t0 < steps; t0 += 8) {
-        uint32_t b8 = 0;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-          const float4 e = stage[G == 16 ? 2 * (t0 + c) + half : t0 + c];
-          const uint32_t w = __float_as_uint(e.w);
-          const float dx = __fsub_rn(e.x, pi.x);
-          const float dy = __fsub_rn(e.y, pi.y);
-          const float dz = __fsub_rn(e.z, pi.z);
-          const float d2f = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
-          const bool in = d2f <= R2hi && (HALF ? (int)(w & GBMD_IDX_MASK) > i : w != self_w);
-          unc |= in && d2f >= R2lo;
-          if (in) b8 |= 1u << c;
+#pragma unroll 8
+      for (int t = 0; t < m; t += (G == 16 ? 2 : 1)) {
+        const float4 e = stage[t + half];
+        const uint32_t w = __float_as_uint(e.w);
+        const float dx = __fsub_rn(e.x, pi.x);
+        const float dy = __fsub_rn(e.y, pi.y);
+        const float dz = __fsub_rn(e.z, pi.z);
+        const float d2f = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
+        // an atom never pairs with itself: its images sit at least one box
+        // edge >= R away, so k == i only ever matters in the home cell.
+        // Keep d2 <= R^2 (1 + 2^-12); flag the atom when d2 >= R^2 (1 - 2^-12).
+        const int k = (int)(w & GBMD_IDX_MASK);
+        const bool in = hv && (HALF ? k > i : k != i) && d2f <= R2hi;
+        unc |= in && d2f >= R2lo;
+        // the slot address is formed on every step and only the store is
+        // conditional, so the walk stays one straight-line block
+        if (G == 16) {
+          const int other = __shfl_xor_sync(FULL, (int)in, 16);
+          const int pos = cnt + (half & other);  // candidate 2t goes first
+          uint32_t* dst = row + (size_t)(pos >> wsh) * stride + (pos & (W - 1));
+          if (in && pos < maxnb) *dst = w;
+          cnt += (int)in + other;
+        } else {
+          uint32_t* dst = row + (size_t)(cnt >> wsh) * stride + (cnt & (W - 1));
+          if (in && cnt < maxnb) *dst = w;
+          cnt += (int)in;
         }
-        if (G == 16 || t0 < 32) mlo |= b8 << t0;
-        else mhi |= b8 << (t0 - 32);
-      }
-      // ---- emit phase: hits in candidate order --------------------------------
-      if (G == 16) {
-        const uint32_t partner = __shfl_xor_sync(FULL, mlo, 16);
-        uint32_t mk = hv ? mlo : 0u;
-        int k = 0;
-        while (mk) {
-          const int t = __ffs(mk) - 1;
-          mk &= mk - 1u;
-          // partner hits before candidate 2t + half: its candidates 2t' + 1 - half
-          const uint32_t before = half ? (0xffffffffu >> (31 - t)) : ((1u << t) - 1u);
-          const int pos = cnt + k + __popc(partner & before);
-          const uint32_t w = __float_as_uint(stage[2 * t + half].w);
-          if (pos < maxnb) row[(size_t)(pos >> wsh) * stride + (pos & (W - 1))] = w;
-          ++k;
-        }
-        cnt += __popc(mlo) + __popc(partner);
-      } else {
-        int k = 0;
-#pragma unroll
-        for (int hh = 0; hh < 2; ++hh) {
-          uint32_t mk = hv ? (hh ? mhi : mlo) : 0u;
-          while (mk) {
-            const int t = __ffs(mk) - 1;
-            mk &= mk - 1u;
-            const int pos = cnt + k;
-            const uint32_t w = __float_as_uint(stage[32 * hh + t].w);
-            if (pos < maxnb) row[(size_t)(pos >> wsh) * stride + (pos & (W - 1))] = w;
-            ++k;
-          }
-        }
-        cnt += __popc(mlo) + __popc(mhi);
       }
     }
     if (G == 16) {
@@ -544,11 +504,10 @@ __device__ __forceinline__ int build_walk(const BuildCell& B, const float4* __re
       const int partner_unc = __shfl_xor_sync(FULL, (int)unc, 16);
       unc = unc || partner_unc != 0;
       __syncwarp();  // the high-half lanes' entries are visible to the low half
-      if (hv && half == 0 && unc)
-        cnt -= build_retest_row(row, min(cnt, maxnb), wsh, W, stride, pf, pi, x, y, z, i, B.cx, B.cy, B.cz, g,
-                                R2, R2lo);
+      if (half == 0 && unc) cnt -= build_retest_row(row, min(cnt, maxnb), wsh, W, stride, pf, pi, x, y, z, i,
+                                                    B.cx, B.cy, B.cz, g, R2, R2lo);
       cnt = __shfl_sync(FULL, cnt, hl);  // the high-half lane takes the corrected count
-    } else if (hv && unc) {
+    } else if (unc) {
       cnt -= build_retest_row(row, min(cnt, maxnb), wsh, W, stride, pf, pi, x, y, z, i, B.cx, B.cy, B.cz, g,
                               R2, R2lo);
     }

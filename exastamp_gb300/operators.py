@@ -317,6 +317,17 @@ class chunk_neighbors(Operator):
         sim.ctx.build_neighbors()
 
 
+class check_and_update_particles(Operator):
+    """check_and_update_particles (data/config/config_move_particles.msp
+    L116-152): trigger_move_particles (particle_displ_over, skin/2) and the
+    full update -- wrap, rebin, neighbour list -- when it fires.  Returns the
+    trigger's value, as the reference publishes it in trigger_move_particles."""
+    name = "check_and_update_particles"
+
+    def execute(self, sim: Simulation) -> bool:
+        return sim.ctx.update_neighbors()
+
+
 class push_f_v_r(Operator):
     name = "push_f_v_r"
 

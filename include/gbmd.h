@@ -245,11 +245,15 @@ int gbmd_push_min(gbmd_context* ctx, double dt, double dt_scale, double tolF);
 int gbmd_run_nve(gbmd_context* ctx, int nsteps, double dt, int rebuild_every, int thermo_every,
                  double* thermo_out, int use_graph);
 /* verlet_nve on a state held in host arrays (the caller's grid, in upload
- * order): gbmd_upload_state(r, v, a) (the skin/2 displacement test decides
- * a rebuild), gbmd_run_nve(nsteps, no thermo, no graph), then r, v, a are
- * written back.  The positions of the last step are final after its first
- * half and go back to the host while its force pass runs; v and a follow.
- * Page-locked arrays are fastest.  Returns once every array is written. */
+ * order): the state goes in (the given accelerations are the forces of the
+ * given positions), nsteps of verlet_nve run (no thermo, no graph), then r,
+ * v, a are written back.  Page-locked arrays with a list in place are read
+ * by one kernel over the host link that also applies step 1's first half,
+ * after which the skin/2 displacement test of the pushed positions decides
+ * a rebuild (check_and_update_particles after verlet_first_half); other
+ * arrays go through gbmd_upload_state.  The positions of the last step are
+ * final after its first half and go back to the host while its force pass
+ * runs; v and a follow.  Returns once every array is written. */
 int gbmd_run_nve_host(gbmd_context* ctx, int nsteps, double dt, int rebuild_every, double* rx, double* ry,
                       double* rz, double* vx, double* vy, double* vz, double* ax, double* ay, double* az);
 /* Minimiser: nsteps of compute forces + push_min (r += a dt^2/2, clipped);

@@ -98,3 +98,43 @@ def test_fixed_interval_build_count(gpu, use_graph):
         b0 = ctx.list_builds()
         ctx.run_nve(101, 0.005, rebuild_every=10, thermo_every=20, use_graph=use_graph)
         assert ctx.list_builds() - b0 == 10
+
+
+def test_operator_graph_with_check_and_update_particles(gpu, oracle):
+    """The verlet_nve operator sequence (config_numerical_schemes.msp L44-52)
+    through the operator mirror -- push_f_v_r, push_f_v,
+    check_and_update_particles (gbmd_update_neighbors), forces, push_f_v --
+    against the oracle's verlet_nve with the displacement trigger: same final
+    state within 1e-10 and the same number of list builds."""
+    from exastamp_gb300 import operators as OP
+    s = S.lj_fcc(ncell=6, T=1.0, seed=41)
+    st = s.state()
+    nsteps, dt = 60, 0.005
+    oracle.run_nve(st, s.masses, s.lo, s.hi, oracle.POT_LJ, oracle.LJParams(1.0, 1.0, 2.5), 0.3, dt, nsteps, -1,
+                   thermo=False)
+    orc_builds = oracle.last_list_builds()
+    sim = OP.Simulation(s)
+    force = OP.lj_compute_force(rcut=2.5, parameters={"epsilon": 1.0, "sigma": 1.0})
+    force.bind(sim)
+    OP.chunk_neighbors().bind(sim, 0.3)
+    sim.set_precision(False)
+    check = OP.check_and_update_particles()
+    p1, p2 = OP.push_f_v_r(dt_scale=1.0), OP.push_f_v(dt_scale=0.5)
+    b0 = sim.ctx.list_builds()
+    force.execute(sim, energy=False)
+    fired = 0
+    for _ in range(nsteps):
+        p1.execute(sim, dt)
+        p2.execute(sim, dt)
+        fired += int(check.execute(sim))
+        force.execute(sim, energy=False)
+        p2.execute(sim, dt)
+    d = sim.ctx.download(("x", "y", "z", "vx", "vy", "vz"))
+    assert sim.ctx.list_builds() - b0 == orc_builds
+    assert fired == orc_builds - 1 and fired > 0
+    for k in ("vx", "vy", "vz"):
+        assert np.abs(d[k] - st[k]).max() < 1e-10
+    for k, dd in (("x", 0), ("y", 1), ("z", 2)):
+        diff = d[k] - st[k]
+        diff -= np.round(diff / s.L[dd]) * s.L[dd]
+        assert np.abs(diff).max() < 1e-10
