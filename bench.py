@@ -682,11 +682,18 @@ def measure(args, w, ws, dev, stream, torch, *, steps, fp64_steps, e2e_steps, dr
         traffic = LJ_MULTI_PAIR_DRAM_BYTES_PER_ATOM * s.n
         traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_lj_mixed<1,4,multi> on the "
                        "864,000-atom mixture (474.0 + 51.9 MB), scaled to %d atoms" % s.n)
+    # the resource that binds the pair kernels (ncu on the 864,000-atom cases)
+    binding = ({"resource": "L1/tex LSU data-pipe wavefronts (neighbour and spline-knot gathers)", "frac": 0.796,
+                "source": "ncu l1tex__data_pipe_lsu_wavefronts.avg.pct_of_peak_sustained_elapsed of "
+                          "k_eam_force_mixed<1,4> (density kernel: 0.858)"}
+               if w["kind"] == "eam" else
+               {"resource": "issue slots + L1/tex (neighbour gathers)", "frac": 0.78,
+                "source": "ncu smsp__issue_active of k_lj_mixed<1,4,multi> (L1/tex throughput 0.75)"})
     out["roofline"] = {"kernel": "k_eam_force (mixed, fused Verlet halves)" if w["kind"] == "eam" else "k_lj",
                        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                        "frac": achieved / peak, "peak_source": peak_kind,
                        "algorithmic_bytes_per_launch": alg_bytes, "bytes_per_atom": per_atom,
-                       "traffic": traffic, "traffic_source": traffic_src, "kernel_ms": prof}
+                       "traffic": traffic, "traffic_source": traffic_src, "binding": binding, "kernel_ms": prof}
 
     single = ws == 1
     # ---- accuracy against the FP64 oracle at the benchmarked state ----------
