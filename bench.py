@@ -32,6 +32,7 @@ Multi-GPU (torchrun): independent replicas, one per rank, weak scaling.
 from __future__ import annotations
 
 import argparse
+import atexit
 import json
 import os
 import statistics
@@ -102,6 +103,8 @@ def parse():
                    help="override the unit cells per edge (small profiling cases of the same workload)")
     p.add_argument("--no-mixture", action="store_true",
                    help="skip the 16.7 M-atom LJ mixture section of the default run")
+    p.add_argument("--no-lj-crystal", action="store_true",
+                   help="skip the 32,000-atom LJ crystal section of the default run")
     p.add_argument("--no-drift", action="store_true",
                    help="skip the 1,000-step mixed / 200-step FP64 NVE drift section")
     p.add_argument("--no-oracle-check", action="store_true",
@@ -155,12 +158,14 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            # the sampler never outlives the bench, also when it fails
+            atexit.register(self.__exit__)
         except Exception:
             self.proc = None
         return self
 
     def __exit__(self, *a):
-        if self.proc:
+        if self.proc and self.proc.poll() is None:
             self.proc.terminate()
             try:
                 self.proc.wait(5)
@@ -428,6 +433,12 @@ def oracle_force_check(ctx, s, w, sample):
         sel = np.arange(s.n)
         F = np.stack([fx, fy, fz], 1) / s.masses[s.type][:, None]
         how = "all %d atoms" % s.n
+    elif w["kind"] == "lj":
+        nl = O.build_neighbors(x, y, z, s.id, s.lo, s.hi, w["rcut"] + w["skin"])
+        fx, fy, fz, _, _ = O.lj_force(x, y, z, nl, s.L, 1.0, 1.0, w["rcut"], virial=False)
+        sel = np.arange(s.n)
+        F = np.stack([fx, fy, fz], 1) / s.masses[s.type][:, None]
+        how = "all %d atoms" % s.n
     else:
         from exastamp_gb300 import systems as S
         perm = np.random.default_rng(7).permutation(s.n)
@@ -550,6 +561,10 @@ def measure(args, w, ws, dev, stream, torch, *, steps, fp64_steps, e2e_steps, dr
     bind_potential(ctx, w)
     t_min = None
     tuned = None
+    # clocks are sampled every 200 ms from here (thermalisation or minimiser,
+    # tuning, warm-up: the GPU under the same kernels) to the end of the
+    # timed region, which alone is too short for more than a sample or two
+    clk = ClockSampler(dev).__enter__()
     if w.get("min_steps"):
         # random positions overlap: the first steps of the clipped minimiser
         # in FP64 (separations far below sigma), the rest in mixed precision
@@ -582,14 +597,18 @@ def measure(args, w, ws, dev, stream, torch, *, steps, fp64_steps, e2e_steps, dr
     # displacement trigger (R = -1) every 20 steps
     thermo_every = 2 * R if R > 0 else (20 if R < 0 else 0)
     # warm-up: at least W steps, and one graph chunk plus a step so that the
-    # CUDA graph is captured here rather than inside the timed region
+    # CUDA graph is captured here rather than inside the timed region; a whole
+    # number of thermo intervals, so the timed run starts from a state whose
+    # energies are current (its step-0 thermo row needs only the reduction)
     warm = max(args.warmup, 3, thermo_every + 1)
+    if thermo_every:
+        warm = -(-warm // thermo_every) * thermo_every
     ctx.run_nve(warm, dt, R, thermo_every, use_graph=True)
     npairs, maxnb, nc = ctx.neighbor_stats()
 
     # ---- timed region: K steps, device resident --------------------------
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(dev) as clk:
+    try:
         barrier(ws)
         torch.cuda.synchronize()
         builds0 = ctx.list_builds()
@@ -599,14 +618,17 @@ def measure(args, w, ws, dev, stream, torch, *, steps, fp64_steps, e2e_steps, dr
         torch.cuda.synchronize()
         barrier(ws)
         rebuilds = ctx.list_builds() - builds0
+    finally:
+        clk.__exit__()
     ms = ev0.elapsed_time(ev1)
     ms = dist_max(ms, ws)
     clocks = clk.summary()
+    clocks["window"] = "sampled every 200 ms from the thermalisation/minimiser through the timed region"
     value = s.n * steps * ws / (ms * 1e-3)
     # EAM: density + force; Newton-3 LJ: half-list pair pass + epilogue
     kernels_per_step = 2 if w["kind"] == "eam" or args.newton3 else 1
     # Launches of the timed gbmd_run_nve call: the pair kernel(s) once per
-    # step and once more for the energies of step 0; the thermo reduction (2)
+    # step; the thermo reduction (2)
     # at step 0 and every thermo_every steps; the standalone first half at
     # the start and after every thermo step but the last; the rebuild chain
     # (wrap/bin, 3 scan kernels, scatter, rank, gather, posf, list build) per
@@ -617,7 +639,8 @@ def measure(args, w, ws, dev, stream, torch, *, steps, fp64_steps, e2e_steps, dr
     # gated launches every step.
     n_thermo = steps // thermo_every if thermo_every else 0
     last_is_thermo = bool(thermo_every) and steps % thermo_every == 0
-    gpu_launches = kernels_per_step * (steps + (1 if thermo_every else 0))
+    # (the warm-up ended on a thermo step: step 0's energies are not recomputed)
+    gpu_launches = kernels_per_step * steps
     gpu_launches += 2 * (n_thermo + (1 if thermo_every else 0))
     gpu_launches += 1 + n_thermo - (1 if last_is_thermo else 0)
     if R < 0:
@@ -688,7 +711,8 @@ def measure(args, w, ws, dev, stream, torch, *, steps, fp64_steps, e2e_steps, dr
                           "k_eam_force_mixed<1,4> (density kernel: 0.858)"}
                if w["kind"] == "eam" else
                {"resource": "issue slots + L1/tex (neighbour gathers)", "frac": 0.78,
-                "source": "ncu smsp__issue_active of k_lj_mixed<1,4,multi> (L1/tex throughput 0.75)"})
+                "source": "ncu smsp__issue_active of k_lj_mixed<1,4,multi> (L1/tex throughput 0.75)"}
+               if w["kind"] == "lj_multi" else None)
     out["roofline"] = {"kernel": "k_eam_force (mixed, fused Verlet halves)" if w["kind"] == "eam" else "k_lj",
                        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                        "frac": achieved / peak, "peak_source": peak_kind,
@@ -781,6 +805,20 @@ def main():
         for k in ("metric", "unit", "n_gpus", "steps", "warmup", "higher_is_better", "scaling", "vs_baseline"):
             mix.pop(k, None)
         out["lj_mixture"] = mix
+    # ---- the 32,000-atom LJ crystal (the CPU-runnable case), in the same line --
+    if eam and not args.no_lj_crystal and not args.ncell and ws == 1:
+        wc = WORKLOADS["lj_fcc_32k"]
+        c1 = measure(args, wc, ws, dev, stream, torch, steps=args.steps, fp64_steps=40, e2e_steps=20,
+                     drift_steps=(100, 100), oracle_sample=0, name="lj_fcc_32k")
+        if not args.no_cpu and rank == 0:
+            rate, info = cpu_oracle_rate(wc, target_s=5.0)
+            c1["cpu_baseline"] = {"value": rate, "unit": "atom-timesteps/s", "cores": info["threads"],
+                                  "kind": "port",
+                                  "sample": "the whole %d-atom workload, %d FP64 NVE steps on the OpenMP oracle "
+                                            "(%.1f s)" % (info["atoms"], info["steps"], info["seconds"])}
+        for k in ("metric", "unit", "n_gpus", "steps", "warmup", "higher_is_better", "scaling", "vs_baseline"):
+            c1.pop(k, None)
+        out["lj_fcc_32k"] = c1
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:

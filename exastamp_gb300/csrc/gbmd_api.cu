@@ -113,7 +113,7 @@ static void drop_graph(gbmd_context* c) {
 
 static void invalidate_list(gbmd_context* c) {
   c->list_valid = false;
-  c->forces_valid_step = c->rho_valid_step = -1;
+  c->energy_step = -1, c->forces_valid_step = c->rho_valid_step = -1;
   drop_graph(c);
 }
 
@@ -603,7 +603,7 @@ static int upload_arrays(gbmd_context* c, const double* const* host, double* con
 // than skin/2 since the last rebuild (config_move_particles.msp L19-22,
 // L116-118), otherwise refresh the FP32/FP64 gather copies.
 static int after_new_positions(gbmd_context* c) {
-  c->forces_valid_step = c->rho_valid_step = -1;
+  c->energy_step = -1, c->forces_valid_step = c->rho_valid_step = -1;
   if (!c->list_valid) {
     // the caller may reuse its arrays once the upload returns
     GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -647,7 +647,7 @@ int gbmd_upload_state(gbmd_context* c, const double* rx, const double* ry, const
   int rc = upload_arrays(c, host, dev, 9);
   if (rc) return rc;
   if ((rc = after_new_positions(c))) return rc;
-  c->forces_valid_step = c->step;
+  c->energy_step = -1, c->forces_valid_step = c->step;
   return GBMD_OK;
 }
 
@@ -913,7 +913,7 @@ int gbmd_set_eam_johnson(gbmd_context* c, const double params[19], double rcut) 
   P.rc2hi = (float)(P.rcut2 * (1.0 + 0x1p-12));
   c->ej = P;
   c->pot = GBMD_POT_EAM_JOHNSON;
-  c->forces_valid_step = c->rho_valid_step = -1;
+  c->energy_step = -1, c->forces_valid_step = c->rho_valid_step = -1;
   set_rlist(c, rcut);
   return GBMD_OK;
 }
@@ -922,7 +922,7 @@ int gbmd_set_precision(gbmd_context* c, int precision) {
   if (!c || (precision != GBMD_PRECISION_FP64 && precision != GBMD_PRECISION_MIXED)) return GBMD_ERR_INVALID;
   if (c->precision != precision) {
     c->precision = precision;
-    c->forces_valid_step = c->rho_valid_step = -1;
+    c->energy_step = -1, c->forces_valid_step = c->rho_valid_step = -1;
     drop_graph(c);
   }
   return GBMD_OK;
@@ -1033,7 +1033,7 @@ int gbmd_build_neighbors(gbmd_context* c) {
   if (!c) return GBMD_ERR_INVALID;
   int rc = do_rebuild(c, true);
   if (rc) return rc;
-  c->forces_valid_step = c->rho_valid_step = -1;
+  c->energy_step = -1, c->forces_valid_step = c->rho_valid_step = -1;
   return GBMD_OK;
 }
 
@@ -1056,7 +1056,7 @@ int gbmd_update_neighbors(gbmd_context* c, int* rebuilt) {
   }
   int rc = do_rebuild(c, true);
   if (rc) return rc;
-  c->forces_valid_step = c->rho_valid_step = -1;
+  c->energy_step = -1, c->forces_valid_step = c->rho_valid_step = -1;
   if (rebuilt) *rebuilt = 1;
   return GBMD_OK;
 }
@@ -1138,14 +1138,14 @@ int gbmd_compute_forces(gbmd_context* c, int flags) {
   rc = launch_forces(c, f);
   if (rc) return rc;
   GBMD_CUDA(c, cudaGetLastError());
-  c->forces_valid_step = c->step;
+  c->energy_step = -1, c->forces_valid_step = c->step;
   return GBMD_OK;
 }
 
 int gbmd_push_f_v_r(gbmd_context* c, double dt, double dt_scale) {
   if (!c) return GBMD_ERR_INVALID;
   launch_push_f_v_r(c, dt, dt_scale);
-  c->forces_valid_step = c->rho_valid_step = -1;
+  c->energy_step = -1, c->forces_valid_step = c->rho_valid_step = -1;
   GBMD_CUDA(c, cudaGetLastError());
   return GBMD_OK;
 }
@@ -1160,7 +1160,7 @@ int gbmd_push_f_v(gbmd_context* c, double dt, double dt_scale) {
 int gbmd_push_min(gbmd_context* c, double dt, double dt_scale, double tolF) {
   if (!c) return GBMD_ERR_INVALID;
   launch_push_min(c, dt, dt_scale, tolF);
-  c->forces_valid_step = c->rho_valid_step = -1;
+  c->energy_step = -1, c->forces_valid_step = c->rho_valid_step = -1;
   GBMD_CUDA(c, cudaGetLastError());
   return GBMD_OK;
 }
@@ -1282,7 +1282,11 @@ int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int 
     c->rows_cap = nrows;
   }
   double* rows = c->d_rows;
-  if (c->forces_valid_step != c->step || want_thermo) {
+  // the state's forces, energies and virials are current when the previous
+  // run ended on a thermo step and nothing changed since: step 0's row then
+  // needs only the reduction
+  const bool energies_current = c->forces_valid_step == c->step && c->energy_step == c->step;
+  if (c->forces_valid_step != c->step || (want_thermo && !energies_current)) {
     ForceFlags f;
     f.energy = f.virial = want_thermo;
     if ((rc = launch_forces(c, f))) return rc;
@@ -1337,7 +1341,9 @@ int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int 
     GBMD_CUDA(c, cudaMemcpyAsync(thermo_out, rows, sizeof(double) * 27 * nrows, cudaMemcpyDeviceToHost, c->stream));
   GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
   c->step += nsteps;
-  c->forces_valid_step = c->step;
+  c->energy_step = -1, c->forces_valid_step = c->step;
+  // the last step computed energies and virials when it was a thermo step
+  if (want_thermo && nsteps % thermo_every == 0) c->energy_step = c->step;
   if (trigger && (rc = collect_device_rebuilds(c))) return rc;
   return check_device_errors(c);
 }
@@ -1368,7 +1374,7 @@ int gbmd_run_nve_host(gbmd_context* c, int nsteps, double dt, int rebuild_every,
       GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_GATE, 0, sizeof(int), c->stream));
       if ((rc = do_rebuild(c, true))) return rc;
     }
-    c->forces_valid_step = c->step;
+    c->energy_step = -1, c->forces_valid_step = c->step;
     c->rho_valid_step = -1;
     c->first_half_done = true;
   } else {
@@ -1405,7 +1411,7 @@ int gbmd_run_minimize(gbmd_context* c, int nsteps, double dt, double tolF, int r
     if (rebuild_every > 0 && s % rebuild_every == 0 && (rc = do_rebuild(c, true))) return rc;
     if (trigger && (rc = rebuild_if_displaced(c))) return rc;
   }
-  c->forces_valid_step = c->rho_valid_step = -1;
+  c->energy_step = -1, c->forces_valid_step = c->rho_valid_step = -1;
   GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
   if (trigger && (rc = collect_device_rebuilds(c))) return rc;
   return check_device_errors(c);
@@ -1559,7 +1565,7 @@ int gbmd_profile_step(gbmd_context* c, int reps, double ms[5]) {
   cudaEventDestroy(e1);
   if (rc) return rc;
   GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
-  c->forces_valid_step = c->rho_valid_step = -1;
+  c->energy_step = -1, c->forces_valid_step = c->rho_valid_step = -1;
   return check_device_errors(c);
 }
 

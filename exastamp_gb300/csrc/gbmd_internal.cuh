@@ -215,6 +215,7 @@ struct gbmd_context {
 
   int64_t step = 0;
   int64_t forces_valid_step = -1;
+  int64_t energy_step = -1;      // step whose per-atom energies and virials ep, vir hold (run_nve thermo steps)
   int64_t rho_valid_step = -1;   // step of the last standalone EAM density pass (-1: none valid)
   int64_t rho_builds = -1;       // list builds at that pass
   bool rho_ev = false;           // that pass stored the embedding energies

@@ -510,3 +510,29 @@ def test_list_regrows_for_a_dense_cluster(gpu, oracle, mixed):
     assert got == ref
     G = np.stack([d["ax"], d["ay"], d["az"]], 1)
     assert rel_rms(G, F) < (FP64_TOL if not mixed else MIXED_FORCE_TOL)
+
+
+def test_consecutive_runs_reuse_current_energies(gpu, oracle):
+    """A run that ended on a thermo step leaves its energies and virials
+    current: the next run's step-0 row reuses them (only the reduction runs)
+    and must equal the same row of one long run, bit for bit; a change of
+    velocities (push_f_v) in between is seen by that row."""
+    s = _jitter(S.lj_fcc(ncell=6, seed=51), 0.03, 51)
+    with gpu_ctx(gpu, s, LJ, 0.3, mixed=True) as ctx:
+        long_rows = ctx.run_nve(60, 0.005, rebuild_every=10, thermo_every=20)
+        long_state = ctx.download(("x", "y", "z", "vx", "vy", "vz"))
+    with gpu_ctx(gpu, s, LJ, 0.3, mixed=True) as ctx:
+        a = ctx.run_nve(40, 0.005, rebuild_every=10, thermo_every=20)
+        b = ctx.run_nve(20, 0.005, rebuild_every=10, thermo_every=20)
+        st = ctx.download(("x", "y", "z", "vx", "vy", "vz"))
+        assert np.array_equal(a, long_rows[:3])
+        assert np.array_equal(b, long_rows[2:])
+        for k in st:
+            assert np.array_equal(st[k], long_state[k]), k
+        # velocities changed after a thermo step: the kinetic terms follow
+        ctx.push_f_v(0.005, 1.0)
+        c = ctx.run_nve(0, 0.005, rebuild_every=10, thermo_every=20)
+        v = ctx.download(("vx", "vy", "vz"))
+        ke = 0.5 * sum((v[k] ** 2).sum() for k in ("vx", "vy", "vz"))
+        assert abs(c[0, 21:24].sum() - ke) < 1e-12 * ke
+        assert c[0, 24] == b[-1, 24]  # same positions: same potential energy
