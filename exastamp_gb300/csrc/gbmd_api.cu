@@ -107,8 +107,11 @@ int ensure_atom_capacity(gbmd_context* c, int64_t n) {
 }
 
 static void drop_graph(gbmd_context* c) {
-  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
-  c->graph_exec = nullptr;
+  for (auto& row : c->graphs)
+    for (auto& g : row) {
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+      g.exec = nullptr;
+    }
 }
 
 static void invalidate_list(gbmd_context* c) {
@@ -1213,54 +1216,69 @@ static int one_step(gbmd_context* c, double dt, const StepPlan& p, bool check, d
 }
 
 // A graph covers G steps: two rebuild intervals (G = 2R) with a fixed
-// interval, or an even G with the displacement trigger (R < 0), so that every
-// buffer swap inside it happens an even number of times and the captured
-// pointers are valid again when it is replayed.  With thermo, the reduction
-// is captured at the chunk's last step only (thermo_every == G).
-static int capture_graph(gbmd_context* c, double dt, int R, int G, bool thermo_end) {
-  drop_graph(c);
+// interval, or an even G with the displacement trigger (R < 0).  Slot 0
+// holds a chunk followed by more steps: every step swaps the position
+// buffers once, so an even G returns to the buffer it started from and the
+// captured pointers are valid again when it is replayed.  Slot 1 holds the
+// chunk that ends a run: its last step keeps full velocities (no fused
+// first half, no swap), so it swaps G - 1 times.  Each slot is kept per
+// parity of the buffer indices it starts from.  With thermo, the reduction is captured at
+// the chunk's last step only (thermo_every == G).
+static int capture_graph(gbmd_context* c, int slot, double dt, int R, int G, bool thermo_end) {
+  gbmd_context::GraphSlot& gs = c->graph_slot(slot);
+  if (gs.exec) cudaGraphExecDestroy(gs.exec);
+  gs.exec = nullptr;
+  const bool tail = slot == 1;
   cudaGraph_t g;
   const int64_t builds = c->list_builds;  // capturing runs nothing
+  const int cur0 = c->cur, cur_s0 = c->cur_s;
   GBMD_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   int rc = GBMD_OK;
   c->capturing = true;
   for (int l = 1; l <= G && rc == GBMD_OK; ++l) {
-    StepPlan p{R > 0 && l % R == 0, thermo_end && l == G, false, R < 0};
+    StepPlan p{R > 0 && l % R == 0, thermo_end && l == G, tail && l == G, R < 0};
     rc = one_step(c, dt, p, false, nullptr);
   }
   c->capturing = false;
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
   c->list_builds = builds;
+  // capturing ran nothing: the buffer indices go back to where the graph starts
+  const int swapped = c->cur ^ cur0, swapped_s = c->cur_s ^ cur_s0;
+  c->cur = cur0;
+  c->cur_s = cur_s0;
   if (rc) {
     if (e == cudaSuccess) cudaGraphDestroy(g);
     return rc;
   }
   if (e != cudaSuccess) return check_cuda(c, e, "cudaStreamEndCapture");
-  e = cudaGraphInstantiate(&c->graph_exec, g, 0);
+  e = cudaGraphInstantiate(&gs.exec, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return check_cuda(c, e, "cudaGraphInstantiate");
-  c->graph_rebuild_every = R;
-  c->graph_chunk = G;
-  c->graph_dt = dt;
-  c->graph_thermo_end = thermo_end ? 1 : 0;
-  c->graph_key_n = c->n;
-  c->graph_key_maxnb = c->maxnb;
-  c->graph_key_tpa = c->tpa;
-  c->graph_key_vec = c->vec;
-  c->graph_key_staged = c->staged ? 1 : 0;
-  c->graph_key_block = c->block;
-  c->graph_key_block_rho = c->block_rho;
-  c->graph_key_prec = c->precision;
+  gs.rebuild_every = R;
+  gs.chunk = G;
+  gs.dt = dt;
+  gs.thermo_end = thermo_end ? 1 : 0;
+  gs.cur0 = cur0;
+  gs.cur_s0 = cur_s0;
+  gs.swaps = swapped;
+  gs.swaps_s = swapped_s;
+  gs.key_n = c->n;
+  gs.key_maxnb = c->maxnb;
+  gs.key_tpa = c->tpa;
+  gs.key_vec = c->vec;
+  gs.key_staged = c->staged ? 1 : 0;
+  gs.key_block = c->block;
+  gs.key_block_rho = c->block_rho;
+  gs.key_prec = c->precision;
   return GBMD_OK;
 }
 
-static bool graph_matches(const gbmd_context* c, double dt, int R, int G, bool thermo_end) {
-  return c->graph_exec && c->graph_rebuild_every == R && c->graph_chunk == G && c->graph_dt == dt &&
-         c->graph_thermo_end == (thermo_end ? 1 : 0) && c->graph_key_n == c->n && c->graph_key_maxnb == c->maxnb &&
-         c->graph_key_tpa == c->tpa && c->graph_key_vec == c->vec && c->graph_key_block == c->block &&
-         c->graph_key_block_rho == c->block_rho &&
-         c->graph_key_staged == (c->staged ? 1 : 0) &&
-         c->graph_key_prec == c->precision;
+static bool graph_matches(const gbmd_context* c, int slot, double dt, int R, int G, bool thermo_end) {
+  const gbmd_context::GraphSlot& gs = const_cast<gbmd_context*>(c)->graph_slot(slot);
+  return gs.exec && gs.rebuild_every == R && gs.chunk == G && gs.dt == dt && gs.thermo_end == (thermo_end ? 1 : 0) &&
+         gs.cur0 == c->cur && gs.cur_s0 == c->cur_s && gs.key_n == c->n && gs.key_maxnb == c->maxnb && gs.key_tpa == c->tpa &&
+         gs.key_vec == c->vec && gs.key_block == c->block && gs.key_block_rho == c->block_rho &&
+         gs.key_staged == (c->staged ? 1 : 0) && gs.key_prec == c->precision;
 }
 
 int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int thermo_every, double* thermo_out,
@@ -1286,7 +1304,8 @@ int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int 
   // run ended on a thermo step and nothing changed since: step 0's row then
   // needs only the reduction
   const bool energies_current = c->forces_valid_step == c->step && c->energy_step == c->step;
-  if (c->forces_valid_step != c->step || (want_thermo && !energies_current)) {
+  const bool recompute = c->forces_valid_step != c->step || (want_thermo && !energies_current);
+  if (recompute) {
     ForceFlags f;
     f.energy = f.virial = want_thermo;
     if ((rc = launch_forces(c, f))) return rc;
@@ -1296,7 +1315,13 @@ int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int 
     GBMD_CUDA(c, cudaMemcpyAsync(rows, c->d_thermo, sizeof(double) * 27, cudaMemcpyDeviceToDevice, c->stream));
   }
   if (nsteps == 0) {
+    if (want_thermo && thermo_out)
+      GBMD_CUDA(c, cudaMemcpyAsync(thermo_out, rows, sizeof(double) * 27, cudaMemcpyDeviceToHost, c->stream));
     GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (recompute) {
+      c->forces_valid_step = c->step;
+      c->energy_step = want_thermo ? c->step : -1;
+    }
     return check_device_errors(c);
   }
   const int R = rebuild_every;
@@ -1318,12 +1343,16 @@ int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int 
   const bool graph_ok = use_graph && G > 0 && G % 2 == 0 && (!want_thermo || thermo_every == G);
   int s = 1;
   while (s <= nsteps) {
-    // a graph chunk covers steps s..s+G-1; it starts right after a rebuild
-    // interval and must end before the last step (which may not fuse the
-    // next first half)
-    if (graph_ok && (s - 1) % G == 0 && s + G - 1 < nsteps) {
-      if (!graph_matches(c, dt, R, G, want_thermo) && (rc = capture_graph(c, dt, R, G, want_thermo))) return rc;
-      GBMD_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
+    // a graph chunk covers steps s..s+G-1 and starts right after a rebuild
+    // interval; the chunk that ends the run is the tail graph (slot 1)
+    if (graph_ok && (s - 1) % G == 0 && s + G - 1 <= nsteps) {
+      const int slot = s + G - 1 == nsteps ? 1 : 0;
+      if (!graph_matches(c, slot, dt, R, G, want_thermo) && (rc = capture_graph(c, slot, dt, R, G, want_thermo)))
+        return rc;
+      const gbmd_context::GraphSlot& gs = c->graph_slot(slot);
+      GBMD_CUDA(c, cudaGraphLaunch(gs.exec, c->stream));
+      c->cur ^= gs.swaps;
+      c->cur_s ^= gs.swaps_s;
       if (R > 0) c->list_builds += G / R;  // replayed rebuilds (trigger ones are counted on the device)
       if (want_thermo)
         GBMD_CUDA(c, cudaMemcpyAsync(rows + 27 * (size_t)((s + G - 1) / thermo_every), c->d_thermo,

@@ -220,15 +220,21 @@ struct gbmd_context {
   int64_t rho_builds = -1;       // list builds at that pass
   bool rho_ev = false;           // that pass stored the embedding energies
 
-  // CUDA graph of a chunk of steps
-  cudaGraphExec_t graph_exec = nullptr;
-  int graph_rebuild_every = 0;
-  int graph_chunk = 0;
-  double graph_dt = 0.0;
-  int graph_thermo_end = 0;
-  int64_t graph_key_n = -1;
-  int graph_key_maxnb = -1, graph_key_tpa = -1, graph_key_block = -1, graph_key_prec = -1, graph_key_vec = -1,
-      graph_key_staged = -1, graph_key_block_rho = -1;
+  // CUDA graphs of a chunk of steps: [0] a chunk followed by more steps,
+  // [1] the chunk that ends a run (its last step keeps full velocities);
+  // one per parity of the buffer indices the chunk starts from (cur, cur_s)
+  struct GraphSlot {
+    cudaGraphExec_t exec = nullptr;
+    int rebuild_every = 0, chunk = 0, thermo_end = 0;
+    double dt = 0.0;
+    int cur0 = -1, cur_s0 = -1;  // buffer indices the graph starts from (positions; v/a/type/id/user)
+    int swaps = 0, swaps_s = 0;  // parity of the swaps inside it
+    int64_t key_n = -1;
+    int key_maxnb = -1, key_tpa = -1, key_block = -1, key_prec = -1, key_vec = -1, key_staged = -1,
+        key_block_rho = -1;
+  };
+  GraphSlot graphs[2][4];
+  GraphSlot& graph_slot(int tail) { return graphs[tail][cur | (cur_s << 1)]; }
 };
 
 // ---------------------------------------------------------------------------

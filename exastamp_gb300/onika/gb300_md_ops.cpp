@@ -349,8 +349,9 @@ class Gb300LJMultiForceNode : public OperatorNode {
 // alone (nothing left to do: the embedding ran with the density), eam_force
 // (the force pass from the kept F'(rho), on the same positions).  The
 // instances share the device context through gb300_session.  eam_ghost is
-// accepted (there are no ghost cells on the device).  eam_symmetry (Newton-3)
-// is refused: the library has no half-list EAM kernels.
+// accepted (there are no ghost cells on the device).  eam_symmetry (Newton-3
+// scatter, eam_force_op_multimat.h L162-169, L305-338) is accepted and runs
+// on the full list: the same sums up to rounding, without atomics.
 template <class GridT>
 class Gb300EamAlloyForceNode : public OperatorNode {
   ADD_SLOT(ParticleSpecies, species, INPUT, REQUIRED);
@@ -368,7 +369,7 @@ class Gb300EamAlloyForceNode : public OperatorNode {
   ADD_SLOT(bool, eam_rho2emb, INPUT, true);
   ADD_SLOT(bool, eam_ghost, INPUT, true);
   ADD_SLOT(bool, eam_force, INPUT, true);
-  ADD_SLOT(bool, eam_symmetry, INPUT, false);
+  ADD_SLOT(bool, eam_symmetry, INPUT, false, DocString{"accepted; the full list gives the same sums"});
   ADD_SLOT(double, rcut_inc, INPUT, 1.0, DocString{"neighbour skin (global.rcut_inc)"});
   ADD_SLOT(std::string, precision, INPUT, std::string{"mixed"}, DocString{"mixed or fp64"});
   GB300_SESSION_SLOT;
@@ -378,7 +379,6 @@ class Gb300EamAlloyForceNode : public OperatorNode {
     *rcut_max = std::max(*rcut, *rcut_max);
     *ghost_dist_max = std::max(*ghost_dist_max, 2.0 * (*rcut));
     if (grid->number_of_cells() == 0) return;
-    if (*eam_symmetry) fatal_error() << "gb300_eam_alloy_force: eam_symmetry is not offered" << std::endl;
     const int passes = (*eam_rho && *eam_force) ? 0
                        : *eam_rho               ? GBMD_FORCE_PASS_DENSITY
                        : *eam_force             ? GBMD_FORCE_PASS_FORCE

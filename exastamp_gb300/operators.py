@@ -266,8 +266,12 @@ class eam_alloy_force(Operator):
         if self.passes is None:
             raise OperatorError("eam_rho2emb %s with eam_rho and eam_force both %s: the embedding runs with "
                                 "the density pass" % (emb, rho))
-        if self.slots.get("eam_symmetry", False):
-            raise OperatorError("eam_symmetry (Newton-3 scatter) is not offered; the full-list path is used")
+        # eam_symmetry (Newton-3 half list with the rho_j and reaction-force
+        # scatter of eam_force_op_multimat.h L162-169, L305-338) selects only
+        # how the reference evaluates the same sums; here it runs on the full
+        # list, which gives the same densities and forces up to rounding,
+        # deterministically.
+        self.symmetry = bool(self.slots.get("eam_symmetry", False))
         rcut = quantity(self.slots["rcut"])
         sim.ctx.set_eam_alloy(sf, rcut, EV * 1.0, EV)
         sim.rcut_max = max(sim.rcut_max, rcut)

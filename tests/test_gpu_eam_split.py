@@ -112,3 +112,33 @@ def test_split_run_file_form(gpu):
         assert np.array_equal(out[0][k], out[1][k]), k
     with pytest.raises(OP.OperatorError):
         OP.eam_alloy_force(**common, eam_rho=True, eam_rho2emb=False, eam_force=True).bind(OP.Simulation(s))
+
+
+def test_eam_symmetry_runs_the_full_list(gpu, oracle):
+    """eam_symmetry: true (the reference's Newton-3 scatter) gives the
+    full-list result bit for bit, and that result matches the oracle."""
+    sf = _eam()
+    s = S.eam_cu_fcc(ncell=5, displace=0.06, seed=9)
+    out = []
+    for sym in (False, True):
+        sim = OP.Simulation(s)
+        try:
+            sim.set_precision(False)
+            op = OP.eam_alloy_force(rcut=5.0, parameters=sf, eam_symmetry=sym)
+            op.bind(sim)
+            OP.chunk_neighbors().bind(sim, 0.3)
+            op.execute(sim, energy=True, virial=True)
+            out.append(sim.ctx.download(virial=True))
+        finally:
+            sim.ctx.close()
+    for k in ("ax", "ay", "az", "ep", "vir"):
+        assert np.array_equal(out[0][k], out[1][k]), k
+    tab = oracle.EamOracleTables.from_setfl(sf, S.EV, S.EV, rcut=5.0)
+    x, y, z = s.x.copy(), s.y.copy(), s.z.copy()
+    oracle.wrap(x, y, z, s.lo, s.hi)
+    nl = oracle.build_neighbors(x, y, z, s.id, s.lo, s.hi, 5.3)
+    fx, fy, fz, ep, vir, _, _ = oracle.eam_forces(x, y, z, s.type, nl, s.L, tab, 5.0)
+    F = np.stack([fx, fy, fz], 1) / s.masses[0]
+    G = np.stack([out[1]["ax"], out[1]["ay"], out[1]["az"]], 1)
+    assert np.abs(G - F).max() < 1e-11 * np.abs(F).max()
+    assert np.abs(out[1]["ep"] - ep).max() < 1e-12 * np.abs(ep).max()

@@ -311,6 +311,30 @@ def test_graph_with_thermo_equals_stepwise_run(gpu):
         assert np.array_equal(outs[0][k], outs[1][k]), k
 
 
+@pytest.mark.parametrize("pot", ["lj", "eam"])
+def test_consecutive_graph_runs_equal_stepwise_runs(gpu, pot):
+    """Runs whose last chunk is a whole graph (the tail graph), one after
+    another: each run flips the parity of the double buffers, so the graphs
+    are kept per parity and replayed only from the buffers they were captured
+    on.  Thermo rows and the final state equal the stepwise runs bit for bit."""
+    if pot == "lj":
+        s, setpot, dt = _jitter(S.lj_fcc(ncell=5, seed=14), 0.03, 14), LJ, 0.005
+    else:
+        sf = SF.tabulate(SF.load_cu_params())
+        s = S.eam_cu_fcc(ncell=5, displace=0.05, seed=15)
+        setpot, dt = (lambda c: c.set_eam_alloy(sf, 5.0, S.EV, S.EV)), 1e-3
+    runs = (40, 20, 20, 20, 60, 20)
+    outs, ths = [], []
+    for use_graph in (False, True):
+        with gpu_ctx(gpu, s, setpot, 0.3, mixed=True) as ctx:
+            ths.append([ctx.run_nve(k, dt, rebuild_every=10, thermo_every=20, use_graph=use_graph) for k in runs])
+            outs.append(ctx.download())
+    for a, b in zip(*ths):
+        assert np.array_equal(a, b)
+    for k in outs[0]:
+        assert np.array_equal(outs[0][k], outs[1][k]), k
+
+
 def test_graph_run_equals_stepwise_run(gpu, oracle):
     s = S.lj_fcc(ncell=5, seed=9)
     outs = []
