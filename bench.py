@@ -118,12 +118,16 @@ def parse():
 
 # ---------------------------------------------------------------------------
 def make_system(w):
+    """The workload's atoms, stored as the reference's grid holds them (cell
+    by cell, z slowest): the caller order of the e2e host arrays."""
     from exastamp_gb300 import systems as S
     if w["kind"] == "eam":
-        return S.eam_cu_fcc(ncell=w["ncell"], a=w["a"], T=w["T"], seed=w["seed"])
-    if w["kind"] == "lj_multi":
-        return S.lj_binary_voids(n=w["n"], seed=w["seed"], nvoids=max(1, round(64 * w["n"] / 16_777_216)))
-    return S.lj_fcc(ncell=w["ncell"], T=w["T"], seed=w["seed"])
+        s = S.eam_cu_fcc(ncell=w["ncell"], a=w["a"], T=w["T"], seed=w["seed"])
+    elif w["kind"] == "lj_multi":
+        s = S.lj_binary_voids(n=w["n"], seed=w["seed"], nvoids=max(1, round(64 * w["n"] / 16_777_216)))
+    else:
+        s = S.lj_fcc(ncell=w["ncell"], T=w["T"], seed=w["seed"])
+    return S.grid_order(s, w["rcut"] + w["skin"])
 
 
 def bind_potential(ctx, w):
@@ -528,7 +532,12 @@ def e2e_section(ctx, s, w, R, steps, ws, torch, stream):
         return ev0.elapsed_time(ev1), wall * 1e3, ctx.list_builds() - b0
 
     sep_ms, sep_wall, _ = loop(False)   # the same step as three calls, for comparison
+    ctx.set_host_pipeline(0)
+    unpiped_ms, unpiped_wall, _ = loop(True)   # one call per step, host link not overlapped
+    ctx.set_host_pipeline(-1)
+    slabs, piped0 = ctx.host_pipeline()
     mse, wall_ms, builds = loop(True)
+    piped = ctx.host_pipeline()[1] - piped0
     mse = dist_max(max(mse, wall_ms), ws)
     sep_ms = max(sep_ms, sep_wall)
     t0 = time.perf_counter()
@@ -543,9 +552,14 @@ def e2e_section(ctx, s, w, R, steps, ws, torch, stream):
             "upload_ms": up_ms, "download_ms": down_ms,
             "h2d_bytes_per_step": 72 * n, "d2h_bytes_per_step": 72 * n, "steps": steps,
             "ms_per_step": mse / steps, "ms_per_step_as_three_calls": sep_ms / steps,
-            "list_builds": builds,
-            "path": "gbmd_run_nve_host(1 step; pinned r,v,a uploaded, skin/2 displacement test, "
-                    "r copied back during the force pass, then v,a)"}
+            "ms_per_step_unpipelined": max(unpiped_ms, unpiped_wall) / steps,
+            "list_builds": builds, "slabs": slabs, "pipelined_steps": piped,
+            "host_order": "grid cells, z slowest (as the reference's grid stores atoms)",
+            "path": "gbmd_run_nve_host(1 step, pinned r,v,a): chunks of the caller order read over the host link "
+                    "with the first half and skin/2 test applied, pair passes slab by slab as their chunks "
+                    "arrive, v,a written back chunk by chunk; a step that needs a rebuild finishes unpipelined"
+            if slabs else "gbmd_run_nve_host(1 step; pinned r,v,a read with the first half applied, skin/2 "
+                          "displacement test, r copied back during the force pass, then v,a)"}
 
 
 def measure(args, w, ws, dev, stream, torch, *, steps, fp64_steps, e2e_steps, drift_steps, oracle_sample,

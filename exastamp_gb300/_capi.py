@@ -97,6 +97,9 @@ def lib(path: str = LIB_PATH):
             "gbmd_lj_loss_grad": ([vp, vp, vp, vp, vp, dbl, dbl, P(dbl), vp], i32),
             "gbmd_lj_multi_loss_grad": ([vp, vp, vp, vp, vp, dbl, dbl, P(dbl), vp, vp], i32),
             "gbmd_list_builds": ([vp, P(i64)], i32),
+            "gbmd_set_host_pipeline": ([vp, i32], i32),
+            "gbmd_set_host_pipeline_link": ([vp, i32, i32], i32),
+            "gbmd_get_host_pipeline": ([vp, P(i32), P(i64)], i32),
             "gbmd_thermo": ([vp, vp], i32),
             "gbmd_device_state": ([vp] + [vp] * 11, i32),
             "gbmd_thermo_reduce_noalloc": ([i64, vp, vp, vp, vp, vp, vp, vp, i32, vp, vp], i32),
@@ -381,6 +384,20 @@ class Context:
         self._chk(self._L.gbmd_lj_multi_loss_grad(self.h, _p(fx), _p(fy), _p(fz), _p(et), float(w_force),
                                                   float(w_energy), C.byref(loss), _p(ge), _p(gs)))
         return loss.value, ge, gs
+
+    def set_host_pipeline(self, slabs):
+        """gbmd_set_host_pipeline: -1 automatic, 0 off, 4..64 slabs."""
+        self._chk(self._L.gbmd_set_host_pipeline(self.h, int(slabs)))
+
+    def set_host_pipeline_link(self, blocks, threads):
+        """gbmd_set_host_pipeline_link: launch shape of the host-link pieces."""
+        self._chk(self._L.gbmd_set_host_pipeline_link(self.h, int(blocks), int(threads)))
+
+    def host_pipeline(self):
+        """(slabs the next host step would use, steps taken through the pipeline)."""
+        sl, st = C.c_int(0), C.c_int64(0)
+        self._chk(self._L.gbmd_get_host_pipeline(self.h, C.byref(sl), C.byref(st)))
+        return sl.value, st.value
 
     def list_builds(self):
         n = C.c_int64(0)

@@ -459,6 +459,7 @@ int gbmd_destroy(gbmd_context* c) {
   }
   if (c->copy_fork) cudaEventDestroy(c->copy_fork);
   if (c->cond_stream) cudaStreamDestroy(c->cond_stream);
+  pipe_free(c);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return GBMD_OK;
@@ -1394,11 +1395,26 @@ int gbmd_run_nve_host(gbmd_context* c, int nsteps, double dt, int rebuild_every,
     GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_GATE, 0, sizeof(int), c->stream));
     const double* hdev[9];
     for (int k = 0; k < 9; ++k) hdev[k] = hd.a[k];
+    const int slabs = nsteps == 1 ? pipe_slabs_for(c) : 0;
     {
       const FusedTriggerScope gate(c, true);
-      launch_host_first_half(c, hdev, inverse_user(c), dt);
+      if (slabs) {
+        // one step with the host link overlapped with the passes
+        // (gbmd_pipeline.cu); it stands unless an atom moved more than skin/2
+        rc = pipe_step(c, dt, hdev, inverse_user(c), slabs);
+        if (rc) return rc;
+      } else {
+        launch_host_first_half(c, hdev, inverse_user(c), dt);
+      }
     }
     if ((rc = sync_error_word(c))) return rc;
+    if (slabs && !c->h_err[ERRW_GATE]) {
+      ++c->pipe_steps;
+      c->step += 1;
+      c->energy_step = -1, c->forces_valid_step = c->step;
+      c->rho_valid_step = -1;
+      return check_device_errors(c);
+    }
     if (c->h_err[ERRW_GATE]) {
       GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_GATE, 0, sizeof(int), c->stream));
       if ((rc = do_rebuild(c, true))) return rc;
@@ -1426,6 +1442,26 @@ int gbmd_run_nve_host(gbmd_context* c, int nsteps, double dt, int rebuild_every,
     if (rc == GBMD_OK && e != cudaSuccess) rc = check_cuda(c, e, "position copy");
   }
   return rc;
+}
+
+int gbmd_set_host_pipeline(gbmd_context* c, int slabs) {
+  if (!c || slabs < -1 || (slabs > 0 && slabs < 4) || slabs > 64) return GBMD_ERR_INVALID;
+  c->pipe_slabs = slabs;
+  return GBMD_OK;
+}
+
+int gbmd_set_host_pipeline_link(gbmd_context* c, int blocks, int threads) {
+  if (!c || blocks < 1 || blocks > 65535 || threads < 32 || threads > 1024 || threads % 32) return GBMD_ERR_INVALID;
+  c->pipe_link_blocks = blocks;
+  c->pipe_link_threads = threads;
+  return GBMD_OK;
+}
+
+int gbmd_get_host_pipeline(const gbmd_context* c, int* slabs, int64_t* steps) {
+  if (!c) return GBMD_ERR_INVALID;
+  if (slabs) *slabs = pipe_slabs_for(c);
+  if (steps) *steps = c->pipe_steps;
+  return GBMD_OK;
 }
 
 int gbmd_run_minimize(gbmd_context* c, int nsteps, double dt, double tolF, int rebuild_every) {

@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(256) k_lj(PairArgs A, LJSingle P, const LJPair
     __syncthreads();
   }
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = gt / T;
+  const int64_t i = A.i0 + gt / T;
   const int lane = (int)(gt % T);
   const bool live = i < A.n;
   const int nn = live ? min(A.nnb[i], A.maxnb) : 0;
@@ -115,7 +115,7 @@ __device__ __forceinline__ int r_knot_d(double r, double rdr, int nr, double& p)
 template <int T, bool EV>
 __global__ void __launch_bounds__(256) k_eam_rho(PairArgs A, EamDev E, double* __restrict__ fpd) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = gt / T;
+  const int64_t i = A.i0 + gt / T;
   const int lane = (int)(gt % T);
   const bool live = i < A.n;
   const int nn = live ? min(A.nnb[i], A.maxnb) : 0;
@@ -167,7 +167,7 @@ __device__ __forceinline__ int z2r_index(int a, int b) {
 template <int T, bool EV>
 __global__ void __launch_bounds__(256) k_eam_force(PairArgs A, EamDev E, const double* __restrict__ fpd) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = gt / T;
+  const int64_t i = A.i0 + gt / T;
   const int lane = (int)(gt % T);
   const bool live = i < A.n;
   const int nn = live ? min(A.nnb[i], A.maxnb) : 0;
@@ -238,7 +238,8 @@ __global__ void __launch_bounds__(256) k_eam_force(PairArgs A, EamDev E, const d
 // ---------------------------------------------------------------------------
 PairArgs make_args(gbmd_context* c, const ForceFlags& f) {
   PairArgs A;
-  A.n = c->n;
+  A.i0 = f.i0;
+  A.n = f.i1 >= 0 ? f.i1 : c->n;
   A.W = list_width(c);
   A.wsh = 0;
   while ((1 << A.wsh) < A.W) ++A.wsh;
@@ -261,6 +262,9 @@ PairArgs make_args(gbmd_context* c, const ForceFlags& f) {
   A.posd_o = c->posd[o];
   A.vx = c->VX(); A.vy = c->VY(); A.vz = c->VZ();
   A.ax = c->AX(); A.ay = c->AY(); A.az = c->AZ();
+  A.vxo = f.v_out ? f.v_out : A.vx;
+  A.vyo = f.v_out ? f.v_out + c->cap : A.vy;
+  A.vzo = f.v_out ? f.v_out + 2 * c->cap : A.vz;
   A.ep = c->ep;
   A.ep_emb = c->epd;
   A.vir = c->vir;
@@ -289,7 +293,7 @@ PairArgs make_args(gbmd_context* c, const ForceFlags& f) {
 template <int T, bool EV>
 static void launch_fp64_T(gbmd_context* c, const PairArgs& A, int part) {
   const int B = c->block;
-  const unsigned grid = (unsigned)((A.n * T + B - 1) / B);
+  const unsigned grid = (unsigned)(((A.n - A.i0) * T + B - 1) / B);
   cudaStream_t s = c->stream;
   if (c->pot != GBMD_POT_EAM_ALLOY && part == 1) return;
   if (c->pot == GBMD_POT_LJ) {
@@ -327,6 +331,12 @@ int launch_forces(gbmd_context* c, const ForceFlags& f) {
   if (c->pot == GBMD_POT_LJ_MULTI && c->ntypes > c->lj.ntypes)
     return set_error(c, GBMD_ERR_INVALID, "%d species but the LJ tables cover %d types", c->ntypes, c->lj.ntypes);
   if (!c->list_valid || !c->nbr) return set_error(c, GBMD_ERR_INVALID, "neighbour list not built");
+  const bool piece = f.i0 != 0 || f.i1 >= 0;
+  if (piece && (f.i0 < 0 || f.i1 < f.i0 || f.i1 > c->n))
+    return set_error(c, GBMD_ERR_INVALID, "atom range [%lld, %lld) outside [0, %lld)", (long long)f.i0,
+                     (long long)f.i1, (long long)c->n);
+  if (piece && (c->newton3 || c->staged || f.fuse == FUSE_PUSH2_PUSH1))
+    return set_error(c, GBMD_ERR_INVALID, "atom ranges: full-list kernels without staging or fused first half");
   const PairArgs A = make_args(c, f);
   const bool ev = f.energy || f.virial;
   const bool mixed = c->precision == GBMD_PRECISION_MIXED;

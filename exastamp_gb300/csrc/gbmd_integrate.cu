@@ -172,37 +172,61 @@ struct HostState9 {
   const double* a[9];
 };
 
+// Caller indices [u0, u1), grid-stride; with `rout` the pushed positions
+// also go back to the caller's arrays (in place: each thread reads its
+// element before writing it).
 __global__ void k_host_first_half(PushArgs P, HostState9 H, const int32_t* __restrict__ inv, double h, double h2,
-                                  double hv) {
-  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (u >= P.n) return;
-  double q[9];
+                                  double hv, int64_t u0, int64_t u1, HostState9 rout) {
+  for (int64_t u = u0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < u1;
+       u += (int64_t)gridDim.x * blockDim.x) {
+    double q[9];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) q[k] = H.a[k][u];
-  const int64_t i = inv[u];
-  const double x = __dadd_rn(q[0], __dadd_rn(__dmul_rn(q[3], h), __dmul_rn(q[6], h2)));
-  const double y = __dadd_rn(q[1], __dadd_rn(__dmul_rn(q[4], h), __dmul_rn(q[7], h2)));
-  const double z = __dadd_rn(q[2], __dadd_rn(__dmul_rn(q[5], h), __dmul_rn(q[8], h2)));
-  P.xo[i] = x;
-  P.yo[i] = y;
-  P.zo[i] = z;
-  P.vx[i] = __dadd_rn(q[3], __dmul_rn(q[6], hv));
-  P.vy[i] = __dadd_rn(q[4], __dmul_rn(q[7], hv));
-  P.vz[i] = __dadd_rn(q[5], __dmul_rn(q[8], hv));
-  P.ax[i] = q[6];
-  P.ay[i] = q[7];
-  P.az[i] = q[8];
-  if (P.refresh) refresh_gather(P.g, i, P.cellpack[i], P.type[i], x, y, z, P.pf, P.pd);
-  if (P.gate) displacement_test(P.gate, P.rref, P.rcap, P.thr2, i, x, y, z);
+    for (int k = 0; k < 9; ++k) q[k] = H.a[k][u];
+    const int64_t i = inv[u];
+    const double x = __dadd_rn(q[0], __dadd_rn(__dmul_rn(q[3], h), __dmul_rn(q[6], h2)));
+    const double y = __dadd_rn(q[1], __dadd_rn(__dmul_rn(q[4], h), __dmul_rn(q[7], h2)));
+    const double z = __dadd_rn(q[2], __dadd_rn(__dmul_rn(q[5], h), __dmul_rn(q[8], h2)));
+    P.xo[i] = x;
+    P.yo[i] = y;
+    P.zo[i] = z;
+    P.vx[i] = __dadd_rn(q[3], __dmul_rn(q[6], hv));
+    P.vy[i] = __dadd_rn(q[4], __dmul_rn(q[7], hv));
+    P.vz[i] = __dadd_rn(q[5], __dmul_rn(q[8], hv));
+    P.ax[i] = q[6];
+    P.ay[i] = q[7];
+    P.az[i] = q[8];
+    if (P.refresh) refresh_gather(P.g, i, P.cellpack[i], P.type[i], x, y, z, P.pf, P.pd);
+    if (P.gate) displacement_test(P.gate, P.rref, P.rcap, P.thr2, i, x, y, z);
+    if (rout.a[0]) {
+      const_cast<double*>(rout.a[0])[u] = x;
+      const_cast<double*>(rout.a[1])[u] = y;
+      const_cast<double*>(rout.a[2])[u] = z;
+    }
+  }
 }
 
 void launch_host_first_half(gbmd_context* c, const double* const host[9], const int32_t* inv, double dt) {
   if (!c->n) return;
-  HostState9 H;
+  HostState9 H, none{};
   for (int k = 0; k < 9; ++k) H.a[k] = host[k];
   const double h = dt * 1.0;
   const double h2 = h * h * 0.5;
-  k_host_first_half<<<nblk(c->n, 256), 256, 0, c->stream>>>(push_args(c), H, inv, h, h2, dt * 0.5);
+  k_host_first_half<<<nblk(c->n, 256), 256, 0, c->stream>>>(push_args(c), H, inv, h, h2, dt * 0.5, 0, c->n, none);
+}
+
+void launch_host_first_half_range(gbmd_context* c, const double* const host[9], const int32_t* inv, double dt,
+                                  int64_t u0, int64_t u1, bool write_back, int blocks, int threads,
+                                  cudaStream_t stream) {
+  if (u1 <= u0) return;
+  HostState9 H, rout{};
+  for (int k = 0; k < 9; ++k) H.a[k] = host[k];
+  if (write_back)
+    for (int k = 0; k < 3; ++k) rout.a[k] = host[k];
+  const double h = dt * 1.0;
+  const double h2 = h * h * 0.5;
+  const int64_t need = (u1 - u0 + threads - 1) / threads;
+  const unsigned grid = (unsigned)(need < blocks ? need : blocks);
+  k_host_first_half<<<grid, threads, 0, stream>>>(push_args(c), H, inv, h, h2, dt * 0.5, u0, u1, rout);
 }
 
 void launch_push_min(gbmd_context* c, double dt, double dt_scale, double tolF) {

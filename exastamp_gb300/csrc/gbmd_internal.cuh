@@ -235,6 +235,22 @@ struct gbmd_context {
   };
   GraphSlot graphs[2][4];
   GraphSlot& graph_slot(int tail) { return graphs[tail][cur | (cur_s << 1)]; }
+
+  // host-link pipeline of one gbmd_run_nve_host step (gbmd_pipeline.cu)
+  int pipe_slabs = -1;          // -1 automatic, 0 off, >= 4: slabs (and caller-order chunks) per step
+  int pipe_link_blocks = 40, pipe_link_threads = 512;  // grid-stride shape of the host-link pieces
+  cudaStream_t pipe_in = nullptr, pipe_out = nullptr;
+  cudaStream_t pipe_cs[3] = {nullptr, nullptr, nullptr};  // compute streams besides the context's
+  cudaEvent_t pipe_start = nullptr, pipe_out_done = nullptr;
+  cudaEvent_t pipe_in_ev[64] = {}, pipe_f_ev[64] = {}, pipe_d_ev[64] = {};
+  int* pipe_dev = nullptr;      // device scratch of the slab map
+  int* pipe_host = nullptr;     // its page-locked mirror
+  int64_t pipe_key_builds = -1, pipe_key_n = -1;
+  int pipe_key_slabs = 0;
+  std::vector<int> pipe_need;          // per slab: last caller chunk holding an atom of the slab or a neighbour slab
+  std::vector<uint64_t> pipe_mask;     // per caller chunk: slabs holding its atoms
+  std::vector<int64_t> pipe_begin;     // slab s = cell-order atoms [begin[s], begin[s+1])
+  int64_t pipe_steps = 0;              // steps that stood as pipelined (no rebuild due)
 };
 
 // ---------------------------------------------------------------------------
@@ -267,8 +283,19 @@ struct ForceFlags {
   int fuse = FUSE_NONE;
   int part = 0;   // 0 all kernels, 1 EAM density pass only, 2 final pair kernel only
   StepParams sp{};
+  int64_t i0 = 0, i1 = -1;    // cell-order atom range [i0, i1) (i1 < 0: all atoms)
+  double* v_out = nullptr;    // fused halves write v here (3 planes of cap) instead of in place
 };
 int launch_forces(gbmd_context* c, const ForceFlags& f);
+
+// host-link pipeline (gbmd_pipeline.cu): compute streams (the context's own
+// and pipe_cs); slabs to use for this context now
+// (0: the step goes the unpipelined way); one pipelined step, all streams
+// synchronised at return (the displacement gate is left in the error word)
+constexpr int PIPE_STREAMS = 4;
+int pipe_slabs_for(const gbmd_context* c);
+int pipe_step(gbmd_context* c, double dt, const double* const host[9], const int32_t* inv, int slabs);
+void pipe_free(gbmd_context* c);
 
 // integration (gbmd_integrate.cu)
 void launch_push_f_v_r(gbmd_context* c, double dt, double dt_scale);
@@ -279,6 +306,11 @@ void launch_first_half_swap(gbmd_context* c, double dt);
 // host: device addresses of page-locked caller arrays r, v, a (caller order);
 // inv: caller index -> cell-sorted index
 void launch_host_first_half(gbmd_context* c, const double* const host[9], const int32_t* inv, double dt);
+// the same over caller indices [u0, u1) on `stream` with at most `blocks`
+// blocks; write_back: the pushed positions also go to host[0..2]
+void launch_host_first_half_range(gbmd_context* c, const double* const host[9], const int32_t* inv, double dt,
+                                  int64_t u0, int64_t u1, bool write_back, int blocks, int threads,
+                                  cudaStream_t stream);
 void launch_thermo(gbmd_context* c, bool with_virial);
 void launch_thermo_raw(int64_t n, const double* vx, const double* vy, const double* vz, const double* ep,
                        const double* vir, const uint8_t* type, const double* mass, int ntypes, double* part,

@@ -96,7 +96,7 @@ __device__ __forceinline__ void ej_term_f(float pre, float k, float x, float c, 
 template <int T, bool EV>
 __global__ void __launch_bounds__(256) k_ej_rho(PairArgs A, JohnsonDev P, double* __restrict__ fpd) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = gt / T;
+  const int64_t i = A.i0 + gt / T;
   const int lane = (int)(gt % T);
   const bool live = i < A.n;
   const int nn = live ? min(A.nnb[i], A.maxnb) : 0;
@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(256) k_ej_rho(PairArgs A, JohnsonDev P, double
 template <int T, bool EV>
 __global__ void __launch_bounds__(256) k_ej_force(PairArgs A, JohnsonDev P, const double* __restrict__ fpd) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = gt / T;
+  const int64_t i = A.i0 + gt / T;
   const int lane = (int)(gt % T);
   const bool live = i < A.n;
   const int nn = live ? min(A.nnb[i], A.maxnb) : 0;
@@ -220,7 +220,7 @@ template <int T, bool EV>
 __global__ void __launch_bounds__(256) k_ej_rho_mixed(PairArgs A, JohnsonDev P, float* __restrict__ fpf,
                                                       float* __restrict__ epf) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = gt / T;
+  const int64_t i = A.i0 + gt / T;
   const int lane = (int)(gt % T);
   const bool live = i < A.n;
   const int nn = live ? min(A.nnb[i], A.maxnb) : 0;
@@ -250,7 +250,7 @@ template <int T, bool EV>
 __global__ void __launch_bounds__(256) k_ej_force_mixed(PairArgs A, JohnsonDev P, const float* __restrict__ fpf,
                                                         const float* __restrict__ epf) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = gt / T;
+  const int64_t i = A.i0 + gt / T;
   const int lane = (int)(gt % T);
   const bool live = i < A.n;
   const int nn = live ? min(A.nnb[i], A.maxnb) : 0;
@@ -322,7 +322,7 @@ __global__ void __launch_bounds__(256) k_ej_force_mixed(PairArgs A, JohnsonDev P
 template <int T, bool EV>
 static void launch_ej_T(gbmd_context* c, const PairArgs& A, int part, bool mixed) {
   const int B = c->block;
-  const unsigned grid = (unsigned)((A.n * T + B - 1) / B);
+  const unsigned grid = (unsigned)(((A.n - A.i0) * T + B - 1) / B);
   cudaStream_t s = c->stream;
   if (mixed) {
     if (part != 2) k_ej_rho_mixed<T, EV><<<grid, B, 0, s>>>(A, c->ej, c->fpf, c->epf);

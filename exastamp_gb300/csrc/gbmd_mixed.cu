@@ -341,7 +341,7 @@ __global__ void __launch_bounds__(256, 4) k_lj_mixed(PairArgs A, LJF P, const LJ
   __shared__ LJTabSmem t;
   if (MULTI) lj_load_table(t, tab, ntypes);
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = gt / T;
+  const int64_t i = A.i0 + gt / T;
   lj_atom<T, V, EV, MULTI>(A, P, t, ntypes, rcmax2, i, (int)(gt % T), i < A.n, GlobalFetch{A.posf});
 }
 
@@ -477,7 +477,7 @@ template <int T, int V, bool EV, bool SINGLE>
 __global__ void __launch_bounds__(256) k_eam_rho_mixed(PairArgs A, EamDev E, float* __restrict__ fpf,
                                                        float* __restrict__ epf, float4* __restrict__ pfp) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = gt / T;
+  const int64_t i = A.i0 + gt / T;
   eam_rho_atom<T, V, EV, SINGLE>(A, E, fpf, epf, pfp, i, (int)(gt % T), i < A.n, GlobalFetch{A.posf});
 }
 
@@ -617,7 +617,7 @@ __global__ void __launch_bounds__(256, 4) k_eam_force_mixed(PairArgs A, EamDev E
                                                          const float* __restrict__ epf,
                                                          const float4* __restrict__ pfp) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = gt / T;
+  const int64_t i = A.i0 + gt / T;
   eam_force_atom<T, V, EV, SINGLE>(A, E, fpf, epf, i, (int)(gt % T), i < A.n,
                                    GlobalFetch{SINGLE ? pfp : A.posf});
 }
@@ -781,9 +781,9 @@ static int launch_newton3(gbmd_context* c, const PairArgs& A, int part) {
 template <int T, int V, bool EV>
 static void launch_mixed_TV(gbmd_context* c, const PairArgs& A, int part) {
   const int B = c->block;
-  const unsigned grid = (unsigned)((A.n * T + B - 1) / B);
+  const unsigned grid = (unsigned)(((A.n - A.i0) * T + B - 1) / B);
   const int Bd = c->block_rho ? c->block_rho : B;  // density kernels
-  const unsigned gridd = (unsigned)((A.n * T + Bd - 1) / Bd);
+  const unsigned gridd = (unsigned)(((A.n - A.i0) * T + Bd - 1) / Bd);
   cudaStream_t s = c->stream;
   if (c->pot == GBMD_POT_LJ) {
     if (part == 1) return;

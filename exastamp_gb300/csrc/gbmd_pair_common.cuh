@@ -19,7 +19,8 @@
 namespace gbmd {
 
 struct PairArgs {
-  int64_t n;
+  int64_t n;                  // atoms [i0, n) are processed (a piece of the cell order, or all)
+  int64_t i0;
   int64_t stride;             // npad * W (words per list row)
   int W, wsh;                 // words per atom per row (lanes x entries per lane), log2 W
   const uint32_t* nbr;
@@ -34,6 +35,7 @@ struct PairArgs {
   float4* posf_o;
   double4_32a* posd_o;
   double *vx, *vy, *vz, *ax, *ay, *az;
+  double *vxo, *vyo, *vzo;    // velocities after the fused halves (vx.. in place, or another buffer)
   double* ep;
   double* ep_emb;             // FP64 EAM: embedding energy F(rho_i) from the density pass
   double* vir;
@@ -137,9 +139,9 @@ __device__ __forceinline__ void atom_epilogue(const PairArgs& A, int64_t i, int 
                                 (float)(z - (double)cz * A.g.h[2] - A.g.lo[2]), __int_as_float(t));
       A.posd_o[i] = make_double4_32a(x, y, z, (double)t);
     }
-    A.vx[i] = vx;
-    A.vy[i] = vy;
-    A.vz[i] = vz;
+    A.vxo[i] = vx;
+    A.vyo[i] = vy;
+    A.vzo[i] = vz;
   }
 }
 

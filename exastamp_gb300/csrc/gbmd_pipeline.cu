@@ -1,0 +1,335 @@
+// gbmd_pipeline.cu -- one gbmd_run_nve_host step with the host link
+// overlapped with the pair passes.
+//
+// The caller's page-locked r, v, a (caller order) are read over the host link
+// in P chunks of the caller order on the input stream; each chunk's first
+// half (k_host_first_half, verlet_first_half's formulas) is applied as it
+// arrives, and its pushed positions go straight back to the caller's arrays.
+// The cell-sorted atoms are cut into S slabs of whole z layers of the cell
+// grid (P = S).  Cells are at least rcut + skin wide, so a slab's density
+// pass (or the single pass of a pair potential) reads the positions of its
+// own and the two neighbouring slabs only, and its force pass the densities
+// of the same three slabs; the output of a caller chunk (v, a) needs the
+// force pass of every slab holding one of its atoms.  A map kernel, run once
+// per neighbour-list build, records for every slab the last caller chunk
+// holding one of its atoms and for every chunk the set of slabs holding its
+// atoms.  From these the host issues each slab's passes on the compute stream
+// right after the input chunk that completes their neighbourhood, and each
+// chunk's output on the output stream right after the force pass that
+// completes it.  When the caller's order follows the cell order along z
+// (exaNBody's grids store atoms cell by cell, z slowest) slab s waits for
+// chunks s-1..s+1 only and the three streams overlap; any other order gives
+// a more serial schedule and the same results: every atom runs the same
+// kernels on the same data whatever the pieces.
+//
+// The force pieces write v(t+dt) into the spare velocity buffer, so that
+// v(t+dt/2) stays in place until the step is known to need no rebuild: the
+// input pieces test every atom against skin/2 as they push it, and a gated
+// copy moves v(t+dt) into place only when none moved that far.  Otherwise
+// the caller finishes the step without the pipeline after a rebuild, from
+// the pushed state (the caller's arrays are all rewritten then).
+#include "gbmd_internal.cuh"
+
+namespace gbmd {
+
+namespace {
+
+constexpr int MAX_SLABS = 64;
+// layout of the slab-map scratch (ints)
+constexpr int OFF_ZSLAB = 0;      // slab of each z layer (<= 1024 layers)
+constexpr int OFF_ZB = 1024;      // first z layer of each slab, S + 1
+constexpr int OFF_NEED = 1096;    // per slab: last caller chunk of its atoms (-1: empty)
+constexpr int OFF_BEGIN = 1160;   // per slab: first cell-order atom, S + 1
+constexpr int OFF_MASK = 1232;    // per chunk: 64-bit slab set (8-byte aligned)
+constexpr int SCRATCH_INTS = 1536;
+
+inline int64_t chunk_begin(int64_t n, int P, int k) { return ((int64_t)k * n + P - 1) / P; }
+
+__global__ void k_pipe_map(int64_t n, int P, const int32_t* __restrict__ cellpack, const int32_t* __restrict__ user,
+                           const int32_t* __restrict__ zslab, int* __restrict__ need,
+                           unsigned long long* __restrict__ mask) {
+  __shared__ int sh_need[MAX_SLABS];
+  __shared__ unsigned long long sh_mask[MAX_SLABS];
+  for (int q = threadIdx.x; q < MAX_SLABS; q += blockDim.x) {
+    sh_need[q] = -1;
+    sh_mask[q] = 0ull;
+  }
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int s = zslab[cellpack[i] >> 20];
+    // chunk k holds caller indices [ceil(k n / P), ceil((k+1) n / P))
+    const int k = (int)((int64_t)user[i] * P / n);
+    atomicMax(&sh_need[s], k);
+    atomicOr(&sh_mask[k], 1ull << s);
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < MAX_SLABS; q += blockDim.x) {
+    if (sh_need[q] >= 0) atomicMax(&need[q], sh_need[q]);
+    if (sh_mask[q]) atomicOr(&mask[q], sh_mask[q]);
+  }
+}
+
+__global__ void k_pipe_bounds(const int32_t* __restrict__ cstart, const int32_t* __restrict__ zb, int S,
+                              int64_t nxy, int* __restrict__ begin) {
+  const int s = threadIdx.x;
+  if (s <= S) begin[s] = cstart[(int64_t)zb[s] * nxy];
+}
+
+struct HostOut6 {
+  double* a[6];
+};
+
+// v(t+dt) and a(t+dt) of caller indices [u0, u1) into the caller's arrays.
+__global__ void k_pipe_out(int64_t u0, int64_t u1, const int32_t* __restrict__ inv, const double* __restrict__ v,
+                           const double* __restrict__ a, int64_t cap, HostOut6 out) {
+  for (int64_t u = u0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < u1;
+       u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = inv[u];
+    const double q0 = v[i], q1 = v[cap + i], q2 = v[2 * cap + i];
+    const double q3 = a[i], q4 = a[cap + i], q5 = a[2 * cap + i];
+    out.a[0][u] = q0;
+    out.a[1][u] = q1;
+    out.a[2][u] = q2;
+    out.a[3][u] = q3;
+    out.a[4][u] = q4;
+    out.a[5][u] = q5;
+  }
+}
+
+// v(t+dt) into place unless the displacement gate is raised.
+__global__ void k_copy_v_gated(int64_t n, int64_t cap, const double* __restrict__ src, double* __restrict__ dst,
+                               const int* __restrict__ gate) {
+  if (*gate) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    dst[i] = src[i];
+    dst[cap + i] = src[cap + i];
+    dst[2 * cap + i] = src[2 * cap + i];
+  }
+}
+
+int ensure_pipe(gbmd_context* c) {
+  if (c->pipe_in) return GBMD_OK;
+  int least = 0, greatest = 0;
+  GBMD_CUDA(c, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  GBMD_CUDA(c, cudaStreamCreateWithPriority(&c->pipe_in, cudaStreamNonBlocking, greatest));
+  GBMD_CUDA(c, cudaStreamCreateWithPriority(&c->pipe_out, cudaStreamNonBlocking, greatest));
+  for (int q = 0; q + 1 < PIPE_STREAMS; ++q)
+    GBMD_CUDA(c, cudaStreamCreateWithFlags(&c->pipe_cs[q], cudaStreamNonBlocking));
+  GBMD_CUDA(c, cudaEventCreateWithFlags(&c->pipe_start, cudaEventDisableTiming));
+  GBMD_CUDA(c, cudaEventCreateWithFlags(&c->pipe_out_done, cudaEventDisableTiming));
+  for (int k = 0; k < MAX_SLABS; ++k) {
+    GBMD_CUDA(c, cudaEventCreateWithFlags(&c->pipe_in_ev[k], cudaEventDisableTiming));
+    GBMD_CUDA(c, cudaEventCreateWithFlags(&c->pipe_f_ev[k], cudaEventDisableTiming));
+    GBMD_CUDA(c, cudaEventCreateWithFlags(&c->pipe_d_ev[k], cudaEventDisableTiming));
+  }
+  GBMD_CUDA(c, cudaMalloc(&c->pipe_dev, sizeof(int) * SCRATCH_INTS));
+  GBMD_CUDA(c, cudaMallocHost(&c->pipe_host, sizeof(int) * SCRATCH_INTS));
+  return GBMD_OK;
+}
+
+// The slab map of the current cell order (stream synchronised).
+int pipe_schedule(gbmd_context* c, int S) {
+  const int P = S;
+  const int64_t n = c->n;
+  const int nz = c->grid.nc[2];
+  const int64_t nxy = (int64_t)c->grid.nc[0] * c->grid.nc[1];
+  int* h = c->pipe_host;
+  int* d = c->pipe_dev;
+  for (int s = 0; s <= S; ++s) h[OFF_ZB + s] = (int)((int64_t)s * nz / S);
+  for (int s = 0; s < S; ++s)
+    for (int z = h[OFF_ZB + s]; z < h[OFF_ZB + s + 1]; ++z) h[OFF_ZSLAB + z] = s;
+  cudaStream_t m = c->stream;
+  GBMD_CUDA(c, cudaMemcpyAsync(d, h, sizeof(int) * OFF_NEED, cudaMemcpyHostToDevice, m));
+  GBMD_CUDA(c, cudaMemsetAsync(d + OFF_NEED, 0xff, sizeof(int) * MAX_SLABS, m));
+  GBMD_CUDA(c, cudaMemsetAsync(d + OFF_MASK, 0, sizeof(unsigned long long) * MAX_SLABS, m));
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 8LL * c->nsm) blocks = 8LL * c->nsm;
+  if (blocks < 1) blocks = 1;
+  k_pipe_map<<<(unsigned)blocks, 256, 0, m>>>(n, P, c->cellpack, c->USER(), d + OFF_ZSLAB, d + OFF_NEED,
+                                              reinterpret_cast<unsigned long long*>(d + OFF_MASK));
+  k_pipe_bounds<<<1, 128, 0, m>>>(c->cell_start, d + OFF_ZB, S, nxy, d + OFF_BEGIN);
+  GBMD_CUDA(c, cudaMemcpyAsync(h + OFF_NEED, d + OFF_NEED, sizeof(int) * (SCRATCH_INTS - OFF_NEED),
+                               cudaMemcpyDeviceToHost, m));
+  GBMD_CUDA(c, cudaStreamSynchronize(m));
+  const int* need = h + OFF_NEED;
+  const unsigned long long* mask = reinterpret_cast<const unsigned long long*>(h + OFF_MASK);
+  c->pipe_need.assign(S, 0);
+  c->pipe_mask.assign(P, 0);
+  c->pipe_begin.assign(S + 1, 0);
+  for (int s = 0; s < S; ++s) {
+    int m3 = need[s];
+    m3 = need[(s + S - 1) % S] > m3 ? need[(s + S - 1) % S] : m3;
+    m3 = need[(s + 1) % S] > m3 ? need[(s + 1) % S] : m3;
+    c->pipe_need[s] = m3 < 0 ? 0 : m3;
+  }
+  for (int k = 0; k < P; ++k) c->pipe_mask[k] = mask[k];
+  for (int s = 0; s <= S; ++s) c->pipe_begin[s] = h[OFF_BEGIN + s];
+  if (c->pipe_begin[0] != 0 || c->pipe_begin[S] != n)
+    return set_error(c, GBMD_ERR_CUDA, "slab map: cell ranges [%lld, %lld) for %lld atoms",
+                     (long long)c->pipe_begin[0], (long long)c->pipe_begin[S], (long long)n);
+  c->pipe_key_builds = c->list_builds;
+  c->pipe_key_n = n;
+  c->pipe_key_slabs = S;
+  return GBMD_OK;
+}
+
+}  // namespace
+
+int pipe_slabs_for(const gbmd_context* c) {
+  if (c->pipe_slabs == 0 || c->newton3 || c->staged || !c->grid_valid || !c->list_valid || c->n == 0) return 0;
+  int S = c->pipe_slabs;
+  if (S < 0) {
+    // below a quarter million atoms the launches of the pieces cost more
+    // than the overlap saves
+    if (c->n < (1 << 18)) return 0;
+    S = 16;
+  }
+  if (S > MAX_SLABS) S = MAX_SLABS;
+  if (S > c->grid.nc[2]) S = c->grid.nc[2];
+  return S >= 4 ? S : 0;
+}
+
+// Launches of launch_forces on another stream of the context.
+struct StreamScope {
+  gbmd_context* c;
+  cudaStream_t saved;
+  StreamScope(gbmd_context* ctx, cudaStream_t s) : c(ctx), saved(ctx->stream) { c->stream = s; }
+  ~StreamScope() { c->stream = saved; }
+};
+
+int pipe_step(gbmd_context* c, double dt, const double* const host[9], const int32_t* inv, int S) {
+  int rc = ensure_pipe(c);
+  if (rc) return rc;
+  if (c->pipe_key_builds != c->list_builds || c->pipe_key_n != c->n || c->pipe_key_slabs != S) {
+    if ((rc = pipe_schedule(c, S))) return rc;
+  }
+  const int P = S;
+  const int64_t n = c->n;
+  // compute pieces go round-robin over PIPE_STREAMS streams (the context's
+  // own first), ordered by events only, so that independent pieces run side
+  // by side and one piece's last wave overlaps the next pieces
+  cudaStream_t m = c->stream;
+  cudaStream_t pool[PIPE_STREAMS];
+  pool[0] = m;
+  for (int q = 1; q < PIPE_STREAMS; ++q) pool[q] = c->pipe_cs[q - 1];
+  int next = 0;
+  auto take = [&]() { const cudaStream_t st = pool[next]; next = (next + 1) % PIPE_STREAMS; return st; };
+  const bool two_pass = c->pot == GBMD_POT_EAM_ALLOY || c->pot == GBMD_POT_EAM_JOHNSON;
+  double* v_spare = c->vbuf[c->cur_s ^ 1];
+  GBMD_CUDA(c, cudaEventRecord(c->pipe_start, m));
+  GBMD_CUDA(c, cudaStreamWaitEvent(c->pipe_in, c->pipe_start, 0));
+  GBMD_CUDA(c, cudaStreamWaitEvent(c->pipe_out, c->pipe_start, 0));
+  for (int q = 1; q < PIPE_STREAMS; ++q) GBMD_CUDA(c, cudaStreamWaitEvent(pool[q], c->pipe_start, 0));
+  for (int k = 0; k < P; ++k) {
+    launch_host_first_half_range(c, host, inv, dt, chunk_begin(n, P, k), chunk_begin(n, P, k + 1), true,
+                                 c->pipe_link_blocks, c->pipe_link_threads, c->pipe_in);
+    GBMD_CUDA(c, cudaEventRecord(c->pipe_in_ev[k], c->pipe_in));
+  }
+  ForceFlags f;
+  f.fuse = FUSE_PUSH2;
+  f.sp.dt = dt;
+  f.sp.dth = dt * 0.5;
+  f.sp.dt2h = dt * dt * 0.5;
+  f.v_out = v_spare;
+  HostOut6 out;
+  for (int q = 0; q < 6; ++q) out.a[q] = const_cast<double*>(host[3 + q]);
+  std::vector<char> dens(S, 0), forced(S, 0), outd(P, 0);
+  uint64_t forced_mask = 0;
+  for (int k = 0; k < P; ++k)
+    if (chunk_begin(n, P, k) == chunk_begin(n, P, k + 1)) outd[k] = 1;
+  auto piece = [&](int s, int part, cudaStream_t st) -> int {
+    ForceFlags g = f;
+    g.part = part;
+    g.i0 = c->pipe_begin[s];
+    g.i1 = c->pipe_begin[s + 1];
+    if (g.i1 <= g.i0) return GBMD_OK;
+    const StreamScope on(c, st);
+    return launch_forces(c, g);
+  };
+  auto force_piece = [&](int s) -> int {
+    const cudaStream_t st = take();
+    if (two_pass) {
+      for (int d = -1; d <= 1; ++d) GBMD_CUDA(c, cudaStreamWaitEvent(st, c->pipe_d_ev[(s + d + S) % S], 0));
+    } else {
+      GBMD_CUDA(c, cudaStreamWaitEvent(st, c->pipe_in_ev[c->pipe_need[s]], 0));
+    }
+    int r = piece(s, 2, st);
+    if (r) return r;
+    forced[s] = 1;
+    forced_mask |= 1ull << s;
+    GBMD_CUDA(c, cudaEventRecord(c->pipe_f_ev[s], st));
+    bool waited = false;
+    for (int k = 0; k < P; ++k) {
+      if (outd[k] || (c->pipe_mask[k] & ~forced_mask)) continue;
+      if (!waited) GBMD_CUDA(c, cudaStreamWaitEvent(c->pipe_out, c->pipe_f_ev[s], 0));
+      waited = true;
+      // the chunk's other slabs were issued earlier: on the other compute
+      // stream they may still run
+      for (int q = 0; q < S; ++q)
+        if (q != s && ((c->pipe_mask[k] >> q) & 1)) GBMD_CUDA(c, cudaStreamWaitEvent(c->pipe_out, c->pipe_f_ev[q], 0));
+      const int64_t u0 = chunk_begin(n, P, k), u1 = chunk_begin(n, P, k + 1);
+      const int T = c->pipe_link_threads;
+      const int64_t need = (u1 - u0 + T - 1) / T;
+      k_pipe_out<<<(unsigned)(need < c->pipe_link_blocks ? need : c->pipe_link_blocks), T, 0, c->pipe_out>>>(
+          u0, u1, inv, v_spare, c->AX(), c->cap, out);
+      outd[k] = 1;
+    }
+    return GBMD_OK;
+  };
+  for (int k = 0; k < P; ++k) {
+    for (int s = 0; s < S; ++s) {
+      if (c->pipe_need[s] != k) continue;
+      if (two_pass) {
+        const cudaStream_t st = take();
+        GBMD_CUDA(c, cudaStreamWaitEvent(st, c->pipe_in_ev[k], 0));
+        if ((rc = piece(s, 1, st))) return rc;
+        GBMD_CUDA(c, cudaEventRecord(c->pipe_d_ev[s], st));
+        dens[s] = 1;
+      } else if ((rc = force_piece(s))) {
+        return rc;
+      }
+    }
+    if (!two_pass) continue;
+    for (int s = 0; s < S; ++s)
+      if (!forced[s] && dens[(s + S - 1) % S] && dens[s] && dens[(s + 1) % S] && (rc = force_piece(s))) return rc;
+  }
+  for (int s = 0; s < S; ++s)
+    if (!forced[s]) return set_error(c, GBMD_ERR_CUDA, "pipeline: slab %d never issued", s);
+  for (int k = 0; k < P; ++k)
+    if (!outd[k]) return set_error(c, GBMD_ERR_CUDA, "pipeline: chunk %d never written", k);
+  // the gate is final once every chunk has been pushed; v(t+dt) is complete
+  // once every force piece has run
+  GBMD_CUDA(c, cudaStreamWaitEvent(m, c->pipe_in_ev[P - 1], 0));
+  for (int s = 0; s < S; ++s) GBMD_CUDA(c, cudaStreamWaitEvent(m, c->pipe_f_ev[s], 0));
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 4LL * c->nsm) blocks = 4LL * c->nsm;
+  if (blocks < 1) blocks = 1;
+  k_copy_v_gated<<<(unsigned)blocks, 256, 0, m>>>(n, c->cap, v_spare, c->VX(), c->d_err + ERRW_GATE);
+  GBMD_CUDA(c, cudaEventRecord(c->pipe_out_done, c->pipe_out));
+  GBMD_CUDA(c, cudaStreamWaitEvent(m, c->pipe_out_done, 0));
+  GBMD_CUDA(c, cudaGetLastError());
+  GBMD_CUDA(c, cudaStreamSynchronize(m));
+  return GBMD_OK;
+}
+
+void pipe_free(gbmd_context* c) {
+  if (c->pipe_in) cudaStreamDestroy(c->pipe_in);
+  if (c->pipe_out) cudaStreamDestroy(c->pipe_out);
+  for (int q = 0; q + 1 < PIPE_STREAMS; ++q) {
+    if (c->pipe_cs[q]) cudaStreamDestroy(c->pipe_cs[q]);
+    c->pipe_cs[q] = nullptr;
+  }
+  if (c->pipe_start) cudaEventDestroy(c->pipe_start);
+  if (c->pipe_out_done) cudaEventDestroy(c->pipe_out_done);
+  for (int k = 0; k < MAX_SLABS; ++k) {
+    if (c->pipe_in_ev[k]) cudaEventDestroy(c->pipe_in_ev[k]);
+    if (c->pipe_f_ev[k]) cudaEventDestroy(c->pipe_f_ev[k]);
+    if (c->pipe_d_ev[k]) cudaEventDestroy(c->pipe_d_ev[k]);
+  }
+  if (c->pipe_dev) cudaFree(c->pipe_dev);
+  if (c->pipe_host) cudaFreeHost(c->pipe_host);
+  c->pipe_in = c->pipe_out = nullptr;
+  c->pipe_dev = c->pipe_host = nullptr;
+}
+
+}  // namespace gbmd

@@ -73,6 +73,21 @@ def lattice(nx: int, ny: int, nz: int, a, basis: np.ndarray):
     return pos, np.zeros(3), hi
 
 
+def grid_order(s: System, R: float) -> System:
+    """The same atoms stored cell by cell in cells at least R wide, cell
+    index (k ny + j) nx + i (z slowest), as an exaNBody grid holds them: a
+    contiguous chunk of the arrays is then a slab of the box along z."""
+    L = s.hi - s.lo
+    nc = np.maximum(np.floor(L / R), 1).astype(np.int64)
+    c = [np.clip(((a - lo) * (m / Ld)).astype(np.int64), 0, m - 1)
+         for a, lo, Ld, m in zip((s.x, s.y, s.z), s.lo, L, nc)]
+    perm = np.argsort((c[2] * nc[1] + c[1]) * nc[0] + c[0], kind="stable")
+    for k in ("x", "y", "z", "vx", "vy", "vz", "type", "id"):
+        setattr(s, k, np.ascontiguousarray(getattr(s, k)[perm]))
+    s.meta = dict(s.meta, order="grid cells of %g, z slowest" % R)
+    return s
+
+
 def maxwell_boltzmann(masses_per_atom: np.ndarray, T: float, kB: float, rng: np.random.Generator):
     """init_temperature_new restated: Gaussian draws, remove v_cm, scale to T."""
     n = len(masses_per_atom)

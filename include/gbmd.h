@@ -253,9 +253,34 @@ int gbmd_run_nve(gbmd_context* ctx, int nsteps, double dt, int rebuild_every, in
  * a rebuild (check_and_update_particles after verlet_first_half); other
  * arrays go through gbmd_upload_state.  The positions of the last step are
  * final after its first half and go back to the host while its force pass
- * runs; v and a follow.  Returns once every array is written. */
+ * runs; v and a follow.  Returns once every array is written.
+ * One step (nsteps == 1) on page-locked arrays is pipelined when
+ * gbmd_set_host_pipeline allows it: the arrays are read in chunks of the
+ * caller order, the pair passes run slab by slab (whole z layers of the
+ * cell grid) as soon as the chunks holding their neighbourhood are in, and
+ * v, a of each chunk go back as soon as its slabs are done, so that the host
+ * link and the passes overlap; the results are those of the unpipelined
+ * step, bit for bit.  The overlap needs a caller order that follows the
+ * cell order along z (atoms stored cell by cell, z slowest, as exaNBody's
+ * grids hold them); another order gives a more serial schedule.  A step
+ * whose first half moves an atom more than skin/2 from its position at the
+ * last rebuild is finished without the pipeline after the rebuild. */
 int gbmd_run_nve_host(gbmd_context* ctx, int nsteps, double dt, int rebuild_every, double* rx, double* ry,
                       double* rz, double* vx, double* vy, double* vz, double* ax, double* ay, double* az);
+/* slabs: -1 automatic (16 slabs from 262,144 atoms up, else off; the
+ * default), 0 off, 4..64 that many slabs (at most one per z layer of the
+ * cell grid).  The pipeline is not used with Newton-3 half lists or staged
+ * neighbour positions. */
+int gbmd_set_host_pipeline(gbmd_context* ctx, int slabs);
+/* Launch shape of the pipeline's host-link pieces (the chunk reads with the
+ * first half, the v, a writes): grid-stride kernels of `blocks` blocks of
+ * `threads` threads (defaults 40 x 512), few enough to leave the SMs to the
+ * pair passes that run alongside. */
+int gbmd_set_host_pipeline_link(gbmd_context* ctx, int blocks, int threads);
+/* slabs the next host step would use (0: unpipelined) and the number of
+ * steps that stood as pipelined so far (a step that needed a rebuild is
+ * finished unpipelined and not counted). */
+int gbmd_get_host_pipeline(const gbmd_context* ctx, int* slabs, int64_t* steps);
 /* Minimiser: nsteps of compute forces + push_min (r += a dt^2/2, clipped);
  * rebuild_every as gbmd_run_nve. */
 int gbmd_run_minimize(gbmd_context* ctx, int nsteps, double dt, double tolF, int rebuild_every);
