@@ -98,7 +98,7 @@ def lib(path: str = LIB_PATH):
             "gbmd_lj_multi_loss_grad": ([vp, vp, vp, vp, vp, dbl, dbl, P(dbl), vp, vp], i32),
             "gbmd_list_builds": ([vp, P(i64)], i32),
             "gbmd_set_host_pipeline": ([vp, i32], i32),
-            "gbmd_set_host_pipeline_link": ([vp, i32, i32], i32),
+            "gbmd_set_host_pipeline_link": ([vp, i32, i32, i32], i32),
             "gbmd_get_host_pipeline": ([vp, P(i32), P(i64)], i32),
             "gbmd_thermo": ([vp, vp], i32),
             "gbmd_device_state": ([vp] + [vp] * 11, i32),
@@ -389,9 +389,9 @@ class Context:
         """gbmd_set_host_pipeline: -1 automatic, 0 off, 4..64 slabs."""
         self._chk(self._L.gbmd_set_host_pipeline(self.h, int(slabs)))
 
-    def set_host_pipeline_link(self, blocks, threads):
-        """gbmd_set_host_pipeline_link: launch shape of the host-link pieces."""
-        self._chk(self._L.gbmd_set_host_pipeline_link(self.h, int(blocks), int(threads)))
+    def set_host_pipeline_link(self, mode, blocks=40, threads=512):
+        """gbmd_set_host_pipeline_link: 0 copy engines, 1 kernels on the page-locked arrays."""
+        self._chk(self._L.gbmd_set_host_pipeline_link(self.h, int(mode), int(blocks), int(threads)))
 
     def host_pipeline(self):
         """(slabs the next host step would use, steps taken through the pipeline)."""

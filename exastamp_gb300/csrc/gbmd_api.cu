@@ -1401,7 +1401,7 @@ int gbmd_run_nve_host(gbmd_context* c, int nsteps, double dt, int rebuild_every,
       if (slabs) {
         // one step with the host link overlapped with the passes
         // (gbmd_pipeline.cu); it stands unless an atom moved more than skin/2
-        rc = pipe_step(c, dt, hdev, inverse_user(c), slabs);
+        rc = pipe_step(c, dt, host, hdev, inverse_user(c), slabs);
         if (rc) return rc;
       } else {
         launch_host_first_half(c, hdev, inverse_user(c), dt);
@@ -1450,8 +1450,10 @@ int gbmd_set_host_pipeline(gbmd_context* c, int slabs) {
   return GBMD_OK;
 }
 
-int gbmd_set_host_pipeline_link(gbmd_context* c, int blocks, int threads) {
-  if (!c || blocks < 1 || blocks > 65535 || threads < 32 || threads > 1024 || threads % 32) return GBMD_ERR_INVALID;
+int gbmd_set_host_pipeline_link(gbmd_context* c, int mode, int blocks, int threads) {
+  if (!c || mode < 0 || mode > 1 || blocks < 1 || blocks > 65535 || threads < 32 || threads > 1024 || threads % 32)
+    return GBMD_ERR_INVALID;
+  c->pipe_link_mode = mode;
   c->pipe_link_blocks = blocks;
   c->pipe_link_threads = threads;
   return GBMD_OK;

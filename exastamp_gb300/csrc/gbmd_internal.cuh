@@ -238,8 +238,12 @@ struct gbmd_context {
 
   // host-link pipeline of one gbmd_run_nve_host step (gbmd_pipeline.cu)
   int pipe_slabs = -1;          // -1 automatic, 0 off, >= 4: slabs (and caller-order chunks) per step
-  int pipe_link_blocks = 40, pipe_link_threads = 512;  // grid-stride shape of the host-link pieces
-  cudaStream_t pipe_in = nullptr, pipe_out = nullptr;
+  int pipe_link_mode = 1;       // 0: copy engines + staging in HBM; 1: kernels on the page-locked arrays
+  int pipe_link_blocks = 40, pipe_link_threads = 512;  // grid-stride shape of those kernels (mode 1)
+  double* pipe_stage = nullptr; // 9 x pipe_stage_cap: r, v, a of the step in caller order (mode 0)
+  int64_t pipe_stage_cap = 0;
+  cudaStream_t pipe_in = nullptr, pipe_out = nullptr, pipe_r = nullptr;
+  cudaEvent_t pipe_r_done = nullptr;
   cudaStream_t pipe_cs[3] = {nullptr, nullptr, nullptr};  // compute streams besides the context's
   cudaEvent_t pipe_start = nullptr, pipe_out_done = nullptr;
   cudaEvent_t pipe_in_ev[64] = {}, pipe_f_ev[64] = {}, pipe_d_ev[64] = {};
@@ -294,7 +298,9 @@ int launch_forces(gbmd_context* c, const ForceFlags& f);
 // synchronised at return (the displacement gate is left in the error word)
 constexpr int PIPE_STREAMS = 4;
 int pipe_slabs_for(const gbmd_context* c);
-int pipe_step(gbmd_context* c, double dt, const double* const host[9], const int32_t* inv, int slabs);
+// host: the caller's arrays; hdev: their device addresses (page-locked)
+int pipe_step(gbmd_context* c, double dt, const double* const host[9], const double* const hdev[9],
+              const int32_t* inv, int slabs);
 void pipe_free(gbmd_context* c);
 
 // integration (gbmd_integrate.cu)

@@ -6,7 +6,10 @@
 // half (k_host_first_half, verlet_first_half's formulas) is applied as it
 // arrives, and its pushed positions go straight back to the caller's arrays.
 // The cell-sorted atoms are cut into S slabs of whole z layers of the cell
-// grid (P = S).  Cells are at least rcut + skin wide, so a slab's density
+// grid, and the caller order into as many chunks of equal atom counts.
+// (Chunks cut at the slabs' atom counts, so that chunk k holds slab k's
+// atoms, were measured 18 % slower at 4 M atoms.)  Cells are at least
+// rcut + skin wide, so a slab's density
 // pass (or the single pass of a pair potential) reads the positions of its
 // own and the two neighbouring slabs only, and its force pass the densities
 // of the same three slabs; the output of a caller chunk (v, a) needs the
@@ -113,6 +116,8 @@ int ensure_pipe(gbmd_context* c) {
   GBMD_CUDA(c, cudaDeviceGetStreamPriorityRange(&least, &greatest));
   GBMD_CUDA(c, cudaStreamCreateWithPriority(&c->pipe_in, cudaStreamNonBlocking, greatest));
   GBMD_CUDA(c, cudaStreamCreateWithPriority(&c->pipe_out, cudaStreamNonBlocking, greatest));
+  GBMD_CUDA(c, cudaStreamCreateWithPriority(&c->pipe_r, cudaStreamNonBlocking, greatest));
+  GBMD_CUDA(c, cudaEventCreateWithFlags(&c->pipe_r_done, cudaEventDisableTiming));
   for (int q = 0; q + 1 < PIPE_STREAMS; ++q)
     GBMD_CUDA(c, cudaStreamCreateWithFlags(&c->pipe_cs[q], cudaStreamNonBlocking));
   GBMD_CUDA(c, cudaEventCreateWithFlags(&c->pipe_start, cudaEventDisableTiming));
@@ -127,6 +132,15 @@ int ensure_pipe(gbmd_context* c) {
   return GBMD_OK;
 }
 
+// First z layer of each slab: equal shares of the nz layers (zb[0] = 0,
+// zb[S] = nz, every slab at least one layer).  Thinner slabs where the
+// periodic z ring closes (they wait for the last chunk) were measured
+// slower: the thicker chunks between them read slower under the concurrent
+// passes.
+void slab_layers(int nz, int S, int* zb) {
+  for (int s = 0; s <= S; ++s) zb[s] = (int)((int64_t)s * nz / S);
+}
+
 // The slab map of the current cell order (stream synchronised).
 int pipe_schedule(gbmd_context* c, int S) {
   const int P = S;
@@ -135,7 +149,8 @@ int pipe_schedule(gbmd_context* c, int S) {
   const int64_t nxy = (int64_t)c->grid.nc[0] * c->grid.nc[1];
   int* h = c->pipe_host;
   int* d = c->pipe_dev;
-  for (int s = 0; s <= S; ++s) h[OFF_ZB + s] = (int)((int64_t)s * nz / S);
+  slab_layers(nz, S, h + OFF_ZB);
+  if (h[OFF_ZB + S] != nz) return set_error(c, GBMD_ERR_CUDA, "slab layers: %d of %d", h[OFF_ZB + S], nz);
   for (int s = 0; s < S; ++s)
     for (int z = h[OFF_ZB + s]; z < h[OFF_ZB + s + 1]; ++z) h[OFF_ZSLAB + z] = s;
   cudaStream_t m = c->stream;
@@ -197,9 +212,21 @@ struct StreamScope {
   ~StreamScope() { c->stream = saved; }
 };
 
-int pipe_step(gbmd_context* c, double dt, const double* const host[9], const int32_t* inv, int S) {
+int pipe_step(gbmd_context* c, double dt, const double* const host[9], const double* const hdev[9],
+              const int32_t* inv, int S) {
   int rc = ensure_pipe(c);
   if (rc) return rc;
+  const bool ce = c->pipe_link_mode == 0;
+  if (ce && c->pipe_stage_cap < c->cap) {
+    if (c->pipe_stage) cudaFree(c->pipe_stage);
+    c->pipe_stage = nullptr;
+    c->pipe_stage_cap = 0;
+    GBMD_CUDA(c, cudaMalloc(&c->pipe_stage, sizeof(double) * 9 * c->cap));
+    c->pipe_stage_cap = c->cap;
+  }
+  const int64_t sc = c->pipe_stage_cap;
+  const double* stage[9];
+  for (int q = 0; q < 9; ++q) stage[q] = c->pipe_stage + q * sc;
   if (c->pipe_key_builds != c->list_builds || c->pipe_key_n != c->n || c->pipe_key_slabs != S) {
     if ((rc = pipe_schedule(c, S))) return rc;
   }
@@ -219,11 +246,35 @@ int pipe_step(gbmd_context* c, double dt, const double* const host[9], const int
   GBMD_CUDA(c, cudaEventRecord(c->pipe_start, m));
   GBMD_CUDA(c, cudaStreamWaitEvent(c->pipe_in, c->pipe_start, 0));
   GBMD_CUDA(c, cudaStreamWaitEvent(c->pipe_out, c->pipe_start, 0));
+  GBMD_CUDA(c, cudaStreamWaitEvent(c->pipe_r, c->pipe_start, 0));
   for (int q = 1; q < PIPE_STREAMS; ++q) GBMD_CUDA(c, cudaStreamWaitEvent(pool[q], c->pipe_start, 0));
+  const int dev_blocks = 2 * (c->nsm > 0 ? c->nsm : 1);
   for (int k = 0; k < P; ++k) {
-    launch_host_first_half_range(c, host, inv, dt, chunk_begin(n, P, k), chunk_begin(n, P, k + 1), true,
-                                 c->pipe_link_blocks, c->pipe_link_threads, c->pipe_in);
-    GBMD_CUDA(c, cudaEventRecord(c->pipe_in_ev[k], c->pipe_in));
+    const int64_t u0 = chunk_begin(n, P, k), u1 = chunk_begin(n, P, k + 1);
+    if (ce) {
+      // the copy engines carry the chunk into the staging arrays (caller
+      // order); the first half then runs from HBM and leaves r' in place,
+      // from where another copy engine returns it
+      const size_t bytes = sizeof(double) * (size_t)(u1 - u0);
+      if (bytes) {
+        for (int q = 0; q < 9; ++q)
+          GBMD_CUDA(c, cudaMemcpyAsync(const_cast<double*>(stage[q]) + u0, host[q] + u0, bytes,
+                                       cudaMemcpyHostToDevice, c->pipe_in));
+      }
+      launch_host_first_half_range(c, stage, inv, dt, u0, u1, true, dev_blocks, 256, c->pipe_in);
+      GBMD_CUDA(c, cudaEventRecord(c->pipe_in_ev[k], c->pipe_in));
+      if (bytes) {
+        GBMD_CUDA(c, cudaStreamWaitEvent(c->pipe_r, c->pipe_in_ev[k], 0));
+        for (int q = 0; q < 3; ++q)
+          GBMD_CUDA(c, cudaMemcpyAsync(const_cast<double*>(host[q]) + u0, stage[q] + u0, bytes,
+                                       cudaMemcpyDeviceToHost, c->pipe_r));
+      }
+    } else {
+      // kernels read the page-locked arrays over the link and write r' back
+      launch_host_first_half_range(c, hdev, inv, dt, u0, u1, true, c->pipe_link_blocks, c->pipe_link_threads,
+                                   c->pipe_in);
+      GBMD_CUDA(c, cudaEventRecord(c->pipe_in_ev[k], c->pipe_in));
+    }
   }
   ForceFlags f;
   f.fuse = FUSE_PUSH2;
@@ -232,7 +283,7 @@ int pipe_step(gbmd_context* c, double dt, const double* const host[9], const int
   f.sp.dt2h = dt * dt * 0.5;
   f.v_out = v_spare;
   HostOut6 out;
-  for (int q = 0; q < 6; ++q) out.a[q] = const_cast<double*>(host[3 + q]);
+  for (int q = 0; q < 6; ++q) out.a[q] = const_cast<double*>(ce ? stage[3 + q] : hdev[3 + q]);
   std::vector<char> dens(S, 0), forced(S, 0), outd(P, 0);
   uint64_t forced_mask = 0;
   for (int k = 0; k < P; ++k)
@@ -268,10 +319,17 @@ int pipe_step(gbmd_context* c, double dt, const double* const host[9], const int
       for (int q = 0; q < S; ++q)
         if (q != s && ((c->pipe_mask[k] >> q) & 1)) GBMD_CUDA(c, cudaStreamWaitEvent(c->pipe_out, c->pipe_f_ev[q], 0));
       const int64_t u0 = chunk_begin(n, P, k), u1 = chunk_begin(n, P, k + 1);
-      const int T = c->pipe_link_threads;
+      const int T = ce ? 256 : c->pipe_link_threads;
+      const int B = ce ? dev_blocks : c->pipe_link_blocks;
       const int64_t need = (u1 - u0 + T - 1) / T;
-      k_pipe_out<<<(unsigned)(need < c->pipe_link_blocks ? need : c->pipe_link_blocks), T, 0, c->pipe_out>>>(
-          u0, u1, inv, v_spare, c->AX(), c->cap, out);
+      k_pipe_out<<<(unsigned)(need < B ? need : B), T, 0, c->pipe_out>>>(u0, u1, inv, v_spare, c->AX(), c->cap, out);
+      if (ce) {
+        // v, a gathered into the staging arrays in caller order, then out
+        const size_t bytes = sizeof(double) * (size_t)(u1 - u0);
+        for (int q = 0; q < 6; ++q)
+          GBMD_CUDA(c, cudaMemcpyAsync(const_cast<double*>(host[3 + q]) + u0, stage[3 + q] + u0, bytes,
+                                       cudaMemcpyDeviceToHost, c->pipe_out));
+      }
       outd[k] = 1;
     }
     return GBMD_OK;
@@ -307,6 +365,8 @@ int pipe_step(gbmd_context* c, double dt, const double* const host[9], const int
   k_copy_v_gated<<<(unsigned)blocks, 256, 0, m>>>(n, c->cap, v_spare, c->VX(), c->d_err + ERRW_GATE);
   GBMD_CUDA(c, cudaEventRecord(c->pipe_out_done, c->pipe_out));
   GBMD_CUDA(c, cudaStreamWaitEvent(m, c->pipe_out_done, 0));
+  GBMD_CUDA(c, cudaEventRecord(c->pipe_r_done, c->pipe_r));
+  GBMD_CUDA(c, cudaStreamWaitEvent(m, c->pipe_r_done, 0));
   GBMD_CUDA(c, cudaGetLastError());
   GBMD_CUDA(c, cudaStreamSynchronize(m));
   return GBMD_OK;
@@ -315,6 +375,13 @@ int pipe_step(gbmd_context* c, double dt, const double* const host[9], const int
 void pipe_free(gbmd_context* c) {
   if (c->pipe_in) cudaStreamDestroy(c->pipe_in);
   if (c->pipe_out) cudaStreamDestroy(c->pipe_out);
+  if (c->pipe_r) cudaStreamDestroy(c->pipe_r);
+  if (c->pipe_r_done) cudaEventDestroy(c->pipe_r_done);
+  if (c->pipe_stage) cudaFree(c->pipe_stage);
+  c->pipe_r = nullptr;
+  c->pipe_r_done = nullptr;
+  c->pipe_stage = nullptr;
+  c->pipe_stage_cap = 0;
   for (int q = 0; q + 1 < PIPE_STREAMS; ++q) {
     if (c->pipe_cs[q]) cudaStreamDestroy(c->pipe_cs[q]);
     c->pipe_cs[q] = nullptr;

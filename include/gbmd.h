@@ -272,11 +272,13 @@ int gbmd_run_nve_host(gbmd_context* ctx, int nsteps, double dt, int rebuild_ever
  * cell grid).  The pipeline is not used with Newton-3 half lists or staged
  * neighbour positions. */
 int gbmd_set_host_pipeline(gbmd_context* ctx, int slabs);
-/* Launch shape of the pipeline's host-link pieces (the chunk reads with the
- * first half, the v, a writes): grid-stride kernels of `blocks` blocks of
- * `threads` threads (defaults 40 x 512), few enough to leave the SMs to the
- * pair passes that run alongside. */
-int gbmd_set_host_pipeline_link(gbmd_context* ctx, int blocks, int threads);
+/* How the pipeline moves the chunks over the host link.  mode 1 (the
+ * default): grid-stride kernels of `blocks` blocks of `threads` threads
+ * (40 x 512 by default) that read and write the page-locked arrays
+ * directly, few enough to leave the SMs to the pair passes.  mode 0: the
+ * copy engines, through staging arrays in HBM (9 doubles per atom; measured
+ * slower at 4 M atoms); blocks and threads are ignored. */
+int gbmd_set_host_pipeline_link(gbmd_context* ctx, int mode, int blocks, int threads);
 /* slabs the next host step would use (0: unpipelined) and the number of
  * steps that stood as pipelined so far (a step that needed a rebuild is
  * finished unpipelined and not counted). */

@@ -60,7 +60,7 @@ def _case(kind):
     raise ValueError(kind)
 
 
-def _host_steps(gpu, s, setpot, skin, dt, mixed, slabs):
+def _host_steps(gpu, s, setpot, skin, dt, mixed, slabs, link=1):
     torch = pytest.importorskip("torch")
     hist = []
     with gpu.Context(0) as ctx:
@@ -69,6 +69,7 @@ def _host_steps(gpu, s, setpot, skin, dt, mixed, slabs):
         ctx.set_skin(skin)
         ctx.set_precision(mixed)
         ctx.set_host_pipeline(slabs)
+        ctx.set_host_pipeline_link(link)
         ctx.compute_forces()
         start = ctx.download(KEYS)
         st = {}
@@ -85,13 +86,16 @@ def _host_steps(gpu, s, setpot, skin, dt, mixed, slabs):
     return hist, used, steps, builds
 
 
-@pytest.mark.parametrize("kind,order", [("lj", "cells"), ("lj", "random"), ("eam", "cells"), ("eam", "lattice"),
-                                        ("eam_fp64", "cells"), ("johnson", "cells"), ("lj_multi_fp64", "cells")])
-def test_pipelined_host_steps_equal_unpipelined(gpu, kind, order):
+@pytest.mark.parametrize("kind,order,link", [("lj", "cells", 1), ("lj", "random", 1), ("eam", "cells", 1),
+                                             ("eam", "lattice", 1), ("eam_fp64", "cells", 1), ("johnson", "cells", 1),
+                                             ("lj_multi_fp64", "cells", 1), ("eam", "cells", 0), ("lj", "random", 0)])
+def test_pipelined_host_steps_equal_unpipelined(gpu, kind, order, link):
+    """link 0: chunks carried by the copy engines through HBM staging;
+    link 1: kernels reading and writing the page-locked arrays."""
     s, setpot, rcut, skin, dt, mixed = _case(kind)
     s = _reorder(s, order, rcut + skin, 7)
     ref, used0, steps0, builds0 = _host_steps(gpu, s, setpot, skin, dt, mixed, 0)
-    got, used, steps, builds = _host_steps(gpu, s, setpot, skin, dt, mixed, 64)
+    got, used, steps, builds = _host_steps(gpu, s, setpot, skin, dt, mixed, 64, link)
     assert used0 == 0 and steps0 == 0
     assert used >= 4
     # the trigger fired on some steps (finished unpipelined), not on most
@@ -119,3 +123,6 @@ def test_pipeline_settings(gpu):
         for bad in (-2, 1, 3, 65):
             with pytest.raises(gpu.GbmdError):
                 ctx.set_host_pipeline(bad)
+        for bad in ((2, 40, 512), (1, 0, 512), (1, 40, 48), (1, 40, 2048)):
+            with pytest.raises(gpu.GbmdError):
+                ctx.set_host_pipeline_link(*bad)
