@@ -538,6 +538,22 @@ def e2e_section(ctx, s, w, R, steps, ws, torch, stream):
     slabs, piped0 = ctx.host_pipeline()
     mse, wall_ms, builds = loop(True)
     piped = ctx.host_pipeline()[1] - piped0
+    timeline = None
+    if slabs:
+        # one more (untimed) step with the pipeline's timeline recorded
+        ctx.set_host_pipeline_trace(True)
+        for k in KEYS9:
+            host[k][:] = start[k]
+        ctx.upload_state(*(host[k] for k in KEYS9))
+        ctx.build_neighbors()
+        ctx._chk(L.gbmd_run_nve_host(ctx.h, 1, dt, R, *[ptr(k) for k in KEYS9]))
+        ctx._chk(L.gbmd_run_nve_host(ctx.h, 1, dt, R, *[ptr(k) for k in KEYS9]))
+        marks = ctx.host_pipeline_trace()
+        ctx.set_host_pipeline_trace(False)
+        last = lambda kind: max((m[0] for m in marks if m[1] == kind), default=None)  # noqa: E731
+        timeline = {"ms_last_chunk_in": last("in"), "ms_last_density": last("density"),
+                    "ms_last_force": last("force"), "ms_last_chunk_out": last("out"), "ms_end": last("end"),
+                    "marks": [[round(m[0], 4), m[1], m[2]] for m in marks]}
     mse = dist_max(max(mse, wall_ms), ws)
     sep_ms = max(sep_ms, sep_wall)
     t0 = time.perf_counter()
@@ -553,7 +569,7 @@ def e2e_section(ctx, s, w, R, steps, ws, torch, stream):
             "h2d_bytes_per_step": 72 * n, "d2h_bytes_per_step": 72 * n, "steps": steps,
             "ms_per_step": mse / steps, "ms_per_step_as_three_calls": sep_ms / steps,
             "ms_per_step_unpipelined": max(unpiped_ms, unpiped_wall) / steps,
-            "list_builds": builds, "slabs": slabs, "pipelined_steps": piped,
+            "list_builds": builds, "slabs": slabs, "pipelined_steps": piped, "pipeline_timeline": timeline,
             "host_order": "grid cells, z slowest (as the reference's grid stores atoms)",
             "path": "gbmd_run_nve_host(1 step, pinned r,v,a): chunks of the caller order read over the host link "
                     "with the first half and skin/2 test applied, pair passes slab by slab as their chunks "

@@ -99,6 +99,8 @@ def lib(path: str = LIB_PATH):
             "gbmd_list_builds": ([vp, P(i64)], i32),
             "gbmd_set_host_pipeline": ([vp, i32], i32),
             "gbmd_set_host_pipeline_link": ([vp, i32, i32, i32], i32),
+            "gbmd_set_host_pipeline_trace": ([vp, i32], i32),
+            "gbmd_get_host_pipeline_trace": ([vp, i32, vp, vp, vp, P(i32)], i32),
             "gbmd_get_host_pipeline": ([vp, P(i32), P(i64)], i32),
             "gbmd_thermo": ([vp, vp], i32),
             "gbmd_device_state": ([vp] + [vp] * 11, i32),
@@ -392,6 +394,20 @@ class Context:
     def set_host_pipeline_link(self, mode, blocks=40, threads=512):
         """gbmd_set_host_pipeline_link: 0 copy engines, 1 kernels on the page-locked arrays."""
         self._chk(self._L.gbmd_set_host_pipeline_link(self.h, int(mode), int(blocks), int(threads)))
+
+    def set_host_pipeline_trace(self, on):
+        self._chk(self._L.gbmd_set_host_pipeline_trace(self.h, 1 if on else 0))
+
+    def host_pipeline_trace(self):
+        """Marks of the last pipelined host step: list of (ms, kind, index),
+        kind one of start, in, density, force, out, end."""
+        cnt = C.c_int(0)
+        self._chk(self._L.gbmd_get_host_pipeline_trace(self.h, 0, None, None, None, C.byref(cnt)))
+        n = cnt.value
+        t, k, i = np.zeros(n), np.zeros(n, np.int32), np.zeros(n, np.int32)
+        self._chk(self._L.gbmd_get_host_pipeline_trace(self.h, n, _p(t), _p(k), _p(i), C.byref(cnt)))
+        names = ("start", "in", "density", "force", "out", "end")
+        return [(float(t[q]), names[k[q]], int(i[q])) for q in range(n)]
 
     def host_pipeline(self):
         """(slabs the next host step would use, steps taken through the pipeline)."""

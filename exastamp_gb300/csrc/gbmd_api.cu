@@ -1459,6 +1459,18 @@ int gbmd_set_host_pipeline_link(gbmd_context* c, int mode, int blocks, int threa
   return GBMD_OK;
 }
 
+int gbmd_set_host_pipeline_trace(gbmd_context* c, int on) {
+  if (!c) return GBMD_ERR_INVALID;
+  c->pipe_trace = on != 0;
+  c->pipe_tr_n = 0;
+  return GBMD_OK;
+}
+
+int gbmd_get_host_pipeline_trace(gbmd_context* c, int cap, double* t_ms, int* kind, int* index, int* count) {
+  if (!c || cap < 0 || !count) return GBMD_ERR_INVALID;
+  return pipe_trace_read(c, cap, t_ms, kind, index, count);
+}
+
 int gbmd_get_host_pipeline(const gbmd_context* c, int* slabs, int64_t* steps) {
   if (!c) return GBMD_ERR_INVALID;
   if (slabs) *slabs = pipe_slabs_for(c);

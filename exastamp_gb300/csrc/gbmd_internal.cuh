@@ -255,6 +255,11 @@ struct gbmd_context {
   std::vector<uint64_t> pipe_mask;     // per caller chunk: slabs holding its atoms
   std::vector<int64_t> pipe_begin;     // slab s = cell-order atoms [begin[s], begin[s+1])
   int64_t pipe_steps = 0;              // steps that stood as pipelined (no rebuild due)
+  // timeline of the last pipelined step (gbmd_set_host_pipeline_trace)
+  bool pipe_trace = false;
+  std::vector<cudaEvent_t> pipe_tr_ev;
+  std::vector<int> pipe_tr_kind, pipe_tr_idx;
+  int pipe_tr_n = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -302,6 +307,8 @@ int pipe_slabs_for(const gbmd_context* c);
 int pipe_step(gbmd_context* c, double dt, const double* const host[9], const double* const hdev[9],
               const int32_t* inv, int slabs);
 void pipe_free(gbmd_context* c);
+// the last pipelined step's timeline marks (ms since its start)
+int pipe_trace_read(gbmd_context* c, int cap, double* t_ms, int* kind, int* index, int* count);
 
 // integration (gbmd_integrate.cu)
 void launch_push_f_v_r(gbmd_context* c, double dt, double dt_scale);

@@ -45,6 +45,7 @@ constexpr int OFF_NEED = 1096;    // per slab: last caller chunk of its atoms (-
 constexpr int OFF_BEGIN = 1160;   // per slab: first cell-order atom, S + 1
 constexpr int OFF_MASK = 1232;    // per chunk: 64-bit slab set (8-byte aligned)
 constexpr int SCRATCH_INTS = 1536;
+constexpr int TRACE_CAP = 4 * MAX_SLABS + 2;
 
 inline int64_t chunk_begin(int64_t n, int P, int k) { return ((int64_t)k * n + P - 1) / P; }
 
@@ -204,6 +205,24 @@ int pipe_slabs_for(const gbmd_context* c) {
   return S >= 4 ? S : 0;
 }
 
+// One mark of the step's timeline (gbmd_get_host_pipeline_trace): an event
+// with timing on `st` after the work issued there so far.
+int trace_mark(gbmd_context* c, cudaStream_t st, int kind, int idx) {
+  if (!c->pipe_trace) return GBMD_OK;
+  if (c->pipe_tr_ev.empty()) {
+    c->pipe_tr_ev.assign(TRACE_CAP, nullptr);
+    for (auto& e : c->pipe_tr_ev) GBMD_CUDA(c, cudaEventCreate(&e));
+    c->pipe_tr_kind.assign(TRACE_CAP, 0);
+    c->pipe_tr_idx.assign(TRACE_CAP, 0);
+  }
+  if (c->pipe_tr_n >= TRACE_CAP) return GBMD_OK;
+  GBMD_CUDA(c, cudaEventRecord(c->pipe_tr_ev[c->pipe_tr_n], st));
+  c->pipe_tr_kind[c->pipe_tr_n] = kind;
+  c->pipe_tr_idx[c->pipe_tr_n] = idx;
+  ++c->pipe_tr_n;
+  return GBMD_OK;
+}
+
 // Launches of launch_forces on another stream of the context.
 struct StreamScope {
   gbmd_context* c;
@@ -243,6 +262,8 @@ int pipe_step(gbmd_context* c, double dt, const double* const host[9], const dou
   auto take = [&]() { const cudaStream_t st = pool[next]; next = (next + 1) % PIPE_STREAMS; return st; };
   const bool two_pass = c->pot == GBMD_POT_EAM_ALLOY || c->pot == GBMD_POT_EAM_JOHNSON;
   double* v_spare = c->vbuf[c->cur_s ^ 1];
+  c->pipe_tr_n = 0;
+  if ((rc = trace_mark(c, m, GBMD_PIPE_MARK_START, -1))) return rc;
   GBMD_CUDA(c, cudaEventRecord(c->pipe_start, m));
   GBMD_CUDA(c, cudaStreamWaitEvent(c->pipe_in, c->pipe_start, 0));
   GBMD_CUDA(c, cudaStreamWaitEvent(c->pipe_out, c->pipe_start, 0));
@@ -263,6 +284,7 @@ int pipe_step(gbmd_context* c, double dt, const double* const host[9], const dou
       }
       launch_host_first_half_range(c, stage, inv, dt, u0, u1, true, dev_blocks, 256, c->pipe_in);
       GBMD_CUDA(c, cudaEventRecord(c->pipe_in_ev[k], c->pipe_in));
+      if ((rc = trace_mark(c, c->pipe_in, GBMD_PIPE_MARK_CHUNK_IN, k))) return rc;
       if (bytes) {
         GBMD_CUDA(c, cudaStreamWaitEvent(c->pipe_r, c->pipe_in_ev[k], 0));
         for (int q = 0; q < 3; ++q)
@@ -274,6 +296,7 @@ int pipe_step(gbmd_context* c, double dt, const double* const host[9], const dou
       launch_host_first_half_range(c, hdev, inv, dt, u0, u1, true, c->pipe_link_blocks, c->pipe_link_threads,
                                    c->pipe_in);
       GBMD_CUDA(c, cudaEventRecord(c->pipe_in_ev[k], c->pipe_in));
+      if ((rc = trace_mark(c, c->pipe_in, GBMD_PIPE_MARK_CHUNK_IN, k))) return rc;
     }
   }
   ForceFlags f;
@@ -309,6 +332,7 @@ int pipe_step(gbmd_context* c, double dt, const double* const host[9], const dou
     forced[s] = 1;
     forced_mask |= 1ull << s;
     GBMD_CUDA(c, cudaEventRecord(c->pipe_f_ev[s], st));
+    if ((r = trace_mark(c, st, GBMD_PIPE_MARK_FORCE, s))) return r;
     bool waited = false;
     for (int k = 0; k < P; ++k) {
       if (outd[k] || (c->pipe_mask[k] & ~forced_mask)) continue;
@@ -331,6 +355,7 @@ int pipe_step(gbmd_context* c, double dt, const double* const host[9], const dou
                                        cudaMemcpyDeviceToHost, c->pipe_out));
       }
       outd[k] = 1;
+      if ((r = trace_mark(c, c->pipe_out, GBMD_PIPE_MARK_CHUNK_OUT, k))) return r;
     }
     return GBMD_OK;
   };
@@ -342,6 +367,7 @@ int pipe_step(gbmd_context* c, double dt, const double* const host[9], const dou
         GBMD_CUDA(c, cudaStreamWaitEvent(st, c->pipe_in_ev[k], 0));
         if ((rc = piece(s, 1, st))) return rc;
         GBMD_CUDA(c, cudaEventRecord(c->pipe_d_ev[s], st));
+        if ((rc = trace_mark(c, st, GBMD_PIPE_MARK_DENSITY, s))) return rc;
         dens[s] = 1;
       } else if ((rc = force_piece(s))) {
         return rc;
@@ -367,12 +393,29 @@ int pipe_step(gbmd_context* c, double dt, const double* const host[9], const dou
   GBMD_CUDA(c, cudaStreamWaitEvent(m, c->pipe_out_done, 0));
   GBMD_CUDA(c, cudaEventRecord(c->pipe_r_done, c->pipe_r));
   GBMD_CUDA(c, cudaStreamWaitEvent(m, c->pipe_r_done, 0));
+  if ((rc = trace_mark(c, m, GBMD_PIPE_MARK_END, -1))) return rc;
   GBMD_CUDA(c, cudaGetLastError());
   GBMD_CUDA(c, cudaStreamSynchronize(m));
   return GBMD_OK;
 }
 
+int pipe_trace_read(gbmd_context* c, int cap, double* t_ms, int* kind, int* index, int* count) {
+  const int n = c->pipe_tr_n;
+  *count = n;
+  for (int i = 0; i < n && i < cap; ++i) {
+    float ms = 0.f;
+    GBMD_CUDA(c, cudaEventElapsedTime(&ms, c->pipe_tr_ev[0], c->pipe_tr_ev[i]));
+    if (t_ms) t_ms[i] = ms;
+    if (kind) kind[i] = c->pipe_tr_kind[i];
+    if (index) index[i] = c->pipe_tr_idx[i];
+  }
+  return GBMD_OK;
+}
+
 void pipe_free(gbmd_context* c) {
+  for (auto& e : c->pipe_tr_ev)
+    if (e) cudaEventDestroy(e);
+  c->pipe_tr_ev.clear();
   if (c->pipe_in) cudaStreamDestroy(c->pipe_in);
   if (c->pipe_out) cudaStreamDestroy(c->pipe_out);
   if (c->pipe_r) cudaStreamDestroy(c->pipe_r);

@@ -279,6 +279,22 @@ int gbmd_set_host_pipeline(gbmd_context* ctx, int slabs);
  * copy engines, through staging arrays in HBM (9 doubles per atom; measured
  * slower at 4 M atoms); blocks and threads are ignored. */
 int gbmd_set_host_pipeline_link(gbmd_context* ctx, int mode, int blocks, int threads);
+/* Timeline of the last pipelined host step, the analogue of onika's
+ * per-operator timers for it: with tracing on, each step records CUDA
+ * events on its streams; gbmd_get_host_pipeline_trace returns up to `cap`
+ * marks of the last step as t_ms (milliseconds since the step's start),
+ * kind (GBMD_PIPE_MARK_*) and index (the chunk or slab), and their number
+ * in *count.  Tracing adds one event record per mark. */
+enum {
+  GBMD_PIPE_MARK_START = 0,
+  GBMD_PIPE_MARK_CHUNK_IN = 1,    /* caller chunk read, first half applied */
+  GBMD_PIPE_MARK_DENSITY = 2,     /* slab's density (embedding) pass done */
+  GBMD_PIPE_MARK_FORCE = 3,       /* slab's force pass done */
+  GBMD_PIPE_MARK_CHUNK_OUT = 4,   /* caller chunk's v, a written back */
+  GBMD_PIPE_MARK_END = 5
+};
+int gbmd_set_host_pipeline_trace(gbmd_context* ctx, int on);
+int gbmd_get_host_pipeline_trace(gbmd_context* ctx, int cap, double* t_ms, int* kind, int* index, int* count);
 /* slabs the next host step would use (0: unpipelined) and the number of
  * steps that stood as pipelined so far (a step that needed a rebuild is
  * finished unpipelined and not counted). */

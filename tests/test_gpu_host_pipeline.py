@@ -126,3 +126,40 @@ def test_pipeline_settings(gpu):
         for bad in ((2, 40, 512), (1, 0, 512), (1, 40, 48), (1, 40, 2048)):
             with pytest.raises(gpu.GbmdError):
                 ctx.set_host_pipeline_link(*bad)
+
+
+def test_pipeline_timeline(gpu):
+    """gbmd_get_host_pipeline_trace: one mark per chunk read, per density and
+    force piece and per chunk written back, in dependency order."""
+    s, setpot, rcut, skin, dt, mixed = _case("eam")
+    s = S.grid_order(s, rcut + skin)
+    torch = pytest.importorskip("torch")
+    with gpu.Context(0) as ctx:
+        ctx.upload_system(s)
+        setpot(ctx)
+        ctx.set_skin(0.3)
+        ctx.set_precision(True)
+        ctx.compute_forces()
+        start = ctx.download(KEYS)
+        st = {k: torch.empty(s.n, dtype=torch.float64, pin_memory=True).numpy() for k in KEYS}
+        for k in KEYS:
+            st[k][:] = start[k]
+        ctx.build_neighbors()
+        ctx.set_host_pipeline(8)
+        ctx.set_host_pipeline_trace(True)
+        ctx.run_nve_host(st, 1, 1e-3, rebuild_every=10)
+        marks = ctx.host_pipeline_trace()
+        assert ctx.host_pipeline()[1] == 1
+    S8 = 8
+    kinds = [m[1] for m in marks]
+    assert kinds[0] == "start" and kinds[-1] == "end"
+    for kind in ("in", "density", "force", "out"):
+        assert sorted(m[2] for m in marks if m[1] == kind) == list(range(S8)), kind
+    t = {(m[1], m[2]): m[0] for m in marks}
+    ins = [t[("in", k)] for k in range(S8)]
+    assert ins == sorted(ins)
+    end = t[("end", -1)]
+    assert all(m[0] <= end for m in marks)
+    for q in range(S8):
+        for d in (-1, 0, 1):
+            assert t[("force", q)] >= t[("density", (q + d) % S8)]
