@@ -183,17 +183,22 @@ class lj_compute_force(Operator):
 
 class lj_compute_force_symetric(lj_compute_force):
     """lj_compute_force_symetric (pair_potential_singlemat_symetric.cpp L44,
-    slots L335-346): lj_compute_force on the Newton-3 half list.  The
-    reference scatters the reaction force under per-particle spin locks
-    (`particle_locks`, accepted and unused here); the library adds it with
-    FP32 atomics.  Mixed precision with one lane x 4 entries per load."""
+    slots L335-346): the forces of lj_compute_force, which the reference
+    evaluates on a Newton-3 half list, scattering each reaction force under
+    per-particle spin locks (`particle_locks`, accepted and unused here).
+    The full list gives the same sums up to rounding, deterministically, and
+    is faster on GB300, so it is the default (as in the plugin);
+    `half_list: true` selects the library's half list, whose reaction forces
+    are added with FP32 atomics (mixed precision, one lane x 4 entries per
+    load)."""
     name = "lj_compute_force_symetric"
 
     def bind(self, sim: Simulation):
         super().bind(sim)
-        sim.set_precision(True)
-        sim.ctx.set_launch(1, 256, 4)
-        sim.ctx.set_newton3(True)
+        if self.slots.get("half_list", False):
+            sim.set_precision(True)
+            sim.ctx.set_launch(1, 256, 4)
+            sim.ctx.set_newton3(True)
 
 
 class lj_multi_force(Operator):

@@ -152,15 +152,19 @@ def test_newton3_unsupported_setups(gpu):
     assert rel_rms(d1["ax"], d0["ax"]) < MIXED_FORCE_TOL
 
 
-def test_symetric_operator_matches_lj_compute_force(gpu, oracle):
+@pytest.mark.parametrize("half_list", [False, True])
+def test_symetric_operator_matches_lj_compute_force(gpu, oracle, half_list):
     """The operator mirror: a run file binding lj_compute_force_symetric to
-    compute_force gives the lj_compute_force result (within the mixed
-    tolerance) on the Newton-3 path."""
+    compute_force gives the lj_compute_force result: on the full list by
+    default (FP64, 1e-12), on the Newton-3 half list with half_list (mixed
+    tolerance)."""
     from exastamp_gb300 import operators as OP
     s = _jitter(S.lj_fcc(ncell=5, seed=6), 0.05, 6)
     F, ep, _ = _lj_oracle(oracle, s)
-    cfg = {"compute_force": "lj_compute_force_symetric",
-           "lj_compute_force_symetric": {"rcut": 2.5, "parameters": {"epsilon": 1.0, "sigma": 1.0}}}
+    par = {"rcut": 2.5, "parameters": {"epsilon": 1.0, "sigma": 1.0}}
+    if half_list:
+        par["half_list"] = True
+    cfg = {"compute_force": "lj_compute_force_symetric", "lj_compute_force_symetric": par}
     sim = OP.Simulation(s)
     try:
         op = OP.compute_force_from_config(cfg)
@@ -168,10 +172,14 @@ def test_symetric_operator_matches_lj_compute_force(gpu, oracle):
         op.bind(sim)
         OP.chunk_neighbors().bind(sim, 0.3)
         op.execute(sim, energy=True)
-        assert sim.ctx.get_newton3()
+        assert sim.ctx.get_newton3() == half_list
         d = sim.ctx.download()
     finally:
         sim.ctx.close()
     G = np.stack([d["ax"], d["ay"], d["az"]], 1)
-    assert rel_rms(G, F) < MIXED_FORCE_TOL
-    assert abs(d["ep"].sum() - ep.sum()) < 1e-6 * abs(ep.sum())
+    if half_list:
+        assert rel_rms(G, F) < MIXED_FORCE_TOL
+        assert abs(d["ep"].sum() - ep.sum()) < 1e-6 * abs(ep.sum())
+    else:
+        assert np.abs(G - F).max() < 1e-12 * np.abs(F).max()
+        assert np.abs(d["ep"] - ep).max() < 1e-12 * np.abs(ep).max()
