@@ -335,13 +335,16 @@ __device__ __forceinline__ void lj_atom(const PairArgs& A, const LJF& P, const L
   }
 }
 
-template <int T, int V, bool EV, bool MULTI>
+// PIECE: the launch covers atoms [A.i0, A.n) only (a separate instantiation:
+// the offset costs registers that the full-range kernel, at the 64-register
+// cap, would spill).
+template <int T, int V, bool EV, bool MULTI, bool PIECE>
 __global__ void __launch_bounds__(256, 4) k_lj_mixed(PairArgs A, LJF P, const LJPair* __restrict__ tab, int ntypes,
                                                   double rcmax2) {
   __shared__ LJTabSmem t;
   if (MULTI) lj_load_table(t, tab, ntypes);
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = A.i0 + gt / T;
+  const int64_t i = PIECE ? A.i0 + gt / T : gt / T;
   lj_atom<T, V, EV, MULTI>(A, P, t, ntypes, rcmax2, i, (int)(gt % T), i < A.n, GlobalFetch{A.posf});
 }
 
@@ -473,11 +476,11 @@ __device__ __forceinline__ void eam_rho_atom(const PairArgs& A, const EamDev& E,
   }
 }
 
-template <int T, int V, bool EV, bool SINGLE>
+template <int T, int V, bool EV, bool SINGLE, bool PIECE>
 __global__ void __launch_bounds__(256) k_eam_rho_mixed(PairArgs A, EamDev E, float* __restrict__ fpf,
                                                        float* __restrict__ epf, float4* __restrict__ pfp) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = A.i0 + gt / T;
+  const int64_t i = PIECE ? A.i0 + gt / T : gt / T;
   eam_rho_atom<T, V, EV, SINGLE>(A, E, fpf, epf, pfp, i, (int)(gt % T), i < A.n, GlobalFetch{A.posf});
 }
 
@@ -612,12 +615,12 @@ __device__ __forceinline__ void eam_force_atom(const PairArgs& A, const EamDev& 
   }
 }
 
-template <int T, int V, bool EV, bool SINGLE>
+template <int T, int V, bool EV, bool SINGLE, bool PIECE>
 __global__ void __launch_bounds__(256, 4) k_eam_force_mixed(PairArgs A, EamDev E, const float* __restrict__ fpf,
                                                          const float* __restrict__ epf,
                                                          const float4* __restrict__ pfp) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = A.i0 + gt / T;
+  const int64_t i = PIECE ? A.i0 + gt / T : gt / T;
   eam_force_atom<T, V, EV, SINGLE>(A, E, fpf, epf, i, (int)(gt % T), i < A.n,
                                    GlobalFetch{SINGLE ? pfp : A.posf});
 }
@@ -778,7 +781,7 @@ static int launch_newton3(gbmd_context* c, const PairArgs& A, int part) {
 // ---------------------------------------------------------------------------
 // dispatch
 // ---------------------------------------------------------------------------
-template <int T, int V, bool EV>
+template <int T, int V, bool EV, bool PIECE>
 static void launch_mixed_TV(gbmd_context* c, const PairArgs& A, int part) {
   const int B = c->block;
   const unsigned grid = (unsigned)(((A.n - A.i0) * T + B - 1) / B);
@@ -789,17 +792,17 @@ static void launch_mixed_TV(gbmd_context* c, const PairArgs& A, int part) {
     if (part == 1) return;
     const LJPair& q = c->lj.p[0];
     LJF P{q.sig2f, q.eps24f, q.eps4f, q.ecutf, q.rc2lo, q.rc2hi, q.rc2, q.rc};
-    k_lj_mixed<T, V, EV, false><<<grid, B, 0, s>>>(A, P, nullptr, 1, c->lj.rcut_max2);
+    k_lj_mixed<T, V, EV, false, PIECE><<<grid, B, 0, s>>>(A, P, nullptr, 1, c->lj.rcut_max2);
   } else if (c->pot == GBMD_POT_LJ_MULTI) {
     if (part == 1) return;
     LJF P{};
-    k_lj_mixed<T, V, EV, true><<<grid, B, 0, s>>>(A, P, c->lj_tab_d, c->lj.ntypes, c->lj.rcut_max2);
+    k_lj_mixed<T, V, EV, true, PIECE><<<grid, B, 0, s>>>(A, P, c->lj_tab_d, c->lj.ntypes, c->lj.rcut_max2);
   } else if (c->eam.nel == 1) {
-    if (part != 2) k_eam_rho_mixed<T, V, EV, true><<<gridd, Bd, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
-    if (part != 1) k_eam_force_mixed<T, V, EV, true><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
+    if (part != 2) k_eam_rho_mixed<T, V, EV, true, PIECE><<<gridd, Bd, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
+    if (part != 1) k_eam_force_mixed<T, V, EV, true, PIECE><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
   } else {
-    if (part != 2) k_eam_rho_mixed<T, V, EV, false><<<gridd, Bd, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
-    if (part != 1) k_eam_force_mixed<T, V, EV, false><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
+    if (part != 2) k_eam_rho_mixed<T, V, EV, false, PIECE><<<gridd, Bd, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
+    if (part != 1) k_eam_force_mixed<T, V, EV, false, PIECE><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->epf, c->pfp);
   }
 }
 
@@ -862,6 +865,24 @@ static bool launch_staged(gbmd_context* c, const PairArgs& A, int part) {
   return true;
 }
 
+template <bool EV, bool PIECE>
+static int launch_mixed_shape(gbmd_context* c, const PairArgs& A, int part) {
+  const int key = c->tpa * 8 + c->vec;
+  switch (key) {
+    case 1 * 8 + 1: launch_mixed_TV<1, 1, EV, PIECE>(c, A, part); break;
+    case 1 * 8 + 4: launch_mixed_TV<1, 4, EV, PIECE>(c, A, part); break;
+    case 2 * 8 + 1: launch_mixed_TV<2, 1, EV, PIECE>(c, A, part); break;
+    case 2 * 8 + 4: launch_mixed_TV<2, 4, EV, PIECE>(c, A, part); break;
+    case 4 * 8 + 1: launch_mixed_TV<4, 1, EV, PIECE>(c, A, part); break;
+    case 4 * 8 + 4: launch_mixed_TV<4, 4, EV, PIECE>(c, A, part); break;
+    case 8 * 8 + 1: launch_mixed_TV<8, 1, EV, PIECE>(c, A, part); break;
+    case 16 * 8 + 1: launch_mixed_TV<16, 1, EV, PIECE>(c, A, part); break;
+    default:
+      return set_error(c, GBMD_ERR_INVALID, "unsupported launch: %d lanes x %d entries per atom", c->tpa, c->vec);
+  }
+  return GBMD_OK;
+}
+
 template <bool EV>
 static int launch_mixed_E(gbmd_context* c, const PairArgs& A, int part) {
   if (c->newton3) {
@@ -871,23 +892,16 @@ static int launch_mixed_E(gbmd_context* c, const PairArgs& A, int part) {
     return launch_newton3<EV>(c, A, part);
   }
   if (c->staged && c->tpa == 1 && c->vec == 4 && launch_staged<EV>(c, A, part)) return GBMD_OK;
-  const int key = c->tpa * 8 + c->vec;
-  switch (key) {
-    case 1 * 8 + 1: launch_mixed_TV<1, 1, EV>(c, A, part); break;
-    case 1 * 8 + 4: launch_mixed_TV<1, 4, EV>(c, A, part); break;
-    case 2 * 8 + 1: launch_mixed_TV<2, 1, EV>(c, A, part); break;
-    case 2 * 8 + 4: launch_mixed_TV<2, 4, EV>(c, A, part); break;
-    case 4 * 8 + 1: launch_mixed_TV<4, 1, EV>(c, A, part); break;
-    case 4 * 8 + 4: launch_mixed_TV<4, 4, EV>(c, A, part); break;
-    case 8 * 8 + 1: launch_mixed_TV<8, 1, EV>(c, A, part); break;
-    case 16 * 8 + 1: launch_mixed_TV<16, 1, EV>(c, A, part); break;
-    default:
-      return set_error(c, GBMD_ERR_INVALID, "unsupported launch: %d lanes x %d entries per atom", c->tpa, c->vec);
-  }
-  return GBMD_OK;
+  return launch_mixed_shape<EV, false>(c, A, part);
 }
 
 int launch_mixed(gbmd_context* c, const PairArgs& A, int part, bool ev) {
+  // a piece of the cell order (the host-step pipeline: no energies, full
+  // list, no staging, checked by launch_forces)
+  if (A.i0 != 0 || A.n != c->n) {
+    if (ev) return set_error(c, GBMD_ERR_INVALID, "atom ranges: no energies or virials");
+    return launch_mixed_shape<false, true>(c, A, part);
+  }
   return ev ? launch_mixed_E<true>(c, A, part) : launch_mixed_E<false>(c, A, part);
 }
 
