@@ -627,20 +627,23 @@ def measure(args, w, ws, dev, stream, torch, *, steps, fp64_steps, e2e_steps, dr
     # displacement trigger (R = -1) every 20 steps
     thermo_every = 2 * R if R > 0 else (20 if R < 0 else 0)
     # warm-up: at least W steps in a whole number of thermo intervals, then
-    # two runs of exactly K steps.  The runner replays CUDA graphs captured
-    # per parity of its double buffers, and a K-step run flips that parity,
-    # so the two K-step runs capture the graphs of both parities here rather
-    # than inside the timed region.  When K is a whole number of thermo
-    # intervals the timed run starts from a state whose energies are current
-    # (its step-0 thermo row needs only the reduction).
+    # two runs of min(K, 2 chunks) steps.  The runner replays CUDA graphs of
+    # 20-step chunks (one for a chunk followed by more steps, one for the
+    # chunk that ends a run), kept per parity of its double buffers; a run
+    # flips that parity, so the two short runs capture both graphs at both
+    # parities here rather than inside the timed region.  When that run
+    # length is a whole number of thermo intervals the timed run starts from
+    # a state whose energies are current (its step-0 thermo row needs only
+    # the reduction).
     warm = max(args.warmup, 3)
     if thermo_every:
         warm = -(-warm // thermo_every) * thermo_every
     ctx.run_nve(warm, dt, R, thermo_every, use_graph=True)
+    short = min(steps, 2 * thermo_every) if thermo_every else steps
     for _ in range(2):
-        ctx.run_nve(steps, dt, R, thermo_every, use_graph=True)
-    warm += 2 * steps
-    energies_reused = bool(thermo_every) and steps % thermo_every == 0
+        ctx.run_nve(short, dt, R, thermo_every, use_graph=True)
+    warm += 2 * short
+    energies_reused = bool(thermo_every) and short % thermo_every == 0
     npairs, maxnb, nc = ctx.neighbor_stats()
 
     # ---- timed region: K steps, device resident --------------------------
