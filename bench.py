@@ -535,9 +535,10 @@ def e2e_section(ctx, s, w, R, steps, ws, torch, stream):
     ctx.set_host_pipeline(0)
     unpiped_ms, unpiped_wall, _ = loop(True)   # one call per step, host link not overlapped
     ctx.set_host_pipeline(-1)
-    slabs, piped0 = ctx.host_pipeline()
+    slabs, piped0, redone0 = ctx.host_pipeline()
     mse, wall_ms, builds = loop(True)
     piped = ctx.host_pipeline()[1] - piped0
+    redone = ctx.host_pipeline()[2] - redone0
     timeline = None
     if slabs:
         # one more (untimed) step with the pipeline's timeline recorded
@@ -569,7 +570,8 @@ def e2e_section(ctx, s, w, R, steps, ws, torch, stream):
             "h2d_bytes_per_step": 72 * n, "d2h_bytes_per_step": 72 * n, "steps": steps,
             "ms_per_step": mse / steps, "ms_per_step_as_three_calls": sep_ms / steps,
             "ms_per_step_unpipelined": max(unpiped_ms, unpiped_wall) / steps,
-            "list_builds": builds, "slabs": slabs, "pipelined_steps": piped, "pipeline_timeline": timeline,
+            "list_builds": builds, "slabs": slabs, "pipelined_steps": piped,
+            "pipelined_steps_discarded_for_a_rebuild": redone, "pipeline_timeline": timeline,
             "host_order": "grid cells, z slowest (as the reference's grid stores atoms)",
             "path": "gbmd_run_nve_host(1 step, pinned r,v,a): chunks of the caller order read over the host link "
                     "with the first half and skin/2 test applied, pair passes slab by slab as their chunks "

@@ -101,7 +101,7 @@ def lib(path: str = LIB_PATH):
             "gbmd_set_host_pipeline_link": ([vp, i32, i32, i32], i32),
             "gbmd_set_host_pipeline_trace": ([vp, i32], i32),
             "gbmd_get_host_pipeline_trace": ([vp, i32, vp, vp, vp, P(i32)], i32),
-            "gbmd_get_host_pipeline": ([vp, P(i32), P(i64)], i32),
+            "gbmd_get_host_pipeline": ([vp, P(i32), P(i64), P(i64)], i32),
             "gbmd_thermo": ([vp, vp], i32),
             "gbmd_device_state": ([vp] + [vp] * 11, i32),
             "gbmd_thermo_reduce_noalloc": ([i64, vp, vp, vp, vp, vp, vp, vp, i32, vp, vp], i32),
@@ -410,10 +410,11 @@ class Context:
         return [(float(t[q]), names[k[q]], int(i[q])) for q in range(n)]
 
     def host_pipeline(self):
-        """(slabs the next host step would use, steps taken through the pipeline)."""
-        sl, st = C.c_int(0), C.c_int64(0)
-        self._chk(self._L.gbmd_get_host_pipeline(self.h, C.byref(sl), C.byref(st)))
-        return sl.value, st.value
+        """(slabs the next host step would use, steps that stood as
+        pipelined, pipelined steps discarded for an unpredicted rebuild)."""
+        sl, st, rd = C.c_int(0), C.c_int64(0), C.c_int64(0)
+        self._chk(self._L.gbmd_get_host_pipeline(self.h, C.byref(sl), C.byref(st), C.byref(rd)))
+        return sl.value, st.value, rd.value
 
     def list_builds(self):
         n = C.c_int64(0)

@@ -1395,7 +1395,11 @@ int gbmd_run_nve_host(gbmd_context* c, int nsteps, double dt, int rebuild_every,
     GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_GATE, 0, sizeof(int), c->stream));
     const double* hdev[9];
     for (int k = 0; k < 9; ++k) hdev[k] = hd.a[k];
-    const int slabs = nsteps == 1 ? pipe_slabs_for(c) : 0;
+    // a step the previous pipelined step predicts to need a rebuild (its
+    // first half from the returned state moves an atom past skin/2) is not
+    // pipelined: the rebuild would discard the speculative passes
+    const int slabs = nsteps == 1 && !c->pipe_expect_rebuild ? pipe_slabs_for(c) : 0;
+    c->pipe_expect_rebuild = false;
     {
       const FusedTriggerScope gate(c, true);
       if (slabs) {
@@ -1408,6 +1412,7 @@ int gbmd_run_nve_host(gbmd_context* c, int nsteps, double dt, int rebuild_every,
       }
     }
     if ((rc = sync_error_word(c))) return rc;
+    if (slabs && c->h_err[ERRW_GATE]) ++c->pipe_redone;
     if (slabs && !c->h_err[ERRW_GATE]) {
       ++c->pipe_steps;
       c->step += 1;
@@ -1471,10 +1476,11 @@ int gbmd_get_host_pipeline_trace(gbmd_context* c, int cap, double* t_ms, int* ki
   return pipe_trace_read(c, cap, t_ms, kind, index, count);
 }
 
-int gbmd_get_host_pipeline(const gbmd_context* c, int* slabs, int64_t* steps) {
+int gbmd_get_host_pipeline(const gbmd_context* c, int* slabs, int64_t* steps, int64_t* redone) {
   if (!c) return GBMD_ERR_INVALID;
   if (slabs) *slabs = pipe_slabs_for(c);
   if (steps) *steps = c->pipe_steps;
+  if (redone) *redone = c->pipe_redone;
   return GBMD_OK;
 }
 

@@ -255,6 +255,8 @@ struct gbmd_context {
   std::vector<uint64_t> pipe_mask;     // per caller chunk: slabs holding its atoms
   std::vector<int64_t> pipe_begin;     // slab s = cell-order atoms [begin[s], begin[s+1])
   int64_t pipe_steps = 0;              // steps that stood as pipelined (no rebuild due)
+  bool pipe_expect_rebuild = false;    // the last pipelined step predicts a rebuild in the next one
+  int64_t pipe_redone = 0;             // pipelined steps discarded for a rebuild nobody predicted
   // timeline of the last pipelined step (gbmd_set_host_pipeline_trace)
   bool pipe_trace = false;
   std::vector<cudaEvent_t> pipe_tr_ev;

@@ -30,7 +30,10 @@
 // input pieces test every atom against skin/2 as they push it, and a gated
 // copy moves v(t+dt) into place only when none moved that far.  Otherwise
 // the caller finishes the step without the pipeline after a rebuild, from
-// the pushed state (the caller's arrays are all rewritten then).
+// the pushed state (the caller's arrays are all rewritten then).  The same
+// end-of-step kernel applies the next step's first half to the state it
+// returns and tests it: when the caller passes that state back unchanged,
+// a step that will need a rebuild is known in advance and not pipelined.
 #include "gbmd_internal.cuh"
 
 namespace gbmd {
@@ -44,6 +47,7 @@ constexpr int OFF_ZB = 1024;      // first z layer of each slab, S + 1
 constexpr int OFF_NEED = 1096;    // per slab: last caller chunk of its atoms (-1: empty)
 constexpr int OFF_BEGIN = 1160;   // per slab: first cell-order atom, S + 1
 constexpr int OFF_MASK = 1232;    // per chunk: 64-bit slab set (8-byte aligned)
+constexpr int OFF_NEXT = 1360;    // the next step will need a rebuild (k_pipe_finish)
 constexpr int SCRATCH_INTS = 1536;
 constexpr int TRACE_CAP = 4 * MAX_SLABS + 2;
 
@@ -100,14 +104,40 @@ __global__ void k_pipe_out(int64_t u0, int64_t u1, const int32_t* __restrict__ i
   }
 }
 
-// v(t+dt) into place unless the displacement gate is raised.
-__global__ void k_copy_v_gated(int64_t n, int64_t cap, const double* __restrict__ src, double* __restrict__ dst,
-                               const int* __restrict__ gate) {
-  if (*gate) return;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    dst[i] = src[i];
-    dst[cap + i] = src[cap + i];
-    dst[2 * cap + i] = src[2 * cap + i];
+// End of a pipelined step: v(t+dt) into place unless the displacement gate
+// is raised, and the next step's first half, as k_host_first_half will
+// compute it from the arrays this step returns (same operations), tested
+// against skin/2: `next` is set when that step will need a rebuild.
+struct FinishArgs {
+  int64_t n, cap;
+  const double* src;        // v(t+dt), 3 planes of cap
+  double* dst;              // the context's v
+  const double *x, *y, *z;  // r(t+dt)
+  const double *ax, *ay, *az;
+  const double* rref;       // positions at the last rebuild, 3 planes of cap
+  double h, h2, thr2;
+  const int* gate;
+  int* next;
+};
+
+// One atom per thread and many short blocks (no grid-stride loop): the
+// write-back kernels on the high-priority output stream get SM slots as
+// these blocks retire.
+__global__ void k_pipe_finish(FinishArgs F) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (*F.gate || i >= F.n) return;
+  {
+    const double vx = F.src[i], vy = F.src[F.cap + i], vz = F.src[2 * F.cap + i];
+    F.dst[i] = vx;
+    F.dst[F.cap + i] = vy;
+    F.dst[2 * F.cap + i] = vz;
+    const double x = __dadd_rn(F.x[i], __dadd_rn(__dmul_rn(vx, F.h), __dmul_rn(F.ax[i], F.h2)));
+    const double y = __dadd_rn(F.y[i], __dadd_rn(__dmul_rn(vy, F.h), __dmul_rn(F.ay[i], F.h2)));
+    const double z = __dadd_rn(F.z[i], __dadd_rn(__dmul_rn(vz, F.h), __dmul_rn(F.az[i], F.h2)));
+    const double dx = __dsub_rn(x, F.rref[i]), dy = __dsub_rn(y, F.rref[F.cap + i]),
+                 dz = __dsub_rn(z, F.rref[2 * F.cap + i]);
+    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    if (d2 > F.thr2) *F.next = 1;
   }
 }
 
@@ -385,10 +415,24 @@ int pipe_step(gbmd_context* c, double dt, const double* const host[9], const dou
   // once every force piece has run
   GBMD_CUDA(c, cudaStreamWaitEvent(m, c->pipe_in_ev[P - 1], 0));
   for (int s = 0; s < S; ++s) GBMD_CUDA(c, cudaStreamWaitEvent(m, c->pipe_f_ev[s], 0));
-  int64_t blocks = (n + 255) / 256;
-  if (blocks > 4LL * c->nsm) blocks = 4LL * c->nsm;
-  if (blocks < 1) blocks = 1;
-  k_copy_v_gated<<<(unsigned)blocks, 256, 0, m>>>(n, c->cap, v_spare, c->VX(), c->d_err + ERRW_GATE);
+  const int64_t blocks = (n + 255) / 256;
+  int* next_flag = c->pipe_dev + OFF_NEXT;
+  GBMD_CUDA(c, cudaMemsetAsync(next_flag, 0, sizeof(int), m));
+  FinishArgs fa;
+  fa.n = n;
+  fa.cap = c->cap;
+  fa.src = v_spare;
+  fa.dst = c->VX();
+  fa.x = c->X(); fa.y = c->Y(); fa.z = c->Z();
+  fa.ax = c->AX(); fa.ay = c->AY(); fa.az = c->AZ();
+  fa.rref = c->rref;
+  fa.h = dt * 1.0;
+  fa.h2 = fa.h * fa.h * 0.5;
+  fa.thr2 = (0.5 * c->skin) * (0.5 * c->skin);
+  fa.gate = c->d_err + ERRW_GATE;
+  fa.next = next_flag;
+  k_pipe_finish<<<(unsigned)blocks, 256, 0, m>>>(fa);
+  GBMD_CUDA(c, cudaMemcpyAsync(c->pipe_host + OFF_NEXT, next_flag, sizeof(int), cudaMemcpyDeviceToHost, m));
   GBMD_CUDA(c, cudaEventRecord(c->pipe_out_done, c->pipe_out));
   GBMD_CUDA(c, cudaStreamWaitEvent(m, c->pipe_out_done, 0));
   GBMD_CUDA(c, cudaEventRecord(c->pipe_r_done, c->pipe_r));
@@ -396,6 +440,7 @@ int pipe_step(gbmd_context* c, double dt, const double* const host[9], const dou
   if ((rc = trace_mark(c, m, GBMD_PIPE_MARK_END, -1))) return rc;
   GBMD_CUDA(c, cudaGetLastError());
   GBMD_CUDA(c, cudaStreamSynchronize(m));
+  c->pipe_expect_rebuild = c->pipe_host[OFF_NEXT] != 0;
   return GBMD_OK;
 }
 

@@ -264,7 +264,10 @@ int gbmd_run_nve(gbmd_context* ctx, int nsteps, double dt, int rebuild_every, in
  * cell order along z (atoms stored cell by cell, z slowest, as exaNBody's
  * grids hold them); another order gives a more serial schedule.  A step
  * whose first half moves an atom more than skin/2 from its position at the
- * last rebuild is finished without the pipeline after the rebuild. */
+ * last rebuild is finished without the pipeline after the rebuild; the
+ * pipelined step also applies the next step's first half to the state it
+ * returns, and when that moves an atom past skin/2 the next step (given
+ * that state back) is run without the pipeline from the start. */
 int gbmd_run_nve_host(gbmd_context* ctx, int nsteps, double dt, int rebuild_every, double* rx, double* ry,
                       double* rz, double* vx, double* vy, double* vz, double* ax, double* ay, double* az);
 /* slabs: -1 automatic (16 slabs from 262,144 atoms up, else off; the
@@ -295,10 +298,11 @@ enum {
 };
 int gbmd_set_host_pipeline_trace(gbmd_context* ctx, int on);
 int gbmd_get_host_pipeline_trace(gbmd_context* ctx, int cap, double* t_ms, int* kind, int* index, int* count);
-/* slabs the next host step would use (0: unpipelined) and the number of
- * steps that stood as pipelined so far (a step that needed a rebuild is
- * finished unpipelined and not counted). */
-int gbmd_get_host_pipeline(const gbmd_context* ctx, int* slabs, int64_t* steps);
+/* slabs the next host step would use (0: unpipelined), the number of
+ * steps that stood as pipelined so far, and the number of pipelined steps
+ * discarded because they needed a rebuild that was not predicted (those are
+ * finished unpipelined).  Any pointer may be NULL. */
+int gbmd_get_host_pipeline(const gbmd_context* ctx, int* slabs, int64_t* steps, int64_t* redone);
 /* Minimiser: nsteps of compute forces + push_min (r += a dt^2/2, clipped);
  * rebuild_every as gbmd_run_nve. */
 int gbmd_run_minimize(gbmd_context* ctx, int nsteps, double dt, double tolF, int rebuild_every);
