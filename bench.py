@@ -195,6 +195,15 @@ class ClockSampler:
                 "samples": len(rows), "reasons": reasons}
 
 
+def measured_clock_mhz():
+    """Maximum SM clock recorded with the measured peaks, if any."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh).get("sm_max_mhz") or 0.0) or None
+    except (OSError, ValueError):
+        return None
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -759,6 +768,21 @@ def measure(args, w, ws, dev, stream, torch, *, steps, fp64_steps, e2e_steps, dr
                        "frac": achieved / peak, "peak_source": peak_kind,
                        "algorithmic_bytes_per_launch": alg_bytes, "bytes_per_atom": per_atom,
                        "traffic": traffic, "traffic_source": traffic_src, "binding": binding, "kernel_ms": prof}
+    if w["kind"] == "eam" and args.precision == "mixed":
+        # the FP-pipe side of the same kernels: useful flops per unordered
+        # pair within rc (density 20, force 54, embedding 14 per atom), the
+        # FCC Cu lattice's 42 neighbours within rc=5.0 A (21 unordered pairs
+        # per atom), against the nominal FP32 rate (no measured FP32 peak)
+        pairs = 21.0 * s.n
+        fp32_peak = 152 * 128 * 2 * (measured_clock_mhz() or 2070.0) * 1e6 / 1e12
+        dens_tf = (20.0 * pairs + 14.0 * s.n) / (prof["density"] * 1e-3) / 1e12
+        force_tf = 54.0 * pairs / (prof["pair"] * 1e-3) / 1e12
+        out["roofline"]["fp32"] = {
+            "useful_flop_per_launch": {"density": 20.0 * pairs + 14.0 * s.n, "force": 54.0 * pairs},
+            "achieved_tflops": {"density": dens_tf, "force": force_tf}, "nominal_peak_tflops": fp32_peak,
+            "frac": {"density": dens_tf / fp32_peak, "force": force_tf / fp32_peak},
+            "peak_source": "nominal: 152 SMs x 128 FP32 lanes x 2 flop x max SM clock (not measured)",
+            "pairs_source": "42 lattice neighbours within rc per atom, counted once per unordered pair"}
 
     single = ws == 1
     # ---- accuracy against the FP64 oracle at the benchmarked state ----------
