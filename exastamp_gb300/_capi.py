@@ -94,6 +94,7 @@ def lib(path: str = LIB_PATH):
             "gbmd_run_nve_host": ([vp, i32, dbl, i32] + [vp] * 9, i32),
             "gbmd_run_minimize": ([vp, i32, dbl, dbl, i32], i32),
             "gbmd_set_eam_johnson": ([vp, vp, dbl], i32),
+            "gbmd_set_eam_sutton_chen": ([vp, vp, dbl], i32),
             "gbmd_lj_loss_grad": ([vp, vp, vp, vp, vp, dbl, dbl, P(dbl), vp], i32),
             "gbmd_lj_multi_loss_grad": ([vp, vp, vp, vp, vp, dbl, dbl, P(dbl), vp, vp], i32),
             "gbmd_list_builds": ([vp, P(i64)], i32),
@@ -359,6 +360,13 @@ class Context:
         if p.shape != (19,):
             raise ValueError("johnson_force takes 19 parameters")
         self._chk(self._L.gbmd_set_eam_johnson(self.h, _p(p), float(rcut)))
+
+    def set_eam_sutton_chen(self, params, rcut):
+        """sutton_chen_force: params = (c, epsilon, a0, n, m), EamSuttonChenParameters order."""
+        p = _f64(params)
+        if p.shape != (5,):
+            raise ValueError("sutton_chen_force takes 5 parameters")
+        self._chk(self._L.gbmd_set_eam_sutton_chen(self.h, _p(p), float(rcut)))
 
     def lj_loss_grad(self, f_target, e_target, w_force, w_energy):
         """Force-matching + energy loss of lj_compute_force and its gradient

@@ -134,6 +134,7 @@ static double pot_rcut_max(const gbmd_context* c) {
   if (c->pot == GBMD_POT_LJ || c->pot == GBMD_POT_LJ_MULTI) return c->lj.rcut_max;
   if (c->pot == GBMD_POT_EAM_ALLOY) return c->eam.rcut;
   if (c->pot == GBMD_POT_EAM_JOHNSON) return c->ej.rcut;
+  if (c->pot == GBMD_POT_EAM_SUTTON_CHEN) return c->esc.rcut;
   return 0.0;
 }
 
@@ -922,6 +923,34 @@ int gbmd_set_eam_johnson(gbmd_context* c, const double params[19], double rcut) 
   return GBMD_OK;
 }
 
+// sutton_chen_force parameters (sutton_chen.h L30-37), see gbmd_johnson.cu
+int gbmd_set_eam_sutton_chen(gbmd_context* c, const double params[5], double rcut) {
+  if (!c || !params || !(rcut > 0.0)) return GBMD_ERR_INVALID;
+  for (int k = 0; k < 5; ++k)
+    if (!std::isfinite(params[k])) return set_error(c, GBMD_ERR_INVALID, "sutton_chen parameter %d not finite", k);
+  gbmd::SuttonChenDev P{};
+  P.c = params[0];
+  P.epsilon = params[1];
+  P.a0 = params[2];
+  P.n = params[3];
+  P.m = params[4];
+  if (!(P.a0 > 0.0)) return set_error(c, GBMD_ERR_INVALID, "sutton_chen a0 must be > 0");
+  P.rcut = rcut;
+  P.rcut2 = rcut * rcut;
+  P.cf = (float)P.c;
+  P.epsf = (float)P.epsilon;
+  P.a0f = (float)P.a0;
+  P.nf = (float)P.n;
+  P.mf = (float)P.m;
+  P.rc2lo = (float)(P.rcut2 * (1.0 - 0x1p-12));
+  P.rc2hi = (float)(P.rcut2 * (1.0 + 0x1p-12));
+  c->esc = P;
+  c->pot = GBMD_POT_EAM_SUTTON_CHEN;
+  c->energy_step = -1, c->forces_valid_step = c->rho_valid_step = -1;
+  set_rlist(c, rcut);
+  return GBMD_OK;
+}
+
 int gbmd_set_precision(gbmd_context* c, int precision) {
   if (!c || (precision != GBMD_PRECISION_FP64 && precision != GBMD_PRECISION_MIXED)) return GBMD_ERR_INVALID;
   if (c->precision != precision) {
@@ -1120,7 +1149,8 @@ int gbmd_compute_forces(gbmd_context* c, int flags) {
   if (f.virial && (rc = ensure_virial(c))) return rc;
   f.fuse = FUSE_NONE;
   const int passes = flags & (GBMD_FORCE_PASS_DENSITY | GBMD_FORCE_PASS_FORCE);
-  const bool eam = c->pot == GBMD_POT_EAM_ALLOY || c->pot == GBMD_POT_EAM_JOHNSON;
+  const bool eam = c->pot == GBMD_POT_EAM_ALLOY || c->pot == GBMD_POT_EAM_JOHNSON ||
+                   c->pot == GBMD_POT_EAM_SUTTON_CHEN;
   if (passes == GBMD_FORCE_PASS_DENSITY) {
     // eam_rho (+ eam_rho2emb): F'(rho) kept in the context for the force pass
     f.part = 1;

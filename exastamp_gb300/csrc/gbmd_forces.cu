@@ -345,7 +345,7 @@ int launch_forces(gbmd_context* c, const ForceFlags& f) {
   if (c->newton3 && !c->h3acc) return set_error(c, GBMD_ERR_INVALID, "Newton-3 accumulators not allocated");
   const int part = f.part;
   int rc;
-  if (c->pot == GBMD_POT_EAM_JOHNSON) rc = launch_johnson(c, A, part, ev, mixed);
+  if (c->pot == GBMD_POT_EAM_JOHNSON || c->pot == GBMD_POT_EAM_SUTTON_CHEN) rc = launch_johnson(c, A, part, ev, mixed);
   else if (mixed) rc = launch_mixed(c, A, part, ev);
   else rc = ev ? launch_fp64<true>(c, A, part) : launch_fp64<false>(c, A, part);
   if (rc) return rc;

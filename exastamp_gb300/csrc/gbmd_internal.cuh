@@ -81,6 +81,14 @@ struct JohnsonDev {
   float rc2lo, rc2hi;
 };
 
+// sutton_chen_force parameters (EamSuttonChenParameters order) in FP64 and FP32.
+struct SuttonChenDev {
+  double c, epsilon, a0, n, m;
+  double rcut, rcut2;
+  float cf, epsf, a0f, nf, mf;
+  float rc2lo, rc2hi;
+};
+
 struct Grid {
   int nc[3];
   double h[3], L[3], lo[3];
@@ -194,6 +202,7 @@ struct gbmd_context {
   // potential
   int pot = GBMD_POT_NONE;
   gbmd::JohnsonDev ej{};
+  gbmd::SuttonChenDev esc{};
   gbmd::LJTable lj{};
   gbmd::EamDev eam{};
   double* eam_d = nullptr;      // device FP64 tables (one allocation)

@@ -1,5 +1,4 @@
-// gbmd_johnson.cu -- johnson_force: the analytic single-element EAM of
-// src/potential/eam_potentials/johnson/johnson.h (L28-176) run by the
+// gbmd_johnson.cu -- the analytic single-element EAM operators run by the
 // mono-material two-pass template (eam_potential.cu L69-193,
 // eam_force_op_singlemat.h L39-171):
 //
@@ -7,18 +6,23 @@
 //   pass 2 (ForceOp): de = (rho'(r) (F'_i + F'_j) + phi'(r)) / r
 //                     f_i += de * (r_j - r_i);  ep_i += phi/2;  vir_i += -f (x) dr / 2
 //
+// johnson_force (src/potential/eam_potentials/johnson/johnson.h L28-176):
 //   phi(r) = A e^{-alpha (x-1)} / (1 + (x-kappa)^20) - B e^{-beta (x-1)} / (1 + (x-lambda)^20)
 //   rho(r) = fe e^{-beta (x-1)} / (1 + (x-lambda)^20),   x = r / re
 //   F(rho): cubic in (rho/rhon - 1) below rhon = 0.85 rhoe, cubic in
 //           (rho/rhoe - 1) below rho0 = 1.15 rhoe, Fo (1 - ln s) s with
 //           s = (rho/rhoe)^eta above.
+// sutton_chen_force (src/potential/eam_potentials/sutton_chen/sutton_chen.h
+// L30-67):
+//   phi(r) = epsilon (a0/r)^n,  rho(r) = (a0/r)^m,  F(rho) = -c epsilon sqrt(rho)
 //
-// FP64 kernels use the reference's formulas (exp, pow(., 20), log) in the
-// same order; the mixed kernels evaluate the same functions in FP32 on the
-// cell-relative coordinates of the main mixed path (the 20th power by
-// repeated squaring), with compensated sums, FP64 embedding and FP64 state.
-// Pair membership (r <= rcut) is exact in both: FP64 directly, mixed through
-// the FP32 screen and the FP64 re-test of the 2^-12 band.
+// The kernels take the functions from a policy (JohnsonFns, SuttonChenFns).
+// FP64 kernels use the reference's formulas in the same order; the mixed
+// kernels evaluate the same functions in FP32 on the cell-relative
+// coordinates of the main mixed path, with compensated sums, FP64 embedding
+// and FP64 state.  Pair membership (r <= rcut) is exact in both: FP64
+// directly, mixed through the FP32 screen and the FP64 re-test of the 2^-12
+// band.
 #include <cmath>
 
 #include "gbmd_pair_common.cuh"
@@ -91,10 +95,70 @@ __device__ __forceinline__ void ej_term_f(float pre, float k, float x, float c, 
 }
 
 // --------------------------------------------------------------------------
+// function policies: FP64 rho/phi/F with derivatives, FP32 rho (density
+// pass) and rho', phi, phi' (force pass)
+// --------------------------------------------------------------------------
+struct JohnsonFns {
+  using Params = JohnsonDev;
+  static __device__ __forceinline__ void rho_d(const Params& p, double r, double& v, double& dv) {
+    ej_rho_d(p, r, v, dv);
+  }
+  static __device__ __forceinline__ void phi_d(const Params& p, double r, double& v, double& dv) {
+    ej_phi_d(p, r, v, dv);
+  }
+  static __device__ __forceinline__ void embed_d(const Params& p, double rho, double& f, double& df) {
+    ej_embed_d(p, rho, f, df);
+  }
+  static __device__ __forceinline__ float rho_f(const Params& p, float r) {
+    float v = 0.f, dv = 0.f;
+    ej_term_f(p.fef, p.betaf, r * p.ire_f, p.lambdaf, p.ire_f, v, dv);
+    return v;
+  }
+  static __device__ __forceinline__ void pair_f(const Params& p, float r, float& rh, float& drh, float& ph,
+                                                float& dph) {
+    const float x = r * p.ire_f;
+    rh = drh = ph = dph = 0.f;
+    ej_term_f(p.fef, p.betaf, x, p.lambdaf, p.ire_f, rh, drh);
+    ej_term_f(p.Af, p.alphaf, x, p.kappaf, p.ire_f, ph, dph);
+    ej_term_f(-p.Bf, p.betaf, x, p.lambdaf, p.ire_f, ph, dph);
+  }
+};
+
+// sutton_chen.h L36-67, the same operations in the same order
+struct SuttonChenFns {
+  using Params = SuttonChenDev;
+  static __device__ __forceinline__ void rho_d(const Params& p, double r, double& v, double& dv) {
+    const double ratio = p.a0 / r;
+    v = pow(ratio, p.m);
+    dv = -1 * p.m * v / r;
+  }
+  static __device__ __forceinline__ void phi_d(const Params& p, double r, double& v, double& dv) {
+    const double ratio = p.a0 / r;
+    v = p.epsilon * pow(ratio, p.n);
+    dv = -1 * p.n * v / r;
+  }
+  static __device__ __forceinline__ void embed_d(const Params& p, double rho, double& f, double& df) {
+    const double sq = sqrt(rho);
+    f = -1. * p.c * p.epsilon * sq;
+    df = 0.5 * f / (rho > 0 ? rho : 0);
+  }
+  static __device__ __forceinline__ float rho_f(const Params& p, float r) { return powf(p.a0f / r, p.mf); }
+  static __device__ __forceinline__ void pair_f(const Params& p, float r, float& rh, float& drh, float& ph,
+                                                float& dph) {
+    const float ratio = p.a0f / r;
+    const float ir = __frcp_rn(r);
+    rh = powf(ratio, p.mf);
+    drh = -p.mf * rh * ir;
+    ph = p.epsf * powf(ratio, p.nf);
+    dph = -p.nf * ph * ir;
+  }
+};
+
+// --------------------------------------------------------------------------
 // FP64 kernels
 // --------------------------------------------------------------------------
-template <int T, bool EV>
-__global__ void __launch_bounds__(256) k_ej_rho(PairArgs A, JohnsonDev P, double* __restrict__ fpd) {
+template <class Fn, int T, bool EV>
+__global__ void __launch_bounds__(256) k_ej_rho(PairArgs A, typename Fn::Params P, double* __restrict__ fpd) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t i = A.i0 + gt / T;
   const int lane = (int)(gt % T);
@@ -115,20 +179,21 @@ __global__ void __launch_bounds__(256) k_ej_rho(PairArgs A, JohnsonDev P, double
     const double d2 = exact_d2(pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, Sx, Sy, Sz, dx, dy, dz);
     if (!(d2 <= P.rcut2)) continue;
     double v, dv;
-    ej_rho_d(P, sqrt(d2), v, dv);
+    Fn::rho_d(P, sqrt(d2), v, dv);
     rho += v;
   }
   rho = group_reduce_d<T>(rho);
   if (live && lane == 0) {
     double f, df;
-    ej_embed_d(P, rho, f, df);
+    Fn::embed_d(P, rho, f, df);
     fpd[i] = df;
     if (EV) A.ep_emb[i] = f;
   }
 }
 
-template <int T, bool EV>
-__global__ void __launch_bounds__(256) k_ej_force(PairArgs A, JohnsonDev P, const double* __restrict__ fpd) {
+template <class Fn, int T, bool EV>
+__global__ void __launch_bounds__(256) k_ej_force(PairArgs A, typename Fn::Params P,
+                                                  const double* __restrict__ fpd) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t i = A.i0 + gt / T;
   const int lane = (int)(gt % T);
@@ -156,8 +221,8 @@ __global__ void __launch_bounds__(256) k_ej_force(PairArgs A, JohnsonDev P, cons
     if (!(d2 <= P.rcut2)) continue;
     const double r = sqrt(d2);
     double rho, drho, phi, dphi;
-    ej_rho_d(P, r, rho, drho);
-    ej_phi_d(P, r, phi, dphi);
+    Fn::rho_d(P, r, rho, drho);
+    Fn::phi_d(P, r, phi, dphi);
     const double de = (drho * (fpi + __ldg(&fpd[j])) + dphi) / r;
     const double fex = de * dx, fey = de * dy, fez = de * dz;
     fx += fex; fy += fey; fz += fez;
@@ -203,7 +268,8 @@ struct EjGeom {
   bool in;
 };
 
-__device__ __forceinline__ EjGeom ej_geom(const PairArgs& A, const JohnsonDev& P, uint32_t ent, const float4& pj,
+template <class Params>
+__device__ __forceinline__ EjGeom ej_geom(const PairArgs& A, const Params& P, uint32_t ent, const float4& pj,
                                           const float4& pi, int64_t i, int cp) {
   EjGeom G;
   G.dx = fmaf(ej_unit((ent >> 26) & 3u), A.g.hf[0], pj.x - pi.x);
@@ -216,8 +282,8 @@ __device__ __forceinline__ EjGeom ej_geom(const PairArgs& A, const JohnsonDev& P
   return G;
 }
 
-template <int T, bool EV>
-__global__ void __launch_bounds__(256) k_ej_rho_mixed(PairArgs A, JohnsonDev P, float* __restrict__ fpf,
+template <class Fn, int T, bool EV>
+__global__ void __launch_bounds__(256) k_ej_rho_mixed(PairArgs A, typename Fn::Params P, float* __restrict__ fpf,
                                                       float* __restrict__ epf) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t i = A.i0 + gt / T;
@@ -233,21 +299,21 @@ __global__ void __launch_bounds__(256) k_ej_rho_mixed(PairArgs A, JohnsonDev P, 
     const float4 pj = __ldg(&A.posf[ent & GBMD_IDX_MASK]);
     const EjGeom G = ej_geom(A, P, ent, pj, pi, i, cp);
     const float r = G.d2 * rsqrtf(G.d2);
-    float v = 0.f, dv = 0.f;
-    ej_term_f(P.fef, P.betaf, r * P.ire_f, P.lambdaf, P.ire_f, v, dv);
+    const float v = Fn::rho_f(P, r);
     kahan_add(rho, crho, G.in ? v : 0.f);
   }
   group_reduce_kahan<T>(rho, crho);
   if (live && lane == 0) {
     double f, df;
-    ej_embed_d(P, (double)(rho - crho), f, df);  // per atom: FP64
+    Fn::embed_d(P, (double)(rho - crho), f, df);  // per atom: FP64
     fpf[i] = (float)df;
     if (EV) epf[i] = (float)f;
   }
 }
 
-template <int T, bool EV>
-__global__ void __launch_bounds__(256) k_ej_force_mixed(PairArgs A, JohnsonDev P, const float* __restrict__ fpf,
+template <class Fn, int T, bool EV>
+__global__ void __launch_bounds__(256) k_ej_force_mixed(PairArgs A, typename Fn::Params P,
+                                                        const float* __restrict__ fpf,
                                                         const float* __restrict__ epf) {
   const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t i = A.i0 + gt / T;
@@ -271,11 +337,8 @@ __global__ void __launch_bounds__(256) k_ej_force_mixed(PairArgs A, JohnsonDev P
     const EjGeom G = ej_geom(A, P, ent, pj, pi, i, cp);
     const float rs = rsqrtf(G.d2);
     const float r = G.d2 * rs;
-    const float x = r * P.ire_f;
-    float rh = 0.f, drh = 0.f, ph = 0.f, dph = 0.f;
-    ej_term_f(P.fef, P.betaf, x, P.lambdaf, P.ire_f, rh, drh);
-    ej_term_f(P.Af, P.alphaf, x, P.kappaf, P.ire_f, ph, dph);
-    ej_term_f(-P.Bf, P.betaf, x, P.lambdaf, P.ire_f, ph, dph);
+    float rh, drh, ph, dph;
+    Fn::pair_f(P, r, rh, drh, ph, dph);
     const float de = G.in ? fmaf(drh, fpi + fpj, dph) * rs : 0.f;
     kahan_add(fx, cfx, de * G.dx);
     kahan_add(fy, cfy, de * G.dy);
@@ -319,35 +382,39 @@ __global__ void __launch_bounds__(256) k_ej_force_mixed(PairArgs A, JohnsonDev P
 // --------------------------------------------------------------------------
 // dispatch
 // --------------------------------------------------------------------------
-template <int T, bool EV>
-static void launch_ej_T(gbmd_context* c, const PairArgs& A, int part, bool mixed) {
+template <class Fn, int T, bool EV>
+static void launch_ej_T(gbmd_context* c, const PairArgs& A, const typename Fn::Params& P, int part, bool mixed) {
   const int B = c->block;
   const unsigned grid = (unsigned)(((A.n - A.i0) * T + B - 1) / B);
   cudaStream_t s = c->stream;
   if (mixed) {
-    if (part != 2) k_ej_rho_mixed<T, EV><<<grid, B, 0, s>>>(A, c->ej, c->fpf, c->epf);
-    if (part != 1) k_ej_force_mixed<T, EV><<<grid, B, 0, s>>>(A, c->ej, c->fpf, c->epf);
+    if (part != 2) k_ej_rho_mixed<Fn, T, EV><<<grid, B, 0, s>>>(A, P, c->fpf, c->epf);
+    if (part != 1) k_ej_force_mixed<Fn, T, EV><<<grid, B, 0, s>>>(A, P, c->fpf, c->epf);
   } else {
-    if (part != 2) k_ej_rho<T, EV><<<grid, B, 0, s>>>(A, c->ej, c->fpd);
-    if (part != 1) k_ej_force<T, EV><<<grid, B, 0, s>>>(A, c->ej, c->fpd);
+    if (part != 2) k_ej_rho<Fn, T, EV><<<grid, B, 0, s>>>(A, P, c->fpd);
+    if (part != 1) k_ej_force<Fn, T, EV><<<grid, B, 0, s>>>(A, P, c->fpd);
   }
 }
 
-template <bool EV>
-static int launch_ej_E(gbmd_context* c, const PairArgs& A, int part, bool mixed) {
+template <class Fn, bool EV>
+static int launch_ej_E(gbmd_context* c, const PairArgs& A, const typename Fn::Params& P, int part, bool mixed) {
   switch (c->tpa) {
-    case 1: launch_ej_T<1, EV>(c, A, part, mixed); break;
-    case 2: launch_ej_T<2, EV>(c, A, part, mixed); break;
-    case 4: launch_ej_T<4, EV>(c, A, part, mixed); break;
-    case 8: launch_ej_T<8, EV>(c, A, part, mixed); break;
-    case 16: launch_ej_T<16, EV>(c, A, part, mixed); break;
+    case 1: launch_ej_T<Fn, 1, EV>(c, A, P, part, mixed); break;
+    case 2: launch_ej_T<Fn, 2, EV>(c, A, P, part, mixed); break;
+    case 4: launch_ej_T<Fn, 4, EV>(c, A, P, part, mixed); break;
+    case 8: launch_ej_T<Fn, 8, EV>(c, A, P, part, mixed); break;
+    case 16: launch_ej_T<Fn, 16, EV>(c, A, P, part, mixed); break;
     default: return set_error(c, GBMD_ERR_INVALID, "unsupported lanes per atom %d", c->tpa);
   }
   return GBMD_OK;
 }
 
 int launch_johnson(gbmd_context* c, const PairArgs& A, int part, bool ev, bool mixed) {
-  return ev ? launch_ej_E<true>(c, A, part, mixed) : launch_ej_E<false>(c, A, part, mixed);
+  if (c->pot == GBMD_POT_EAM_SUTTON_CHEN)
+    return ev ? launch_ej_E<SuttonChenFns, true>(c, A, c->esc, part, mixed)
+              : launch_ej_E<SuttonChenFns, false>(c, A, c->esc, part, mixed);
+  return ev ? launch_ej_E<JohnsonFns, true>(c, A, c->ej, part, mixed)
+            : launch_ej_E<JohnsonFns, false>(c, A, c->ej, part, mixed);
 }
 
 }  // namespace gbmd

@@ -70,7 +70,7 @@ int launch_lj_multi_loss_grad(gbmd_context* c, const PairArgs& A, const double* 
 size_t lj_multi_adj_args_size();
 int launch_lj_loss_grad(gbmd_context* c, const PairArgs& A, const double* const targets[4], double wF, double wE,
                         double* scratch);
-// johnson_force kernels, both precisions (gbmd_johnson.cu).
+// johnson_force and sutton_chen_force kernels, both precisions (gbmd_johnson.cu).
 int launch_johnson(gbmd_context* c, const PairArgs& A, int part, bool ev, bool mixed);
 
 // Integer image of the stencil cell of `code` seen from home cell (cx,cy,cz).

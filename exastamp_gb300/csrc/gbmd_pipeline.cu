@@ -290,7 +290,8 @@ int pipe_step(gbmd_context* c, double dt, const double* const host[9], const dou
   for (int q = 1; q < PIPE_STREAMS; ++q) pool[q] = c->pipe_cs[q - 1];
   int next = 0;
   auto take = [&]() { const cudaStream_t st = pool[next]; next = (next + 1) % PIPE_STREAMS; return st; };
-  const bool two_pass = c->pot == GBMD_POT_EAM_ALLOY || c->pot == GBMD_POT_EAM_JOHNSON;
+  const bool two_pass = c->pot == GBMD_POT_EAM_ALLOY || c->pot == GBMD_POT_EAM_JOHNSON ||
+                        c->pot == GBMD_POT_EAM_SUTTON_CHEN;
   double* v_spare = c->vbuf[c->cur_s ^ 1];
   c->pipe_tr_n = 0;
   if ((rc = trace_mark(c, m, GBMD_PIPE_MARK_START, -1))) return rc;

@@ -16,6 +16,7 @@
 //   gb300_eam_alloy_force   eam_alloy_force   (eam_potential_multimat.cu L88-109), with the
 //                           eam_rho / eam_rho2emb / eam_force split as separate instances
 //   gb300_johnson_force     johnson_force     (johnson.h, eam_potential.cu L69-193)
+//   gb300_sutton_chen_force sutton_chen_force (sutton_chen.h, eam_potential.cu L69-193)
 //   gb300_force             any of them, chosen by the slot `potential`
 // Whole-step operators (config_numerical_schemes.msp L23-28, L44-52;
 // config_move_particles.msp L116-152):
@@ -51,6 +52,7 @@
 #include <onika/physics/units.h>
 #include <yaml-cpp/yaml.h>
 #include "johnson.h"  // src/potential/eam_potentials/johnson (EamJohnsonParameters + its YAML decoder)
+#include "sutton_chen.h"  // src/potential/eam_potentials/sutton_chen (EamSuttonChenParameters + YAML)
 
 #include <gbmd.h>
 
@@ -433,6 +435,40 @@ class Gb300JohnsonForceNode : public OperatorNode {
   }
 };
 
+// sutton_chen_force (sutton_chen.h L30-67 through the same template).
+template <class GridT>
+class Gb300SuttonChenForceNode : public OperatorNode {
+  ADD_SLOT(EamSuttonChenParameters, parameters, INPUT, REQUIRED);
+  ADD_SLOT(double, rcut, INPUT, REQUIRED);
+  ADD_SLOT(double, rcut_max, INPUT_OUTPUT, 0.0);
+  ADD_SLOT(double, ghost_dist_max, INPUT_OUTPUT, 0.0);
+  ADD_SLOT(exanb::GridChunkNeighbors, chunk_neighbors, INPUT, exanb::GridChunkNeighbors{}, DocString{"unused"});
+  ADD_SLOT(ParticleSpecies, species, INPUT, REQUIRED);
+  ADD_SLOT(GridT, grid, INPUT_OUTPUT);
+  ADD_SLOT(Domain, domain, INPUT, REQUIRED);
+  ADD_SLOT(bool, trigger_thermo_state, INPUT, OPTIONAL);
+  ADD_SLOT(bool, compute_virial, INPUT, false);
+  ADD_SLOT(double, rcut_inc, INPUT, 1.0, DocString{"neighbour skin (global.rcut_inc)"});
+  ADD_SLOT(std::string, precision, INPUT, std::string{"mixed"}, DocString{"mixed or fp64"});
+  GB300_SESSION_SLOT;
+
+ public:
+  inline void execute() override final {
+    *rcut_max = std::max(*rcut, *rcut_max);
+    *ghost_dist_max = std::max(*ghost_dist_max, 2.0 * (*rcut));
+    if (grid->number_of_cells() == 0) return;
+    gb300::Session& s = session_for(*gb300_session, *domain, *species);
+    if (!s.potential_set) {
+      const EamSuttonChenParameters& q = *parameters;
+      const double sp[5] = {q.c, q.epsilon, q.a0, q.n, q.m};
+      gb300_ops::ok(s.ctx, gbmd_set_eam_sutton_chen(s.ctx, sp, *rcut), "gbmd_set_eam_sutton_chen");
+      finish_setup(s, *rcut_inc, *precision);
+    }
+    const bool energy = trigger_thermo_state.has_value() && *trigger_thermo_state;
+    compute_force_call("gb300_sutton_chen_force", s, *grid, *species, energy, energy && *compute_virial, 0);
+  }
+};
+
 template <class GridT>
 class Gb300ForceNode : public OperatorNode {
   ADD_SLOT(std::string, potential, INPUT, REQUIRED, DocString{"lj, eam_alloy or johnson"});
@@ -568,6 +604,8 @@ using Gb300EamAlloyForceTmpl = Gb300EamAlloyForceNode<GridT>;
 template <class GridT>
 using Gb300JohnsonForceTmpl = Gb300JohnsonForceNode<GridT>;
 template <class GridT>
+using Gb300SuttonChenForceTmpl = Gb300SuttonChenForceNode<GridT>;
+template <class GridT>
 using Gb300PushFVRTmpl = Gb300PushNode<GridT, true>;
 template <class GridT>
 using Gb300PushFVTmpl = Gb300PushNode<GridT, false>;
@@ -587,6 +625,8 @@ ONIKA_AUTORUN_INIT(gb300_md_ops) {
                                                     make_grid_variant_operator<Gb300EamAlloyForceTmpl>);
   OperatorNodeFactory::instance()->register_factory("gb300_johnson_force",
                                                     make_grid_variant_operator<Gb300JohnsonForceTmpl>);
+  OperatorNodeFactory::instance()->register_factory("gb300_sutton_chen_force",
+                                                    make_grid_variant_operator<Gb300SuttonChenForceTmpl>);
   OperatorNodeFactory::instance()->register_factory("gb300_push_f_v_r", make_grid_variant_operator<Gb300PushFVRTmpl>);
   OperatorNodeFactory::instance()->register_factory("gb300_push_f_v", make_grid_variant_operator<Gb300PushFVTmpl>);
   OperatorNodeFactory::instance()->register_factory("gb300_neighbors", make_grid_variant_operator<Gb300NeighborsTmpl>);

@@ -313,6 +313,32 @@ class johnson_force(Operator):
         sim.ctx.compute_forces(energy=energy, virial=virial)
 
 
+class sutton_chen_force(Operator):
+    """The mono-material analytic EAM sutton_chen_force (sutton_chen.h
+    L30-67 through the two-pass template, eam_potential.cu L69-193): both
+    passes in one call.  `parameters` holds c, epsilon, a0, n, m as
+    quantities, converted as the reference's YAML decoder does (L73-89)."""
+    name = "sutton_chen_force"
+    required = ("rcut", "parameters")
+
+    def bind(self, sim: Simulation):
+        from .systems import SUTTON_CHEN_PARAM_NAMES
+        p = self.slots["parameters"]
+        missing = [k for k in SUTTON_CHEN_PARAM_NAMES if k not in p]
+        if missing:
+            raise OperatorError("sutton_chen_force: missing parameters %s" % ", ".join(missing))
+        if len(sim.species) > 1:
+            raise OperatorError("sutton_chen_force: single material potential, %d species declared"
+                                % len(sim.species))
+        rcut = quantity(self.slots["rcut"])
+        sim.ctx.set_eam_sutton_chen(np.array([quantity(p[k]) for k in SUTTON_CHEN_PARAM_NAMES]), rcut)
+        sim.rcut_max = max(sim.rcut_max, rcut)
+        sim.ghost_dist_max = max(sim.ghost_dist_max, 2.0 * rcut)
+
+    def execute(self, sim: Simulation, energy=True, virial=False):
+        sim.ctx.compute_forces(energy=energy, virial=virial)
+
+
 class chunk_neighbors(Operator):
     name = "chunk_neighbors"
 
@@ -426,7 +452,8 @@ def verlet_nve(sim: Simulation, nsteps: int, dt: float, rebuild_every: int = 10,
 
 FORCE_OPERATORS = {"lj_compute_force": lj_compute_force, "lj_compute_force_symetric": lj_compute_force_symetric,
                    "lj_multi_force": lj_multi_force,
-                   "eam_alloy_force": eam_alloy_force, "johnson_force": johnson_force}
+                   "eam_alloy_force": eam_alloy_force, "johnson_force": johnson_force,
+                   "sutton_chen_force": sutton_chen_force}
 
 
 def compute_force_from_config(cfg: dict) -> Operator:

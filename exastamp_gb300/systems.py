@@ -158,6 +158,17 @@ def johnson_ta_params(conv: float = EV) -> np.ndarray:
     return np.array([v[k] * (conv if k in scaled else 1.0) for k in JOHNSON_PARAM_NAMES])
 
 
+# sutton_chen_force parameter order (EamSuttonChenParameters, sutton_chen.h L30-37)
+SUTTON_CHEN_PARAM_NAMES = ("c", "epsilon", "a0", "n", "m")
+
+
+def sutton_chen_cu_params() -> np.ndarray:
+    """The Cu parameter set of the reference's sutton_chen_force regression
+    case (data/regression_new/potentials/eam/eam_sutton_chen/single_specy.msp
+    L8-13) in internal units: c, epsilon (3.605e-21 J), a0 (0.327 nm), n, m."""
+    return np.array([3.317e+01, 3.605e-21 / _DA_A2_PS2_J, 3.27, 9.050, 5.005])
+
+
 def ta_bcc(ncell: int = 20, a: float = 3.3, T: float = 300.0, noise: float = 0.05, seed: int = 7,
            mass: float = 180.95) -> System:
     """BCC tantalum as in the johnson_force regression case (20^3 cells of

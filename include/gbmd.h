@@ -58,7 +58,8 @@ enum gbmd_potential {
   GBMD_POT_LJ = 1,          /* lj_compute_force */
   GBMD_POT_LJ_MULTI = 2,    /* lj_multi_force */
   GBMD_POT_EAM_ALLOY = 3,   /* eam_alloy_force (rho, rho2emb, force passes) */
-  GBMD_POT_EAM_JOHNSON = 4  /* johnson_force: analytic single-element EAM, 2 passes */
+  GBMD_POT_EAM_JOHNSON = 4, /* johnson_force: analytic single-element EAM, 2 passes */
+  GBMD_POT_EAM_SUTTON_CHEN = 5 /* sutton_chen_force: analytic single-element EAM, 2 passes */
 };
 
 enum gbmd_force_flags {
@@ -150,6 +151,13 @@ int gbmd_set_eam_alloy(gbmd_context* ctx, int nelements, int nrho, double drho, 
  * (energies in the energy unit, re in the length unit; alpha, beta, kappa,
  * lambda and eta dimensionless).  Every atom must be of type 0. */
 int gbmd_set_eam_johnson(gbmd_context* ctx, const double params[19], double rcut);
+/* sutton_chen_force (src/potential/eam_potentials/sutton_chen/sutton_chen.h
+ * L30-67 with the same mono-material 2-pass template): phi(r) = epsilon
+ * (a0/r)^n, rho(r) = (a0/r)^m, F(rho) = -c epsilon sqrt(rho).  params[5] in
+ * the order of EamSuttonChenParameters: c, epsilon, a0, n, m, in the
+ * caller's units (epsilon an energy, a0 a length; c, n, m dimensionless).
+ * Every atom must be of type 0. */
+int gbmd_set_eam_sutton_chen(gbmd_context* ctx, const double params[5], double rcut);
 int gbmd_load_setfl(gbmd_context* ctx, const char* path, double rcut, double conv_z2r,
                     double conv_frho);
 

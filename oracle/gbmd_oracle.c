@@ -17,6 +17,9 @@
  *   EAM spline   src/potential/eam_potentials/eam_alloy/eam_alloy.cpp L29-58
  *   EAM lookups  src/potential/eam_potentials/eam_alloy/eam_alloy.h L198-313
  *   EAM passes   src/potential/eam_potential_template/eam_force_op_multimat.h L114-343
+ *   mono-material EAM passes  src/potential/eam_potential_template/eam_force_op_singlemat.h L39-171
+ *   johnson      src/potential/eam_potentials/johnson/johnson.h L55-176
+ *   sutton_chen  src/potential/eam_potentials/sutton_chen/sutton_chen.h L40-66
  *   zero / accel src/compute/zero_force_energy.cu L38-47, src/compute/force_to_accel.cu L42-48
  *   push         src/numerical_schemes/push_vec3_2nd_order_xform_minimization.cpp L33-38, L116-149
  *   thermo       src/thermo_state/simulation_thermodynamic_state.cpp L101-163
@@ -675,13 +678,36 @@ void orc_ej_embed(const orc_johnson_params* p, double rho, double* f, double* df
   }
 }
 
+/* sutton_chen_force: phi = epsilon (a0/r)^n (sutton_chen.h L40-46), rho =
+ * (a0/r)^m (L48-56), F = -c epsilon sqrt(rho) (L58-66), derivatives as there */
+void orc_sc_phi(const orc_sutton_chen_params* p, double r, double* phi, double* dphi) {
+  const double ratio = p->a0 / r;
+  *phi = p->epsilon * pow(ratio, p->n);
+  *dphi = -1 * p->n * *phi / r;
+}
+
+void orc_sc_rho(const orc_sutton_chen_params* p, double r, double* rho, double* drho) {
+  const double ratio = p->a0 / r;
+  *rho = pow(ratio, p->m);
+  *drho = -1 * p->m * *rho / r;
+}
+
+void orc_sc_embed(const orc_sutton_chen_params* p, double rho, double* f, double* df) {
+  const double sq = sqrt(rho);
+  *f = -1. * p->c * p->epsilon * sq;
+  *df = 0.5 * *f / (rho > 0 ? rho : 0);
+}
+
+typedef void (*orc_pair_fn)(const void* p, double r, double* v, double* dv);
+
 /* The two passes of the mono-material template (eam_potential.cu L125-170):
  * EmbOp (eam_force_op_singlemat.h L39-84): rho_i, ep_i = F(rho_i), F'_i;
  * ForceOp (L86-171): de = (rho'(F'_i + F'_j) + phi')/r, f_i += de*dr,
  * ep_i += phi/2, vir_i += -1/2 f (x) dr.  fp receives F'. */
-void orc_ej_forces(int64_t n, const double* x, const double* y, const double* z, const int64_t* off,
-                   const int32_t* nbr, const int8_t* img, const double L[3], const orc_johnson_params* p,
-                   double rcut, double* fp, double* fx, double* fy, double* fz, double* ep, double* vir) {
+static void analytic_two_pass(int64_t n, const double* x, const double* y, const double* z, const int64_t* off,
+                              const int32_t* nbr, const int8_t* img, const double L[3], const void* p,
+                              orc_pair_fn rho_fn, orc_pair_fn phi_fn, orc_pair_fn emb_fn, double rcut,
+                              double* fp, double* fx, double* fy, double* fz, double* ep, double* vir) {
   const double rc2 = rcut * rcut;
 #pragma omp parallel for schedule(dynamic, 256)
   for (int64_t i = 0; i < n; ++i) {
@@ -692,11 +718,11 @@ void orc_ej_forces(int64_t n, const double* x, const double* y, const double* z,
       const double d2 = pair_d2(x, y, z, i, nbr[k], nn, L, &dx, &dy, &dz);
       if (!(d2 <= rc2)) continue;
       double v, dv;
-      orc_ej_rho(p, sqrt(d2), &v, &dv);
+      rho_fn(p, sqrt(d2), &v, &dv);
       rho += v;
     }
     double f, df;
-    orc_ej_embed(p, rho, &f, &df);
+    emb_fn(p, rho, &f, &df);
     fp[i] = df;
     if (ep) ep[i] = f;
   }
@@ -711,8 +737,8 @@ void orc_ej_forces(int64_t n, const double* x, const double* y, const double* z,
       if (!(d2 <= rc2)) continue;
       const double r = sqrt(d2);
       double rh, drh, ph, dph;
-      orc_ej_rho(p, r, &rh, &drh);
-      orc_ej_phi(p, r, &ph, &dph);
+      rho_fn(p, r, &rh, &drh);
+      phi_fn(p, r, &ph, &dph);
       const double de = (drh * (fp[i] + fp[j]) + dph) / r;
       const double fex = de * dx, fey = de * dy, fez = de * dz;
       _fx += fex; _fy += fey; _fz += fez;
@@ -723,6 +749,25 @@ void orc_ej_forces(int64_t n, const double* x, const double* y, const double* z,
     if (ep) ep[i] += _ep;
     if (vir) for (int q = 0; q < 9; ++q) vir[9 * i + q] = _v[q];
   }
+}
+
+static void ej_rho_v(const void* p, double r, double* v, double* dv) { orc_ej_rho((const orc_johnson_params*)p, r, v, dv); }
+static void ej_phi_v(const void* p, double r, double* v, double* dv) { orc_ej_phi((const orc_johnson_params*)p, r, v, dv); }
+static void ej_emb_v(const void* p, double r, double* v, double* dv) { orc_ej_embed((const orc_johnson_params*)p, r, v, dv); }
+static void sc_rho_v(const void* p, double r, double* v, double* dv) { orc_sc_rho((const orc_sutton_chen_params*)p, r, v, dv); }
+static void sc_phi_v(const void* p, double r, double* v, double* dv) { orc_sc_phi((const orc_sutton_chen_params*)p, r, v, dv); }
+static void sc_emb_v(const void* p, double r, double* v, double* dv) { orc_sc_embed((const orc_sutton_chen_params*)p, r, v, dv); }
+
+void orc_ej_forces(int64_t n, const double* x, const double* y, const double* z, const int64_t* off,
+                   const int32_t* nbr, const int8_t* img, const double L[3], const orc_johnson_params* p,
+                   double rcut, double* fp, double* fx, double* fy, double* fz, double* ep, double* vir) {
+  analytic_two_pass(n, x, y, z, off, nbr, img, L, p, ej_rho_v, ej_phi_v, ej_emb_v, rcut, fp, fx, fy, fz, ep, vir);
+}
+
+void orc_sc_forces(int64_t n, const double* x, const double* y, const double* z, const int64_t* off,
+                   const int32_t* nbr, const int8_t* img, const double L[3], const orc_sutton_chen_params* p,
+                   double rcut, double* fp, double* fx, double* fy, double* fz, double* ep, double* vir) {
+  analytic_two_pass(n, x, y, z, off, nbr, img, L, p, sc_rho_v, sc_phi_v, sc_emb_v, rcut, fp, fx, fy, fz, ep, vir);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1080,6 +1125,7 @@ static double pot_rcut(int pot_kind, const void* pot) {
   if (pot_kind == ORC_POT_LJ) return ((const orc_lj_params*)pot)->rcut;
   if (pot_kind == ORC_POT_LJ_MULTI) return ((const orc_lj_multi_params*)pot)->rcut_max;
   if (pot_kind == ORC_POT_EAM_JOHNSON) return ((const orc_johnson_pot*)pot)->rcut;
+  if (pot_kind == ORC_POT_EAM_SUTTON_CHEN) return ((const orc_sutton_chen_pot*)pot)->rcut;
   return ((const orc_eam_pot*)pot)->rcut;
 }
 
@@ -1091,6 +1137,9 @@ static void all_forces(int64_t n, const double* x, const double* y, const double
   if (pot_kind == ORC_POT_EAM_JOHNSON) {
     const orc_johnson_pot* p = (const orc_johnson_pot*)pot;
     orc_ej_forces(n, x, y, z, l->off, l->nbr, l->img, L, &p->p, p->rcut, rho, ax, ay, az, ep, vir);
+  } else if (pot_kind == ORC_POT_EAM_SUTTON_CHEN) {
+    const orc_sutton_chen_pot* p = (const orc_sutton_chen_pot*)pot;
+    orc_sc_forces(n, x, y, z, l->off, l->nbr, l->img, L, &p->p, p->rcut, rho, ax, ay, az, ep, vir);
   } else if (pot_kind == ORC_POT_EAM) {
     const orc_eam_pot* p = (const orc_eam_pot*)pot;
     orc_eam_density(n, x, y, z, type, l->off, l->nbr, l->img, L, &p->t, p->rcut, rho);

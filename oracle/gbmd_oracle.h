@@ -48,7 +48,7 @@ typedef struct {
 } orc_eam_pot;
 
 /* Kinds for orc_run_nve */
-enum { ORC_POT_LJ = 0, ORC_POT_LJ_MULTI = 1, ORC_POT_EAM = 2, ORC_POT_EAM_JOHNSON = 3 };
+enum { ORC_POT_LJ = 0, ORC_POT_LJ_MULTI = 1, ORC_POT_EAM = 2, ORC_POT_EAM_JOHNSON = 3, ORC_POT_EAM_SUTTON_CHEN = 4 };
 
 /* johnson_force parameters, EamJohnsonParameters order (johnson.h L28-49) */
 typedef struct {
@@ -59,6 +59,16 @@ typedef struct {
   orc_johnson_params p;
   double rcut;
 } orc_johnson_pot;
+
+/* sutton_chen_force parameters, EamSuttonChenParameters order (sutton_chen.h L30-37) */
+typedef struct {
+  double c, epsilon, a0, n, m;
+} orc_sutton_chen_params;
+
+typedef struct {
+  orc_sutton_chen_params p;
+  double rcut;
+} orc_sutton_chen_pot;
 
 typedef struct {
   double epsilon, sigma, rcut;
@@ -165,6 +175,13 @@ int64_t orc_last_list_builds(void);
 void orc_ej_phi(const orc_johnson_params* p, double r, double* phi, double* dphi);
 void orc_ej_rho(const orc_johnson_params* p, double r, double* rho, double* drho);
 void orc_ej_embed(const orc_johnson_params* p, double rho, double* f, double* df);
+void orc_sc_phi(const orc_sutton_chen_params* p, double r, double* phi, double* dphi);
+void orc_sc_rho(const orc_sutton_chen_params* p, double r, double* rho, double* drho);
+void orc_sc_embed(const orc_sutton_chen_params* p, double rho, double* f, double* df);
+/* Both passes of sutton_chen_force over a CSR list; fp receives F'(rho_i). */
+void orc_sc_forces(int64_t n, const double* x, const double* y, const double* z, const int64_t* off,
+                   const int32_t* nbr, const int8_t* img, const double L[3], const orc_sutton_chen_params* p,
+                   double rcut, double* fp, double* fx, double* fy, double* fz, double* ep, double* vir);
 /* Both passes of johnson_force over a CSR list; fp receives F'(rho_i). */
 void orc_ej_forces(int64_t n, const double* x, const double* y, const double* z, const int64_t* off,
                    const int32_t* nbr, const int8_t* img, const double L[3], const orc_johnson_params* p,

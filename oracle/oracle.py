@@ -58,7 +58,7 @@ class LJMultiParams(C.Structure):
                 ("sigma", C.c_void_p), ("rcut", C.c_void_p), ("rcut_max", C.c_double)]
 
 
-POT_LJ, POT_LJ_MULTI, POT_EAM, POT_EAM_JOHNSON = 0, 1, 2, 3
+POT_LJ, POT_LJ_MULTI, POT_EAM, POT_EAM_JOHNSON, POT_EAM_SUTTON_CHEN = 0, 1, 2, 3, 4
 
 
 class JohnsonParams(C.Structure):
@@ -75,6 +75,21 @@ class Johnson:
 
     def __init__(self, params, rcut):
         self.pot = JohnsonPot(JohnsonParams(*[float(v) for v in params]), float(rcut))
+
+
+class SuttonChenParams(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("c", "epsilon", "a0", "n", "m")]
+
+
+class SuttonChenPot(C.Structure):
+    _fields_ = [("p", SuttonChenParams), ("rcut", C.c_double)]
+
+
+class SuttonChen:
+    """sutton_chen_force parameters (c, epsilon, a0, n, m) + rcut."""
+
+    def __init__(self, params, rcut):
+        self.pot = SuttonChenPot(SuttonChenParams(*[float(v) for v in params]), float(rcut))
 
 _lib = None
 
@@ -125,7 +140,9 @@ def lib():
         L.orc_lj_loss_grad.argtypes = [i64] + [vp] * 7 + [vp] + [vp] * 4 + [dbl, dbl, vp]
         L.orc_ej_forces.restype = None
         L.orc_ej_forces.argtypes = [i64] + [vp] * 7 + [vp, dbl] + [vp] * 6
-        for f in ("orc_ej_phi", "orc_ej_rho", "orc_ej_embed"):
+        L.orc_sc_forces.restype = None
+        L.orc_sc_forces.argtypes = [i64] + [vp] * 7 + [vp, dbl] + [vp] * 6
+        for f in ("orc_ej_phi", "orc_ej_rho", "orc_ej_embed", "orc_sc_phi", "orc_sc_rho", "orc_sc_embed"):
             getattr(L, f).restype = None
             getattr(L, f).argtypes = [vp, dbl, vp, vp]
         L.orc_num_threads.restype = i32
@@ -296,6 +313,23 @@ def ej_forces(x, y, z, nl, L, pot, virial=True):
     fx, fy, fz, ep, v = _outs(n, virial)
     fp = np.zeros(n)
     lib().orc_ej_forces(n, _p(x), _p(y), _p(z), _p(nl.off), _p(nl.nbr), _p(nl.img), _p(_f64(L)),
+                        C.addressof(pot.pot.p), pot.pot.rcut, _p(fp), _p(fx), _p(fy), _p(fz), _p(ep), _p(v))
+    return fx, fy, fz, ep, v, fp
+
+
+def sc_function(name, pot, arg):
+    """(value, derivative) of orc_sc_phi / orc_sc_rho / orc_sc_embed."""
+    a, b = C.c_double(), C.c_double()
+    getattr(lib(), "orc_sc_" + name)(C.addressof(pot.pot.p), float(arg), C.addressof(a), C.addressof(b))
+    return a.value, b.value
+
+
+def sc_forces(x, y, z, nl, L, pot, virial=True):
+    """sutton_chen_force, both passes: returns (fx, fy, fz, ep, vir, F')."""
+    n = len(x)
+    fx, fy, fz, ep, v = _outs(n, virial)
+    fp = np.zeros(n)
+    lib().orc_sc_forces(n, _p(x), _p(y), _p(z), _p(nl.off), _p(nl.nbr), _p(nl.img), _p(_f64(L)),
                         C.addressof(pot.pot.p), pot.pot.rcut, _p(fp), _p(fx), _p(fy), _p(fz), _p(ep), _p(v))
     return fx, fy, fz, ep, v, fp
 

@@ -5,6 +5,7 @@ import ctypes
 import os
 import subprocess
 
+import numpy as np
 import pytest
 
 from exastamp_gb300 import operators as OP
@@ -42,6 +43,21 @@ def test_quantity_units():
     assert OP.quantity(2.5) == 2.5
     with pytest.raises(OP.OperatorError):
         OP.quantity("3 furlong")
+
+
+def test_sutton_chen_regression_parameters_in_internal_units():
+    """The run file's quantities (single_specy.msp L8-13) convert to the
+    parameter vector the tests use; a missing parameter is refused."""
+    from exastamp_gb300 import systems as S
+    got = [OP.quantity(v) for v in (3.317e01, "3.605e-21 J", "0.327e-09 m", 9.050, 5.005)]
+    assert np.allclose(got, S.sutton_chen_cu_params(), rtol=1e-15, atol=0.0)
+    assert S.SUTTON_CHEN_PARAM_NAMES == ("c", "epsilon", "a0", "n", "m")
+    op = OP.compute_force_from_config({"compute_force": "sutton_chen_force",
+                                       "sutton_chen_force": {"rcut": "7.29 ang",
+                                                             "parameters": {"c": 1.0, "epsilon": 1.0}}})
+    assert isinstance(op, OP.sutton_chen_force)
+    with pytest.raises(OP.OperatorError):
+        op.bind(None)
 
 
 def test_required_slots_raise():

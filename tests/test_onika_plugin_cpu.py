@@ -14,7 +14,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PLUGIN = os.path.join(ROOT, "exastamp_gb300", "onika", "gb300_md_ops.cpp")
 
 OPERATORS = ("gb300_force", "gb300_lj_force", "gb300_lj_force_symetric", "gb300_lj_multi_force",
-             "gb300_eam_alloy_force", "gb300_johnson_force", "gb300_push_f_v_r", "gb300_push_f_v",
+             "gb300_eam_alloy_force", "gb300_johnson_force", "gb300_sutton_chen_force", "gb300_push_f_v_r",
+             "gb300_push_f_v",
              "gb300_neighbors", "gb300_sync_grid")
 
 
@@ -40,7 +41,8 @@ def test_every_operator_instantiated_for_both_grid_flavours(plugin_object):
     lines = _symbols(plugin_object)
     text = "\n".join(lines)
     for cls in ("Gb300ForceNode", "Gb300LJForceNode", "Gb300LJMultiForceNode", "Gb300EamAlloyForceNode",
-                "Gb300JohnsonForceNode", "Gb300PushNode", "Gb300NeighborsNode", "Gb300SyncGridNode"):
+                "Gb300JohnsonForceNode", "Gb300SuttonChenForceNode", "Gb300PushNode", "Gb300NeighborsNode",
+                "Gb300SyncGridNode"):
         for flavour in ("StubGrid<false>", "StubGrid<true>"):
             assert any(cls + "<exanb::" + flavour in ln and "::execute()" in ln for ln in lines), (cls, flavour)
     src = open(PLUGIN).read()
