@@ -235,6 +235,8 @@ int pipe_slabs_for(const gbmd_context* c) {
   return S >= 4 ? S : 0;
 }
 
+namespace {
+
 // One mark of the step's timeline (gbmd_get_host_pipeline_trace): an event
 // with timing on `st` after the work issued there so far.
 int trace_mark(gbmd_context* c, cudaStream_t st, int kind, int idx) {
@@ -261,8 +263,8 @@ struct StreamScope {
   ~StreamScope() { c->stream = saved; }
 };
 
-int pipe_step(gbmd_context* c, double dt, const double* const host[9], const double* const hdev[9],
-              const int32_t* inv, int S) {
+int pipe_issue(gbmd_context* c, double dt, const double* const host[9], const double* const hdev[9],
+               const int32_t* inv, int S) {
   int rc = ensure_pipe(c);
   if (rc) return rc;
   const bool ce = c->pipe_link_mode == 0;
@@ -445,6 +447,27 @@ int pipe_step(gbmd_context* c, double dt, const double* const host[9], const dou
   return GBMD_OK;
 }
 
+// Every stream the step issued on has finished (errors ignored): after a
+// failed launch the pieces already issued may still read and write the
+// caller's arrays, and the caller may free them once the call returns.
+void pipe_drain(gbmd_context* c) {
+  cudaStreamSynchronize(c->stream);
+  if (c->pipe_in) cudaStreamSynchronize(c->pipe_in);
+  if (c->pipe_out) cudaStreamSynchronize(c->pipe_out);
+  if (c->pipe_r) cudaStreamSynchronize(c->pipe_r);
+  for (int q = 0; q + 1 < PIPE_STREAMS; ++q)
+    if (c->pipe_cs[q]) cudaStreamSynchronize(c->pipe_cs[q]);
+}
+
+}  // namespace
+
+int pipe_step(gbmd_context* c, double dt, const double* const host[9], const double* const hdev[9],
+              const int32_t* inv, int S) {
+  const int rc = pipe_issue(c, dt, host, hdev, inv, S);
+  if (rc) pipe_drain(c);
+  return rc;
+}
+
 int pipe_trace_read(gbmd_context* c, int cap, double* t_ms, int* kind, int* index, int* count) {
   const int n = c->pipe_tr_n;
   *count = n;
@@ -477,10 +500,12 @@ void pipe_free(gbmd_context* c) {
   }
   if (c->pipe_start) cudaEventDestroy(c->pipe_start);
   if (c->pipe_out_done) cudaEventDestroy(c->pipe_out_done);
+  c->pipe_start = c->pipe_out_done = nullptr;
   for (int k = 0; k < MAX_SLABS; ++k) {
     if (c->pipe_in_ev[k]) cudaEventDestroy(c->pipe_in_ev[k]);
     if (c->pipe_f_ev[k]) cudaEventDestroy(c->pipe_f_ev[k]);
     if (c->pipe_d_ev[k]) cudaEventDestroy(c->pipe_d_ev[k]);
+    c->pipe_in_ev[k] = c->pipe_f_ev[k] = c->pipe_d_ev[k] = nullptr;
   }
   if (c->pipe_dev) cudaFree(c->pipe_dev);
   if (c->pipe_host) cudaFreeHost(c->pipe_host);
