@@ -82,6 +82,10 @@ def parse():
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     p.add_argument("--rebuild-every", type=int, default=10,
                    help="list rebuild interval in steps; -1 rebuilds on the skin/2 displacement trigger")
+    p.add_argument("--list-buffer", type=float, default=-1.0,
+                   help="two-level neighbour list: outer buffer beyond rcut + skin (0, the default: off)")
+    p.add_argument("--no-two-level", action="store_true",
+                   help="skip the 200-step comparison of the one- and two-level lists (EAM workload)")
     p.add_argument("--e2e-steps", type=int, default=20)
     p.add_argument("--fp64-steps", type=int, default=40)
     p.add_argument("--no-cpu", action="store_true")
@@ -110,6 +114,8 @@ def parse():
     p.add_argument("--no-oracle-check", action="store_true",
                    help="skip the force error against the FP64 oracle at the benchmarked state")
     a = p.parse_args()
+    if a.list_buffer >= 0.0:
+        WORKLOADS[a.workload] = dict(WORKLOADS[a.workload], list_buffer=a.list_buffer)
     if a.ncell:
         extra = {"n": 4 * a.ncell ** 3} if WORKLOADS[a.workload]["kind"] == "lj_multi" else {}
         WORKLOADS[a.workload] = dict(WORKLOADS[a.workload], ncell=a.ncell, **extra)
@@ -141,6 +147,7 @@ def bind_potential(ctx, w):
     else:
         ctx.set_lj(1.0, 1.0, w["rcut"])
     ctx.set_skin(w["skin"])
+    ctx.set_list_buffer(w.get("list_buffer", 0.0))
 
 
 class ClockSampler:
@@ -500,6 +507,37 @@ def nve_drift(ctx, s, w, R, mixed_steps, fp64_steps):
     return out
 
 
+def two_level_section(ctx, s, w, R, torch, stream, steps=200, buffer=1.0):
+    """From one saved state: `steps` NVE steps (rebuild every R, CUDA graphs)
+    with the one-level list, then the same steps with the two-level list
+    (gbmd_set_list_buffer(buffer)), each after a fresh full build.  An outer
+    build comes every ~100 steps in this state, so a window of this length
+    holds its amortised cost (a 20-step window holds one or none)."""
+    st = ctx.download(KEYS9)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {"steps": steps, "list_buffer": buffer, "rebuild_every": R}
+    for name, b in (("one_level", 0.0), ("two_level", buffer)):
+        ctx.upload_state(*(st[k] for k in KEYS9))
+        ctx.set_list_buffer(b)
+        ctx.build_neighbors()
+        ctx.run_nve(2 * R, w["dt"], R, 0, use_graph=True)  # graph capture
+        ctx.upload_state(*(st[k] for k in KEYS9))
+        ctx.build_neighbors()
+        b0, o0 = ctx.list_builds(), ctx.list_buffer()[1]
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        ctx.run_nve(steps, w["dt"], R, 0, use_graph=True)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = {"ms_per_step": ev0.elapsed_time(ev1) / steps, "list_builds": ctx.list_builds() - b0,
+                     "outer_builds": ctx.list_buffer()[1] - o0}
+    out["one_level_over_two_level"] = out["one_level"]["ms_per_step"] / out["two_level"]["ms_per_step"]
+    ctx.set_list_buffer(w.get("list_buffer", 0.0))
+    ctx.upload_state(*(st[k] for k in KEYS9))
+    ctx.build_neighbors()
+    return out
+
+
 def e2e_section(ctx, s, w, R, steps, ws, torch, stream):
     """The same step through the C ABI with the grid state in pinned host
     arrays: gbmd_run_nve_host per step, copies inside the timed region."""
@@ -663,12 +701,14 @@ def measure(args, w, ws, dev, stream, torch, *, steps, fp64_steps, e2e_steps, dr
         barrier(ws)
         torch.cuda.synchronize()
         builds0 = ctx.list_builds()
+        outer0 = ctx.list_buffer()[1]
         ev0.record(stream)
         ctx.run_nve(steps, dt, R, thermo_every, use_graph=True)
         ev1.record(stream)
         torch.cuda.synchronize()
         barrier(ws)
         rebuilds = ctx.list_builds() - builds0
+        outer_builds = ctx.list_buffer()[1] - outer0
     finally:
         clk.__exit__()
     ms = ev0.elapsed_time(ev1)
@@ -695,9 +735,17 @@ def measure(args, w, ws, dev, stream, torch, *, steps, fp64_steps, e2e_steps, dr
     gpu_launches = kernels_per_step * (steps if energies_reused else steps + 1)
     gpu_launches += 2 * (n_thermo + (1 if thermo_every else 0))
     gpu_launches += 1 + n_thermo - (1 if last_is_thermo else 0)
+    # With a list buffer a rebuild is the outer test, the conditional's
+    # setter and the filter (3), plus 13 for an outer build (2 fills, the
+    # chain, copy-back, outer positions); with the trigger all 16 are gated
+    # launches inside its body.
+    two_level = w.get("list_buffer", 0.0) > 0.0
     if R < 0:
         n_graph = (steps // thermo_every) * thermo_every
-        gpu_launches += n_graph + 13 * rebuilds + 13 * (steps - n_graph)
+        per = 16 if two_level else 13
+        gpu_launches += n_graph + per * rebuilds + per * (steps - n_graph)
+    elif two_level:
+        gpu_launches += 3 * rebuilds + 13 * outer_builds
     else:
         gpu_launches += 9 * rebuilds
 
@@ -711,6 +759,8 @@ def measure(args, w, ws, dev, stream, torch, *, steps, fp64_steps, e2e_steps, dr
                       "precision": args.precision, "thermo_every": thermo_every,
                       "rebuild_every": R if R >= 0 else "on displacement > skin/2",
                       "list_builds_in_timed_region": rebuilds,
+                      "list_buffer": w.get("list_buffer", 0.0),
+                      "outer_list_builds_in_timed_region": outer_builds,
                       "warmup_steps_run": warm,
                       "neighbours_per_atom": npairs / s.n, "cells": nc.tolist(),
                       "lanes_per_atom": ctx.get_launch_ex()[0], "list_entries_per_load": ctx.get_launch_ex()[1],
@@ -817,6 +867,10 @@ def measure(args, w, ws, dev, stream, torch, *, steps, fp64_steps, e2e_steps, dr
     # ---- NVE energy drift, mixed vs FP64 from one state -----------------------
     if single and not args.no_drift and drift_steps:
         out["nve_drift"] = nve_drift(ctx, s, w, R, *drift_steps)
+
+    # ---- one- and two-level neighbour lists over 200 steps ----------------------
+    if single and not args.no_two_level and w["kind"] == "eam" and R > 0:
+        out["two_level_list"] = two_level_section(ctx, s, w, R, torch, stream)
 
     # ---- end-to-end through the C ABI with host buffers -----------------------
     if not args.no_e2e:

@@ -82,6 +82,8 @@ def lib(path: str = LIB_PATH):
             "gbmd_get_neighbor_staging": ([vp, P(i32)], i32),
             "gbmd_get_launch_ex": ([vp, P(i32), P(i32), P(i32)], i32),
             "gbmd_set_skin": ([vp, dbl], i32),
+            "gbmd_set_list_buffer": ([vp, dbl], i32),
+            "gbmd_get_list_buffer": ([vp, P(dbl), P(i64)], i32),
             "gbmd_build_neighbors": ([vp], i32),
             "gbmd_update_neighbors": ([vp, P(i32)], i32),
             "gbmd_export_pairs": ([vp, i64, vp, vp, vp, P(i64)], i32),
@@ -278,6 +280,18 @@ class Context:
         self._chk(self._L.gbmd_set_skin(self.h, float(skin)))
 
     # -- operators --------------------------------------------------------
+    def set_list_buffer(self, buffer):
+        """Two-level list: an outer list of radius rcut + skin + buffer, the
+        list filtered from it at each rebuild (gbmd_set_list_buffer)."""
+        self._chk(self._L.gbmd_set_list_buffer(self.h, float(buffer)))
+
+    def list_buffer(self):
+        """(buffer, outer list builds so far)."""
+        b = C.c_double()
+        k = C.c_int64()
+        self._chk(self._L.gbmd_get_list_buffer(self.h, C.byref(b), C.byref(k)))
+        return b.value, k.value
+
     def build_neighbors(self):
         self._chk(self._L.gbmd_build_neighbors(self.h))
 

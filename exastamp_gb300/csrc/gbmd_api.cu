@@ -34,7 +34,7 @@ int check_cuda(gbmd_context* c, cudaError_t e, const char* what) {
 }
 
 int sync_error_word(gbmd_context* c) {
-  GBMD_CUDA(c, cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int) * 8, cudaMemcpyDeviceToHost, c->stream));
+  GBMD_CUDA(c, cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int) * ERRW_WORDS, cudaMemcpyDeviceToHost, c->stream));
   GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
   return GBMD_OK;
 }
@@ -64,6 +64,7 @@ static void free_atoms(gbmd_context* c) {
   c->fpd = c->stage = c->rref = nullptr;
   c->nnb = nullptr;
   c->d_part = nullptr;
+  free_outer(c);
   c->cap = 0;
 }
 
@@ -116,6 +117,7 @@ static void drop_graph(gbmd_context* c) {
 
 static void invalidate_list(gbmd_context* c) {
   c->list_valid = false;
+  c->outer_valid = false;
   c->energy_step = -1, c->forces_valid_step = c->rho_valid_step = -1;
   drop_graph(c);
 }
@@ -125,7 +127,7 @@ static void set_rlist(gbmd_context* c, double rcut_max) {
   if (R != c->rlist) {
     c->rlist = R;
     c->grid_valid = false;
-    c->maxnb = 0;
+    c->maxnb = c->maxnb_out = 0;
   }
   invalidate_list(c);
 }
@@ -279,7 +281,18 @@ static int copy_rref(gbmd_context* c) {
   return GBMD_OK;
 }
 
+// A rebuild of the list the pair kernels read, and the positions the
+// displacement trigger measures from.  With a list buffer the outer list is
+// rebuilt only when needed.
 static int do_rebuild(gbmd_context* c, bool check) {
+  int rc = two_level(c) ? rebuild_two_level(c, check) : rebuild(c, check);
+  if (rc) return rc;
+  return copy_rref(c);
+}
+
+// The same with the sort into cells and the cell walk in any case (an
+// explicit gbmd_build_neighbors: rows in the canonical order of a fresh build).
+static int do_full_rebuild(gbmd_context* c, bool check) {
   int rc = rebuild(c, check);
   if (rc) return rc;
   return copy_rref(c);
@@ -293,32 +306,7 @@ __global__ void k_set_conditional(cudaGraphConditionalHandle h, const int* __res
   cudaGraphSetConditional(h, *gate ? 1u : 0u);
 }
 
-static int rebuild_if_displaced(gbmd_context* c) {
-  if (c->n == 0) return GBMD_OK;
-  int* gate = c->d_err + ERRW_GATE;
-  const double thr = 0.5 * c->skin;
-  if (!c->fused_trigger) {
-    GBMD_CUDA(c, cudaMemsetAsync(gate, 0, sizeof(int), c->stream));
-    k_displ_over<<<nblk(c->n, 256), 256, 0, c->stream>>>(c->n, c->X(), c->Y(), c->Z(), c->rref, c->cap, thr * thr,
-                                                          gate);
-  }
-  // fused_trigger: the kernel that moved the atoms (the force pass's fused
-  // first half, or k_first_half) has already tested them and raised the gate;
-  // it is cleared once the chain has read it, for the next such kernel
-  if (!c->capturing) {
-    // launched step by step: the chain's kernels check the gate themselves
-    int rc = rebuild(c, false, gate);
-    if (rc) return rc;
-    k_copy_rref_gated<<<chain_blocks(c, c->n, 256, gate, 8), 256, 0, c->stream>>>(
-        c->n, c->rbuf[c->cur], c->rref, c->cap, gate, c->d_err + ERRW_REBUILDS);
-    if (c->fused_trigger) GBMD_CUDA(c, cudaMemsetAsync(gate, 0, sizeof(int), c->stream));
-    return GBMD_OK;
-  }
-  // Inside a graph capture the chain goes into the body of an IF conditional
-  // node that the device opens only when the gate is set, so a step without
-  // a rebuild launches none of it.  The body keeps the gated variant's
-  // semantics (spare buffers, copy back) so the graph's buffer indices do not
-  // depend on the outcome.
+int capture_if(gbmd_context* c, const int* gate, int (*body)(gbmd_context*, const int*)) {
   cudaStreamCaptureStatus st;
   cudaGraph_t graph;
   const cudaGraphNode_t* deps = nullptr;
@@ -335,35 +323,77 @@ static int rebuild_if_displaced(gbmd_context* c) {
   np.conditional.size = 1;
   cudaGraphNode_t node;
   GBMD_CUDA(c, cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &np));
-  cudaGraph_t body = np.conditional.phGraph_out[0];
+  cudaGraph_t cond_body = np.conditional.phGraph_out[0];
   if (!c->cond_stream) GBMD_CUDA(c, cudaStreamCreateWithFlags(&c->cond_stream, cudaStreamNonBlocking));
-  GBMD_CUDA(c, cudaStreamBeginCaptureToGraph(c->cond_stream, body, nullptr, nullptr, 0,
+  GBMD_CUDA(c, cudaStreamBeginCaptureToGraph(c->cond_stream, cond_body, nullptr, nullptr, 0,
                                              cudaStreamCaptureModeThreadLocal));
   cudaStream_t main_stream = c->stream;
   c->stream = c->cond_stream;
-  c->full_chain_grids = true;
-  int rc = rebuild(c, false, gate);
-  if (rc == GBMD_OK)
-    k_copy_rref_gated<<<nblk(c->n, 256), 256, 0, c->stream>>>(c->n, c->rbuf[c->cur], c->rref, c->cap, gate,
-                                                               c->d_err + ERRW_REBUILDS);
-  c->full_chain_grids = false;
+  const int rc = body(c, gate);
   c->stream = main_stream;
   cudaGraph_t body_out = nullptr;
   const cudaError_t e = cudaStreamEndCapture(c->cond_stream, &body_out);
   if (rc) return rc;
   if (e != cudaSuccess) return check_cuda(c, e, "conditional body capture");
   GBMD_CUDA(c, cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  return GBMD_OK;
+}
+
+// the rebuild of a step whose displacement trigger fired, as the body of its
+// conditional node (full grids: the body runs only when there is work)
+static int triggered_rebuild_body(gbmd_context* c, const int* gate) {
+  c->full_chain_grids = true;
+  int rc = two_level(c) ? rebuild_two_level(c, false, gate) : rebuild(c, false, gate);
+  if (rc == GBMD_OK)
+    k_copy_rref_gated<<<nblk(c->n, 256), 256, 0, c->stream>>>(c->n, c->rbuf[c->cur], c->rref, c->cap, gate,
+                                                               c->d_err + ERRW_REBUILDS);
+  c->full_chain_grids = false;
+  return rc;
+}
+
+static int rebuild_if_displaced(gbmd_context* c) {
+  if (c->n == 0) return GBMD_OK;
+  int* gate = c->d_err + ERRW_GATE;
+  const double thr = 0.5 * c->skin;
+  if (!c->fused_trigger) {
+    GBMD_CUDA(c, cudaMemsetAsync(gate, 0, sizeof(int), c->stream));
+    k_displ_over<<<nblk(c->n, 256), 256, 0, c->stream>>>(c->n, c->X(), c->Y(), c->Z(), c->rref, c->cap, thr * thr,
+                                                          gate);
+  }
+  // fused_trigger: the kernel that moved the atoms (the force pass's fused
+  // first half, or k_first_half) has already tested them and raised the gate;
+  // it is cleared once the chain has read it, for the next such kernel
+  if (!c->capturing) {
+    // launched step by step: the chain's kernels check the gate themselves
+    int rc = two_level(c) ? rebuild_two_level(c, false, gate) : rebuild(c, false, gate);
+    if (rc) return rc;
+    k_copy_rref_gated<<<chain_blocks(c, c->n, 256, gate, 8), 256, 0, c->stream>>>(
+        c->n, c->rbuf[c->cur], c->rref, c->cap, gate, c->d_err + ERRW_REBUILDS);
+    if (c->fused_trigger) GBMD_CUDA(c, cudaMemsetAsync(gate, 0, sizeof(int), c->stream));
+    return GBMD_OK;
+  }
+  // Inside a graph capture the chain goes into the body of an IF conditional
+  // node that the device opens only when the gate is set, so a step without
+  // a rebuild launches none of it.  The body keeps the gated variant's
+  // semantics (spare buffers, copy back) so the graph's buffer indices do not
+  // depend on the outcome.
+  int rc = capture_if(c, gate, triggered_rebuild_body);
+  if (rc) return rc;
   if (c->fused_trigger) GBMD_CUDA(c, cudaMemsetAsync(gate, 0, sizeof(int), c->stream));
   return GBMD_OK;
 }
 
-// folds the device-side rebuild count into list_builds (stream synchronised)
+// folds the device-side counts of displacement-triggered rebuilds and of
+// outer list builds into list_builds and outer_builds (stream synchronised)
 static int collect_device_rebuilds(gbmd_context* c) {
-  int cnt = 0;
-  GBMD_CUDA(c, cudaMemcpyAsync(&cnt, c->d_err + ERRW_REBUILDS, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  int cnt[5] = {0, 0, 0, 0, 0};
+  static_assert(ERRW_OUTER_BUILDS - ERRW_REBUILDS == 4, "counter words");
+  GBMD_CUDA(c, cudaMemcpyAsync(cnt, c->d_err + ERRW_REBUILDS, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
   GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_REBUILDS, 0, sizeof(int), c->stream));
+  GBMD_CUDA(c, cudaMemsetAsync(c->d_err + ERRW_OUTER_BUILDS, 0, sizeof(int), c->stream));
   GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
-  c->list_builds += cnt;
+  c->list_builds += cnt[0];
+  c->outer_builds += cnt[4];
   return GBMD_OK;
 }
 
@@ -429,15 +459,15 @@ int gbmd_create(gbmd_context** out, int device, void* stream) {
     }
     c->own_stream = true;
   }
-  if (cudaMalloc(&c->d_err, sizeof(int) * 8) != cudaSuccess ||
-      cudaMallocHost(&c->h_err, sizeof(int) * 8) != cudaSuccess ||
+  if (cudaMalloc(&c->d_err, sizeof(int) * ERRW_WORDS) != cudaSuccess ||
+      cudaMallocHost(&c->h_err, sizeof(int) * ERRW_WORDS) != cudaSuccess ||
       cudaMalloc(&c->d_thermo, sizeof(double) * 27) != cudaSuccess ||
       cudaMallocHost(&c->h_thermo, sizeof(double) * 27) != cudaSuccess ||
       cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
     gbmd_destroy(c);
     return GBMD_ERR_CUDA;
   }
-  int init[8] = {0, 0, 0, -1, -1, 0, 0, 0};
+  int init[ERRW_WORDS] = {0, 0, 0, -1, -1};
   cudaMemcpy(c->d_err, init, sizeof(init), cudaMemcpyHostToDevice);
   *out = c;
   return GBMD_OK;
@@ -449,7 +479,7 @@ int gbmd_destroy(gbmd_context* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   drop_graph(c);
   free_atoms(c);
-  cudaFree(c->cell_start); cudaFree(c->cell_fill); cudaFree(c->scan_tmp); cudaFree(c->nbr);
+  cudaFree(c->cell_start); cudaFree(c->cell_fill); cudaFree(c->scan_tmp); cudaFree(c->nbr); cudaFree(c->nbr_out);
   cudaFree(c->eam_d); cudaFree(c->eam_f); cudaFree(c->lj_tab_d);
   cudaFree(c->d_err); cudaFree(c->d_thermo); cudaFree(c->d_rows); cudaFree(c->adj_scratch);
   if (c->h_err) cudaFreeHost(c->h_err);
@@ -531,7 +561,7 @@ int gbmd_upload_atoms(gbmd_context* c, int64_t n, const double* rx, const double
   if (id) GBMD_CUDA(c, cudaMemcpyAsync(c->ID(), id, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, s));
   GBMD_CUDA(c, cudaMemsetAsync(c->ep, 0, b, s));
   if (n > 0) k_iota<<<nblk(n, 256), 256, 0, s>>>(n, c->USER(), c->ID(), id ? 0 : 1);
-  int init[8] = {0, 0, 0, -1, -1, 0, 0, 0};
+  int init[ERRW_WORDS] = {0, 0, 0, -1, -1};
   GBMD_CUDA(c, cudaMemcpyAsync(c->d_err, init, sizeof(init), cudaMemcpyHostToDevice, s));
   GBMD_CUDA(c, cudaStreamSynchronize(s));
   invalidate_list(c);
@@ -1062,9 +1092,26 @@ int gbmd_set_skin(gbmd_context* c, double skin) {
   return GBMD_OK;
 }
 
+int gbmd_set_list_buffer(gbmd_context* c, double buffer) {
+  if (!c || !(buffer >= 0.0) || !std::isfinite(buffer)) return GBMD_ERR_INVALID;
+  if (buffer == c->list_buffer) return GBMD_OK;
+  c->list_buffer = buffer;
+  c->grid_valid = false;  // cells of at least the outer radius
+  c->maxnb = c->maxnb_out = 0;
+  invalidate_list(c);
+  return GBMD_OK;
+}
+
+int gbmd_get_list_buffer(const gbmd_context* c, double* buffer, int64_t* outer_builds) {
+  if (!c) return GBMD_ERR_INVALID;
+  if (buffer) *buffer = c->list_buffer;
+  if (outer_builds) *outer_builds = c->outer_builds;
+  return GBMD_OK;
+}
+
 int gbmd_build_neighbors(gbmd_context* c) {
   if (!c) return GBMD_ERR_INVALID;
-  int rc = do_rebuild(c, true);
+  int rc = do_full_rebuild(c, true);
   if (rc) return rc;
   c->energy_step = -1, c->forces_valid_step = c->rho_valid_step = -1;
   return GBMD_OK;
@@ -1126,7 +1173,7 @@ static int check_device_errors(gbmd_context* c) {
   if (rc) return rc;
   const int f = c->h_err[ERRW_FLAGS];
   if (!f) return GBMD_OK;
-  int init[8] = {0, 0, 0, -1, -1, 0, 0, 0};
+  int init[ERRW_WORDS] = {0, 0, 0, -1, -1};
   cudaMemcpy(c->d_err, init, sizeof(init), cudaMemcpyHostToDevice);
   if (f & GBMD_DEVERR_LOST_ATOM) return set_error(c, GBMD_ERR_LOST_ATOM, "%d atoms lost", c->h_err[ERRW_LOST]);
   if (f & GBMD_DEVERR_NBR_OVERFLOW)
@@ -1404,7 +1451,7 @@ int gbmd_run_nve(gbmd_context* c, int nsteps, double dt, int rebuild_every, int 
   c->energy_step = -1, c->forces_valid_step = c->step;
   // the last step computed energies and virials when it was a thermo step
   if (want_thermo && nsteps % thermo_every == 0) c->energy_step = c->step;
-  if (trigger && (rc = collect_device_rebuilds(c))) return rc;
+  if ((trigger || two_level(c)) && (rc = collect_device_rebuilds(c))) return rc;
   return check_device_errors(c);
 }
 
@@ -1528,7 +1575,7 @@ int gbmd_run_minimize(gbmd_context* c, int nsteps, double dt, double tolF, int r
   }
   c->energy_step = -1, c->forces_valid_step = c->rho_valid_step = -1;
   GBMD_CUDA(c, cudaStreamSynchronize(c->stream));
-  if (trigger && (rc = collect_device_rebuilds(c))) return rc;
+  if ((trigger || two_level(c)) && (rc = collect_device_rebuilds(c))) return rc;
   return check_device_errors(c);
 }
 

@@ -24,7 +24,7 @@
 #define GBMD_IDX_MASK ((1u << GBMD_IDX_BITS) - 1u)
 #define GBMD_MAX_ATOMS (1ll << GBMD_IDX_BITS)
 
-// device error word layout (int[8])
+// device error word layout (int[ERRW_WORDS])
 enum {
   ERRW_FLAGS = 0,     // bitmask of GBMD_DEVERR_*
   ERRW_MAXNB = 1,     // largest neighbour count seen by the last list build
@@ -34,6 +34,9 @@ enum {
   ERRW_REBUILDS = 5,  // displacement-triggered rebuilds run on the device
   ERRW_GATE = 6,      // this step's displacement trigger (gate of the rebuild chain)
   ERRW_DISPL = 7,     // displacement check of gbmd_upload_positions
+  ERRW_OUTER = 8,     // two-level list: some atom moved more than half the outer buffer
+  ERRW_OUTER_BUILDS = 9,  // outer lists built on the device (graph replays, gated chains)
+  ERRW_WORDS = 16,
 };
 enum {
   GBMD_DEVERR_NBR_OVERFLOW = 1,
@@ -197,6 +200,19 @@ struct gbmd_context {
   double skin = 0.0, rlist = 0.0;
   bool list_valid = false;
   int64_t list_builds = 0;
+  // two-level list (gbmd_set_list_buffer): an outer list of radius rlist +
+  // list_buffer, built with the sort into cells, and the list the pair
+  // kernels read (radius rlist) filtered from it at every rebuild while no
+  // atom has moved more than list_buffer / 2 since the outer build
+  double list_buffer = 0.0;
+  uint32_t* nbr_out = nullptr;
+  int32_t* nnb_out = nullptr;
+  int64_t nbr_out_cap = 0;
+  int maxnb_out = 0;
+  double* rout = nullptr;       // 3 planes of cap: positions at the outer build
+  int64_t outer_cap = 0;        // atoms rout and nnb_out hold
+  bool outer_valid = false;
+  int64_t outer_builds = 0;
   int64_t npad = 0;
 
   // potential
@@ -289,7 +305,21 @@ int sync_error_word(gbmd_context* c);  // copies device error word, returns stat
 int grid_dims(const double lo[3], const double hi[3], double R, int nc[3]);
 // gate: device word; non-null makes every kernel of the chain return at once
 // while it holds 0, and keeps the buffer indices unchanged (see gbmd_neighbors.cu)
+// A full list build: wrap, sort into cells and build the list the pair
+// kernels read (with a list buffer set: the outer list, then the filter).
 int rebuild(gbmd_context* c, bool check_capacity, const int* gate = nullptr);
+// With a list buffer set and an outer list in place: the outer list is
+// rebuilt (with the sort) only when some atom moved more than half the
+// buffer since it was built, and the list is filtered from it.  `gate`
+// (device word) gates the whole rebuild as in rebuild(); without a gate the
+// decision is read back on the host, or put in a conditional graph node
+// while the stream is being captured.
+int rebuild_two_level(gbmd_context* c, bool check_capacity, const int* gate = nullptr);
+bool two_level(const gbmd_context* c);
+void free_outer(gbmd_context* c);
+// a device-side conditional graph node around `body`, opened when *gate != 0
+// (the stream must be capturing; body issues on c->stream)
+int capture_if(gbmd_context* c, const int* gate, int (*body)(gbmd_context*, const int*));
 void launch_posf(gbmd_context* c, const int* gate = nullptr);
 // blocks for a rebuild-chain kernel over `items` (per_block per block): all
 // of them ungated, at most per_sm per SM when gated (grid-stride kernels)

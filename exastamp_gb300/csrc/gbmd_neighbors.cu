@@ -28,6 +28,7 @@
 // buffer parity the captured pointers rely on does not depend on the outcome.
 #include <cstdio>
 #include <cstring>
+#include <utility>
 
 #include "gbmd_internal.cuh"
 
@@ -640,7 +641,9 @@ static int build_list(gbmd_context* c, const int* gate) {
   return GBMD_OK;
 }
 
-int rebuild(gbmd_context* c, bool check_capacity, const int* gate) {
+// The rebuild chain for the list in c->nbr / c->nnb / c->maxnb at radius
+// c->rlist (the outer list's buffers and radius while an OuterScope holds).
+static int rebuild_chain(gbmd_context* c, bool check_capacity, const int* gate) {
   if (gate && (!c->list_valid || !c->grid_valid || c->maxnb <= 0))
     return set_error(c, GBMD_ERR_INVALID, "gated rebuild needs a built list");
   if (!c->box_set) return set_error(c, GBMD_ERR_INVALID, "box not set");
@@ -653,7 +656,9 @@ int rebuild(gbmd_context* c, bool check_capacity, const int* gate) {
   if (!c->grid_valid) {
     int nc[3];
     const int rc = grid_dims(c->lo, c->hi, R, nc);
-    if (rc != 0) return set_error(c, GBMD_ERR_INVALID, "box edge shorter than neighbour radius %g", R);
+    if (rc != 0)
+      return set_error(c, GBMD_ERR_INVALID, "box edge shorter than neighbour radius %g%s", R,
+                       c->list_buffer > 0.0 ? " (list radius + list buffer)" : "");
     Grid& g = c->grid;
     g.ncells = (int64_t)nc[0] * nc[1] * nc[2];
     if (g.ncells > (1ll << 27)) return set_error(c, GBMD_ERR_TOO_LARGE, "too many cells");
@@ -730,7 +735,6 @@ int rebuild(gbmd_context* c, bool check_capacity, const int* gate) {
   rc = build_list(c, gate);
   if (rc) return rc;
   c->list_valid = true;
-  if (!gate) c->list_builds++;
   if (check_capacity) {
     rc = sync_error_word(c);
     if (c->h_err[ERRW_FLAGS] & GBMD_DEVERR_LOST_ATOM)
@@ -749,6 +753,285 @@ int rebuild(gbmd_context* c, bool check_capacity, const int* gate) {
     }
   }
   return GBMD_OK;
+}
+
+// --- two-level list ---------------------------------------------------------
+//
+// With a list buffer d set, the sort into cells and the cell walk build an
+// outer list of radius R + d (R = rcut + skin), and every rebuild filters the
+// list the pair kernels read (radius R) from it: the outer row's entries that
+// lie within R now, in the outer row's order.  The filter is complete while
+// no atom has moved more than d/2 since the outer build: a pair within R now
+// was then within R + d.  So a rebuild first tests every atom against d/2
+// from its position at the outer build and runs the outer build again only
+// when one moved that far.  Between outer builds the atoms keep their cells
+// and are not wrapped into the box, so the cell-relative FP32 copies, the
+// stencil codes and the FP64 band re-test all see continuous coordinates.
+// The filtered list holds the same pairs as a fresh build; its rows follow
+// the cell order of the outer build.
+
+bool two_level(const gbmd_context* c) { return c->list_buffer > 0.0; }
+
+void free_outer(gbmd_context* c) {
+  cudaFree(c->rout);
+  cudaFree(c->nnb_out);
+  c->rout = nullptr;
+  c->nnb_out = nullptr;
+  c->outer_cap = 0;
+  c->outer_valid = false;
+}
+
+static int ensure_outer(gbmd_context* c) {
+  if (c->rout && c->outer_cap >= c->cap) return GBMD_OK;
+  free_outer(c);
+  GBMD_CUDA(c, cudaMalloc(&c->rout, sizeof(double) * 3 * c->cap));
+  GBMD_CUDA(c, cudaMalloc(&c->nnb_out, sizeof(int32_t) * c->cap));
+  c->outer_cap = c->cap;
+  return GBMD_OK;
+}
+
+// The outer list's buffers and radius in the fields the rebuild chain uses.
+struct OuterScope {
+  gbmd_context* c;
+  double saved;
+  explicit OuterScope(gbmd_context* ctx) : c(ctx), saved(ctx->rlist) {
+    swap();
+    c->rlist = saved + c->list_buffer;
+  }
+  ~OuterScope() {
+    c->rlist = saved;
+    swap();
+  }
+  void swap() {
+    std::swap(c->nbr, c->nbr_out);
+    std::swap(c->nnb, c->nnb_out);
+    std::swap(c->nbr_cap, c->nbr_out_cap);
+    std::swap(c->maxnb, c->maxnb_out);
+  }
+};
+
+// flag = 1 when some atom moved more than sqrt(thr2) since the outer build
+// (|dr|^2 summed x, y, z without contraction); with a gate, only when *gate
+__global__ void k_outer_check(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
+                              const double* __restrict__ z, const double* __restrict__ rout, int64_t cap,
+                              double thr2, const int* __restrict__ gate, int* __restrict__ flag) {
+  if (gate && !*gate) return;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const double dx = __dsub_rn(x[p], rout[p]), dy = __dsub_rn(y[p], rout[cap + p]),
+                 dz = __dsub_rn(z[p], rout[2 * cap + p]);
+    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    if (d2 > thr2) *flag = 1;
+  }
+}
+
+// positions at a gated outer build; thread 0 counts the build
+__global__ void k_save_outer(int64_t n, const double* __restrict__ r, double* __restrict__ rout, int64_t cap,
+                             const int* __restrict__ gate, int* __restrict__ count) {
+  if (!*gate) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(count, 1);
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) rout[d * cap + p] = r[d * cap + p];
+  }
+}
+
+// One thread per atom: the entries of its outer row within R now, in order.
+// The FP32 distance of the cell-relative copies (the builder's expression)
+// decides outside the band R^2 (1 -+ 2^-12); band entries are re-tested in
+// FP64 with the pair-set rounding.  A row never grows, so the list has the
+// outer list's capacity.  V4 (rows interleaved in groups of a multiple of 4
+// entries): the row is read 4 entries per 16-byte load with the next load in
+// flight, and the 4 neighbour positions are gathered together.
+struct FilterArgs {
+  int64_t n;
+  const float4* pf;
+  const double *x, *y, *z;
+  const int32_t* cellpack;
+  const uint32_t* outer;
+  const int32_t* nnb_out;
+  uint32_t* nbr;
+  int32_t* nnb;
+  int maxnb_out, W, wsh;
+  int64_t stride;
+  double R2;
+  float R2lo, R2hi;
+};
+
+__device__ __forceinline__ bool filter_keep(const FilterArgs& A, const Grid& g, int64_t i, const float4& pi,
+                                            uint32_t w, const float4& pj, int cx, int cy, int cz) {
+  const uint32_t code = w >> GBMD_IDX_BITS;
+  const float sx = __fmul_rn((float)((int)(code & 3u) - 1), g.hf[0]);
+  const float sy = __fmul_rn((float)((int)((code >> 2) & 3u) - 1), g.hf[1]);
+  const float sz = __fmul_rn((float)((int)(code >> 4) - 1), g.hf[2]);
+  const float dx = __fsub_rn(__fadd_rn(pj.x, sx), pi.x);
+  const float dy = __fsub_rn(__fadd_rn(pj.y, sy), pi.y);
+  const float dz = __fsub_rn(__fadd_rn(pj.z, sz), pi.z);
+  const float d2f = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
+  if (d2f > A.R2hi) return false;
+  if (d2f < A.R2lo) return true;
+  return exact_within(A.x, A.y, A.z, i, (int64_t)(w & GBMD_IDX_MASK), code, cx, cy, cz, g, A.R2);
+}
+
+template <bool V4>
+__global__ void __launch_bounds__(256) k_filter_list(FilterArgs A, Grid g, const int* __restrict__ gate) {
+  if (gate && !*gate) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < A.n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int nn = min(A.nnb_out[i], A.maxnb_out);
+    const float4 pi = A.pf[i];
+    const int cp = A.cellpack[i];
+    const int cx = cp & 1023, cy = (cp >> 10) & 1023, cz = cp >> 20;
+    const uint32_t* orow = A.outer + (size_t)i * A.W;
+    uint32_t* row = A.nbr + (size_t)i * A.W;
+    int cnt = 0;
+    auto put = [&](uint32_t w) {
+      row[(size_t)(cnt >> A.wsh) * A.stride + (cnt & (A.W - 1))] = w;
+      ++cnt;
+    };
+    if (V4) {
+      // slot k at orow[(k >> wsh) * stride + (k & (W - 1))]; W is a multiple
+      // of 4, so 4 consecutive slots from a multiple of 4 are one aligned uint4
+      // (rows hold maxnb_out slots, a multiple of W: the last load stays in)
+      auto group = [&](int k) {
+        return *reinterpret_cast<const uint4*>(orow + (size_t)(k >> A.wsh) * A.stride + (k & (A.W - 1)));
+      };
+      const int ng = (nn + 3) >> 2;
+      uint4 cur = ng > 0 ? group(0) : make_uint4(0u, 0u, 0u, 0u);
+      for (int t = 0; t < ng; ++t) {
+        const int k0 = t << 2;
+        uint4 nxt = cur;
+        if (t + 1 < ng) nxt = group(k0 + 4);
+        const uint32_t e[4] = {cur.x, cur.y, cur.z, cur.w};
+        float4 pj[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) pj[q] = A.pf[k0 + q < nn ? (int64_t)(e[q] & GBMD_IDX_MASK) : i];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (k0 + q < nn && filter_keep(A, g, i, pi, e[q], pj[q], cx, cy, cz)) put(e[q]);
+        cur = nxt;
+      }
+    } else {
+      for (int k = 0; k < nn; ++k) {
+        const uint32_t w = orow[(size_t)(k >> A.wsh) * A.stride + (k & (A.W - 1))];
+        const float4 pj = A.pf[w & GBMD_IDX_MASK];
+        if (filter_keep(A, g, i, pi, w, pj, cx, cy, cz)) put(w);
+      }
+    }
+    A.nnb[i] = cnt;
+  }
+}
+
+// The outer list: the rebuild chain at radius R + d into the outer buffers,
+// then the positions it leaves saved for the displacement test.
+static int outer_chain(gbmd_context* c, bool check_capacity, const int* gate) {
+  int rc;
+  if (!gate) {
+    if ((rc = ensure_outer(c))) return rc;
+  } else if (!c->rout || c->outer_cap < c->n) {
+    return set_error(c, GBMD_ERR_INVALID, "gated rebuild needs an outer list");
+  }
+  {
+    const OuterScope on(c);
+    rc = rebuild_chain(c, check_capacity, gate);
+  }
+  if (rc) return rc;
+  if (gate) {
+    k_save_outer<<<chain_blocks(c, c->n, 256, gate, 8), 256, 0, c->stream>>>(c->n, c->rbuf[c->cur], c->rout, c->cap,
+                                                                          gate, c->d_err + ERRW_OUTER_BUILDS);
+  } else {
+    for (int d = 0; d < 3; ++d)
+      GBMD_CUDA(c, cudaMemcpyAsync(c->rout + d * c->cap, c->rbuf[c->cur] + d * c->cap, sizeof(double) * c->n,
+                                   cudaMemcpyDeviceToDevice, c->stream));
+    c->outer_builds++;
+    c->outer_valid = true;
+  }
+  return GBMD_OK;
+}
+
+static int filter_list(gbmd_context* c, const int* gate) {
+  const int W = list_width(c);
+  int wsh = 0;
+  while ((1 << wsh) < W) ++wsh;
+  const int64_t stride = c->npad * W;
+  const int64_t need = (int64_t)(c->maxnb_out / W) * stride;
+  if (need > c->nbr_cap) {
+    if (gate || c->capturing) return set_error(c, GBMD_ERR_INVALID, "the list outgrew its buffer in a gated rebuild");
+    if (c->nbr) cudaFree(c->nbr);
+    c->nbr = nullptr;
+    c->nbr_cap = 0;
+    GBMD_CUDA(c, cudaMalloc(&c->nbr, sizeof(uint32_t) * (size_t)need));
+    c->nbr_cap = need;
+  }
+  c->maxnb = c->maxnb_out;
+  const double R2 = c->rlist * c->rlist;
+  const float R2lo = (float)(R2 * (1.0 - 0x1p-12));
+  const float R2hi = (float)(R2 * (1.0 + 0x1p-12));
+  FilterArgs A;
+  A.n = c->n;
+  A.pf = c->POSF();
+  A.x = c->X(); A.y = c->Y(); A.z = c->Z();
+  A.cellpack = c->cellpack;
+  A.outer = c->nbr_out;
+  A.nnb_out = c->nnb_out;
+  A.nbr = c->nbr;
+  A.nnb = c->nnb;
+  A.maxnb_out = c->maxnb_out;
+  A.W = W;
+  A.wsh = wsh;
+  A.stride = stride;
+  A.R2 = R2;
+  A.R2lo = R2lo;
+  A.R2hi = R2hi;
+  const unsigned blocks = gate ? chain_blocks(c, c->n, 256, gate, 8) : nblk(c->n, 256);
+  if (W % 4 == 0) k_filter_list<true><<<blocks, 256, 0, c->stream>>>(A, c->grid, gate);
+  else k_filter_list<false><<<blocks, 256, 0, c->stream>>>(A, c->grid, gate);
+  c->list_valid = true;
+  if (!gate) c->list_builds++;
+  return GBMD_OK;
+}
+
+int rebuild(gbmd_context* c, bool check_capacity, const int* gate) {
+  if (c->n == 0 || !two_level(c)) {
+    const int rc = rebuild_chain(c, check_capacity, gate);
+    if (rc == GBMD_OK && !gate) c->list_builds++;
+    return rc;
+  }
+  if (gate && !c->outer_valid) return set_error(c, GBMD_ERR_INVALID, "gated rebuild needs an outer list");
+  const int rc = outer_chain(c, check_capacity, gate);
+  if (rc) return rc;
+  return filter_list(c, gate);
+}
+
+static int outer_body(gbmd_context* c, const int* flag) {
+  c->full_chain_grids = true;
+  const int rc = outer_chain(c, false, flag);
+  c->full_chain_grids = false;
+  return rc;
+}
+
+int rebuild_two_level(gbmd_context* c, bool check_capacity, const int* gate) {
+  if (c->n == 0 || !c->outer_valid || !c->list_valid || !c->grid_valid) {
+    if (gate || c->capturing) return set_error(c, GBMD_ERR_INVALID, "gated or captured rebuild needs an outer list");
+    return rebuild(c, check_capacity, nullptr);
+  }
+  int* flag = c->d_err + ERRW_OUTER;
+  cudaStream_t s = c->stream;
+  GBMD_CUDA(c, cudaMemsetAsync(flag, 0, sizeof(int), s));
+  const double h = 0.5 * c->list_buffer;
+  const double thr2 = h * h * (1.0 - 0x1p-20);  // a margin far above the rounding of the test
+  const unsigned blocks = gate ? chain_blocks(c, c->n, 256, gate, 8) : nblk(c->n, 256);
+  k_outer_check<<<blocks, 256, 0, s>>>(c->n, c->X(), c->Y(), c->Z(), c->rout, c->cap, thr2, gate, flag);
+  int rc;
+  if (gate) {
+    // the flag stays 0 unless the gate is open: it gates the outer chain
+    rc = outer_chain(c, false, flag);
+  } else if (c->capturing) {
+    rc = capture_if(c, flag, outer_body);
+  } else {
+    if ((rc = sync_error_word(c))) return rc;
+    rc = c->h_err[ERRW_OUTER] ? outer_chain(c, check_capacity, nullptr) : GBMD_OK;
+  }
+  if (rc) return rc;
+  return filter_list(c, gate);
 }
 
 int export_pairs(gbmd_context* c, int64_t cap, uint64_t* id_i, uint64_t* id_j, int8_t* img, int64_t* count) {

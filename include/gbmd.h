@@ -204,7 +204,24 @@ int gbmd_get_newton3(const gbmd_context* ctx, int* enabled);
  * d2 <= (rcut_max+skin)^2} with d2 from ((x_j + n L) - x_i) in FP64 without
  * contraction. */
 int gbmd_set_skin(gbmd_context* ctx, double skin);
+/* Always a full build: wrap, rebin into cells, list (with a list buffer set,
+ * the outer list too, on cells of the outer radius, and the list filtered
+ * from it: the same pairs, rows in the order of those cells). */
 int gbmd_build_neighbors(gbmd_context* ctx);
+/* Two-level list (no reference counterpart; the pair set is unchanged).
+ * With buffer d > 0 a full build also makes an outer list of radius
+ * rcut_max + skin + d, and every later rebuild filters the list from it
+ * (the entries within rcut_max + skin now, band entries re-tested in FP64
+ * as above, in the outer rows' order) without the wrap and rebin.  The outer
+ * list, with the wrap and rebin, is built again only when some atom moved
+ * more than d/2 since it was built: then every pair within rcut_max + skin
+ * is in it.  Between outer builds the atoms keep their cells and their
+ * coordinates run on past the box faces.  Cells are at least
+ * rcut_max + skin + d wide, so each box edge must be that long.  0 (the
+ * default) turns it off.  Invalidates the list. */
+int gbmd_set_list_buffer(gbmd_context* ctx, double buffer);
+/* buffer and the number of outer builds so far (either may be NULL). */
+int gbmd_get_list_buffer(const gbmd_context* ctx, double* buffer, int64_t* outer_builds);
 /* check_and_update_particles (data/config/config_move_particles.msp L116-152:
  * trigger_move_particles = particle_displ_over, L19-22, then the full update
  * when it fires): the skin/2 displacement test of the current positions
@@ -332,7 +349,8 @@ int gbmd_lj_multi_loss_grad(gbmd_context* ctx, const double* fx_target, const do
 
 /* Number of neighbour-list builds since the context was created, including
  * the displacement-triggered ones (counted on the device, folded in when
- * gbmd_run_nve / gbmd_run_minimize return). */
+ * gbmd_run_nve / gbmd_run_minimize return) and, with a list buffer, the
+ * lists filtered from the outer list. */
 int gbmd_list_builds(const gbmd_context* ctx, int64_t* count);
 
 /* ---- thermodynamic state ---------------------------------------------------

@@ -60,13 +60,14 @@ def _case(kind):
     raise ValueError(kind)
 
 
-def _host_steps(gpu, s, setpot, skin, dt, mixed, slabs, link=1):
+def _host_steps(gpu, s, setpot, skin, dt, mixed, slabs, link=1, buffer=0.0):
     torch = pytest.importorskip("torch")
     hist = []
     with gpu.Context(0) as ctx:
         ctx.upload_system(s)
         setpot(ctx)
         ctx.set_skin(skin)
+        ctx.set_list_buffer(buffer)
         ctx.set_precision(mixed)
         ctx.set_host_pipeline(slabs)
         ctx.set_host_pipeline_link(link)
@@ -86,16 +87,18 @@ def _host_steps(gpu, s, setpot, skin, dt, mixed, slabs, link=1):
     return hist, used, steps, builds, redone
 
 
-@pytest.mark.parametrize("kind,order,link", [("lj", "cells", 1), ("lj", "random", 1), ("eam", "cells", 1),
-                                             ("eam", "lattice", 1), ("eam_fp64", "cells", 1), ("johnson", "cells", 1),
-                                             ("lj_multi_fp64", "cells", 1), ("eam", "cells", 0), ("lj", "random", 0)])
-def test_pipelined_host_steps_equal_unpipelined(gpu, kind, order, link):
+@pytest.mark.parametrize("kind,order,link,buffer", [
+    ("lj", "cells", 1, 0.0), ("lj", "random", 1, 0.0), ("eam", "cells", 1, 0.0), ("eam", "lattice", 1, 0.0),
+    ("eam_fp64", "cells", 1, 0.0), ("johnson", "cells", 1, 0.0), ("lj_multi_fp64", "cells", 1, 0.0),
+    ("eam", "cells", 0, 0.0), ("lj", "random", 0, 0.0), ("eam", "cells", 1, 0.3), ("lj", "cells", 1, 0.2)])
+def test_pipelined_host_steps_equal_unpipelined(gpu, kind, order, link, buffer):
     """link 0: chunks carried by the copy engines through HBM staging;
-    link 1: kernels reading and writing the page-locked arrays."""
+    link 1: kernels reading and writing the page-locked arrays.  buffer > 0:
+    both runs rebuild through a two-level list (gbmd_set_list_buffer)."""
     s, setpot, rcut, skin, dt, mixed = _case(kind)
     s = _reorder(s, order, rcut + skin, 7)
-    ref, used0, steps0, builds0, _ = _host_steps(gpu, s, setpot, skin, dt, mixed, 0)
-    got, used, steps, builds, redone = _host_steps(gpu, s, setpot, skin, dt, mixed, 64, link)
+    ref, used0, steps0, builds0, _ = _host_steps(gpu, s, setpot, skin, dt, mixed, 0, buffer=buffer)
+    got, used, steps, builds, redone = _host_steps(gpu, s, setpot, skin, dt, mixed, 64, link, buffer=buffer)
     assert used0 == 0 and steps0 == 0
     assert used >= 4
     # the trigger fired on some steps, not on most; each was predicted by
