@@ -219,3 +219,50 @@ def test_box_shorter_than_the_outer_radius_is_refused(gpu):
         for bad in (-1.0, float("nan"), float("inf")):
             with pytest.raises(gpu.GbmdError):
                 ctx.set_list_buffer(bad)
+
+
+def test_newton3_half_list_filtered(gpu):
+    """Newton-3 half lists (each unordered pair once, j after i in the outer
+    build's cell order) filtered from a half outer list: 40 NVE steps stay
+    within 1e-6 of the same run on the one-level half list."""
+    s = S.lj_fcc(ncell=8, seed=19)
+    out = []
+    for buffer in (0.0, 0.5):
+        with gpu_ctx(gpu, s, LJ, 0.3, mixed=True, tpa=1, block=256, vec=4) as ctx:
+            ctx.set_newton3(True)
+            ctx.set_list_buffer(buffer)
+            th = ctx.run_nve(40, 0.005, rebuild_every=10, thermo_every=10)
+            out.append((th, ctx.download(), ctx.list_builds()))
+    (t0, d0, b0), (t1, d1, b1) = out
+    assert b0 == b1
+    for k in ("x", "y", "z"):
+        assert _min_image(d1[k] - d0[k], s.L[0]).max() < 1e-6, k
+    e0 = t0[:, 21:24].sum(1) + t0[:, 24]
+    e1 = t1[:, 21:24].sum(1) + t1[:, 24]
+    assert np.abs(e1 - e0).max() < 1e-6 * np.abs(e0).max()
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_split_eam_passes_on_the_filtered_list(gpu, mixed):
+    """eam_rho then eam_force on a filtered list give the fused pass bit for
+    bit; after more steps (ending with a filtered rebuild) a force pass
+    needs a new density pass."""
+    sf = SF.tabulate(SF.load_cu_params())
+    s = S.eam_cu_fcc(ncell=8, seed=20)
+    with gpu_ctx(gpu, s, lambda c: c.set_eam_alloy(sf, 5.0, S.EV, S.EV), 0.3, mixed=mixed) as ctx:
+        ctx.set_list_buffer(0.6)
+        ctx.run_nve(30, 1e-3, rebuild_every=10)
+        assert ctx.list_buffer()[1] == 1
+        ctx.compute_forces(energy=True, virial=True)
+        fused = ctx.download(virial=True)
+        ctx.compute_forces(energy=True, virial=True, passes="density")
+        ctx.compute_forces(energy=True, virial=True, passes="force")
+        split = ctx.download(virial=True)
+        for k in ("ax", "ay", "az", "ep", "vir"):
+            assert np.array_equal(split[k], fused[k]), k
+        ctx.compute_forces(passes="density")
+        ctx.run_nve(10, 1e-3, rebuild_every=10)   # ends with a filtered rebuild
+        assert ctx.list_buffer()[1] == 1
+        with pytest.raises(gpu.GbmdError) as e:
+            ctx.compute_forces(passes="force")
+        assert e.value.code == INVALID
