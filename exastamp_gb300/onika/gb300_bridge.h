@@ -38,6 +38,7 @@
 #include <gbmd.h>
 
 #include <cstdint>
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <stdexcept>
@@ -71,6 +72,12 @@ struct Session {
   bool grid_stale = false;    // the device state changed since the last write-back
   bool density_fresh = false; // a split EAM density pass ran on the uploaded positions
   int64_t full_uploads = 0, position_uploads = 0;  // counters (tests and logs)
+  // diagonal xform of the domain: physical coordinates = scale x grid
+  // coordinates (the device works in physical ones); next_scale is the
+  // domain's current one, applied before the next device work
+  double scale[3] = {1.0, 1.0, 1.0}, next_scale[3] = {1.0, 1.0, 1.0};
+  double glo[3] = {0.0, 0.0, 0.0}, ghi[3] = {0.0, 0.0, 0.0};  // domain bounds, grid coordinates
+  int periodic[3] = {1, 1, 1};
   // staging, reused from call to call
   std::vector<double> r[3], v[3], a[3], ep, vir;
   std::vector<uint8_t> type;
@@ -86,17 +93,48 @@ struct Session {
 };
 using SessionPtr = std::shared_ptr<Session>;
 
+inline void check_scale(const double scale[3]) {
+  for (int d = 0; d < 3; ++d)
+    if (!(scale[d] > 0.0) || !std::isfinite(scale[d])) throw Error("xform scale factors must be positive and finite");
+}
+
+// The physical box of the session's bounds and current scale.
+inline void set_physical_box(Session& s) {
+  double lo[3], hi[3];
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = s.glo[d] * s.scale[d];
+    hi[d] = s.ghi[d] * s.scale[d];
+  }
+  check(s.ctx, gbmd_set_box(s.ctx, lo, hi, s.periodic), "gbmd_set_box");
+}
+
 // The device context of the session, created on first use: device 0 on the
-// given stream (may be null), box [lo, hi) (fully periodic), species masses.
+// given stream (may be null), box [lo, hi) in grid coordinates (fully
+// periodic), species masses, and the domain's diagonal xform (scale; null:
+// identity).
 inline void ensure_context(Session& s, void* stream, const double lo[3], const double hi[3], const int periodic[3],
-                           const std::vector<double>& masses) {
+                           const std::vector<double>& masses, const double* scale = nullptr) {
   if (s.ctx) return;
+  if (scale) check_scale(scale);
   gbmd_context* c = nullptr;
   const int rc = gbmd_create(&c, 0, stream);
   if (rc != GBMD_OK) throw Error("gbmd_create failed (no GPU?)");
   s.ctx = c;
-  check(c, gbmd_set_box(c, lo, hi, periodic), "gbmd_set_box");
+  for (int d = 0; d < 3; ++d) {
+    s.glo[d] = lo[d];
+    s.ghi[d] = hi[d];
+    s.periodic[d] = periodic[d];
+    s.scale[d] = s.next_scale[d] = scale ? scale[d] : 1.0;
+  }
+  set_physical_box(s);
   check(c, gbmd_set_species(c, (int)masses.size(), masses.data()), "gbmd_set_species");
+}
+
+// The domain's current diagonal xform (a deformation run changes it between
+// operator calls); applied before the session's next device work.
+inline void set_xform_scale(Session& s, const double scale[3]) {
+  check_scale(scale);
+  for (int d = 0; d < 3; ++d) s.next_scale[d] = scale[d];
 }
 
 // The inner particles' layout and positions (velocities too with `with_v`)
@@ -119,9 +157,9 @@ void gather(Session& s, const G& g, bool with_v) {
     const size_t c = g.cell_index(k);
     const size_t np = g.cell_size(c);
     for (size_t p = 0; p < np; ++p, ++q) {
-      s.r[0][q] = g.get(c, RX, p);
-      s.r[1][q] = g.get(c, RY, p);
-      s.r[2][q] = g.get(c, RZ, p);
+      s.r[0][q] = g.get(c, RX, p) * s.scale[0];
+      s.r[1][q] = g.get(c, RY, p) * s.scale[1];
+      s.r[2][q] = g.get(c, RZ, p) * s.scale[2];
       if (with_v) {
         s.v[0][q] = g.get(c, VX, p);
         s.v[1][q] = g.get(c, VY, p);
@@ -191,6 +229,26 @@ void write_forces(Session& s, G& g, bool energy, bool virial, bool as_force) {
   }
 }
 
+template <class G>
+void sync_grid(Session& s, G& g, bool energy, bool virial);
+
+// A changed xform (set_xform_scale) before new device work: the device's
+// state, newer than the grid's, goes back into the grid with the old scale
+// (r, v and the accelerations; energies and virials are recomputed by the
+// next force call), the physical box follows the new scale, and the next
+// call uploads every field again.  Grid coordinates do not change: the
+// atoms move with the deformation.
+template <class G>
+void apply_xform(Session& s, G& g) {
+  if (s.scale[0] == s.next_scale[0] && s.scale[1] == s.next_scale[1] && s.scale[2] == s.next_scale[2]) return;
+  if (s.resident && s.grid_stale) sync_grid(s, g, false, false);
+  s.resident = false;
+  s.uploaded = false;
+  s.density_fresh = false;
+  for (int d = 0; d < 3; ++d) s.scale[d] = s.next_scale[d];
+  set_physical_box(s);
+}
+
 // Flags of a force call: energy (trigger_thermo_state), virial
 // (compute_virial) and the split EAM pass bits.
 inline int force_flags(bool energy, bool virial, int passes) {
@@ -202,6 +260,7 @@ inline int force_flags(bool energy, bool virial, int passes) {
 // the same positions: the force pass reuses the density pass's upload).
 template <class G>
 void compute_forces(Session& s, G& g, bool energy, bool virial, int passes) {
+  apply_xform(s, g);
   if (s.resident) {
     check(s.ctx, gbmd_compute_forces(s.ctx, force_flags(energy, virial, passes)), "gbmd_compute_forces");
     s.grid_stale = true;
@@ -248,14 +307,16 @@ void make_resident(Session& s, const G& g) {
 // device's copy (exaNBody's push operators; formula
 // push_vec3_2nd_order_xform_minimization.cpp L33-38).
 template <class G>
-void push_f_v_r(Session& s, const G& g, double dt, double dt_scale) {
+void push_f_v_r(Session& s, G& g, double dt, double dt_scale) {
+  apply_xform(s, g);
   make_resident(s, g);
   check(s.ctx, gbmd_push_f_v_r(s.ctx, dt, dt_scale), "gbmd_push_f_v_r");
   s.grid_stale = true;
 }
 
 template <class G>
-void push_f_v(Session& s, const G& g, double dt, double dt_scale) {
+void push_f_v(Session& s, G& g, double dt, double dt_scale) {
+  apply_xform(s, g);
   make_resident(s, g);
   check(s.ctx, gbmd_push_f_v(s.ctx, dt, dt_scale), "gbmd_push_f_v");
   s.grid_stale = true;
@@ -264,7 +325,8 @@ void push_f_v(Session& s, const G& g, double dt, double dt_scale) {
 // check_and_update_particles on the device's copy: rebuild when some atom
 // moved more than skin/2.  Returns whether it rebuilt.
 template <class G>
-bool update_neighbors(Session& s, const G& g) {
+bool update_neighbors(Session& s, G& g) {
+  apply_xform(s, g);
   make_resident(s, g);
   int rebuilt = 0;
   check(s.ctx, gbmd_update_neighbors(s.ctx, &rebuilt), "gbmd_update_neighbors");
@@ -293,9 +355,9 @@ void sync_grid(Session& s, G& g, bool energy, bool virial) {
         "gbmd_download");
   for (size_t k = 0; k < n; ++k) {
     const size_t c = s.cell[k], p = s.slot[k];
-    g.set(c, RX, p, s.r[0][k]);
-    g.set(c, RY, p, s.r[1][k]);
-    g.set(c, RZ, p, s.r[2][k]);
+    g.set(c, RX, p, s.r[0][k] / s.scale[0]);
+    g.set(c, RY, p, s.r[1][k] / s.scale[1]);
+    g.set(c, RZ, p, s.r[2][k] / s.scale[2]);
     g.set(c, VX, p, s.v[0][k]);
     g.set(c, VY, p, s.v[1][k]);
     g.set(c, VZ, p, s.v[2][k]);

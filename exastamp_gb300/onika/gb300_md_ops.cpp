@@ -134,22 +134,43 @@ class GridView {
   std::vector<size_t> m_inner;
 };
 
-// The shared session, created on first use with the domain and species.
+// The domain's xform as per-axis scale factors: identity, or diagonal with
+// positive entries (orthorhombic scaling, as a uniaxial deformation makes).
+// A shear (off-diagonal terms) is refused.
+inline void xform_scale(const Domain& domain, double scale[3]) {
+  scale[0] = scale[1] = scale[2] = 1.0;
+  if (domain.xform_is_identity()) return;
+  const Mat3d& m = domain.xform();
+  if (m.m12 != 0.0 || m.m13 != 0.0 || m.m21 != 0.0 || m.m23 != 0.0 || m.m31 != 0.0 || m.m32 != 0.0 ||
+      !(m.m11 > 0.0) || !(m.m22 > 0.0) || !(m.m33 > 0.0))
+    fatal_error() << "gb300: only identity or diagonal xforms (orthorhombic domains) are supported" << std::endl;
+  scale[0] = m.m11;
+  scale[1] = m.m22;
+  scale[2] = m.m33;
+}
+
+// The shared session, created on first use with the domain and species; the
+// domain's current xform is handed to it on every call.
 inline gb300::Session& session_for(gb300::SessionPtr& ptr, const Domain& domain, const ParticleSpecies& species) {
   if (!ptr) ptr = std::make_shared<gb300::Session>();
+  double scale[3];
+  xform_scale(domain, scale);
   if (!ptr->ctx) {
     const Vec3d lo = domain.bounds().bmin, hi = domain.bounds().bmax;
     const double blo[3] = {lo.x, lo.y, lo.z}, bhi[3] = {hi.x, hi.y, hi.z};
     const int per[3] = {domain.periodic_boundary_x(), domain.periodic_boundary_y(), domain.periodic_boundary_z()};
-    if (!domain.xform_is_identity())
-      fatal_error() << "gb300: only orthorhombic domains (identity xform) are supported" << std::endl;
     std::vector<double> m(species.size());
     for (size_t t = 0; t < m.size(); ++t) m[t] = species.at(t).m_mass;
     try {
-      gb300::ensure_context(*ptr, parallel_execution_context()->gpu_stream(), blo, bhi, per, m);
+      gb300::ensure_context(*ptr, parallel_execution_context()->gpu_stream(), blo, bhi, per, m, scale);
     } catch (const gb300::Error& e) {
       fatal_error() << "gb300: " << e.what() << std::endl;
     }
+  }
+  try {
+    gb300::set_xform_scale(*ptr, scale);
+  } catch (const gb300::Error& e) {
+    fatal_error() << "gb300: " << e.what() << std::endl;
   }
   return *ptr;
 }
@@ -523,7 +544,9 @@ class Gb300ForceNode : public OperatorNode {
 // config_numerical_schemes.msp L23-28; formula
 // push_vec3_2nd_order_xform_minimization.cpp L33-38) on the device's copy of
 // the state: r += v dt' + a dt'^2 / 2 (R) or v += a dt' (V), dt' = dt dt_scale.
-// xform_mode is accepted for orthorhombic domains (identity xform) only.
+// With a diagonal xform the device pushes physical coordinates, and the grid
+// gets them back divided by the scale: INV_XFORM for the positions,
+// IDENTITY for the velocities, as the run files set xform_mode.
 template <class GridT, bool R>
 class Gb300PushNode : public OperatorNode {
   ADD_SLOT(GridT, grid, INPUT_OUTPUT);

@@ -1152,11 +1152,11 @@ static void all_forces(int64_t n, const double* x, const double* y, const double
   orc_force_to_accel(n, ax, ay, az, type, masses);
 }
 
-int orc_run_nve(int64_t n, double* x, double* y, double* z, double* vx, double* vy, double* vz,
-                double* ax, double* ay, double* az, double* ep, const uint8_t* type, const uint64_t* id,
-                const double* masses, const double lo[3], const double hi[3], int pot_kind,
-                const void* pot, double skin, double dt, int nsteps, int rebuild_every,
-                double* thermo_out) {
+static int run_nve_impl(int64_t n, double* x, double* y, double* z, double* vx, double* vy, double* vz,
+                        double* ax, double* ay, double* az, double* ep, const uint8_t* type, const uint64_t* id,
+                        const double* masses, const double lo[3], const double hi[3], int pot_kind,
+                        const void* pot, double skin, double dt, int nsteps, int rebuild_every,
+                        double* thermo_out, int initial_forces) {
   const double L[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
   const double R = pot_rcut(pot_kind, pot) + skin;
   orc_list l = {(int64_t*)malloc(sizeof(int64_t) * (size_t)(n + 1)), NULL, NULL, 0};
@@ -1168,7 +1168,11 @@ int orc_run_nve(int64_t n, double* x, double* y, double* z, double* vx, double* 
   g_list_builds = 1;
   if ((rc = list_rebuild(&l, n, x, y, z, id, lo, hi, R)) != 0) goto done;
   take_rref(n, x, y, z, rref);
-  all_forces(n, x, y, z, type, &l, L, pot_kind, pot, masses, rho, ax, ay, az, ep, vir);
+  if (initial_forces) {
+    all_forces(n, x, y, z, type, &l, L, pot_kind, pot, masses, rho, ax, ay, az, ep, vir);
+  } else {
+    for (int64_t i = 0; i < n; ++i) ep[i] = 0.0;
+  }
   if (thermo_out) orc_thermo(n, vx, vy, vz, ep, vir, type, masses, thermo_out);
   for (int s = 1; s <= nsteps; ++s) {
     orc_push_f_v_r(n, x, y, z, vx, vy, vz, ax, ay, az, dt, 1.0);
@@ -1186,6 +1190,24 @@ done:
   free(vir);
   free(rref);
   return rc;
+}
+
+int orc_run_nve(int64_t n, double* x, double* y, double* z, double* vx, double* vy, double* vz,
+                double* ax, double* ay, double* az, double* ep, const uint8_t* type, const uint64_t* id,
+                const double* masses, const double lo[3], const double hi[3], int pot_kind,
+                const void* pot, double skin, double dt, int nsteps, int rebuild_every,
+                double* thermo_out) {
+  return run_nve_impl(n, x, y, z, vx, vy, vz, ax, ay, az, ep, type, id, masses, lo, hi, pot_kind, pot, skin, dt,
+                      nsteps, rebuild_every, thermo_out, 1);
+}
+
+int orc_run_nve_from(int64_t n, double* x, double* y, double* z, double* vx, double* vy, double* vz,
+                     double* ax, double* ay, double* az, double* ep, const uint8_t* type, const uint64_t* id,
+                     const double* masses, const double lo[3], const double hi[3], int pot_kind,
+                     const void* pot, double skin, double dt, int nsteps, int rebuild_every,
+                     double* thermo_out) {
+  return run_nve_impl(n, x, y, z, vx, vy, vz, ax, ay, az, ep, type, id, masses, lo, hi, pot_kind, pot, skin, dt,
+                      nsteps, rebuild_every, thermo_out, 0);
 }
 
 int orc_run_minimize(int64_t n, double* x, double* y, double* z, double* ax, double* ay, double* az,

@@ -158,6 +158,16 @@ int orc_run_nve(int64_t n, double* x, double* y, double* z, double* vx, double* 
                 const double* masses, const double lo[3], const double hi[3], int pot_kind,
                 const void* pot, double skin, double dt, int nsteps, int rebuild_every,
                 double* thermo_out);
+/* The same continuing from the given accelerations (ax, ay, az as the last
+ * force pass left them, e.g. before the domain was rescaled): the first step
+ * pushes with them instead of recomputing the forces first.  The step-0
+ * thermo row then has the given state's kinetic terms and zero potential
+ * terms. */
+int orc_run_nve_from(int64_t n, double* x, double* y, double* z, double* vx, double* vy, double* vz,
+                     double* ax, double* ay, double* az, double* ep, const uint8_t* type, const uint64_t* id,
+                     const double* masses, const double lo[3], const double hi[3], int pot_kind,
+                     const void* pot, double skin, double dt, int nsteps, int rebuild_every,
+                     double* thermo_out);
 
 /* The minimisation graph: forces, clipped push r += a*dt^2/2
  * (push_vec3_2nd_order_xform_minimization.cpp L116-149), list rebuilt every

@@ -133,6 +133,8 @@ def lib():
         L.orc_thermo.argtypes = [i64, vp, vp, vp, vp, vp, vp, vp, vp]
         L.orc_run_nve.restype = i32
         L.orc_run_nve.argtypes = [i64] + [vp] * 15 + [i32, vp, dbl, dbl, i32, i32, vp]
+        L.orc_run_nve_from.restype = i32
+        L.orc_run_nve_from.argtypes = [i64] + [vp] * 15 + [i32, vp, dbl, dbl, i32, i32, vp]
         L.orc_run_minimize.restype = i32
         L.orc_run_minimize.argtypes = [i64] + [vp] * 12 + [i32, vp, dbl, dbl, dbl, i32, i32]
         L.orc_last_list_builds.restype = i64
@@ -451,10 +453,12 @@ def thermo(vx, vy, vz, ep, vir, types, masses):
     return out
 
 
-def run_nve(state, masses, lo, hi, pot_kind, pot, skin, dt, nsteps, rebuild_every, thermo=True):
+def run_nve(state, masses, lo, hi, pot_kind, pot, skin, dt, nsteps, rebuild_every, thermo=True,
+            initial_forces=True):
     """Run the verlet_nve graph in place on `state` (dict of numpy arrays).
 
-    pot: LJParams / _Multi / EamOracleTables (its .pot is used)."""
+    pot: LJParams / _Multi / EamOracleTables (its .pot is used).
+    initial_forces=False: continue from the state's ax, ay, az (orc_run_nve_from)."""
     n = len(state["x"])
     th = np.zeros((nsteps + 1, 27)) if thermo else None
     if pot_kind == POT_LJ:
@@ -464,10 +468,11 @@ def run_nve(state, masses, lo, hi, pot_kind, pot, skin, dt, nsteps, rebuild_ever
     else:
         pp = C.addressof(pot.pot)
     s = state
-    rc = lib().orc_run_nve(n, _p(s["x"]), _p(s["y"]), _p(s["z"]), _p(s["vx"]), _p(s["vy"]), _p(s["vz"]),
-                           _p(s["ax"]), _p(s["ay"]), _p(s["az"]), _p(s["ep"]), _p(s["type"]), _p(s["id"]),
-                           _p(_f64(masses)), _p(_f64(lo)), _p(_f64(hi)), pot_kind, pp, float(skin),
-                           float(dt), int(nsteps), int(rebuild_every), _p(th))
+    run = lib().orc_run_nve if initial_forces else lib().orc_run_nve_from
+    rc = run(n, _p(s["x"]), _p(s["y"]), _p(s["z"]), _p(s["vx"]), _p(s["vy"]), _p(s["vz"]),
+             _p(s["ax"]), _p(s["ay"]), _p(s["az"]), _p(s["ep"]), _p(s["type"]), _p(s["id"]),
+             _p(_f64(masses)), _p(_f64(lo)), _p(_f64(hi)), pot_kind, pp, float(skin),
+             float(dt), int(nsteps), int(rebuild_every), _p(th))
     if rc != 0:
         raise RuntimeError("oracle run_nve failed with code %d" % rc)
     return th

@@ -4,7 +4,12 @@
 // tests/test_gpu_onika_bridge.py, which writes the input and checks the
 // output against the FP64 oracle.
 //
-//   bridge_driver <input.bin> <output.bin>
+//   bridge_driver <input.bin> <output.bin> [sx sy sz [tx ty tz]]
+//
+// With sx sy sz the domain has the diagonal xform diag(sx, sy, sz): the input
+// positions and bounds are grid coordinates, the physical ones are scaled.
+// With tx ty tz the xform becomes diag(tx, ty, tz) half-way through phase D
+// (before that step's push_f_v_r), as a deformation run changes it.
 //
 // Input (little endian): int64 n, ntypes, nsteps, ncell[3]; double lo[3],
 // hi[3], epsilon, sigma, rcut, skin, dt; double masses[ntypes];
@@ -27,6 +32,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <random>
 #include <vector>
@@ -101,10 +107,13 @@ void dump(FILE* out, const FakeGrid& g, const gb300::Session& s) {
 }  // namespace
 
 int main(int argc, char** argv) {
-  if (argc != 3) {
-    std::fprintf(stderr, "usage: bridge_driver input.bin output.bin\n");
+  if (argc != 3 && argc != 6 && argc != 9) {
+    std::fprintf(stderr, "usage: bridge_driver input.bin output.bin [sx sy sz [tx ty tz]]\n");
     return 2;
   }
+  double scale1[3] = {1.0, 1.0, 1.0}, scale2[3] = {1.0, 1.0, 1.0};
+  for (int d = 0; d < 3 && argc >= 6; ++d) scale1[d] = std::strtod(argv[3 + d], nullptr);
+  for (int d = 0; d < 3 && argc == 9; ++d) scale2[d] = std::strtod(argv[6 + d], nullptr);
   FILE* in = std::fopen(argv[1], "rb");
   if (!in) return 2;
   int64_t hdr[6];
@@ -141,7 +150,7 @@ int main(int argc, char** argv) {
   try {
     gb300::Session s;
     const int per[3] = {1, 1, 1};
-    gb300::ensure_context(s, nullptr, lo, hi, per, g.masses);
+    gb300::ensure_context(s, nullptr, lo, hi, per, g.masses, argc >= 6 ? scale1 : nullptr);
     gb300::check(s.ctx, gbmd_set_lj(s.ctx, eps, sig, rcut), "gbmd_set_lj");
     gb300::check(s.ctx, gbmd_set_skin(s.ctx, skin), "gbmd_set_skin");
     gb300::check(s.ctx, gbmd_set_precision(s.ctx, GBMD_PRECISION_FP64), "gbmd_set_precision");
@@ -179,6 +188,7 @@ int main(int argc, char** argv) {
         for (int d = 0; d < 3; ++d) c.f[gb300::FX + d][p] /= g.masses[c.type[p]];
     }
     for (int64_t st = 0; st < nsteps; ++st) {
+      if (argc == 9 && st == nsteps / 2) gb300::set_xform_scale(s, scale2);
       gb300::push_f_v_r(s, g, dt, 1.0);
       gb300::push_f_v(s, g, dt, 0.5);
       gb300::update_neighbors(s, g);

@@ -18,8 +18,10 @@ class Domain {
   bool periodic_boundary_y() const { return true; }
   bool periodic_boundary_z() const { return true; }
   bool xform_is_identity() const { return true; }
+  const Mat3d& xform() const { return m_xform; }
 
  private:
   AABB m_bounds;
+  Mat3d m_xform{1, 0, 0, 0, 1, 0, 0, 0, 1};
 };
 }  // namespace exanb

@@ -137,3 +137,70 @@ def test_plugin_bridge_per_call_reorder_and_whole_step(driver, oracle, tmp_path)
     assert _close(d["f"], np.stack([st["ax"], st["ay"], st["az"]], 1), 1e-10)
     assert _close(d["ep"], st["ep"], 1e-10)
     assert d["counts"][0] == 3  # one full upload when the whole-step mode took over
+
+
+def test_plugin_bridge_diagonal_xform_and_rescale(driver, oracle, tmp_path):
+    """A domain with the diagonal xform diag(1.05, 0.97, 1.02): the grid holds
+    grid coordinates (physical / scale) and the bridge hands the library the
+    physical ones.  Half-way through the whole-step phase the xform becomes
+    diag(1.07, 0.96, 1.01) (a deformation step): the device state goes back
+    into the grid with the old scale and comes back with the new one, the
+    atoms moving with the box.  Forces, energies and virials of phases A-C
+    within 1e-12 of the oracle on the physical coordinates; the trajectory
+    across the rescale within 1e-10 of the oracle's, which continues from
+    the accelerations of before the rescale as the device does."""
+    s = _system()
+    s1 = np.array([1.05, 0.97, 1.02])
+    s2 = np.array([1.07, 0.96, 1.01])
+    glo, ghi = s.lo / s1, s.hi / s1
+    gx, gy, gz = s.x / s1[0], s.y / s1[1], s.z / s1[2]
+    eps, sig, rcut, skin, dt = 1.0, 1.0, 2.5, 0.3, 0.004
+    inp, outp = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    with open(inp, "wb") as fh:
+        np.array([s.n, len(s.masses), NSTEPS, 3, 3, 3], np.int64).tofile(fh)
+        np.concatenate([glo, ghi, [eps, sig, rcut, skin, dt]]).astype(np.float64).tofile(fh)
+        np.asarray(s.masses, np.float64).tofile(fh)
+        for a in (gx, gy, gz, s.vx, s.vy, s.vz):
+            np.asarray(a, np.float64).tofile(fh)
+        np.asarray(s.type, np.uint8).tofile(fh)
+        np.asarray(s.id, np.uint64).tofile(fh)
+    subprocess.run([driver, inp, outp] + ["%.17g" % v for v in np.concatenate([s1, s2])], check=True, timeout=300)
+    ph = _read_phases(outp, s.n)
+    order = np.argsort(s.id)
+    types, ids = s.type[order], s.id[order]
+    lo1, hi1 = glo * s1, ghi * s1
+    lo2, hi2 = glo * s2, ghi * s2
+
+    for k in range(3):
+        r = ph[k]["r"] * s1            # the physical coordinates the library saw
+        x, y, z = (np.ascontiguousarray(r[:, d]) for d in range(3))
+        oracle.wrap(x, y, z, lo1, hi1)
+        nl = oracle.build_neighbors(x, y, z, ids, lo1, hi1, rcut + skin)
+        fx, fy, fz, ep, vir = oracle.lj_force(x, y, z, nl, hi1 - lo1, eps, sig, rcut)
+        assert _close(ph[k]["f"], np.stack([fx, fy, fz], 1), 1e-12), k
+        assert _close(ph[k]["ep"], ep, 1e-12), k
+        assert _close(ph[k]["vir"], vir, 1e-12), k
+    # D: the first half with diag(s1), the second with diag(s2)
+    r = ph[2]["r"] * s1
+    st = {"x": r[:, 0].copy(), "y": r[:, 1].copy(), "z": r[:, 2].copy(),
+          "vx": ph[2]["v"][:, 0].copy(), "vy": ph[2]["v"][:, 1].copy(), "vz": ph[2]["v"][:, 2].copy(),
+          "ax": np.zeros(s.n), "ay": np.zeros(s.n), "az": np.zeros(s.n), "ep": np.zeros(s.n),
+          "type": np.ascontiguousarray(types), "id": np.ascontiguousarray(ids)}
+    pot = oracle.LJParams(eps, sig, rcut)
+    half = NSTEPS // 2
+    oracle.run_nve(st, s.masses, lo1, hi1, oracle.POT_LJ, pot, skin, dt, half, -1, thermo=False)
+    for d, k in enumerate(("x", "y", "z")):
+        st[k] = (st[k] / s1[d]) * s2[d]
+    oracle.run_nve(st, s.masses, lo2, hi2, oracle.POT_LJ, pot, skin, dt, NSTEPS - half, -1, thermo=False,
+                   initial_forces=False)
+    d = ph[3]
+    got = [np.ascontiguousarray(d["r"][:, q] * s2[q]) for q in range(3)]
+    oracle.wrap(*got, lo2, hi2)
+    ref = [st["x"].copy(), st["y"].copy(), st["z"].copy()]
+    oracle.wrap(*ref, lo2, hi2)
+    dr = np.stack(got, 1) - np.stack(ref, 1)
+    dr -= np.round(dr / (hi2 - lo2)) * (hi2 - lo2)
+    assert np.abs(dr).max() < 1e-10
+    assert _close(d["v"], np.stack([st["vx"], st["vy"], st["vz"]], 1), 1e-10)
+    assert _close(d["f"], np.stack([st["ax"], st["ay"], st["az"]], 1), 1e-10)
+    assert d["counts"][0] == 4  # whole-step mode, then again after the rescale

@@ -238,6 +238,22 @@ def test_oracle_nve_conserves_energy(oracle):
     assert np.allclose(th[:, 18:21], 0.0, atol=1e-9)
 
 
+def test_oracle_nve_continues_from_given_accelerations(oracle):
+    """20 steps in one call equal 10 steps, then 10 more that start from the
+    accelerations the first call left (orc_run_nve_from), bit for bit: the
+    list is rebuilt from the same positions at step 10 in both."""
+    s = S.lj_fcc(ncell=4, seed=2)
+    pot = oracle.LJParams(1.0, 1.0, 2.5)
+    one = s.state()
+    oracle.run_nve(one, s.masses, s.lo, s.hi, oracle.POT_LJ, pot, 0.3, 0.005, 20, 10, thermo=False)
+    two = s.state()
+    oracle.run_nve(two, s.masses, s.lo, s.hi, oracle.POT_LJ, pot, 0.3, 0.005, 10, 10, thermo=False)
+    oracle.run_nve(two, s.masses, s.lo, s.hi, oracle.POT_LJ, pot, 0.3, 0.005, 10, 10, thermo=False,
+                   initial_forces=False)
+    for k in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az"):
+        assert np.array_equal(one[k], two[k]), k
+
+
 def test_oracle_minimiser_lowers_energy_and_clips(oracle):
     """Clipped minimiser on an overlapping random binary mixture: the
     potential energy falls and no step moves an atom further than
