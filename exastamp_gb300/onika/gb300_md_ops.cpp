@@ -573,12 +573,16 @@ class Gb300PushNode : public OperatorNode {
 // device's copy: trigger_move_particles (particle_displ_over against skin/2,
 // L19-22) and the full update (wrap, rebin, neighbour list) when it fires.
 // The outcome is published in trigger_move_particles for the graph's other
-// operators (load balancing logs, counters).
+// operators (load balancing logs, counters).  list_buffer > 0 makes the
+// rebuilds two-level (gbmd_set_list_buffer: the list filtered from an outer
+// list of rcut + skin + list_buffer, which is rebuilt with the sort into
+// cells only when an atom moved half the buffer); 0 keeps full rebuilds.
 template <class GridT>
 class Gb300NeighborsNode : public OperatorNode {
   ADD_SLOT(GridT, grid, INPUT_OUTPUT);
   ADD_SLOT(Domain, domain, INPUT, REQUIRED);
   ADD_SLOT(ParticleSpecies, species, INPUT, REQUIRED);
+  ADD_SLOT(double, list_buffer, INPUT, 0.0, DocString{"two-level list: outer buffer beyond rcut + skin (0: off)"});
   ADD_SLOT(bool, trigger_move_particles, OUTPUT);
   GB300_SESSION_SLOT;
 
@@ -586,6 +590,7 @@ class Gb300NeighborsNode : public OperatorNode {
   inline void execute() override final {
     if (grid->number_of_cells() == 0) return;
     gb300::Session& s = session_for(*gb300_session, *domain, *species);
+    gb300_ops::ok(s.ctx, gbmd_set_list_buffer(s.ctx, *list_buffer), "gbmd_set_list_buffer");
     gb300_ops::GridView<GridT> view(*grid, *species);
     bool rebuilt = false;
     gb300_ops::guarded("gb300_neighbors", [&] { rebuilt = gb300::update_neighbors(s, view); });
