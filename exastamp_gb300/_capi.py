@@ -76,6 +76,7 @@ def lib(path: str = LIB_PATH):
             "gbmd_set_launch_ex": ([vp, i32, i32, i32], i32),
             "gbmd_set_neighbor_staging": ([vp, i32], i32),
             "gbmd_set_newton3": ([vp, i32], i32),
+            "gbmd_check_errors": ([vp], i32),
             "gbmd_get_newton3": ([vp, P(i32)], i32),
             "gbmd_set_density_block": ([vp, i32], i32),
             "gbmd_get_density_block": ([vp, P(i32)], i32),
@@ -260,6 +261,11 @@ class Context:
         e = C.c_int()
         self._chk(self._L.gbmd_get_neighbor_staging(self.h, C.byref(e)))
         return bool(e.value)
+
+    def check_errors(self):
+        """Wait for the stream and raise on the device error word
+        (gbmd_check_errors)."""
+        self._chk(self._L.gbmd_check_errors(self.h))
 
     def set_newton3(self, enable):
         """Half list + scattered reaction forces (LJ, mixed precision)."""

@@ -100,8 +100,8 @@ int ensure_atom_capacity(gbmd_context* c, int64_t n) {
   c->cap = cap;
   if (c->newton3) {
     // zeroed once; the Newton-3 epilogue clears each atom's slots after reading them
-    GBMD_CUDA(c, cudaMalloc(&c->h3acc, sizeof(float4) * 3 * cap));
-    GBMD_CUDA(c, cudaMemset(c->h3acc, 0, sizeof(float4) * 3 * cap));
+    GBMD_CUDA(c, cudaMalloc(&c->h3acc, sizeof(long long) * 10 * cap));
+    GBMD_CUDA(c, cudaMemset(c->h3acc, 0, sizeof(long long) * 10 * cap));
   }
   c->cur = c->cur_s = 0;
   return GBMD_OK;
@@ -1056,8 +1056,8 @@ int gbmd_set_newton3(gbmd_context* c, int enable) {
   cudaSetDevice(c->device);
   if ((enable != 0) == c->newton3) return GBMD_OK;
   if (enable && c->cap > 0 && !c->h3acc) {
-    GBMD_CUDA(c, cudaMalloc(&c->h3acc, sizeof(float4) * 3 * c->cap));
-    GBMD_CUDA(c, cudaMemset(c->h3acc, 0, sizeof(float4) * 3 * c->cap));
+    GBMD_CUDA(c, cudaMalloc(&c->h3acc, sizeof(long long) * 10 * c->cap));
+    GBMD_CUDA(c, cudaMemset(c->h3acc, 0, sizeof(long long) * 10 * c->cap));
   }
   c->newton3 = enable != 0;
   c->list_valid = false;  // the half and the full list differ
@@ -1181,7 +1181,16 @@ static int check_device_errors(gbmd_context* c) {
                      c->h_err[ERRW_MAXNB], c->maxnb);
   if (f & GBMD_DEVERR_NONFINITE)
     return set_error(c, GBMD_ERR_NONFINITE, "non-finite force on atom %d", c->h_err[ERRW_BADATOM]);
+  if (f & GBMD_DEVERR_RANGE)
+    return set_error(c, GBMD_ERR_TOO_LARGE,
+                     "a Newton-3 pair force beyond 2^16 x 24 eps/sigma (the fixed-point range); use the full list");
   return set_error(c, GBMD_ERR_CUDA, "device error flags %d", f);
+}
+
+int gbmd_check_errors(gbmd_context* c) {
+  if (!c) return GBMD_ERR_INVALID;
+  cudaSetDevice(c->device);
+  return check_device_errors(c);
 }
 
 int gbmd_compute_forces(gbmd_context* c, int flags) {

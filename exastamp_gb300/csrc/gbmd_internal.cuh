@@ -43,6 +43,7 @@ enum {
   GBMD_DEVERR_LOST_ATOM = 2,
   GBMD_DEVERR_NONFINITE = 4,
   GBMD_DEVERR_TABLE_RANGE = 8,
+  GBMD_DEVERR_RANGE = 16,     // a Newton-3 contribution beyond the fixed-point range
 };
 
 namespace gbmd {
@@ -194,7 +195,7 @@ struct gbmd_context {
   bool fused_trigger = false;   // run_nve with the displacement trigger: kernels that move atoms test them
   bool first_half_done = false; // gbmd_run_nve_host pushed the first half while reading the state in
   bool newton3 = false;         // half list (j > i in cell order) + scattered reaction forces (LJ, mixed)
-  float4* h3acc = nullptr;      // Newton-3 accumulators, 3 float4 per atom: (f, ep), virial xx yy zz xy, xz yz
+  long long* h3acc = nullptr;   // Newton-3 fixed-point accumulators, 10 planes of cap: f (3), ep, virial (6)
   int block = 256;              // threads per block of the pair / force kernels (autotuned)
   int block_rho = 128;          // threads per block of the EAM density kernels (autotuned; 0 = block)
   double skin = 0.0, rlist = 0.0;

@@ -19,6 +19,9 @@
 // of a row are added in FP32, the row sum goes into the compensated sum.
 // 1/r and r come from one rsqrt; the stencil offset decodes to an exact
 // float in two integer/FP ops per axis.
+#include <algorithm>
+#include <cmath>
+
 #include "gbmd_pair_common.cuh"
 
 namespace gbmd {
@@ -645,24 +648,52 @@ __global__ void __launch_bounds__(256) k_eam_force_staged(PairArgs A, EamDev E, 
 // Newton-3 LJ (lj_compute_force_symetric, pair_potential_singlemat_symetric.cpp
 // L230-320): every unordered pair once, from the half list (j after i in cell
 // order).  The pair's force, half its energy and half its virial go to i's
-// register sums and -- the force negated -- to j's accumulators through
-// float4 / float2 atomic additions (the reference takes a spin lock on j);
-// i's own sums are added to its accumulators once at the end, since other
-// threads add to them as well.  The accumulators are three planes of `cap`
-// float4: (f, ep), (vxx, vyy, vzz, vxy), (vxz, vyz).  k_h3_epilogue turns
-// them into the acceleration (and the fused Verlet half steps) and clears
-// them for the next pass.  The atomic order varies from run to run, so the
-// result is not bit-reproducible (the full-list kernels are).
+// register sums and -- the force negated -- to j's accumulators (the
+// reference takes a spin lock on j); i's own sums are added to its
+// accumulators once at the end, since other threads add to them as well.
+//
+// The accumulators are 64-bit fixed-point integers, so the sums do not depend
+// on the order the additions arrive in and the results are the same from run
+// to run.  Ten planes of `cap`: f (3), ep, virial xx yy zz xy xz yz.  A value
+// x is stored as round(x * 2^38 / b), b a power of two bounding its kind (24
+// eps/sigma for forces, 4 eps for energies, that force times rcut for
+// virials): x * 2^38 / b is exact in FP32 and the rounding is deterministic.
+// A pair's contribution must stay below 2^16 b, i's own sum below 2^24 b, so
+// that 512 of them cannot overflow 2^63; a larger one raises
+// GBMD_DEVERR_RANGE.  k_h3_epilogue turns the sums into the acceleration
+// (and the fused Verlet half steps) and clears them for the next pass.
 // ---------------------------------------------------------------------------
+struct FixScale {
+  float f, e, v;       // 2^38 / bound for forces, energies, virials
+  double inv_f, inv_e, inv_v;
+  int* err;
+};
+
+constexpr float FIX_PAIR_LIMIT = 0x1p54f;  // |x * scale| of one pair's contribution
+constexpr float FIX_SUM_LIMIT = 0x1p62f;   // |x * scale| of an atom's own sum
+
+__device__ __forceinline__ long long fix_q(float x, float scale, float limit, int* err) {
+  float y = x * scale;
+  if (!(fabsf(y) <= limit)) {
+    atomicOr(err, GBMD_DEVERR_RANGE);
+    y = y != y ? 0.f : copysignf(limit, y);
+  }
+  return __float2ll_rn(y);
+}
+
+__device__ __forceinline__ void fix_add(long long* p, long long q) {
+  // two's complement: the unsigned sum is the signed one modulo 2^64
+  atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)q);
+}
+
 template <bool EV, bool MULTI>
 __global__ void __launch_bounds__(256, EV ? 1 : 4) k_lj_half(PairArgs A, LJF P, const LJPair* __restrict__ tab, int ntypes,
-                                                 double rcmax2, float4* __restrict__ acc, int64_t cap) {
+                                                 double rcmax2, long long* __restrict__ acc, int64_t cap,
+                                                 FixScale X) {
   __shared__ LJTabSmem tb;
   if (MULTI) lj_load_table(tb, tab, ntypes);
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= A.n) return;
-  float4* acc1 = acc + cap;
-  float4* acc2 = acc + 2 * cap;
   const int nn = min(A.nnb[i], A.maxnb);
   const float4 pi = A.posf[i];
   const int cp = A.cellpack[i];
@@ -711,18 +742,21 @@ __global__ void __launch_bounds__(256, EV ? 1 : 4) k_lj_half(PairArgs A, LJF P, 
         rx -= gx;
         ry -= gy;
         rz -= gz;
+        fix_add(acc + j, fix_q(gx, X.f, FIX_PAIR_LIMIT, X.err));
+        fix_add(acc + cap + j, fix_q(gy, X.f, FIX_PAIR_LIMIT, X.err));
+        fix_add(acc + 2 * cap + j, fix_q(gz, X.f, FIX_PAIR_LIMIT, X.err));
         if (EV) {
           const float eh = 0.5f * fmaf(eps4, s12 - s6, -ecut);
           const float h = 0.5f * fpair;
-          const float w0 = h * G.dx * G.dx, w1 = h * G.dy * G.dy, w2 = h * G.dz * G.dz;
-          const float w3 = h * G.dx * G.dy, w4 = h * G.dx * G.dz, w5 = h * G.dy * G.dz;
+          const float w[6] = {h * G.dx * G.dx, h * G.dy * G.dy, h * G.dz * G.dz,
+                              h * G.dx * G.dy, h * G.dx * G.dz, h * G.dy * G.dz};
           re += eh;
-          v[0] += w0; v[1] += w1; v[2] += w2; v[3] += w3; v[4] += w4; v[5] += w5;
-          atomicAdd(acc + j, make_float4(gx, gy, gz, eh));
-          atomicAdd(acc1 + j, make_float4(w0, w1, w2, w3));
-          atomicAdd(reinterpret_cast<float2*>(acc2 + j), make_float2(w4, w5));
-        } else {
-          atomicAdd(acc + j, make_float4(gx, gy, gz, 0.f));
+          fix_add(acc + 3 * cap + j, fix_q(eh, X.e, FIX_PAIR_LIMIT, X.err));
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            v[k] += w[k];
+            fix_add(acc + (4 + k) * cap + j, fix_q(w[k], X.v, FIX_PAIR_LIMIT, X.err));
+          }
         }
       }
     }
@@ -733,31 +767,67 @@ __global__ void __launch_bounds__(256, EV ? 1 : 4) k_lj_half(PairArgs A, LJF P, 
 #pragma unroll
     for (int q = 0; q < 4; ++q) ent[q] = nxt[q];
   }
-  atomicAdd(acc + i, make_float4(fx - cfx, fy - cfy, fz - cfz, EV ? e - ce : 0.f));
+  fix_add(acc + i, fix_q(fx - cfx, X.f, FIX_SUM_LIMIT, X.err));
+  fix_add(acc + cap + i, fix_q(fy - cfy, X.f, FIX_SUM_LIMIT, X.err));
+  fix_add(acc + 2 * cap + i, fix_q(fz - cfz, X.f, FIX_SUM_LIMIT, X.err));
   if (EV) {
-    atomicAdd(acc1 + i, make_float4(v[0], v[1], v[2], v[3]));
-    atomicAdd(reinterpret_cast<float2*>(acc2 + i), make_float2(v[4], v[5]));
+    fix_add(acc + 3 * cap + i, fix_q(e - ce, X.e, FIX_SUM_LIMIT, X.err));
+#pragma unroll
+    for (int k = 0; k < 6; ++k) fix_add(acc + (4 + k) * cap + i, fix_q(v[k], X.v, FIX_SUM_LIMIT, X.err));
   }
 }
 
 template <bool EV>
-__global__ void __launch_bounds__(256) k_h3_epilogue(PairArgs A, float4* __restrict__ acc, int64_t cap) {
+__global__ void __launch_bounds__(256) k_h3_epilogue(PairArgs A, long long* __restrict__ acc, int64_t cap,
+                                                     FixScale X) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= A.n) return;
-  const float4 f = acc[i];
-  acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  double f[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    f[d] = (double)acc[d * cap + i] * X.inv_f;
+    acc[d * cap + i] = 0;
+  }
   const int t = __float_as_int(A.posf[i].w);
   const float im = A.inv_massf[t];
   double o[9];
+  double epv = 0.0;
   if (EV) {
-    const float4 w = acc[cap + i];
-    const float4 u = acc[2 * cap + i];
-    acc[cap + i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    acc[2 * cap + i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float v[6] = {w.x, w.y, w.z, w.w, u.x, u.y};
+    epv = (double)acc[3 * cap + i] * X.inv_e;
+    acc[3 * cap + i] = 0;
+    float v[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      v[k] = (float)((double)acc[(4 + k) * cap + i] * X.inv_v);
+      acc[(4 + k) * cap + i] = 0;
+    }
     vir9(v, o);
   }
-  atom_epilogue<true>(A, i, t, 0., 0., 0., f.x * im, f.y * im, f.z * im, EV ? (double)f.w : 0.0, EV ? o : nullptr);
+  atom_epilogue<true>(A, i, t, 0., 0., 0., (float)f[0] * im, (float)f[1] * im, (float)f[2] * im, epv,
+                      EV ? o : nullptr);
+}
+
+// Power-of-two fixed-point scales of the bounds above, from the LJ table.
+static FixScale fix_scales(const gbmd_context* c) {
+  double fmax = 0.0, emax = 0.0;
+  const int nt = c->pot == GBMD_POT_LJ ? 1 : c->lj.ntypes;
+  for (int a = 0; a < nt * nt; ++a) {
+    const LJPair& q = c->lj.p[a];
+    fmax = std::max(fmax, 24.0 * std::fabs(q.eps) / q.sig);
+    emax = std::max(emax, 4.0 * std::fabs(q.eps));
+  }
+  const double vmax = fmax * c->lj.rcut_max;
+  auto pow2_above = [](double x) { return std::ldexp(1.0, (int)std::ceil(std::log2(std::max(x, 1e-300)))); };
+  const double bf = pow2_above(fmax), be = pow2_above(emax), bv = pow2_above(vmax);
+  FixScale X;
+  X.f = (float)std::ldexp(1.0 / bf, 38);
+  X.e = (float)std::ldexp(1.0 / be, 38);
+  X.v = (float)std::ldexp(1.0 / bv, 38);
+  X.inv_f = std::ldexp(bf, -38);
+  X.inv_e = std::ldexp(be, -38);
+  X.inv_v = std::ldexp(bv, -38);
+  X.err = c->d_err + ERRW_FLAGS;
+  return X;
 }
 
 template <bool EV>
@@ -766,15 +836,16 @@ static int launch_newton3(gbmd_context* c, const PairArgs& A, int part) {
   const int B = 256;
   const unsigned grid = (unsigned)((A.n + B - 1) / B);
   cudaStream_t s = c->stream;
+  const FixScale X = fix_scales(c);
   if (c->pot == GBMD_POT_LJ) {
     const LJPair& q = c->lj.p[0];
     LJF P{q.sig2f, q.eps24f, q.eps4f, q.ecutf, q.rc2lo, q.rc2hi, q.rc2, q.rc};
-    k_lj_half<EV, false><<<grid, B, 0, s>>>(A, P, nullptr, 1, c->lj.rcut_max2, c->h3acc, c->cap);
+    k_lj_half<EV, false><<<grid, B, 0, s>>>(A, P, nullptr, 1, c->lj.rcut_max2, c->h3acc, c->cap, X);
   } else {
     LJF P{};
-    k_lj_half<EV, true><<<grid, B, 0, s>>>(A, P, c->lj_tab_d, c->lj.ntypes, c->lj.rcut_max2, c->h3acc, c->cap);
+    k_lj_half<EV, true><<<grid, B, 0, s>>>(A, P, c->lj_tab_d, c->lj.ntypes, c->lj.rcut_max2, c->h3acc, c->cap, X);
   }
-  k_h3_epilogue<EV><<<grid, B, 0, s>>>(A, c->h3acc, c->cap);
+  k_h3_epilogue<EV><<<grid, B, 0, s>>>(A, c->h3acc, c->cap, X);
   return GBMD_OK;
 }
 

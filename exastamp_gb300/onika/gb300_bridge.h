@@ -218,6 +218,8 @@ void write_forces(Session& s, G& g, bool energy, bool virial, bool as_force) {
   check(s.ctx, gbmd_download(s.ctx, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, s.a[0].data(), s.a[1].data(),
                              s.a[2].data(), energy ? s.ep.data() : nullptr, vir ? s.vir.data() : nullptr),
         "gbmd_download");
+  // non-finite or out-of-range forces, list overflow: the reference aborts
+  check(s.ctx, gbmd_check_errors(s.ctx), "gbmd_check_errors");
   for (size_t k = 0; k < n; ++k) {
     const size_t c = s.cell[k], p = s.slot[k];
     const double m = as_force ? g.mass(s.type[k]) : 1.0;
@@ -353,6 +355,7 @@ void sync_grid(Session& s, G& g, bool energy, bool virial) {
                              s.v[2].data(), s.a[0].data(), s.a[1].data(), s.a[2].data(),
                              energy ? s.ep.data() : nullptr, vir ? s.vir.data() : nullptr),
         "gbmd_download");
+  check(s.ctx, gbmd_check_errors(s.ctx), "gbmd_check_errors");
   for (size_t k = 0; k < n; ++k) {
     const size_t c = s.cell[k], p = s.slot[k];
     g.set(c, RX, p, s.r[0][k] / s.scale[0]);

@@ -188,10 +188,13 @@ int gbmd_get_neighbor_staging(const gbmd_context* ctx, int* enabled);
  * src/potential/pair_potential_template/pair_potential_singlemat_symetric.cpp
  * L44, L230-320): the list keeps each unordered pair once (j after i in
  * cell order) and the LJ kernels add the reaction force, half the pair
- * energy and half the pair virial to j with FP32 atomics.  LJ potentials in
- * mixed precision with the 1 lane x 4 entries launch only; other set-ups
- * return GBMD_ERR_UNSUPPORTED at the force call.  Results are not
- * bit-reproducible from run to run (atomic order).  Default 0. */
+ * energy and half the pair virial to j with 64-bit fixed-point integer
+ * atomics, so the sums do not depend on the order of the additions and runs
+ * are bit-reproducible.  A pair force beyond 2^16 x 24 eps/sigma (pairs
+ * closer than ~0.49 sigma) is outside the fixed-point range: the force call
+ * returns GBMD_ERR_TOO_LARGE.  LJ potentials in mixed precision with the
+ * 1 lane x 4 entries launch only; other set-ups return
+ * GBMD_ERR_UNSUPPORTED at the force call.  Default 0. */
 int gbmd_set_newton3(gbmd_context* ctx, int enable);
 int gbmd_get_newton3(const gbmd_context* ctx, int* enabled);
 
@@ -243,6 +246,13 @@ int gbmd_neighbor_stats(gbmd_context* ctx, int64_t* npairs, int* maxnb, int* nc3
  * call a* holds f/m, ep the per-atom energy (GBMD_FORCE_ENERGY) and vir the
  * per-atom virial (GBMD_FORCE_VIRIAL). Builds the list first if needed. */
 int gbmd_compute_forces(gbmd_context* ctx, int flags);
+/* Waits for the context's stream and reports the device error word, then
+ * clears it: GBMD_ERR_NONFINITE (a non-finite force), GBMD_ERR_TOO_LARGE (a
+ * Newton-3 contribution beyond the fixed-point range),
+ * GBMD_ERR_NEIGHBOR_OVERFLOW, GBMD_ERR_LOST_ATOM.  The force call returns
+ * before its kernels finish; gbmd_run_nve and gbmd_run_minimize check on
+ * their own. */
+int gbmd_check_errors(gbmd_context* ctx);
 
 /* ---- integration -----------------------------------------------------------
  * push_f_v_r: r += v*dt' + a*dt'^2/2, dt' = dt*dt_scale; push_f_v: v += a*dt*

@@ -1,11 +1,14 @@
-"""Newton-3 mode (lj_compute_force_symetric): half list + scattered reaction
-forces, called through the C ABI, against the FP64 oracle.
+"""Newton-3 mode (lj_compute_force_symetric): half list + reaction forces
+scattered through 64-bit fixed-point atomics, called through the C ABI,
+against the FP64 oracle.
 
 Bars: the half list holds each pair of the full list exactly once (bit-exact
 pair set after mirroring); forces within 1e-5 relative RMS (the mixed
 tolerance), total energy within 1e-6 relative, virial within 1e-5 relative
-RMS; an NVE run stays close to the full-list run; the set-ups without a
-Newton-3 kernel answer GBMD_ERR_UNSUPPORTED.
+RMS; two runs are bit-identical (the integer sums do not depend on the
+order of the atomics); an NVE run stays close to the full-list run; a pair
+force beyond the fixed-point range answers GBMD_ERR_TOO_LARGE; the set-ups
+without a Newton-3 kernel answer GBMD_ERR_UNSUPPORTED.
 """
 import numpy as np
 import pytest
@@ -19,6 +22,7 @@ pytestmark = pytest.mark.gpu
 
 MIXED_FORCE_TOL = 1e-5
 UNSUPPORTED = 8  # GBMD_ERR_UNSUPPORTED
+TOO_LARGE = 9    # GBMD_ERR_TOO_LARGE
 
 
 def _n3_ctx(gpu, s, pot, skin=0.3):
@@ -183,3 +187,44 @@ def test_symetric_operator_matches_lj_compute_force(gpu, oracle, half_list):
     else:
         assert np.abs(G - F).max() < 1e-12 * np.abs(F).max()
         assert np.abs(d["ep"] - ep).max() < 1e-12 * np.abs(ep).max()
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_newton3_runs_are_bit_reproducible(gpu, use_graph):
+    """The same 40 steps twice (LJ mixture types, energies and virials on
+    thermo steps): every array equal bit for bit."""
+    s = _jitter(S.lj_fcc(ncell=8, seed=21), 0.05, 21)
+    rng = np.random.default_rng(21)
+    s.type = (rng.random(s.n) < 0.2).astype(np.uint8)
+    s.masses = np.array([1.0, 2.0])
+    eps, sig, rc = S.kob_andersen_tables()
+    out = []
+    for _ in range(2):
+        with _n3_ctx(gpu, s, lambda c: c.set_lj_multi(eps, sig, rc, 0.0)) as ctx:
+            th = ctx.run_nve(40, 0.002, rebuild_every=10, thermo_every=20, use_graph=use_graph)
+            ctx.compute_forces(energy=True, virial=True)
+            out.append((th, ctx.download(virial=True)))
+    assert np.array_equal(out[0][0], out[1][0])
+    for k in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "ep", "vir"):
+        assert np.array_equal(out[0][1][k], out[1][1][k]), k
+
+
+def test_newton3_force_beyond_the_fixed_point_range(gpu):
+    """Two atoms 0.4 sigma apart: a pair force of ~7e6 (beyond 2^16 x 24
+    eps/sigma) is refused on the half list; the full list computes it."""
+    s = S.lj_fcc(ncell=4, seed=22)
+    s.x[1], s.y[1], s.z[1] = s.x[0] + 0.4, s.y[0], s.z[0]
+    with _n3_ctx(gpu, s, LJ) as ctx:
+        ctx.compute_forces()
+        with pytest.raises(gpu.GbmdError) as e:
+            ctx.check_errors()
+        assert e.value.code == TOO_LARGE
+        ctx.check_errors()  # cleared once reported
+        with pytest.raises(gpu.GbmdError) as e:
+            ctx.run_nve(1, 0.001, rebuild_every=0)
+        assert e.value.code == TOO_LARGE
+        ctx.set_newton3(False)
+        ctx.compute_forces()
+        ctx.check_errors()
+        d = ctx.download()
+    assert np.isfinite(d["ax"]).all() and abs(d["ax"][0]) > 1e6
