@@ -817,7 +817,9 @@ static FixScale fix_scales(const gbmd_context* c) {
     emax = std::max(emax, 4.0 * std::fabs(q.eps));
   }
   const double vmax = fmax * c->lj.rcut_max;
-  auto pow2_above = [](double x) { return std::ldexp(1.0, (int)std::ceil(std::log2(std::max(x, 1e-300)))); };
+  // bounds of at least 2^-60 keep the FP32 scales finite (all-zero epsilon
+  // tables give zero forces, which any scale represents)
+  auto pow2_above = [](double x) { return std::ldexp(1.0, (int)std::ceil(std::log2(std::max(x, 0x1p-60)))); };
   const double bf = pow2_above(fmax), be = pow2_above(emax), bv = pow2_above(vmax);
   FixScale X;
   X.f = (float)std::ldexp(1.0 / bf, 38);
