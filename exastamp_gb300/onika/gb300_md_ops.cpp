@@ -267,8 +267,9 @@ using gb300_ops::session_for;
 // energy shifted by e(rcut) as the reference does (L373-377).  SYM: the
 // lj_compute_force_symetric slots (pair_potential_singlemat_symetric.cpp
 // L335-346; particle_locks accepted and unused).  The forces are the same;
-// the library's full list is faster on GB300 and deterministic, so the
-// Newton-3 half list (atomic reaction forces) is opt-in through half_list.
+// the library's full list is faster on GB300, so the Newton-3 half list
+// (reaction forces through fixed-point atomics, also deterministic) is
+// opt-in through half_list.
 template <class GridT, bool SYM = false>
 class Gb300LJForceNode : public OperatorNode {
   ADD_SLOT(LennardJonesParms, parameters, INPUT, LennardJonesParms{});

@@ -186,11 +186,11 @@ class lj_compute_force_symetric(lj_compute_force):
     slots L335-346): the forces of lj_compute_force, which the reference
     evaluates on a Newton-3 half list, scattering each reaction force under
     per-particle spin locks (`particle_locks`, accepted and unused here).
-    The full list gives the same sums up to rounding, deterministically, and
-    is faster on GB300, so it is the default (as in the plugin);
-    `half_list: true` selects the library's half list, whose reaction forces
-    are added with FP32 atomics (mixed precision, one lane x 4 entries per
-    load)."""
+    The full list gives the same sums up to rounding and is faster on
+    GB300, so it is the default (as in the plugin); `half_list: true`
+    selects the library's half list, whose reaction forces are added with
+    64-bit fixed-point atomics, deterministic as well (mixed precision, one
+    lane x 4 entries per load)."""
     name = "lj_compute_force_symetric"
 
     def bind(self, sim: Simulation):
