@@ -77,7 +77,7 @@ def test_eam_autograd_gradient(gpu, oracle):
         # central differences of the forward, on the three largest components
         fd = {}
         for k in np.argsort(-np.abs(g))[:3]:
-            h = 1e-4 * abs(float(p[k]))
+            h = 1e-4 * abs(float(p.detach()[k]))
             pp, pm = p.detach().clone(), p.detach().clone()
             pp[k] += h
             pm[k] -= h
