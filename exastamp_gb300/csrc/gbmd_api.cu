@@ -888,6 +888,7 @@ int gbmd_set_eam_alloy(gbmd_context* c, int nel, int nrho, double drho, int nr, 
   E.rc2f = (float)E.rcut2;
   E.rc2lo = (float)(E.rcut2 * (1.0 - 0x1p-12));
   E.rc2hi = (float)(E.rcut2 * (1.0 + 0x1p-12));
+  c->eam_fix_ok = false;
   c->pot = GBMD_POT_EAM_ALLOY;
   set_rlist(c, rcut);
   return GBMD_OK;

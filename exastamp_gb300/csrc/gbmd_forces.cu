@@ -340,8 +340,10 @@ int launch_forces(gbmd_context* c, const ForceFlags& f) {
   const PairArgs A = make_args(c, f);
   const bool ev = f.energy || f.virial;
   const bool mixed = c->precision == GBMD_PRECISION_MIXED;
-  if (c->newton3 && !(mixed && (c->pot == GBMD_POT_LJ || c->pot == GBMD_POT_LJ_MULTI)))
-    return set_error(c, GBMD_ERR_UNSUPPORTED, "Newton-3 half lists: LJ potentials in mixed precision only");
+  if (c->newton3 &&
+      !(mixed && (c->pot == GBMD_POT_LJ || c->pot == GBMD_POT_LJ_MULTI || c->pot == GBMD_POT_EAM_ALLOY)))
+    return set_error(c, GBMD_ERR_UNSUPPORTED,
+                     "Newton-3 half lists: LJ potentials and eam_alloy in mixed precision only");
   if (c->newton3 && !c->h3acc) return set_error(c, GBMD_ERR_INVALID, "Newton-3 accumulators not allocated");
   const int part = f.part;
   int rc;

@@ -196,6 +196,8 @@ struct gbmd_context {
   bool first_half_done = false; // gbmd_run_nve_host pushed the first half while reading the state in
   bool newton3 = false;         // half list (j > i in cell order) + scattered reaction forces (LJ, mixed)
   long long* h3acc = nullptr;   // Newton-3 fixed-point accumulators, 10 planes of cap: f (3), ep, virial (6)
+  double eam_fix_bound[4] = {1.0, 1.0, 1.0, 1.0};  // Newton-3 eam_alloy bounds: rho, force, energy, virial
+  bool eam_fix_ok = false;      // eam_fix_bound is that of the current tables
   int block = 256;              // threads per block of the pair / force kernels (autotuned)
   int block_rho = 128;          // threads per block of the EAM density kernels (autotuned; 0 = block)
   double skin = 0.0, rlist = 0.0;

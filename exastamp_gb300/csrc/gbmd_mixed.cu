@@ -664,8 +664,8 @@ __global__ void __launch_bounds__(256) k_eam_force_staged(PairArgs A, EamDev E, 
 // (and the fused Verlet half steps) and clears them for the next pass.
 // ---------------------------------------------------------------------------
 struct FixScale {
-  float f, e, v;       // 2^38 / bound for forces, energies, virials
-  double inv_f, inv_e, inv_v;
+  float f, e, v, r;    // 2^38 / bound for forces, energies, virials, EAM densities
+  double inv_f, inv_e, inv_v, inv_r;
   int* err;
 };
 
@@ -779,7 +779,7 @@ __global__ void __launch_bounds__(256, EV ? 1 : 4) k_lj_half(PairArgs A, LJF P, 
 
 template <bool EV>
 __global__ void __launch_bounds__(256) k_h3_epilogue(PairArgs A, long long* __restrict__ acc, int64_t cap,
-                                                     FixScale X) {
+                                                     FixScale X, const float* __restrict__ epf) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= A.n) return;
   double f[3];
@@ -793,7 +793,7 @@ __global__ void __launch_bounds__(256) k_h3_epilogue(PairArgs A, long long* __re
   double o[9];
   double epv = 0.0;
   if (EV) {
-    epv = (double)acc[3 * cap + i] * X.inv_e;
+    epv = (double)acc[3 * cap + i] * X.inv_e + (epf ? (double)epf[i] : 0.0);
     acc[3 * cap + i] = 0;
     float v[6];
 #pragma unroll
@@ -807,6 +807,194 @@ __global__ void __launch_bounds__(256) k_h3_epilogue(PairArgs A, long long* __re
                       EV ? o : nullptr);
 }
 
+// Newton-3 eam_alloy (eam_symmetry: eam_force_op_multimat.h L162-169 rho_j
+// scatter, L305-338 reaction force): the same per-pair FP32 expressions as
+// k_eam_rho_mixed / k_eam_force_mixed on the half list.  The density pass
+// adds rho_tj(r) to i's own sum and rho_ti(r) to j's fixed-point plane (the
+// energy plane, free until the force pass); k_eam_embed_half turns the sums
+// into F'(rho) (and F(rho)); the force pass adds u_ij psi'_ij / r to i and
+// its opposite to j, half of phi to both, the pair virial to both.
+template <bool SINGLE>
+__global__ void __launch_bounds__(256, 4) k_eam_rho_half(PairArgs A, EamDev E, long long* __restrict__ racc,
+                                                         FixScale X) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= A.n) return;
+  const int nn = min(A.nnb[i], A.maxnb);
+  const float4 pi = A.posf[i];
+  const int cp = A.cellpack[i];
+  const int ti = SINGLE ? 0 : __float_as_int(pi.w);
+  const int nr = E.nr, nr1 = E.nr + 1;
+  float rho = 0.f, crho = 0.f;
+  const ListRows<1, 4> L(A.nbr, i, 0, A.stride, nn);
+  const GlobalFetch fetch{A.posf};
+  uint32_t ent[4], nxt[4];
+  if (L.nrow > 0) L.load(0, ent);
+  for (int r = 0; r < L.nrow; ++r) {
+    if (r + 1 < L.nrow) L.load(r + 1, nxt);
+    float4 pj[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (!L.valid(r, q)) ent[q] = L.standin;
+      pj[q] = fetch(ent[q], ent[q] & GBMD_IDX_MASK);
+    }
+    float rr = 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t j = ent[q] & GBMD_IDX_MASK;
+      const GeomF G = geom_f(ent[q], pj[q], pi, A.g);
+      bool in = G.d2 < E.rc2lo;
+      if (!in && G.d2 <= E.rc2hi && L.valid(r, q))
+        in = exact_inside(A.posd, i, j, ent[q] >> GBMD_IDX_BITS, cp, A.g, E.rcut2, 0.0);
+      const float rd = G.d2 * rsqrtf(G.d2);
+      float t;
+      const int m = knot_f(rd, E.rdrf, nr, t);
+      const int tj = SINGLE ? 0 : __float_as_int(pj[q].w);
+      const float vj = spline_val(__ldg(&E.rhor4[tj * nr1 + m]), t);
+      const float vi = (SINGLE || ti == tj) ? vj : spline_val(__ldg(&E.rhor4[ti * nr1 + m]), t);
+      rr += in ? vj : 0.f;
+      if (in) fix_add(racc + j, fix_q(vi, X.r, FIX_PAIR_LIMIT, X.err));
+    }
+    kahan_add(rho, crho, rr);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ent[q] = nxt[q];
+  }
+  fix_add(racc + i, fix_q(rho - crho, X.r, FIX_SUM_LIMIT, X.err));
+}
+
+// Rho2EmbOp / eam_alloy_fEmbed on the summed densities (the embedding of
+// eam_rho_atom): F'(rho), F(rho) on energy steps, linear continuation above
+// rhomax; the density plane is cleared for the energies of the force pass.
+template <bool EV, bool SINGLE>
+__global__ void __launch_bounds__(256) k_eam_embed_half(PairArgs A, EamDev E, long long* __restrict__ racc,
+                                                        FixScale X, float* __restrict__ fpf, float* __restrict__ epf,
+                                                        float4* __restrict__ pfp) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= A.n) return;
+  const float R = (float)((double)racc[i] * X.inv_r);
+  racc[i] = 0;
+  const float4 pi = A.posf[i];
+  const int ti = SINGLE ? 0 : __float_as_int(pi.w);
+  float q = fmaf(R, E.rdrhof, 1.0f);
+  int m = (int)q;
+  m = max(1, min(m, E.nrho - 1));
+  q = fminf(q - (float)m, 1.0f);
+  const float4 c = __ldg(&E.frho4[(SINGLE ? 0 : ti * (E.nrho + 1)) + m]);
+  const float fp = spline_der(c, q, E.rdrhof);
+  fpf[i] = fp;
+  if (SINGLE) pfp[i] = make_float4(pi.x, pi.y, pi.z, fp);
+  if (EV) {
+    float phi = spline_val(c, q);
+    if (R > E.rhomaxf) phi = fmaf(fp, R - E.rhomaxf, phi);
+    epf[i] = phi;
+  }
+}
+
+template <bool EV, bool SINGLE>
+__global__ void __launch_bounds__(256, EV ? 1 : 4) k_eam_force_half(PairArgs A, EamDev E,
+                                                                    const float* __restrict__ fpf,
+                                                                    const float4* __restrict__ pfp,
+                                                                    long long* __restrict__ acc, int64_t cap,
+                                                                    FixScale X) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= A.n) return;
+  const int nn = min(A.nnb[i], A.maxnb);
+  const float4 pi = A.posf[i];
+  const int cp = A.cellpack[i];
+  const float fpi = fpf[i];
+  const int ti = SINGLE ? 0 : __float_as_int(pi.w);
+  const int nr = E.nr, nr1 = E.nr + 1;
+  const float rdr = E.rdrf;
+  float fx = 0.f, fy = 0.f, fz = 0.f, cfx = 0.f, cfy = 0.f, cfz = 0.f, e = 0.f, ce = 0.f;
+  float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  const ListRows<1, 4> L(A.nbr, i, 0, A.stride, nn);
+  const GlobalFetch fetch{SINGLE ? pfp : A.posf};
+  uint32_t ent[4], nxt[4];
+  if (L.nrow > 0) L.load(0, ent);
+  for (int r = 0; r < L.nrow; ++r) {
+    if (r + 1 < L.nrow) L.load(r + 1, nxt);
+    float4 pj[4];
+    float fpj[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (!L.valid(r, q)) ent[q] = L.standin;
+      const uint32_t j = ent[q] & GBMD_IDX_MASK;
+      pj[q] = fetch(ent[q], j);
+      fpj[q] = SINGLE ? pj[q].w : __ldg(&fpf[j]);
+    }
+    float rx = 0.f, ry = 0.f, rz = 0.f, re = 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t j = ent[q] & GBMD_IDX_MASK;
+      const GeomF G = geom_f(ent[q], pj[q], pi, A.g);
+      bool in = G.d2 < E.rc2lo;
+      if (!in && G.d2 <= E.rc2hi && L.valid(r, q))
+        in = exact_inside(A.posd, i, j, ent[q] >> GBMD_IDX_BITS, cp, A.g, E.rcut2, 0.0);
+      const float rs = rsqrtf(G.d2);
+      const float rd = G.d2 * rs;
+      float t;
+      const int m = knot_f(rd, rdr, nr, t);
+      const int tj = SINGLE ? 0 : __float_as_int(pj[q].w);
+      const float4 dj = __ldg(&E.rhod4[tj * nr1 + m]);
+      const float4 cz = __ldg(&E.z2r4[z2r_index_d(ti, tj) * nr1 + m]);
+      const float rhojp = fmaf(fmaf(dj.x, t, dj.y), t, dj.z);
+      float rhoip = rhojp;
+      if (!SINGLE && ti != tj) {
+        const float4 di = __ldg(&E.rhod4[ti * nr1 + m]);
+        rhoip = fmaf(fmaf(di.x, t, di.y), t, di.z);
+      }
+      const float t1 = fmaf(cz.x, t, cz.y);
+      const float z2 = fmaf(fmaf(t1, t, cz.z), t, cz.w);
+      const float z2d = fmaf(fmaf(cz.x, t, t1 + t1), t, cz.z);
+      const float phi = z2 * rs;
+      const float phip = fmaf(z2d * rdr, rs, -phi * rs);
+      const float psip = fmaf(fpi, rhojp, fmaf(fpj[q], rhoip, phip));
+      const float fpair = in ? psip * rs : 0.f;
+      const float gx = G.dx * fpair, gy = G.dy * fpair, gz = G.dz * fpair;
+      rx += gx;
+      ry += gy;
+      rz += gz;
+      if (in) {
+        fix_add(acc + j, fix_q(-gx, X.f, FIX_PAIR_LIMIT, X.err));
+        fix_add(acc + cap + j, fix_q(-gy, X.f, FIX_PAIR_LIMIT, X.err));
+        fix_add(acc + 2 * cap + j, fix_q(-gz, X.f, FIX_PAIR_LIMIT, X.err));
+        if (EV) {
+          const float eh = 0.5f * phi;
+          const float h = -0.5f * fpair;
+          const float w[6] = {h * G.dx * G.dx, h * G.dy * G.dy, h * G.dz * G.dz,
+                              h * G.dx * G.dy, h * G.dx * G.dz, h * G.dy * G.dz};
+          re += eh;
+          fix_add(acc + 3 * cap + j, fix_q(eh, X.e, FIX_PAIR_LIMIT, X.err));
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            v[k] += w[k];
+            fix_add(acc + (4 + k) * cap + j, fix_q(w[k], X.v, FIX_PAIR_LIMIT, X.err));
+          }
+        }
+      }
+    }
+    kahan_add(fx, cfx, rx);
+    kahan_add(fy, cfy, ry);
+    kahan_add(fz, cfz, rz);
+    if (EV) kahan_add(e, ce, re);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ent[q] = nxt[q];
+  }
+  fix_add(acc + i, fix_q(fx - cfx, X.f, FIX_SUM_LIMIT, X.err));
+  fix_add(acc + cap + i, fix_q(fy - cfy, X.f, FIX_SUM_LIMIT, X.err));
+  fix_add(acc + 2 * cap + i, fix_q(fz - cfz, X.f, FIX_SUM_LIMIT, X.err));
+  if (EV) {
+    fix_add(acc + 3 * cap + i, fix_q(e - ce, X.e, FIX_SUM_LIMIT, X.err));
+#pragma unroll
+    for (int k = 0; k < 6; ++k) fix_add(acc + (4 + k) * cap + i, fix_q(v[k], X.v, FIX_SUM_LIMIT, X.err));
+  }
+}
+
+// the power of two at or above x (at least 2^-60, which keeps the FP32
+// scales finite: all-zero tables give zero contributions at any scale)
+static double pow2_at_least(double x) {
+  return std::ldexp(1.0, (int)std::ceil(std::log2(std::max(x, 0x1p-60))));
+}
+
 // Power-of-two fixed-point scales of the bounds above, from the LJ table.
 static FixScale fix_scales(const gbmd_context* c) {
   double fmax = 0.0, emax = 0.0;
@@ -817,10 +1005,7 @@ static FixScale fix_scales(const gbmd_context* c) {
     emax = std::max(emax, 4.0 * std::fabs(q.eps));
   }
   const double vmax = fmax * c->lj.rcut_max;
-  // bounds of at least 2^-60 keep the FP32 scales finite (all-zero epsilon
-  // tables give zero forces, which any scale represents)
-  auto pow2_above = [](double x) { return std::ldexp(1.0, (int)std::ceil(std::log2(std::max(x, 0x1p-60)))); };
-  const double bf = pow2_above(fmax), be = pow2_above(emax), bv = pow2_above(vmax);
+  const double bf = pow2_at_least(fmax), be = pow2_at_least(emax), bv = pow2_at_least(vmax);
   FixScale X;
   X.f = (float)std::ldexp(1.0 / bf, 38);
   X.e = (float)std::ldexp(1.0 / be, 38);
@@ -828,15 +1013,89 @@ static FixScale fix_scales(const gbmd_context* c) {
   X.inv_f = std::ldexp(bf, -38);
   X.inv_e = std::ldexp(be, -38);
   X.inv_v = std::ldexp(bv, -38);
+  X.r = 1.f;
+  X.inv_r = 1.0;
   X.err = c->d_err + ERRW_FLAGS;
   return X;
 }
 
+// eam_alloy: bounds from the host spline copies over the knots from 0.3 rcut
+// to rcut (closer pairs are far from any physical state; their
+// contributions still fit below 2^16 times the bounds unless they are
+// extreme).  Knot m holds the spline on [m dr, (m+1) dr) with value s[6]
+// and slope s[5] / dr at its start.  |psi'| <= 2 max|F'| max|rho'| +
+// max|phi'|, doubled; energies half phi; virials that force times rcut.
+static FixScale eam_fix_scales(gbmd_context* c) {
+  if (!c->eam_fix_ok) {
+    const EamDev& E = c->eam;
+    const double dr = 1.0 / E.rdr, drho = 1.0 / E.rdrho;
+    const size_t kr = (size_t)E.nr + 1, kp = (size_t)E.nrho + 1;
+    const size_t m0 = std::max<size_t>(1, (size_t)(0.3 * E.rcut / dr));
+    const size_t m1 = std::min(kr - 1, (size_t)(E.rcut / dr) + 1);
+    double rho = 0.0, rhop = 0.0, phi = 0.0, phip = 0.0, fp = 0.0;
+    for (int e = 0; e < E.nel; ++e) {
+      for (size_t m = m0; m <= m1; ++m) {
+        const double* s = &c->eam_host_rhor[((size_t)e * kr + m) * 8];
+        rho = std::max(rho, std::fabs(s[6]));
+        rhop = std::max(rhop, std::fabs(s[5]) / dr);
+      }
+      for (size_t m = 0; m < kp; ++m)
+        fp = std::max(fp, std::fabs(c->eam_host_frho[((size_t)e * kp + m) * 8 + 5]) / drho * E.conv_frho);
+    }
+    for (int p = 0; p < E.npairs; ++p)
+      for (size_t m = m0; m <= m1; ++m) {
+        const double* s = &c->eam_host_z2r[((size_t)p * kr + m) * 8];
+        const double r = (double)m * dr, z2 = s[6] * E.conv_z2r, z2d = s[5] / dr * E.conv_z2r;
+        phi = std::max(phi, std::fabs(z2 / r));
+        phip = std::max(phip, std::fabs((z2d - z2 / r) / r));
+      }
+    const double f = 2.0 * (2.0 * fp * rhop + phip);
+    c->eam_fix_bound[0] = pow2_at_least(2.0 * rho);
+    c->eam_fix_bound[1] = pow2_at_least(f);
+    c->eam_fix_bound[2] = pow2_at_least(phi);
+    c->eam_fix_bound[3] = pow2_at_least(f * E.rcut);
+    c->eam_fix_ok = true;
+  }
+  const double* b = c->eam_fix_bound;
+  FixScale X;
+  X.r = (float)std::ldexp(1.0 / b[0], 38);
+  X.f = (float)std::ldexp(1.0 / b[1], 38);
+  X.e = (float)std::ldexp(1.0 / b[2], 38);
+  X.v = (float)std::ldexp(1.0 / b[3], 38);
+  X.inv_r = std::ldexp(b[0], -38);
+  X.inv_f = std::ldexp(b[1], -38);
+  X.inv_e = std::ldexp(b[2], -38);
+  X.inv_v = std::ldexp(b[3], -38);
+  X.err = c->d_err + ERRW_FLAGS;
+  return X;
+}
+
+template <bool EV, bool SINGLE>
+static void launch_eam_newton3(gbmd_context* c, const PairArgs& A, int part, unsigned grid, int B) {
+  cudaStream_t s = c->stream;
+  const FixScale X = eam_fix_scales(c);
+  long long* racc = c->h3acc + 3 * c->cap;  // the energy plane, free until the force pass
+  if (part != 2) {
+    k_eam_rho_half<SINGLE><<<grid, B, 0, s>>>(A, c->eam, racc, X);
+    k_eam_embed_half<EV, SINGLE><<<grid, B, 0, s>>>(A, c->eam, racc, X, c->fpf, c->epf, c->pfp);
+  }
+  if (part != 1) {
+    k_eam_force_half<EV, SINGLE><<<grid, B, 0, s>>>(A, c->eam, c->fpf, c->pfp, c->h3acc, c->cap, X);
+    k_h3_epilogue<EV><<<grid, B, 0, s>>>(A, c->h3acc, c->cap, X, EV ? c->epf : nullptr);
+  }
+}
+
 template <bool EV>
 static int launch_newton3(gbmd_context* c, const PairArgs& A, int part) {
-  if (part == 1 || A.n == 0) return GBMD_OK;
+  if (A.n == 0) return GBMD_OK;
   const int B = 256;
   const unsigned grid = (unsigned)((A.n + B - 1) / B);
+  if (c->pot == GBMD_POT_EAM_ALLOY) {
+    if (c->eam.nel == 1) launch_eam_newton3<EV, true>(c, A, part, grid, B);
+    else launch_eam_newton3<EV, false>(c, A, part, grid, B);
+    return GBMD_OK;
+  }
+  if (part == 1) return GBMD_OK;
   cudaStream_t s = c->stream;
   const FixScale X = fix_scales(c);
   if (c->pot == GBMD_POT_LJ) {
@@ -847,7 +1106,7 @@ static int launch_newton3(gbmd_context* c, const PairArgs& A, int part) {
     LJF P{};
     k_lj_half<EV, true><<<grid, B, 0, s>>>(A, P, c->lj_tab_d, c->lj.ntypes, c->lj.rcut_max2, c->h3acc, c->cap, X);
   }
-  k_h3_epilogue<EV><<<grid, B, 0, s>>>(A, c->h3acc, c->cap, X);
+  k_h3_epilogue<EV><<<grid, B, 0, s>>>(A, c->h3acc, c->cap, X, nullptr);
   return GBMD_OK;
 }
 

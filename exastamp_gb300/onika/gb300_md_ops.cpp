@@ -285,7 +285,7 @@ class Gb300LJForceNode : public OperatorNode {
   ADD_SLOT(bool, compute_virial, INPUT, false);
   ADD_SLOT(double, rcut_inc, INPUT, 1.0, DocString{"neighbour skin (global.rcut_inc)"});
   ADD_SLOT(std::string, precision, INPUT, std::string{"mixed"}, DocString{"mixed or fp64"});
-  ADD_SLOT(bool, half_list, INPUT, false, DocString{"Newton-3 half list with atomic reaction forces"});
+  ADD_SLOT(bool, half_list, INPUT, false, DocString{"Newton-3 half list, reaction forces through fixed-point atomics"});
   ADD_SLOT(GridParticleLocks, particle_locks, INPUT, OPTIONAL, DocString{"unused"});
   GB300_SESSION_SLOT;
 
@@ -374,8 +374,10 @@ class Gb300LJMultiForceNode : public OperatorNode {
 // (the force pass from the kept F'(rho), on the same positions).  The
 // instances share the device context through gb300_session.  eam_ghost is
 // accepted (there are no ghost cells on the device).  eam_symmetry (Newton-3
-// scatter, eam_force_op_multimat.h L162-169, L305-338) is accepted and runs
-// on the full list: the same sums up to rounding, without atomics.
+// scatter, eam_force_op_multimat.h L162-169, L305-338) runs on the full list
+// by default: the same sums up to rounding, and faster on GB300.  With
+// half_list it runs on the Newton-3 half list, rho_j and the reaction forces
+// added through fixed-point atomics (deterministic; mixed precision).
 template <class GridT>
 class Gb300EamAlloyForceNode : public OperatorNode {
   ADD_SLOT(ParticleSpecies, species, INPUT, REQUIRED);
@@ -393,7 +395,8 @@ class Gb300EamAlloyForceNode : public OperatorNode {
   ADD_SLOT(bool, eam_rho2emb, INPUT, true);
   ADD_SLOT(bool, eam_ghost, INPUT, true);
   ADD_SLOT(bool, eam_force, INPUT, true);
-  ADD_SLOT(bool, eam_symmetry, INPUT, false, DocString{"accepted; the full list gives the same sums"});
+  ADD_SLOT(bool, eam_symmetry, INPUT, false, DocString{"Newton-3 scatter; on the full list unless half_list"});
+  ADD_SLOT(bool, half_list, INPUT, false, DocString{"with eam_symmetry: the Newton-3 half list"});
   ADD_SLOT(double, rcut_inc, INPUT, 1.0, DocString{"neighbour skin (global.rcut_inc)"});
   ADD_SLOT(std::string, precision, INPUT, std::string{"mixed"}, DocString{"mixed or fp64"});
   GB300_SESSION_SLOT;
@@ -415,6 +418,11 @@ class Gb300EamAlloyForceNode : public OperatorNode {
                                    EXASTAMP_CONST_QUANTITY(1. * eV * ang), EXASTAMP_CONST_QUANTITY(1.0 * eV)),
                    "gbmd_load_setfl");
       finish_setup(s, *rcut_inc, *precision);
+      if (*eam_symmetry && *half_list) {
+        // the half-list kernels: mixed precision, one lane x 4 entries per load
+        gb300_ops::ok(s.ctx, gbmd_set_launch_ex(s.ctx, 1, 4, 256), "gbmd_set_launch_ex");
+        gb300_ops::ok(s.ctx, gbmd_set_newton3(s.ctx, 1), "gbmd_set_newton3");
+      }
     }
     const bool energy = trigger_thermo_state.has_value() && *trigger_thermo_state;
     compute_force_call("gb300_eam_alloy_force", s, *grid, *species, energy, energy && *compute_virial, passes);

@@ -272,13 +272,19 @@ class eam_alloy_force(Operator):
             raise OperatorError("eam_rho2emb %s with eam_rho and eam_force both %s: the embedding runs with "
                                 "the density pass" % (emb, rho))
         # eam_symmetry (Newton-3 half list with the rho_j and reaction-force
-        # scatter of eam_force_op_multimat.h L162-169, L305-338) selects only
-        # how the reference evaluates the same sums; here it runs on the full
-        # list, which gives the same densities and forces up to rounding,
-        # deterministically.
+        # scatter of eam_force_op_multimat.h L162-169, L305-338) selects how
+        # the reference evaluates the same sums; here it runs on the full
+        # list, which gives the same densities and forces up to rounding and
+        # is faster, unless half_list asks for the library's half list (rho_j
+        # and reaction forces through fixed-point atomics, deterministic,
+        # mixed precision).
         self.symmetry = bool(self.slots.get("eam_symmetry", False))
         rcut = quantity(self.slots["rcut"])
         sim.ctx.set_eam_alloy(sf, rcut, EV * 1.0, EV)
+        if self.symmetry and self.slots.get("half_list", False):
+            sim.set_precision(True)
+            sim.ctx.set_launch(1, 256, 4)
+            sim.ctx.set_newton3(True)
         sim.rcut_max = max(sim.rcut_max, rcut)
         if (rho or frc) and self.slots.get("eam_ghost", True):
             sim.ghost_dist_max = max(sim.ghost_dist_max, 2.0 * rcut)

@@ -186,14 +186,18 @@ int gbmd_set_neighbor_staging(gbmd_context* ctx, int enable);
 int gbmd_get_neighbor_staging(const gbmd_context* ctx, int* enabled);
 /* Newton-3 mode (lj_compute_force_symetric,
  * src/potential/pair_potential_template/pair_potential_singlemat_symetric.cpp
- * L44, L230-320): the list keeps each unordered pair once (j after i in
- * cell order) and the LJ kernels add the reaction force, half the pair
- * energy and half the pair virial to j with 64-bit fixed-point integer
- * atomics, so the sums do not depend on the order of the additions and runs
- * are bit-reproducible.  A pair force beyond 2^16 x 24 eps/sigma (pairs
- * closer than ~0.49 sigma) is outside the fixed-point range: the force call
- * returns GBMD_ERR_TOO_LARGE.  LJ potentials in mixed precision with the
- * 1 lane x 4 entries launch only; other set-ups return
+ * L44, L230-320; eam_alloy's eam_symmetry,
+ * src/potential/eam_potential_template/eam_force_op_multimat.h L162-169,
+ * L305-338): the list keeps each unordered pair once (j after i in cell
+ * order).  The kernels add to j, with 64-bit fixed-point integer atomics,
+ * what the pair gives it: the reaction force, half the pair energy and half
+ * the pair virial, and for eam_alloy its density rho_ti(r).  The sums do not
+ * depend on the order of the additions, so runs are bit-reproducible.  A
+ * contribution beyond 2^16 times its kind's bound (an LJ pair force beyond
+ * 2^16 x 24 eps/sigma, i.e. pairs closer than ~0.49 sigma) is outside the
+ * fixed-point range; gbmd_check_errors / gbmd_run_nve then return
+ * GBMD_ERR_TOO_LARGE.  LJ potentials and eam_alloy in mixed precision with
+ * the 1 lane x 4 entries launch only; other set-ups return
  * GBMD_ERR_UNSUPPORTED at the force call.  Default 0. */
 int gbmd_set_newton3(gbmd_context* ctx, int enable);
 int gbmd_get_newton3(const gbmd_context* ctx, int* enabled);

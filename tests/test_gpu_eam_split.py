@@ -142,3 +142,32 @@ def test_eam_symmetry_runs_the_full_list(gpu, oracle):
     G = np.stack([out[1]["ax"], out[1]["ay"], out[1]["az"]], 1)
     assert np.abs(G - F).max() < 1e-11 * np.abs(F).max()
     assert np.abs(out[1]["ep"] - ep).max() < 1e-12 * np.abs(ep).max()
+
+
+def test_eam_symmetry_half_list_operator(gpu, oracle):
+    """eam_symmetry with half_list: the operator mirror switches the context
+    to the Newton-3 half list (mixed precision, fixed-point scatter); the
+    forces, energies and virials match the oracle at the mixed tolerances."""
+    sf = _eam()
+    s = S.eam_cu_fcc(ncell=5, displace=0.06, seed=10)
+    sim = OP.Simulation(s)
+    try:
+        op = OP.eam_alloy_force(rcut=5.0, parameters=sf, eam_symmetry=True, half_list=True)
+        op.bind(sim)
+        OP.chunk_neighbors().bind(sim, 0.3)
+        assert sim.ctx.get_newton3()
+        op.execute(sim, energy=True, virial=True)
+        sim.ctx.check_errors()
+        d = sim.ctx.download(virial=True)
+    finally:
+        sim.ctx.close()
+    tab = oracle.EamOracleTables.from_setfl(sf, S.EV, S.EV, rcut=5.0)
+    x, y, z = s.x.copy(), s.y.copy(), s.z.copy()
+    oracle.wrap(x, y, z, s.lo, s.hi)
+    nl = oracle.build_neighbors(x, y, z, s.id, s.lo, s.hi, 5.3)
+    fx, fy, fz, ep, vir, _, _ = oracle.eam_forces(x, y, z, s.type, nl, s.L, tab, 5.0)
+    F = np.stack([fx, fy, fz], 1) / s.masses[0]
+    G = np.stack([d["ax"], d["ay"], d["az"]], 1)
+    assert np.sqrt(((G - F) ** 2).sum() / (F ** 2).sum()) < 1e-5
+    assert abs(d["ep"].sum() - ep.sum()) < 1e-6 * abs(ep.sum())
+    assert np.sqrt(((d["vir"] - vir) ** 2).sum() / (vir ** 2).sum()) < 1e-5

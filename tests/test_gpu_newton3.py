@@ -16,7 +16,7 @@ import pytest
 from exastamp_gb300 import systems as S
 from exastamp_gb300 import setfl as SF
 
-from test_gpu_parity import LJ, _jitter, _lj_oracle, gpu_ctx, rel_rms
+from test_gpu_parity import LJ, _jitter, _lj_oracle, _two_element_setfl, gpu_ctx, oracle_lists, rel_rms
 
 pytestmark = pytest.mark.gpu
 
@@ -137,11 +137,18 @@ def test_newton3_unsupported_setups(gpu):
         with pytest.raises(gpu.GbmdError) as e:
             ctx.compute_forces()
         assert e.value.code == UNSUPPORTED
-    # EAM
+    # eam_alloy in FP64, and the analytic EAM operators
     sf = SF.tabulate(SF.load_cu_params())
     c = S.eam_cu_fcc(ncell=4, displace=0.05, seed=4)
-    with gpu_ctx(gpu, c, lambda k: k.set_eam_alloy(sf, 5.0, S.EV, S.EV), 0.3, mixed=True, tpa=1, block=256,
+    with gpu_ctx(gpu, c, lambda k: k.set_eam_alloy(sf, 5.0, S.EV, S.EV), 0.3, mixed=False, tpa=1, block=256,
                  vec=4) as ctx:
+        ctx.set_newton3(True)
+        with pytest.raises(gpu.GbmdError) as e:
+            ctx.compute_forces()
+        assert e.value.code == UNSUPPORTED
+    ta = S.ta_bcc(ncell=5, seed=4)
+    with gpu_ctx(gpu, ta, lambda k: k.set_eam_johnson(S.johnson_ta_params(), 6.1), 0.3, mixed=True, tpa=1,
+                 block=256, vec=4) as ctx:
         ctx.set_newton3(True)
         with pytest.raises(gpu.GbmdError) as e:
             ctx.compute_forces()
@@ -228,3 +235,72 @@ def test_newton3_force_beyond_the_fixed_point_range(gpu):
         ctx.check_errors()
         d = ctx.download()
     assert np.isfinite(d["ax"]).all() and abs(d["ax"][0]) > 1e6
+
+
+def _eam_case(kind):
+    if kind == "cu":
+        sf = SF.tabulate(SF.load_cu_params())
+        s = S.eam_cu_fcc(ncell=5, displace=0.08, seed=23)
+    else:
+        sf = _two_element_setfl()
+        s = S.eam_cu_fcc(ncell=5, displace=0.08, seed=24)
+        rng = np.random.default_rng(24)
+        s.type = (rng.random(s.n) < 0.3).astype(np.uint8)
+        s.masses = np.array(sf.masses)
+    return sf, s
+
+
+@pytest.mark.parametrize("kind", ["cu", "two_elements"])
+def test_eam_newton3_matches_oracle(gpu, oracle, kind):
+    """eam_symmetry on the half list: rho_j and the reaction force scattered
+    through fixed-point atomics; forces, energies and virials against the
+    FP64 oracle at the mixed tolerances."""
+    sf, s = _eam_case(kind)
+    tab = oracle.EamOracleTables.from_setfl(sf, S.EV, S.EV, rcut=5.0)
+    _, (x, y, z), nl = oracle_lists(oracle, s, 5.3)
+    fx, fy, fz, ep, vir, fp, rho = oracle.eam_forces(x, y, z, s.type, nl, s.L, tab, 5.0)
+    F = np.stack([fx, fy, fz], 1) / s.masses[s.type][:, None]
+    with _n3_ctx(gpu, s, lambda c: c.set_eam_alloy(sf, 5.0, S.EV, S.EV)) as ctx:
+        for _ in range(2):  # the second call sees the planes cleared by the first
+            ctx.compute_forces(energy=True, virial=True)
+            ctx.check_errors()
+            d = ctx.download(virial=True)
+            G = np.stack([d["ax"], d["ay"], d["az"]], 1)
+            assert rel_rms(G, F) < MIXED_FORCE_TOL, rel_rms(G, F)
+            assert abs(d["ep"].sum() - ep.sum()) < 1e-6 * abs(ep.sum())
+            assert rel_rms(d["ep"], ep) < 1e-5
+            assert rel_rms(d["vir"], vir) < 1e-5
+        ctx.compute_forces()
+        d = ctx.download()
+        assert rel_rms(np.stack([d["ax"], d["ay"], d["az"]], 1), F) < MIXED_FORCE_TOL
+
+
+def test_eam_newton3_split_passes_and_reruns(gpu):
+    """The density pass then the force pass give the fused pass bit for bit;
+    two 40-step runs are bit-identical and stay within 1e-6 of the
+    full-list run."""
+    sf, s = _eam_case("cu")
+    setpot = lambda c: c.set_eam_alloy(sf, 5.0, S.EV, S.EV)  # noqa: E731
+    with _n3_ctx(gpu, s, setpot) as ctx:
+        ctx.compute_forces(energy=True, virial=True)
+        fused = ctx.download(virial=True)
+        ctx.compute_forces(energy=True, virial=True, passes="density")
+        ctx.compute_forces(energy=True, virial=True, passes="force")
+        split = ctx.download(virial=True)
+    for k in ("ax", "ay", "az", "ep", "vir"):
+        assert np.array_equal(split[k], fused[k]), k
+    out = []
+    for n3 in (True, True, False):
+        with gpu_ctx(gpu, s, setpot, 0.3, mixed=True, tpa=1, block=256, vec=4) as ctx:
+            ctx.set_newton3(n3)
+            th = ctx.run_nve(40, 1e-3, rebuild_every=10, thermo_every=20, use_graph=True)
+            out.append((th, ctx.download()))
+    assert np.array_equal(out[0][0], out[1][0])
+    for k in ("x", "y", "z", "vx", "vy", "vz", "ax"):
+        assert np.array_equal(out[0][1][k], out[1][1][k]), k
+        if k in ("x", "y", "z"):
+            dd = np.abs(out[0][1][k] - out[2][1][k])
+            assert np.minimum(dd, s.L[0] - dd).max() < 1e-6, k
+    e0 = out[2][0][:, 21:24].sum(1) + out[2][0][:, 24]
+    e1 = out[0][0][:, 21:24].sum(1) + out[0][0][:, 24]
+    assert np.abs(e1 - e0).max() < 1e-6 * np.abs(e0).max()
