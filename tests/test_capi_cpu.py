@@ -37,6 +37,19 @@ def test_no_fallback_without_device(gbmd_lib):
     assert rc in (2, 3)
 
 
+def test_entry_points_refuse_a_null_context(gbmd_lib):
+    """Argument checks that need no device: every setter and getter of the
+    list buffer, the Newton-3 switch and the error check answer
+    GBMD_ERR_INVALID (1) for a null context, before any CUDA call."""
+    L = gbmd_lib.lib()
+    d, k = ctypes.c_double(), ctypes.c_int64()
+    assert L.gbmd_set_list_buffer(None, ctypes.c_double(1.0)) == 1
+    assert L.gbmd_get_list_buffer(None, ctypes.byref(d), ctypes.byref(k)) == 1
+    assert L.gbmd_check_errors(None) == 1
+    assert L.gbmd_set_newton3(None, 1) == 1
+    assert L.gbmd_set_eam_sutton_chen(None, None, ctypes.c_double(5.0)) == 1
+
+
 def test_quantity_units():
     assert OP.quantity("5 ang") == 5.0
     assert abs(OP.quantity("1 eV") - 1.602176634e-19 / 1.66053906660e-23) < 1e-9
