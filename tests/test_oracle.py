@@ -254,6 +254,51 @@ def test_oracle_nve_continues_from_given_accelerations(oracle):
         assert np.array_equal(one[k], two[k]), k
 
 
+def test_two_level_filter_is_complete(oracle):
+    """The claim behind the two-level list (gbmd_set_list_buffer): filter an
+    outer list of radius R + d, built at positions x0, by the distance at
+    positions x1 that moved less than d/2, and the result is the pair set
+    of a fresh radius-R build at x1.  Checked with the oracle's own builder
+    (FP64) on a jittered LJ crystal: displacements uniform in a ball of
+    radius 0.999 d/2, separations taken with the outer build's images."""
+    s = _jitter_cpu(S.lj_fcc(ncell=7, seed=5), 0.04, 5)
+    R, d = 2.8, 0.6
+    x0, y0, z0 = s.x.copy(), s.y.copy(), s.z.copy()
+    oracle.wrap(x0, y0, z0, s.lo, s.hi)
+    outer = oracle.build_neighbors(x0, y0, z0, s.id, s.lo, s.hi, R + d)
+    n = s.n
+    ii = np.repeat(np.arange(n), np.diff(outer.off))
+    jj = outer.nbr
+
+    def filtered_and_fresh(reach, seed):
+        rng = np.random.default_rng(seed)
+        u = rng.normal(size=(n, 3))
+        u *= (reach * rng.random(n) ** (1 / 3) / np.linalg.norm(u, axis=1))[:, None]
+        x1, y1, z1 = x0 + u[:, 0], y0 + u[:, 1], z0 + u[:, 2]
+        sep = np.stack([x1[jj] + outer.img[:, 0] * s.L[0] - x1[ii], y1[jj] + outer.img[:, 1] * s.L[1] - y1[ii],
+                        z1[jj] + outer.img[:, 2] * s.L[2] - z1[ii]], 1)
+        keep = ((sep[:, 0] * sep[:, 0] + sep[:, 1] * sep[:, 1]) + sep[:, 2] * sep[:, 2]) <= R * R
+        xw, yw, zw = x1.copy(), y1.copy(), z1.copy()
+        oracle.wrap(xw, yw, zw, s.lo, s.hi)
+        fresh = oracle.build_neighbors(xw, yw, zw, s.id, s.lo, s.hi, R)
+        fi = np.repeat(np.arange(n), np.diff(fresh.off))
+        return set(zip(ii[keep].tolist(), jj[keep].tolist())), set(zip(fi.tolist(), fresh.nbr.tolist()))
+
+    filtered, fresh = filtered_and_fresh(0.999 * 0.5 * d, 6)
+    assert filtered == fresh
+    assert 0 < len(filtered) < outer.npairs
+    # moved farther than d/2 the filter misses pairs (the check is not vacuous)
+    filtered, fresh = filtered_and_fresh(1.5 * d, 7)
+    assert filtered < fresh
+
+
+def _jitter_cpu(s, sig, seed):
+    rng = np.random.default_rng(seed)
+    for a in (s.x, s.y, s.z):
+        a += rng.normal(0.0, sig, s.n)
+    return s
+
+
 def test_oracle_minimiser_lowers_energy_and_clips(oracle):
     """Clipped minimiser on an overlapping random binary mixture: the
     potential energy falls and no step moves an atom further than
